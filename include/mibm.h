@@ -1,0 +1,198 @@
+/*
+ * mibm.h -- C-ABI of the GB300 melt_IBM fluid RK3 substep.
+ *
+ * The reference (kevzhong/melt_IBM, Fortran 90) implements the substep as
+ * argument-less *external* subroutines that read and write module globals
+ * (param.f90:4-266).  gfortran exports external subroutines as lowercase
+ * symbols with a trailing underscore and passes every argument by reference,
+ * so the drop-in entry points below keep exactly that shape: a Fortran host
+ * that links libmibm.so instead of the reference objects calls the same
+ * names with the same arguments.
+ *
+ * Because the routines take no arguments, the module globals they read are
+ * handed over once through a registration layer (mibm_register_*): the host
+ * passes the address of each Fortran array (with its bounds) and of each
+ * scalar.  The library keeps device mirrors of every registered array;
+ * between mibm_sync_from_host_ / mibm_sync_to_host_ calls the device copy is
+ * authoritative.  Scalars (al, ga, ro, dt, ...) are read through their
+ * registered host address at every call, as the Fortran routines read the
+ * module variable.
+ *
+ * Errors: the reference routines return nothing and `stop` / MPI_Abort on
+ * failure (mlsWeight.f90:121-124, particle.f90:206-224).  The drop-ins keep
+ * void signatures; failures are recorded and read with mibm_last_status_()
+ * and mibm_last_message().  No device trap is ever raised: device-side
+ * failures (singular MLS matrix, non-finite field, wait limit) set a flag
+ * that the host reads after the launch sequence.
+ *
+ * Threading: one context per case.  A context is bound to the calling host
+ * thread (mibm_context_bind_); every drop-in acts on the bound context.
+ */
+#ifndef MIBM_H
+#define MIBM_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ */
+/* Status codes                                                        */
+/* ------------------------------------------------------------------ */
+enum {
+  MIBM_OK = 0,
+  MIBM_EINVAL = 1,     /* bad dimension / argument                        */
+  MIBM_ENOTREG = 2,    /* a required array or scalar was not registered   */
+  MIBM_ECUDA = 3,      /* CUDA runtime error                              */
+  MIBM_ENOMEM = 4,     /* device allocation failed                        */
+  MIBM_ESTATE = 5,     /* call out of order (e.g. before mibm_init_)      */
+  MIBM_ETIMEOUT = 6,   /* bounded device wait ran out                     */
+  MIBM_ENUMERIC = 7,   /* singular MLS matrix (the reference `stop`s)     */
+  MIBM_EBUDGET = 8,    /* serving layer: HBM budget refused the case      */
+  MIBM_EABORT = 9      /* body volume below threshold (particle.f90:218)  */
+};
+
+/* ------------------------------------------------------------------ */
+/* Registered 3-D fields.  Shapes are the reference's (init.f90:15-83): */
+/*   GHOSTED  : (n1, n2,   0:n3m+1)  n1 = n1m+1, n2 = n2m+1             */
+/*   DPH      : (n1, n2+1, 0:n3m+1)                                     */
+/*   PLAIN    : (n1, n2,   1:n3m)                                       */
+/* `base` is the address of element (1,1,klo).                          */
+/* ------------------------------------------------------------------ */
+enum {
+  MIBM_F_VX = 0, MIBM_F_VY = 1, MIBM_F_VZ = 2, MIBM_F_TEMP = 3, MIBM_F_PR = 4,
+  MIBM_F_DPH = 5,
+  MIBM_F_RHS = 6, MIBM_F_DQ = 7, MIBM_F_QCAP = 8, MIBM_F_HTEMP = 9,
+  MIBM_F_RU1 = 10, MIBM_F_RU2 = 11, MIBM_F_RU3 = 12, MIBM_F_RUT = 13,
+  MIBM_F_FORCX = 14, MIBM_F_FORCY = 15, MIBM_F_FORCZ = 16,
+  MIBM_F_VOFX = 17, MIBM_F_VOFY = 18, MIBM_F_VOFZ = 19, MIBM_F_VOFP = 20,
+  MIBM_F_FORXC = 21, MIBM_F_FORYC = 22, MIBM_F_FORZC = 23, MIBM_F_FORTEMP = 24,
+  MIBM_F_SDF = 25,
+  MIBM_NFIELDS = 26
+};
+
+/* Lagrangian mesh arrays (allotri.f90:1-88), single particle.            */
+/* Element type is double unless marked (i32) = Fortran default integer /  */
+/* logical (4 bytes, .true. = nonzero).                                    */
+enum {
+  MIBM_M_XYZV = 0,        /* (3, maxnv)                                  */
+  MIBM_M_VERT_OF_FACE = 1,/* (3, maxnf)  i32, 1-based                    */
+  MIBM_M_TRI_BAR = 2,     /* (3, maxnf)                                  */
+  MIBM_M_TRI_NOR = 3,     /* (3, maxnf)                                  */
+  MIBM_M_VERT_NOR = 4,    /* (3, maxnv)                                  */
+  MIBM_M_SUR = 5,         /* (maxnf)                                     */
+  MIBM_M_AVERT = 6,       /* (maxnv)                                     */
+  MIBM_M_VEL_TRI = 7,     /* (3, maxnf)                                  */
+  MIBM_M_CFAC = 8,        /* (maxnf)                                     */
+  MIBM_M_GHOST_FACE = 9,  /* (maxnf)  i32 logical                        */
+  MIBM_M_GHOST_VERT = 10, /* (maxnv)  i32 logical                        */
+  MIBM_M_PIND = 11,       /* (6, maxnf) i32                              */
+  MIBM_M_PTXAB_Q1 = 12,   /* (27, maxnf)                                 */
+  MIBM_M_PTXAB_Q2 = 13,
+  MIBM_M_PTXAB_Q3 = 14,
+  MIBM_M_PTXAB_TEMP = 15,
+  MIBM_M_QW_O = 16,       /* (maxnf)                                     */
+  MIBM_M_QW_I = 17,
+  MIBM_M_QW_OVERT = 18,   /* (maxnv)                                     */
+  MIBM_M_QW_IVERT = 19,
+  MIBM_M_VMELT = 20,      /* (3, maxnv)                                  */
+  MIBM_M_VMELT_M1 = 21,
+  MIBM_M_VERT_OF_EDGE = 22,  /* (2, maxne) i32                           */
+  MIBM_M_EDGE_OF_FACE = 23,  /* (3, maxnf) i32                           */
+  MIBM_M_GHOST_EDGE = 24,    /* (maxne) i32 logical                      */
+  MIBM_M_ELENGTHS = 25,      /* (maxne)                                  */
+  MIBM_M_SKEWNESS = 26,      /* (maxnf)                                  */
+  MIBM_NMESH = 27
+};
+
+/* Scalars (double), registered by address.  Vectors take 3 consecutive  */
+/* doubles at the registered address.                                    */
+enum {
+  MIBM_S_DT = 0, MIBM_S_AL, MIBM_S_GA, MIBM_S_RO, MIBM_S_BETA,
+  MIBM_S_REN, MIBM_S_PEC, MIBM_S_BETAGZ, MIBM_S_TMELT, MIBM_S_TLIQ,
+  MIBM_S_TSOL, MIBM_S_LATHEAT, MIBM_S_CPLIQUID, MIBM_S_DTMAX, MIBM_S_CFLFIX,
+  MIBM_S_CFLM, MIBM_S_H_EULERIAN, MIBM_S_CELVOL, MIBM_S_VOLUME, MIBM_S_SURFACE,
+  MIBM_S_POS_CM, MIBM_S_VEL_CM, MIBM_S_OMEGA_C, MIBM_S_WCON, MIBM_S_WSCL,
+  MIBM_S_E_THRESH, MIBM_S_V_THRESH, MIBM_S_DENS_RATIO, MIBM_S_TIME,
+  MIBM_NSCALARS
+};
+
+/* Integer flags (Fortran default integer / logical), registered by address. */
+enum {
+  MIBM_I_IMLSFOR = 0, MIBM_I_IMLSSTR, MIBM_I_IMELT, MIBM_I_IREMESH,
+  MIBM_I_TAGTYPE, MIBM_I_FORCING, MIBM_I_IDTV, MIBM_I_NTIME,
+  MIBM_I_STATIONARY, MIBM_I_NSST,
+  MIBM_NINTS
+};
+
+/* ------------------------------------------------------------------ */
+/* Context, registration, synchronisation                              */
+/* ------------------------------------------------------------------ */
+int  mibm_context_create_(void);               /* returns id > 0 (bound) */
+int  mibm_context_bind_(const int* id);
+int  mibm_context_destroy_(const int* id);
+int  mibm_last_status_(void);
+const char* mibm_last_message(void);
+
+/* Grid of the case: replaces the bou.in read (papero.f90:289-306) and    */
+/* cordin (cordin.f90:1-99).  n1m must equal n2m (phcalc.f90:24-33).      */
+void mibm_set_grid_(const int* n1m, const int* n2m, const int* n3m,
+                    const double* xlen, const double* ylen, const double* zlen);
+void mibm_set_mesh_sizes_(const int* maxnv, const int* maxne, const int* maxnf);
+void mibm_register_field_(const int* id, double* base);
+void mibm_register_mesh_(const int* id, void* base);
+void mibm_register_scalar_(const int* id, double* addr);
+void mibm_register_int_(const int* id, int* addr);
+/* After registration: allocate device mirrors, wavenumbers (phini.f90:4-59),
+ * coordinates; copies every registered array host -> device. */
+void mibm_init_(void);
+/* mask bit b (0..25) selects field b; bit 32+m selects mesh array m. */
+void mibm_sync_from_host_(const long long* mask);
+void mibm_sync_to_host_(const long long* mask);
+/* Visible CUDA devices (0 without a GPU); kernels launched by the bound
+ * context so far (libmibm.so only). */
+int  mibm_device_count_(void);
+unsigned long long mibm_launch_count_(void);
+
+/* ------------------------------------------------------------------ */
+/* Drop-in routines (reference file:line of the routine each replaces) */
+/* ------------------------------------------------------------------ */
+void tschem_(void);       /* tsch.f90:1-99  (3 RK3 substeps, fused path)   */
+void hdnl1_(void);        /* hdnl1.f90:1-80                                 */
+void hdnl2_(void);        /* hdnl2.f90:1-81                                 */
+void hdnl3_(void);        /* hdnl3.f90:1-91                                 */
+void hdnlte_(void);       /* hdnlte.f90:1-161                               */
+void invtr1_(void);       /* invtr1.f90:1-77                                */
+void invtr2_(void);       /* invtr2.f90:1-71                                */
+void invtr3_(void);       /* invtr3.f90:1-65                                */
+void invtrte_(void);      /* invtrte.f90:1-67                               */
+void solxi_(const double* betadx);             /* solxi.f90:1-52        */
+void solxj_(const double* betadx);             /* solxj.f90:1-40        */
+void solxk_(double* q, const double* betadx);  /* solxk.f90:1-60; q =
+                              address of vx/vy/vz/temp(1,1,kstart)     */
+void divg_(void);         /* divg.f90:1-24                                  */
+void phcalc_(void);       /* phcalc.f90:11-97                               */
+void updvp_(void);        /* updvp.f90:8-34                                 */
+void prcalc_(void);       /* prcalc.f90:5-35                                */
+void findcentroidindices_(void);  /* findCentroidIndices.f90:6-53           */
+void mlsweight_(void);    /* mlsWeight.f90:1-45 (wght1/2/3/temp)            */
+void mlsforce_(void);     /* mlsForce.f90:1-36 (forc1/2/3/forctemp)         */
+void velforce_(void);     /* velforce.f90:1-59                              */
+void tempforce_(void);    /* tempforce.f90:1-46                             */
+void findprobeindices_(void);     /* findProbeIndices.f90:9-76              */
+void mls_heatflux_(void); /* mls_heatFlux.f90:1-158 (wght_gradT, faceToVert) */
+void apply_stefancondition_(void);/* stefanCondition.f90:1-61               */
+void tagcells_(void);     /* tagCells.f90:4-27 (narrow band + interp_vof)   */
+void particle_(void);     /* particle.f90:1-230 (forcing, melt, geometry)   */
+void cfl_(void);          /* cfl.f90:1-31                                   */
+void get_dt_(void);       /* cfl.f90:33-77                                  */
+void interp_(double* arrold, double* arrnew, const int* n1o, const int* n2o,
+             const int* n3o, const int* intvar, const int* kstarto,
+             const int* kendo);                  /* interp.f90:1-221    */
+/* Initial full cell tagging at t = 0 (pencil_rayTag.f90:37-165 with the  */
+/* narrow band, tagCells.f90:17-23 with initial_tag = .true.).            */
+void tagcells_initial_(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MIBM_H */

@@ -1,0 +1,120 @@
+"""ctypes binding of the C-ABI in include/mibm.h.
+
+The same binding drives two shared libraries with identical exports: the
+product library ``libmibm.so`` (CUDA, sm_103a) and, in the test suite only,
+the CPU oracle.  Constants are parsed from the header so that the Python side
+cannot drift from the C side.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(_HERE)
+HEADER = os.path.join(ROOT, "include", "mibm.h")
+
+
+def _parse_enums(path: str) -> dict[str, int]:
+    text = open(path).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    out: dict[str, int] = {}
+    for body in re.findall(r"enum\s*\{(.*?)\}", text, flags=re.S):
+        val = -1
+        for item in body.split(","):
+            item = item.strip()
+            if not item:
+                continue
+            if "=" in item:
+                name, v = (s.strip() for s in item.split("="))
+                val = int(v, 0)
+            else:
+                name = item
+                val += 1
+            out[name] = val
+    return out
+
+
+ENUMS = _parse_enums(HEADER)
+globals().update(ENUMS)
+
+#: exported function name -> (restype, argtypes)
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int)
+_L = C.POINTER(C.c_longlong)
+SIGNATURES: dict[str, tuple] = {
+    "mibm_context_create_": (C.c_int, []),
+    "mibm_context_bind_": (C.c_int, [_I]),
+    "mibm_context_destroy_": (C.c_int, [_I]),
+    "mibm_last_status_": (C.c_int, []),
+    "mibm_last_message": (C.c_char_p, []),
+    "mibm_set_grid_": (None, [_I, _I, _I, _D, _D, _D]),
+    "mibm_set_mesh_sizes_": (None, [_I, _I, _I]),
+    "mibm_register_field_": (None, [_I, C.c_void_p]),
+    "mibm_register_mesh_": (None, [_I, C.c_void_p]),
+    "mibm_register_scalar_": (None, [_I, C.c_void_p]),
+    "mibm_register_int_": (None, [_I, C.c_void_p]),
+    "mibm_init_": (None, []),
+    "mibm_sync_from_host_": (None, [_L]),
+    "mibm_sync_to_host_": (None, [_L]),
+    "mibm_device_count_": (C.c_int, []),
+    "mibm_launch_count_": (C.c_ulonglong, []),
+    "solxi_": (None, [_D]),
+    "solxj_": (None, [_D]),
+    "solxk_": (None, [C.c_void_p, _D]),
+    "interp_": (None, [C.c_void_p, C.c_void_p, _I, _I, _I, _I, _I, _I]),
+}
+VOID_ROUTINES = [
+    "tschem_", "hdnl1_", "hdnl2_", "hdnl3_", "hdnlte_", "invtr1_", "invtr2_", "invtr3_",
+    "invtrte_", "divg_", "phcalc_", "updvp_", "prcalc_", "findcentroidindices_",
+    "mlsweight_", "mlsforce_", "velforce_", "tempforce_", "findprobeindices_",
+    "mls_heatflux_", "apply_stefancondition_", "tagcells_", "particle_", "cfl_", "get_dt_",
+    "tagcells_initial_",
+]
+for _n in VOID_ROUTINES:
+    SIGNATURES[_n] = (None, [])
+
+
+def header_symbols() -> list[str]:
+    """Every function name declared in include/mibm.h."""
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    return re.findall(r"\b([a-z_][a-z0-9_]*)\s*\((?:[^;{]*?)\)\s*;", text)
+
+
+class Lib:
+    """A loaded library exporting the mibm C-ABI."""
+
+    def __init__(self, path: str):
+        self.path = path
+        self.dll = C.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(self.dll, name)
+            fn.restype = res
+            fn.argtypes = args
+        self._extra()
+
+    def _extra(self) -> None:
+        pass
+
+    def __getattr__(self, name):
+        return getattr(self.dll, name)
+
+    def check(self, what: str = "") -> None:
+        st = self.dll.mibm_last_status_()
+        if st != 0:
+            msg = self.dll.mibm_last_message()
+            raise RuntimeError(f"{os.path.basename(self.path)}: {what} failed with status {st}: "
+                               f"{msg.decode() if msg else ''}")
+
+
+def ref_int(v: int):
+    return C.byref(C.c_int(int(v)))
+
+
+def ref_double(v: float):
+    return C.byref(C.c_double(float(v)))
+
+
+def ref_ll(v: int):
+    return C.byref(C.c_longlong(int(v)))

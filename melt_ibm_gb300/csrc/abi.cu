@@ -1,0 +1,160 @@
+// abi.cu -- drop-in entry points of include/mibm.h and the fused RK3 step.
+//
+// Every routine keeps the reference's name, argument list and side effects on
+// the registered arrays (with the device copy authoritative until
+// mibm_sync_to_host_).  `tschem_` replays tsch.f90:32-97 with two fusions
+// that leave the results unchanged up to rounding:
+//   * the explicit term of each component is computed inside its RHS kernel
+//     (hdnl* + invtr* RHS), so dq/dph/qcap/htemp are not materialised;
+//   * the four RHS fields are separate buffers, so all explicit terms are
+//     formed from the substep's initial fields exactly as tsch.f90:49-57
+//     orders them (every invtr only advances its own component).
+#include <cstdio>
+#include <cstring>
+
+#include "common.cuh"
+
+namespace mibm {
+
+void tri_free(Ctx* c);
+void fft_free(Ctx* c);
+
+// Copy the current host scalars to device slot `slot` (stream ordered; the
+// source is pageable, so the host may reuse it as soon as the call returns).
+static const StepParams* push_params(Ctx* c, int slot) {
+  StepParams p = host_params(c);
+  cudaMemcpyAsync(c->dparams + slot, &p, sizeof(StepParams), cudaMemcpyHostToDevice, c->stream);
+  return c->dparams + slot;
+}
+
+static int field_of_plane1(Ctx* c, const double* q) {
+  size_t n1 = c->g.n1m + 1;
+  for (int id = 0; id < MIBM_NFIELDS; ++id) {
+    int ny, klo, nk;
+    field_host_shape(c, id, ny, klo, nk);
+    const double* p1 = c->hf[id] + (klo == 0 ? n1 * (size_t)ny : 0);
+    if (p1 == q) return id;
+  }
+  return -1;
+}
+
+static void invtr(Ctx* c, int which) {
+  const StepParams* dp = push_params(c, 3);
+  double* rhs = c->df[MIBM_F_RHS];
+  k_invtr_rhs(c, which, dp, rhs);
+  static const int fid[4] = {MIBM_F_VX, MIBM_F_VY, MIBM_F_VZ, MIBM_F_TEMP};
+  double al = c->S(MIBM_S_AL), dt = c->S(MIBM_S_DT);
+  double b1, b2, b3;
+  if (which < 3) {
+    double beta = c->S(MIBM_S_BETA);
+    b1 = beta * al * c->g.dx1q; b2 = beta * al * c->g.dx2q; b3 = beta * al * c->g.dx3q;
+  } else {
+    double pec = c->S(MIBM_S_PEC);
+    b1 = dt / pec * 0.5 * al * c->g.dx1q; b2 = dt / pec * 0.5 * al * c->g.dx2q; b3 = dt / pec * 0.5 * al * c->g.dx3q;
+  }
+  k_solve_x(c, rhs, b1);
+  k_solve_y(c, rhs, b2);
+  k_solve_z(c, rhs, b3, c->df[fid[which]]);
+}
+
+// tsch.f90:18-97 on the device
+static void tschem(Ctx* c) {
+  static const double gam[3] = {8.0 / 15.0, 5.0 / 12.0, 3.0 / 4.0};
+  static const double rom[3] = {0.0, -17.0 / 60.0, -5.0 / 12.0};
+  const Grid& g = c->g;
+  if (!c->rhs4) {
+    if (!cuda_ok(c, cudaMalloc(&c->rhs4, 4 * g.cells * sizeof(double)), "rhs4")) return;
+  }
+  *c->hs[MIBM_S_BETA] = c->S(MIBM_S_DT) / c->S(MIBM_S_REN) * 0.5;
+  static const int fid[4] = {MIBM_F_VX, MIBM_F_VY, MIBM_F_VZ, MIBM_F_TEMP};
+  for (int ns = 0; ns < 3; ++ns) {
+    *c->hs[MIBM_S_AL] = gam[ns] + rom[ns];
+    *c->hs[MIBM_S_GA] = gam[ns];
+    *c->hs[MIBM_S_RO] = rom[ns];
+    const StepParams* dp = push_params(c, ns);
+    if (!c->I(MIBM_I_STATIONARY) && c->I(MIBM_I_IMLSFOR) == 1) lagr_tag_narrow_band(c);
+    k_fused_rhs(c, dp);
+    double al = c->S(MIBM_S_AL), dt = c->S(MIBM_S_DT), beta = c->S(MIBM_S_BETA), pec = c->S(MIBM_S_PEC);
+    for (int q = 0; q < 4; ++q) {
+      double f = (q < 3) ? beta * al : dt / pec * 0.5 * al;
+      double* r = c->rhs4 + (size_t)q * g.cells;
+      k_solve_x(c, r, f * g.dx1q);
+      k_solve_y(c, r, f * g.dx2q);
+      k_solve_z(c, r, f * g.dx3q, c->df[fid[q]]);
+    }
+    lagr_particle(c, dp);
+    if (c->status != MIBM_OK) return;
+    k_divg(c, dp);
+    k_phcalc(c);
+    k_updvp(c, dp);
+    k_prcalc(c, dp);
+    if (c->status != MIBM_OK) return;
+  }
+}
+
+}  // namespace mibm
+
+using namespace mibm;
+
+#define DROPIN_BEGIN          \
+  Ctx* c = current();         \
+  if (!ready(c)) return;
+#define DROPIN_END cuda_ok(c, cudaGetLastError(), __func__);
+
+extern "C" {
+
+void tschem_(void) { DROPIN_BEGIN tschem(c); DROPIN_END }
+void hdnl1_(void) { DROPIN_BEGIN k_hdnl(c, 0, push_params(c, 3)); DROPIN_END }
+void hdnl2_(void) { DROPIN_BEGIN k_hdnl(c, 1, push_params(c, 3)); DROPIN_END }
+void hdnl3_(void) { DROPIN_BEGIN k_hdnl(c, 2, push_params(c, 3)); DROPIN_END }
+void hdnlte_(void) { DROPIN_BEGIN k_hdnl(c, 3, push_params(c, 3)); DROPIN_END }
+void invtr1_(void) { DROPIN_BEGIN invtr(c, 0); DROPIN_END }
+void invtr2_(void) { DROPIN_BEGIN invtr(c, 1); DROPIN_END }
+void invtr3_(void) { DROPIN_BEGIN invtr(c, 2); DROPIN_END }
+void invtrte_(void) { DROPIN_BEGIN invtr(c, 3); DROPIN_END }
+void solxi_(const double* betadx) { DROPIN_BEGIN k_solve_x(c, c->df[MIBM_F_RHS], *betadx); DROPIN_END }
+void solxj_(const double* betadx) { DROPIN_BEGIN k_solve_y(c, c->df[MIBM_F_RHS], *betadx); DROPIN_END }
+void solxk_(double* q, const double* betadx) {
+  DROPIN_BEGIN
+  int id = field_of_plane1(c, q);
+  if (id < 0) { fail(c, MIBM_EINVAL, "solxk_: q is not element (1,1,kstart) of a registered field"); return; }
+  k_solve_z(c, c->df[MIBM_F_RHS], *betadx, c->df[id]);
+  DROPIN_END
+}
+void divg_(void) { DROPIN_BEGIN k_divg(c, push_params(c, 3)); DROPIN_END }
+void phcalc_(void) { DROPIN_BEGIN k_phcalc(c); DROPIN_END }
+void updvp_(void) { DROPIN_BEGIN k_updvp(c, push_params(c, 3)); DROPIN_END }
+void prcalc_(void) { DROPIN_BEGIN k_prcalc(c, push_params(c, 3)); DROPIN_END }
+void findcentroidindices_(void) { DROPIN_BEGIN lagr_find_centroid_indices(c); DROPIN_END }
+void mlsweight_(void) { DROPIN_BEGIN lagr_mls_weight(c); DROPIN_END }
+void mlsforce_(void) { DROPIN_BEGIN lagr_mls_force(c, push_params(c, 3), true); DROPIN_END }
+void velforce_(void) { DROPIN_BEGIN lagr_velforce(c); DROPIN_END }
+void tempforce_(void) { DROPIN_BEGIN lagr_tempforce(c); DROPIN_END }
+void findprobeindices_(void) { DROPIN_BEGIN lagr_find_probe_indices(c); DROPIN_END }
+void mls_heatflux_(void) { DROPIN_BEGIN lagr_heat_flux(c); DROPIN_END }
+void apply_stefancondition_(void) { DROPIN_BEGIN lagr_stefan(c, push_params(c, 3)); DROPIN_END }
+void tagcells_(void) { DROPIN_BEGIN lagr_tag_narrow_band(c); DROPIN_END }
+void tagcells_initial_(void) { DROPIN_BEGIN lagr_tag_initial(c); DROPIN_END }
+void particle_(void) { DROPIN_BEGIN lagr_particle(c, push_params(c, 3)); DROPIN_END }
+
+void cfl_(void) {
+  DROPIN_BEGIN
+  *c->hs[MIBM_S_CFLM] = k_cfl(c);
+  DROPIN_END
+}
+
+void get_dt_(void) {
+  DROPIN_BEGIN
+  double dt = c->S(MIBM_S_DT);
+  double buf = k_get_dt_buffer(c, dt, c->S(MIBM_S_REN));
+  if (buf > 0.0) *c->hs[MIBM_S_DT] = dt * c->S(MIBM_S_CFLFIX) / buf;
+  DROPIN_END
+}
+
+void interp_(double*, double*, const int*, const int*, const int*, const int*, const int*, const int*) {
+  DROPIN_BEGIN
+  fail(c, MIBM_EINVAL, "interp_: not available in this build");
+  DROPIN_END
+}
+
+}  // extern "C"

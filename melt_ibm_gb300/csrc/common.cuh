@@ -1,0 +1,204 @@
+// common.cuh -- shared context, device layout and helpers of libmibm.so.
+//
+// Device layout of a cell field (compact, no ghost planes):
+//   q(i, j, k), 0-based i < n1m, j < n2m, k < n3m  ->  q[i + P*(j + n2m*k)]
+// with row pitch P = n1m rounded up to a multiple of 4 elements (32-byte rows
+// in FP64, 16-byte rows in FP32).  The Fortran ghost planes k = 0, n3m+1 of
+// the host arrays are periodic copies (mpi_routines.f90:139-210 on one rank),
+// so kernels wrap k instead of storing them; they are rebuilt on the host
+// copy at mibm_sync_to_host_.  The Fortran padding column i = n1 of vx and row
+// j = n2 of vy are read only by `cfl` (cfl.f90:19-26); their values are kept
+// in two small device planes (pad_vx, pad_vy).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/mibm.h"
+
+namespace mibm {
+
+constexpr int kMaxCtx = 4096;
+
+// Per-substep scalars read by the kernels.  The fused RK3 path keeps one
+// copy per substep on the device so that a captured graph reads the values
+// of the current step (dt changes every step in CFL mode).
+struct StepParams {
+  double al, ga, ro, dt, beta;
+  double alre;      // al / ren
+  double pec, ren;
+  double betagz, tliq, tmelt;
+  double pos[3], vel[3], om[3];
+};
+
+struct Grid {
+  int n1m, n2m, n3m;         // cells per direction
+  int P;                     // row pitch (elements)
+  size_t plane, cells;       // P*n2m, plane*n3m
+  double xlen, ylen, zlen;
+  double dx1, dx2, dx3, dx1q, dx2q, dx3q;
+  int H, HP;                 // n1m/2+1 complex columns, padded pitch
+};
+
+// Device pointer bundle passed by value to kernels.
+struct DevFields {
+  double* f[MIBM_NFIELDS];
+};
+
+struct Ctx {
+  int id = 0;
+  int status = MIBM_OK;
+  std::string msg;
+  int device = 0;
+  bool grid_set = false, inited = false;
+  Grid g{};
+  // host registration
+  double* hf[MIBM_NFIELDS] = {nullptr};
+  void* hm[MIBM_NMESH] = {nullptr};
+  double* hs[MIBM_NSCALARS] = {nullptr};
+  int* hi[MIBM_NINTS] = {nullptr};
+  int maxnv = 0, maxne = 0, maxnf = 0;
+  // device storage
+  double* df[MIBM_NFIELDS] = {nullptr};   // compact fields
+  double* pad_vx = nullptr;               // vx(n1, j, k), j<n2m, k<n3m
+  double* pad_vy = nullptr;               // vy(i, n2, k), i<n1m, k<n3m
+  void* dm[MIBM_NMESH] = {nullptr};       // mesh mirrors
+  double* stage = nullptr;                // host<->device staging (one Fortran field)
+  size_t stage_bytes = 0;
+  // spectral work for phcalc: complex [k][j][kx], kx pitch HP
+  double2* spec = nullptr;
+  // modified wavenumbers (phini.f90:28-56) and coordinates (cordin.f90)
+  double *ak1 = nullptr, *ak2 = nullptr, *ak3 = nullptr;
+  double *xc = nullptr, *xm = nullptr, *yc = nullptr, *ym = nullptr, *zc = nullptr, *zm = nullptr;
+  int coord_off = 0;                      // coordinate arrays cover [-coord_off, ...)
+  // scratch for reductions / Lagrangian work
+  double* red = nullptr;                  // reduction scratch: [0,64) results, [64,...) partials
+  size_t red_elems = 0;
+  double* red_host = nullptr;             // pinned
+  int* dflag = nullptr;                   // device error flags
+  int* hflag = nullptr;                   // pinned copy
+  // Lagrangian scatter plan (sorted cell keys), see lagr.cu
+  struct Plan {
+    int n = 0, cap = 0;                   // entries (27 per triangle)
+    int nseg = 0;
+    int* key = nullptr;                   // sorted cell index
+    int* src = nullptr;                   // triangle*27 + slot
+    int* seg_start = nullptr;             // start offset of each unique key
+    int* seg_key = nullptr;
+    int* tmp_key = nullptr; int* tmp_src = nullptr;
+    int* hist = nullptr;
+    int* nseg_dev = nullptr;
+    bool valid = false;
+  } plan[4];
+  double* tri_coef = nullptr;             // per triangle & component: cfac*(target-Um)
+  double* lag_red = nullptr;              // per-triangle partial sums
+  cudaStream_t stream = nullptr;
+  // fused-step state
+  StepParams* dparams = nullptr;          // [3] device copies (one per substep)
+  StepParams* hparams = nullptr;          // pinned
+  double* rhs4 = nullptr;                 // 4 RHS fields for the fused path
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  bool use_graph = true;
+  uint64_t launches = 0;                  // kernels launched through this context
+
+  double S(int id) const { return *hs[id]; }
+  int I(int id) const { return *hi[id]; }
+};
+
+Ctx* current();
+void fail(Ctx* c, int st, const std::string& m);
+bool cuda_ok(Ctx* c, cudaError_t e, const char* what);
+bool ready(Ctx* c);
+StepParams host_params(Ctx* c);
+
+#define MIBM_LAUNCH_CHECK(c, what) cuda_ok((c), cudaGetLastError(), (what))
+
+inline __host__ __device__ size_t cidx(const Grid& g, int i, int j, int k) {
+  return (size_t)i + (size_t)g.P * ((size_t)j + (size_t)g.n2m * (size_t)k);
+}
+inline __host__ __device__ int wrap(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
+inline __host__ __device__ int fmod_pos(int a, int n) { int r = a % n; return r < 0 ? r + n : r; }
+
+inline unsigned div_up(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
+
+// layout of Ctx::red
+constexpr size_t kRedOut = 0;        // small results
+constexpr size_t kRedPart = 64;      // per-block partials (up to 3 * n2m * n3m)
+
+// mesh helpers
+inline size_t mesh_elems(Ctx* c, int id) {
+  switch (id) {
+    case MIBM_M_XYZV: case MIBM_M_VERT_NOR: case MIBM_M_VMELT: case MIBM_M_VMELT_M1: return 3 * (size_t)c->maxnv;
+    case MIBM_M_VERT_OF_FACE: case MIBM_M_TRI_BAR: case MIBM_M_TRI_NOR: case MIBM_M_VEL_TRI:
+    case MIBM_M_EDGE_OF_FACE: return 3 * (size_t)c->maxnf;
+    case MIBM_M_SUR: case MIBM_M_CFAC: case MIBM_M_GHOST_FACE: case MIBM_M_QW_O: case MIBM_M_QW_I:
+    case MIBM_M_SKEWNESS: return (size_t)c->maxnf;
+    case MIBM_M_AVERT: case MIBM_M_GHOST_VERT: case MIBM_M_QW_OVERT: case MIBM_M_QW_IVERT: return (size_t)c->maxnv;
+    case MIBM_M_PIND: return 6 * (size_t)c->maxnf;
+    case MIBM_M_PTXAB_Q1: case MIBM_M_PTXAB_Q2: case MIBM_M_PTXAB_Q3: case MIBM_M_PTXAB_TEMP: return 27 * (size_t)c->maxnf;
+    case MIBM_M_VERT_OF_EDGE: return 2 * (size_t)c->maxne;
+    case MIBM_M_GHOST_EDGE: return (size_t)c->maxne;
+    case MIBM_M_ELENGTHS: return (size_t)c->maxne;
+  }
+  return 0;
+}
+inline bool mesh_is_int(int id) {
+  return id == MIBM_M_VERT_OF_FACE || id == MIBM_M_GHOST_FACE || id == MIBM_M_GHOST_VERT || id == MIBM_M_PIND ||
+         id == MIBM_M_VERT_OF_EDGE || id == MIBM_M_EDGE_OF_FACE || id == MIBM_M_GHOST_EDGE;
+}
+inline size_t mesh_bytes(Ctx* c, int id) { return mesh_elems(c, id) * (mesh_is_int(id) ? 4 : 8); }
+
+// Fortran host shape of a registered field
+inline void field_host_shape(const Ctx* c, int id, int& ny, int& klo, int& nk) {
+  ny = (id == MIBM_F_DPH) ? c->g.n2m + 2 : c->g.n2m + 1;
+  bool plain = (id >= MIBM_F_RHS && id <= MIBM_F_RUT) || id == MIBM_F_SDF;
+  klo = plain ? 1 : 0;
+  nk = plain ? c->g.n3m : c->g.n3m + 2;
+}
+
+// ---------------------------------------------------------------------
+// kernel-launch entry points implemented in the .cu files
+// ---------------------------------------------------------------------
+// stencil.cu
+void k_hdnl(Ctx* c, int which, const StepParams* dp);
+void k_invtr_rhs(Ctx* c, int which, const StepParams* dp, double* rhs_out);
+void k_fused_rhs(Ctx* c, const StepParams* dp);
+void k_divg(Ctx* c, const StepParams* dp);
+void k_updvp(Ctx* c, const StepParams* dp);
+void k_prcalc(Ctx* c, const StepParams* dp);
+void k_add_field(Ctx* c, double* q, const double* r);
+double k_cfl(Ctx* c);
+double k_get_dt_buffer(Ctx* c, double dt, double ren);
+void k_interp_vof(Ctx* c);
+void k_velforce_apply(Ctx* c, const double* mean3);
+void k_tempforce_apply(Ctx* c);
+// tridiag.cu
+void k_solve_x(Ctx* c, double* rhs, double betadx);
+void k_solve_y(Ctx* c, double* rhs, double betadx);
+void k_solve_z(Ctx* c, double* rhs, double betadx, double* q);
+// fft.cu
+void k_phcalc(Ctx* c);
+// lagr.cu
+void lagr_find_centroid_indices(Ctx* c);
+void lagr_mls_weight(Ctx* c);
+void lagr_mls_force(Ctx* c, const StepParams* dp, bool dense_forces);
+void lagr_velforce(Ctx* c);
+void lagr_tempforce(Ctx* c);
+void lagr_find_probe_indices(Ctx* c);
+void lagr_heat_flux(Ctx* c);
+void lagr_stefan(Ctx* c, const StepParams* dp);
+void lagr_geometry_refresh(Ctx* c, bool imelt);
+void lagr_tag_narrow_band(Ctx* c);
+void lagr_tag_initial(Ctx* c);
+void lagr_particle(Ctx* c, const StepParams* dp);
+void lagr_free(Ctx* c);
+// ctx.cu
+bool ensure_params(Ctx* c);
+bool validate_mesh(Ctx* c);
+void release(Ctx* c);
+
+}  // namespace mibm

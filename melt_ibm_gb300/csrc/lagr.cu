@@ -1,0 +1,1233 @@
+// lagr.cu -- immersed-boundary (Lagrangian) part of the substep.
+//
+// Restates on the device:
+//   findCentroidIndices.f90:14-50           centroid cage indices
+//   mlsWeight.f90:48-412, geom.f90:24-53     MLS shape functions (FP64 4x4 LU)
+//   mlsForce.f90:13-33, forc1/2/3/temp.f90  interpolation + force spreading
+//   velforce.f90:13-52, tempforce.f90:13-40 mean removal and field update
+//   findProbeIndices.f90:20-74              +/- normal probe cages
+//   mls_heatFlux.f90:77-395                 MLS gradient of T, face->vertex
+//   stefanCondition.f90:12-31               Stefan front advance
+//   triaux.f90:53-323, RigidAuxRoutines.f90:653-780  geometry refresh
+//   genSDF.f90:120-365, tagCells.f90:85-111 narrow-band tagging
+//   pencil_rayTag.f90:37-460                initial full tagging
+//
+// Determinism: no floating-point atomics anywhere.  Force spreading is an
+// atomics-free sorted scatter: the 27 cage cells of every triangle are keyed
+// by cell index and stably radix-sorted once per geometry (the key order
+// depends only on the mesh), then each unique cell sums its contributions in
+// triangle order -- the reference's summation order.  Face->vertex sums use
+// a vertex->face adjacency list in ascending face order.  The narrow band
+// takes the minimum distance with 64-bit integer atomicMin on the
+// (non-negative) IEEE bit pattern and the earliest triangle among equal
+// distances, exactly the strict "<" update rule of genSDF.f90:167.
+#include <climits>
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+
+namespace mibm {
+
+// ---------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------
+struct LagArgs {
+  Grid g;
+  int nf, nv, coff, clen;
+  const double* xc; const double* xm; const double* yc; const double* ym; const double* zc; const double* zm;
+  double wcon, wscl;
+};
+
+static LagArgs lag_args(Ctx* c) {
+  LagArgs a;
+  a.g = c->g; a.nf = c->maxnf; a.nv = c->maxnv; a.coff = c->coord_off; a.clen = 3 * c->coord_off;
+  a.xc = c->xc; a.xm = c->xm; a.yc = c->yc; a.ym = c->ym; a.zc = c->zc; a.zm = c->zm;
+  a.wcon = c->S(MIBM_S_WCON); a.wscl = c->S(MIBM_S_WSCL);
+  return a;
+}
+
+template <typename T> static T* M(Ctx* c, int id) { return (T*)c->dm[id]; }
+
+__device__ __forceinline__ int ffloor(double x) { return (int)floor(x); }
+__device__ __forceinline__ int fnint(double x) { return (int)round(x); }
+__device__ __forceinline__ double sqd(double x) { return x * x; }
+
+__device__ __forceinline__ double coord(const LagArgs& A, int dir, int sel, int idx) {
+  // sel 0 = c (face) coordinates, 1 = m (centre).  The tables span
+  // [-coff, 2*coff) grid indices, more than the reference's -n..2n; a body
+  // outside that range is clamped instead of read out of bounds.
+  int t = min(max(idx + A.coff, 0), A.clen - 1);
+  if (dir == 0) return sel == 0 ? A.xc[t] : A.xm[t];
+  if (dir == 1) return sel == 0 ? A.yc[t] : A.ym[t];
+  return sel == 0 ? A.zc[t] : A.zm[t];
+}
+
+__device__ __forceinline__ double mls_gaussian(double r, double rcoef) { return (r > 1.0) ? 0.0 : exp(-sqd(r / rcoef)); }
+__device__ __forceinline__ double mls_gauss_deriv(double r, double rcoef) {
+  return (r > 1.0) ? 0.0 : -2.0 * r / sqd(rcoef) * exp(-sqd(r / rcoef));
+}
+
+// In-place inverse of a 4x4 column-major matrix: LU with partial pivoting
+// (dgetrf semantics, first maximal pivot) and inversion from the factors
+// (dgetri).  Returns false if a pivot is exactly zero.
+__device__ bool inv4(double* a) {
+  const int n = 4;
+  int ipiv[4];
+  for (int j = 0; j < n; ++j) {
+    int p = j;
+    double amax = fabs(a[j + n * j]);
+    for (int i = j + 1; i < n; ++i)
+      if (fabs(a[i + n * j]) > amax) { amax = fabs(a[i + n * j]); p = i; }
+    ipiv[j] = p;
+    if (a[p + n * j] == 0.0) return false;
+    if (p != j)
+      for (int cc = 0; cc < n; ++cc) { double t = a[j + n * cc]; a[j + n * cc] = a[p + n * cc]; a[p + n * cc] = t; }
+    double r = 1.0 / a[j + n * j];
+    for (int i = j + 1; i < n; ++i) a[i + n * j] *= r;
+    for (int cc = j + 1; cc < n; ++cc) {
+      double t = a[j + n * cc];
+      for (int i = j + 1; i < n; ++i) a[i + n * cc] -= t * a[i + n * j];
+    }
+  }
+  for (int j = 0; j < n; ++j) {
+    a[j + n * j] = 1.0 / a[j + n * j];
+    double ajj = -a[j + n * j];
+    for (int i = 0; i < j; ++i) {
+      double s = 0;
+      for (int k = i; k < j; ++k) s += a[i + n * k] * a[k + n * j];
+      a[i + n * j] = s;
+    }
+    for (int i = 0; i < j; ++i) a[i + n * j] *= ajj;
+  }
+  double work[4];
+  for (int j = n - 1; j >= 0; --j) {
+    for (int i = j + 1; i < n; ++i) { work[i] = a[i + n * j]; a[i + n * j] = 0.0; }
+    if (j < n - 1)
+      for (int i = 0; i < n; ++i) {
+        double s = 0;
+        for (int k = j + 1; k < n; ++k) s += a[i + n * k] * work[k];
+        a[i + n * j] -= s;
+      }
+  }
+  for (int j = n - 2; j >= 0; --j) {
+    int jp = ipiv[j];
+    if (jp != j)
+      for (int i = 0; i < n; ++i) { double t = a[i + n * j]; a[i + n * j] = a[i + n * jp]; a[i + n * jp] = t; }
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------
+// findCentroidIndices / findProbeIndices
+// ---------------------------------------------------------------------
+__global__ void centroid_idx_kernel(LagArgs A, const double* __restrict__ tri_bar, const int* __restrict__ ghost,
+                                    int* __restrict__ pind) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= A.nf || ghost[t]) return;
+  const Grid& g = A.g;
+  double px = tri_bar[3 * t], py = tri_bar[3 * t + 1], pz = tri_bar[3 * t + 2];
+  int i1 = ffloor(px * g.dx1) + 1, ist = fnint(px * g.dx1) + 1;
+  int j1 = ffloor(py * g.dx2) + 1, jst = fnint(py * g.dx2) + 1;
+  int k1 = ffloor(pz * g.dx3) + 1, kst = fnint(pz * g.dx3) + 1;
+  k1 = fmod_pos(k1 - 1, g.n3m) + 1;
+  kst = fmod_pos(kst - 1, g.n3m) + 1;
+  int* p = pind + 6 * t;
+  p[0] = i1; p[1] = j1; p[2] = k1; p[3] = ist; p[4] = jst; p[5] = kst;
+}
+
+__global__ void probe_idx_kernel(LagArgs A, const double* __restrict__ tri_bar, const double* __restrict__ tri_nor,
+                                 const int* __restrict__ ghost, double h, int* __restrict__ pind) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= A.nf || ghost[t]) return;
+  const Grid& g = A.g;
+  double n0 = tri_nor[3 * t], n1 = tri_nor[3 * t + 1], n2 = tri_nor[3 * t + 2];
+  double s = sqrt(n0 * n0 + n1 * n1 + n2 * n2);
+  for (int side = 0; side < 2; ++side) {
+    double pos[3];
+    for (int d = 0; d < 3; ++d) {
+      double nd = tri_nor[3 * t + d];
+      pos[d] = side == 0 ? tri_bar[3 * t + d] + h * nd / s : tri_bar[3 * t + d] - h * nd / s;
+    }
+    int i1 = ffloor(pos[0] * g.dx1) + 1, j1 = ffloor(pos[1] * g.dx2) + 1, k1 = ffloor(pos[2] * g.dx3) + 1;
+    k1 = fmod_pos(k1 - 1, g.n3m) + 1;
+    pind[6 * t + 3 * side + 0] = i1; pind[6 * t + 3 * side + 1] = j1; pind[6 * t + 3 * side + 2] = k1;
+  }
+}
+
+// ---------------------------------------------------------------------
+// mlsWeight: one thread per (triangle, component)
+// component 0 = wght1 (vx), 1 = wght2 (vy), 2 = wght3 (vz), 3 = wghttemp
+// ---------------------------------------------------------------------
+struct CageSpec {
+  int ix, iy;      // pind slot (0-based) of the x and y cage centre
+  int sx, sy, sz;  // coordinate selector per axis (0 = c, 1 = m)
+  bool znint;      // z centre from nint (wght3) or floor
+};
+__device__ __forceinline__ CageSpec cage_spec(int comp) {
+  switch (comp) {
+    case 0: return CageSpec{3, 1, 0, 1, 1, false};   // xc, ym, zm ; pind(4), pind(2)
+    case 1: return CageSpec{0, 4, 1, 0, 1, false};   // xm, yc, zm ; pind(1), pind(5)
+    case 2: return CageSpec{0, 1, 1, 1, 0, true};    // xm, ym, zc ; pind(1), pind(2)
+  }
+  return CageSpec{0, 1, 1, 1, 1, false};             // xm, ym, zm ; pind(1), pind(2)
+}
+
+__global__ void mls_weight_kernel(LagArgs A, const double* __restrict__ tri_bar, const int* __restrict__ ghost,
+                                  const int* __restrict__ pind, double* __restrict__ p1, double* __restrict__ p2,
+                                  double* __restrict__ p3, double* __restrict__ pt, int* __restrict__ flag) {
+  int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  int t = gid >> 2, comp = gid & 3;
+  if (t >= A.nf || ghost[t]) return;
+  const Grid& g = A.g;
+  double pos[3] = {tri_bar[3 * t], tri_bar[3 * t + 1], tri_bar[3 * t + 2]};
+  double ptx[4] = {1.0, pos[0], pos[1], pos[2]};
+  CageSpec cs = cage_spec(comp);
+  int i0 = pind[6 * t + cs.ix], j0 = pind[6 * t + cs.iy];
+  int k0 = cs.znint ? fnint(pos[2] * g.dx3) + 1 : ffloor(pos[2] * g.dx3) + 1;
+  // separable Gaussian weights (the reference evaluates the same 9 values)
+  double wz[3], wy[3], wx[3], cz[3], cy[3], cx[3];
+  for (int q = 0; q < 3; ++q) {
+    cz[q] = coord(A, 2, cs.sz, k0 - 1 + q);
+    cy[q] = coord(A, 1, cs.sy, j0 - 1 + q);
+    cx[q] = coord(A, 0, cs.sx, i0 - 1 + q);
+    wz[q] = mls_gaussian(fabs(cz[q] - pos[2]) / (A.wscl / g.dx3), A.wcon);
+    wy[q] = mls_gaussian(fabs(cy[q] - pos[1]) / (A.wscl / g.dx2), A.wcon);
+    wx[q] = mls_gaussian(fabs(cx[q] - pos[0]) / (A.wscl / g.dx1), A.wcon);
+  }
+  double Am[16];
+  for (int q = 0; q < 16; ++q) Am[q] = 0.0;
+  double W[27];
+  for (int kk = 0; kk < 3; ++kk)
+    for (int jj = 0; jj < 3; ++jj) {
+      double w23 = wy[jj] * wz[kk];
+      for (int ii = 0; ii < 3; ++ii) {
+        double wtx = wx[ii] * w23;
+        W[ii + 3 * jj + 9 * kk] = wtx;
+        double pk[4] = {1.0, cx[ii], cy[jj], cz[kk]};
+        for (int cc = 0; cc < 4; ++cc) {
+          double tt = wtx * pk[cc];
+          for (int r = 0; r < 4; ++r) Am[r + 4 * cc] = Am[r + 4 * cc] + tt * pk[r];
+        }
+      }
+    }
+  if (!inv4(Am)) { atomicOr(flag, 1); return; }
+  double ptxA[4];
+  for (int cc = 0; cc < 4; ++cc) {
+    double s = 0;
+    for (int r = 0; r < 4; ++r) s += ptx[r] * Am[r + 4 * cc];
+    ptxA[cc] = s;
+  }
+  double* out = (comp == 0) ? p1 : (comp == 1) ? p2 : (comp == 2) ? p3 : pt;
+  out += 27 * (size_t)t;
+  for (int kk = 0; kk < 3; ++kk)
+    for (int jj = 0; jj < 3; ++jj)
+      for (int ii = 0; ii < 3; ++ii) {
+        int n = ii + 3 * jj + 9 * kk;
+        double wtx = W[n];
+        // B(:,n) = wtx * [1, x, y, z]
+        double s = ptxA[0] * (wtx * 1.0) + ptxA[1] * (wtx * cx[ii]) + ptxA[2] * (wtx * cy[jj]) + ptxA[3] * (wtx * cz[kk]);
+        out[n] = s;
+      }
+}
+
+// ---------------------------------------------------------------------
+// mlsForce: interpolation Um per (triangle, component) and coefficient
+// cfac*(target - Um); the spread goes through the sorted scatter plan.
+// ---------------------------------------------------------------------
+struct ForceArgs {
+  const double* q[4];       // vx, vy, vz, temp (compact)
+  const double* ptx[4];
+  const double* vel_tri;
+  const double* cfac;
+  const int* pind;
+  const int* ghost;
+};
+
+__device__ __forceinline__ void cage_center(int comp, const int* p, int& i0, int& j0, int& k0) {
+  // forc1: pind(4), pind(2), pind(3); forc2: pind(1), pind(5), pind(3)
+  // forc3: pind(1), pind(2), pind(6); forctemp: pind(1), pind(2), pind(3)
+  switch (comp) {
+    case 0: i0 = p[3]; j0 = p[1]; k0 = p[2]; return;
+    case 1: i0 = p[0]; j0 = p[4]; k0 = p[2]; return;
+    case 2: i0 = p[0]; j0 = p[1]; k0 = p[5]; return;
+  }
+  i0 = p[0]; j0 = p[1]; k0 = p[2];
+}
+
+__device__ __forceinline__ size_t cage_cell(const Grid& g, int i0, int j0, int k0, int slot) {
+  int ii = fmod_pos(i0 - 2 + slot % 3, g.n1m);
+  int jj = fmod_pos(j0 - 2 + (slot / 3) % 3, g.n2m);
+  int kk = fmod_pos(k0 - 2 + slot / 9, g.n3m);
+  return cidx(g, ii, jj, kk);
+}
+
+__global__ void force_coef_kernel(Grid g, int nf, ForceArgs F, double tmelt, double* __restrict__ coef) {
+  int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  int t = gid >> 2, comp = gid & 3;
+  if (t >= nf) return;
+  if (F.ghost[t]) { coef[comp * (size_t)nf + t] = 0.0; return; }
+  int i0, j0, k0;
+  cage_center(comp, F.pind + 6 * t, i0, j0, k0);
+  const double* phi = F.ptx[comp] + 27 * (size_t)t;
+  const double* q = F.q[comp];
+  double Um = 0.0;
+  for (int s = 0; s < 27; ++s) Um = Um + q[cage_cell(g, i0, j0, k0, s)] * phi[s];
+  double target = (comp == 3) ? tmelt : F.vel_tri[3 * t + comp];
+  coef[comp * (size_t)nf + t] = F.cfac[t] * (target - Um);
+}
+
+// ---------------------------------------------------------------------
+// Stable LSD radix sort of (key, value) pairs, 8-bit digits.
+// ---------------------------------------------------------------------
+constexpr int kSortChunk = 4096;
+
+__global__ void plan_keys_kernel(Grid g, int nf, int comp, const int* __restrict__ pind, const int* __restrict__ ghost,
+                                 int* __restrict__ key, int* __restrict__ src) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= 27 * nf) return;
+  int t = e / 27, s = e % 27;
+  if (ghost[t]) { key[e] = INT_MAX; src[e] = e; return; }
+  int i0, j0, k0;
+  cage_center(comp, pind + 6 * t, i0, j0, k0);
+  key[e] = (int)cage_cell(g, i0, j0, k0, s);
+  src[e] = e;
+}
+
+__global__ void radix_hist_kernel(const int* __restrict__ key, int n, int shift, int nblk, int* __restrict__ hist) {
+  __shared__ int h[256];
+  for (int d = threadIdx.x; d < 256; d += blockDim.x) h[d] = 0;
+  __syncthreads();
+  int b = blockIdx.x;
+  int end = min(n, (b + 1) * kSortChunk);
+  for (int e = b * kSortChunk + threadIdx.x; e < end; e += blockDim.x) atomicAdd(&h[(key[e] >> shift) & 255], 1);
+  __syncthreads();
+  for (int d = threadIdx.x; d < 256; d += blockDim.x) hist[d * nblk + b] = h[d];
+}
+
+// exclusive scan of m ints by one block of 1024 threads
+__global__ void scan_kernel(int* __restrict__ a, int m) {
+  __shared__ int part[1024];
+  int per = (m + blockDim.x - 1) / blockDim.x;
+  int lo = threadIdx.x * per, hi = min(m, lo + per);
+  int s = 0;
+  for (int q = lo; q < hi; ++q) s += a[q];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int off = 1; off < blockDim.x; off <<= 1) {
+    int v = (threadIdx.x >= off) ? part[threadIdx.x - off] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int run = (threadIdx.x == 0) ? 0 : part[threadIdx.x - 1];
+  for (int q = lo; q < hi; ++q) { int v = a[q]; a[q] = run; run += v; }
+}
+
+__global__ void radix_scatter_kernel(const int* __restrict__ kin, const int* __restrict__ vin, int* __restrict__ kout,
+                                     int* __restrict__ vout, int n, int shift, int nblk, const int* __restrict__ offs) {
+  __shared__ int base[256];
+  __shared__ int wcnt[8][256];
+  int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  for (int d = tid; d < 256; d += 256) base[d] = offs[d * nblk + b];
+  __syncthreads();
+  int end = min(n, (b + 1) * kSortChunk);
+  for (int start = b * kSortChunk; start < end; start += 256) {
+    int idx = start + tid;
+    bool valid = idx < end;
+    int key = valid ? kin[idx] : 0;
+    int dig = valid ? ((key >> shift) & 255) : 256;
+    for (int q = tid; q < 8 * 256; q += 256) (&wcnt[0][0])[q] = 0;
+    __syncthreads();
+    unsigned peers = __match_any_sync(0xffffffffu, dig);
+    int rank = __popc(peers & ((1u << lane) - 1u));
+    int leader = __ffs(peers) - 1;
+    if (valid && lane == leader) wcnt[w][dig] = __popc(peers);
+    __syncthreads();
+    if (valid) {
+      int pre = 0;
+      for (int q = 0; q < w; ++q) pre += wcnt[q][dig];
+      int pos = base[dig] + pre + rank;
+      kout[pos] = key;
+      vout[pos] = vin[idx];
+    }
+    __syncthreads();
+    for (int d = tid; d < 256; d += 256) {
+      int tot = 0;
+      for (int q = 0; q < 8; ++q) tot += wcnt[q][d];
+      base[d] += tot;
+    }
+    __syncthreads();
+  }
+}
+
+static bool plan_alloc(Ctx* c, Ctx::Plan& p, int n) {
+  if (p.cap >= n) return true;
+  cudaFree(p.key); cudaFree(p.src); cudaFree(p.tmp_key); cudaFree(p.tmp_src); cudaFree(p.hist);
+  int nblk = (n + kSortChunk - 1) / kSortChunk;
+  bool ok = cuda_ok(c, cudaMalloc(&p.key, sizeof(int) * n), "plan") && cuda_ok(c, cudaMalloc(&p.src, sizeof(int) * n), "plan") &&
+            cuda_ok(c, cudaMalloc(&p.tmp_key, sizeof(int) * n), "plan") &&
+            cuda_ok(c, cudaMalloc(&p.tmp_src, sizeof(int) * n), "plan") &&
+            cuda_ok(c, cudaMalloc(&p.hist, sizeof(int) * 256 * (size_t)nblk), "plan");
+  if (ok) p.cap = n;
+  return ok;
+}
+
+// Build the sorted scatter plan of one component: keys = cage cell indices.
+static void build_plan(Ctx* c, int comp) {
+  Ctx::Plan& p = c->plan[comp];
+  int nf = c->maxnf, n = 27 * nf;
+  if (n == 0) { p.n = 0; p.valid = true; return; }
+  if (!plan_alloc(c, p, n)) return;
+  p.n = n;
+  plan_keys_kernel<<<div_up(n, 256), 256, 0, c->stream>>>(c->g, nf, comp, M<int>(c, MIBM_M_PIND),
+                                                          M<int>(c, MIBM_M_GHOST_FACE), p.tmp_key, p.tmp_src);
+  ++c->launches;
+  int nblk = (n + kSortChunk - 1) / kSortChunk;
+  // cell keys < cells (< 2^31); INT_MAX marks ghost faces
+  int bits = 31;
+  int* kin = p.tmp_key; int* vin = p.tmp_src; int* kout = p.key; int* vout = p.src;
+  int passes = (bits + 7) / 8;
+  for (int ps = 0; ps < passes; ++ps) {
+    int shift = 8 * ps;
+    radix_hist_kernel<<<nblk, 256, 0, c->stream>>>(kin, n, shift, nblk, p.hist);
+    scan_kernel<<<1, 1024, 0, c->stream>>>(p.hist, 256 * nblk);
+    radix_scatter_kernel<<<nblk, 256, 0, c->stream>>>(kin, vin, kout, vout, n, shift, nblk, p.hist);
+    c->launches += 3;
+    std::swap(kin, kout); std::swap(vin, vout);
+  }
+  // after an even number of passes the result is in tmp_*; make key/src hold it
+  if (kin != p.key) { std::swap(p.key, p.tmp_key); std::swap(p.src, p.tmp_src); }
+  p.valid = MIBM_LAUNCH_CHECK(c, "build_plan");
+}
+
+// Segment heads of the sorted keys sum their run in order and add the sum
+// to the dense force field (each cell written by exactly one thread).
+__global__ void scatter_apply_kernel(int n, const int* __restrict__ key, const int* __restrict__ src,
+                                     const double* __restrict__ coef, const double* __restrict__ phi,
+                                     double* __restrict__ out) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  int k = key[e];
+  if (k == INT_MAX || (e > 0 && key[e - 1] == k)) return;
+  double s = 0.0;
+  for (int q = e; q < n && key[q] == k; ++q) {
+    int sr = src[q];
+    int t = sr / 27;
+    s = s + coef[t] * phi[sr];
+  }
+  out[k] = out[k] + s;
+}
+
+// ---------------------------------------------------------------------
+// deterministic sums
+// ---------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// per-block partial sums of up to 3 fields over the owned cells, fixed order
+__global__ void field_sum_kernel(Grid g, const double* __restrict__ a, const double* __restrict__ b,
+                                 const double* __restrict__ cc, double* __restrict__ part) {
+  int j = blockIdx.x, k = blockIdx.y;
+  double s[3] = {0, 0, 0};
+  for (int i = threadIdx.x; i < g.n1m; i += blockDim.x) {
+    size_t c0 = cidx(g, i, j, k);
+    s[0] += a[c0]; s[1] += b[c0]; s[2] += cc[c0];
+  }
+  __shared__ double sm[3][32];
+  for (int q = 0; q < 3; ++q) {
+    double v = warp_sum(s[q]);
+    if ((threadIdx.x & 31) == 0) sm[q][threadIdx.x >> 5] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    int nw = blockDim.x >> 5;
+    for (int q = 0; q < 3; ++q) {
+      double v = (threadIdx.x < nw) ? sm[q][threadIdx.x] : 0.0;
+      v = warp_sum(v);
+      if (threadIdx.x == 0) part[3 * ((size_t)j + (size_t)g.n2m * k) + q] = v;
+    }
+  }
+}
+
+// sum m triples in fixed order, divide by the cell count -> mean3
+__global__ void mean3_kernel(const double* __restrict__ part, int m, double ncell, double* __restrict__ out) {
+  __shared__ double sm[3][1024];
+  double s[3] = {0, 0, 0};
+  for (int t = threadIdx.x; t < m; t += blockDim.x)
+    for (int q = 0; q < 3; ++q) s[q] += part[3 * (size_t)t + q];
+  for (int q = 0; q < 3; ++q) sm[q][threadIdx.x] = s[q];
+  __syncthreads();
+  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off)
+      for (int q = 0; q < 3; ++q) sm[q][threadIdx.x] += sm[q][threadIdx.x + off];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int q = 0; q < 3; ++q) out[q] = sm[q][0] / ncell;
+}
+
+// ---------------------------------------------------------------------
+// heat flux (wght_gradT, mls_heatFlux.f90:161-376): one thread per
+// (triangle, side); result qw_o / qw_i per face
+// ---------------------------------------------------------------------
+__global__ void heat_flux_kernel(LagArgs A, const double* __restrict__ temp, const double* __restrict__ tri_bar,
+                                 const double* __restrict__ tri_nor, const int* __restrict__ ghost,
+                                 const int* __restrict__ pind, double h, double pec, double* __restrict__ qw_o,
+                                 double* __restrict__ qw_i, int* __restrict__ flag) {
+  int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  int t = gid >> 1, side = gid & 1;
+  if (t >= A.nf) return;
+  double* qout = side == 0 ? qw_o : qw_i;
+  if (ghost[t]) { qout[t] = 0.0; return; }
+  const Grid& g = A.g;
+  double n0 = tri_nor[3 * t], n1 = tri_nor[3 * t + 1], n2 = tri_nor[3 * t + 2];
+  double s = sqrt(n0 * n0 + n1 * n1 + n2 * n2);
+  double pos[3];
+  for (int d = 0; d < 3; ++d) {
+    double nd = tri_nor[3 * t + d];
+    pos[d] = side == 0 ? tri_bar[3 * t + d] + h * nd / s : tri_bar[3 * t + d] - h * nd / s;
+  }
+  double ptx[4] = {1.0, pos[0], pos[1], pos[2]};
+  int pi1 = pind[6 * t + 3 * side + 0], pi2 = pind[6 * t + 3 * side + 1];
+  const double eps = 2.220446049250313e-16;
+  int k1 = ffloor(pos[2] * g.dx3) + 1;
+  int kin[3] = {k1 - 1, k1, k1};                  // mls_heatFlux.f90:213 (third layer repeats k1)
+  int k1w = fmod_pos(k1 - 1, g.n3m) + 1;
+  int keul[3] = {k1w - 1, k1w, k1w + 1};
+  double Am[16], dA[3][16];
+  for (int q = 0; q < 16; ++q) { Am[q] = 0; dA[0][q] = 0; dA[1][q] = 0; dA[2][q] = 0; }
+  double W[27], dW[3][27], Tn[27], px[3], py[3], pzv[3];
+  double wx[3], wy[3], wz[3], dwx[3], dwy[3], dwz[3];
+  for (int q = 0; q < 3; ++q) {
+    int k = kin[q];
+    pzv[q] = coord(A, 2, 1, k);
+    double np3 = fabs(pos[2] - pzv[q]) / (A.wscl / g.dx3);
+    wz[q] = mls_gaussian(np3, A.wcon);
+    if (np3 < eps) dwz[q] = 0.0;
+    else dwz[q] = mls_gauss_deriv(np3, A.wcon) * ((pos[2] - pzv[q]) / fabs(pos[2] - pzv[q]) / (A.wscl / g.dx3));
+    int j = pi2 - 1 + q;
+    py[q] = coord(A, 1, 1, j);
+    double np2 = fabs(pos[1] - py[q]) / (A.wscl / g.dx2);
+    wy[q] = mls_gaussian(np2, A.wcon);
+    if (np2 < eps) dwy[q] = 0.0;
+    else dwy[q] = mls_gauss_deriv(np2, A.wcon) * ((pos[1] - py[q]) / fabs(pos[1] - py[q]) / (A.wscl / g.dx2));
+    int i = pi1 - 1 + q;
+    px[q] = coord(A, 0, 1, i);
+    double np1 = fabs(pos[0] - px[q]) / (A.wscl / g.dx1);
+    wx[q] = mls_gaussian(np1, A.wcon);
+    if (np1 < eps) dwx[q] = 0.0;
+    else dwx[q] = mls_gauss_deriv(np1, A.wcon) * ((pos[0] - px[q]) / fabs(pos[0] - px[q]) / (A.wscl / g.dx1));
+  }
+  for (int kk = 0; kk < 3; ++kk)
+    for (int jj = 0; jj < 3; ++jj)
+      for (int ii = 0; ii < 3; ++ii) {
+        int n = ii + 3 * jj + 9 * kk;
+        double wtx = wx[ii] * (wy[jj] * wz[kk]);
+        double dwdx = dwx[ii] * wy[jj] * wz[kk];
+        double dwdy = wx[ii] * dwy[jj] * wz[kk];
+        double dwdz = wx[ii] * wy[jj] * dwz[kk];
+        W[n] = wtx; dW[0][n] = dwdx; dW[1][n] = dwdy; dW[2][n] = dwdz;
+        double pk[4] = {1.0, px[ii], py[jj], pzv[kk]};
+        for (int cc = 0; cc < 4; ++cc) {
+          double a0 = wtx * pk[cc], a1 = dwdx * pk[cc], a2 = dwdy * pk[cc], a3 = dwdz * pk[cc];
+          for (int r = 0; r < 4; ++r) {
+            Am[r + 4 * cc] += a0 * pk[r];
+            dA[0][r + 4 * cc] += a1 * pk[r];
+            dA[1][r + 4 * cc] += a2 * pk[r];
+            dA[2][r + 4 * cc] += a3 * pk[r];
+          }
+        }
+        int ii_ = fmod_pos(pi1 - 1 + ii - 1, g.n1m), jj_ = fmod_pos(pi2 - 1 + jj - 1, g.n2m);
+        int kk_ = wrap(keul[kk] - 1, g.n3m);
+        Tn[n] = temp[cidx(g, ii_, jj_, kk_)];
+      }
+  if (!inv4(Am)) { atomicOr(flag, 1); qout[t] = 0.0; return; }
+  double gam[4];
+  for (int r = 0; r < 4; ++r) {
+    double a = 0;
+    for (int cc = 0; cc < 4; ++cc) a += Am[r + 4 * cc] * ptx[cc];
+    gam[r] = a;
+  }
+  double grad[3];
+  for (int d = 0; d < 3; ++d) {
+    double pk[4] = {0, 0, 0, 0};
+    pk[d + 1] = 1.0;
+    for (int r = 0; r < 4; ++r) {
+      double a = 0;
+      for (int cc = 0; cc < 4; ++cc) a += dA[d][r + 4 * cc] * gam[cc];
+      pk[r] = pk[r] - a;
+    }
+    double dg[4];
+    for (int r = 0; r < 4; ++r) {
+      double a = 0;
+      for (int cc = 0; cc < 4; ++cc) a += Am[r + 4 * cc] * pk[cc];
+      dg[r] = a;
+    }
+    double acc = 0;
+    for (int kk = 0; kk < 3; ++kk)
+      for (int jj = 0; jj < 3; ++jj)
+        for (int ii = 0; ii < 3; ++ii) {
+          int n = ii + 3 * jj + 9 * kk;
+          double pk2[4] = {1.0, px[ii], py[jj], pzv[kk]};
+          double t1 = 0, t2 = 0;
+          for (int r = 0; r < 4; ++r) t1 += dg[r] * (W[n] * pk2[r]);
+          for (int r = 0; r < 4; ++r) t2 += gam[r] * (dW[d][n] * pk2[r]);
+          acc += (t1 + t2) * Tn[n];
+        }
+    grad[d] = acc;
+  }
+  double qv = n0 * grad[0] + n1 * grad[1] + n2 * grad[2];
+  qout[t] = qv / pec;
+}
+
+// face -> vertex: qw_v(v) = sum over adjacent faces (ascending) of q_f*(A_f/3/A_v)
+__global__ void face_to_vert_kernel(int nv, const int* __restrict__ adj_off, const int* __restrict__ adj_face,
+                                    const double* __restrict__ sur, const double* __restrict__ avert,
+                                    const double* __restrict__ qf_o, const double* __restrict__ qf_i,
+                                    double* __restrict__ qv_o, double* __restrict__ qv_i) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  double so = 0.0, si = 0.0, av = avert[v];
+  for (int q = adj_off[v]; q < adj_off[v + 1]; ++q) {
+    int f = adj_face[q];
+    double w = sur[f] / 3.0 / av;
+    so = so + qf_o[f] * w;
+    si = si + qf_i[f] * w;
+  }
+  qv_o[v] = so;
+  qv_i[v] = si;
+}
+
+__global__ void stefan_kernel(int nv, const int* __restrict__ ghostv, const double* __restrict__ vert_nor,
+                              const double* __restrict__ qv_o, const double* __restrict__ qv_i, double cp_over_L,
+                              const StepParams* __restrict__ pp, double* __restrict__ vmelt,
+                              double* __restrict__ vmelt_m1, double* __restrict__ xyzv) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  double dt = pp->dt, ga = pp->ga, ro = pp->ro;
+  for (int d = 0; d < 3; ++d) vmelt_m1[3 * v + d] = vmelt[3 * v + d];
+  if (ghostv[v]) return;
+  double dq = qv_i[v] - qv_o[v];
+  for (int d = 0; d < 3; ++d) {
+    double vm = cp_over_L * dq * vert_nor[3 * v + d];
+    vmelt[3 * v + d] = vm;
+    xyzv[3 * v + d] = xyzv[3 * v + d] + dt * (ga * vm + ro * vmelt_m1[3 * v + d]);
+  }
+}
+
+// ---------------------------------------------------------------------
+// geometry refresh (particle.f90:165-193)
+// ---------------------------------------------------------------------
+__global__ void face_geom_kernel(int nf, const int* __restrict__ vof, const int* __restrict__ ghost,
+                                 const double* __restrict__ x, double* __restrict__ sur, double* __restrict__ nor,
+                                 double* __restrict__ bar, double* __restrict__ part /* 11 per face */) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nf) return;
+  double* pp = part + 11 * (size_t)t;
+  if (ghost[t]) { for (int q = 0; q < 11; ++q) pp[q] = 0.0; return; }
+  int a = vof[3 * t] - 1, b = vof[3 * t + 1] - 1, d = vof[3 * t + 2] - 1;
+  double x1 = x[3 * a], y1 = x[3 * a + 1], z1 = x[3 * a + 2];
+  double x2 = x[3 * b], y2 = x[3 * b + 1], z2 = x[3 * b + 2];
+  double x3 = x[3 * d], y3 = x[3 * d + 1], z3 = x[3 * d + 2];
+  // calculate_area (triaux.f90:82-119)
+  double d12 = sqrt(sqd(x1 - x2) + sqd(y1 - y2) + sqd(z1 - z2));
+  double d23 = sqrt(sqd(x2 - x3) + sqd(y2 - y3) + sqd(z2 - z3));
+  double d31 = sqrt(sqd(x3 - x1) + sqd(y3 - y1) + sqd(z3 - z1));
+  double sp = (d12 + d23 + d31) / 2.0;
+  double ar = sqrt(sp * (sp - d12) * (sp - d23) * (sp - d31));
+  sur[t] = ar;
+  // update_tri_normal (triaux.f90:183-232)
+  double e1x = x2 - x1, e1y = y2 - y1, e1z = z2 - z1, e2x = x3 - x1, e2y = y3 - y1, e2z = z3 - z1;
+  double n0 = e1y * e2z - e1z * e2y, n1 = e1z * e2x - e1x * e2z, n2 = e1x * e2y - e1y * e2x;
+  double m = sqrt(n0 * n0 + n1 * n1 + n2 * n2);
+  nor[3 * t] = n0 / m; nor[3 * t + 1] = n1 / m; nor[3 * t + 2] = n2 / m;
+  // calc_centroids_from_vert (triaux.f90:308-323)
+  bar[3 * t] = (x1 + x2 + x3) / 3.0; bar[3 * t + 1] = (y1 + y2 + y3) / 3.0; bar[3 * t + 2] = (z1 + z2 + z3) / 3.0;
+  // calculate_volume summand (triaux.f90:53-80)
+  double vol = x1 * (y2 * z3 - z2 * y3) + x2 * (y3 * z1 - z3 * y1) + x3 * (y1 * z2 - z1 * y2);
+  // calc_rigidBody_params summands (RigidAuxRoutines.f90:704-733)
+  double v = x1 * y2 * z3 + y1 * z2 * x3 + x2 * y3 * z1 - (x3 * y2 * z1 + x2 * y1 * z3 + y3 * z2 * x1);
+  double x4 = x1 + x2 + x3, y4 = y1 + y2 + y3, z4 = z1 + z2 + z3;
+  pp[0] = ar; pp[1] = vol; pp[2] = v; pp[3] = v * x4; pp[4] = v * y4; pp[5] = v * z4;
+  pp[6] = v * (x1 * x1 + x2 * x2 + x3 * x3 + x4 * x4);
+  pp[7] = v * (y1 * y1 + y2 * y2 + y3 * y3 + y4 * y4);
+  pp[8] = v * (z1 * z1 + z2 * z2 + z3 * z3 + z4 * z4);
+  pp[9] = v * (y1 * x1 + y2 * x2 + y3 * x3 + y4 * x4);
+  pp[10] = v * (z1 * x1 + z2 * x2 + z3 * x3 + z4 * x4);
+}
+
+__global__ void vert_geom_kernel(int nv, const int* __restrict__ adj_off, const int* __restrict__ adj_face,
+                                 const int* __restrict__ ghostv, const double* __restrict__ sur,
+                                 const double* __restrict__ nor, double* __restrict__ avert,
+                                 double* __restrict__ vnor) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  double av = 0, a0 = 0, a1 = 0, a2 = 0;
+  for (int q = adj_off[v]; q < adj_off[v + 1]; ++q) {
+    int f = adj_face[q];
+    double s = sur[f];
+    av = av + s / 3.0;
+    a0 = a0 + s * nor[3 * f]; a1 = a1 + s * nor[3 * f + 1]; a2 = a2 + s * nor[3 * f + 2];
+  }
+  avert[v] = av;
+  if (ghostv[v]) { vnor[3 * v] = a0; vnor[3 * v + 1] = a1; vnor[3 * v + 2] = a2; return; }
+  double m = sqrt(a0 * a0 + a1 * a1 + a2 * a2);
+  vnor[3 * v] = a0 / m; vnor[3 * v + 1] = a1 / m; vnor[3 * v + 2] = a2 / m;
+}
+
+// fixed-order reduction of the 11 per-face sums by one block; writes
+// [Surface, Volume, pos_CM(3), ...] into out
+__global__ void geom_reduce_kernel(int nf, const double* __restrict__ part, double* __restrict__ out) {
+  __shared__ double sm[11][256];
+  double s[11];
+  for (int q = 0; q < 11; ++q) s[q] = 0.0;
+  for (int t = threadIdx.x; t < nf; t += blockDim.x)
+    for (int q = 0; q < 11; ++q) s[q] += part[11 * (size_t)t + q];
+  for (int q = 0; q < 11; ++q) sm[q][threadIdx.x] = s[q];
+  __syncthreads();
+  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off)
+      for (int q = 0; q < 11; ++q) sm[q][threadIdx.x] += sm[q][threadIdx.x + off];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double Surface = sm[0][0], Volume1 = sm[1][0] / 6.0;
+    double Vol = sm[2][0], Cx = sm[3][0], Cy = sm[4][0], Cz = sm[5][0];
+    double r = 1.0 / (4.0 * Vol);
+    Cx = Cx * r; Cy = Cy * r; Cz = Cz * r;
+    Vol = Vol / 6.0;
+    out[0] = Surface; out[1] = Volume1; out[2] = Vol;
+    out[3] = Cx; out[4] = Cy; out[5] = Cz;
+  }
+}
+
+__global__ void cfac_kernel(int nf, const double* __restrict__ sur, double h, double celvol, double* __restrict__ cfac) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nf) cfac[t] = (sur[t] * h) / celvol;
+}
+
+// ---------------------------------------------------------------------
+// narrow-band tagging (genSDF.f90:120-192)
+// ---------------------------------------------------------------------
+__device__ double point_tri_dist(const double P[3], const double V0[3], const double V1[3], const double V2[3]) {
+  double E0[3], E1[3], DE[3];
+  for (int d = 0; d < 3; ++d) { E0[d] = V1[d] - V0[d]; E1[d] = V2[d] - V0[d]; DE[d] = V0[d] - P[d]; }
+  double a = E0[0] * E0[0] + E0[1] * E0[1] + E0[2] * E0[2];
+  double b = E0[0] * E1[0] + E0[1] * E1[1] + E0[2] * E1[2];
+  double cc = E1[0] * E1[0] + E1[1] * E1[1] + E1[2] * E1[2];
+  double d = E0[0] * DE[0] + E0[1] * DE[1] + E0[2] * DE[2];
+  double e = E1[0] * DE[0] + E1[1] * DE[1] + E1[2] * DE[2];
+  double det = a * cc - b * b, s = b * e - cc * d, t = b * d - a * e;
+  if (s + t <= det) {
+    if (s < 0.0) {
+      if (t < 0.0) {
+        if (d < 0.0) { t = 0.0; s = (-d >= a) ? 1.0 : -d / a; }
+        else { s = 0.0; if (e >= 0.0) t = 0.0; else if (-e >= cc) t = 1.0; else t = -e / cc; }
+      } else {
+        s = 0.0; if (e >= 0.0) t = 0.0; else if (-e >= cc) t = 1.0; else t = -e / cc;
+      }
+    } else if (t < 0.0) {
+      t = 0.0; if (d >= 0.0) s = 0.0; else if (-d >= a) s = 1.0; else s = -d / a;
+    } else {
+      double invDet = 1.0 / det; s = s * invDet; t = t * invDet;
+    }
+  } else {
+    if (s < 0.0) {
+      double tmp0 = b + d, tmp1 = cc + e;
+      if (tmp1 > tmp0) {
+        double numer = tmp1 - tmp0, denom = a - 2.0 * b + cc;
+        if (numer >= denom) { s = 1.0; t = 0.0; } else { s = numer / denom; t = 1.0 - s; }
+      } else {
+        s = 0.0; if (tmp1 <= 0.0) t = 1.0; else if (e >= 0.0) t = 0.0; else t = -e / cc;
+      }
+    } else if (t < 0.0) {
+      double tmp0 = b + e, tmp1 = a + d;
+      if (tmp1 > tmp0) {
+        double numer = tmp1 - tmp0, denom = a - 2.0 * b + cc;
+        if (numer >= denom) { t = 1.0; s = 0.0; } else { t = numer / denom; s = 1.0 - t; }
+      } else {
+        t = 0.0; if (tmp1 <= 0.0) s = 1.0; else if (d >= 0.0) s = 0.0; else s = -d / a;
+      }
+    } else {
+      double numer = cc + e - b - d, denom = a - 2.0 * b + cc;
+      if (numer <= 0.0) s = 0.0; else if (numer >= denom) s = 1.0; else s = numer / denom;
+      t = 1.0 - s;
+    }
+  }
+  double D0 = (V0[0] + s * E0[0] + t * E1[0]) - P[0];
+  double D1 = (V0[1] + s * E0[1] + t * E1[1]) - P[1];
+  double D2 = (V0[2] + s * E0[2] + t * E1[2]) - P[2];
+  return sqrt(D0 * D0 + D1 * D1 + D2 * D2);
+}
+
+struct TagArgs {
+  LagArgs L;
+  const double* x; const int* vof; const int* ghost; const double* bar; const double* nor;
+};
+
+__device__ __forceinline__ void tri_verts(const TagArgs& T, int f, double V0[3], double V1[3], double V2[3]) {
+  int a = T.vof[3 * f] - 1, b = T.vof[3 * f + 1] - 1, c = T.vof[3 * f + 2] - 1;
+  for (int d = 0; d < 3; ++d) { V0[d] = T.x[3 * a + d]; V1[d] = T.x[3 * b + d]; V2[d] = T.x[3 * c + d]; }
+}
+
+__global__ void sdf_reset_kernel(Grid g, unsigned long long* __restrict__ sdf_bits, int* __restrict__ winner) {
+  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.cells) return;
+  sdf_bits[t] = (unsigned long long)__double_as_longlong(999.0);   // genSDF.f90:138
+  winner[t] = INT_MAX;
+}
+
+// one thread per (triangle, band cell); pass 0: min distance, pass 1: the
+// earliest triangle at that distance, pass 2: the winner writes sdf and VOF
+__global__ void band_kernel(TagArgs T, int pass, unsigned long long* __restrict__ sdf_bits, int* __restrict__ winner,
+                            double* __restrict__ vofp) {
+  long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  int f = (int)(gid / 125), q = (int)(gid % 125);
+  const LagArgs& A = T.L;
+  if (f >= A.nf || T.ghost[f]) return;
+  const Grid& g = A.g;
+  double pos[3] = {T.bar[3 * f], T.bar[3 * f + 1], T.bar[3 * f + 2]};
+  int i = ffloor(pos[0] * g.dx1) + 1, j = ffloor(pos[1] * g.dx2) + 1, k = ffloor(pos[2] * g.dx3) + 1;
+  int ii = i - 2 + q % 5, jj = j - 2 + (q / 5) % 5, kk = k - 2 + q / 25;
+  double P[3] = {coord(A, 0, 1, ii), coord(A, 1, 1, jj), coord(A, 2, 1, kk)};
+  double V0[3], V1[3], V2[3];
+  tri_verts(T, f, V0, V1, V2);
+  double dist = point_tri_dist(P, V0, V1, V2);
+  int im = fmod_pos(ii - 1, g.n1m), jm = fmod_pos(jj - 1, g.n1m), km = fmod_pos(kk - 1, g.n3m);
+  size_t c0 = cidx(g, im, jm, km);
+  unsigned long long bits = (unsigned long long)__double_as_longlong(dist);
+  if (pass == 0) {
+    atomicMin(&sdf_bits[c0], bits);
+  } else if (pass == 1) {
+    if (sdf_bits[c0] == bits && dist < 999.0) atomicMin(&winner[c0], f);
+  } else {
+    if (winner[c0] != f || sdf_bits[c0] != bits) return;
+    double Q0 = pos[0] - P[0], Q1 = pos[1] - P[1], Q2 = pos[2] - P[2];
+    double dotval = T.nor[3 * f] * Q0 + T.nor[3 * f + 1] * Q1 + T.nor[3 * f + 2] * Q2;
+    double sgnd = dist * (-copysign(1.0, dotval));
+    double eps = 1.0 / g.dx1, vof;
+    const double pi = 3.141592653589793238462643;
+    if (sgnd <= -eps) vof = 0.0;
+    else if (sgnd >= eps) vof = 1.0;
+    else vof = 0.5 * (1.0 + sgnd * g.dx1 + (1.0 / pi) * sin(pi * sgnd * g.dx1));
+    vofp[c0] = vof;
+    sdf_bits[c0] = (unsigned long long)__double_as_longlong(sgnd);
+  }
+}
+
+__global__ void sdf_finish_kernel(Grid g, const unsigned long long* __restrict__ bits, double* __restrict__ sdf) {
+  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.cells) return;
+  sdf[t] = __longlong_as_double((long long)bits[t]);
+}
+
+// initial full tagging: one thread per cell of the bounding box
+__device__ bool ray_tri(const double C[3], const double Q[3], const double V0[3], const double V1[3],
+                        const double V2[3], double ip[3]) {
+  const double EPS = 1e-12;
+  double dir[3] = {Q[0] - C[0], Q[1] - C[1], Q[2] - C[2]};
+  double e1[3], e2[3], h[3], s[3], q[3];
+  for (int d = 0; d < 3; ++d) { e1[d] = V1[d] - V0[d]; e2[d] = V2[d] - V0[d]; }
+  h[0] = dir[1] * e2[2] - dir[2] * e2[1]; h[1] = dir[2] * e2[0] - dir[0] * e2[2]; h[2] = dir[0] * e2[1] - dir[1] * e2[0];
+  double a = e1[0] * h[0] + e1[1] * h[1] + e1[2] * h[2];
+  if (fabs(a) < EPS) return false;
+  double f = 1.0 / a;
+  for (int d = 0; d < 3; ++d) s[d] = C[d] - V0[d];
+  double u = f * (s[0] * h[0] + s[1] * h[1] + s[2] * h[2]);
+  if (u < 0.0 || u > 1.0) return false;
+  q[0] = s[1] * e1[2] - s[2] * e1[1]; q[1] = s[2] * e1[0] - s[0] * e1[2]; q[2] = s[0] * e1[1] - s[1] * e1[0];
+  double v = f * (dir[0] * q[0] + dir[1] * q[1] + dir[2] * q[2]);
+  if (v < 0.0 || u + v > 1.0) return false;
+  double t = f * (e2[0] * q[0] + e2[1] * q[1] + e2[2] * q[2]);
+  if (t < 0.0 || t > 1.0) return false;
+  for (int d = 0; d < 3; ++d) ip[d] = C[d] + t * dir[d];
+  return true;
+}
+
+// pass A: ray parity / interface rule per bounding-box cell (rayTagQ_pencil,
+// pencil_rayTag.f90:381-460) -> tmp[gid]
+__global__ void initial_tag_kernel(TagArgs T, int bx0, int by0, int bz0, int nbx, int nby, int nbz,
+                                   double* __restrict__ tmp) {
+  long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= (long long)nbx * nby * nbz) return;
+  const LagArgs& A = T.L;
+  const Grid& g = A.g;
+  int i = bx0 + (int)(gid % nbx), j = by0 + (int)((gid / nbx) % nby), kk = bz0 + (int)(gid / ((long long)nbx * nby));
+  double Q[3] = {coord(A, 0, 1, i), coord(A, 1, 1, j), coord(A, 2, 1, kk)};
+  double C[3] = {-g.xlen * 10.0, Q[1], Q[2]};
+  double ymin = Q[1] - 0.5 / g.dx2, ymax = Q[1] + 0.5 / g.dx2, zmin = Q[2] - 0.5 / g.dx3, zmax = Q[2] + 0.5 / g.dx3;
+  double xmin = Q[0] - 0.5 / g.dx1, xmax = Q[0] + 0.5 / g.dx1;
+  int count = 0;
+  double vof = -1.0;
+  for (int f = 0; f < A.nf; ++f) {
+    if (T.ghost[f]) continue;
+    double V0[3], V1[3], V2[3];
+    tri_verts(T, f, V0, V1, V2);
+    double ylo = fmin(V0[1], fmin(V1[1], V2[1])), yhi = fmax(V0[1], fmax(V1[1], V2[1]));
+    double zlo = fmin(V0[2], fmin(V1[2], V2[2])), zhi = fmax(V0[2], fmax(V1[2], V2[2]));
+    if (yhi < ymin || ylo > ymax || zhi < zmin || zlo > zmax) continue;
+    double xlo = fmin(V0[0], fmin(V1[0], V2[0])), xhi = fmax(V0[0], fmax(V1[0], V2[0]));
+    if (!(xhi < xmin || xlo > xmax)) { vof = 0.5; break; }
+    double ip[3];
+    if (ray_tri(C, Q, V0, V1, V2, ip)) {
+      if (ip[0] >= xmin && ip[0] <= xmax && ip[1] >= ymin && ip[1] <= ymax && ip[2] >= zmin && ip[2] <= zmax) {
+        vof = 0.5;
+        break;
+      }
+      ++count;
+    }
+  }
+  if (vof < 0) vof = (count % 2 == 0) ? 1.0 : 0.0;
+  tmp[gid] = vof;
+}
+
+// reference loop order (i outermost, kk innermost) as an integer key
+__device__ __forceinline__ int box_order(long long gid, int nbx, int nby, int nbz) {
+  int io = (int)(gid % nbx), jo = (int)((gid / nbx) % nby), ko = (int)(gid / ((long long)nbx * nby));
+  return (io * nby + jo) * nbz + ko;
+}
+
+// pass B/C: a cell reached through several periodic images keeps the first
+// value below 1 in loop order (pencil_rayTag.f90:298-302)
+__global__ void initial_claim_kernel(Grid g, int bx0, int by0, int bz0, int nbx, int nby, int nbz,
+                                     const double* __restrict__ tmp, int* __restrict__ claim, double* __restrict__ vofp,
+                                     int pass) {
+  long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= (long long)nbx * nby * nbz) return;
+  double v = tmp[gid];
+  if (!(v < 1.0)) return;
+  int i = bx0 + (int)(gid % nbx), j = by0 + (int)((gid / nbx) % nby), kk = bz0 + (int)(gid / ((long long)nbx * nby));
+  size_t c0 = cidx(g, fmod_pos(i - 1, g.n1m), fmod_pos(j - 1, g.n2m), fmod_pos(kk - 1, g.n3m));
+  int key = box_order(gid, nbx, nby, nbz);
+  if (pass == 0) atomicMin(&claim[c0], key);
+  else if (claim[c0] == key) vofp[c0] = v;
+}
+
+__global__ void fill_kernel(Grid g, double* __restrict__ a, double v) {
+  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < g.cells) a[t] = v;
+}
+
+// ---------------------------------------------------------------------
+// adjacency (vertex -> faces, ascending) built on the host per topology
+// ---------------------------------------------------------------------
+struct LagState {
+  Ctx* c = nullptr;
+  int* adj_off = nullptr;
+  int* adj_face = nullptr;
+  int adj_nf = -1, adj_nv = -1;
+  double* face_part = nullptr;
+  double* geom_out = nullptr;   // device [Surface, Volume1, Vol, Cx, Cy, Cz]
+  double* mean3 = nullptr;
+  unsigned long long* sdf_bits = nullptr;
+  int* winner = nullptr;
+};
+static std::vector<LagState*> g_lag;
+
+static LagState* lag_of(Ctx* c) {
+  for (auto* s : g_lag)
+    if (s->c == c) return s;
+  LagState* s = new LagState();
+  s->c = c;
+  g_lag.push_back(s);
+  return s;
+}
+
+static bool ensure_adjacency(Ctx* c) {
+  LagState* s = lag_of(c);
+  if (s->adj_off && s->adj_nf == c->maxnf && s->adj_nv == c->maxnv) return true;
+  std::vector<int> vof(3 * (size_t)c->maxnf), ghost(c->maxnf);
+  cudaMemcpy(vof.data(), c->dm[MIBM_M_VERT_OF_FACE], vof.size() * 4, cudaMemcpyDeviceToHost);
+  cudaMemcpy(ghost.data(), c->dm[MIBM_M_GHOST_FACE], ghost.size() * 4, cudaMemcpyDeviceToHost);
+  std::vector<int> cnt(c->maxnv + 1, 0);
+  for (int f = 0; f < c->maxnf; ++f) {
+    if (ghost[f]) continue;
+    for (int q = 0; q < 3; ++q) {
+      int v = vof[3 * f + q] - 1;
+      if (v < 0 || v >= c->maxnv) { fail(c, MIBM_EINVAL, "vert_of_face out of range"); return false; }
+      cnt[v + 1]++;
+    }
+  }
+  for (int v = 0; v < c->maxnv; ++v) cnt[v + 1] += cnt[v];
+  std::vector<int> face(cnt[c->maxnv]), fill(cnt.begin(), cnt.end() - 1);
+  for (int f = 0; f < c->maxnf; ++f) {      // ascending face order per vertex
+    if (ghost[f]) continue;
+    for (int q = 0; q < 3; ++q) face[fill[vof[3 * f + q] - 1]++] = f;
+  }
+  cudaFree(s->adj_off); cudaFree(s->adj_face);
+  if (!cuda_ok(c, cudaMalloc(&s->adj_off, cnt.size() * 4), "adj")) return false;
+  if (!cuda_ok(c, cudaMalloc(&s->adj_face, std::max<size_t>(1, face.size()) * 4), "adj")) return false;
+  cudaMemcpy(s->adj_off, cnt.data(), cnt.size() * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(s->adj_face, face.data(), face.size() * 4, cudaMemcpyHostToDevice);
+  s->adj_nf = c->maxnf; s->adj_nv = c->maxnv;
+  return true;
+}
+
+static bool ensure_lag_buffers(Ctx* c) {
+  LagState* s = lag_of(c);
+  if (!s->face_part) {
+    if (!cuda_ok(c, cudaMalloc(&s->face_part, sizeof(double) * 11 * std::max(1, c->maxnf)), "lag")) return false;
+    if (!cuda_ok(c, cudaMalloc(&s->geom_out, sizeof(double) * 8), "lag")) return false;
+    if (!cuda_ok(c, cudaMalloc(&s->mean3, sizeof(double) * 4), "lag")) return false;
+  }
+  if (!c->tri_coef)
+    if (!cuda_ok(c, cudaMalloc(&c->tri_coef, sizeof(double) * 4 * std::max(1, c->maxnf)), "lag")) return false;
+  return true;
+}
+
+static bool check_flag(Ctx* c, const char* what) {
+  cudaMemcpyAsync(c->hflag, c->dflag, 4, cudaMemcpyDeviceToHost, c->stream);
+  if (!cuda_ok(c, cudaStreamSynchronize(c->stream), what)) return false;
+  if (c->hflag[0]) {
+    fail(c, MIBM_ENUMERIC, std::string(what) + ": singular MLS moment matrix (dgetrf info /= 0)");
+    cudaMemsetAsync(c->dflag, 0, 4, c->stream);
+    return false;
+  }
+  return true;
+}
+
+// Host check of the connectivity every Lagrangian kernel dereferences
+// (vertex indices in 1..maxnv); also builds the vertex->face lists.
+bool validate_mesh(Ctx* c) {
+  LagState* s = lag_of(c);
+  s->adj_nf = -1;   // force a rebuild from the current device copy
+  return ensure_adjacency(c);
+}
+
+// ---------------------------------------------------------------------
+// entry points
+// ---------------------------------------------------------------------
+void lagr_find_centroid_indices(Ctx* c) {
+  if (c->maxnf == 0) return;
+  centroid_idx_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(
+      lag_args(c), M<double>(c, MIBM_M_TRI_BAR), M<int>(c, MIBM_M_GHOST_FACE), M<int>(c, MIBM_M_PIND));
+  ++c->launches;
+  for (int q = 0; q < 4; ++q) c->plan[q].valid = false;
+  MIBM_LAUNCH_CHECK(c, "findCentroidIndices");
+}
+
+void lagr_mls_weight(Ctx* c) {
+  if (c->maxnf == 0) return;
+  mls_weight_kernel<<<div_up(4 * (size_t)c->maxnf, 128), 128, 0, c->stream>>>(
+      lag_args(c), M<double>(c, MIBM_M_TRI_BAR), M<int>(c, MIBM_M_GHOST_FACE), M<int>(c, MIBM_M_PIND),
+      M<double>(c, MIBM_M_PTXAB_Q1), M<double>(c, MIBM_M_PTXAB_Q2), M<double>(c, MIBM_M_PTXAB_Q3),
+      M<double>(c, MIBM_M_PTXAB_TEMP), c->dflag);
+  ++c->launches;
+  if (MIBM_LAUNCH_CHECK(c, "mlsWeight")) check_flag(c, "mlsWeight");
+}
+
+void lagr_mls_force(Ctx* c, const StepParams* dp, bool) {
+  if (c->maxnf == 0) return;
+  if (!ensure_lag_buffers(c)) return;
+  ForceArgs F;
+  F.q[0] = c->df[MIBM_F_VX]; F.q[1] = c->df[MIBM_F_VY]; F.q[2] = c->df[MIBM_F_VZ]; F.q[3] = c->df[MIBM_F_TEMP];
+  F.ptx[0] = M<double>(c, MIBM_M_PTXAB_Q1); F.ptx[1] = M<double>(c, MIBM_M_PTXAB_Q2);
+  F.ptx[2] = M<double>(c, MIBM_M_PTXAB_Q3); F.ptx[3] = M<double>(c, MIBM_M_PTXAB_TEMP);
+  F.vel_tri = M<double>(c, MIBM_M_VEL_TRI); F.cfac = M<double>(c, MIBM_M_CFAC);
+  F.pind = M<int>(c, MIBM_M_PIND); F.ghost = M<int>(c, MIBM_M_GHOST_FACE);
+  (void)dp;
+  force_coef_kernel<<<div_up(4 * (size_t)c->maxnf, 128), 128, 0, c->stream>>>(c->g, c->maxnf, F, c->S(MIBM_S_TMELT),
+                                                                                c->tri_coef);
+  ++c->launches;
+  static const int outf[4] = {MIBM_F_FORXC, MIBM_F_FORYC, MIBM_F_FORZC, MIBM_F_FORTEMP};
+  for (int comp = 0; comp < 4; ++comp) {
+    if (!c->plan[comp].valid) build_plan(c, comp);
+    Ctx::Plan& p = c->plan[comp];
+    if (p.n == 0) continue;
+    scatter_apply_kernel<<<div_up(p.n, 256), 256, 0, c->stream>>>(p.n, p.key, p.src,
+                                                                   c->tri_coef + (size_t)comp * c->maxnf,
+                                                                   F.ptx[comp], c->df[outf[comp]]);
+    ++c->launches;
+  }
+  MIBM_LAUNCH_CHECK(c, "mlsForce");
+}
+
+void lagr_velforce(Ctx* c) {
+  if (!ensure_lag_buffers(c)) return;
+  LagState* s = lag_of(c);
+  dim3 grid(c->g.n2m, c->g.n3m);
+  field_sum_kernel<<<grid, 128, 0, c->stream>>>(c->g, c->df[MIBM_F_FORXC], c->df[MIBM_F_FORYC], c->df[MIBM_F_FORZC],
+                                                c->red + kRedPart);
+  double ncell = (double)c->g.n1m * (double)c->g.n2m * (double)c->g.n3m;
+  mean3_kernel<<<1, 1024, 0, c->stream>>>(c->red + kRedPart, c->g.n2m * c->g.n3m, ncell, s->mean3);
+  c->launches += 2;
+  k_velforce_apply(c, s->mean3);
+}
+
+void lagr_tempforce(Ctx* c) { k_tempforce_apply(c); }
+
+void lagr_find_probe_indices(Ctx* c) {
+  if (c->maxnf == 0) return;
+  probe_idx_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(
+      lag_args(c), M<double>(c, MIBM_M_TRI_BAR), M<double>(c, MIBM_M_TRI_NOR), M<int>(c, MIBM_M_GHOST_FACE),
+      c->S(MIBM_S_H_EULERIAN), M<int>(c, MIBM_M_PIND));
+  ++c->launches;
+  for (int q = 0; q < 4; ++q) c->plan[q].valid = false;
+  MIBM_LAUNCH_CHECK(c, "findProbeIndices");
+}
+
+void lagr_heat_flux(Ctx* c) {
+  if (c->maxnf == 0) return;
+  if (!ensure_adjacency(c)) return;
+  LagState* s = lag_of(c);
+  heat_flux_kernel<<<div_up(2 * (size_t)c->maxnf, 64), 64, 0, c->stream>>>(
+      lag_args(c), c->df[MIBM_F_TEMP], M<double>(c, MIBM_M_TRI_BAR), M<double>(c, MIBM_M_TRI_NOR),
+      M<int>(c, MIBM_M_GHOST_FACE), M<int>(c, MIBM_M_PIND), c->S(MIBM_S_H_EULERIAN), c->S(MIBM_S_PEC),
+      M<double>(c, MIBM_M_QW_O), M<double>(c, MIBM_M_QW_I), c->dflag);
+  face_to_vert_kernel<<<div_up(c->maxnv, 128), 128, 0, c->stream>>>(
+      c->maxnv, s->adj_off, s->adj_face, M<double>(c, MIBM_M_SUR), M<double>(c, MIBM_M_AVERT),
+      M<double>(c, MIBM_M_QW_O), M<double>(c, MIBM_M_QW_I), M<double>(c, MIBM_M_QW_OVERT), M<double>(c, MIBM_M_QW_IVERT));
+  c->launches += 2;
+  if (MIBM_LAUNCH_CHECK(c, "mls_heatFlux")) check_flag(c, "mls_heatFlux");
+}
+
+void lagr_stefan(Ctx* c, const StepParams* dp) {
+  if (c->maxnv == 0) return;
+  stefan_kernel<<<div_up(c->maxnv, 128), 128, 0, c->stream>>>(
+      c->maxnv, M<int>(c, MIBM_M_GHOST_VERT), M<double>(c, MIBM_M_VERT_NOR), M<double>(c, MIBM_M_QW_OVERT),
+      M<double>(c, MIBM_M_QW_IVERT), c->S(MIBM_S_CPLIQUID) / c->S(MIBM_S_LATHEAT), dp, M<double>(c, MIBM_M_VMELT),
+      M<double>(c, MIBM_M_VMELT_M1), M<double>(c, MIBM_M_XYZV));
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "stefan");
+}
+
+// Refresh areas, normals, centroids, vertex areas/normals, volume and centre
+// of mass; the scalars land in the registered host Surface/Volume/pos_CM.
+void lagr_geometry_refresh(Ctx* c, bool imelt) {
+  if (c->maxnf == 0) return;
+  if (!ensure_adjacency(c) || !ensure_lag_buffers(c)) return;
+  LagState* s = lag_of(c);
+  face_geom_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(
+      c->maxnf, M<int>(c, MIBM_M_VERT_OF_FACE), M<int>(c, MIBM_M_GHOST_FACE), M<double>(c, MIBM_M_XYZV),
+      M<double>(c, MIBM_M_SUR), M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_TRI_BAR), s->face_part);
+  vert_geom_kernel<<<div_up(c->maxnv, 128), 128, 0, c->stream>>>(
+      c->maxnv, s->adj_off, s->adj_face, M<int>(c, MIBM_M_GHOST_VERT), M<double>(c, MIBM_M_SUR),
+      M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_AVERT), M<double>(c, MIBM_M_VERT_NOR));
+  geom_reduce_kernel<<<1, 256, 0, c->stream>>>(c->maxnf, s->face_part, s->geom_out);
+  c->launches += 3;
+  if (imelt) {
+    cfac_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(c->maxnf, M<double>(c, MIBM_M_SUR),
+                                                              c->S(MIBM_S_H_EULERIAN), c->S(MIBM_S_CELVOL),
+                                                              M<double>(c, MIBM_M_CFAC));
+    ++c->launches;
+  }
+  cudaMemcpyAsync(c->red_host, s->geom_out, sizeof(double) * 6, cudaMemcpyDeviceToHost, c->stream);
+  if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "geometry")) return;
+  *c->hs[MIBM_S_SURFACE] = c->red_host[0];
+  *c->hs[MIBM_S_VOLUME] = c->red_host[2];        // calc_rigidBody_params writes Volume last
+  c->hs[MIBM_S_POS_CM][0] = c->red_host[3];
+  c->hs[MIBM_S_POS_CM][1] = c->red_host[4];
+  c->hs[MIBM_S_POS_CM][2] = c->red_host[5];
+}
+
+void lagr_tag_narrow_band(Ctx* c) {
+  if (c->maxnf == 0) return;
+  LagState* s = lag_of(c);
+  if (!s->sdf_bits) {
+    if (!cuda_ok(c, cudaMalloc(&s->sdf_bits, sizeof(unsigned long long) * c->g.cells), "band")) return;
+    if (!cuda_ok(c, cudaMalloc(&s->winner, sizeof(int) * c->g.cells), "band")) return;
+  }
+  TagArgs T;
+  T.L = lag_args(c);
+  T.x = M<double>(c, MIBM_M_XYZV); T.vof = M<int>(c, MIBM_M_VERT_OF_FACE); T.ghost = M<int>(c, MIBM_M_GHOST_FACE);
+  T.bar = M<double>(c, MIBM_M_TRI_BAR); T.nor = M<double>(c, MIBM_M_TRI_NOR);
+  sdf_reset_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, s->sdf_bits, s->winner);
+  size_t nthr = (size_t)c->maxnf * 125;
+  for (int pass = 0; pass < 3; ++pass)
+    band_kernel<<<div_up(nthr, 128), 128, 0, c->stream>>>(T, pass, s->sdf_bits, s->winner, c->df[MIBM_F_VOFP]);
+  sdf_finish_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, s->sdf_bits, c->df[MIBM_F_SDF]);
+  c->launches += 5;
+  k_interp_vof(c);
+  MIBM_LAUNCH_CHECK(c, "narrowBandTagging");
+}
+
+void lagr_tag_initial(Ctx* c) {
+  if (c->maxnf == 0) return;
+  // bounding box (tagCells.f90:32-66, dx1 on all axes as in the reference)
+  std::vector<double> x(3 * (size_t)c->maxnv);
+  std::vector<int> gv(c->maxnv);
+  cudaMemcpy(x.data(), c->dm[MIBM_M_XYZV], x.size() * 8, cudaMemcpyDeviceToHost);
+  cudaMemcpy(gv.data(), c->dm[MIBM_M_GHOST_VERT], gv.size() * 4, cudaMemcpyDeviceToHost);
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (int v = 0; v < c->maxnv; ++v) {
+    if (gv[v]) continue;
+    for (int d = 0; d < 3; ++d) { lo[d] = std::min(lo[d], x[3 * v + d]); hi[d] = std::max(hi[d], x[3 * v + d]); }
+  }
+  int b0[3], nb[3];
+  for (int d = 0; d < 3; ++d) {
+    b0[d] = (int)std::floor(lo[d] * c->g.dx1) + 1 - 2;
+    int b1 = (int)std::floor(hi[d] * c->g.dx1) + 1 + 2;
+    nb[d] = b1 - b0[d] + 1;
+  }
+  int vids[4] = {MIBM_F_VOFP, MIBM_F_VOFX, MIBM_F_VOFY, MIBM_F_VOFZ};
+  for (int q = 0; q < 4; ++q) {
+    fill_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, c->df[vids[q]], 1.0);
+    ++c->launches;
+  }
+  TagArgs T;
+  T.L = lag_args(c);
+  T.x = M<double>(c, MIBM_M_XYZV); T.vof = M<int>(c, MIBM_M_VERT_OF_FACE); T.ghost = M<int>(c, MIBM_M_GHOST_FACE);
+  T.bar = M<double>(c, MIBM_M_TRI_BAR); T.nor = M<double>(c, MIBM_M_TRI_NOR);
+  size_t ncell = (size_t)nb[0] * nb[1] * nb[2];
+  LagState* s = lag_of(c);
+  if (!s->sdf_bits) {
+    if (!cuda_ok(c, cudaMalloc(&s->sdf_bits, sizeof(unsigned long long) * c->g.cells), "band")) return;
+    if (!cuda_ok(c, cudaMalloc(&s->winner, sizeof(int) * c->g.cells), "band")) return;
+  }
+  double* tmp = nullptr;
+  if (!cuda_ok(c, cudaMalloc(&tmp, sizeof(double) * std::max<size_t>(1, ncell)), "initial tag")) return;
+  sdf_reset_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, s->sdf_bits, s->winner);
+  initial_tag_kernel<<<div_up(ncell, 128), 128, 0, c->stream>>>(T, b0[0], b0[1], b0[2], nb[0], nb[1], nb[2], tmp);
+  for (int pass = 0; pass < 2; ++pass)
+    initial_claim_kernel<<<div_up(ncell, 256), 256, 0, c->stream>>>(c->g, b0[0], b0[1], b0[2], nb[0], nb[1], nb[2], tmp,
+                                                                    s->winner, c->df[MIBM_F_VOFP], pass);
+  c->launches += 4;
+  bool ok = MIBM_LAUNCH_CHECK(c, "initial tag");
+  cudaStreamSynchronize(c->stream);
+  cudaFree(tmp);
+  if (!ok) return;
+  lagr_tag_narrow_band(c);
+}
+
+// particle.f90:38-193 without remeshing / Newton-Euler (flags off)
+void lagr_particle(Ctx* c, const StepParams* dp) {
+  if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0) return;
+  lagr_find_centroid_indices(c);
+  lagr_mls_weight(c);
+  if (c->status != MIBM_OK) return;
+  static const int fo[4] = {MIBM_F_FORXC, MIBM_F_FORYC, MIBM_F_FORZC, MIBM_F_FORTEMP};
+  for (int q = 0; q < 4; ++q) cudaMemsetAsync(c->df[fo[q]], 0, c->g.cells * sizeof(double), c->stream);
+  lagr_mls_force(c, dp, true);
+  bool imelt = c->I(MIBM_I_IMELT) == 1;
+  if (imelt) {
+    lagr_find_probe_indices(c);
+    lagr_heat_flux(c);
+    if (c->status != MIBM_OK) return;
+  }
+  lagr_velforce(c);
+  lagr_tempforce(c);
+  if (imelt) lagr_stefan(c, dp);
+  lagr_geometry_refresh(c, imelt);
+  if (c->S(MIBM_S_VOLUME) < c->S(MIBM_S_V_THRESH)) fail(c, MIBM_EABORT, "Geometry V/VE smaller than threshold");
+}
+
+void lagr_free(Ctx* c) {
+  for (int q = 0; q < 4; ++q) {
+    Ctx::Plan& p = c->plan[q];
+    cudaFree(p.key); cudaFree(p.src); cudaFree(p.tmp_key); cudaFree(p.tmp_src); cudaFree(p.hist);
+  }
+  for (size_t q = 0; q < g_lag.size(); ++q)
+    if (g_lag[q]->c == c) {
+      LagState* s = g_lag[q];
+      cudaFree(s->adj_off); cudaFree(s->adj_face); cudaFree(s->face_part); cudaFree(s->geom_out);
+      cudaFree(s->mean3); cudaFree(s->sdf_bits); cudaFree(s->winner);
+      delete s;
+      g_lag.erase(g_lag.begin() + q);
+      break;
+    }
+}
+
+}  // namespace mibm

@@ -1,0 +1,482 @@
+// stencil.cu -- staggered second-order stencils of the RK3 substep.
+//
+// Kernels restate, per cell:
+//   hdnl1.f90:15-77, hdnl2.f90:16-78, hdnl3.f90:16-88, hdnlte.f90:45-158
+//   invtr1.f90:25-64, invtr2.f90:22-59, invtr3.f90:20-58, invtrte.f90:17-59
+//   divg.f90:9-23, updvp.f90:16-31, prcalc.f90:17-33, cfl.f90:1-77,
+//   velforce.f90:44-52, tempforce.f90:32-40, interp_vof tagCells.f90:85-111
+// on the compact device layout (common.cuh) with periodic index wraps in
+// place of the Fortran ghost planes.  One thread per cell, x fastest; the
+// grid covers (x/32, y/8, z).  The FP64 form of these kernels is bounded by
+// the FP64 FMA rate of the part, not by HBM, so the code avoids divisions
+// (reciprocals are taken once on the host) and skips terms that are zero by
+// configuration (HIT forcing off).
+#include "common.cuh"
+
+namespace mibm {
+
+struct StencilArgs {
+  Grid g;
+  const double* __restrict__ vx;
+  const double* __restrict__ vy;
+  const double* __restrict__ vz;
+  const double* __restrict__ temp;
+  const double* __restrict__ pr;
+  const double* __restrict__ vofx;
+  const double* __restrict__ vofy;
+  const double* __restrict__ vofz;
+  const double* __restrict__ vofp;
+  const double* __restrict__ forcx;
+  const double* __restrict__ forcy;
+  const double* __restrict__ forcz;
+  const double* __restrict__ xc;   // coordinate tables, offset coord_off
+  const double* __restrict__ xm;
+  const double* __restrict__ yc;
+  const double* __restrict__ ym;
+  const double* __restrict__ zc;
+  const double* __restrict__ zm;
+  int coff;
+  int forcing;
+};
+
+static StencilArgs make_args(Ctx* c) {
+  StencilArgs a;
+  a.g = c->g;
+  a.vx = c->df[MIBM_F_VX]; a.vy = c->df[MIBM_F_VY]; a.vz = c->df[MIBM_F_VZ];
+  a.temp = c->df[MIBM_F_TEMP]; a.pr = c->df[MIBM_F_PR];
+  a.vofx = c->df[MIBM_F_VOFX]; a.vofy = c->df[MIBM_F_VOFY]; a.vofz = c->df[MIBM_F_VOFZ]; a.vofp = c->df[MIBM_F_VOFP];
+  a.forcx = c->df[MIBM_F_FORCX]; a.forcy = c->df[MIBM_F_FORCY]; a.forcz = c->df[MIBM_F_FORCZ];
+  a.xc = c->xc; a.xm = c->xm; a.yc = c->yc; a.ym = c->ym; a.zc = c->zc; a.zm = c->zm;
+  a.coff = c->coord_off;
+  a.forcing = c->I(MIBM_I_FORCING);
+  return a;
+}
+
+#define CELL_INDEX                                                   \
+  const Grid& g = A.g;                                               \
+  int i = blockIdx.x * blockDim.x + threadIdx.x;                     \
+  int j = blockIdx.y * blockDim.y + threadIdx.y;                     \
+  int k = blockIdx.z;                                                \
+  if (i >= g.n1m || j >= g.n2m) return;                              \
+  const int ip = (i + 1 == g.n1m) ? 0 : i + 1;                       \
+  const int im = (i == 0) ? g.n1m - 1 : i - 1;                       \
+  const size_t P = g.P;                                              \
+  const size_t PL = g.plane;                                         \
+  const size_t c0 = cidx(g, i, j, k);                                \
+  const ptrdiff_t dip = (ptrdiff_t)ip - i, dim = (ptrdiff_t)im - i;   \
+  const ptrdiff_t djp = (j + 1 == g.n2m) ? -(ptrdiff_t)(g.n2m - 1) * (ptrdiff_t)P : (ptrdiff_t)P; \
+  const ptrdiff_t djm = (j == 0) ? (ptrdiff_t)(g.n2m - 1) * (ptrdiff_t)P : -(ptrdiff_t)P;         \
+  const ptrdiff_t dkp = (k + 1 == g.n3m) ? -(ptrdiff_t)(g.n3m - 1) * (ptrdiff_t)PL : (ptrdiff_t)PL; \
+  const ptrdiff_t dkm = (k == 0) ? (ptrdiff_t)(g.n3m - 1) * (ptrdiff_t)PL : -(ptrdiff_t)PL;         \
+  (void)dip; (void)dim; (void)djp; (void)djm; (void)dkp; (void)dkm; (void)P;
+
+// ---------------------------------------------------------------------
+// explicit terms
+// ---------------------------------------------------------------------
+__device__ __forceinline__ double h_x(const StencilArgs& A, size_t c0, ptrdiff_t dip, ptrdiff_t dim, ptrdiff_t djp,
+                                      ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm) {
+  const Grid& g = A.g;
+  const double* vx = A.vx; const double* vy = A.vy; const double* vz = A.vz;
+  double udx1 = g.dx1 * 0.25, udx2 = g.dx2 * 0.25, udx3 = g.dx3 * 0.25;
+  double vxc = vx[c0];
+  double a = vx[c0 + dip] + vxc, b = vx[c0 + dim] + vxc;
+  double h11 = (a * a - b * b) * udx1;
+  double h12 = ((vy[c0 + djp] + vy[c0 + dim + djp]) * (vx[c0 + djp] + vxc) -
+                (vy[c0] + vy[c0 + dim]) * (vxc + vx[c0 + djm])) * udx2;
+  double h13 = ((vz[c0 + dkp] + vz[c0 + dim + dkp]) * (vx[c0 + dkp] + vxc) -
+                (vz[c0] + vz[c0 + dim]) * (vxc + vx[c0 + dkm])) * udx3;
+  double h = -(h11 + h12 + h13);
+  if (A.forcing) h = h + A.vofx[c0] * A.forcx[c0] / g.xlen;
+  return h;
+}
+
+__device__ __forceinline__ double h_y(const StencilArgs& A, size_t c0, ptrdiff_t dip, ptrdiff_t dim, ptrdiff_t djp,
+                                      ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm) {
+  const Grid& g = A.g;
+  const double* vx = A.vx; const double* vy = A.vy; const double* vz = A.vz;
+  double udx1 = g.dx1 * 0.25, udx2 = g.dx2 * 0.25, udx3 = g.dx3 * 0.25;
+  double vyc = vy[c0];
+  double h21 = ((vy[c0 + dip] + vyc) * (vx[c0 + dip] + vx[c0 + dip + djm]) -
+                (vyc + vy[c0 + dim]) * (vx[c0] + vx[c0 + djm])) * udx1;
+  double a = vy[c0 + djp] + vyc, b = vy[c0 + djm] + vyc;
+  double h22 = (a * a - b * b) * udx2;
+  double h23 = ((vz[c0 + dkp] + vz[c0 + djm + dkp]) * (vy[c0 + dkp] + vyc) -
+                (vz[c0] + vz[c0 + djm]) * (vyc + vy[c0 + dkm])) * udx3;
+  double h = -(h21 + h22 + h23);
+  if (A.forcing) h = h + A.vofy[c0] * A.forcy[c0] / g.ylen;
+  return h;
+}
+
+__device__ __forceinline__ double h_z(const StencilArgs& A, size_t c0, ptrdiff_t dip, ptrdiff_t dim, ptrdiff_t djp,
+                                      ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm, const StepParams& p) {
+  const Grid& g = A.g;
+  const double* vx = A.vx; const double* vy = A.vy; const double* vz = A.vz;
+  double udx1 = g.dx1 * 0.25, udx2 = g.dx2 * 0.25, udx3 = g.dx3 * 0.25;
+  double vzc = vz[c0];
+  double h31 = ((vx[c0 + dip] + vx[c0 + dip + dkm]) * (vz[c0 + dip] + vzc) -
+                (vx[c0] + vx[c0 + dkm]) * (vzc + vz[c0 + dim])) * udx1;
+  double h32 = ((vy[c0 + djp] + vy[c0 + djp + dkm]) * (vz[c0 + djp] + vzc) -
+                (vy[c0] + vy[c0 + dkm]) * (vzc + vz[c0 + djm])) * udx2;
+  double a = vz[c0 + dkp] + vzc, b = vzc + vz[c0 + dkm];
+  double h33 = (a * a - b * b) * udx3;
+  double h = -(h31 + h32 + h33);
+  if (p.betagz != 0.0) {
+    double T_interp = (A.temp[c0] + A.temp[c0 + dkm]) * 0.5;
+    h = h + p.betagz * (T_interp - p.tliq);
+  }
+  if (A.forcing) h = h + A.vofz[c0] * A.forcz[c0] / g.zlen;
+  return h;
+}
+
+__device__ __forceinline__ double nint_d(double x) { return round(x); }   // Fortran NINT semantics
+
+__device__ __forceinline__ double h_t(const StencilArgs& A, int i, int j, int k, size_t c0, ptrdiff_t dip,
+                                      ptrdiff_t dim, ptrdiff_t djp, ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm,
+                                      const StepParams& p) {
+  const Grid& g = A.g;
+  const double* vx = A.vx; const double* vy = A.vy; const double* vz = A.vz; const double* T = A.temp;
+  double udx1 = g.dx1 * 0.5, udx2 = g.dx2 * 0.5, udx3 = g.dx3 * 0.5;
+  double tc = T[c0], tip = T[c0 + dip], tim = T[c0 + dim], tjp = T[c0 + djp], tjm = T[c0 + djm];
+  double tkp = T[c0 + dkp], tkm = T[c0 + dkm];
+  double h31 = (vx[c0 + dip] * (tip + tc) - vx[c0] * (tc + tim)) * udx1;
+  double h32 = (vy[c0 + djp] * (tjp + tc) - vy[c0] * (tc + tjm)) * udx2;
+  double h33 = (vz[c0 + dkp] * (tkp + tc) - vz[c0] * (tc + tkm)) * udx3;
+  double vp = A.vofp[c0];
+  double ht = -(h31 + h32 + h33) * vp;
+  double sv = 1.0 - vp;
+  if (sv != 0.0) {
+    // solid-body advection, hdnlte.f90:94-153 (Fortran indices i+1, j+1, k+1)
+    int fi = i + 1, fj = j + 1, fk = k + 1;
+    double r0 = A.xc[fi + A.coff] - p.pos[0], r1 = A.ym[fj + A.coff] - p.pos[1], r2 = A.zm[fk + A.coff] - p.pos[2];
+    r0 = r0 - g.xlen * nint_d(r0 / g.xlen); r1 = r1 - g.ylen * nint_d(r1 / g.ylen); r2 = r2 - g.zlen * nint_d(r2 / g.zlen);
+    double u_imh = p.vel[0] + p.om[1] * r2 - p.om[2] * r1;
+    h31 = u_imh * (tip - tim) * udx1;
+    r0 = A.xm[fi + A.coff] - p.pos[0]; r1 = A.yc[fj + A.coff] - p.pos[1]; r2 = A.zm[fk + A.coff] - p.pos[2];
+    r0 = r0 - g.xlen * nint_d(r0 / g.xlen); r1 = r1 - g.ylen * nint_d(r1 / g.ylen); r2 = r2 - g.zlen * nint_d(r2 / g.zlen);
+    double v_jmh = p.vel[1] + p.om[2] * r0 - p.om[0] * r2;
+    h32 = v_jmh * (tjp - tjm) * udx2;
+    r0 = A.xm[fi + A.coff] - p.pos[0]; r1 = A.ym[fj + A.coff] - p.pos[1]; r2 = A.zc[fk + A.coff] - p.pos[2];
+    double w_kmh = p.vel[2] + p.om[0] * r1 - p.om[1] * r0;
+    h33 = w_kmh * (tkp - tkm) * udx3;
+    ht = ht - (h31 + h32 + h33) * sv;
+  }
+  return ht;
+}
+
+__global__ void hdnl_kernel(StencilArgs A, int which, const StepParams* __restrict__ pp, double* __restrict__ out) {
+  CELL_INDEX
+  StepParams p = *pp;
+  double h;
+  if (which == 0) h = h_x(A, c0, dip, dim, djp, djm, dkp, dkm);
+  else if (which == 1) h = h_y(A, c0, dip, dim, djp, djm, dkp, dkm);
+  else if (which == 2) h = h_z(A, c0, dip, dim, djp, djm, dkp, dkm, p);
+  else h = h_t(A, i, j, k, c0, dip, dim, djp, djm, dkp, dkm, p);
+  out[c0] = h;
+}
+
+// ---------------------------------------------------------------------
+// RHS of the factored implicit step
+// ---------------------------------------------------------------------
+__device__ __forceinline__ double lap(const double* q, size_t c0, ptrdiff_t dip, ptrdiff_t dim, ptrdiff_t djp,
+                                      ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm, const Grid& g, bool fortran_order_t) {
+  double qc = q[c0];
+  double d1 = (q[c0 + dip] - 2.0 * qc + q[c0 + dim]) * g.dx1q;
+  double d2 = (q[c0 + djp] - 2.0 * qc + q[c0 + djm]) * g.dx2q;
+  double d3 = (q[c0 + dkp] - 2.0 * qc + q[c0 + dkm]) * g.dx3q;
+  // invtr1/2: d11+d22+d33 ; invtr3/invtrte: d22+d33+d11
+  return fortran_order_t ? (d2 + d3) + d1 : (d1 + d2) + d3;
+}
+
+__device__ __forceinline__ double rhs_value(const StencilArgs& A, int which, double h, double ru, size_t c0,
+                                            ptrdiff_t dip, ptrdiff_t dim, ptrdiff_t djp, ptrdiff_t djm, ptrdiff_t dkp,
+                                            ptrdiff_t dkm, const StepParams& p) {
+  const Grid& g = A.g;
+  if (which == 0) {
+    double dcvx = lap(A.vx, c0, dip, dim, djp, djm, dkp, dkm, g, false);
+    double dpx11 = (A.pr[c0] - A.pr[c0 + dim]) * (g.dx1 * p.al);
+    return (p.ga * h + p.ro * ru + p.alre * dcvx - dpx11) * p.dt;
+  } else if (which == 1) {
+    double dcvy = lap(A.vy, c0, dip, dim, djp, djm, dkp, dkm, g, false);
+    double dpx22 = (A.pr[c0] - A.pr[c0 + djm]) * (g.dx2 * p.al);
+    return (p.ga * h + p.ro * ru + p.alre * dcvy - dpx22) * p.dt;
+  } else if (which == 2) {
+    double dcvz = lap(A.vz, c0, dip, dim, djp, djm, dkp, dkm, g, true);
+    double dpx33 = (A.pr[c0] - A.pr[c0 + dkm]) * (p.al * g.dx3);
+    return (p.ga * h + p.ro * ru + p.alre * dcvz - dpx33) * p.dt;
+  }
+  double dcte = lap(A.temp, c0, dip, dim, djp, djm, dkp, dkm, g, true);
+  return p.dt * (p.ga * h + p.ro * ru) + (p.al / p.pec) * dcte * p.dt;
+}
+
+// invtr drop-in: reads H from the explicit-term array, writes rhs, ru = H
+__global__ void invtr_rhs_kernel(StencilArgs A, int which, const StepParams* __restrict__ pp,
+                                 const double* __restrict__ H, double* __restrict__ ru, double* __restrict__ rhs) {
+  CELL_INDEX
+  StepParams p = *pp;
+  double h = H[c0];
+  rhs[c0] = rhs_value(A, which, h, ru[c0], c0, dip, dim, djp, djm, dkp, dkm, p);
+  ru[c0] = h;
+}
+
+// fused path: explicit term computed in registers (hdnl + invtr RHS)
+__global__ void fused_rhs_kernel(StencilArgs A, int which, const StepParams* __restrict__ pp, double* __restrict__ ru,
+                                 double* __restrict__ rhs) {
+  CELL_INDEX
+  StepParams p = *pp;
+  double h;
+  if (which == 0) h = h_x(A, c0, dip, dim, djp, djm, dkp, dkm);
+  else if (which == 1) h = h_y(A, c0, dip, dim, djp, djm, dkp, dkm);
+  else if (which == 2) h = h_z(A, c0, dip, dim, djp, djm, dkp, dkm, p);
+  else h = h_t(A, i, j, k, c0, dip, dim, djp, djm, dkp, dkm, p);
+  rhs[c0] = rhs_value(A, which, h, ru[c0], c0, dip, dim, djp, djm, dkp, dkm, p);
+  ru[c0] = h;
+}
+
+// ---------------------------------------------------------------------
+// projection stencils
+// ---------------------------------------------------------------------
+__global__ void divg_kernel(StencilArgs A, const StepParams* __restrict__ pp, double* __restrict__ dph) {
+  CELL_INDEX
+  double usdtal = 1.0 / (pp->dt * pp->al);
+  double dq = (A.vx[c0 + dip] - A.vx[c0]) * g.dx1 + (A.vy[c0 + djp] - A.vy[c0]) * g.dx2 +
+              (A.vz[c0 + dkp] - A.vz[c0]) * g.dx3;
+  dph[c0] = dq * usdtal;
+}
+
+__global__ void updvp_kernel(StencilArgs A, const StepParams* __restrict__ pp, const double* __restrict__ dph,
+                             double* __restrict__ vx, double* __restrict__ vy, double* __restrict__ vz) {
+  CELL_INDEX
+  double al = pp->al, dt = pp->dt;
+  double udx1 = al * dt * g.dx1, udx2 = al * dt * g.dx2, udx3 = al * dt * g.dx3;
+  double loc = dph[c0];
+  vx[c0] = vx[c0] - (loc - dph[c0 + dim]) * udx1;
+  vy[c0] = vy[c0] - (loc - dph[c0 + djm]) * udx2;
+  vz[c0] = vz[c0] - (loc - dph[c0 + dkm]) * udx3;
+}
+
+__global__ void prcalc_kernel(StencilArgs A, const StepParams* __restrict__ pp, const double* __restrict__ dph,
+                              double* __restrict__ pr) {
+  CELL_INDEX
+  double be = pp->al * pp->beta;
+  double d = dph[c0];
+  pr[c0] = pr[c0] + d - be * ((dph[c0 + dip] - 2.0 * d + dph[c0 + dim]) * g.dx1q +
+                              (dph[c0 + djp] - 2.0 * d + dph[c0 + djm]) * g.dx2q +
+                              (dph[c0 + dkp] - 2.0 * d + dph[c0 + dkm]) * g.dx3q);
+}
+
+__global__ void add_kernel(Grid g, double* __restrict__ q, const double* __restrict__ r) {
+  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < g.cells) q[t] = q[t] + r[t];
+}
+
+__global__ void interp_vof_kernel(StencilArgs A, double* __restrict__ vofx, double* __restrict__ vofy,
+                                  double* __restrict__ vofz) {
+  CELL_INDEX
+  const double* vp = A.vofp;
+  double c = vp[c0];
+  vofx[c0] = 0.5 * (vp[c0 + dim] + c);
+  vofy[c0] = 0.5 * (vp[c0 + djm] + c);
+  vofz[c0] = 0.5 * (vp[c0 + dkm] + c);
+}
+
+__global__ void velforce_apply_kernel(Grid g, const double* __restrict__ mean3, const double* __restrict__ fx,
+                                      const double* __restrict__ fy, const double* __restrict__ fz,
+                                      double* __restrict__ vx, double* __restrict__ vy, double* __restrict__ vz) {
+  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.cells) return;
+  vx[t] = vx[t] + fx[t] - mean3[0];
+  vy[t] = vy[t] + fy[t] - mean3[1];
+  vz[t] = vz[t] + fz[t] - mean3[2];
+}
+
+__global__ void tempforce_apply_kernel(Grid g, const double* __restrict__ ft, double* __restrict__ T) {
+  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.cells) return;
+  T[t] = T[t] + ft[t];
+}
+
+// ---------------------------------------------------------------------
+// CFL reductions (max is order independent: bitwise deterministic)
+// ---------------------------------------------------------------------
+__device__ __forceinline__ double warp_max(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// cfl.f90:11-26: i+1, j+1, k+1 are not wrapped -- column n1 / row n2 are the
+// stored padding values, plane n3m+1 is the periodic ghost.
+__global__ void cfl_kernel(StencilArgs A, const double* __restrict__ padx, const double* __restrict__ pady,
+                           double* __restrict__ part) {
+  const Grid& g = A.g;
+  int j = blockIdx.y, k = blockIdx.z;
+  double m = 0.0;
+  for (int i = threadIdx.x; i < g.n1m; i += blockDim.x) {
+    size_t c0 = cidx(g, i, j, k);
+    double vxp = (i + 1 < g.n1m) ? A.vx[c0 + 1] : padx[j + (size_t)g.n2m * k];
+    double vyp = (j + 1 < g.n2m) ? A.vy[c0 + g.P] : pady[i + (size_t)g.n1m * k];
+    double vzp = A.vz[cidx(g, i, j, (k + 1 == g.n3m) ? 0 : k + 1)];
+    double qcf = fabs((A.vx[c0] + vxp) * 0.5 * g.dx1) + fabs((A.vy[c0] + vyp) * 0.5 * g.dx2) +
+                 fabs((A.vz[c0] + vzp) * 0.5 * g.dx3);
+    m = fmax(m, qcf);
+  }
+  m = warp_max(m);
+  __shared__ double sm[32];
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = (threadIdx.x < (blockDim.x >> 5)) ? sm[threadIdx.x] : 0.0;
+    v = warp_max(v);
+    if (threadIdx.x == 0) part[j + (size_t)g.n2m * k] = v;
+  }
+}
+
+// get_dt advective term: max(|u| dt dx1 + |v| dt dx2 + |w| dt dx3)
+__global__ void getdt_kernel(StencilArgs A, double dt, double* __restrict__ part) {
+  const Grid& g = A.g;
+  int j = blockIdx.y, k = blockIdx.z;
+  double m = 0.0;
+  for (int i = threadIdx.x; i < g.n1m; i += blockDim.x) {
+    size_t c0 = cidx(g, i, j, k);
+    double v = fabs(A.vx[c0]) * dt * g.dx1 + fabs(A.vy[c0]) * dt * g.dx2 + fabs(A.vz[c0]) * dt * g.dx3;
+    m = fmax(m, v);
+  }
+  m = warp_max(m);
+  __shared__ double sm[32];
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = (threadIdx.x < (blockDim.x >> 5)) ? sm[threadIdx.x] : 0.0;
+    v = warp_max(v);
+    if (threadIdx.x == 0) part[j + (size_t)g.n2m * k] = v;
+  }
+}
+
+__global__ void max_reduce_kernel(const double* __restrict__ part, size_t n, double* __restrict__ out) {
+  double m = 0.0;
+  for (size_t t = threadIdx.x; t < n; t += blockDim.x) m = fmax(m, part[t]);
+  m = warp_max(m);
+  __shared__ double sm[32];
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = (threadIdx.x < (blockDim.x >> 5)) ? sm[threadIdx.x] : 0.0;
+    v = warp_max(v);
+    if (threadIdx.x == 0) out[0] = v;
+  }
+}
+
+// ---------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------
+static dim3 cell_grid(const Grid& g) { return dim3(div_up(g.n1m, 32), div_up(g.n2m, 8), g.n3m); }
+static const dim3 kCellBlock(32, 8);
+
+static double* hdnl_out(Ctx* c, int which) {
+  switch (which) {
+    case 0: return c->df[MIBM_F_DQ];
+    case 1: return c->df[MIBM_F_DPH];
+    case 2: return c->df[MIBM_F_QCAP];
+  }
+  return c->df[MIBM_F_HTEMP];
+}
+static double* ru_of(Ctx* c, int which) {
+  switch (which) {
+    case 0: return c->df[MIBM_F_RU1];
+    case 1: return c->df[MIBM_F_RU2];
+    case 2: return c->df[MIBM_F_RU3];
+  }
+  return c->df[MIBM_F_RUT];
+}
+
+void k_hdnl(Ctx* c, int which, const StepParams* dp) {
+  hdnl_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), which, dp, hdnl_out(c, which));
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "hdnl");
+}
+
+void k_invtr_rhs(Ctx* c, int which, const StepParams* dp, double* rhs_out) {
+  invtr_rhs_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), which, dp, hdnl_out(c, which),
+                                                                   ru_of(c, which), rhs_out);
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "invtr_rhs");
+}
+
+void k_fused_rhs(Ctx* c, const StepParams* dp) {
+  for (int w = 0; w < 4; ++w) {
+    fused_rhs_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), w, dp, ru_of(c, w),
+                                                                     c->rhs4 + (size_t)w * c->g.cells);
+    ++c->launches;
+  }
+  MIBM_LAUNCH_CHECK(c, "fused_rhs");
+}
+
+void k_divg(Ctx* c, const StepParams* dp) {
+  divg_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, c->df[MIBM_F_DPH]);
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "divg");
+}
+
+void k_updvp(Ctx* c, const StepParams* dp) {
+  updvp_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, c->df[MIBM_F_DPH], c->df[MIBM_F_VX],
+                                                               c->df[MIBM_F_VY], c->df[MIBM_F_VZ]);
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "updvp");
+}
+
+void k_prcalc(Ctx* c, const StepParams* dp) {
+  prcalc_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, c->df[MIBM_F_DPH], c->df[MIBM_F_PR]);
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "prcalc");
+}
+
+void k_add_field(Ctx* c, double* q, const double* r) {
+  add_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, q, r);
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "add");
+}
+
+void k_interp_vof(Ctx* c) {
+  interp_vof_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), c->df[MIBM_F_VOFX],
+                                                                    c->df[MIBM_F_VOFY], c->df[MIBM_F_VOFZ]);
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "interp_vof");
+}
+
+void k_velforce_apply(Ctx* c, const double* mean3) {
+  velforce_apply_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(
+      c->g, mean3, c->df[MIBM_F_FORXC], c->df[MIBM_F_FORYC], c->df[MIBM_F_FORZC], c->df[MIBM_F_VX], c->df[MIBM_F_VY],
+      c->df[MIBM_F_VZ]);
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "velforce");
+}
+
+void k_tempforce_apply(Ctx* c) {
+  tempforce_apply_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, c->df[MIBM_F_FORTEMP],
+                                                                          c->df[MIBM_F_TEMP]);
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "tempforce");
+}
+
+double k_cfl(Ctx* c) {
+  dim3 grid(1, c->g.n2m, c->g.n3m);
+  cfl_kernel<<<grid, 128, 0, c->stream>>>(make_args(c), c->pad_vx, c->pad_vy, c->red + kRedPart);
+  max_reduce_kernel<<<1, 1024, 0, c->stream>>>(c->red + kRedPart, (size_t)c->g.n2m * c->g.n3m, c->red + kRedOut);
+  c->launches += 2;
+  cudaMemcpyAsync(c->red_host, c->red + kRedOut, 8, cudaMemcpyDeviceToHost, c->stream);
+  if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "cfl")) return 0.0;
+  // cfl.f90:448 starts the max at 1e-8
+  return fmax(0.00000001, c->red_host[0]);
+}
+
+double k_get_dt_buffer(Ctx* c, double dt, double ren) {
+  dim3 grid(1, c->g.n2m, c->g.n3m);
+  getdt_kernel<<<grid, 128, 0, c->stream>>>(make_args(c), dt, c->red + kRedPart);
+  max_reduce_kernel<<<1, 1024, 0, c->stream>>>(c->red + kRedPart, (size_t)c->g.n2m * c->g.n3m, c->red + kRedOut);
+  c->launches += 2;
+  cudaMemcpyAsync(c->red_host, c->red + kRedOut, 8, cudaMemcpyDeviceToHost, c->stream);
+  if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "get_dt")) return 0.0;
+  // viscous restriction 6/ren*dt*dx1**2 (cfl.f90:499), the same for every cell
+  return fmax(c->red_host[0], 6.0 / ren * dt * (c->g.dx1 * c->g.dx1));
+}
+
+}  // namespace mibm

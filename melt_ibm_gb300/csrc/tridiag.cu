@@ -1,0 +1,257 @@
+// tridiag.cu -- periodic tridiagonal line solves of the approximate
+// factorisation (solxi.f90:30-44, solxj.f90:17-31, solxk.f90:20-50).
+//
+// The reference assembles, for every line, the constant-coefficient system
+//   -G/(1+2G) x_{i-1} + x_i - G/(1+2G) x_{i+1} = rhs_i/(1+2G)   (periodic)
+// and solves it with tridiag_periodic.f90:1-60 (Thomas sweep plus a
+// periodic closure).  Every quantity of that algorithm that does not involve
+// the right-hand side (q, s, the pivots p and the closure denominator) is the
+// same for all N^2 lines, so it is evaluated once on the host, in the same
+// operation order as the reference, and the device only runs the three
+// data-dependent recurrences:
+//   forward   y_i = a_i r_i - b_i y_{i-1}      (a_i = p_i/(1+2G), b_i = ami p_i)
+//   backward  f_i = y_i + q_i f_{i+1}
+//   closure   x_n = (r_n/(1+2G) - api f_1 - ami f_{n-1}) / den
+//             x_i = x_n s_i + f_i
+// = 4 FP64 operations per element, one read and one write of the line.
+//
+// Lines are staged through shared memory in tiles of up to 32 lines that are
+// contiguous in the fastest address direction, so global loads and stores
+// are coalesced in every direction: x-lines are rows (tile = 32 rows of one
+// k-plane, row pitch n+1 in shared memory), y- and z-lines are columns
+// (tile = 32 adjacent i).  One thread runs one line's recurrences.
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+
+namespace mibm {
+
+struct TriTable {
+  int n = 0;
+  double betadx = -1.0;
+  std::vector<double> h;      // [a | b | q | s] * n, then ackl_b, api, ami, inv_den
+};
+
+// Host evaluation of the line-independent part of tridiag_periodic.
+static void build_table(int n, double betadx, std::vector<double>& t) {
+  double ackl_b = 1.0 / (1.0 + 2.0 * betadx);
+  double api = -betadx * ackl_b, ami = -betadx * ackl_b, aci = 1.0;
+  std::vector<double> q(n + 1), s(n + 1), p(n + 1);
+  q[1] = -api / aci;
+  s[1] = -ami / aci;
+  p[1] = 1.0;
+  for (int i = 2; i <= n; ++i) {
+    p[i] = 1.0 / (aci + ami * q[i - 1]);
+    q[i] = -api * p[i];
+    s[i] = -ami * s[i - 1] * p[i];
+  }
+  s[n] = 1.0;
+  for (int i = n - 1; i >= 1; --i) s[i] = s[i] + q[i] * s[i + 1];
+  double den = api * s[1] + ami * s[n - 1] + aci;
+  t.assign(4 * (size_t)n + 4, 0.0);
+  for (int i = 1; i <= n; ++i) {
+    t[i - 1] = (i == 1) ? ackl_b / aci : ackl_b * p[i];     // a_i
+    t[n + i - 1] = (i == 1) ? 0.0 : ami * p[i];              // b_i
+    t[2 * n + i - 1] = q[i];
+    t[3 * n + i - 1] = s[i];
+  }
+  t[4 * n + 0] = ackl_b;
+  t[4 * n + 1] = api;
+  t[4 * n + 2] = ami;
+  t[4 * n + 3] = 1.0 / den;
+}
+
+// Device table cache: small ring of slots, refilled when (n, betadx) changes.
+struct TriCache {
+  double* dev = nullptr;
+  double* pinned = nullptr;
+  int slots = 0, len = 0, next = 0;
+  std::vector<int> n;
+  std::vector<double> bd;
+};
+static TriCache g_cache_dummy;
+
+struct CtxTri {
+  TriCache cache;
+};
+
+static std::vector<std::pair<Ctx*, CtxTri*>> g_tri;
+
+static CtxTri* tri_of(Ctx* c) {
+  for (auto& e : g_tri)
+    if (e.first == c) return e.second;
+  CtxTri* t = new CtxTri();
+  g_tri.emplace_back(c, t);
+  return t;
+}
+
+// Returns a device pointer to the table of (n, betadx).  The table is
+// written to a pinned slot and copied on the context stream, so the value is
+// stream-ordered with the solve that uses it.
+static const double* table_for(Ctx* c, int n, double betadx) {
+  TriCache& tc = tri_of(c)->cache;
+  int nmax = std::max(c->g.n1m, c->g.n3m);
+  if (!tc.dev) {
+    tc.slots = 64;
+    tc.len = 4 * nmax + 4;
+    if (!cuda_ok(c, cudaMalloc(&tc.dev, sizeof(double) * tc.len * tc.slots), "tri table")) return nullptr;
+    if (!cuda_ok(c, cudaMallocHost(&tc.pinned, sizeof(double) * tc.len * tc.slots), "tri table")) return nullptr;
+    tc.n.assign(tc.slots, -1);
+    tc.bd.assign(tc.slots, -1.0);
+  }
+  for (int s = 0; s < tc.slots; ++s)
+    if (tc.n[s] == n && tc.bd[s] == betadx) return tc.dev + (size_t)s * tc.len;
+  int s = tc.next;
+  tc.next = (tc.next + 1) % tc.slots;
+  std::vector<double> t;
+  build_table(n, betadx, t);
+  // a slot may still be read by an in-flight kernel: order the refill on the stream
+  cudaStreamSynchronize(c->stream);
+  std::copy(t.begin(), t.end(), tc.pinned + (size_t)s * tc.len);
+  cudaMemcpyAsync(tc.dev + (size_t)s * tc.len, tc.pinned + (size_t)s * tc.len, sizeof(double) * t.size(),
+                  cudaMemcpyHostToDevice, c->stream);
+  tc.n[s] = n;
+  tc.bd[s] = betadx;
+  return tc.dev + (size_t)s * tc.len;
+}
+
+void tri_free(Ctx* c) {
+  for (size_t q = 0; q < g_tri.size(); ++q)
+    if (g_tri[q].first == c) {
+      cudaFree(g_tri[q].second->cache.dev);
+      cudaFreeHost(g_tri[q].second->cache.pinned);
+      delete g_tri[q].second;
+      g_tri.erase(g_tri.begin() + q);
+      return;
+    }
+}
+
+// One thread: solve the line held in shared memory at base[e*stride], e=0..n-1
+__device__ __forceinline__ void solve_line(double* base, int stride, int n, const double* __restrict__ T) {
+  const double* a = T;
+  const double* b = T + n;
+  const double* q = T + 2 * n;
+  const double* s = T + 3 * n;
+  double ackl_b = T[4 * n + 0], api = T[4 * n + 1], ami = T[4 * n + 2], inv_den = T[4 * n + 3];
+  double rn = base[(size_t)(n - 1) * stride];
+  double y = a[0] * base[0];
+  base[0] = y;
+  for (int e = 1; e < n - 1; ++e) {
+    double r = base[(size_t)e * stride];
+    y = a[e] * r - b[e] * y;
+    base[(size_t)e * stride] = y;
+  }
+  double f = 0.0;   // f_n = 0
+  for (int e = n - 2; e >= 0; --e) {
+    f = base[(size_t)e * stride] + q[e] * f;
+    base[(size_t)e * stride] = f;
+  }
+  double f1 = base[0], fnm1 = base[(size_t)(n - 2) * stride];
+  double xn = (rn * ackl_b - api * f1 - ami * fnm1) * inv_den;
+  for (int e = 0; e < n - 1; ++e) base[(size_t)e * stride] = xn * s[e] + base[(size_t)e * stride];
+  base[(size_t)(n - 1) * stride] = xn;
+}
+
+constexpr int kLines = 32;
+
+// x-lines: tile = up to 32 rows (j) of one plane k.
+__global__ void solve_x_kernel(Grid g, double* __restrict__ rhs, const double* __restrict__ T) {
+  extern __shared__ double sm[];
+  int n = g.n1m, pitch = n + 1;
+  int j0 = blockIdx.x * kLines, k = blockIdx.y;
+  int nl = min(kLines, g.n2m - j0);
+  for (int l = 0; l < nl; ++l)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) sm[l * pitch + i] = rhs[cidx(g, i, j0 + l, k)];
+  __syncthreads();
+  if (threadIdx.x < nl) solve_line(sm + threadIdx.x * pitch, 1, n, T);
+  __syncthreads();
+  for (int l = 0; l < nl; ++l)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) rhs[cidx(g, i, j0 + l, k)] = sm[l * pitch + i];
+}
+
+// y-lines: tile = up to 32 adjacent i of one plane k; smem[j][l]
+__global__ void solve_y_kernel(Grid g, double* __restrict__ rhs, const double* __restrict__ T) {
+  extern __shared__ double sm[];
+  int n = g.n2m;
+  int i0 = blockIdx.x * kLines, k = blockIdx.y;
+  int nl = min(kLines, g.n1m - i0);
+  for (int t = threadIdx.x; t < n * kLines; t += blockDim.x) {
+    int j = t / kLines, l = t % kLines;
+    if (l < nl) sm[t] = rhs[cidx(g, i0 + l, j, k)];
+  }
+  __syncthreads();
+  if (threadIdx.x < nl) solve_line(sm + threadIdx.x, kLines, n, T);
+  __syncthreads();
+  for (int t = threadIdx.x; t < n * kLines; t += blockDim.x) {
+    int j = t / kLines, l = t % kLines;
+    if (l < nl) rhs[cidx(g, i0 + l, j, k)] = sm[t];
+  }
+}
+
+// z-lines: tile = up to 32 adjacent i of one row j; smem[k][l]; then q += x
+// (solxk.f90:44-50), optionally leaving rhs holding the increment.
+__global__ void solve_z_kernel(Grid g, double* __restrict__ rhs, const double* __restrict__ T, double* __restrict__ q,
+                               int write_rhs) {
+  extern __shared__ double sm[];
+  int n = g.n3m;
+  int i0 = blockIdx.x * kLines, j = blockIdx.y;
+  int nl = min(kLines, g.n1m - i0);
+  for (int t = threadIdx.x; t < n * kLines; t += blockDim.x) {
+    int k = t / kLines, l = t % kLines;
+    if (l < nl) sm[t] = rhs[cidx(g, i0 + l, j, k)];
+  }
+  __syncthreads();
+  if (threadIdx.x < nl) solve_line(sm + threadIdx.x, kLines, n, T);
+  __syncthreads();
+  for (int t = threadIdx.x; t < n * kLines; t += blockDim.x) {
+    int k = t / kLines, l = t % kLines;
+    if (l < nl) {
+      size_t c0 = cidx(g, i0 + l, j, k);
+      double x = sm[t];
+      if (write_rhs) rhs[c0] = x;
+      q[c0] = q[c0] + x;
+    }
+  }
+}
+
+static bool smem_ok(Ctx* c, const void* fn, size_t bytes) {
+  if (bytes > 48 * 1024)
+    return cuda_ok(c, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes), "smem attr");
+  return true;
+}
+
+void k_solve_x(Ctx* c, double* rhs, double betadx) {
+  const double* T = table_for(c, c->g.n1m, betadx);
+  if (!T) return;
+  size_t sm = (size_t)kLines * (c->g.n1m + 1) * sizeof(double);
+  if (!smem_ok(c, (const void*)solve_x_kernel, sm)) return;
+  dim3 grid(div_up(c->g.n2m, kLines), c->g.n3m);
+  solve_x_kernel<<<grid, 128, sm, c->stream>>>(c->g, rhs, T);
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "solve_x");
+}
+
+void k_solve_y(Ctx* c, double* rhs, double betadx) {
+  const double* T = table_for(c, c->g.n2m, betadx);
+  if (!T) return;
+  size_t sm = (size_t)kLines * c->g.n2m * sizeof(double);
+  if (!smem_ok(c, (const void*)solve_y_kernel, sm)) return;
+  dim3 grid(div_up(c->g.n1m, kLines), c->g.n3m);
+  solve_y_kernel<<<grid, 128, sm, c->stream>>>(c->g, rhs, T);
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "solve_y");
+}
+
+void k_solve_z(Ctx* c, double* rhs, double betadx, double* q) {
+  const double* T = table_for(c, c->g.n3m, betadx);
+  if (!T) return;
+  size_t sm = (size_t)kLines * c->g.n3m * sizeof(double);
+  if (!smem_ok(c, (const void*)solve_z_kernel, sm)) return;
+  dim3 grid(div_up(c->g.n1m, kLines), c->g.n2m);
+  solve_z_kernel<<<grid, 128, sm, c->stream>>>(c->g, rhs, T, q, 1);
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "solve_z");
+}
+
+}  // namespace mibm

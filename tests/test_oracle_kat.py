@@ -1,0 +1,239 @@
+"""Known-answer tests of the CPU oracle (the checker).
+
+The reference ships no tests, golden vectors or fixtures, and cannot be
+built here, so the oracle's restatement is pinned by mathematics: each test
+states the property the reference's own algorithm guarantees and checks the
+oracle against it, or against numpy/scipy.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+
+import numpy as np
+import pytest
+
+from melt_ibm_gb300 import abi
+from melt_ibm_gb300.case import Case
+from melt_ibm_gb300.fields import discrete_divergence_max
+from melt_ibm_gb300.mesh import icosphere
+from tests.helpers import small_config
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+DP = C.POINTER(C.c_double)
+
+
+def _p(a):
+    return a.ctypes.data_as(DP)
+
+
+@pytest.mark.parametrize("n", [8, 12, 48, 64, 96])
+def test_tridiag_periodic_matches_dense_solve(oracle_lib, n):
+    """tridiag_periodic.f90 == dense periodic solve (KAT 1)."""
+    rng = np.random.default_rng(n)
+    G = 0.37
+    ack = 1.0 / (1.0 + 2.0 * G)
+    am = np.full(n, -G * ack); ap = am.copy(); ac = np.ones(n)
+    r = rng.standard_normal(n)
+    x = r.copy()
+    oracle_lib.dll.oracle_tridiag_periodic(_p(am), _p(ac), _p(ap), _p(x), C.c_int(n))
+    M = np.diag(ac) + np.diag(am[1:], -1) + np.diag(ap[:-1], 1)
+    M[0, -1] = am[0]
+    M[-1, 0] = ap[-1]
+    ref = np.linalg.solve(M, r)
+    assert np.max(np.abs(x - ref)) <= 1e-13 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("n", [8, 12, 48, 64, 96, 192, 256])
+@pytest.mark.parametrize("sign", [-1, 1])
+def test_dft_matches_numpy(oracle_lib, n, sign):
+    rng = np.random.default_rng(n + 5)
+    z = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    re, im = z.real.copy(), z.imag.copy()
+    oracle_lib.dll.oracle_dft(_p(re), _p(im), C.c_int(n), C.c_int(sign))
+    ref = np.fft.fft(z) if sign < 0 else np.fft.ifft(z) * n
+    assert np.max(np.abs(re + 1j * im - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+def test_lu_inverse_matches_numpy(oracle_lib):
+    rng = np.random.default_rng(3)
+    for _ in range(50):
+        a = rng.standard_normal((4, 4)) + 4 * np.eye(4)
+        a[rng.integers(4)] *= 10
+        b = np.asfortranarray(a.copy())
+        assert oracle_lib.dll.oracle_lu_inverse(_p(b), C.c_int(4)) == 0
+        assert np.allclose(b, np.linalg.inv(a), rtol=1e-12, atol=1e-13)
+    z = np.zeros((4, 4), order="F")
+    assert oracle_lib.dll.oracle_lu_inverse(_p(z), C.c_int(4)) != 0
+
+
+def test_point_triangle_distance_kat(oracle_lib):
+    f = oracle_lib.dll.oracle_point_triangle_distance
+    f.restype = C.c_double
+    V0, V1, V2 = np.array([0.0, 0, 0]), np.array([1.0, 0, 0]), np.array([0.0, 1, 0])
+    cases = [([0.2, 0.2, 0.5], 0.5), ([2.0, 0, 0], 1.0), ([-1.0, -1.0, 0], np.sqrt(2)),
+             ([1.0, 1.0, 0], np.sqrt(0.5)), ([0.5, -2, 0], 2.0)]
+    for P, d in cases:
+        assert abs(f(_p(np.array(P)), _p(V0), _p(V1), _p(V2)) - d) < 1e-14
+
+
+def _projection_case(oracle_lib, n):
+    cfg = small_config(n=n, imlsfor=0, imelt=0)
+    c = Case(cfg)
+    rng = np.random.default_rng(11)
+    for fid in (abi.MIBM_F_VX, abi.MIBM_F_VY, abi.MIBM_F_VZ):
+        c.fields[fid][...] = rng.standard_normal(c.fields[fid].shape)
+        c.fill_ghosts(fid)
+    c.attach(oracle_lib, initial_tag=False)
+    c.set_S(abi.MIBM_S_DT, 0.01)
+    c.set_S(abi.MIBM_S_AL, 8 / 15)
+    c.set_S(abi.MIBM_S_BETA, 0.01 / c.S(abi.MIBM_S_REN) * 0.5)
+    return c
+
+
+@pytest.mark.parametrize("n", [8, 12, 32])
+def test_projection_is_exact_for_discrete_laplacian(oracle_lib, n):
+    """divg -> phcalc -> updvp leaves round-off divergence (KAT 2, phini.f90:35-55)."""
+    c = _projection_case(oracle_lib, n)
+    oracle_lib.divg_()
+    oracle_lib.phcalc_()
+    c.fill_ghosts(abi.MIBM_F_DPH)
+    oracle_lib.updvp_()
+    u, v, w = (c.interior(f) for f in (abi.MIBM_F_VX, abi.MIBM_F_VY, abi.MIBM_F_VZ))
+    assert discrete_divergence_max(u, v, w, c.xlen, c.ylen, c.zlen) < 1e-12 * n
+
+
+def test_phcalc_matches_numpy_poisson(oracle_lib):
+    c = _projection_case(oracle_lib, 16)
+    oracle_lib.divg_()
+    rhs = c.interior(abi.MIBM_F_DPH).copy()
+    oracle_lib.phcalc_()
+    phi = c.interior(abi.MIBM_F_DPH)
+    from melt_ibm_gb300.fields import modified_wavenumbers
+    n = 16
+    a = modified_wavenumbers(n, c.xlen)
+    den = -(a[:, None, None] + a[None, :, None] + a[None, None, :])
+    den[0, 0, 0] = 1.0
+    h = np.fft.fftn(rhs) / den
+    h[0, 0, 0] = 0
+    ref = np.real(np.fft.ifftn(h))
+    assert np.max(np.abs(phi - ref)) < 1e-12 * np.max(np.abs(ref))
+
+
+def test_mls_reproduces_linear_fields(oracle_lib):
+    """MLS with a linear basis interpolates linear fields exactly (KAT 3)."""
+    cfg = small_config(n=24, level=2, imelt=1)
+    c = Case(cfg)
+    c.attach(oracle_lib, initial_tag=False)
+    oracle_lib.findcentroidindices_()
+    oracle_lib.mlsweight_()
+    oracle_lib.check("mlsweight")
+    # a linear temperature field T = a + b.x at cell centres
+    a, b = 0.3, np.array([0.2, -0.7, 0.5])
+    X, Y, Z = np.meshgrid(c.xm, c.ym, c.zm, indexing="ij")
+    bar = c.mesh_arrays[abi.MIBM_M_TRI_BAR]
+    pind = c.mesh_arrays[abi.MIBM_M_PIND]
+    phi = c.mesh_arrays[abi.MIBM_M_PTXAB_TEMP]
+    assert np.allclose(phi.sum(axis=0), 1.0, atol=1e-12)          # partition of unity
+    dx = c.dx1
+    for t in range(0, c.maxnf, 7):
+        i0, j0 = pind[0, t], pind[1, t]
+        k0 = int(np.floor(bar[2, t] * c.dx3)) + 1
+        val = 0.0
+        s = 0
+        for k in range(k0 - 1, k0 + 2):
+            for j in range(j0 - 1, j0 + 2):
+                for i in range(i0 - 1, i0 + 2):
+                    x = ((i - 1) + 0.5) / dx
+                    y = ((j - 1) + 0.5) / c.dx2
+                    z = ((k - 1) + 0.5) / c.dx3
+                    val += phi[s, t] * (a + b @ np.array([x, y, z]))
+                    s += 1
+        assert abs(val - (a + b @ bar[:, t])) < 1e-9
+
+
+def test_heat_flux_gradient_of_linear_field(oracle_lib):
+    """wght_gradT returns the exact gradient of a T linear in x and y.
+
+    The reference builds the z-layers of the cage as k_inds = [k1-1, k1, k1]
+    for the coordinates but reads the field at [k1-1, k1, k1+1]
+    (mls_heatFlux.f90:213-217); the oracle keeps that quirk, so exactness
+    holds for fields without z-variation only.
+    """
+    cfg = small_config(n=32, level=2, imelt=1, tliq=1.0)
+    c = Case(cfg)
+    b = np.array([0.2, -0.7, 0.0])
+    X, Y, Z = np.meshgrid(c.xm, c.ym, c.zm, indexing="ij")
+    T = c.fields[abi.MIBM_F_TEMP]
+    T[:c.n1m, :c.n2m, 1:c.n3m + 1] = 1.0 + b[0] * X + b[1] * Y + b[2] * Z
+    c.fill_ghosts(abi.MIBM_F_TEMP)
+    c.attach(oracle_lib, initial_tag=False)
+    oracle_lib.findprobeindices_()
+    oracle_lib.mls_heatflux_()
+    oracle_lib.check("heatflux")
+    nor = c.mesh_arrays[abi.MIBM_M_TRI_NOR]
+    bar = c.mesh_arrays[abi.MIBM_M_TRI_BAR]
+    qo = c.mesh_arrays[abi.MIBM_M_QW_O]
+    expect = (nor.T @ b) / c.S(abi.MIBM_S_PEC)
+    # the basis [1, x, y, z] uses absolute coordinates (mlsWeight.f90:105-108),
+    # so the moment matrix has a condition number ~1e8: exact to ~1e-8 relative
+    assert np.max(np.abs(qo - expect)) < 1e-6 * np.max(np.abs(expect))
+
+
+def test_kallay_volume_converges_to_sphere():
+    """Kallay volume / centre of the icosphere (KAT 4, RigidAuxRoutines.f90:653-780)."""
+    prev = None
+    for lev in (2, 3, 4):
+        m = icosphere(lev)
+        x = m.xyz
+        f = m.vert_of_face - 1
+        v = np.einsum("ij,ij->i", x[f[:, 0]], np.cross(x[f[:, 1]], x[f[:, 2]])).sum() / 6.0
+        err = abs(v - 4.0 / 3.0 * np.pi)
+        if prev is not None:
+            assert err < prev / 3.5
+        prev = err
+    assert prev < 1e-2
+
+
+def test_sdf_to_vof_limits(oracle_lib):
+    """genSDF.f90:347-365 limits: VOF 0 deep inside, 1 outside, 1/2 on the surface (KAT 6)."""
+    cfg = small_config(n=32, level=3, imelt=1)
+    c = Case(cfg)
+    c.attach(oracle_lib, initial_tag=True)
+    vofp = c.interior(abi.MIBM_F_VOFP)
+    X, Y, Z = np.meshgrid(c.xm, c.ym, c.zm, indexing="ij")
+    r = np.sqrt((X - np.pi) ** 2 + (Y - np.pi) ** 2 + (Z - np.pi) ** 2)
+    R = cfg.rad_p
+    h = 1.0 / c.dx1
+    assert np.all(vofp[r < R - 2 * h] == 0.0)
+    assert np.all(vofp[r > R + 2 * h] == 1.0)
+    band = np.abs(r - R) < 0.25 * h
+    assert np.all(np.abs(vofp[band] - 0.5) < 0.45)
+
+
+def test_oracle_step_divergence_free(oracle_lib):
+    """A full RK3 step of the oracle leaves post-projection divergence <= 1e-12."""
+    cfg = small_config(n=16, level=2)
+    c = Case(cfg)
+    c.attach(oracle_lib)
+    c.run(oracle_lib, 2)
+    u, v, w = (c.interior(f) for f in (abi.MIBM_F_VX, abi.MIBM_F_VY, abi.MIBM_F_VZ))
+    assert discrete_divergence_max(u, v, w, c.xlen, c.ylen, c.zlen) < 1e-12
+
+
+def test_oracle_golden_checksums(oracle_lib):
+    """The oracle reproduces its committed fixture (same numbers on x86 and Arm)."""
+    path = os.path.join(GOLDEN, "oracle_c16_2steps.json")
+    gold = json.load(open(path))
+    cfg = small_config(n=16, level=2)
+    c = Case(cfg)
+    c.attach(oracle_lib)
+    c.run(oracle_lib, 2)
+    for name, fid in (("vx", abi.MIBM_F_VX), ("vy", abi.MIBM_F_VY), ("vz", abi.MIBM_F_VZ),
+                      ("temp", abi.MIBM_F_TEMP), ("pr", abi.MIBM_F_PR)):
+        a = c.interior(fid)
+        assert abs(float(np.sum(a)) - gold[name]["sum"]) <= 1e-12 * max(1.0, abs(gold[name]["sum"])) + 1e-12
+        assert abs(float(np.sqrt(np.sum(a * a))) - gold[name]["l2"]) <= 1e-12 * gold[name]["l2"]
+    assert abs(c.S(abi.MIBM_S_DT) - gold["dt"]) <= 1e-15
+    assert abs(c.S(abi.MIBM_S_VOLUME) - gold["volume"]) <= 1e-14
