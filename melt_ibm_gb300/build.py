@@ -19,7 +19,12 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libmibm.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Host code (coordinate, wavenumber and line-solve tables) is compiled without
+# floating-point contraction: gcc on Arm fuses a*b+c into FMAs by default,
+# which moves knife-edge decisions of the reference's arithmetic (e.g. the
+# MLS weight cut-off r > 1 when a marker sits exactly on a cell face).
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
+         "-Xcompiler", "-ffp-contract=off",
          "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 
 

@@ -26,6 +26,8 @@ def randomize(case: Case, seed: int = 7, forcing: bool = True) -> None:
     """Fill the state a routine reads with seeded noise (test inputs only)."""
     rng = np.random.default_rng(seed)
     A = abi
+    for fid in (A.MIBM_F_VX, A.MIBM_F_VY, A.MIBM_F_VZ):     # not divergence-free
+        case.fields[fid][...] += 0.1 * rng.standard_normal(case.fields[fid].shape)
     for fid in (A.MIBM_F_PR, A.MIBM_F_RU1, A.MIBM_F_RU2, A.MIBM_F_RU3, A.MIBM_F_RUT,
                 A.MIBM_F_DQ, A.MIBM_F_QCAP, A.MIBM_F_HTEMP):
         case.fields[fid][...] = rng.standard_normal(case.fields[fid].shape)
