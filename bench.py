@@ -1,0 +1,354 @@
+#!/usr/bin/env python3
+"""Benchmark of the melt_IBM RK3 step on GB300 (one JSON line on stdout).
+
+A "step" is one iteration of the reference time loop (gcurv.f90:151-172):
+cfl -> get_dt -> tschem (3 RK3 substeps: explicit terms, factored implicit
+line solves, MLS immersed-boundary forcing with melting, FFT pressure
+projection).  Metric: Mcell-steps/s = N^3 * steps / seconds.
+
+value      device time of K steps with every field resident in HBM (CUDA events
+           on the library's stream, synchronised on both sides).
+e2e        the same K steps driven the way a Fortran host drives the C-ABI:
+           every step copies u, v, w, T, p and the vertex coordinates from host
+           arrays to the device (mibm_sync_from_host_), runs cfl_/get_dt_/tschem_
+           and copies the five fields and the vertices back (mibm_sync_to_host_);
+           wall-clock time.
+roofline   the dominant kernel's algorithmic bytes per launch / its average
+           launch time, both measured live in the timed region (per-kernel CUDA
+           events on the launching stream, second timed pass), against the
+           measured HBM copy bandwidth.
+cpu_baseline / --impl reference
+           the CPU oracle (C++ restatement of the reference's algorithm, OpenMP,
+           all host threads) on the same workload: the reference itself (Fortran +
+           MPI + FFTW + HDF5) cannot be built on this machine or the GPU machine.
+
+Inputs are larger than L2 (each field is N^3 doubles; > 30 fields resident).
+Multi-GPU: independent replicas, one per rank (the case does not shard across
+GPUs in this build); value = all ranks' cell-steps / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+from melt_ibm_gb300 import abi  # noqa: E402
+from melt_ibm_gb300.case import Case, CaseConfig  # noqa: E402
+
+# Workload: the grid, body, viscosity and Stefan number of the 128^3 FP64
+# configuration (icosphere subdivided 4 times, r = 0.4, nu = 0.005, St = 1,
+# seeded random-phase initial field, seed 1), with the body held fixed.
+WORKLOADS = {
+    "melt128_fixed": dict(n=128, mesh_level=4, rad_p=0.4, ren=200.0, prandtl=1.0, latheat=1.0, cpliquid=1.0,
+                          imelt=1, imlsstr=0, seed=1, v_on_ve=0.0),
+    "melt64_c0": dict(n=64, mesh_level=3, rad_p=0.5, ren=100.0, prandtl=1.0, latheat=1.0, cpliquid=1.0,
+                      imelt=1, imlsstr=0, seed=0, v_on_ve=0.0),
+    "melt256_fixed": dict(n=256, mesh_level=5, rad_p=0.4, ren=400.0, prandtl=1.0, latheat=2.0, cpliquid=1.0,
+                          imelt=1, imlsstr=0, seed=2, v_on_ve=0.0),
+}
+WORKLOAD_TEXT = {
+    "melt128_fixed": "128^3 FP64, icosphere level 4 (5120 tri) r=0.4 melting (St=1), nu=0.005, body fixed "
+                     "(Newton-Euler, linear HIT forcing and remeshing of the 128^3 configuration not built)",
+    "melt64_c0": "64^3 FP64 plain configuration: icosphere level 3 r=0.5, nu=kappa=0.01, St=1",
+    "melt256_fixed": "256^3 FP64, icosphere level 5 r=0.4 melting (St=2), nu=0.0025, body fixed",
+}
+
+# Algorithmic bytes per launch of the kernels that can be dominant (FP64,
+# compulsory field reads + writes of that kernel, N^3 cells): see the design doc.
+ALGO_PASSES = {
+    "fused_rhs": 7.0,      # x/y/z/T average: reads u,v,w(,T),p,ru ; writes rhs, ru
+    "solve_x": 2.0, "solve_y": 2.0, "solve_z": 4.0,
+    "fft_x_fwd": 1.0 + 1.125, "fft_y": 2.25, "fft_z_solve": 2.25, "fft_x_inv": 1.125 + 1.0,
+    "divg": 4.0, "updvp": 7.0, "prcalc": 3.0, "hdnl": 6.0,
+}
+
+FIELD_MASK = sum(1 << f for f in (abi.MIBM_F_VX, abi.MIBM_F_VY, abi.MIBM_F_VZ, abi.MIBM_F_TEMP, abi.MIBM_F_PR))
+MESH_MASK = 1 << (32 + abi.MIBM_M_XYZV)
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def measured_peaks() -> dict:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Barrier / max-reduce over ranks (gloo over the loopback; replicas only)."""
+
+    def __init__(self):
+        self.ws, self.rank, self.local = dist_env()
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as td
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.ws > 1:
+            self.td.barrier()
+
+    def max(self, v: float) -> float:
+        if self.ws == 1:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.td.destroy_process_group()
+
+
+def cpu_baseline(workload: str, steps: int, threads: int | None = None) -> dict:
+    """Time the CPU oracle on a bounded sample of the same workload."""
+    import oracle
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    lib = abi.Lib(oracle.build())
+    case = Case(CaseConfig(**WORKLOADS[workload]))
+    case.attach(lib)
+    case.step(lib, 1)                       # warm-up step (also the reference's ntime = 1)
+    t0 = time.perf_counter()
+    for nt in range(2, 2 + steps):
+        case.step(lib, nt)
+    dt = time.perf_counter() - t0
+    n3 = case.n1m * case.n2m * case.n3m
+    nthreads = int(lib.dll.oracle_num_threads())
+    case.detach(lib)
+    return {"value": n3 * steps / dt / 1e6, "unit": "Mcell-steps/s", "cores": nthreads, "kind": "port",
+            "sample": f"{steps} RK3 steps of {workload} after 1 warm-up step, {dt:.1f} s, "
+                      f"CPU oracle (C++ restatement, not the reference binary), {nthreads} OpenMP threads"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    steps = args.steps
+    base = cpu_baseline(args.workload, steps)
+    line = {"metric": "Mcell-steps/s", "value": base["value"], "unit": "Mcell-steps/s", "n_gpus": args.gpus,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": args.workload, "description": WORKLOAD_TEXT[args.workload],
+                       "l2": "inputs larger than L2"},
+            "cpu_baseline": {"value": base["value"], "unit": base["unit"], "cores": base["cores"],
+                             "kind": base["kind"], "sample": base["sample"]},
+            "e2e": {"value": base["value"], "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    n3 = WORKLOADS[args.workload]["n"] ** 3
+    line["ms_per_step"] = 1e3 * n3 / (base["value"] * 1e6)
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    from melt_ibm_gb300 import build as mbuild
+    dist = Dist()
+    lib = abi.Lib(mbuild.build())
+    ndev = lib.mibm_device_count_()
+    if ndev < 1:
+        raise SystemExit("bench: no CUDA device visible (libmibm.so needs a GPU)")
+    dev = dist.local % ndev
+    lib.mibm_select_device_(abi.ref_int(dev))
+    cfg = CaseConfig(**WORKLOADS[args.workload])
+    case = Case(cfg)
+    case.attach(lib)
+    lib.check("attach")
+    n3 = case.n1m * case.n2m * case.n3m
+    nt = 1
+    for _ in range(args.warmup):
+        case.step(lib, nt)
+        nt += 1
+    case.sync_to_host(lib, 0)               # drains the stream
+    # ---------------- timed region: device-resident ----------------
+    dist.barrier()
+    l0 = lib.mibm_launch_count_()
+    with ClockSampler(dev) as clk:
+        lib.mibm_timer_mark_(abi.ref_int(0))
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            case.step(lib, nt)
+            nt += 1
+        lib.mibm_timer_mark_(abi.ref_int(1))
+        ms = lib.mibm_timer_ms_(abi.ref_int(0), abi.ref_int(1))
+        wall = time.perf_counter() - t0
+    launches = int(lib.mibm_launch_count_() - l0)
+    lib.check("timed steps")
+    dist.barrier()
+    ms_max = dist.max(ms)
+    value = dist.ws * n3 * args.steps / (ms_max * 1e-3) / 1e6
+    clocks = clk.summary()
+    # ---------------- per-kernel pass (roofline of the dominant kernel) ----------------
+    lib.mibm_profile_(abi.ref_int(1))
+    for _ in range(args.steps):
+        case.step(lib, nt)
+        nt += 1
+    lib.mibm_profile_(abi.ref_int(0))
+    prof = lib.profile()
+    total = sum(v[0] for v in prof.values()) or 1.0
+    dominant = max(prof.items(), key=lambda kv: kv[1][0])
+    dname, (dms, dcnt) = dominant
+    avg_ms = dms / max(1, dcnt)
+    passes = ALGO_PASSES.get(dname)
+    peaks = measured_peaks()
+    roofline = None
+    if passes is not None:
+        algo_bytes = passes * 8.0 * n3
+        achieved = algo_bytes / (avg_ms * 1e-3) / 1e9
+        roofline = {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peaks["hbm_gbs"],
+                    "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                    "algo_bytes_per_launch": algo_bytes, "avg_launch_ms": avg_ms,
+                    "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs)",
+                    "note": "FP64 stencils are bounded by the FP64 FMA rate (about 1.2 TFLOP/s measured), "
+                            "not HBM; see profiles/"}
+    kernels = {k: {"ms_per_step": v[0] / args.steps, "launches_per_step": v[1] / args.steps,
+                   "share": v[0] / total} for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
+    # ---------------- e2e: host buffers, copies inside the timed region ----------------
+    h2d = 0
+    d2h = 0
+    for fid in (abi.MIBM_F_VX, abi.MIBM_F_VY, abi.MIBM_F_VZ, abi.MIBM_F_TEMP, abi.MIBM_F_PR):
+        a = case.fields[fid]
+        h2d += a.nbytes                                  # whole Fortran array (mibm_sync_from_host_)
+        wx = case.n1m + 1 if fid == abi.MIBM_F_VX else case.n1m     # owned cells (+ padding read by cfl)
+        hy = case.n2m + 1 if fid == abi.MIBM_F_VY else case.n2m
+        d2h += 8 * wx * hy * a.shape[2]
+    h2d += case.mesh_arrays[abi.MIBM_M_XYZV].nbytes
+    d2h += case.mesh_arrays[abi.MIBM_M_XYZV].nbytes
+    case.sync_to_host(lib, FIELD_MASK | MESH_MASK)
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        case.sync_from_host(lib, FIELD_MASK | MESH_MASK)
+        case.step(lib, nt)
+        nt += 1
+        case.sync_to_host(lib, FIELD_MASK | MESH_MASK)
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e_value = dist.ws * n3 * args.steps / e2e_s / 1e6
+    lib.check("e2e")
+    case.detach(lib)
+    dist.barrier()
+    if dist.rank != 0:
+        dist.close()
+        return
+    line = {"metric": "Mcell-steps/s", "value": value, "unit": "Mcell-steps/s", "n_gpus": dist.ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded random-phase velocity, tanh temperature, generated icosphere)",
+            "config": {"workload": args.workload, "description": WORKLOAD_TEXT[args.workload],
+                       "grid": [case.n1m, case.n2m, case.n3m], "triangles": case.maxnf,
+                       "parallelism": f"replicas x{dist.ws}" if dist.ws > 1 else "single GPU",
+                       "l2": "inputs larger than L2 (>30 fields of N^3 doubles resident)"},
+            "e2e": {"value": e2e_value, "unit": "Mcell-steps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "roofline": roofline, "gpu_launches": launches, "clocks": clocks,
+            "host_wall_ms_per_step": 1e3 * wall / args.steps, "kernels": kernels}
+    if dist.ws == 1 and not args.no_cpu:
+        try:
+            line["cpu_baseline"] = cpu_baseline(args.workload, args.cpu_steps)
+        except Exception as e:  # noqa: BLE001
+            line["cpu_baseline"] = {"value": None, "error": str(e)}
+    print(json.dumps(line), flush=True)
+    dist.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["mibm", "reference"], default="mibm")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="melt128_fixed")
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        log("bench: warm-up raised to 3 steps")
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

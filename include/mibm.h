@@ -152,6 +152,19 @@ void mibm_sync_to_host_(const long long* mask);
  * context so far (libmibm.so only). */
 int  mibm_device_count_(void);
 unsigned long long mibm_launch_count_(void);
+/* Select the CUDA device for contexts created afterwards by this thread. */
+int  mibm_select_device_(const int* dev);
+/* Phase timers (the reference's TIMED clocks, tsch.f90:26-84): record CUDA
+ * event `slot` (0..63) on the bound context's stream; elapsed milliseconds
+ * between two recorded slots (waits for the later one). */
+void mibm_timer_mark_(const int* slot);
+double mibm_timer_ms_(const int* a, const int* b);
+/* Per-kernel profile of the bound context: on = 1 starts (and clears),
+ * 0 stops; entries give kernel name, summed event time and launch count. */
+void mibm_profile_(const int* on);
+int  mibm_profile_count_(void);
+int  mibm_profile_get_(const int* idx, char* name, const int* cap, double* total_ms,
+                       long long* launches);
 
 /* ------------------------------------------------------------------ */
 /* Drop-in routines (reference file:line of the routine each replaces) */

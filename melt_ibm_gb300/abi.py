@@ -60,6 +60,12 @@ SIGNATURES: dict[str, tuple] = {
     "mibm_sync_to_host_": (None, [_L]),
     "mibm_device_count_": (C.c_int, []),
     "mibm_launch_count_": (C.c_ulonglong, []),
+    "mibm_select_device_": (C.c_int, [_I]),
+    "mibm_timer_mark_": (None, [_I]),
+    "mibm_timer_ms_": (C.c_double, [_I, _I]),
+    "mibm_profile_": (None, [_I]),
+    "mibm_profile_count_": (C.c_int, []),
+    "mibm_profile_get_": (C.c_int, [_I, C.c_char_p, _I, _D, C.POINTER(C.c_longlong)]),
     "solxi_": (None, [_D]),
     "solxj_": (None, [_D]),
     "solxk_": (None, [C.c_void_p, _D]),
@@ -99,6 +105,17 @@ class Lib:
 
     def __getattr__(self, name):
         return getattr(self.dll, name)
+
+    def profile(self) -> dict[str, tuple[float, int]]:
+        """Per-kernel totals of the bound context: name -> (ms, launches)."""
+        out = {}
+        n = self.dll.mibm_profile_count_()
+        buf = C.create_string_buffer(128)
+        for i in range(n):
+            ms, cnt = C.c_double(), C.c_longlong()
+            self.dll.mibm_profile_get_(C.byref(C.c_int(i)), buf, C.byref(C.c_int(128)), C.byref(ms), C.byref(cnt))
+            out[buf.value.decode()] = (ms.value, cnt.value)
+        return out
 
     def check(self, what: str = "") -> None:
         st = self.dll.mibm_last_status_()

@@ -104,6 +104,7 @@ struct Ctx {
   cudaGraphExec_t graph_exec = nullptr;
   bool use_graph = true;
   uint64_t launches = 0;                  // kernels launched through this context
+  cudaEvent_t timers[64] = {nullptr};
 
   double S(int id) const { return *hs[id]; }
   int I(int id) const { return *hi[id]; }
@@ -116,6 +117,20 @@ bool ready(Ctx* c);
 StepParams host_params(Ctx* c);
 
 #define MIBM_LAUNCH_CHECK(c, what) cuda_ok((c), cudaGetLastError(), (what))
+
+// Brackets the launches in its scope with CUDA events when profiling is on
+// (prof.cu); a no-op otherwise.
+class ProfScope {
+ public:
+  ProfScope(Ctx* c, const char* name);
+  ~ProfScope();
+ private:
+  Ctx* c_;
+  int idx_;
+};
+#define MIBM_PROF(c, name) ::mibm::ProfScope _mibm_prof_scope_((c), (name))
+void prof_release(Ctx* c);
+void prof_flush_if_full(Ctx* c);
 
 inline __host__ __device__ size_t cidx(const Grid& g, int i, int j, int k) {
   return (size_t)i + (size_t)g.P * ((size_t)j + (size_t)g.n2m * (size_t)k);

@@ -233,6 +233,9 @@ void release(Ctx* c) {
   if (c->red_host) cudaFreeHost(c->red_host);
   if (c->hflag) cudaFreeHost(c->hflag);
   if (c->hparams) cudaFreeHost(c->hparams);
+  for (int q = 0; q < 64; ++q)
+    if (c->timers[q]) cudaEventDestroy(c->timers[q]);
+  prof_release(c);
   lagr_free(c);
   tri_free(c);
   fft_free(c);
@@ -411,6 +414,27 @@ int mibm_device_count_(void) {
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess) { cudaGetLastError(); return 0; }
   return n;
+}
+
+int mibm_select_device_(const int* dev) {
+  cudaError_t e = cudaSetDevice(*dev);
+  if (e != cudaSuccess) { t_status = MIBM_ECUDA; t_msg = cudaGetErrorString(e); return MIBM_ECUDA; }
+  return MIBM_OK;
+}
+
+void mibm_timer_mark_(const int* slot) {
+  Ctx* c = current(); if (!c || *slot < 0 || *slot >= 64) return;
+  if (!c->timers[*slot] && !cuda_ok(c, cudaEventCreate(&c->timers[*slot]), "event")) return;
+  cuda_ok(c, cudaEventRecord(c->timers[*slot], c->stream), "event record");
+}
+
+double mibm_timer_ms_(const int* a, const int* b) {
+  Ctx* c = current();
+  if (!c || *a < 0 || *a >= 64 || *b < 0 || *b >= 64 || !c->timers[*a] || !c->timers[*b]) return -1.0;
+  if (!cuda_ok(c, cudaEventSynchronize(c->timers[*b]), "event sync")) return -1.0;
+  float ms = 0.f;
+  if (!cuda_ok(c, cudaEventElapsedTime(&ms, c->timers[*a], c->timers[*b]), "event elapsed")) return -1.0;
+  return (double)ms;
 }
 
 // Number of kernels launched through the bound context (for the benchmark's

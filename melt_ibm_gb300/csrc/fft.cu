@@ -319,11 +319,11 @@ void k_phcalc(Ctx* c) {
   dim3 gx(div_up(g.n2m / 2, kRowPairs), g.n3m);
   dim3 gy(div_up(g.H, kCols), g.n3m);
   dim3 gz(div_up(g.H, kCols), g.n2m);
-  fft_x_fwd<<<gx, 256, smx, c->stream>>>(F, dph, c->spec);
-  fft_y<<<gy, 256, smy, c->stream>>>(F, c->spec, -1);
-  fft_z_solve<<<gz, 256, smz, c->stream>>>(F, c->spec);
-  fft_y<<<gy, 256, smy, c->stream>>>(F, c->spec, +1);
-  fft_x_inv<<<gx, 256, smx, c->stream>>>(F, c->spec, dph);
+  { MIBM_PROF(c, "fft_x_fwd"); fft_x_fwd<<<gx, 256, smx, c->stream>>>(F, dph, c->spec); }
+  { MIBM_PROF(c, "fft_y"); fft_y<<<gy, 256, smy, c->stream>>>(F, c->spec, -1); }
+  { MIBM_PROF(c, "fft_z_solve"); fft_z_solve<<<gz, 256, smz, c->stream>>>(F, c->spec); }
+  { MIBM_PROF(c, "fft_y"); fft_y<<<gy, 256, smy, c->stream>>>(F, c->spec, +1); }
+  { MIBM_PROF(c, "fft_x_inv"); fft_x_inv<<<gx, 256, smx, c->stream>>>(F, c->spec, dph); }
   c->launches += 5;
   MIBM_LAUNCH_CHECK(c, "phcalc");
 }

@@ -380,8 +380,8 @@ static void build_plan(Ctx* c, int comp) {
   if (n == 0) { p.n = 0; p.valid = true; return; }
   if (!plan_alloc(c, p, n)) return;
   p.n = n;
-  plan_keys_kernel<<<div_up(n, 256), 256, 0, c->stream>>>(c->g, nf, comp, M<int>(c, MIBM_M_PIND),
-                                                          M<int>(c, MIBM_M_GHOST_FACE), p.tmp_key, p.tmp_src);
+  { MIBM_PROF(c, "plan_keys"); plan_keys_kernel<<<div_up(n, 256), 256, 0, c->stream>>>(c->g, nf, comp, M<int>(c, MIBM_M_PIND),
+                                                          M<int>(c, MIBM_M_GHOST_FACE), p.tmp_key, p.tmp_src); }
   ++c->launches;
   int nblk = (n + kSortChunk - 1) / kSortChunk;
   // cell keys < cells (< 2^31); INT_MAX marks ghost faces
@@ -390,9 +390,9 @@ static void build_plan(Ctx* c, int comp) {
   int passes = (bits + 7) / 8;
   for (int ps = 0; ps < passes; ++ps) {
     int shift = 8 * ps;
-    radix_hist_kernel<<<nblk, 256, 0, c->stream>>>(kin, n, shift, nblk, p.hist);
+    { MIBM_PROF(c, "radix_hist"); radix_hist_kernel<<<nblk, 256, 0, c->stream>>>(kin, n, shift, nblk, p.hist); }
     scan_kernel<<<1, 1024, 0, c->stream>>>(p.hist, 256 * nblk);
-    radix_scatter_kernel<<<nblk, 256, 0, c->stream>>>(kin, vin, kout, vout, n, shift, nblk, p.hist);
+    { MIBM_PROF(c, "radix_scatter"); radix_scatter_kernel<<<nblk, 256, 0, c->stream>>>(kin, vin, kout, vout, n, shift, nblk, p.hist); }
     c->launches += 3;
     std::swap(kin, kout); std::swap(vin, vout);
   }
@@ -1002,8 +1002,8 @@ bool validate_mesh(Ctx* c) {
 // ---------------------------------------------------------------------
 void lagr_find_centroid_indices(Ctx* c) {
   if (c->maxnf == 0) return;
-  centroid_idx_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(
-      lag_args(c), M<double>(c, MIBM_M_TRI_BAR), M<int>(c, MIBM_M_GHOST_FACE), M<int>(c, MIBM_M_PIND));
+  { MIBM_PROF(c, "centroid_idx"); centroid_idx_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(
+      lag_args(c), M<double>(c, MIBM_M_TRI_BAR), M<int>(c, MIBM_M_GHOST_FACE), M<int>(c, MIBM_M_PIND)); }
   ++c->launches;
   for (int q = 0; q < 4; ++q) c->plan[q].valid = false;
   MIBM_LAUNCH_CHECK(c, "findCentroidIndices");
@@ -1011,10 +1011,10 @@ void lagr_find_centroid_indices(Ctx* c) {
 
 void lagr_mls_weight(Ctx* c) {
   if (c->maxnf == 0) return;
-  mls_weight_kernel<<<div_up(4 * (size_t)c->maxnf, 128), 128, 0, c->stream>>>(
+  { MIBM_PROF(c, "mls_weight"); mls_weight_kernel<<<div_up(4 * (size_t)c->maxnf, 128), 128, 0, c->stream>>>(
       lag_args(c), M<double>(c, MIBM_M_TRI_BAR), M<int>(c, MIBM_M_GHOST_FACE), M<int>(c, MIBM_M_PIND),
       M<double>(c, MIBM_M_PTXAB_Q1), M<double>(c, MIBM_M_PTXAB_Q2), M<double>(c, MIBM_M_PTXAB_Q3),
-      M<double>(c, MIBM_M_PTXAB_TEMP), c->dflag);
+      M<double>(c, MIBM_M_PTXAB_TEMP), c->dflag); }
   ++c->launches;
   if (MIBM_LAUNCH_CHECK(c, "mlsWeight")) check_flag(c, "mlsWeight");
 }
@@ -1029,17 +1029,17 @@ void lagr_mls_force(Ctx* c, const StepParams* dp, bool) {
   F.vel_tri = M<double>(c, MIBM_M_VEL_TRI); F.cfac = M<double>(c, MIBM_M_CFAC);
   F.pind = M<int>(c, MIBM_M_PIND); F.ghost = M<int>(c, MIBM_M_GHOST_FACE);
   (void)dp;
-  force_coef_kernel<<<div_up(4 * (size_t)c->maxnf, 128), 128, 0, c->stream>>>(c->g, c->maxnf, F, c->S(MIBM_S_TMELT),
-                                                                                c->tri_coef);
+  { MIBM_PROF(c, "force_coef"); force_coef_kernel<<<div_up(4 * (size_t)c->maxnf, 128), 128, 0, c->stream>>>(c->g, c->maxnf, F, c->S(MIBM_S_TMELT),
+                                                                                c->tri_coef); }
   ++c->launches;
   static const int outf[4] = {MIBM_F_FORXC, MIBM_F_FORYC, MIBM_F_FORZC, MIBM_F_FORTEMP};
   for (int comp = 0; comp < 4; ++comp) {
     if (!c->plan[comp].valid) build_plan(c, comp);
     Ctx::Plan& p = c->plan[comp];
     if (p.n == 0) continue;
-    scatter_apply_kernel<<<div_up(p.n, 256), 256, 0, c->stream>>>(p.n, p.key, p.src,
+    { MIBM_PROF(c, "scatter_apply"); scatter_apply_kernel<<<div_up(p.n, 256), 256, 0, c->stream>>>(p.n, p.key, p.src,
                                                                    c->tri_coef + (size_t)comp * c->maxnf,
-                                                                   F.ptx[comp], c->df[outf[comp]]);
+                                                                   F.ptx[comp], c->df[outf[comp]]); }
     ++c->launches;
   }
   MIBM_LAUNCH_CHECK(c, "mlsForce");
@@ -1049,8 +1049,8 @@ void lagr_velforce(Ctx* c) {
   if (!ensure_lag_buffers(c)) return;
   LagState* s = lag_of(c);
   dim3 grid(c->g.n2m, c->g.n3m);
-  field_sum_kernel<<<grid, 128, 0, c->stream>>>(c->g, c->df[MIBM_F_FORXC], c->df[MIBM_F_FORYC], c->df[MIBM_F_FORZC],
-                                                c->red + kRedPart);
+  { MIBM_PROF(c, "field_sum"); field_sum_kernel<<<grid, 128, 0, c->stream>>>(c->g, c->df[MIBM_F_FORXC], c->df[MIBM_F_FORYC], c->df[MIBM_F_FORZC],
+                                                c->red + kRedPart); }
   double ncell = (double)c->g.n1m * (double)c->g.n2m * (double)c->g.n3m;
   mean3_kernel<<<1, 1024, 0, c->stream>>>(c->red + kRedPart, c->g.n2m * c->g.n3m, ncell, s->mean3);
   c->launches += 2;
@@ -1061,9 +1061,9 @@ void lagr_tempforce(Ctx* c) { k_tempforce_apply(c); }
 
 void lagr_find_probe_indices(Ctx* c) {
   if (c->maxnf == 0) return;
-  probe_idx_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(
+  { MIBM_PROF(c, "probe_idx"); probe_idx_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(
       lag_args(c), M<double>(c, MIBM_M_TRI_BAR), M<double>(c, MIBM_M_TRI_NOR), M<int>(c, MIBM_M_GHOST_FACE),
-      c->S(MIBM_S_H_EULERIAN), M<int>(c, MIBM_M_PIND));
+      c->S(MIBM_S_H_EULERIAN), M<int>(c, MIBM_M_PIND)); }
   ++c->launches;
   for (int q = 0; q < 4; ++q) c->plan[q].valid = false;
   MIBM_LAUNCH_CHECK(c, "findProbeIndices");
@@ -1073,23 +1073,23 @@ void lagr_heat_flux(Ctx* c) {
   if (c->maxnf == 0) return;
   if (!ensure_adjacency(c)) return;
   LagState* s = lag_of(c);
-  heat_flux_kernel<<<div_up(2 * (size_t)c->maxnf, 64), 64, 0, c->stream>>>(
+  { MIBM_PROF(c, "heat_flux"); heat_flux_kernel<<<div_up(2 * (size_t)c->maxnf, 64), 64, 0, c->stream>>>(
       lag_args(c), c->df[MIBM_F_TEMP], M<double>(c, MIBM_M_TRI_BAR), M<double>(c, MIBM_M_TRI_NOR),
       M<int>(c, MIBM_M_GHOST_FACE), M<int>(c, MIBM_M_PIND), c->S(MIBM_S_H_EULERIAN), c->S(MIBM_S_PEC),
-      M<double>(c, MIBM_M_QW_O), M<double>(c, MIBM_M_QW_I), c->dflag);
-  face_to_vert_kernel<<<div_up(c->maxnv, 128), 128, 0, c->stream>>>(
+      M<double>(c, MIBM_M_QW_O), M<double>(c, MIBM_M_QW_I), c->dflag); }
+  { MIBM_PROF(c, "face_to_vert"); face_to_vert_kernel<<<div_up(c->maxnv, 128), 128, 0, c->stream>>>(
       c->maxnv, s->adj_off, s->adj_face, M<double>(c, MIBM_M_SUR), M<double>(c, MIBM_M_AVERT),
-      M<double>(c, MIBM_M_QW_O), M<double>(c, MIBM_M_QW_I), M<double>(c, MIBM_M_QW_OVERT), M<double>(c, MIBM_M_QW_IVERT));
+      M<double>(c, MIBM_M_QW_O), M<double>(c, MIBM_M_QW_I), M<double>(c, MIBM_M_QW_OVERT), M<double>(c, MIBM_M_QW_IVERT)); }
   c->launches += 2;
   if (MIBM_LAUNCH_CHECK(c, "mls_heatFlux")) check_flag(c, "mls_heatFlux");
 }
 
 void lagr_stefan(Ctx* c, const StepParams* dp) {
   if (c->maxnv == 0) return;
-  stefan_kernel<<<div_up(c->maxnv, 128), 128, 0, c->stream>>>(
+  { MIBM_PROF(c, "stefan"); stefan_kernel<<<div_up(c->maxnv, 128), 128, 0, c->stream>>>(
       c->maxnv, M<int>(c, MIBM_M_GHOST_VERT), M<double>(c, MIBM_M_VERT_NOR), M<double>(c, MIBM_M_QW_OVERT),
       M<double>(c, MIBM_M_QW_IVERT), c->S(MIBM_S_CPLIQUID) / c->S(MIBM_S_LATHEAT), dp, M<double>(c, MIBM_M_VMELT),
-      M<double>(c, MIBM_M_VMELT_M1), M<double>(c, MIBM_M_XYZV));
+      M<double>(c, MIBM_M_VMELT_M1), M<double>(c, MIBM_M_XYZV)); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "stefan");
 }
@@ -1100,12 +1100,12 @@ void lagr_geometry_refresh(Ctx* c, bool imelt) {
   if (c->maxnf == 0) return;
   if (!ensure_adjacency(c) || !ensure_lag_buffers(c)) return;
   LagState* s = lag_of(c);
-  face_geom_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(
+  { MIBM_PROF(c, "face_geom"); face_geom_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(
       c->maxnf, M<int>(c, MIBM_M_VERT_OF_FACE), M<int>(c, MIBM_M_GHOST_FACE), M<double>(c, MIBM_M_XYZV),
-      M<double>(c, MIBM_M_SUR), M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_TRI_BAR), s->face_part);
-  vert_geom_kernel<<<div_up(c->maxnv, 128), 128, 0, c->stream>>>(
+      M<double>(c, MIBM_M_SUR), M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_TRI_BAR), s->face_part); }
+  { MIBM_PROF(c, "vert_geom"); vert_geom_kernel<<<div_up(c->maxnv, 128), 128, 0, c->stream>>>(
       c->maxnv, s->adj_off, s->adj_face, M<int>(c, MIBM_M_GHOST_VERT), M<double>(c, MIBM_M_SUR),
-      M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_AVERT), M<double>(c, MIBM_M_VERT_NOR));
+      M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_AVERT), M<double>(c, MIBM_M_VERT_NOR)); }
   geom_reduce_kernel<<<1, 256, 0, c->stream>>>(c->maxnf, s->face_part, s->geom_out);
   c->launches += 3;
   if (imelt) {
@@ -1134,11 +1134,11 @@ void lagr_tag_narrow_band(Ctx* c) {
   T.L = lag_args(c);
   T.x = M<double>(c, MIBM_M_XYZV); T.vof = M<int>(c, MIBM_M_VERT_OF_FACE); T.ghost = M<int>(c, MIBM_M_GHOST_FACE);
   T.bar = M<double>(c, MIBM_M_TRI_BAR); T.nor = M<double>(c, MIBM_M_TRI_NOR);
-  sdf_reset_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, s->sdf_bits, s->winner);
+  { MIBM_PROF(c, "sdf_reset"); sdf_reset_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, s->sdf_bits, s->winner); }
   size_t nthr = (size_t)c->maxnf * 125;
   for (int pass = 0; pass < 3; ++pass)
-    band_kernel<<<div_up(nthr, 128), 128, 0, c->stream>>>(T, pass, s->sdf_bits, s->winner, c->df[MIBM_F_VOFP]);
-  sdf_finish_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, s->sdf_bits, c->df[MIBM_F_SDF]);
+    { MIBM_PROF(c, "band"); band_kernel<<<div_up(nthr, 128), 128, 0, c->stream>>>(T, pass, s->sdf_bits, s->winner, c->df[MIBM_F_VOFP]); }
+  { MIBM_PROF(c, "sdf_finish"); sdf_finish_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, s->sdf_bits, c->df[MIBM_F_SDF]); }
   c->launches += 5;
   k_interp_vof(c);
   MIBM_LAUNCH_CHECK(c, "narrowBandTagging");
@@ -1179,7 +1179,7 @@ void lagr_tag_initial(Ctx* c) {
   }
   double* tmp = nullptr;
   if (!cuda_ok(c, cudaMalloc(&tmp, sizeof(double) * std::max<size_t>(1, ncell)), "initial tag")) return;
-  sdf_reset_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, s->sdf_bits, s->winner);
+  { MIBM_PROF(c, "sdf_reset"); sdf_reset_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, s->sdf_bits, s->winner); }
   initial_tag_kernel<<<div_up(ncell, 128), 128, 0, c->stream>>>(T, b0[0], b0[1], b0[2], nb[0], nb[1], nb[2], tmp);
   for (int pass = 0; pass < 2; ++pass)
     initial_claim_kernel<<<div_up(ncell, 256), 256, 0, c->stream>>>(c->g, b0[0], b0[1], b0[2], nb[0], nb[1], nb[2], tmp,

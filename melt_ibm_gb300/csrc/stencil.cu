@@ -389,77 +389,77 @@ static double* ru_of(Ctx* c, int which) {
 }
 
 void k_hdnl(Ctx* c, int which, const StepParams* dp) {
-  hdnl_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), which, dp, hdnl_out(c, which));
+  { MIBM_PROF(c, "hdnl"); hdnl_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), which, dp, hdnl_out(c, which)); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "hdnl");
 }
 
 void k_invtr_rhs(Ctx* c, int which, const StepParams* dp, double* rhs_out) {
-  invtr_rhs_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), which, dp, hdnl_out(c, which),
-                                                                   ru_of(c, which), rhs_out);
+  { MIBM_PROF(c, "invtr_rhs"); invtr_rhs_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), which, dp, hdnl_out(c, which),
+                                                                   ru_of(c, which), rhs_out); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "invtr_rhs");
 }
 
 void k_fused_rhs(Ctx* c, const StepParams* dp) {
   for (int w = 0; w < 4; ++w) {
-    fused_rhs_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), w, dp, ru_of(c, w),
-                                                                     c->rhs4 + (size_t)w * c->g.cells);
+    { MIBM_PROF(c, "fused_rhs"); fused_rhs_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), w, dp, ru_of(c, w),
+                                                                     c->rhs4 + (size_t)w * c->g.cells); }
     ++c->launches;
   }
   MIBM_LAUNCH_CHECK(c, "fused_rhs");
 }
 
 void k_divg(Ctx* c, const StepParams* dp) {
-  divg_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, c->df[MIBM_F_DPH]);
+  { MIBM_PROF(c, "divg"); divg_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, c->df[MIBM_F_DPH]); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "divg");
 }
 
 void k_updvp(Ctx* c, const StepParams* dp) {
-  updvp_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, c->df[MIBM_F_DPH], c->df[MIBM_F_VX],
-                                                               c->df[MIBM_F_VY], c->df[MIBM_F_VZ]);
+  { MIBM_PROF(c, "updvp"); updvp_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, c->df[MIBM_F_DPH], c->df[MIBM_F_VX],
+                                                               c->df[MIBM_F_VY], c->df[MIBM_F_VZ]); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "updvp");
 }
 
 void k_prcalc(Ctx* c, const StepParams* dp) {
-  prcalc_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, c->df[MIBM_F_DPH], c->df[MIBM_F_PR]);
+  { MIBM_PROF(c, "prcalc"); prcalc_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, c->df[MIBM_F_DPH], c->df[MIBM_F_PR]); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "prcalc");
 }
 
 void k_add_field(Ctx* c, double* q, const double* r) {
-  add_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, q, r);
+  { MIBM_PROF(c, "add"); add_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, q, r); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "add");
 }
 
 void k_interp_vof(Ctx* c) {
-  interp_vof_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), c->df[MIBM_F_VOFX],
-                                                                    c->df[MIBM_F_VOFY], c->df[MIBM_F_VOFZ]);
+  { MIBM_PROF(c, "interp_vof"); interp_vof_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), c->df[MIBM_F_VOFX],
+                                                                    c->df[MIBM_F_VOFY], c->df[MIBM_F_VOFZ]); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "interp_vof");
 }
 
 void k_velforce_apply(Ctx* c, const double* mean3) {
-  velforce_apply_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(
+  { MIBM_PROF(c, "velforce_apply"); velforce_apply_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(
       c->g, mean3, c->df[MIBM_F_FORXC], c->df[MIBM_F_FORYC], c->df[MIBM_F_FORZC], c->df[MIBM_F_VX], c->df[MIBM_F_VY],
-      c->df[MIBM_F_VZ]);
+      c->df[MIBM_F_VZ]); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "velforce");
 }
 
 void k_tempforce_apply(Ctx* c) {
-  tempforce_apply_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, c->df[MIBM_F_FORTEMP],
-                                                                          c->df[MIBM_F_TEMP]);
+  { MIBM_PROF(c, "tempforce_apply"); tempforce_apply_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, c->df[MIBM_F_FORTEMP],
+                                                                          c->df[MIBM_F_TEMP]); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "tempforce");
 }
 
 double k_cfl(Ctx* c) {
   dim3 grid(1, c->g.n2m, c->g.n3m);
-  cfl_kernel<<<grid, 128, 0, c->stream>>>(make_args(c), c->pad_vx, c->pad_vy, c->red + kRedPart);
+  { MIBM_PROF(c, "cfl"); cfl_kernel<<<grid, 128, 0, c->stream>>>(make_args(c), c->pad_vx, c->pad_vy, c->red + kRedPart); }
   max_reduce_kernel<<<1, 1024, 0, c->stream>>>(c->red + kRedPart, (size_t)c->g.n2m * c->g.n3m, c->red + kRedOut);
   c->launches += 2;
   cudaMemcpyAsync(c->red_host, c->red + kRedOut, 8, cudaMemcpyDeviceToHost, c->stream);
@@ -470,7 +470,7 @@ double k_cfl(Ctx* c) {
 
 double k_get_dt_buffer(Ctx* c, double dt, double ren) {
   dim3 grid(1, c->g.n2m, c->g.n3m);
-  getdt_kernel<<<grid, 128, 0, c->stream>>>(make_args(c), dt, c->red + kRedPart);
+  { MIBM_PROF(c, "getdt"); getdt_kernel<<<grid, 128, 0, c->stream>>>(make_args(c), dt, c->red + kRedPart); }
   max_reduce_kernel<<<1, 1024, 0, c->stream>>>(c->red + kRedPart, (size_t)c->g.n2m * c->g.n3m, c->red + kRedOut);
   c->launches += 2;
   cudaMemcpyAsync(c->red_host, c->red + kRedOut, 8, cudaMemcpyDeviceToHost, c->stream);

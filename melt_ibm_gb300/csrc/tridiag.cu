@@ -227,7 +227,7 @@ void k_solve_x(Ctx* c, double* rhs, double betadx) {
   size_t sm = (size_t)kLines * (c->g.n1m + 1) * sizeof(double);
   if (!smem_ok(c, (const void*)solve_x_kernel, sm)) return;
   dim3 grid(div_up(c->g.n2m, kLines), c->g.n3m);
-  solve_x_kernel<<<grid, 128, sm, c->stream>>>(c->g, rhs, T);
+  { MIBM_PROF(c, "solve_x"); solve_x_kernel<<<grid, 128, sm, c->stream>>>(c->g, rhs, T); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "solve_x");
 }
@@ -238,7 +238,7 @@ void k_solve_y(Ctx* c, double* rhs, double betadx) {
   size_t sm = (size_t)kLines * c->g.n2m * sizeof(double);
   if (!smem_ok(c, (const void*)solve_y_kernel, sm)) return;
   dim3 grid(div_up(c->g.n1m, kLines), c->g.n3m);
-  solve_y_kernel<<<grid, 128, sm, c->stream>>>(c->g, rhs, T);
+  { MIBM_PROF(c, "solve_y"); solve_y_kernel<<<grid, 128, sm, c->stream>>>(c->g, rhs, T); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "solve_y");
 }
@@ -249,7 +249,7 @@ void k_solve_z(Ctx* c, double* rhs, double betadx, double* q) {
   size_t sm = (size_t)kLines * c->g.n3m * sizeof(double);
   if (!smem_ok(c, (const void*)solve_z_kernel, sm)) return;
   dim3 grid(div_up(c->g.n1m, kLines), c->g.n2m);
-  solve_z_kernel<<<grid, 128, sm, c->stream>>>(c->g, rhs, T, q, 1);
+  { MIBM_PROF(c, "solve_z"); solve_z_kernel<<<grid, 128, sm, c->stream>>>(c->g, rhs, T, q, 1); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "solve_z");
 }

@@ -28,6 +28,7 @@
 // Single rank: kstart = 1, kend = n3m.  MPI halo exchanges reduce to the
 // periodic self-exchange of mpi_routines.f90:139-210 and the ghost folds of
 // mpi_routines.f90:274-362; Allreduce of one rank is the identity.
+#include <chrono>
 #include <cmath>
 #include <complex>
 #include <cstdint>
@@ -1619,6 +1620,16 @@ int mibm_context_destroy_(const int* id) {
   return MIBM_OK;
 }
 int mibm_device_count_(void) { return 0; }
+int mibm_select_device_(const int*) { return MIBM_OK; }
+static double g_marks[64];
+void mibm_timer_mark_(const int* slot) {
+  if (*slot >= 0 && *slot < 64)
+    g_marks[*slot] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+double mibm_timer_ms_(const int* a, const int* b) { return g_marks[*b] - g_marks[*a]; }
+void mibm_profile_(const int*) {}
+int mibm_profile_count_(void) { return 0; }
+int mibm_profile_get_(const int*, char*, const int*, double*, long long*) { return MIBM_EINVAL; }
 unsigned long long mibm_launch_count_(void) { return 0; }
 int mibm_last_status_(void) { return t_cur ? t_cur->status : t_status; }
 const char* mibm_last_message(void) { return t_cur ? t_cur->msg.c_str() : t_msg.c_str(); }
