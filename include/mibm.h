@@ -205,6 +205,28 @@ void interp_(double* arrold, double* arrnew, const int* n1o, const int* n2o,
 /* narrow band, tagCells.f90:17-23 with initial_tag = .true.).            */
 void tagcells_initial_(void);
 
+/* ------------------------------------------------------------------ */
+/* Allocation-free x-line solve.  No counterpart in the reference: it is  */
+/* for callers whose device memory belongs to someone else -- a CUDA      */
+/* Fortran or OpenACC host that passes its own device arrays, or a        */
+/* process that has handed all free HBM to a case pool -- and that cannot */
+/* let a library call cudaMalloc (it would exceed their budget or fail).  */
+/* It runs the same periodic tridiagonal solve as solxi_ in place on       */
+/* `rhs`, a device array in the compact layout x fastest with row pitch    */
+/* `pitch` (elements), n2m rows and n3m planes, on `stream` (NULL = the   */
+/* legacy default stream).  Its only scratch, the line-factor table, is a  */
+/* file-scope device array sized for lines up to 512 cells (16.4 KB, held */
+/* by every GPU that loads the library until exit); n1m > 512 returns      */
+/* MIBM_EINVAL without launching.  The first call on a device looks up     */
+/* that array's device address (once per device, with the device          */
+/* current): make that first call before any stream capture.  All calls    */
+/* share the one table, rewritten in full by every call before it is read; */
+/* calls that overlap on the GPU race on it.  Nothing is allocated: no     */
+/* cudaMalloc, cudaFree or allocating library routine.  Returns a status.  */
+/* ------------------------------------------------------------------ */
+int mibm_solxi_noalloc(double* rhs, int n1m, int n2m, int n3m, int pitch, double betadx,
+                       void* stream);
+
 #ifdef __cplusplus
 }
 #endif

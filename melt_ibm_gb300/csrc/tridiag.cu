@@ -21,6 +21,7 @@
 // k-plane, row pitch n+1 in shared memory), y- and z-lines are columns
 // (tile = 32 adjacent i).  One thread runs one line's recurrences.
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -254,4 +255,87 @@ void k_solve_z(Ctx* c, double* rhs, double betadx, double* q) {
   MIBM_LAUNCH_CHECK(c, "solve_z");
 }
 
+// ---------------------------------------------------------------------
+// Allocation-free x-line solve (mibm_solxi_noalloc, see include/mibm.h).
+//
+// Same kernel and same factor table as solxi_, but the table lives in a
+// file-scope device array instead of memory the library allocates.  Every
+// GPU that loads the library holds this array until the process exits.
+// ---------------------------------------------------------------------
+constexpr int kNoAllocMaxN = 512;                      // longest x-line
+constexpr int kNoAllocTable = 4 * kNoAllocMaxN + 4;    // [a|b|q|s]*n + 4 scalars
+static __device__ __align__(256) double g_noalloc_table[kNoAllocTable];
+
+// Host-side stand-in of g_noalloc_table is not a device address: the device
+// address is looked up once per device with that device current.
+static std::mutex g_noalloc_mu;
+static double* g_noalloc_addr[64] = {nullptr};
+
+static cudaError_t noalloc_table_address(int dev, double** out) {
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (!g_noalloc_addr[dev]) {
+    double* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress((void**)&p, g_noalloc_table);
+    if (e != cudaSuccess) return e;
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return cudaSuccess;
+}
+
 }  // namespace mibm
+
+extern "C" int mibm_solxi_noalloc(double* rhs, int n1m, int n2m, int n3m, int pitch, double betadx,
+                                  void* stream) {
+  using namespace mibm;
+  if (!rhs || n1m < 2 || n2m < 1 || n3m < 1 || pitch < n1m) return MIBM_EINVAL;
+  if (n1m > kNoAllocMaxN) return MIBM_EINVAL;      // table would not fit the static scratch
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return MIBM_ECUDA;
+  double* table = nullptr;
+  if (noalloc_table_address(dev, &table) != cudaSuccess) return MIBM_ECUDA;
+  // line-independent factors, evaluated on the host into a fixed per-thread
+  // buffer (no heap), then copied in stream order ahead of the solve
+  static thread_local double host[kNoAllocTable];
+  {
+    int n = n1m;
+    double ackl_b = 1.0 / (1.0 + 2.0 * betadx);
+    double api = -betadx * ackl_b, ami = -betadx * ackl_b, aci = 1.0;
+    double* a = host; double* b = host + n; double* q = host + 2 * n; double* s = host + 3 * n;
+    // q, s and the pivots p of tridiag_periodic.f90:22-45 (0-based)
+    q[0] = -api / aci;
+    s[0] = -ami / aci;
+    a[0] = ackl_b / aci;
+    b[0] = 0.0;
+    for (int i = 1; i < n; ++i) {
+      double p = 1.0 / (aci + ami * q[i - 1]);
+      q[i] = -api * p;
+      s[i] = -ami * s[i - 1] * p;
+      a[i] = ackl_b * p;
+      b[i] = ami * p;
+    }
+    s[n - 1] = 1.0;
+    for (int i = n - 2; i >= 0; --i) s[i] = s[i] + q[i] * s[i + 1];
+    double den = api * s[0] + ami * s[n - 2] + aci;
+    host[4 * n + 0] = ackl_b;
+    host[4 * n + 1] = api;
+    host[4 * n + 2] = ami;
+    host[4 * n + 3] = 1.0 / den;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = cudaMemcpyAsync(table, host, sizeof(double) * (4 * (size_t)n1m + 4), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return MIBM_ECUDA;
+  Grid g{};
+  g.n1m = n1m; g.n2m = n2m; g.n3m = n3m; g.P = pitch;
+  g.plane = (size_t)pitch * n2m; g.cells = g.plane * n3m;
+  size_t sm = (size_t)kLines * (n1m + 1) * sizeof(double);
+  if (sm > 48 * 1024 &&
+      cudaFuncSetAttribute((const void*)solve_x_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
+          cudaSuccess)
+    return MIBM_ECUDA;
+  dim3 grid(div_up(n2m, kLines), n3m);
+  solve_x_kernel<<<grid, 128, sm, st>>>(g, rhs, table);
+  return cudaGetLastError() == cudaSuccess ? MIBM_OK : MIBM_ECUDA;
+}
+

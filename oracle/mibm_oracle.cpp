@@ -1628,6 +1628,7 @@ void mibm_timer_mark_(const int* slot) {
 }
 double mibm_timer_ms_(const int* a, const int* b) { return g_marks[*b] - g_marks[*a]; }
 void mibm_profile_(const int*) {}
+int mibm_solxi_noalloc(double*, int, int, int, int, double, void*) { return MIBM_EINVAL; }
 int mibm_profile_count_(void) { return 0; }
 int mibm_profile_get_(const int*, char*, const int*, double*, long long*) { return MIBM_EINVAL; }
 unsigned long long mibm_launch_count_(void) { return 0; }
