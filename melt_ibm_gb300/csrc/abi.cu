@@ -67,6 +67,22 @@ static void tschem(Ctx* c) {
   }
   *c->hs[MIBM_S_BETA] = c->S(MIBM_S_DT) / c->S(MIBM_S_REN) * 0.5;
   static const int fid[4] = {MIBM_F_VX, MIBM_F_VY, MIBM_F_VZ, MIBM_F_TEMP};
+  // factor tables of all 18 line solves of the step (invtr*.f90 betadx)
+  double bd[3][2][3];
+  {
+    double dt = c->S(MIBM_S_DT), beta = c->S(MIBM_S_BETA), pec = c->S(MIBM_S_PEC);
+    const double dq[3] = {g.dx1q, g.dx2q, g.dx3q};
+    for (int ns = 0; ns < 3; ++ns) {
+      double al = gam[ns] + rom[ns];
+      for (int d = 0; d < 3; ++d) {
+        bd[ns][0][d] = beta * al * dq[d];
+        bd[ns][1][d] = dt / pec * 0.5 * al * dq[d];
+      }
+    }
+  }
+  int tlen = 0;
+  const double* tables = tri_step_prepare(c, bd, &tlen);
+  if (!tables) return;
   for (int ns = 0; ns < 3; ++ns) {
     *c->hs[MIBM_S_AL] = gam[ns] + rom[ns];
     *c->hs[MIBM_S_GA] = gam[ns];
@@ -74,22 +90,23 @@ static void tschem(Ctx* c) {
     const StepParams* dp = push_params(c, ns);
     if (!c->I(MIBM_I_STATIONARY) && c->I(MIBM_I_IMLSFOR) == 1) lagr_tag_narrow_band(c);
     k_fused_rhs(c, dp);
-    double al = c->S(MIBM_S_AL), dt = c->S(MIBM_S_DT), beta = c->S(MIBM_S_BETA), pec = c->S(MIBM_S_PEC);
     for (int q = 0; q < 4; ++q) {
-      double f = (q < 3) ? beta * al : dt / pec * 0.5 * al;
+      int f = (q < 3) ? 0 : 1;
+      const double* T = tables + (size_t)((ns * 2 + f) * 3) * tlen;
       double* r = c->rhs4 + (size_t)q * g.cells;
-      k_solve_x(c, r, f * g.dx1q);
-      k_solve_y(c, r, f * g.dx2q);
-      k_solve_z(c, r, f * g.dx3q, c->df[fid[q]]);
+      k_solve_x_T(c, r, T);
+      k_solve_y_T(c, r, T + tlen);
+      k_solve_z_T(c, r, T + 2 * tlen, c->df[fid[q]], 0);
     }
-    lagr_particle(c, dp);
+    const double* mean3 = lagr_particle_fused(c, dp);
     if (c->status != MIBM_OK) return;
     k_divg(c, dp);
     k_phcalc(c);
-    k_updvp(c, dp);
+    k_updvp(c, dp, mean3);
     k_prcalc(c, dp);
     if (c->status != MIBM_OK) return;
   }
+  lagr_step_finish(c);
 }
 
 }  // namespace mibm

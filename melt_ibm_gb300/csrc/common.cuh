@@ -80,19 +80,6 @@ struct Ctx {
   double* red_host = nullptr;             // pinned
   int* dflag = nullptr;                   // device error flags
   int* hflag = nullptr;                   // pinned copy
-  // Lagrangian scatter plan (sorted cell keys), see lagr.cu
-  struct Plan {
-    int n = 0, cap = 0;                   // entries (27 per triangle)
-    int nseg = 0;
-    int* key = nullptr;                   // sorted cell index
-    int* src = nullptr;                   // triangle*27 + slot
-    int* seg_start = nullptr;             // start offset of each unique key
-    int* seg_key = nullptr;
-    int* tmp_key = nullptr; int* tmp_src = nullptr;
-    int* hist = nullptr;
-    int* nseg_dev = nullptr;
-    bool valid = false;
-  } plan[4];
   double* tri_coef = nullptr;             // per triangle & component: cfac*(target-Um)
   double* lag_red = nullptr;              // per-triangle partial sums
   cudaStream_t stream = nullptr;
@@ -183,7 +170,7 @@ void k_hdnl(Ctx* c, int which, const StepParams* dp);
 void k_invtr_rhs(Ctx* c, int which, const StepParams* dp, double* rhs_out);
 void k_fused_rhs(Ctx* c, const StepParams* dp);
 void k_divg(Ctx* c, const StepParams* dp);
-void k_updvp(Ctx* c, const StepParams* dp);
+void k_updvp(Ctx* c, const StepParams* dp, const double* mean3 = nullptr);
 void k_prcalc(Ctx* c, const StepParams* dp);
 void k_add_field(Ctx* c, double* q, const double* r);
 double k_cfl(Ctx* c);
@@ -195,6 +182,10 @@ void k_tempforce_apply(Ctx* c);
 void k_solve_x(Ctx* c, double* rhs, double betadx);
 void k_solve_y(Ctx* c, double* rhs, double betadx);
 void k_solve_z(Ctx* c, double* rhs, double betadx, double* q);
+void k_solve_x_T(Ctx* c, double* rhs, const double* T);
+void k_solve_y_T(Ctx* c, double* rhs, const double* T);
+void k_solve_z_T(Ctx* c, double* rhs, const double* T, double* q, int write_rhs);
+const double* tri_step_prepare(Ctx* c, const double betadx[3][2][3], int* len_out);
 // fft.cu
 void k_phcalc(Ctx* c);
 // lagr.cu
@@ -210,6 +201,10 @@ void lagr_geometry_refresh(Ctx* c, bool imelt);
 void lagr_tag_narrow_band(Ctx* c);
 void lagr_tag_initial(Ctx* c);
 void lagr_particle(Ctx* c, const StepParams* dp);
+const double* lagr_particle_fused(Ctx* c, const StepParams* dp);
+void lagr_step_finish(Ctx* c);
+void lagr_geometry_to_host(Ctx* c);
+void lagr_invalidate(Ctx* c);
 void lagr_free(Ctx* c);
 // ctx.cu
 bool ensure_params(Ctx* c);

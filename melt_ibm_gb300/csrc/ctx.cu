@@ -391,8 +391,8 @@ void mibm_sync_from_host_(const long long* mask) {
   for (int i = 0; i < MIBM_NMESH && c->maxnf > 0; ++i)
     if ((m >> 32) & (1ull << i))
       cuda_ok(c, cudaMemcpyAsync(c->dm[i], c->hm[i], mesh_bytes(c, i), cudaMemcpyHostToDevice, c->stream), "H2D mesh");
-  // the scatter plans depend on the mesh
-  for (int q = 0; q < 4; ++q) c->plan[q].valid = false;
+  // the scatter plan and the MLS weights depend on the mesh
+  if ((m >> 32) != 0) lagr_invalidate(c);
   cuda_ok(c, cudaStreamSynchronize(c->stream), "sync_from_host");
   if (c->maxnf > 0 && ((m >> 32) & ((1ull << MIBM_M_VERT_OF_FACE) | (1ull << MIBM_M_GHOST_FACE)))) validate_mesh(c);
 }

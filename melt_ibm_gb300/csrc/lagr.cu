@@ -173,6 +173,8 @@ __device__ __forceinline__ CageSpec cage_spec(int comp) {
   return CageSpec{0, 1, 1, 1, 1, false};             // xm, ym, zm ; pind(1), pind(2)
 }
 
+// One thread per (triangle, component): the serial order of the reference,
+// and the fewest FP64 operations (the part's scarce resource).
 __global__ void mls_weight_kernel(LagArgs A, const double* __restrict__ tri_bar, const int* __restrict__ ghost,
                                   const int* __restrict__ pind, double* __restrict__ p1, double* __restrict__ p2,
                                   double* __restrict__ p3, double* __restrict__ pt, int* __restrict__ flag) {
@@ -282,19 +284,49 @@ __global__ void force_coef_kernel(Grid g, int nf, ForceArgs F, double tmelt, dou
 // ---------------------------------------------------------------------
 constexpr int kSortChunk = 4096;
 
-__global__ void plan_keys_kernel(Grid g, int nf, int comp, const int* __restrict__ pind, const int* __restrict__ ghost,
-                                 int* __restrict__ key, int* __restrict__ src) {
+// The four cage sets (x, y, z staggered, cell-centred) are merged into one
+// plan: entry e = comp*27*nf + 27*t + slot, key = comp*cells + cage cell
+// (4*cells, after every cell, for ghost faces).  The plan depends only on the cage centres
+// (pind) and the ghost flags; `plan_check` compares them with the values the
+// plan was built from and every kernel of the rebuild returns at once when
+// nothing changed, so a rebuild costs nothing on a stationary cage.
+__global__ void plan_check_kernel(int nf, const int* __restrict__ pind, const int* __restrict__ ghost,
+                                  const int* __restrict__ saved, int* __restrict__ dirty) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nf) return;
+  const int* sv = saved + 7 * (size_t)t;
+  bool diff = (sv[6] != ghost[t]);
+  if (!ghost[t])
+    for (int q = 0; q < 6; ++q) diff = diff || (sv[q] != pind[6 * t + q]);
+  if (diff) atomicOr(dirty, 1);
+}
+
+__global__ void plan_commit_kernel(int nf, const int* __restrict__ pind, const int* __restrict__ ghost,
+                                   int* __restrict__ saved, const int* __restrict__ dirty) {
+  if (!*dirty) return;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nf) return;
+  for (int q = 0; q < 6; ++q) saved[7 * (size_t)t + q] = pind[6 * t + q];
+  saved[7 * (size_t)t + 6] = ghost[t];
+}
+
+__global__ void plan_keys_kernel(Grid g, int nf, const int* __restrict__ pind, const int* __restrict__ ghost,
+                                 const int* __restrict__ dirty, int* __restrict__ key, int* __restrict__ src) {
+  if (!*dirty) return;
   int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= 27 * nf) return;
-  int t = e / 27, s = e % 27;
-  if (ghost[t]) { key[e] = INT_MAX; src[e] = e; return; }
+  int per = 27 * nf;
+  if (e >= 4 * per) return;
+  int comp = e / per, r = e % per, t = r / 27, sl = r % 27;
+  if (ghost[t]) { key[e] = (int)(4 * g.cells); src[e] = e; return; }   // sorts after every cell
   int i0, j0, k0;
   cage_center(comp, pind + 6 * t, i0, j0, k0);
-  key[e] = (int)cage_cell(g, i0, j0, k0, s);
+  key[e] = (int)((size_t)comp * g.cells + cage_cell(g, i0, j0, k0, sl));
   src[e] = e;
 }
 
-__global__ void radix_hist_kernel(const int* __restrict__ key, int n, int shift, int nblk, int* __restrict__ hist) {
+__global__ void radix_hist_kernel(const int* __restrict__ key, int n, int shift, int nblk,
+                                  const int* __restrict__ dirty, int* __restrict__ hist) {
+  if (!*dirty) return;
   __shared__ int h[256];
   for (int d = threadIdx.x; d < 256; d += blockDim.x) h[d] = 0;
   __syncthreads();
@@ -305,27 +337,48 @@ __global__ void radix_hist_kernel(const int* __restrict__ key, int n, int shift,
   for (int d = threadIdx.x; d < 256; d += blockDim.x) hist[d * nblk + b] = h[d];
 }
 
-// exclusive scan of m ints by one block of 1024 threads
-__global__ void scan_kernel(int* __restrict__ a, int m) {
-  __shared__ int part[1024];
-  int per = (m + blockDim.x - 1) / blockDim.x;
-  int lo = threadIdx.x * per, hi = min(m, lo + per);
-  int s = 0;
-  for (int q = lo; q < hi; ++q) s += a[q];
-  part[threadIdx.x] = s;
+// exclusive scan of m ints by one block of 1024 threads: coalesced tiles
+// of 1024, warp-shuffle scans inside a tile, a running carry across tiles
+__global__ void scan_kernel(int* __restrict__ a, int m, const int* __restrict__ dirty) {
+  if (!*dirty) return;
+  __shared__ int wsum[32];
+  __shared__ int carry;
+  const unsigned FULL = 0xffffffffu;
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (threadIdx.x == 0) carry = 0;
   __syncthreads();
-  for (int off = 1; off < blockDim.x; off <<= 1) {
-    int v = (threadIdx.x >= off) ? part[threadIdx.x - off] : 0;
+  for (int base = 0; base < m; base += blockDim.x) {
+    int idx = base + threadIdx.x;
+    int v = (idx < m) ? a[idx] : 0;
+    int x = v;
+    for (int off = 1; off < 32; off <<= 1) {
+      int u = __shfl_up_sync(FULL, x, off);
+      if (lane >= off) x += u;
+    }
+    if (lane == 31) wsum[w] = x;
     __syncthreads();
-    part[threadIdx.x] += v;
+    if (w == 0) {
+      int y = wsum[lane];
+      for (int off = 1; off < 32; off <<= 1) {
+        int u = __shfl_up_sync(FULL, y, off);
+        if (lane >= off) y += u;
+      }
+      wsum[lane] = y;                       // inclusive warp totals
+    }
+    __syncthreads();
+    int incl = x + (w > 0 ? wsum[w - 1] : 0);
+    if (idx < m) a[idx] = carry + incl - v;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry += incl;
     __syncthreads();
   }
-  int run = (threadIdx.x == 0) ? 0 : part[threadIdx.x - 1];
-  for (int q = lo; q < hi; ++q) { int v = a[q]; a[q] = run; run += v; }
 }
 
+// stable scatter: chunk order, then warp order, then lane order
 __global__ void radix_scatter_kernel(const int* __restrict__ kin, const int* __restrict__ vin, int* __restrict__ kout,
-                                     int* __restrict__ vout, int n, int shift, int nblk, const int* __restrict__ offs) {
+                                     int* __restrict__ vout, int n, int shift, int nblk, const int* __restrict__ offs,
+                                     const int* __restrict__ dirty) {
+  if (!*dirty) return;
   __shared__ int base[256];
   __shared__ int wcnt[8][256];
   int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -361,62 +414,78 @@ __global__ void radix_scatter_kernel(const int* __restrict__ kin, const int* __r
   }
 }
 
-static bool plan_alloc(Ctx* c, Ctx::Plan& p, int n) {
-  if (p.cap >= n) return true;
-  cudaFree(p.key); cudaFree(p.src); cudaFree(p.tmp_key); cudaFree(p.tmp_src); cudaFree(p.hist);
-  int nblk = (n + kSortChunk - 1) / kSortChunk;
-  bool ok = cuda_ok(c, cudaMalloc(&p.key, sizeof(int) * n), "plan") && cuda_ok(c, cudaMalloc(&p.src, sizeof(int) * n), "plan") &&
-            cuda_ok(c, cudaMalloc(&p.tmp_key, sizeof(int) * n), "plan") &&
-            cuda_ok(c, cudaMalloc(&p.tmp_src, sizeof(int) * n), "plan") &&
-            cuda_ok(c, cudaMalloc(&p.hist, sizeof(int) * 256 * (size_t)nblk), "plan");
-  if (ok) p.cap = n;
-  return ok;
+// Heads of the runs of equal keys (one cell of one component) sum their run
+// in triangle order and add the sum to that component's target field; with
+// `segval` the head also records the sum (for the mean force).
+struct ScatterOut {
+  double* f[4];
+  const double* phi[4];
+};
+
+__device__ __forceinline__ int key_comp(int k, size_t cells) {
+  size_t u = (size_t)k;
+  return (u >= cells) + (u >= 2 * cells) + (u >= 3 * cells) + (u >= 4 * cells);   // 4 = ghost face
 }
 
-// Build the sorted scatter plan of one component: keys = cage cell indices.
-static void build_plan(Ctx* c, int comp) {
-  Ctx::Plan& p = c->plan[comp];
-  int nf = c->maxnf, n = 27 * nf;
-  if (n == 0) { p.n = 0; p.valid = true; return; }
-  if (!plan_alloc(c, p, n)) return;
-  p.n = n;
-  { MIBM_PROF(c, "plan_keys"); plan_keys_kernel<<<div_up(n, 256), 256, 0, c->stream>>>(c->g, nf, comp, M<int>(c, MIBM_M_PIND),
-                                                          M<int>(c, MIBM_M_GHOST_FACE), p.tmp_key, p.tmp_src); }
-  ++c->launches;
-  int nblk = (n + kSortChunk - 1) / kSortChunk;
-  // cell keys < cells (< 2^31); INT_MAX marks ghost faces
-  int bits = 31;
-  int* kin = p.tmp_key; int* vin = p.tmp_src; int* kout = p.key; int* vout = p.src;
-  int passes = (bits + 7) / 8;
-  for (int ps = 0; ps < passes; ++ps) {
-    int shift = 8 * ps;
-    { MIBM_PROF(c, "radix_hist"); radix_hist_kernel<<<nblk, 256, 0, c->stream>>>(kin, n, shift, nblk, p.hist); }
-    scan_kernel<<<1, 1024, 0, c->stream>>>(p.hist, 256 * nblk);
-    { MIBM_PROF(c, "radix_scatter"); radix_scatter_kernel<<<nblk, 256, 0, c->stream>>>(kin, vin, kout, vout, n, shift, nblk, p.hist); }
-    c->launches += 3;
-    std::swap(kin, kout); std::swap(vin, vout);
-  }
-  // after an even number of passes the result is in tmp_*; make key/src hold it
-  if (kin != p.key) { std::swap(p.key, p.tmp_key); std::swap(p.src, p.tmp_src); }
-  p.valid = MIBM_LAUNCH_CHECK(c, "build_plan");
-}
-
-// Segment heads of the sorted keys sum their run in order and add the sum
-// to the dense force field (each cell written by exactly one thread).
-__global__ void scatter_apply_kernel(int n, const int* __restrict__ key, const int* __restrict__ src,
-                                     const double* __restrict__ coef, const double* __restrict__ phi,
-                                     double* __restrict__ out) {
+__global__ void scatter_apply_kernel(int n, int nf, size_t cells, const int* __restrict__ key,
+                                     const int* __restrict__ src, const double* __restrict__ coef, ScatterOut O,
+                                     int comp_lo, int comp_hi, double* __restrict__ segval) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n) return;
   int k = key[e];
-  if (k == INT_MAX || (e > 0 && key[e - 1] == k)) return;
-  double s = 0.0;
-  for (int q = e; q < n && key[q] == k; ++q) {
-    int sr = src[q];
-    int t = sr / 27;
-    s = s + coef[t] * phi[sr];
+  int comp = key_comp(k, cells);
+  bool head = (comp < 4) && (e == 0 || key[e - 1] != k);
+  if (!head || comp < comp_lo || comp >= comp_hi) {
+    if (segval && comp >= comp_lo && comp < comp_hi) segval[e] = 0.0;
+    return;
   }
-  out[k] = out[k] + s;
+  size_t cell = (size_t)k - (size_t)comp * cells;
+  int per = 27 * nf;
+  double sum = 0.0;
+  for (int q = e; q < n && key[q] == k; ++q) {
+    int sr = src[q] - comp * per;
+    int t = sr / 27;
+    sum = sum + coef[(size_t)comp * nf + t] * O.phi[comp][sr];
+  }
+  O.f[comp][cell] = O.f[comp][cell] + sum;
+  if (segval) segval[e] = sum;
+}
+
+// fixed-order sum of the recorded run sums per velocity component: 256
+// blocks over contiguous ranges, then one block over the 256 partials
+constexpr int kMeanBlocks = 256;
+__global__ void seg_partial_kernel(int n, size_t cells, const int* __restrict__ key, const double* __restrict__ segval,
+                                   double* __restrict__ part) {
+  __shared__ double sm[3][256];
+  int per = (n + gridDim.x - 1) / gridDim.x;
+  int lo = blockIdx.x * per, hi = min(n, lo + per);
+  double s[3] = {0, 0, 0};
+  for (int e = lo + threadIdx.x; e < hi; e += blockDim.x) {
+    int comp = key_comp(key[e], cells);
+    if (comp < 3) s[comp] += segval[e];
+  }
+  for (int q = 0; q < 3; ++q) sm[q][threadIdx.x] = s[q];
+  __syncthreads();
+  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off)
+      for (int q = 0; q < 3; ++q) sm[q][threadIdx.x] += sm[q][threadIdx.x + off];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int q = 0; q < 3; ++q) part[3 * blockIdx.x + q] = sm[q][0];
+}
+
+__global__ void seg_final_kernel(const double* __restrict__ part, double ncell, double* __restrict__ mean3) {
+  __shared__ double sm[3][kMeanBlocks];
+  for (int q = 0; q < 3; ++q) sm[q][threadIdx.x] = part[3 * threadIdx.x + q];
+  __syncthreads();
+  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off)
+      for (int q = 0; q < 3; ++q) sm[q][threadIdx.x] += sm[q][threadIdx.x + off];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int q = 0; q < 3; ++q) mean3[q] = sm[q][0] / ncell;
 }
 
 // ---------------------------------------------------------------------
@@ -780,10 +849,11 @@ __global__ void sdf_reset_kernel(Grid g, unsigned long long* __restrict__ sdf_bi
   winner[t] = INT_MAX;
 }
 
-// one thread per (triangle, band cell); pass 0: min distance, pass 1: the
-// earliest triangle at that distance, pass 2: the winner writes sdf and VOF
+// one thread per (triangle, band cell); pass 0: distance (stored) and the
+// minimum per cell, pass 1: the earliest triangle at that distance, pass 2:
+// the winner writes the signed distance and the VOF
 __global__ void band_kernel(TagArgs T, int pass, unsigned long long* __restrict__ sdf_bits, int* __restrict__ winner,
-                            double* __restrict__ vofp) {
+                            double* __restrict__ vofp, double* __restrict__ dist_buf) {
   long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   int f = (int)(gid / 125), q = (int)(gid % 125);
   const LagArgs& A = T.L;
@@ -792,30 +862,36 @@ __global__ void band_kernel(TagArgs T, int pass, unsigned long long* __restrict_
   double pos[3] = {T.bar[3 * f], T.bar[3 * f + 1], T.bar[3 * f + 2]};
   int i = ffloor(pos[0] * g.dx1) + 1, j = ffloor(pos[1] * g.dx2) + 1, k = ffloor(pos[2] * g.dx3) + 1;
   int ii = i - 2 + q % 5, jj = j - 2 + (q / 5) % 5, kk = k - 2 + q / 25;
-  double P[3] = {coord(A, 0, 1, ii), coord(A, 1, 1, jj), coord(A, 2, 1, kk)};
-  double V0[3], V1[3], V2[3];
-  tri_verts(T, f, V0, V1, V2);
-  double dist = point_tri_dist(P, V0, V1, V2);
   int im = fmod_pos(ii - 1, g.n1m), jm = fmod_pos(jj - 1, g.n1m), km = fmod_pos(kk - 1, g.n3m);
   size_t c0 = cidx(g, im, jm, km);
-  unsigned long long bits = (unsigned long long)__double_as_longlong(dist);
+  double dist;
   if (pass == 0) {
-    atomicMin(&sdf_bits[c0], bits);
-  } else if (pass == 1) {
-    if (sdf_bits[c0] == bits && dist < 999.0) atomicMin(&winner[c0], f);
-  } else {
-    if (winner[c0] != f || sdf_bits[c0] != bits) return;
-    double Q0 = pos[0] - P[0], Q1 = pos[1] - P[1], Q2 = pos[2] - P[2];
-    double dotval = T.nor[3 * f] * Q0 + T.nor[3 * f + 1] * Q1 + T.nor[3 * f + 2] * Q2;
-    double sgnd = dist * (-copysign(1.0, dotval));
-    double eps = 1.0 / g.dx1, vof;
-    const double pi = 3.141592653589793238462643;
-    if (sgnd <= -eps) vof = 0.0;
-    else if (sgnd >= eps) vof = 1.0;
-    else vof = 0.5 * (1.0 + sgnd * g.dx1 + (1.0 / pi) * sin(pi * sgnd * g.dx1));
-    vofp[c0] = vof;
-    sdf_bits[c0] = (unsigned long long)__double_as_longlong(sgnd);
+    double P[3] = {coord(A, 0, 1, ii), coord(A, 1, 1, jj), coord(A, 2, 1, kk)};
+    double V0[3], V1[3], V2[3];
+    tri_verts(T, f, V0, V1, V2);
+    dist = point_tri_dist(P, V0, V1, V2);
+    dist_buf[gid] = dist;
+    atomicMin(&sdf_bits[c0], (unsigned long long)__double_as_longlong(dist));
+    return;
   }
+  dist = dist_buf[gid];
+  unsigned long long bits = (unsigned long long)__double_as_longlong(dist);
+  if (pass == 1) {
+    if (sdf_bits[c0] == bits && dist < 999.0) atomicMin(&winner[c0], f);
+    return;
+  }
+  if (winner[c0] != f || sdf_bits[c0] != bits) return;
+  double P[3] = {coord(A, 0, 1, ii), coord(A, 1, 1, jj), coord(A, 2, 1, kk)};
+  double Q0 = pos[0] - P[0], Q1 = pos[1] - P[1], Q2 = pos[2] - P[2];
+  double dotval = T.nor[3 * f] * Q0 + T.nor[3 * f + 1] * Q1 + T.nor[3 * f + 2] * Q2;
+  double sgnd = dist * (-copysign(1.0, dotval));
+  double eps = 1.0 / g.dx1, vof;
+  const double pi = 3.141592653589793238462643;
+  if (sgnd <= -eps) vof = 0.0;
+  else if (sgnd >= eps) vof = 1.0;
+  else vof = 0.5 * (1.0 + sgnd * g.dx1 + (1.0 / pi) * sin(pi * sgnd * g.dx1));
+  vofp[c0] = vof;
+  sdf_bits[c0] = (unsigned long long)__double_as_longlong(sgnd);
 }
 
 __global__ void sdf_finish_kernel(Grid g, const unsigned long long* __restrict__ bits, double* __restrict__ sdf) {
@@ -912,7 +988,7 @@ __global__ void fill_kernel(Grid g, double* __restrict__ a, double v) {
 }
 
 // ---------------------------------------------------------------------
-// adjacency (vertex -> faces, ascending) built on the host per topology
+// per-context Lagrangian state
 // ---------------------------------------------------------------------
 struct LagState {
   Ctx* c = nullptr;
@@ -924,6 +1000,16 @@ struct LagState {
   double* mean3 = nullptr;
   unsigned long long* sdf_bits = nullptr;
   int* winner = nullptr;
+  double* dist_buf = nullptr;
+  // merged scatter plan
+  int plan_n = 0, plan_cap = 0, nblk = 0;
+  int *key = nullptr, *src = nullptr, *tmp_key = nullptr, *tmp_src = nullptr, *hist = nullptr;
+  int *res_key = nullptr, *res_src = nullptr;   // buffers holding the sorted result
+  int* saved = nullptr;                          // 7 ints per face: pind(1:6), ghost
+  int* dirty = nullptr;
+  double* segval = nullptr;
+  bool force_rebuild = true;
+  bool weights_valid = false;                    // stationary cages: weights kept
 };
 static std::vector<LagState*> g_lag;
 
@@ -934,6 +1020,12 @@ static LagState* lag_of(Ctx* c) {
   s->c = c;
   g_lag.push_back(s);
   return s;
+}
+
+void lagr_invalidate(Ctx* c) {
+  LagState* s = lag_of(c);
+  s->force_rebuild = true;
+  s->weights_valid = false;
 }
 
 static bool ensure_adjacency(Ctx* c) {
@@ -972,12 +1064,30 @@ static bool ensure_lag_buffers(Ctx* c) {
     if (!cuda_ok(c, cudaMalloc(&s->face_part, sizeof(double) * 11 * std::max(1, c->maxnf)), "lag")) return false;
     if (!cuda_ok(c, cudaMalloc(&s->geom_out, sizeof(double) * 8), "lag")) return false;
     if (!cuda_ok(c, cudaMalloc(&s->mean3, sizeof(double) * 4), "lag")) return false;
+    cudaMemsetAsync(s->mean3, 0, sizeof(double) * 4, c->stream);
   }
   if (!c->tri_coef)
     if (!cuda_ok(c, cudaMalloc(&c->tri_coef, sizeof(double) * 4 * std::max(1, c->maxnf)), "lag")) return false;
+  if (!s->key) {
+    int n = 4 * 27 * std::max(1, c->maxnf);
+    s->nblk = (n + kSortChunk - 1) / kSortChunk;
+    bool ok = cuda_ok(c, cudaMalloc(&s->key, sizeof(int) * n), "plan") &&
+              cuda_ok(c, cudaMalloc(&s->src, sizeof(int) * n), "plan") &&
+              cuda_ok(c, cudaMalloc(&s->tmp_key, sizeof(int) * n), "plan") &&
+              cuda_ok(c, cudaMalloc(&s->tmp_src, sizeof(int) * n), "plan") &&
+              cuda_ok(c, cudaMalloc(&s->hist, sizeof(int) * 256 * (size_t)s->nblk), "plan") &&
+              cuda_ok(c, cudaMalloc(&s->saved, sizeof(int) * 7 * (size_t)std::max(1, c->maxnf)), "plan") &&
+              cuda_ok(c, cudaMalloc(&s->dirty, sizeof(int)), "plan") &&
+              cuda_ok(c, cudaMalloc(&s->segval, sizeof(double) * n), "plan");
+    if (!ok) return false;
+    s->plan_n = n;
+    cudaMemsetAsync(s->saved, 0xff, sizeof(int) * 7 * (size_t)std::max(1, c->maxnf), c->stream);
+  }
   return true;
 }
 
+// Flags raised by device kernels (singular MLS matrix).  In the fused step
+// they are read once at the end of the step.
 static bool check_flag(Ctx* c, const char* what) {
   cudaMemcpyAsync(c->hflag, c->dflag, 4, cudaMemcpyDeviceToHost, c->stream);
   if (!cuda_ok(c, cudaStreamSynchronize(c->stream), what)) return false;
@@ -997,51 +1107,110 @@ bool validate_mesh(Ctx* c) {
   return ensure_adjacency(c);
 }
 
-// ---------------------------------------------------------------------
-// entry points
-// ---------------------------------------------------------------------
-void lagr_find_centroid_indices(Ctx* c) {
-  if (c->maxnf == 0) return;
-  { MIBM_PROF(c, "centroid_idx"); centroid_idx_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(
-      lag_args(c), M<double>(c, MIBM_M_TRI_BAR), M<int>(c, MIBM_M_GHOST_FACE), M<int>(c, MIBM_M_PIND)); }
-  ++c->launches;
-  for (int q = 0; q < 4; ++q) c->plan[q].valid = false;
-  MIBM_LAUNCH_CHECK(c, "findCentroidIndices");
+// (Re)build the merged scatter plan when the cage centres changed.
+static void update_plan(Ctx* c) {
+  LagState* s = lag_of(c);
+  int nf = c->maxnf, n = s->plan_n;
+  if (s->force_rebuild) {
+    int one = 1;
+    cudaMemcpyAsync(s->dirty, &one, sizeof(int), cudaMemcpyHostToDevice, c->stream);
+    s->force_rebuild = false;
+  } else {
+    cudaMemsetAsync(s->dirty, 0, sizeof(int), c->stream);
+  }
+  const int* pind = M<int>(c, MIBM_M_PIND);
+  const int* ghost = M<int>(c, MIBM_M_GHOST_FACE);
+  { MIBM_PROF(c, "plan_check");
+    plan_check_kernel<<<div_up(nf, 256), 256, 0, c->stream>>>(nf, pind, ghost, s->saved, s->dirty); }
+  { MIBM_PROF(c, "plan_keys");
+    plan_keys_kernel<<<div_up(n, 256), 256, 0, c->stream>>>(c->g, nf, pind, ghost, s->dirty, s->tmp_key, s->tmp_src); }
+  int* kin = s->tmp_key; int* vin = s->tmp_src; int* kout = s->key; int* vout = s->src;
+  int bits = 1;
+  while ((size_t(1) << bits) <= 4 * c->g.cells) ++bits;
+  int passes = (bits + 7) / 8;
+  for (int ps = 0; ps < passes; ++ps) {
+    int shift = 8 * ps;
+    { MIBM_PROF(c, "radix_hist");
+      radix_hist_kernel<<<s->nblk, 256, 0, c->stream>>>(kin, n, shift, s->nblk, s->dirty, s->hist); }
+    { MIBM_PROF(c, "radix_scan");
+      scan_kernel<<<1, 1024, 0, c->stream>>>(s->hist, 256 * s->nblk, s->dirty); }
+    { MIBM_PROF(c, "radix_scatter");
+      radix_scatter_kernel<<<s->nblk, 256, 0, c->stream>>>(kin, vin, kout, vout, n, shift, s->nblk, s->hist, s->dirty); }
+    std::swap(kin, kout); std::swap(vin, vout);
+  }
+  s->res_key = kin; s->res_src = vin;         // fixed per grid: the buffers of the last pass
+  { MIBM_PROF(c, "plan_commit");
+    plan_commit_kernel<<<div_up(nf, 256), 256, 0, c->stream>>>(nf, pind, ghost, s->saved, s->dirty); }
+  c->launches += 3 + 3 * passes;
+  MIBM_LAUNCH_CHECK(c, "scatter plan");
 }
 
-void lagr_mls_weight(Ctx* c) {
-  if (c->maxnf == 0) return;
-  { MIBM_PROF(c, "mls_weight"); mls_weight_kernel<<<div_up(4 * (size_t)c->maxnf, 128), 128, 0, c->stream>>>(
-      lag_args(c), M<double>(c, MIBM_M_TRI_BAR), M<int>(c, MIBM_M_GHOST_FACE), M<int>(c, MIBM_M_PIND),
-      M<double>(c, MIBM_M_PTXAB_Q1), M<double>(c, MIBM_M_PTXAB_Q2), M<double>(c, MIBM_M_PTXAB_Q3),
-      M<double>(c, MIBM_M_PTXAB_TEMP), c->dflag); }
-  ++c->launches;
-  if (MIBM_LAUNCH_CHECK(c, "mlsWeight")) check_flag(c, "mlsWeight");
+static ScatterOut scatter_out(Ctx* c, bool into_fields) {
+  ScatterOut O;
+  static const int fo[4] = {MIBM_F_FORXC, MIBM_F_FORYC, MIBM_F_FORZC, MIBM_F_FORTEMP};
+  static const int fq[4] = {MIBM_F_VX, MIBM_F_VY, MIBM_F_VZ, MIBM_F_TEMP};
+  for (int q = 0; q < 4; ++q) O.f[q] = c->df[into_fields ? fq[q] : fo[q]];
+  O.phi[0] = M<double>(c, MIBM_M_PTXAB_Q1); O.phi[1] = M<double>(c, MIBM_M_PTXAB_Q2);
+  O.phi[2] = M<double>(c, MIBM_M_PTXAB_Q3); O.phi[3] = M<double>(c, MIBM_M_PTXAB_TEMP);
+  return O;
 }
 
-void lagr_mls_force(Ctx* c, const StepParams* dp, bool) {
-  if (c->maxnf == 0) return;
-  if (!ensure_lag_buffers(c)) return;
+static void force_coefficients(Ctx* c) {
   ForceArgs F;
   F.q[0] = c->df[MIBM_F_VX]; F.q[1] = c->df[MIBM_F_VY]; F.q[2] = c->df[MIBM_F_VZ]; F.q[3] = c->df[MIBM_F_TEMP];
   F.ptx[0] = M<double>(c, MIBM_M_PTXAB_Q1); F.ptx[1] = M<double>(c, MIBM_M_PTXAB_Q2);
   F.ptx[2] = M<double>(c, MIBM_M_PTXAB_Q3); F.ptx[3] = M<double>(c, MIBM_M_PTXAB_TEMP);
   F.vel_tri = M<double>(c, MIBM_M_VEL_TRI); F.cfac = M<double>(c, MIBM_M_CFAC);
   F.pind = M<int>(c, MIBM_M_PIND); F.ghost = M<int>(c, MIBM_M_GHOST_FACE);
-  (void)dp;
-  { MIBM_PROF(c, "force_coef"); force_coef_kernel<<<div_up(4 * (size_t)c->maxnf, 128), 128, 0, c->stream>>>(c->g, c->maxnf, F, c->S(MIBM_S_TMELT),
-                                                                                c->tri_coef); }
+  { MIBM_PROF(c, "force_coef");
+    force_coef_kernel<<<div_up(4 * (size_t)c->maxnf, 128), 128, 0, c->stream>>>(c->g, c->maxnf, F, c->S(MIBM_S_TMELT),
+                                                                                  c->tri_coef); }
   ++c->launches;
-  static const int outf[4] = {MIBM_F_FORXC, MIBM_F_FORYC, MIBM_F_FORZC, MIBM_F_FORTEMP};
-  for (int comp = 0; comp < 4; ++comp) {
-    if (!c->plan[comp].valid) build_plan(c, comp);
-    Ctx::Plan& p = c->plan[comp];
-    if (p.n == 0) continue;
-    { MIBM_PROF(c, "scatter_apply"); scatter_apply_kernel<<<div_up(p.n, 256), 256, 0, c->stream>>>(p.n, p.key, p.src,
-                                                                   c->tri_coef + (size_t)comp * c->maxnf,
-                                                                   F.ptx[comp], c->df[outf[comp]]); }
-    ++c->launches;
-  }
+}
+
+static void scatter(Ctx* c, bool into_fields, int lo, int hi, bool record) {
+  LagState* s = lag_of(c);
+  { MIBM_PROF(c, "scatter_apply");
+    scatter_apply_kernel<<<div_up(s->plan_n, 256), 256, 0, c->stream>>>(
+        s->plan_n, c->maxnf, c->g.cells, s->res_key, s->res_src, c->tri_coef, scatter_out(c, into_fields), lo, hi,
+        record ? s->segval : nullptr); }
+  ++c->launches;
+}
+
+// ---------------------------------------------------------------------
+// entry points
+// ---------------------------------------------------------------------
+void lagr_find_centroid_indices(Ctx* c) {
+  if (c->maxnf == 0) return;
+  { MIBM_PROF(c, "centroid_idx");
+    centroid_idx_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(
+        lag_args(c), M<double>(c, MIBM_M_TRI_BAR), M<int>(c, MIBM_M_GHOST_FACE), M<int>(c, MIBM_M_PIND)); }
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "findCentroidIndices");
+}
+
+static void mls_weight_launch(Ctx* c) {
+  { MIBM_PROF(c, "mls_weight");
+    mls_weight_kernel<<<div_up(4 * (size_t)c->maxnf, 64), 64, 0, c->stream>>>(
+        lag_args(c), M<double>(c, MIBM_M_TRI_BAR), M<int>(c, MIBM_M_GHOST_FACE), M<int>(c, MIBM_M_PIND),
+        M<double>(c, MIBM_M_PTXAB_Q1), M<double>(c, MIBM_M_PTXAB_Q2), M<double>(c, MIBM_M_PTXAB_Q3),
+        M<double>(c, MIBM_M_PTXAB_TEMP), c->dflag); }
+  ++c->launches;
+}
+
+void lagr_mls_weight(Ctx* c) {
+  if (c->maxnf == 0) return;
+  mls_weight_launch(c);
+  if (MIBM_LAUNCH_CHECK(c, "mlsWeight")) check_flag(c, "mlsWeight");
+}
+
+// mlsforce_ drop-in: spreads into the dense for_* fields
+void lagr_mls_force(Ctx* c, const StepParams*, bool) {
+  if (c->maxnf == 0) return;
+  if (!ensure_lag_buffers(c)) return;
+  force_coefficients(c);
+  update_plan(c);
+  scatter(c, false, 0, 4, false);
   MIBM_LAUNCH_CHECK(c, "mlsForce");
 }
 
@@ -1049,10 +1218,12 @@ void lagr_velforce(Ctx* c) {
   if (!ensure_lag_buffers(c)) return;
   LagState* s = lag_of(c);
   dim3 grid(c->g.n2m, c->g.n3m);
-  { MIBM_PROF(c, "field_sum"); field_sum_kernel<<<grid, 128, 0, c->stream>>>(c->g, c->df[MIBM_F_FORXC], c->df[MIBM_F_FORYC], c->df[MIBM_F_FORZC],
-                                                c->red + kRedPart); }
+  { MIBM_PROF(c, "field_sum");
+    field_sum_kernel<<<grid, 128, 0, c->stream>>>(c->g, c->df[MIBM_F_FORXC], c->df[MIBM_F_FORYC],
+                                                  c->df[MIBM_F_FORZC], c->red + kRedPart); }
   double ncell = (double)c->g.n1m * (double)c->g.n2m * (double)c->g.n3m;
-  mean3_kernel<<<1, 1024, 0, c->stream>>>(c->red + kRedPart, c->g.n2m * c->g.n3m, ncell, s->mean3);
+  { MIBM_PROF(c, "mean3");
+    mean3_kernel<<<1, 1024, 0, c->stream>>>(c->red + kRedPart, c->g.n2m * c->g.n3m, ncell, s->mean3); }
   c->launches += 2;
   k_velforce_apply(c, s->mean3);
 }
@@ -1061,66 +1232,92 @@ void lagr_tempforce(Ctx* c) { k_tempforce_apply(c); }
 
 void lagr_find_probe_indices(Ctx* c) {
   if (c->maxnf == 0) return;
-  { MIBM_PROF(c, "probe_idx"); probe_idx_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(
-      lag_args(c), M<double>(c, MIBM_M_TRI_BAR), M<double>(c, MIBM_M_TRI_NOR), M<int>(c, MIBM_M_GHOST_FACE),
-      c->S(MIBM_S_H_EULERIAN), M<int>(c, MIBM_M_PIND)); }
+  { MIBM_PROF(c, "probe_idx");
+    probe_idx_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(
+        lag_args(c), M<double>(c, MIBM_M_TRI_BAR), M<double>(c, MIBM_M_TRI_NOR), M<int>(c, MIBM_M_GHOST_FACE),
+        c->S(MIBM_S_H_EULERIAN), M<int>(c, MIBM_M_PIND)); }
   ++c->launches;
-  for (int q = 0; q < 4; ++q) c->plan[q].valid = false;
   MIBM_LAUNCH_CHECK(c, "findProbeIndices");
+}
+
+static void heat_flux_launch(Ctx* c) {
+  LagState* s = lag_of(c);
+  { MIBM_PROF(c, "heat_flux");
+    heat_flux_kernel<<<div_up(2 * (size_t)c->maxnf, 64), 64, 0, c->stream>>>(
+        lag_args(c), c->df[MIBM_F_TEMP], M<double>(c, MIBM_M_TRI_BAR), M<double>(c, MIBM_M_TRI_NOR),
+        M<int>(c, MIBM_M_GHOST_FACE), M<int>(c, MIBM_M_PIND), c->S(MIBM_S_H_EULERIAN), c->S(MIBM_S_PEC),
+        M<double>(c, MIBM_M_QW_O), M<double>(c, MIBM_M_QW_I), c->dflag); }
+  { MIBM_PROF(c, "face_to_vert");
+    face_to_vert_kernel<<<div_up(c->maxnv, 128), 128, 0, c->stream>>>(
+        c->maxnv, s->adj_off, s->adj_face, M<double>(c, MIBM_M_SUR), M<double>(c, MIBM_M_AVERT),
+        M<double>(c, MIBM_M_QW_O), M<double>(c, MIBM_M_QW_I), M<double>(c, MIBM_M_QW_OVERT),
+        M<double>(c, MIBM_M_QW_IVERT)); }
+  c->launches += 2;
 }
 
 void lagr_heat_flux(Ctx* c) {
   if (c->maxnf == 0) return;
   if (!ensure_adjacency(c)) return;
-  LagState* s = lag_of(c);
-  { MIBM_PROF(c, "heat_flux"); heat_flux_kernel<<<div_up(2 * (size_t)c->maxnf, 64), 64, 0, c->stream>>>(
-      lag_args(c), c->df[MIBM_F_TEMP], M<double>(c, MIBM_M_TRI_BAR), M<double>(c, MIBM_M_TRI_NOR),
-      M<int>(c, MIBM_M_GHOST_FACE), M<int>(c, MIBM_M_PIND), c->S(MIBM_S_H_EULERIAN), c->S(MIBM_S_PEC),
-      M<double>(c, MIBM_M_QW_O), M<double>(c, MIBM_M_QW_I), c->dflag); }
-  { MIBM_PROF(c, "face_to_vert"); face_to_vert_kernel<<<div_up(c->maxnv, 128), 128, 0, c->stream>>>(
-      c->maxnv, s->adj_off, s->adj_face, M<double>(c, MIBM_M_SUR), M<double>(c, MIBM_M_AVERT),
-      M<double>(c, MIBM_M_QW_O), M<double>(c, MIBM_M_QW_I), M<double>(c, MIBM_M_QW_OVERT), M<double>(c, MIBM_M_QW_IVERT)); }
-  c->launches += 2;
+  heat_flux_launch(c);
   if (MIBM_LAUNCH_CHECK(c, "mls_heatFlux")) check_flag(c, "mls_heatFlux");
 }
 
 void lagr_stefan(Ctx* c, const StepParams* dp) {
   if (c->maxnv == 0) return;
-  { MIBM_PROF(c, "stefan"); stefan_kernel<<<div_up(c->maxnv, 128), 128, 0, c->stream>>>(
-      c->maxnv, M<int>(c, MIBM_M_GHOST_VERT), M<double>(c, MIBM_M_VERT_NOR), M<double>(c, MIBM_M_QW_OVERT),
-      M<double>(c, MIBM_M_QW_IVERT), c->S(MIBM_S_CPLIQUID) / c->S(MIBM_S_LATHEAT), dp, M<double>(c, MIBM_M_VMELT),
-      M<double>(c, MIBM_M_VMELT_M1), M<double>(c, MIBM_M_XYZV)); }
+  { MIBM_PROF(c, "stefan");
+    stefan_kernel<<<div_up(c->maxnv, 128), 128, 0, c->stream>>>(
+        c->maxnv, M<int>(c, MIBM_M_GHOST_VERT), M<double>(c, MIBM_M_VERT_NOR), M<double>(c, MIBM_M_QW_OVERT),
+        M<double>(c, MIBM_M_QW_IVERT), c->S(MIBM_S_CPLIQUID) / c->S(MIBM_S_LATHEAT), dp, M<double>(c, MIBM_M_VMELT),
+        M<double>(c, MIBM_M_VMELT_M1), M<double>(c, MIBM_M_XYZV)); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "stefan");
+  lag_of(c)->weights_valid = false;
 }
 
-// Refresh areas, normals, centroids, vertex areas/normals, volume and centre
-// of mass; the scalars land in the registered host Surface/Volume/pos_CM.
-void lagr_geometry_refresh(Ctx* c, bool imelt) {
-  if (c->maxnf == 0) return;
-  if (!ensure_adjacency(c) || !ensure_lag_buffers(c)) return;
+// Geometry refresh (particle.f90:165-193): kernels only; the scalars stay
+// in the device buffer until geometry_to_host.
+static void geometry_launch(Ctx* c, bool imelt) {
   LagState* s = lag_of(c);
-  { MIBM_PROF(c, "face_geom"); face_geom_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(
-      c->maxnf, M<int>(c, MIBM_M_VERT_OF_FACE), M<int>(c, MIBM_M_GHOST_FACE), M<double>(c, MIBM_M_XYZV),
-      M<double>(c, MIBM_M_SUR), M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_TRI_BAR), s->face_part); }
-  { MIBM_PROF(c, "vert_geom"); vert_geom_kernel<<<div_up(c->maxnv, 128), 128, 0, c->stream>>>(
-      c->maxnv, s->adj_off, s->adj_face, M<int>(c, MIBM_M_GHOST_VERT), M<double>(c, MIBM_M_SUR),
-      M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_AVERT), M<double>(c, MIBM_M_VERT_NOR)); }
-  geom_reduce_kernel<<<1, 256, 0, c->stream>>>(c->maxnf, s->face_part, s->geom_out);
+  { MIBM_PROF(c, "face_geom");
+    face_geom_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(
+        c->maxnf, M<int>(c, MIBM_M_VERT_OF_FACE), M<int>(c, MIBM_M_GHOST_FACE), M<double>(c, MIBM_M_XYZV),
+        M<double>(c, MIBM_M_SUR), M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_TRI_BAR), s->face_part); }
+  { MIBM_PROF(c, "vert_geom");
+    vert_geom_kernel<<<div_up(c->maxnv, 128), 128, 0, c->stream>>>(
+        c->maxnv, s->adj_off, s->adj_face, M<int>(c, MIBM_M_GHOST_VERT), M<double>(c, MIBM_M_SUR),
+        M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_AVERT), M<double>(c, MIBM_M_VERT_NOR)); }
+  { MIBM_PROF(c, "geom_reduce");
+    geom_reduce_kernel<<<1, 256, 0, c->stream>>>(c->maxnf, s->face_part, s->geom_out); }
   c->launches += 3;
   if (imelt) {
-    cfac_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(c->maxnf, M<double>(c, MIBM_M_SUR),
-                                                              c->S(MIBM_S_H_EULERIAN), c->S(MIBM_S_CELVOL),
-                                                              M<double>(c, MIBM_M_CFAC));
+    { MIBM_PROF(c, "cfac");
+      cfac_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(c->maxnf, M<double>(c, MIBM_M_SUR),
+                                                                c->S(MIBM_S_H_EULERIAN), c->S(MIBM_S_CELVOL),
+                                                                M<double>(c, MIBM_M_CFAC)); }
     ++c->launches;
   }
+}
+
+// Surface, Volume and centre of mass to the registered host scalars
+// (calc_rigidBody_params writes Volume last, RigidAuxRoutines.f90:738).
+void lagr_geometry_to_host(Ctx* c) {
+  if (c->maxnf == 0) return;
+  LagState* s = lag_of(c);
+  if (!s->geom_out) return;
   cudaMemcpyAsync(c->red_host, s->geom_out, sizeof(double) * 6, cudaMemcpyDeviceToHost, c->stream);
   if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "geometry")) return;
   *c->hs[MIBM_S_SURFACE] = c->red_host[0];
-  *c->hs[MIBM_S_VOLUME] = c->red_host[2];        // calc_rigidBody_params writes Volume last
+  *c->hs[MIBM_S_VOLUME] = c->red_host[2];
   c->hs[MIBM_S_POS_CM][0] = c->red_host[3];
   c->hs[MIBM_S_POS_CM][1] = c->red_host[4];
   c->hs[MIBM_S_POS_CM][2] = c->red_host[5];
+}
+
+void lagr_geometry_refresh(Ctx* c, bool imelt) {
+  if (c->maxnf == 0) return;
+  if (!ensure_adjacency(c) || !ensure_lag_buffers(c)) return;
+  geometry_launch(c, imelt);
+  lagr_geometry_to_host(c);
 }
 
 void lagr_tag_narrow_band(Ctx* c) {
@@ -1130,15 +1327,22 @@ void lagr_tag_narrow_band(Ctx* c) {
     if (!cuda_ok(c, cudaMalloc(&s->sdf_bits, sizeof(unsigned long long) * c->g.cells), "band")) return;
     if (!cuda_ok(c, cudaMalloc(&s->winner, sizeof(int) * c->g.cells), "band")) return;
   }
+  if (!s->dist_buf)
+    if (!cuda_ok(c, cudaMalloc(&s->dist_buf, sizeof(double) * 125 * (size_t)c->maxnf), "band")) return;
   TagArgs T;
   T.L = lag_args(c);
   T.x = M<double>(c, MIBM_M_XYZV); T.vof = M<int>(c, MIBM_M_VERT_OF_FACE); T.ghost = M<int>(c, MIBM_M_GHOST_FACE);
   T.bar = M<double>(c, MIBM_M_TRI_BAR); T.nor = M<double>(c, MIBM_M_TRI_NOR);
-  { MIBM_PROF(c, "sdf_reset"); sdf_reset_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, s->sdf_bits, s->winner); }
+  { MIBM_PROF(c, "sdf_reset");
+    sdf_reset_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, s->sdf_bits, s->winner); }
   size_t nthr = (size_t)c->maxnf * 125;
-  for (int pass = 0; pass < 3; ++pass)
-    { MIBM_PROF(c, "band"); band_kernel<<<div_up(nthr, 128), 128, 0, c->stream>>>(T, pass, s->sdf_bits, s->winner, c->df[MIBM_F_VOFP]); }
-  { MIBM_PROF(c, "sdf_finish"); sdf_finish_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, s->sdf_bits, c->df[MIBM_F_SDF]); }
+  for (int pass = 0; pass < 3; ++pass) {
+    MIBM_PROF(c, "band");
+    band_kernel<<<div_up(nthr, 128), 128, 0, c->stream>>>(T, pass, s->sdf_bits, s->winner, c->df[MIBM_F_VOFP],
+                                                           s->dist_buf);
+  }
+  { MIBM_PROF(c, "sdf_finish");
+    sdf_finish_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, s->sdf_bits, c->df[MIBM_F_SDF]); }
   c->launches += 5;
   k_interp_vof(c);
   MIBM_LAUNCH_CHECK(c, "narrowBandTagging");
@@ -1179,7 +1383,7 @@ void lagr_tag_initial(Ctx* c) {
   }
   double* tmp = nullptr;
   if (!cuda_ok(c, cudaMalloc(&tmp, sizeof(double) * std::max<size_t>(1, ncell)), "initial tag")) return;
-  { MIBM_PROF(c, "sdf_reset"); sdf_reset_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, s->sdf_bits, s->winner); }
+  sdf_reset_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, s->sdf_bits, s->winner);
   initial_tag_kernel<<<div_up(ncell, 128), 128, 0, c->stream>>>(T, b0[0], b0[1], b0[2], nb[0], nb[1], nb[2], tmp);
   for (int pass = 0; pass < 2; ++pass)
     initial_claim_kernel<<<div_up(ncell, 256), 256, 0, c->stream>>>(c->g, b0[0], b0[1], b0[2], nb[0], nb[1], nb[2], tmp,
@@ -1192,7 +1396,7 @@ void lagr_tag_initial(Ctx* c) {
   lagr_tag_narrow_band(c);
 }
 
-// particle.f90:38-193 without remeshing / Newton-Euler (flags off)
+// particle.f90:38-193 (drop-in particle_): dense force fields, host checks
 void lagr_particle(Ctx* c, const StepParams* dp) {
   if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0) return;
   lagr_find_centroid_indices(c);
@@ -1214,16 +1418,59 @@ void lagr_particle(Ctx* c, const StepParams* dp) {
   if (c->S(MIBM_S_VOLUME) < c->S(MIBM_S_V_THRESH)) fail(c, MIBM_EABORT, "Geometry V/VE smaller than threshold");
 }
 
-void lagr_free(Ctx* c) {
-  for (int q = 0; q < 4; ++q) {
-    Ctx::Plan& p = c->plan[q];
-    cudaFree(p.key); cudaFree(p.src); cudaFree(p.tmp_key); cudaFree(p.tmp_src); cudaFree(p.hist);
+// particle.f90:38-193 inside the fused step: no host synchronisation.  The
+// forces are added straight into u, v, w (the mean force is left in
+// `mean3` for the projection update to subtract) and, after the heat flux
+// has read the unforced temperature, into T.  MLS weights of a stationary
+// cage are reused.  Flags and geometry scalars are read by the caller at the
+// end of the step.
+const double* lagr_particle_fused(Ctx* c, const StepParams* dp) {
+  if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0) return nullptr;
+  if (!ensure_adjacency(c) || !ensure_lag_buffers(c)) return nullptr;
+  LagState* s = lag_of(c);
+  bool stationary = c->I(MIBM_I_STATIONARY) != 0;
+  lagr_find_centroid_indices(c);
+  if (!(stationary && s->weights_valid)) {
+    mls_weight_launch(c);
+    s->weights_valid = stationary;
   }
+  force_coefficients(c);
+  update_plan(c);
+  scatter(c, true, 0, 3, true);
+  double ncell = (double)c->g.n1m * (double)c->g.n2m * (double)c->g.n3m;
+  { MIBM_PROF(c, "seg_mean");
+    seg_partial_kernel<<<kMeanBlocks, 256, 0, c->stream>>>(s->plan_n, c->g.cells, s->res_key, s->segval,
+                                                           c->red + kRedPart);
+    seg_final_kernel<<<1, kMeanBlocks, 0, c->stream>>>(c->red + kRedPart, ncell, s->mean3); }
+  c->launches += 2;
+  bool imelt = c->I(MIBM_I_IMELT) == 1;
+  if (imelt) {
+    lagr_find_probe_indices(c);
+    heat_flux_launch(c);
+  }
+  scatter(c, true, 3, 4, false);
+  if (imelt) lagr_stefan(c, dp);
+  geometry_launch(c, imelt);
+  MIBM_LAUNCH_CHECK(c, "particle");
+  return s->mean3;
+}
+
+// end-of-step checks of the fused path: MLS flags, geometry scalars, volume
+void lagr_step_finish(Ctx* c) {
+  if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0) return;
+  if (!check_flag(c, "particle")) return;
+  lagr_geometry_to_host(c);
+  if (c->S(MIBM_S_VOLUME) < c->S(MIBM_S_V_THRESH)) fail(c, MIBM_EABORT, "Geometry V/VE smaller than threshold");
+}
+
+void lagr_free(Ctx* c) {
   for (size_t q = 0; q < g_lag.size(); ++q)
     if (g_lag[q]->c == c) {
       LagState* s = g_lag[q];
       cudaFree(s->adj_off); cudaFree(s->adj_face); cudaFree(s->face_part); cudaFree(s->geom_out);
-      cudaFree(s->mean3); cudaFree(s->sdf_bits); cudaFree(s->winner);
+      cudaFree(s->mean3); cudaFree(s->sdf_bits); cudaFree(s->winner); cudaFree(s->dist_buf);
+      cudaFree(s->key); cudaFree(s->src); cudaFree(s->tmp_key); cudaFree(s->tmp_src); cudaFree(s->hist);
+      cudaFree(s->saved); cudaFree(s->dirty); cudaFree(s->segval);
       delete s;
       g_lag.erase(g_lag.begin() + q);
       break;

@@ -243,15 +243,20 @@ __global__ void divg_kernel(StencilArgs A, const StepParams* __restrict__ pp, do
   dph[c0] = dq * usdtal;
 }
 
+// mean3 (fused step only): the mean IBM force of velforce.f90:21-50, removed
+// here instead of in a separate pass (a constant does not change divg)
 __global__ void updvp_kernel(StencilArgs A, const StepParams* __restrict__ pp, const double* __restrict__ dph,
-                             double* __restrict__ vx, double* __restrict__ vy, double* __restrict__ vz) {
+                             double* __restrict__ vx, double* __restrict__ vy, double* __restrict__ vz,
+                             const double* __restrict__ mean3) {
   CELL_INDEX
   double al = pp->al, dt = pp->dt;
   double udx1 = al * dt * g.dx1, udx2 = al * dt * g.dx2, udx3 = al * dt * g.dx3;
   double loc = dph[c0];
-  vx[c0] = vx[c0] - (loc - dph[c0 + dim]) * udx1;
-  vy[c0] = vy[c0] - (loc - dph[c0 + djm]) * udx2;
-  vz[c0] = vz[c0] - (loc - dph[c0 + dkm]) * udx3;
+  double mx = 0.0, my = 0.0, mz = 0.0;
+  if (mean3) { mx = mean3[0]; my = mean3[1]; mz = mean3[2]; }
+  vx[c0] = (vx[c0] - mx) - (loc - dph[c0 + dim]) * udx1;
+  vy[c0] = (vy[c0] - my) - (loc - dph[c0 + djm]) * udx2;
+  vz[c0] = (vz[c0] - mz) - (loc - dph[c0 + dkm]) * udx3;
 }
 
 __global__ void prcalc_kernel(StencilArgs A, const StepParams* __restrict__ pp, const double* __restrict__ dph,
@@ -416,9 +421,9 @@ void k_divg(Ctx* c, const StepParams* dp) {
   MIBM_LAUNCH_CHECK(c, "divg");
 }
 
-void k_updvp(Ctx* c, const StepParams* dp) {
+void k_updvp(Ctx* c, const StepParams* dp, const double* mean3) {
   { MIBM_PROF(c, "updvp"); updvp_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, c->df[MIBM_F_DPH], c->df[MIBM_F_VX],
-                                                               c->df[MIBM_F_VY], c->df[MIBM_F_VZ]); }
+                                                               c->df[MIBM_F_VY], c->df[MIBM_F_VZ], mean3); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "updvp");
 }

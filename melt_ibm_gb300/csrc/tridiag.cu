@@ -71,7 +71,6 @@ struct TriCache {
   std::vector<int> n;
   std::vector<double> bd;
 };
-static TriCache g_cache_dummy;
 
 struct CtxTri {
   TriCache cache;
@@ -117,7 +116,10 @@ static const double* table_for(Ctx* c, int n, double betadx) {
   return tc.dev + (size_t)s * tc.len;
 }
 
+static void steptab_free(Ctx* c);
+
 void tri_free(Ctx* c) {
+  steptab_free(c);
   for (size_t q = 0; q < g_tri.size(); ++q)
     if (g_tri[q].first == c) {
       cudaFree(g_tri[q].second->cache.dev);
@@ -128,7 +130,10 @@ void tri_free(Ctx* c) {
     }
 }
 
-// One thread: solve the line held in shared memory at base[e*stride], e=0..n-1
+// One thread: solve the line held in shared memory at base[e*stride],
+// e = 0..n-1, with the factor table T (also in shared memory).  The loops
+// are unrolled by 4 with the independent loads (line values and factors)
+// issued ahead of the dependent FMA chain.
 __device__ __forceinline__ void solve_line(double* base, int stride, int n, const double* __restrict__ T) {
   const double* a = T;
   const double* b = T + n;
@@ -138,20 +143,44 @@ __device__ __forceinline__ void solve_line(double* base, int stride, int n, cons
   double rn = base[(size_t)(n - 1) * stride];
   double y = a[0] * base[0];
   base[0] = y;
-  for (int e = 1; e < n - 1; ++e) {
-    double r = base[(size_t)e * stride];
-    y = a[e] * r - b[e] * y;
+  int e = 1;
+  for (; e + 4 <= n - 1; e += 4) {
+    double r0 = base[(size_t)e * stride], r1 = base[(size_t)(e + 1) * stride];
+    double r2 = base[(size_t)(e + 2) * stride], r3 = base[(size_t)(e + 3) * stride];
+    double a0 = a[e] * r0, a1 = a[e + 1] * r1, a2 = a[e + 2] * r2, a3 = a[e + 3] * r3;
+    y = a0 - b[e] * y;     base[(size_t)e * stride] = y;
+    y = a1 - b[e + 1] * y; base[(size_t)(e + 1) * stride] = y;
+    y = a2 - b[e + 2] * y; base[(size_t)(e + 2) * stride] = y;
+    y = a3 - b[e + 3] * y; base[(size_t)(e + 3) * stride] = y;
+  }
+  for (; e < n - 1; ++e) {
+    y = a[e] * base[(size_t)e * stride] - b[e] * y;
     base[(size_t)e * stride] = y;
   }
   double f = 0.0;   // f_n = 0
-  for (int e = n - 2; e >= 0; --e) {
+  e = n - 2;
+  for (; e - 3 >= 0; e -= 4) {
+    double y0 = base[(size_t)e * stride], y1 = base[(size_t)(e - 1) * stride];
+    double y2 = base[(size_t)(e - 2) * stride], y3 = base[(size_t)(e - 3) * stride];
+    f = y0 + q[e] * f;     base[(size_t)e * stride] = f;
+    f = y1 + q[e - 1] * f; base[(size_t)(e - 1) * stride] = f;
+    f = y2 + q[e - 2] * f; base[(size_t)(e - 2) * stride] = f;
+    f = y3 + q[e - 3] * f; base[(size_t)(e - 3) * stride] = f;
+  }
+  for (; e >= 0; --e) {
     f = base[(size_t)e * stride] + q[e] * f;
     base[(size_t)e * stride] = f;
   }
   double f1 = base[0], fnm1 = base[(size_t)(n - 2) * stride];
   double xn = (rn * ackl_b - api * f1 - ami * fnm1) * inv_den;
-  for (int e = 0; e < n - 1; ++e) base[(size_t)e * stride] = xn * s[e] + base[(size_t)e * stride];
+  for (e = 0; e < n - 1; ++e) base[(size_t)e * stride] = xn * s[e] + base[(size_t)e * stride];
   base[(size_t)(n - 1) * stride] = xn;
+}
+
+// copy the factor table (4n + 4 doubles) into shared memory
+__device__ __forceinline__ const double* stage_table(double* sT, const double* __restrict__ T, int n) {
+  for (int q = threadIdx.x; q < 4 * n + 4; q += blockDim.x) sT[q] = T[q];
+  return sT;
 }
 
 constexpr int kLines = 32;
@@ -162,13 +191,25 @@ __global__ void solve_x_kernel(Grid g, double* __restrict__ rhs, const double* _
   int n = g.n1m, pitch = n + 1;
   int j0 = blockIdx.x * kLines, k = blockIdx.y;
   int nl = min(kLines, g.n2m - j0);
-  for (int l = 0; l < nl; ++l)
-    for (int i = threadIdx.x; i < n; i += blockDim.x) sm[l * pitch + i] = rhs[cidx(g, i, j0 + l, k)];
+  const double* sT = stage_table(sm + kLines * pitch, T, n);
+  int total = nl * n;
+  for (int t0 = threadIdx.x; t0 < total; t0 += 8 * blockDim.x) {
+    double v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      int t = t0 + u * blockDim.x;
+      v[u] = (t < total) ? rhs[cidx(g, t % n, j0 + t / n, k)] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      int t = t0 + u * blockDim.x;
+      if (t < total) sm[(t / n) * pitch + t % n] = v[u];
+    }
+  }
   __syncthreads();
-  if (threadIdx.x < nl) solve_line(sm + threadIdx.x * pitch, 1, n, T);
+  if (threadIdx.x < nl) solve_line(sm + threadIdx.x * pitch, 1, n, sT);
   __syncthreads();
-  for (int l = 0; l < nl; ++l)
-    for (int i = threadIdx.x; i < n; i += blockDim.x) rhs[cidx(g, i, j0 + l, k)] = sm[l * pitch + i];
+  for (int t = threadIdx.x; t < total; t += blockDim.x) rhs[cidx(g, t % n, j0 + t / n, k)] = sm[(t / n) * pitch + t % n];
 }
 
 // y-lines: tile = up to 32 adjacent i of one plane k; smem[j][l]
@@ -177,12 +218,23 @@ __global__ void solve_y_kernel(Grid g, double* __restrict__ rhs, const double* _
   int n = g.n2m;
   int i0 = blockIdx.x * kLines, k = blockIdx.y;
   int nl = min(kLines, g.n1m - i0);
-  for (int t = threadIdx.x; t < n * kLines; t += blockDim.x) {
-    int j = t / kLines, l = t % kLines;
-    if (l < nl) sm[t] = rhs[cidx(g, i0 + l, j, k)];
+  const double* sT = stage_table(sm + n * kLines, T, n);
+  for (int t0 = threadIdx.x; t0 < n * kLines; t0 += 8 * blockDim.x) {
+    double v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      int t = t0 + u * blockDim.x;
+      int j = t / kLines, l = t % kLines;
+      v[u] = (t < n * kLines && l < nl) ? rhs[cidx(g, i0 + l, j, k)] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      int t = t0 + u * blockDim.x;
+      if (t < n * kLines) sm[t] = v[u];
+    }
   }
   __syncthreads();
-  if (threadIdx.x < nl) solve_line(sm + threadIdx.x, kLines, n, T);
+  if (threadIdx.x < nl) solve_line(sm + threadIdx.x, kLines, n, sT);
   __syncthreads();
   for (int t = threadIdx.x; t < n * kLines; t += blockDim.x) {
     int j = t / kLines, l = t % kLines;
@@ -198,12 +250,23 @@ __global__ void solve_z_kernel(Grid g, double* __restrict__ rhs, const double* _
   int n = g.n3m;
   int i0 = blockIdx.x * kLines, j = blockIdx.y;
   int nl = min(kLines, g.n1m - i0);
-  for (int t = threadIdx.x; t < n * kLines; t += blockDim.x) {
-    int k = t / kLines, l = t % kLines;
-    if (l < nl) sm[t] = rhs[cidx(g, i0 + l, j, k)];
+  const double* sT = stage_table(sm + n * kLines, T, n);
+  for (int t0 = threadIdx.x; t0 < n * kLines; t0 += 8 * blockDim.x) {
+    double v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      int t = t0 + u * blockDim.x;
+      int k = t / kLines, l = t % kLines;
+      v[u] = (t < n * kLines && l < nl) ? rhs[cidx(g, i0 + l, j, k)] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      int t = t0 + u * blockDim.x;
+      if (t < n * kLines) sm[t] = v[u];
+    }
   }
   __syncthreads();
-  if (threadIdx.x < nl) solve_line(sm + threadIdx.x, kLines, n, T);
+  if (threadIdx.x < nl) solve_line(sm + threadIdx.x, kLines, n, sT);
   __syncthreads();
   for (int t = threadIdx.x; t < n * kLines; t += blockDim.x) {
     int k = t / kLines, l = t % kLines;
@@ -216,16 +279,78 @@ __global__ void solve_z_kernel(Grid g, double* __restrict__ rhs, const double* _
   }
 }
 
+
+// Tables of one fused RK3 step: [substep][velocity|temperature][x|y|z].
+// Built on the host once per step into one of two pinned buffers (the one
+// not read by the previous step's copy) and copied in stream order.
+struct StepTables {
+  double* dev = nullptr;
+  double* pinned[2] = {nullptr, nullptr};
+  cudaEvent_t copied[2] = {nullptr, nullptr};
+  int parity = 0, len = 0;
+};
+static std::vector<std::pair<Ctx*, StepTables*>> g_steptab;
+
+static StepTables* steptab_of(Ctx* c) {
+  for (auto& e : g_steptab)
+    if (e.first == c) return e.second;
+  StepTables* t = new StepTables();
+  g_steptab.emplace_back(c, t);
+  return t;
+}
+
+const double* tri_step_prepare(Ctx* c, const double betadx[3][2][3], int* len_out) {
+  StepTables* st = steptab_of(c);
+  int nmax = std::max(c->g.n1m, c->g.n3m);
+  if (!st->dev) {
+    st->len = 4 * nmax + 4;
+    size_t bytes = sizeof(double) * 18 * (size_t)st->len;
+    if (!cuda_ok(c, cudaMalloc(&st->dev, bytes), "step tables")) return nullptr;
+    for (int q = 0; q < 2; ++q) {
+      if (!cuda_ok(c, cudaMallocHost(&st->pinned[q], bytes), "step tables")) return nullptr;
+      if (!cuda_ok(c, cudaEventCreateWithFlags(&st->copied[q], cudaEventDisableTiming), "step tables")) return nullptr;
+    }
+  }
+  int p = st->parity;
+  st->parity ^= 1;
+  cudaEventSynchronize(st->copied[p]);            // the copy that last read pinned[p]
+  const int n[3] = {c->g.n1m, c->g.n2m, c->g.n3m};
+  std::vector<double> t;
+  for (int ns = 0; ns < 3; ++ns)
+    for (int f = 0; f < 2; ++f)
+      for (int d = 0; d < 3; ++d) {
+        build_table(n[d], betadx[ns][f][d], t);
+        std::copy(t.begin(), t.end(), st->pinned[p] + (size_t)((ns * 2 + f) * 3 + d) * st->len);
+      }
+  cudaMemcpyAsync(st->dev, st->pinned[p], sizeof(double) * 18 * (size_t)st->len, cudaMemcpyHostToDevice, c->stream);
+  cudaEventRecord(st->copied[p], c->stream);
+  *len_out = st->len;
+  return st->dev;
+}
+
+static void steptab_free(Ctx* c) {
+  for (size_t q = 0; q < g_steptab.size(); ++q)
+    if (g_steptab[q].first == c) {
+      StepTables* t = g_steptab[q].second;
+      cudaFree(t->dev);
+      for (int p = 0; p < 2; ++p) {
+        if (t->pinned[p]) cudaFreeHost(t->pinned[p]);
+        if (t->copied[p]) cudaEventDestroy(t->copied[p]);
+      }
+      delete t;
+      g_steptab.erase(g_steptab.begin() + q);
+      return;
+    }
+}
+
 static bool smem_ok(Ctx* c, const void* fn, size_t bytes) {
   if (bytes > 48 * 1024)
     return cuda_ok(c, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes), "smem attr");
   return true;
 }
 
-void k_solve_x(Ctx* c, double* rhs, double betadx) {
-  const double* T = table_for(c, c->g.n1m, betadx);
-  if (!T) return;
-  size_t sm = (size_t)kLines * (c->g.n1m + 1) * sizeof(double);
+void k_solve_x_T(Ctx* c, double* rhs, const double* T) {
+  size_t sm = ((size_t)kLines * (c->g.n1m + 1) + 4 * (size_t)c->g.n1m + 4) * sizeof(double);
   if (!smem_ok(c, (const void*)solve_x_kernel, sm)) return;
   dim3 grid(div_up(c->g.n2m, kLines), c->g.n3m);
   { MIBM_PROF(c, "solve_x"); solve_x_kernel<<<grid, 128, sm, c->stream>>>(c->g, rhs, T); }
@@ -233,10 +358,8 @@ void k_solve_x(Ctx* c, double* rhs, double betadx) {
   MIBM_LAUNCH_CHECK(c, "solve_x");
 }
 
-void k_solve_y(Ctx* c, double* rhs, double betadx) {
-  const double* T = table_for(c, c->g.n2m, betadx);
-  if (!T) return;
-  size_t sm = (size_t)kLines * c->g.n2m * sizeof(double);
+void k_solve_y_T(Ctx* c, double* rhs, const double* T) {
+  size_t sm = ((size_t)kLines * c->g.n2m + 4 * (size_t)c->g.n2m + 4) * sizeof(double);
   if (!smem_ok(c, (const void*)solve_y_kernel, sm)) return;
   dim3 grid(div_up(c->g.n1m, kLines), c->g.n3m);
   { MIBM_PROF(c, "solve_y"); solve_y_kernel<<<grid, 128, sm, c->stream>>>(c->g, rhs, T); }
@@ -244,15 +367,28 @@ void k_solve_y(Ctx* c, double* rhs, double betadx) {
   MIBM_LAUNCH_CHECK(c, "solve_y");
 }
 
-void k_solve_z(Ctx* c, double* rhs, double betadx, double* q) {
-  const double* T = table_for(c, c->g.n3m, betadx);
-  if (!T) return;
-  size_t sm = (size_t)kLines * c->g.n3m * sizeof(double);
+void k_solve_z_T(Ctx* c, double* rhs, const double* T, double* q, int write_rhs) {
+  size_t sm = ((size_t)kLines * c->g.n3m + 4 * (size_t)c->g.n3m + 4) * sizeof(double);
   if (!smem_ok(c, (const void*)solve_z_kernel, sm)) return;
   dim3 grid(div_up(c->g.n1m, kLines), c->g.n2m);
-  { MIBM_PROF(c, "solve_z"); solve_z_kernel<<<grid, 128, sm, c->stream>>>(c->g, rhs, T, q, 1); }
+  { MIBM_PROF(c, "solve_z"); solve_z_kernel<<<grid, 128, sm, c->stream>>>(c->g, rhs, T, q, write_rhs); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "solve_z");
+}
+
+void k_solve_x(Ctx* c, double* rhs, double betadx) {
+  const double* T = table_for(c, c->g.n1m, betadx);
+  if (T) k_solve_x_T(c, rhs, T);
+}
+
+void k_solve_y(Ctx* c, double* rhs, double betadx) {
+  const double* T = table_for(c, c->g.n2m, betadx);
+  if (T) k_solve_y_T(c, rhs, T);
+}
+
+void k_solve_z(Ctx* c, double* rhs, double betadx, double* q) {
+  const double* T = table_for(c, c->g.n3m, betadx);
+  if (T) k_solve_z_T(c, rhs, T, q, 1);
 }
 
 // ---------------------------------------------------------------------
@@ -329,7 +465,7 @@ extern "C" int mibm_solxi_noalloc(double* rhs, int n1m, int n2m, int n3m, int pi
   Grid g{};
   g.n1m = n1m; g.n2m = n2m; g.n3m = n3m; g.P = pitch;
   g.plane = (size_t)pitch * n2m; g.cells = g.plane * n3m;
-  size_t sm = (size_t)kLines * (n1m + 1) * sizeof(double);
+  size_t sm = ((size_t)kLines * (n1m + 1) + 4 * (size_t)n1m + 4) * sizeof(double);
   if (sm > 48 * 1024 &&
       cudaFuncSetAttribute((const void*)solve_x_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
           cudaSuccess)
