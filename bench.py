@@ -7,7 +7,12 @@ line solves, MLS immersed-boundary forcing with melting, FFT pressure
 projection).  Metric: Mcell-steps/s = N^3 * steps / seconds.
 
 value      device time of K steps with every field resident in HBM (CUDA events
-           on the library's stream, synchronised on both sides).
+           on the library's stream, synchronised on both sides), plain FP64 form.
+fp32_refined
+           the same K steps in the precision form (FP32 explicit terms, line
+           solves and FFTs on FP64 fields, projection refined on the FP64
+           divergence residual) from identical inputs; per-field relative L2
+           error against the FP64 run after the same number of steps.
 e2e        the same K steps driven the way a Fortran host drives the C-ABI:
            every step copies u, v, w, T, p and the vertex coordinates from host
            arrays to the device (mibm_sync_from_host_), runs cfl_/get_dt_/tschem_
@@ -73,7 +78,8 @@ ALGO_PASSES = {
     "divg": 4.0, "updvp": 7.0, "prcalc": 3.0, "hdnl": 6.0,
 }
 
-FIELD_MASK = sum(1 << f for f in (abi.MIBM_F_VX, abi.MIBM_F_VY, abi.MIBM_F_VZ, abi.MIBM_F_TEMP, abi.MIBM_F_PR))
+FIELDS = {"u": abi.MIBM_F_VX, "v": abi.MIBM_F_VY, "w": abi.MIBM_F_VZ, "T": abi.MIBM_F_TEMP, "p": abi.MIBM_F_PR}
+FIELD_MASK = sum(1 << f for f in FIELDS.values())
 MESH_MASK = 1 << (32 + abi.MIBM_M_XYZV)
 
 
@@ -232,6 +238,7 @@ def run_gpu(args):
     lib.mibm_select_device_(abi.ref_int(dev))
     cfg = CaseConfig(**WORKLOADS[args.workload])
     case = Case(cfg)
+    case32 = case.clone()                  # identical inputs for the precision form
     case.attach(lib)
     lib.check("attach")
     n3 = case.n1m * case.n2m * case.n3m
@@ -254,6 +261,9 @@ def run_gpu(args):
         wall = time.perf_counter() - t0
     launches = int(lib.mibm_launch_count_() - l0)
     lib.check("timed steps")
+    div64 = lib.mibm_divergence_max_()
+    case.sync_to_host(lib, FIELD_MASK)
+    snap64 = {k: case.interior(f).copy() for k, f in FIELDS.items()}
     dist.barrier()
     ms_max = dist.max(ms)
     value = dist.ws * n3 * args.steps / (ms_max * 1e-3) / 1e6
@@ -306,6 +316,48 @@ def run_gpu(args):
     e2e_value = dist.ws * n3 * args.steps / e2e_s / 1e6
     lib.check("e2e")
     case.detach(lib)
+    # ---------------- precision form: FP32 compute, FP64 fields, refined projection ----------------
+    fp32 = None
+    if not args.no_fp32:
+        case32.attach(lib)
+        case32.bind(lib)
+        lib.mibm_set_precision_(abi.ref_int(1), abi.ref_int(args.nproj))
+        lib.check("set_precision")
+        nt32 = 1
+        for _ in range(args.warmup):
+            case32.step(lib, nt32)
+            nt32 += 1
+        case32.sync_to_host(lib, 0)
+        dist.barrier()
+        lib.mibm_timer_mark_(abi.ref_int(2))
+        for _ in range(args.steps):
+            case32.step(lib, nt32)
+            nt32 += 1
+        lib.mibm_timer_mark_(abi.ref_int(3))
+        ms32 = dist.max(lib.mibm_timer_ms_(abi.ref_int(2), abi.ref_int(3)))
+        lib.check("precision form")
+        div32 = lib.mibm_divergence_max_()
+        case32.sync_to_host(lib, FIELD_MASK)
+        errs = {}
+        for k, f in FIELDS.items():
+            a, b = case32.interior(f), snap64[k]
+            errs[k] = float(np.sqrt(np.sum((a - b) ** 2)) / np.sqrt(np.sum(b * b)))
+        lib.mibm_profile_(abi.ref_int(1))
+        for _ in range(args.steps):
+            case32.step(lib, nt32)
+            nt32 += 1
+        lib.mibm_profile_(abi.ref_int(0))
+        prof32 = lib.profile()
+        tot32 = sum(v[0] for v in prof32.values()) or 1.0
+        kern32 = {k: {"ms_per_step": v[0] / args.steps, "launches_per_step": v[1] / args.steps, "share": v[0] / tot32}
+                  for k, v in sorted(prof32.items(), key=lambda kv: -kv[1][0])}
+        case32.detach(lib)
+        v32 = dist.ws * n3 * args.steps / (ms32 * 1e-3) / 1e6
+        fp32 = {"value": v32, "unit": "Mcell-steps/s", "ms_per_step": ms32 / args.steps,
+                "speedup_vs_fp64": v32 / value, "nproj": args.nproj,
+                "rel_l2_vs_fp64": errs, "divergence_max": div32, "divergence_max_fp64": div64,
+                "compared_after_steps": args.warmup + args.steps, "kernels": kern32,
+                "dtype": "f32 compute, f64 fields (u, v, w, T, p), f64 MLS / Stefan / divergence residual"}
     dist.barrier()
     if dist.rank != 0:
         dist.close()
@@ -320,7 +372,7 @@ def run_gpu(args):
                        "l2": "inputs larger than L2 (>30 fields of N^3 doubles resident)"},
             "e2e": {"value": e2e_value, "unit": "Mcell-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "roofline": roofline, "gpu_launches": launches, "clocks": clocks,
+            "roofline": roofline, "gpu_launches": launches, "clocks": clocks, "fp32_refined": fp32,
             "host_wall_ms_per_step": 1e3 * wall / args.steps, "kernels": kernels}
     if dist.ws == 1 and not args.no_cpu:
         try:
@@ -340,6 +392,8 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="melt128_fixed")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp32", action="store_true", help="skip the precision-form measurement")
+    ap.add_argument("--nproj", type=int, default=2, help="Poisson solves per substep in the precision form")
     args = ap.parse_args()
     if args.warmup < 3:
         log("bench: warm-up raised to 3 steps")

@@ -201,6 +201,14 @@ void get_dt_(void);       /* cfl.f90:33-77                                  */
 void interp_(double* arrold, double* arrnew, const int* n1o, const int* n2o,
              const int* n3o, const int* intvar, const int* kstarto,
              const int* kendo);                  /* interp.f90:1-221    */
+/* Form of tschem_ (no counterpart in the reference, which is FP64 only):
+ * mode 0 = plain FP64 (default); mode 1 = precision form -- FP32 explicit
+ * terms, RHS, line solves and FFTs on FP64 fields, with the pressure
+ * projection repeated `nproj` times on the FP64 divergence residual. */
+void mibm_set_precision_(const int* mode, const int* nproj);
+/* max over the owned cells of |div u| as divgck computes it
+ * (divg.f90:26-56); synchronises with the device. */
+double mibm_divergence_max_(void);
 /* Initial full cell tagging at t = 0 (pencil_rayTag.f90:37-165 with the  */
 /* narrow band, tagCells.f90:17-23 with initial_tag = .true.).            */
 void tagcells_initial_(void);

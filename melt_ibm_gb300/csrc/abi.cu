@@ -57,6 +57,66 @@ static void invtr(Ctx* c, int which) {
   k_solve_z(c, rhs, b3, c->df[fid[which]]);
 }
 
+__global__ void cast_kernel(size_t n, const double* __restrict__ a, float* __restrict__ b) {
+  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) b[t] = (float)a[t];
+}
+
+static bool ensure_f32(Ctx* c) {
+  const Grid& g = c->g;
+  if (!c->ru32) {
+    if (!cuda_ok(c, cudaMalloc(&c->ru32, 4 * g.cells * sizeof(float)), "ru32")) return false;
+    if (!cuda_ok(c, cudaMalloc(&c->rhs32, 4 * g.cells * sizeof(float)), "rhs32")) return false;
+    if (!cuda_ok(c, cudaMalloc(&c->phi32, g.cells * sizeof(float)), "phi32")) return false;
+    static const int ru[4] = {MIBM_F_RU1, MIBM_F_RU2, MIBM_F_RU3, MIBM_F_RUT};
+    for (int q = 0; q < 4; ++q) {
+      cast_kernel<<<div_up(g.cells, 256), 256, 0, c->stream>>>(g.cells, c->df[ru[q]], c->ru32 + (size_t)q * g.cells);
+      ++c->launches;
+    }
+  }
+  return MIBM_LAUNCH_CHECK(c, "precision buffers");
+}
+
+// Precision form of tsch.f90:18-97: FP32 explicit terms, RHS, line solves
+// and FFTs on FP64 fields; the projection is repeated `nproj` times, each
+// time on the FP64 divergence residual (iterative refinement), so the final
+// divergence is at FP64 round-off.  MLS inversions, Stefan front and
+// geometry stay FP64.
+static void tschem_f32(Ctx* c, const double* gam, const double* rom, const double bd[3][2][3]) {
+  const Grid& g = c->g;
+  if (!ensure_f32(c)) return;
+  int tlen = 0;
+  const float* tf = nullptr;
+  if (!tri_step_prepare(c, bd, &tlen, &tf)) return;
+  static const int fid[4] = {MIBM_F_VX, MIBM_F_VY, MIBM_F_VZ, MIBM_F_TEMP};
+  for (int ns = 0; ns < 3; ++ns) {
+    *c->hs[MIBM_S_AL] = gam[ns] + rom[ns];
+    *c->hs[MIBM_S_GA] = gam[ns];
+    *c->hs[MIBM_S_RO] = rom[ns];
+    const StepParams* dp = push_params(c, ns);
+    if (!c->I(MIBM_I_STATIONARY) && c->I(MIBM_I_IMLSFOR) == 1) lagr_tag_narrow_band(c);
+    k_fused_rhs_f32(c, dp, c->ru32, c->rhs32);
+    for (int q = 0; q < 4; ++q) {
+      int f = (q < 3) ? 0 : 1;
+      const float* T = tf + (size_t)((ns * 2 + f) * 3) * tlen;
+      float* r = c->rhs32 + (size_t)q * g.cells;
+      k_solve_x_f32(c, r, T);
+      k_solve_y_f32(c, r, T + tlen);
+      k_solve_z_f32(c, r, T + 2 * tlen, c->df[fid[q]]);
+    }
+    const double* mean3 = lagr_particle_fused(c, dp);
+    if (c->status != MIBM_OK) return;
+    for (int it = 0; it < c->nproj; ++it) {
+      k_divg(c, dp);                                   // FP64 residual
+      k_phcalc_f32(c, c->df[MIBM_F_DPH], c->phi32);    // FP32 Poisson solve
+      k_updvp_f32(c, dp, c->phi32, it == 0 ? mean3 : nullptr);
+      k_prcalc_f32(c, dp, c->phi32);
+    }
+    if (c->status != MIBM_OK) return;
+  }
+  lagr_step_finish(c);
+}
+
 // tsch.f90:18-97 on the device
 static void tschem(Ctx* c) {
   static const double gam[3] = {8.0 / 15.0, 5.0 / 12.0, 3.0 / 4.0};
@@ -80,8 +140,9 @@ static void tschem(Ctx* c) {
       }
     }
   }
+  if (c->precision == 1) { tschem_f32(c, gam, rom, bd); return; }
   int tlen = 0;
-  const double* tables = tri_step_prepare(c, bd, &tlen);
+  const double* tables = tri_step_prepare(c, bd, &tlen, nullptr);
   if (!tables) return;
   for (int ns = 0; ns < 3; ++ns) {
     *c->hs[MIBM_S_AL] = gam[ns] + rom[ns];
@@ -166,6 +227,36 @@ void get_dt_(void) {
   double buf = k_get_dt_buffer(c, dt, c->S(MIBM_S_REN));
   if (buf > 0.0) *c->hs[MIBM_S_DT] = dt * c->S(MIBM_S_CFLFIX) / buf;
   DROPIN_END
+}
+
+// Select the form of tschem_: 0 = plain FP64 (default), 1 = FP32 compute
+// with FP64 fields and refined projection; nproj = Poisson solves per
+// substep in the precision form (>= 1).
+void mibm_set_precision_(const int* mode, const int* nproj) {
+  Ctx* c = current(); if (!ready(c)) return;
+  if (*mode < 0 || *mode > 1 || *nproj < 1 || *nproj > 8) { fail(c, MIBM_EINVAL, "set_precision: mode 0|1, nproj 1..8"); return; }
+  if (*mode == 1 && c->precision == 0 && c->ru32) {
+    static const int ru[4] = {MIBM_F_RU1, MIBM_F_RU2, MIBM_F_RU3, MIBM_F_RUT};
+    for (int q = 0; q < 4; ++q) {
+      cast_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g.cells, c->df[ru[q]], c->ru32 + (size_t)q * c->g.cells);
+      ++c->launches;
+    }
+  }
+  c->precision = *mode;
+  c->nproj = *nproj;
+}
+
+// max over owned cells of |div u| (divgck, divg.f90:26-56); synchronises
+double mibm_divergence_max_(void) {
+  Ctx* c = current(); if (!ready(c)) return -1.0;
+  if (!c->divmax && !cuda_ok(c, cudaMalloc(&c->divmax, sizeof(unsigned long long)), "divmax")) return -1.0;
+  k_divmax(c, c->divmax);
+  unsigned long long bits = 0;
+  cudaMemcpyAsync(&bits, c->divmax, sizeof(bits), cudaMemcpyDeviceToHost, c->stream);
+  if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "divergence")) return -1.0;
+  double v;
+  memcpy(&v, &bits, sizeof(v));
+  return v;
 }
 
 void interp_(double*, double*, const int*, const int*, const int*, const int*, const int*, const int*) {

@@ -87,6 +87,13 @@ struct Ctx {
   StepParams* dparams = nullptr;          // [3] device copies (one per substep)
   StepParams* hparams = nullptr;          // pinned
   double* rhs4 = nullptr;                 // 4 RHS fields for the fused path
+  // precision form (FP32 compute, FP64 fields, refined projection)
+  int precision = 0;                      // 0 = plain FP64, 1 = FP32 + refinement
+  int nproj = 2;                          // Poisson solves per substep in precision form
+  float* ru32 = nullptr;                  // 4 explicit-term histories (FP32)
+  float* rhs32 = nullptr;                 // 4 RHS / line-solve fields (FP32)
+  float* phi32 = nullptr;                 // FP32 pressure correction
+  unsigned long long* divmax = nullptr;   // device max|div u| (IEEE bits)
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   bool use_graph = true;
@@ -169,6 +176,10 @@ inline void field_host_shape(const Ctx* c, int id, int& ny, int& klo, int& nk) {
 void k_hdnl(Ctx* c, int which, const StepParams* dp);
 void k_invtr_rhs(Ctx* c, int which, const StepParams* dp, double* rhs_out);
 void k_fused_rhs(Ctx* c, const StepParams* dp);
+void k_fused_rhs_f32(Ctx* c, const StepParams* dp, float* ru4, float* rhs4);
+void k_updvp_f32(Ctx* c, const StepParams* dp, const float* phi, const double* mean3);
+void k_prcalc_f32(Ctx* c, const StepParams* dp, const float* phi);
+void k_divmax(Ctx* c, unsigned long long* out);
 void k_divg(Ctx* c, const StepParams* dp);
 void k_updvp(Ctx* c, const StepParams* dp, const double* mean3 = nullptr);
 void k_prcalc(Ctx* c, const StepParams* dp);
@@ -185,9 +196,13 @@ void k_solve_z(Ctx* c, double* rhs, double betadx, double* q);
 void k_solve_x_T(Ctx* c, double* rhs, const double* T);
 void k_solve_y_T(Ctx* c, double* rhs, const double* T);
 void k_solve_z_T(Ctx* c, double* rhs, const double* T, double* q, int write_rhs);
-const double* tri_step_prepare(Ctx* c, const double betadx[3][2][3], int* len_out);
+const double* tri_step_prepare(Ctx* c, const double betadx[3][2][3], int* len_out, const float** f32_out);
+void k_solve_x_f32(Ctx* c, float* rhs, const float* T);
+void k_solve_y_f32(Ctx* c, float* rhs, const float* T);
+void k_solve_z_f32(Ctx* c, float* rhs, const float* T, double* q);
 // fft.cu
 void k_phcalc(Ctx* c);
+void k_phcalc_f32(Ctx* c, const double* src, float* phi);
 // lagr.cu
 void lagr_find_centroid_indices(Ctx* c);
 void lagr_mls_weight(Ctx* c);

@@ -40,96 +40,106 @@ static Plan1D make_plan(int n) {
   return p;
 }
 
-__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
-  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ double2 conjd(double2 a) { return make_double2(a.x, -a.y); }
+// complex helpers for double2 / float2
+template <typename C> struct Real;
+template <> struct Real<double2> { typedef double T; };
+template <> struct Real<float2> { typedef float T; };
+template <typename C> __device__ __forceinline__ C mk(typename Real<C>::T x, typename Real<C>::T y) { C r; r.x = x; r.y = y; return r; }
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) { return mk<C>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { return mk<C>(a.x + b.x, a.y + b.y); }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { return mk<C>(a.x - b.x, a.y - b.y); }
+template <typename C> __device__ __forceinline__ C conjc(C a) { return mk<C>(a.x, -a.y); }
 
 // Batched Stockham FFT of `nl` lines of length n held in shared memory.
 // Element e of line l lives at buf[l*LS + e*ES].  Ping-pong between A and B;
 // returns the buffer that holds the result.  sign = -1 forward, +1 inverse.
 // tw[m] = e^{-2 pi i m / n}.
-__device__ double2* fft_lines(double2* A, double2* B, int n, int nl, int LS, int ES, const Plan1D& plan,
-                              const double2* tw, int sign) {
+template <typename C>
+__device__ C* fft_lines(C* A, C* B, int n, int nl, int LS, int ES, const Plan1D& plan, const C* tw, int sign) {
+  typedef typename Real<C>::T R;
   int Ns = 1;
   for (int st = 0; st < plan.nst; ++st) {
-    int R = plan.radix[st];
-    int nb = n / R;                 // butterflies per line
+    int Rdx = plan.radix[st];
+    int nb = n / Rdx;                 // butterflies per line
     int total = nb * nl;
     for (int t = threadIdx.x; t < total; t += blockDim.x) {
       int l, j;
       if (LS == 1) { l = t % nl; j = t / nl; } else { j = t % nb; l = t / nb; }
       int kk = j % Ns;
-      int tstep = n / (Ns * R);     // twiddle index step
-      double2 v[4];
-      for (int r = 0; r < R; ++r) v[r] = A[l * LS + (j + r * nb) * ES];
-      for (int r = 1; r < R; ++r) {
-        double2 w = tw[(kk * r * tstep) % n];
+      int tstep = n / (Ns * Rdx);     // twiddle index step
+      C v[4];
+      for (int r = 0; r < Rdx; ++r) v[r] = A[l * LS + (j + r * nb) * ES];
+      for (int r = 1; r < Rdx; ++r) {
+        C w = tw[(kk * r * tstep) % n];
         if (sign > 0) w.y = -w.y;
         v[r] = cmul(v[r], w);
       }
-      if (R == 4) {
-        double2 a02p = cadd(v[0], v[2]), a02m = csub(v[0], v[2]);
-        double2 a13p = cadd(v[1], v[3]), a13m = csub(v[1], v[3]);
+      if (Rdx == 4) {
+        C a02p = cadd(v[0], v[2]), a02m = csub(v[0], v[2]);
+        C a13p = cadd(v[1], v[3]), a13m = csub(v[1], v[3]);
         // -i*(a1-a3) for the forward sign, +i*(a1-a3) for the inverse
-        double2 rot = (sign < 0) ? make_double2(a13m.y, -a13m.x) : make_double2(-a13m.y, a13m.x);
+        C rot = (sign < 0) ? mk<C>(a13m.y, -a13m.x) : mk<C>(-a13m.y, a13m.x);
         v[0] = cadd(a02p, a13p);
         v[2] = csub(a02p, a13p);
         v[1] = cadd(a02m, rot);
         v[3] = csub(a02m, rot);
-      } else if (R == 2) {
-        double2 a = v[0], b = v[1];
+      } else if (Rdx == 2) {
+        C a = v[0], b = v[1];
         v[0] = cadd(a, b);
         v[1] = csub(a, b);
-      } else {  // R == 3
-        const double s3 = 0.86602540378443864676;   // sqrt(3)/2
-        double2 t1 = cadd(v[1], v[2]), t2 = csub(v[1], v[2]);
-        double2 m = make_double2(v[0].x - 0.5 * t1.x, v[0].y - 0.5 * t1.y);
+      } else {  // radix 3
+        const R s3 = R(0.86602540378443864676);   // sqrt(3)/2
+        C t1 = cadd(v[1], v[2]), t2 = csub(v[1], v[2]);
+        C m = mk<C>(v[0].x - R(0.5) * t1.x, v[0].y - R(0.5) * t1.y);
         // forward: -i*s3*t2 ; inverse: +i*s3*t2
-        double2 s = (sign < 0) ? make_double2(s3 * t2.y, -s3 * t2.x) : make_double2(-s3 * t2.y, s3 * t2.x);
+        C sv = (sign < 0) ? mk<C>(s3 * t2.y, -s3 * t2.x) : mk<C>(-s3 * t2.y, s3 * t2.x);
         v[0] = cadd(v[0], t1);
-        v[1] = cadd(m, s);
-        v[2] = csub(m, s);
+        v[1] = cadd(m, sv);
+        v[2] = csub(m, sv);
       }
-      int idxD = (j / Ns) * Ns * R + kk;
-      for (int r = 0; r < R; ++r) B[l * LS + (idxD + r * Ns) * ES] = v[r];
+      int idxD = (j / Ns) * Ns * Rdx + kk;
+      for (int r = 0; r < Rdx; ++r) B[l * LS + (idxD + r * Ns) * ES] = v[r];
     }
     __syncthreads();
-    double2* t = A; A = B; B = t;
-    Ns *= R;
+    C* tmp = A; A = B; B = tmp;
+    Ns *= Rdx;
   }
   return A;
 }
 
+template <typename C>
 struct FftArgs {
+  typedef typename Real<C>::T R;
   Grid g;
   Plan1D px, py, pz;
-  const double2* twx;
-  const double2* twy;
-  const double2* twz;
-  const double* ak1;
-  const double* ak2;
-  const double* ak3;
-  double inv_nn;
+  const C* twx;
+  const C* twy;
+  const C* twz;
+  const R* ak1;
+  const R* ak2;
+  const R* ak3;
+  R inv_nn;
 };
 
-__device__ __forceinline__ void load_tw(double2* s, const double2* tw, int n) {
+template <typename C>
+__device__ __forceinline__ void load_tw(C* s, const C* tw, int n) {
   for (int m = threadIdx.x; m < n; m += blockDim.x) s[m] = tw[m];
 }
 
 constexpr int kRowPairs = 4;   // X passes: 4 complex lines (8 real rows) per CTA
 constexpr int kCols = 8;       // Y/Z passes: 8 adjacent kx columns per CTA
 
-// X forward: real rows (j, j+1) of plane k -> spec half spectra
-__global__ void fft_x_fwd(FftArgs F, const double* __restrict__ src, double2* __restrict__ spec) {
-  extern __shared__ double2 sh[];
+// X forward: real rows (j, j+1) of plane k (FP64 input) -> half spectra
+template <typename C>
+__global__ void fft_x_fwd(FftArgs<C> F, const double* __restrict__ src, C* __restrict__ spec) {
+  typedef typename Real<C>::T R;
+  extern __shared__ __align__(16) unsigned char shraw[];
+  C* sh = (C*)shraw;
   const Grid& g = F.g;
   int n = g.n1m;
-  double2* tws = sh;
-  double2* A = sh + n;
-  double2* B = A + kRowPairs * n;
+  C* tws = sh;
+  C* A = sh + n;
+  C* B = A + kRowPairs * n;
   load_tw(tws, F.twx, n);
   int k = blockIdx.y;
   int jp0 = blockIdx.x * kRowPairs;               // first row pair
@@ -137,33 +147,36 @@ __global__ void fft_x_fwd(FftArgs F, const double* __restrict__ src, double2* __
   for (int t = threadIdx.x; t < npairs * n; t += blockDim.x) {
     int l = t / n, i = t % n;
     int j = 2 * (jp0 + l);
-    A[l * n + i] = make_double2(src[cidx(g, i, j, k)], src[cidx(g, i, j + 1, k)]);
+    A[l * n + i] = mk<C>(R(src[cidx(g, i, j, k)]), R(src[cidx(g, i, j + 1, k)]));
   }
   __syncthreads();
-  double2* R = fft_lines(A, B, n, npairs, n, 1, F.px, tws, -1);
+  C* Rr = fft_lines(A, B, n, npairs, n, 1, F.px, tws, -1);
   int H = g.H;
   for (int t = threadIdx.x; t < npairs * H; t += blockDim.x) {
     int l = t / H, kx = t % H;
-    double2 z = R[l * n + kx];
-    double2 zc = conjd(R[l * n + ((n - kx) % n)]);
+    C z = Rr[l * n + kx];
+    C zc = conjc(Rr[l * n + ((n - kx) % n)]);
     // X_a = (Z + conj Z_-)/2 ; X_b = (Z - conj Z_-)/(2i)
-    double2 xa = make_double2(0.5 * (z.x + zc.x), 0.5 * (z.y + zc.y));
-    double2 d = csub(z, zc);
-    double2 xb = make_double2(0.5 * d.y, -0.5 * d.x);
+    C xa = mk<C>(R(0.5) * (z.x + zc.x), R(0.5) * (z.y + zc.y));
+    C d = csub(z, zc);
+    C xb = mk<C>(R(0.5) * d.y, R(-0.5) * d.x);
     int j = 2 * (jp0 + l);
     spec[(size_t)kx + (size_t)g.HP * ((size_t)j + (size_t)g.n2m * k)] = xa;
     spec[(size_t)kx + (size_t)g.HP * ((size_t)(j + 1) + (size_t)g.n2m * k)] = xb;
   }
 }
 
-// X inverse (c2r): half spectra of rows (j, j+1) -> real rows
-__global__ void fft_x_inv(FftArgs F, const double2* __restrict__ spec, double* __restrict__ dst) {
-  extern __shared__ double2 sh[];
+// X inverse (c2r): half spectra of rows (j, j+1) -> real rows of type R
+template <typename C>
+__global__ void fft_x_inv(FftArgs<C> F, const C* __restrict__ spec, typename Real<C>::T* __restrict__ dst) {
+  typedef typename Real<C>::T R;
+  extern __shared__ __align__(16) unsigned char shraw[];
+  C* sh = (C*)shraw;
   const Grid& g = F.g;
   int n = g.n1m, H = g.H;
-  double2* tws = sh;
-  double2* A = sh + n;
-  double2* B = A + kRowPairs * n;
+  C* tws = sh;
+  C* A = sh + n;
+  C* B = A + kRowPairs * n;
   load_tw(tws, F.twx, n);
   int k = blockIdx.y;
   int jp0 = blockIdx.x * kRowPairs;
@@ -172,104 +185,123 @@ __global__ void fft_x_inv(FftArgs F, const double2* __restrict__ spec, double* _
     int l = t / n, kx = t % n;
     int j = 2 * (jp0 + l);
     int src_kx = (kx < H) ? kx : n - kx;
-    double2 xa = spec[(size_t)src_kx + (size_t)g.HP * ((size_t)j + (size_t)g.n2m * k)];
-    double2 xb = spec[(size_t)src_kx + (size_t)g.HP * ((size_t)(j + 1) + (size_t)g.n2m * k)];
-    if (src_kx == 0 || 2 * src_kx == n) { xa.y = 0.0; xb.y = 0.0; }
+    C xa = spec[(size_t)src_kx + (size_t)g.HP * ((size_t)j + (size_t)g.n2m * k)];
+    C xb = spec[(size_t)src_kx + (size_t)g.HP * ((size_t)(j + 1) + (size_t)g.n2m * k)];
+    if (src_kx == 0 || 2 * src_kx == n) { xa.y = R(0); xb.y = R(0); }
     if (kx >= H) { xa.y = -xa.y; xb.y = -xb.y; }
     // Z = Xa + i Xb
-    A[l * n + kx] = make_double2(xa.x - xb.y, xa.y + xb.x);
+    A[l * n + kx] = mk<C>(xa.x - xb.y, xa.y + xb.x);
   }
   __syncthreads();
-  double2* R = fft_lines(A, B, n, npairs, n, 1, F.px, tws, +1);
+  C* Rr = fft_lines(A, B, n, npairs, n, 1, F.px, tws, +1);
   for (int t = threadIdx.x; t < npairs * n; t += blockDim.x) {
     int l = t / n, i = t % n;
     int j = 2 * (jp0 + l);
-    double2 z = R[l * n + i];
+    C z = Rr[l * n + i];
     dst[cidx(g, i, j, k)] = z.x;
     dst[cidx(g, i, j + 1, k)] = z.y;
   }
 }
 
 // Y pass (forward or inverse) on a tile of kCols kx columns of plane k
-__global__ void fft_y(FftArgs F, double2* __restrict__ spec, int sign) {
-  extern __shared__ double2 sh[];
+template <typename C>
+__global__ void fft_y(FftArgs<C> F, C* __restrict__ spec, int sign) {
+  extern __shared__ __align__(16) unsigned char shraw[];
+  C* sh = (C*)shraw;
   const Grid& g = F.g;
   int n = g.n2m;
-  double2* tws = sh;
-  double2* A = sh + n;
-  double2* B = A + kCols * n;
+  C* tws = sh;
+  C* A = sh + n;
+  C* B = A + kCols * n;
   load_tw(tws, F.twy, n);
   int kx0 = blockIdx.x * kCols, k = blockIdx.y;
   int nc = min(kCols, g.H - kx0);
   for (int t = threadIdx.x; t < kCols * n; t += blockDim.x) {
     int j = t / kCols, l = t % kCols;
-    A[t] = (l < nc) ? spec[(size_t)(kx0 + l) + (size_t)g.HP * ((size_t)j + (size_t)g.n2m * k)] : make_double2(0, 0);
+    A[t] = (l < nc) ? spec[(size_t)(kx0 + l) + (size_t)g.HP * ((size_t)j + (size_t)g.n2m * k)] : mk<C>(0, 0);
   }
   __syncthreads();
-  double2* R = fft_lines(A, B, n, kCols, 1, kCols, F.py, tws, sign);
+  C* Rr = fft_lines(A, B, n, kCols, 1, kCols, F.py, tws, sign);
   for (int t = threadIdx.x; t < kCols * n; t += blockDim.x) {
     int j = t / kCols, l = t % kCols;
-    if (l < nc) spec[(size_t)(kx0 + l) + (size_t)g.HP * ((size_t)j + (size_t)g.n2m * k)] = R[t];
+    if (l < nc) spec[(size_t)(kx0 + l) + (size_t)g.HP * ((size_t)j + (size_t)g.n2m * k)] = Rr[t];
   }
 }
 
 // Z pass: forward, scale, eigenvalue division, zero mode, inverse
-__global__ void fft_z_solve(FftArgs F, double2* __restrict__ spec) {
-  extern __shared__ double2 sh[];
+template <typename C>
+__global__ void fft_z_solve(FftArgs<C> F, C* __restrict__ spec) {
+  typedef typename Real<C>::T R;
+  extern __shared__ __align__(16) unsigned char shraw[];
+  C* sh = (C*)shraw;
   const Grid& g = F.g;
   int n = g.n3m;
-  double2* tws = sh;
-  double2* A = sh + n;
-  double2* B = A + kCols * n;
+  C* tws = sh;
+  C* A = sh + n;
+  C* B = A + kCols * n;
   load_tw(tws, F.twz, n);
   int kx0 = blockIdx.x * kCols, j = blockIdx.y;
   int nc = min(kCols, g.H - kx0);
   size_t zstride = (size_t)g.HP * g.n2m;
   for (int t = threadIdx.x; t < kCols * n; t += blockDim.x) {
     int k = t / kCols, l = t % kCols;
-    A[t] = (l < nc) ? spec[(size_t)(kx0 + l) + (size_t)g.HP * j + zstride * k] : make_double2(0, 0);
+    A[t] = (l < nc) ? spec[(size_t)(kx0 + l) + (size_t)g.HP * j + zstride * k] : mk<C>(0, 0);
   }
   __syncthreads();
-  double2* R = fft_lines(A, B, n, kCols, 1, kCols, F.pz, tws, -1);
-  double2* O = (R == A) ? B : A;
-  double a2 = F.ak2[j];
+  C* Rr = fft_lines(A, B, n, kCols, 1, kCols, F.pz, tws, -1);
+  C* O = (Rr == A) ? B : A;
+  R a2 = F.ak2[j];
   for (int t = threadIdx.x; t < kCols * n; t += blockDim.x) {
     int k = t / kCols, l = t % kCols;
-    double2 v = R[t];
+    C v = Rr[t];
     if (l < nc) {
       v.x *= F.inv_nn; v.y *= F.inv_nn;                 // buft / float(n1m*n2m*n3m)
-      double d = -F.ak3[k] - F.ak1[kx0 + l] - a2;       // -ak3(k)-ak1(i)-ak2(j)
-      if (k == 0 && kx0 + l == 0 && j == 0) v = make_double2(0.0, 0.0);
-      else { double rd = 1.0 / d; v.x *= rd; v.y *= rd; }
+      R d = -F.ak3[k] - F.ak1[kx0 + l] - a2;            // -ak3(k)-ak1(i)-ak2(j)
+      if (k == 0 && kx0 + l == 0 && j == 0) v = mk<C>(0, 0);
+      else { R rd = R(1) / d; v.x *= rd; v.y *= rd; }
     } else {
-      v = make_double2(0.0, 0.0);
+      v = mk<C>(0, 0);
     }
-    R[t] = v;
+    Rr[t] = v;
   }
   __syncthreads();
-  double2* S = fft_lines(R, O, n, kCols, 1, kCols, F.pz, tws, +1);
+  C* S = fft_lines(Rr, O, n, kCols, 1, kCols, F.pz, tws, +1);
   for (int t = threadIdx.x; t < kCols * n; t += blockDim.x) {
     int k = t / kCols, l = t % kCols;
     if (l < nc) spec[(size_t)(kx0 + l) + (size_t)g.HP * j + zstride * k] = S[t];
   }
 }
 
-// twiddle tables per context
+// twiddle and eigenvalue tables per context (FP64 and FP32)
 struct FftCache {
   Ctx* c = nullptr;
   double2 *twx = nullptr, *twy = nullptr, *twz = nullptr;
+  float2 *ftwx = nullptr, *ftwy = nullptr, *ftwz = nullptr;
+  float *fak1 = nullptr, *fak2 = nullptr, *fak3 = nullptr;
 };
 static std::vector<FftCache> g_fft;
 
-static double2* make_tw(Ctx* c, int n) {
-  std::vector<double2> h(n);
+template <typename C>
+static C* make_tw(Ctx* c, int n) {
+  std::vector<C> h(n);
   for (int m = 0; m < n; ++m) {
     double a = 2.0 * M_PI * (double)m / (double)n;
-    h[m] = make_double2(std::cos(a), -std::sin(a));
+    h[m].x = std::cos(a);
+    h[m].y = -std::sin(a);
   }
-  double2* d = nullptr;
-  if (!cuda_ok(c, cudaMalloc(&d, sizeof(double2) * n), "twiddles")) return nullptr;
-  cudaMemcpy(d, h.data(), sizeof(double2) * n, cudaMemcpyHostToDevice);
+  C* d = nullptr;
+  if (!cuda_ok(c, cudaMalloc(&d, sizeof(C) * n), "twiddles")) return nullptr;
+  cudaMemcpy(d, h.data(), sizeof(C) * n, cudaMemcpyHostToDevice);
+  return d;
+}
+
+static float* make_fak(Ctx* c, const double* ak, int n) {
+  std::vector<double> h(n);
+  cudaMemcpy(h.data(), ak, sizeof(double) * n, cudaMemcpyDeviceToHost);
+  std::vector<float> f(h.begin(), h.end());
+  float* d = nullptr;
+  if (!cuda_ok(c, cudaMalloc(&d, sizeof(float) * n), "eigenvalues")) return nullptr;
+  cudaMemcpy(d, f.data(), sizeof(float) * n, cudaMemcpyHostToDevice);
   return d;
 }
 
@@ -278,9 +310,15 @@ static FftCache* fft_of(Ctx* c) {
     if (e.c == c) return &e;
   FftCache f;
   f.c = c;
-  f.twx = make_tw(c, c->g.n1m);
-  f.twy = make_tw(c, c->g.n2m);
-  f.twz = make_tw(c, c->g.n3m);
+  f.twx = make_tw<double2>(c, c->g.n1m);
+  f.twy = make_tw<double2>(c, c->g.n2m);
+  f.twz = make_tw<double2>(c, c->g.n3m);
+  f.ftwx = make_tw<float2>(c, c->g.n1m);
+  f.ftwy = make_tw<float2>(c, c->g.n2m);
+  f.ftwz = make_tw<float2>(c, c->g.n3m);
+  f.fak1 = make_fak(c, c->ak1, c->g.n1m);
+  f.fak2 = make_fak(c, c->ak2, c->g.n2m);
+  f.fak3 = make_fak(c, c->ak3, c->g.n3m);
   g_fft.push_back(f);
   return &g_fft.back();
 }
@@ -288,44 +326,65 @@ static FftCache* fft_of(Ctx* c) {
 void fft_free(Ctx* c) {
   for (size_t q = 0; q < g_fft.size(); ++q)
     if (g_fft[q].c == c) {
-      cudaFree(g_fft[q].twx); cudaFree(g_fft[q].twy); cudaFree(g_fft[q].twz);
+      FftCache& f = g_fft[q];
+      cudaFree(f.twx); cudaFree(f.twy); cudaFree(f.twz);
+      cudaFree(f.ftwx); cudaFree(f.ftwy); cudaFree(f.ftwz);
+      cudaFree(f.fak1); cudaFree(f.fak2); cudaFree(f.fak3);
       g_fft.erase(g_fft.begin() + q);
       return;
     }
+}
+
+template <typename C>
+static void phcalc_launch(Ctx* c, FftArgs<C> F, const double* src, typename Real<C>::T* dst, const char* tag) {
+  const Grid& g = c->g;
+  C* spec = (C*)c->spec;
+  size_t smx = sizeof(C) * (g.n1m + 2 * kRowPairs * g.n1m);
+  size_t smy = sizeof(C) * (g.n2m + 2 * kCols * g.n2m);
+  size_t smz = sizeof(C) * (g.n3m + 2 * kCols * g.n3m);
+  cudaFuncSetAttribute((const void*)fft_x_fwd<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  cudaFuncSetAttribute((const void*)fft_x_inv<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  cudaFuncSetAttribute((const void*)fft_y<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  cudaFuncSetAttribute((const void*)fft_z_solve<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  dim3 gx(div_up(g.n2m / 2, kRowPairs), g.n3m);
+  dim3 gy(div_up(g.H, kCols), g.n3m);
+  dim3 gz(div_up(g.H, kCols), g.n2m);
+  bool f32 = sizeof(C) == sizeof(float2);
+  { MIBM_PROF(c, f32 ? "fft_x_fwd_f32" : "fft_x_fwd"); fft_x_fwd<C><<<gx, 256, smx, c->stream>>>(F, src, spec); }
+  { MIBM_PROF(c, f32 ? "fft_y_f32" : "fft_y"); fft_y<C><<<gy, 256, smy, c->stream>>>(F, spec, -1); }
+  { MIBM_PROF(c, f32 ? "fft_z_solve_f32" : "fft_z_solve"); fft_z_solve<C><<<gz, 256, smz, c->stream>>>(F, spec); }
+  { MIBM_PROF(c, f32 ? "fft_y_f32" : "fft_y"); fft_y<C><<<gy, 256, smy, c->stream>>>(F, spec, +1); }
+  { MIBM_PROF(c, f32 ? "fft_x_inv_f32" : "fft_x_inv"); fft_x_inv<C><<<gx, 256, smx, c->stream>>>(F, spec, dst); }
+  c->launches += 5;
+  MIBM_LAUNCH_CHECK(c, tag);
 }
 
 void k_phcalc(Ctx* c) {
   const Grid& g = c->g;
   FftCache* fc = fft_of(c);
   if (!fc->twx || !fc->twy || !fc->twz) return;
-  FftArgs F;
+  FftArgs<double2> F;
   F.g = g;
   F.px = make_plan(g.n1m); F.py = make_plan(g.n2m); F.pz = make_plan(g.n3m);
   F.twx = fc->twx; F.twy = fc->twy; F.twz = fc->twz;
   F.ak1 = c->ak1; F.ak2 = c->ak2; F.ak3 = c->ak3;
   F.inv_nn = 1.0 / ((double)g.n1m * (double)g.n2m * (double)g.n3m);
-  double* dph = c->df[MIBM_F_DPH];
-  size_t smx = sizeof(double2) * (g.n1m + 2 * kRowPairs * g.n1m);
-  size_t smy = sizeof(double2) * (g.n2m + 2 * kCols * g.n2m);
-  size_t smz = sizeof(double2) * (g.n3m + 2 * kCols * g.n3m);
-  static bool attr_done = false;
-  if (!attr_done) {
-    cudaFuncSetAttribute((const void*)fft_x_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute((const void*)fft_x_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute((const void*)fft_y, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute((const void*)fft_z_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr_done = true;
-  }
-  dim3 gx(div_up(g.n2m / 2, kRowPairs), g.n3m);
-  dim3 gy(div_up(g.H, kCols), g.n3m);
-  dim3 gz(div_up(g.H, kCols), g.n2m);
-  { MIBM_PROF(c, "fft_x_fwd"); fft_x_fwd<<<gx, 256, smx, c->stream>>>(F, dph, c->spec); }
-  { MIBM_PROF(c, "fft_y"); fft_y<<<gy, 256, smy, c->stream>>>(F, c->spec, -1); }
-  { MIBM_PROF(c, "fft_z_solve"); fft_z_solve<<<gz, 256, smz, c->stream>>>(F, c->spec); }
-  { MIBM_PROF(c, "fft_y"); fft_y<<<gy, 256, smy, c->stream>>>(F, c->spec, +1); }
-  { MIBM_PROF(c, "fft_x_inv"); fft_x_inv<<<gx, 256, smx, c->stream>>>(F, c->spec, dph); }
-  c->launches += 5;
-  MIBM_LAUNCH_CHECK(c, "phcalc");
+  phcalc_launch<double2>(c, F, c->df[MIBM_F_DPH], c->df[MIBM_F_DPH], "phcalc");
+}
+
+// Precision form: the same solve in FP32 on the FP64 right-hand side
+// `src`, result phi in FP32.
+void k_phcalc_f32(Ctx* c, const double* src, float* phi) {
+  const Grid& g = c->g;
+  FftCache* fc = fft_of(c);
+  if (!fc->ftwx || !fc->fak1) return;
+  FftArgs<float2> F;
+  F.g = g;
+  F.px = make_plan(g.n1m); F.py = make_plan(g.n2m); F.pz = make_plan(g.n3m);
+  F.twx = fc->ftwx; F.twy = fc->ftwy; F.twz = fc->ftwz;
+  F.ak1 = fc->fak1; F.ak2 = fc->fak2; F.ak3 = fc->fak3;
+  F.inv_nn = (float)(1.0 / ((double)g.n1m * (double)g.n2m * (double)g.n3m));
+  phcalc_launch<float2>(c, F, src, phi, "phcalc_f32");
 }
 
 }  // namespace mibm

@@ -71,93 +71,99 @@ static StencilArgs make_args(Ctx* c) {
   (void)dip; (void)dim; (void)djp; (void)djm; (void)dkp; (void)dkm; (void)P;
 
 // ---------------------------------------------------------------------
-// explicit terms
+// explicit terms, templated on the compute type R: R = double is the plain
+// FP64 form (bit-identical to a double-only build), R = float the precision
+// form (fields stay FP64 in memory and are rounded once on load).
 // ---------------------------------------------------------------------
-__device__ __forceinline__ double h_x(const StencilArgs& A, size_t c0, ptrdiff_t dip, ptrdiff_t dim, ptrdiff_t djp,
-                                      ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm) {
+template <typename R>
+__device__ __forceinline__ R h_x(const StencilArgs& A, size_t c0, ptrdiff_t dip, ptrdiff_t dim, ptrdiff_t djp,
+                                 ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm) {
   const Grid& g = A.g;
   const double* vx = A.vx; const double* vy = A.vy; const double* vz = A.vz;
-  double udx1 = g.dx1 * 0.25, udx2 = g.dx2 * 0.25, udx3 = g.dx3 * 0.25;
-  double vxc = vx[c0];
-  double a = vx[c0 + dip] + vxc, b = vx[c0 + dim] + vxc;
-  double h11 = (a * a - b * b) * udx1;
-  double h12 = ((vy[c0 + djp] + vy[c0 + dim + djp]) * (vx[c0 + djp] + vxc) -
-                (vy[c0] + vy[c0 + dim]) * (vxc + vx[c0 + djm])) * udx2;
-  double h13 = ((vz[c0 + dkp] + vz[c0 + dim + dkp]) * (vx[c0 + dkp] + vxc) -
-                (vz[c0] + vz[c0 + dim]) * (vxc + vx[c0 + dkm])) * udx3;
-  double h = -(h11 + h12 + h13);
-  if (A.forcing) h = h + A.vofx[c0] * A.forcx[c0] / g.xlen;
+  R udx1 = R(g.dx1 * 0.25), udx2 = R(g.dx2 * 0.25), udx3 = R(g.dx3 * 0.25);
+  R vxc = R(vx[c0]);
+  R a = R(vx[c0 + dip]) + vxc, b = R(vx[c0 + dim]) + vxc;
+  R h11 = (a * a - b * b) * udx1;
+  R h12 = ((R(vy[c0 + djp]) + R(vy[c0 + dim + djp])) * (R(vx[c0 + djp]) + vxc) -
+           (R(vy[c0]) + R(vy[c0 + dim])) * (vxc + R(vx[c0 + djm]))) * udx2;
+  R h13 = ((R(vz[c0 + dkp]) + R(vz[c0 + dim + dkp])) * (R(vx[c0 + dkp]) + vxc) -
+           (R(vz[c0]) + R(vz[c0 + dim])) * (vxc + R(vx[c0 + dkm]))) * udx3;
+  R h = -(h11 + h12 + h13);
+  if (A.forcing) h = h + R(A.vofx[c0]) * R(A.forcx[c0]) / R(g.xlen);
   return h;
 }
 
-__device__ __forceinline__ double h_y(const StencilArgs& A, size_t c0, ptrdiff_t dip, ptrdiff_t dim, ptrdiff_t djp,
-                                      ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm) {
+template <typename R>
+__device__ __forceinline__ R h_y(const StencilArgs& A, size_t c0, ptrdiff_t dip, ptrdiff_t dim, ptrdiff_t djp,
+                                 ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm) {
   const Grid& g = A.g;
   const double* vx = A.vx; const double* vy = A.vy; const double* vz = A.vz;
-  double udx1 = g.dx1 * 0.25, udx2 = g.dx2 * 0.25, udx3 = g.dx3 * 0.25;
-  double vyc = vy[c0];
-  double h21 = ((vy[c0 + dip] + vyc) * (vx[c0 + dip] + vx[c0 + dip + djm]) -
-                (vyc + vy[c0 + dim]) * (vx[c0] + vx[c0 + djm])) * udx1;
-  double a = vy[c0 + djp] + vyc, b = vy[c0 + djm] + vyc;
-  double h22 = (a * a - b * b) * udx2;
-  double h23 = ((vz[c0 + dkp] + vz[c0 + djm + dkp]) * (vy[c0 + dkp] + vyc) -
-                (vz[c0] + vz[c0 + djm]) * (vyc + vy[c0 + dkm])) * udx3;
-  double h = -(h21 + h22 + h23);
-  if (A.forcing) h = h + A.vofy[c0] * A.forcy[c0] / g.ylen;
+  R udx1 = R(g.dx1 * 0.25), udx2 = R(g.dx2 * 0.25), udx3 = R(g.dx3 * 0.25);
+  R vyc = R(vy[c0]);
+  R h21 = ((R(vy[c0 + dip]) + vyc) * (R(vx[c0 + dip]) + R(vx[c0 + dip + djm])) -
+           (vyc + R(vy[c0 + dim])) * (R(vx[c0]) + R(vx[c0 + djm]))) * udx1;
+  R a = R(vy[c0 + djp]) + vyc, b = R(vy[c0 + djm]) + vyc;
+  R h22 = (a * a - b * b) * udx2;
+  R h23 = ((R(vz[c0 + dkp]) + R(vz[c0 + djm + dkp])) * (R(vy[c0 + dkp]) + vyc) -
+           (R(vz[c0]) + R(vz[c0 + djm])) * (vyc + R(vy[c0 + dkm]))) * udx3;
+  R h = -(h21 + h22 + h23);
+  if (A.forcing) h = h + R(A.vofy[c0]) * R(A.forcy[c0]) / R(g.ylen);
   return h;
 }
 
-__device__ __forceinline__ double h_z(const StencilArgs& A, size_t c0, ptrdiff_t dip, ptrdiff_t dim, ptrdiff_t djp,
-                                      ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm, const StepParams& p) {
+template <typename R>
+__device__ __forceinline__ R h_z(const StencilArgs& A, size_t c0, ptrdiff_t dip, ptrdiff_t dim, ptrdiff_t djp,
+                                 ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm, const StepParams& p) {
   const Grid& g = A.g;
   const double* vx = A.vx; const double* vy = A.vy; const double* vz = A.vz;
-  double udx1 = g.dx1 * 0.25, udx2 = g.dx2 * 0.25, udx3 = g.dx3 * 0.25;
-  double vzc = vz[c0];
-  double h31 = ((vx[c0 + dip] + vx[c0 + dip + dkm]) * (vz[c0 + dip] + vzc) -
-                (vx[c0] + vx[c0 + dkm]) * (vzc + vz[c0 + dim])) * udx1;
-  double h32 = ((vy[c0 + djp] + vy[c0 + djp + dkm]) * (vz[c0 + djp] + vzc) -
-                (vy[c0] + vy[c0 + dkm]) * (vzc + vz[c0 + djm])) * udx2;
-  double a = vz[c0 + dkp] + vzc, b = vzc + vz[c0 + dkm];
-  double h33 = (a * a - b * b) * udx3;
-  double h = -(h31 + h32 + h33);
+  R udx1 = R(g.dx1 * 0.25), udx2 = R(g.dx2 * 0.25), udx3 = R(g.dx3 * 0.25);
+  R vzc = R(vz[c0]);
+  R h31 = ((R(vx[c0 + dip]) + R(vx[c0 + dip + dkm])) * (R(vz[c0 + dip]) + vzc) -
+           (R(vx[c0]) + R(vx[c0 + dkm])) * (vzc + R(vz[c0 + dim]))) * udx1;
+  R h32 = ((R(vy[c0 + djp]) + R(vy[c0 + djp + dkm])) * (R(vz[c0 + djp]) + vzc) -
+           (R(vy[c0]) + R(vy[c0 + dkm])) * (vzc + R(vz[c0 + djm]))) * udx2;
+  R a = R(vz[c0 + dkp]) + vzc, b = vzc + R(vz[c0 + dkm]);
+  R h33 = (a * a - b * b) * udx3;
+  R h = -(h31 + h32 + h33);
   if (p.betagz != 0.0) {
-    double T_interp = (A.temp[c0] + A.temp[c0 + dkm]) * 0.5;
-    h = h + p.betagz * (T_interp - p.tliq);
+    R T_interp = (R(A.temp[c0]) + R(A.temp[c0 + dkm])) * R(0.5);
+    h = h + R(p.betagz) * (T_interp - R(p.tliq));
   }
-  if (A.forcing) h = h + A.vofz[c0] * A.forcz[c0] / g.zlen;
+  if (A.forcing) h = h + R(A.vofz[c0]) * R(A.forcz[c0]) / R(g.zlen);
   return h;
 }
 
 __device__ __forceinline__ double nint_d(double x) { return round(x); }   // Fortran NINT semantics
 
-__device__ __forceinline__ double h_t(const StencilArgs& A, int i, int j, int k, size_t c0, ptrdiff_t dip,
-                                      ptrdiff_t dim, ptrdiff_t djp, ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm,
-                                      const StepParams& p) {
+template <typename R>
+__device__ __forceinline__ R h_t(const StencilArgs& A, int i, int j, int k, size_t c0, ptrdiff_t dip, ptrdiff_t dim,
+                                 ptrdiff_t djp, ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm, const StepParams& p) {
   const Grid& g = A.g;
   const double* vx = A.vx; const double* vy = A.vy; const double* vz = A.vz; const double* T = A.temp;
-  double udx1 = g.dx1 * 0.5, udx2 = g.dx2 * 0.5, udx3 = g.dx3 * 0.5;
-  double tc = T[c0], tip = T[c0 + dip], tim = T[c0 + dim], tjp = T[c0 + djp], tjm = T[c0 + djm];
-  double tkp = T[c0 + dkp], tkm = T[c0 + dkm];
-  double h31 = (vx[c0 + dip] * (tip + tc) - vx[c0] * (tc + tim)) * udx1;
-  double h32 = (vy[c0 + djp] * (tjp + tc) - vy[c0] * (tc + tjm)) * udx2;
-  double h33 = (vz[c0 + dkp] * (tkp + tc) - vz[c0] * (tc + tkm)) * udx3;
-  double vp = A.vofp[c0];
-  double ht = -(h31 + h32 + h33) * vp;
-  double sv = 1.0 - vp;
-  if (sv != 0.0) {
-    // solid-body advection, hdnlte.f90:94-153 (Fortran indices i+1, j+1, k+1)
+  R udx1 = R(g.dx1 * 0.5), udx2 = R(g.dx2 * 0.5), udx3 = R(g.dx3 * 0.5);
+  R tc = R(T[c0]), tip = R(T[c0 + dip]), tim = R(T[c0 + dim]), tjp = R(T[c0 + djp]), tjm = R(T[c0 + djm]);
+  R tkp = R(T[c0 + dkp]), tkm = R(T[c0 + dkm]);
+  R h31 = (R(vx[c0 + dip]) * (tip + tc) - R(vx[c0]) * (tc + tim)) * udx1;
+  R h32 = (R(vy[c0 + djp]) * (tjp + tc) - R(vy[c0]) * (tc + tjm)) * udx2;
+  R h33 = (R(vz[c0 + dkp]) * (tkp + tc) - R(vz[c0]) * (tc + tkm)) * udx3;
+  R vp = R(A.vofp[c0]);
+  R ht = -(h31 + h32 + h33) * vp;
+  R sv = R(1.0) - vp;
+  if (sv != R(0.0)) {
+    // solid-body advection, hdnlte.f90:94-153 (Fortran indices i+1, j+1, k+1);
+    // positions and the rigid-body velocity in FP64
     int fi = i + 1, fj = j + 1, fk = k + 1;
     double r0 = A.xc[fi + A.coff] - p.pos[0], r1 = A.ym[fj + A.coff] - p.pos[1], r2 = A.zm[fk + A.coff] - p.pos[2];
     r0 = r0 - g.xlen * nint_d(r0 / g.xlen); r1 = r1 - g.ylen * nint_d(r1 / g.ylen); r2 = r2 - g.zlen * nint_d(r2 / g.zlen);
     double u_imh = p.vel[0] + p.om[1] * r2 - p.om[2] * r1;
-    h31 = u_imh * (tip - tim) * udx1;
+    h31 = R(u_imh) * (tip - tim) * udx1;
     r0 = A.xm[fi + A.coff] - p.pos[0]; r1 = A.yc[fj + A.coff] - p.pos[1]; r2 = A.zm[fk + A.coff] - p.pos[2];
     r0 = r0 - g.xlen * nint_d(r0 / g.xlen); r1 = r1 - g.ylen * nint_d(r1 / g.ylen); r2 = r2 - g.zlen * nint_d(r2 / g.zlen);
     double v_jmh = p.vel[1] + p.om[2] * r0 - p.om[0] * r2;
-    h32 = v_jmh * (tjp - tjm) * udx2;
+    h32 = R(v_jmh) * (tjp - tjm) * udx2;
     r0 = A.xm[fi + A.coff] - p.pos[0]; r1 = A.ym[fj + A.coff] - p.pos[1]; r2 = A.zc[fk + A.coff] - p.pos[2];
     double w_kmh = p.vel[2] + p.om[0] * r1 - p.om[1] * r0;
-    h33 = w_kmh * (tkp - tkm) * udx3;
+    h33 = R(w_kmh) * (tkp - tkm) * udx3;
     ht = ht - (h31 + h32 + h33) * sv;
   }
   return ht;
@@ -167,45 +173,48 @@ __global__ void hdnl_kernel(StencilArgs A, int which, const StepParams* __restri
   CELL_INDEX
   StepParams p = *pp;
   double h;
-  if (which == 0) h = h_x(A, c0, dip, dim, djp, djm, dkp, dkm);
-  else if (which == 1) h = h_y(A, c0, dip, dim, djp, djm, dkp, dkm);
-  else if (which == 2) h = h_z(A, c0, dip, dim, djp, djm, dkp, dkm, p);
-  else h = h_t(A, i, j, k, c0, dip, dim, djp, djm, dkp, dkm, p);
+  if (which == 0) h = h_x<double>(A, c0, dip, dim, djp, djm, dkp, dkm);
+  else if (which == 1) h = h_y<double>(A, c0, dip, dim, djp, djm, dkp, dkm);
+  else if (which == 2) h = h_z<double>(A, c0, dip, dim, djp, djm, dkp, dkm, p);
+  else h = h_t<double>(A, i, j, k, c0, dip, dim, djp, djm, dkp, dkm, p);
   out[c0] = h;
 }
 
 // ---------------------------------------------------------------------
 // RHS of the factored implicit step
 // ---------------------------------------------------------------------
-__device__ __forceinline__ double lap(const double* q, size_t c0, ptrdiff_t dip, ptrdiff_t dim, ptrdiff_t djp,
-                                      ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm, const Grid& g, bool fortran_order_t) {
-  double qc = q[c0];
-  double d1 = (q[c0 + dip] - 2.0 * qc + q[c0 + dim]) * g.dx1q;
-  double d2 = (q[c0 + djp] - 2.0 * qc + q[c0 + djm]) * g.dx2q;
-  double d3 = (q[c0 + dkp] - 2.0 * qc + q[c0 + dkm]) * g.dx3q;
+template <typename R>
+__device__ __forceinline__ R lap(const double* q, size_t c0, ptrdiff_t dip, ptrdiff_t dim, ptrdiff_t djp,
+                                 ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm, const Grid& g, bool fortran_order_t) {
+  R qc = R(q[c0]);
+  R d1 = (R(q[c0 + dip]) - R(2.0) * qc + R(q[c0 + dim])) * R(g.dx1q);
+  R d2 = (R(q[c0 + djp]) - R(2.0) * qc + R(q[c0 + djm])) * R(g.dx2q);
+  R d3 = (R(q[c0 + dkp]) - R(2.0) * qc + R(q[c0 + dkm])) * R(g.dx3q);
   // invtr1/2: d11+d22+d33 ; invtr3/invtrte: d22+d33+d11
   return fortran_order_t ? (d2 + d3) + d1 : (d1 + d2) + d3;
 }
 
-__device__ __forceinline__ double rhs_value(const StencilArgs& A, int which, double h, double ru, size_t c0,
-                                            ptrdiff_t dip, ptrdiff_t dim, ptrdiff_t djp, ptrdiff_t djm, ptrdiff_t dkp,
-                                            ptrdiff_t dkm, const StepParams& p) {
+template <typename R>
+__device__ __forceinline__ R rhs_value(const StencilArgs& A, int which, R h, R ru, size_t c0, ptrdiff_t dip,
+                                       ptrdiff_t dim, ptrdiff_t djp, ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm,
+                                       const StepParams& p) {
   const Grid& g = A.g;
+  R ga = R(p.ga), ro = R(p.ro), alre = R(p.alre), dt = R(p.dt);
   if (which == 0) {
-    double dcvx = lap(A.vx, c0, dip, dim, djp, djm, dkp, dkm, g, false);
-    double dpx11 = (A.pr[c0] - A.pr[c0 + dim]) * (g.dx1 * p.al);
-    return (p.ga * h + p.ro * ru + p.alre * dcvx - dpx11) * p.dt;
+    R dcvx = lap<R>(A.vx, c0, dip, dim, djp, djm, dkp, dkm, g, false);
+    R dpx11 = (R(A.pr[c0]) - R(A.pr[c0 + dim])) * R(g.dx1 * p.al);
+    return (ga * h + ro * ru + alre * dcvx - dpx11) * dt;
   } else if (which == 1) {
-    double dcvy = lap(A.vy, c0, dip, dim, djp, djm, dkp, dkm, g, false);
-    double dpx22 = (A.pr[c0] - A.pr[c0 + djm]) * (g.dx2 * p.al);
-    return (p.ga * h + p.ro * ru + p.alre * dcvy - dpx22) * p.dt;
+    R dcvy = lap<R>(A.vy, c0, dip, dim, djp, djm, dkp, dkm, g, false);
+    R dpx22 = (R(A.pr[c0]) - R(A.pr[c0 + djm])) * R(g.dx2 * p.al);
+    return (ga * h + ro * ru + alre * dcvy - dpx22) * dt;
   } else if (which == 2) {
-    double dcvz = lap(A.vz, c0, dip, dim, djp, djm, dkp, dkm, g, true);
-    double dpx33 = (A.pr[c0] - A.pr[c0 + dkm]) * (p.al * g.dx3);
-    return (p.ga * h + p.ro * ru + p.alre * dcvz - dpx33) * p.dt;
+    R dcvz = lap<R>(A.vz, c0, dip, dim, djp, djm, dkp, dkm, g, true);
+    R dpx33 = (R(A.pr[c0]) - R(A.pr[c0 + dkm])) * R(p.al * g.dx3);
+    return (ga * h + ro * ru + alre * dcvz - dpx33) * dt;
   }
-  double dcte = lap(A.temp, c0, dip, dim, djp, djm, dkp, dkm, g, true);
-  return p.dt * (p.ga * h + p.ro * ru) + (p.al / p.pec) * dcte * p.dt;
+  R dcte = lap<R>(A.temp, c0, dip, dim, djp, djm, dkp, dkm, g, true);
+  return dt * (ga * h + ro * ru) + R(p.al / p.pec) * dcte * dt;
 }
 
 // invtr drop-in: reads H from the explicit-term array, writes rhs, ru = H
@@ -214,21 +223,23 @@ __global__ void invtr_rhs_kernel(StencilArgs A, int which, const StepParams* __r
   CELL_INDEX
   StepParams p = *pp;
   double h = H[c0];
-  rhs[c0] = rhs_value(A, which, h, ru[c0], c0, dip, dim, djp, djm, dkp, dkm, p);
+  rhs[c0] = rhs_value<double>(A, which, h, ru[c0], c0, dip, dim, djp, djm, dkp, dkm, p);
   ru[c0] = h;
 }
 
-// fused path: explicit term computed in registers (hdnl + invtr RHS)
-__global__ void fused_rhs_kernel(StencilArgs A, int which, const StepParams* __restrict__ pp, double* __restrict__ ru,
-                                 double* __restrict__ rhs) {
+// fused path: explicit term computed in registers (hdnl + invtr RHS); R is
+// the compute type, ru and rhs are stored in R
+template <typename R>
+__global__ void fused_rhs_kernel(StencilArgs A, int which, const StepParams* __restrict__ pp, R* __restrict__ ru,
+                                 R* __restrict__ rhs) {
   CELL_INDEX
   StepParams p = *pp;
-  double h;
-  if (which == 0) h = h_x(A, c0, dip, dim, djp, djm, dkp, dkm);
-  else if (which == 1) h = h_y(A, c0, dip, dim, djp, djm, dkp, dkm);
-  else if (which == 2) h = h_z(A, c0, dip, dim, djp, djm, dkp, dkm, p);
-  else h = h_t(A, i, j, k, c0, dip, dim, djp, djm, dkp, dkm, p);
-  rhs[c0] = rhs_value(A, which, h, ru[c0], c0, dip, dim, djp, djm, dkp, dkm, p);
+  R h;
+  if (which == 0) h = h_x<R>(A, c0, dip, dim, djp, djm, dkp, dkm);
+  else if (which == 1) h = h_y<R>(A, c0, dip, dim, djp, djm, dkp, dkm);
+  else if (which == 2) h = h_z<R>(A, c0, dip, dim, djp, djm, dkp, dkm, p);
+  else h = h_t<R>(A, i, j, k, c0, dip, dim, djp, djm, dkp, dkm, p);
+  rhs[c0] = rhs_value<R>(A, which, h, ru[c0], c0, dip, dim, djp, djm, dkp, dkm, p);
   ru[c0] = h;
 }
 
@@ -257,6 +268,44 @@ __global__ void updvp_kernel(StencilArgs A, const StepParams* __restrict__ pp, c
   vx[c0] = (vx[c0] - mx) - (loc - dph[c0 + dim]) * udx1;
   vy[c0] = (vy[c0] - my) - (loc - dph[c0 + djm]) * udx2;
   vz[c0] = (vz[c0] - mz) - (loc - dph[c0 + dkm]) * udx3;
+}
+
+// precision form: u -= al dt grad(phi) with phi from the FP32 Poisson solve
+// (FP64 update of the FP64 velocity), optional mean-force removal
+__global__ void updvp_f32_kernel(StencilArgs A, const StepParams* __restrict__ pp, const float* __restrict__ phi,
+                                 double* __restrict__ vx, double* __restrict__ vy, double* __restrict__ vz,
+                                 const double* __restrict__ mean3) {
+  CELL_INDEX
+  double al = pp->al, dt = pp->dt;
+  double udx1 = al * dt * g.dx1, udx2 = al * dt * g.dx2, udx3 = al * dt * g.dx3;
+  double loc = phi[c0];
+  double mx = 0.0, my = 0.0, mz = 0.0;
+  if (mean3) { mx = mean3[0]; my = mean3[1]; mz = mean3[2]; }
+  vx[c0] = (vx[c0] - mx) - (loc - (double)phi[c0 + dim]) * udx1;
+  vy[c0] = (vy[c0] - my) - (loc - (double)phi[c0 + djm]) * udx2;
+  vz[c0] = (vz[c0] - mz) - (loc - (double)phi[c0 + dkm]) * udx3;
+}
+
+// precision form: p += phi - al beta lap(phi), increment in FP32
+__global__ void prcalc_f32_kernel(StencilArgs A, const StepParams* __restrict__ pp, const float* __restrict__ phi,
+                                  double* __restrict__ pr) {
+  CELL_INDEX
+  float be = (float)(pp->al * pp->beta);
+  float d = phi[c0];
+  float inc = d - be * ((phi[c0 + dip] - 2.0f * d + phi[c0 + dim]) * (float)g.dx1q +
+                        (phi[c0 + djp] - 2.0f * d + phi[c0 + djm]) * (float)g.dx2q +
+                        (phi[c0 + dkp] - 2.0f * d + phi[c0 + dkm]) * (float)g.dx3q);
+  pr[c0] = pr[c0] + (double)inc;
+}
+
+// max |div u| (divgck semantics, divg.f90:26-56) into bits of `out`
+__global__ void divmax_kernel(StencilArgs A, unsigned long long* __restrict__ out) {
+  CELL_INDEX
+  double dq = (A.vx[c0 + dip] - A.vx[c0]) * g.dx1 + (A.vy[c0 + djp] - A.vy[c0]) * g.dx2 +
+              (A.vz[c0 + dkp] - A.vz[c0]) * g.dx3;
+  double v = fabs(dq);
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(v));
 }
 
 __global__ void prcalc_kernel(StencilArgs A, const StepParams* __restrict__ pp, const double* __restrict__ dph,
@@ -408,11 +457,24 @@ void k_invtr_rhs(Ctx* c, int which, const StepParams* dp, double* rhs_out) {
 
 void k_fused_rhs(Ctx* c, const StepParams* dp) {
   for (int w = 0; w < 4; ++w) {
-    { MIBM_PROF(c, "fused_rhs"); fused_rhs_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), w, dp, ru_of(c, w),
-                                                                     c->rhs4 + (size_t)w * c->g.cells); }
+    { MIBM_PROF(c, "fused_rhs");
+      fused_rhs_kernel<double><<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), w, dp, ru_of(c, w),
+                                                                             c->rhs4 + (size_t)w * c->g.cells); }
     ++c->launches;
   }
   MIBM_LAUNCH_CHECK(c, "fused_rhs");
+}
+
+// precision form: FP32 explicit terms and RHS into FP32 ru / rhs buffers
+void k_fused_rhs_f32(Ctx* c, const StepParams* dp, float* ru4, float* rhs4) {
+  for (int w = 0; w < 4; ++w) {
+    { MIBM_PROF(c, "fused_rhs_f32");
+      fused_rhs_kernel<float><<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), w, dp,
+                                                                            ru4 + (size_t)w * c->g.cells,
+                                                                            rhs4 + (size_t)w * c->g.cells); }
+    ++c->launches;
+  }
+  MIBM_LAUNCH_CHECK(c, "fused_rhs_f32");
 }
 
 void k_divg(Ctx* c, const StepParams* dp) {
@@ -426,6 +488,30 @@ void k_updvp(Ctx* c, const StepParams* dp, const double* mean3) {
                                                                c->df[MIBM_F_VY], c->df[MIBM_F_VZ], mean3); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "updvp");
+}
+
+void k_updvp_f32(Ctx* c, const StepParams* dp, const float* phi, const double* mean3) {
+  { MIBM_PROF(c, "updvp_f32");
+    updvp_f32_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, phi, c->df[MIBM_F_VX],
+                                                                     c->df[MIBM_F_VY], c->df[MIBM_F_VZ], mean3); }
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "updvp_f32");
+}
+
+void k_prcalc_f32(Ctx* c, const StepParams* dp, const float* phi) {
+  { MIBM_PROF(c, "prcalc_f32");
+    prcalc_f32_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, phi, c->df[MIBM_F_PR]); }
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "prcalc_f32");
+}
+
+// max |div u| over the owned cells (device), cleared first
+void k_divmax(Ctx* c, unsigned long long* out) {
+  cudaMemsetAsync(out, 0, sizeof(unsigned long long), c->stream);
+  { MIBM_PROF(c, "divmax");
+    divmax_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), out); }
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "divmax");
 }
 
 void k_prcalc(Ctx* c, const StepParams* dp) {

@@ -134,20 +134,21 @@ void tri_free(Ctx* c) {
 // e = 0..n-1, with the factor table T (also in shared memory).  The loops
 // are unrolled by 4 with the independent loads (line values and factors)
 // issued ahead of the dependent FMA chain.
-__device__ __forceinline__ void solve_line(double* base, int stride, int n, const double* __restrict__ T) {
-  const double* a = T;
-  const double* b = T + n;
-  const double* q = T + 2 * n;
-  const double* s = T + 3 * n;
-  double ackl_b = T[4 * n + 0], api = T[4 * n + 1], ami = T[4 * n + 2], inv_den = T[4 * n + 3];
-  double rn = base[(size_t)(n - 1) * stride];
-  double y = a[0] * base[0];
+template <typename V>
+__device__ __forceinline__ void solve_line(V* base, int stride, int n, const V* __restrict__ T) {
+  const V* a = T;
+  const V* b = T + n;
+  const V* q = T + 2 * n;
+  const V* s = T + 3 * n;
+  V ackl_b = T[4 * n + 0], api = T[4 * n + 1], ami = T[4 * n + 2], inv_den = T[4 * n + 3];
+  V rn = base[(size_t)(n - 1) * stride];
+  V y = a[0] * base[0];
   base[0] = y;
   int e = 1;
   for (; e + 4 <= n - 1; e += 4) {
-    double r0 = base[(size_t)e * stride], r1 = base[(size_t)(e + 1) * stride];
-    double r2 = base[(size_t)(e + 2) * stride], r3 = base[(size_t)(e + 3) * stride];
-    double a0 = a[e] * r0, a1 = a[e + 1] * r1, a2 = a[e + 2] * r2, a3 = a[e + 3] * r3;
+    V r0 = base[(size_t)e * stride], r1 = base[(size_t)(e + 1) * stride];
+    V r2 = base[(size_t)(e + 2) * stride], r3 = base[(size_t)(e + 3) * stride];
+    V a0 = a[e] * r0, a1 = a[e + 1] * r1, a2 = a[e + 2] * r2, a3 = a[e + 3] * r3;
     y = a0 - b[e] * y;     base[(size_t)e * stride] = y;
     y = a1 - b[e + 1] * y; base[(size_t)(e + 1) * stride] = y;
     y = a2 - b[e + 2] * y; base[(size_t)(e + 2) * stride] = y;
@@ -157,11 +158,11 @@ __device__ __forceinline__ void solve_line(double* base, int stride, int n, cons
     y = a[e] * base[(size_t)e * stride] - b[e] * y;
     base[(size_t)e * stride] = y;
   }
-  double f = 0.0;   // f_n = 0
+  V f = V(0.0);   // f_n = 0
   e = n - 2;
   for (; e - 3 >= 0; e -= 4) {
-    double y0 = base[(size_t)e * stride], y1 = base[(size_t)(e - 1) * stride];
-    double y2 = base[(size_t)(e - 2) * stride], y3 = base[(size_t)(e - 3) * stride];
+    V y0 = base[(size_t)e * stride], y1 = base[(size_t)(e - 1) * stride];
+    V y2 = base[(size_t)(e - 2) * stride], y3 = base[(size_t)(e - 3) * stride];
     f = y0 + q[e] * f;     base[(size_t)e * stride] = f;
     f = y1 + q[e - 1] * f; base[(size_t)(e - 1) * stride] = f;
     f = y2 + q[e - 2] * f; base[(size_t)(e - 2) * stride] = f;
@@ -171,14 +172,15 @@ __device__ __forceinline__ void solve_line(double* base, int stride, int n, cons
     f = base[(size_t)e * stride] + q[e] * f;
     base[(size_t)e * stride] = f;
   }
-  double f1 = base[0], fnm1 = base[(size_t)(n - 2) * stride];
-  double xn = (rn * ackl_b - api * f1 - ami * fnm1) * inv_den;
+  V f1 = base[0], fnm1 = base[(size_t)(n - 2) * stride];
+  V xn = (rn * ackl_b - api * f1 - ami * fnm1) * inv_den;
   for (e = 0; e < n - 1; ++e) base[(size_t)e * stride] = xn * s[e] + base[(size_t)e * stride];
   base[(size_t)(n - 1) * stride] = xn;
 }
 
 // copy the factor table (4n + 4 doubles) into shared memory
-__device__ __forceinline__ const double* stage_table(double* sT, const double* __restrict__ T, int n) {
+template <typename V>
+__device__ __forceinline__ const V* stage_table(V* sT, const V* __restrict__ T, int n) {
   for (int q = threadIdx.x; q < 4 * n + 4; q += blockDim.x) sT[q] = T[q];
   return sT;
 }
@@ -186,19 +188,21 @@ __device__ __forceinline__ const double* stage_table(double* sT, const double* _
 constexpr int kLines = 32;
 
 // x-lines: tile = up to 32 rows (j) of one plane k.
-__global__ void solve_x_kernel(Grid g, double* __restrict__ rhs, const double* __restrict__ T) {
-  extern __shared__ double sm[];
+template <typename V>
+__global__ void solve_x_kernel(Grid g, V* __restrict__ rhs, const V* __restrict__ T) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  V* sm = (V*)smraw;
   int n = g.n1m, pitch = n + 1;
   int j0 = blockIdx.x * kLines, k = blockIdx.y;
   int nl = min(kLines, g.n2m - j0);
-  const double* sT = stage_table(sm + kLines * pitch, T, n);
+  const V* sT = stage_table(sm + kLines * pitch, T, n);
   int total = nl * n;
   for (int t0 = threadIdx.x; t0 < total; t0 += 8 * blockDim.x) {
-    double v[8];
+    V v[8];
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
       int t = t0 + u * blockDim.x;
-      v[u] = (t < total) ? rhs[cidx(g, t % n, j0 + t / n, k)] : 0.0;
+      v[u] = (t < total) ? rhs[cidx(g, t % n, j0 + t / n, k)] : V(0.0);
     }
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
@@ -213,19 +217,21 @@ __global__ void solve_x_kernel(Grid g, double* __restrict__ rhs, const double* _
 }
 
 // y-lines: tile = up to 32 adjacent i of one plane k; smem[j][l]
-__global__ void solve_y_kernel(Grid g, double* __restrict__ rhs, const double* __restrict__ T) {
-  extern __shared__ double sm[];
+template <typename V>
+__global__ void solve_y_kernel(Grid g, V* __restrict__ rhs, const V* __restrict__ T) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  V* sm = (V*)smraw;
   int n = g.n2m;
   int i0 = blockIdx.x * kLines, k = blockIdx.y;
   int nl = min(kLines, g.n1m - i0);
-  const double* sT = stage_table(sm + n * kLines, T, n);
+  const V* sT = stage_table(sm + n * kLines, T, n);
   for (int t0 = threadIdx.x; t0 < n * kLines; t0 += 8 * blockDim.x) {
-    double v[8];
+    V v[8];
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
       int t = t0 + u * blockDim.x;
       int j = t / kLines, l = t % kLines;
-      v[u] = (t < n * kLines && l < nl) ? rhs[cidx(g, i0 + l, j, k)] : 0.0;
+      v[u] = (t < n * kLines && l < nl) ? rhs[cidx(g, i0 + l, j, k)] : V(0.0);
     }
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
@@ -244,20 +250,22 @@ __global__ void solve_y_kernel(Grid g, double* __restrict__ rhs, const double* _
 
 // z-lines: tile = up to 32 adjacent i of one row j; smem[k][l]; then q += x
 // (solxk.f90:44-50), optionally leaving rhs holding the increment.
-__global__ void solve_z_kernel(Grid g, double* __restrict__ rhs, const double* __restrict__ T, double* __restrict__ q,
+template <typename V>
+__global__ void solve_z_kernel(Grid g, V* __restrict__ rhs, const V* __restrict__ T, double* __restrict__ q,
                                int write_rhs) {
-  extern __shared__ double sm[];
+  extern __shared__ __align__(16) unsigned char smraw[];
+  V* sm = (V*)smraw;
   int n = g.n3m;
   int i0 = blockIdx.x * kLines, j = blockIdx.y;
   int nl = min(kLines, g.n1m - i0);
-  const double* sT = stage_table(sm + n * kLines, T, n);
+  const V* sT = stage_table(sm + n * kLines, T, n);
   for (int t0 = threadIdx.x; t0 < n * kLines; t0 += 8 * blockDim.x) {
-    double v[8];
+    V v[8];
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
       int t = t0 + u * blockDim.x;
       int k = t / kLines, l = t % kLines;
-      v[u] = (t < n * kLines && l < nl) ? rhs[cidx(g, i0 + l, j, k)] : 0.0;
+      v[u] = (t < n * kLines && l < nl) ? rhs[cidx(g, i0 + l, j, k)] : V(0.0);
     }
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
@@ -272,9 +280,9 @@ __global__ void solve_z_kernel(Grid g, double* __restrict__ rhs, const double* _
     int k = t / kLines, l = t % kLines;
     if (l < nl) {
       size_t c0 = cidx(g, i0 + l, j, k);
-      double x = sm[t];
+      V x = sm[t];
       if (write_rhs) rhs[c0] = x;
-      q[c0] = q[c0] + x;
+      q[c0] = q[c0] + (double)x;
     }
   }
 }
@@ -285,6 +293,7 @@ __global__ void solve_z_kernel(Grid g, double* __restrict__ rhs, const double* _
 // not read by the previous step's copy) and copied in stream order.
 struct StepTables {
   double* dev = nullptr;
+  float* devf = nullptr;                 // FP32 copy for the precision form
   double* pinned[2] = {nullptr, nullptr};
   cudaEvent_t copied[2] = {nullptr, nullptr};
   int parity = 0, len = 0;
@@ -299,15 +308,16 @@ static StepTables* steptab_of(Ctx* c) {
   return t;
 }
 
-const double* tri_step_prepare(Ctx* c, const double betadx[3][2][3], int* len_out) {
+const double* tri_step_prepare(Ctx* c, const double betadx[3][2][3], int* len_out, const float** f32_out) {
   StepTables* st = steptab_of(c);
   int nmax = std::max(c->g.n1m, c->g.n3m);
   if (!st->dev) {
     st->len = 4 * nmax + 4;
     size_t bytes = sizeof(double) * 18 * (size_t)st->len;
     if (!cuda_ok(c, cudaMalloc(&st->dev, bytes), "step tables")) return nullptr;
+    if (!cuda_ok(c, cudaMalloc(&st->devf, bytes / 2), "step tables")) return nullptr;
     for (int q = 0; q < 2; ++q) {
-      if (!cuda_ok(c, cudaMallocHost(&st->pinned[q], bytes), "step tables")) return nullptr;
+      if (!cuda_ok(c, cudaMallocHost(&st->pinned[q], bytes + bytes / 2), "step tables")) return nullptr;
       if (!cuda_ok(c, cudaEventCreateWithFlags(&st->copied[q], cudaEventDisableTiming), "step tables")) return nullptr;
     }
   }
@@ -323,6 +333,12 @@ const double* tri_step_prepare(Ctx* c, const double betadx[3][2][3], int* len_ou
         std::copy(t.begin(), t.end(), st->pinned[p] + (size_t)((ns * 2 + f) * 3 + d) * st->len);
       }
   cudaMemcpyAsync(st->dev, st->pinned[p], sizeof(double) * 18 * (size_t)st->len, cudaMemcpyHostToDevice, c->stream);
+  if (f32_out) {
+    float* hf = (float*)(st->pinned[p] + 18 * (size_t)st->len);
+    for (size_t q = 0; q < 18 * (size_t)st->len; ++q) hf[q] = (float)st->pinned[p][q];
+    cudaMemcpyAsync(st->devf, hf, sizeof(float) * 18 * (size_t)st->len, cudaMemcpyHostToDevice, c->stream);
+    *f32_out = st->devf;
+  }
   cudaEventRecord(st->copied[p], c->stream);
   *len_out = st->len;
   return st->dev;
@@ -333,6 +349,7 @@ static void steptab_free(Ctx* c) {
     if (g_steptab[q].first == c) {
       StepTables* t = g_steptab[q].second;
       cudaFree(t->dev);
+      cudaFree(t->devf);
       for (int p = 0; p < 2; ++p) {
         if (t->pinned[p]) cudaFreeHost(t->pinned[p]);
         if (t->copied[p]) cudaEventDestroy(t->copied[p]);
@@ -349,32 +366,44 @@ static bool smem_ok(Ctx* c, const void* fn, size_t bytes) {
   return true;
 }
 
-void k_solve_x_T(Ctx* c, double* rhs, const double* T) {
-  size_t sm = ((size_t)kLines * (c->g.n1m + 1) + 4 * (size_t)c->g.n1m + 4) * sizeof(double);
-  if (!smem_ok(c, (const void*)solve_x_kernel, sm)) return;
+template <typename V>
+static void solve_x_launch(Ctx* c, V* rhs, const V* T, const char* name) {
+  size_t sm = ((size_t)kLines * (c->g.n1m + 1) + 4 * (size_t)c->g.n1m + 4) * sizeof(V);
+  if (!smem_ok(c, (const void*)solve_x_kernel<V>, sm)) return;
   dim3 grid(div_up(c->g.n2m, kLines), c->g.n3m);
-  { MIBM_PROF(c, "solve_x"); solve_x_kernel<<<grid, 128, sm, c->stream>>>(c->g, rhs, T); }
+  { MIBM_PROF(c, name); solve_x_kernel<V><<<grid, 128, sm, c->stream>>>(c->g, rhs, T); }
   ++c->launches;
-  MIBM_LAUNCH_CHECK(c, "solve_x");
+  MIBM_LAUNCH_CHECK(c, name);
 }
 
-void k_solve_y_T(Ctx* c, double* rhs, const double* T) {
-  size_t sm = ((size_t)kLines * c->g.n2m + 4 * (size_t)c->g.n2m + 4) * sizeof(double);
-  if (!smem_ok(c, (const void*)solve_y_kernel, sm)) return;
+template <typename V>
+static void solve_y_launch(Ctx* c, V* rhs, const V* T, const char* name) {
+  size_t sm = ((size_t)kLines * c->g.n2m + 4 * (size_t)c->g.n2m + 4) * sizeof(V);
+  if (!smem_ok(c, (const void*)solve_y_kernel<V>, sm)) return;
   dim3 grid(div_up(c->g.n1m, kLines), c->g.n3m);
-  { MIBM_PROF(c, "solve_y"); solve_y_kernel<<<grid, 128, sm, c->stream>>>(c->g, rhs, T); }
+  { MIBM_PROF(c, name); solve_y_kernel<V><<<grid, 128, sm, c->stream>>>(c->g, rhs, T); }
   ++c->launches;
-  MIBM_LAUNCH_CHECK(c, "solve_y");
+  MIBM_LAUNCH_CHECK(c, name);
 }
 
-void k_solve_z_T(Ctx* c, double* rhs, const double* T, double* q, int write_rhs) {
-  size_t sm = ((size_t)kLines * c->g.n3m + 4 * (size_t)c->g.n3m + 4) * sizeof(double);
-  if (!smem_ok(c, (const void*)solve_z_kernel, sm)) return;
+template <typename V>
+static void solve_z_launch(Ctx* c, V* rhs, const V* T, double* q, int write_rhs, const char* name) {
+  size_t sm = ((size_t)kLines * c->g.n3m + 4 * (size_t)c->g.n3m + 4) * sizeof(V);
+  if (!smem_ok(c, (const void*)solve_z_kernel<V>, sm)) return;
   dim3 grid(div_up(c->g.n1m, kLines), c->g.n2m);
-  { MIBM_PROF(c, "solve_z"); solve_z_kernel<<<grid, 128, sm, c->stream>>>(c->g, rhs, T, q, write_rhs); }
+  { MIBM_PROF(c, name); solve_z_kernel<V><<<grid, 128, sm, c->stream>>>(c->g, rhs, T, q, write_rhs); }
   ++c->launches;
-  MIBM_LAUNCH_CHECK(c, "solve_z");
+  MIBM_LAUNCH_CHECK(c, name);
 }
+
+void k_solve_x_T(Ctx* c, double* rhs, const double* T) { solve_x_launch<double>(c, rhs, T, "solve_x"); }
+void k_solve_y_T(Ctx* c, double* rhs, const double* T) { solve_y_launch<double>(c, rhs, T, "solve_y"); }
+void k_solve_z_T(Ctx* c, double* rhs, const double* T, double* q, int write_rhs) {
+  solve_z_launch<double>(c, rhs, T, q, write_rhs, "solve_z");
+}
+void k_solve_x_f32(Ctx* c, float* rhs, const float* T) { solve_x_launch<float>(c, rhs, T, "solve_x_f32"); }
+void k_solve_y_f32(Ctx* c, float* rhs, const float* T) { solve_y_launch<float>(c, rhs, T, "solve_y_f32"); }
+void k_solve_z_f32(Ctx* c, float* rhs, const float* T, double* q) { solve_z_launch<float>(c, rhs, T, q, 0, "solve_z_f32"); }
 
 void k_solve_x(Ctx* c, double* rhs, double betadx) {
   const double* T = table_for(c, c->g.n1m, betadx);
@@ -467,11 +496,11 @@ extern "C" int mibm_solxi_noalloc(double* rhs, int n1m, int n2m, int n3m, int pi
   g.plane = (size_t)pitch * n2m; g.cells = g.plane * n3m;
   size_t sm = ((size_t)kLines * (n1m + 1) + 4 * (size_t)n1m + 4) * sizeof(double);
   if (sm > 48 * 1024 &&
-      cudaFuncSetAttribute((const void*)solve_x_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
+      cudaFuncSetAttribute((const void*)solve_x_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
           cudaSuccess)
     return MIBM_ECUDA;
   dim3 grid(div_up(n2m, kLines), n3m);
-  solve_x_kernel<<<grid, 128, sm, st>>>(g, rhs, table);
+  solve_x_kernel<double><<<grid, 128, sm, st>>>(g, rhs, table);
   return cudaGetLastError() == cudaSuccess ? MIBM_OK : MIBM_ECUDA;
 }
 

@@ -1628,6 +1628,21 @@ void mibm_timer_mark_(const int* slot) {
 }
 double mibm_timer_ms_(const int* a, const int* b) { return g_marks[*b] - g_marks[*a]; }
 void mibm_profile_(const int*) {}
+void mibm_set_precision_(const int*, const int*) {}
+double mibm_divergence_max_(void) {
+  Ctx* c = cur();
+  if (!ready(c)) return -1.0;
+  const F3 &vx = c->f[MIBM_F_VX], &vy = c->f[MIBM_F_VY], &vz = c->f[MIBM_F_VZ];
+  double m = 0.0;
+  for (int k = 1; k <= c->n3m; ++k)
+    for (int j = 1; j <= c->n2m; ++j)
+      for (int i = 1; i <= c->n1m; ++i) {
+        double dq = (vx(c->ipv[i], j, k) - vx(i, j, k)) * c->dx1 + (vy(i, c->jpv[j], k) - vy(i, j, k)) * c->dx2 +
+                    (vz(i, j, k + 1) - vz(i, j, k)) * c->dx3;
+        m = std::max(m, std::fabs(dq));
+      }
+  return m;
+}
 int mibm_solxi_noalloc(double*, int, int, int, int, double, void*) { return MIBM_EINVAL; }
 int mibm_profile_count_(void) { return 0; }
 int mibm_profile_get_(const int*, char*, const int*, double*, long long*) { return MIBM_EINVAL; }
