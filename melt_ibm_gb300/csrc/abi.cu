@@ -57,10 +57,7 @@ static void invtr(Ctx* c, int which) {
   k_solve_z(c, rhs, b3, c->df[fid[which]]);
 }
 
-__global__ void cast_kernel(size_t n, const double* __restrict__ a, float* __restrict__ b) {
-  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < n) b[t] = (float)a[t];
-}
+static const int kRuFields[4] = {MIBM_F_RU1, MIBM_F_RU2, MIBM_F_RU3, MIBM_F_RUT};
 
 static bool ensure_f32(Ctx* c) {
   const Grid& g = c->g;
@@ -68,20 +65,41 @@ static bool ensure_f32(Ctx* c) {
     if (!cuda_ok(c, cudaMalloc(&c->ru32, 4 * g.cells * sizeof(float)), "ru32")) return false;
     if (!cuda_ok(c, cudaMalloc(&c->rhs32, 4 * g.cells * sizeof(float)), "rhs32")) return false;
     if (!cuda_ok(c, cudaMalloc(&c->phi32, g.cells * sizeof(float)), "phi32")) return false;
-    static const int ru[4] = {MIBM_F_RU1, MIBM_F_RU2, MIBM_F_RU3, MIBM_F_RUT};
-    for (int q = 0; q < 4; ++q) {
-      cast_kernel<<<div_up(g.cells, 256), 256, 0, c->stream>>>(g.cells, c->df[ru[q]], c->ru32 + (size_t)q * g.cells);
-      ++c->launches;
-    }
+    if (!cuda_ok(c, cudaMalloc(&c->res32, g.cells * sizeof(float)), "res32")) return false;
+    if (!cuda_ok(c, cudaMalloc(&c->q32, 5 * g.cells * sizeof(float)), "q32")) return false;
+    for (int q = 0; q < 4; ++q) k_cast_d2f(c, g.cells, c->df[kRuFields[q]], c->ru32 + (size_t)q * g.cells);
+    c->q32_valid = false;
+  }
+  if (!c->q32_valid) {
+    k_mirror_fields(c);
+    c->q32_valid = true;
   }
   return MIBM_LAUNCH_CHECK(c, "precision buffers");
 }
 
+void precision_before_download(Ctx* c, unsigned long long mask) {
+  if (c->precision != 1 || !c->ru32) return;
+  for (int q = 0; q < 4; ++q)
+    if (mask & (1ull << kRuFields[q])) k_cast_f2d(c, c->g.cells, c->ru32 + (size_t)q * c->g.cells, c->df[kRuFields[q]]);
+}
+
+void precision_after_upload(Ctx* c, unsigned long long mask) {
+  static const int prog[5] = {MIBM_F_VX, MIBM_F_VY, MIBM_F_VZ, MIBM_F_TEMP, MIBM_F_PR};
+  for (int q = 0; q < 5; ++q)
+    if (mask & (1ull << prog[q])) c->q32_valid = false;
+  if (c->precision != 1 || !c->ru32) return;
+  for (int q = 0; q < 4; ++q)
+    if (mask & (1ull << kRuFields[q])) k_cast_d2f(c, c->g.cells, c->df[kRuFields[q]], c->ru32 + (size_t)q * c->g.cells);
+}
+
 // Precision form of tsch.f90:18-97: FP32 explicit terms, RHS, line solves
-// and FFTs on FP64 fields; the projection is repeated `nproj` times, each
-// time on the FP64 divergence residual (iterative refinement), so the final
-// divergence is at FP64 round-off.  MLS inversions, Stefan front and
-// geometry stay FP64.
+// and FFTs; u, v, w, T, p stay FP64 and every FP32 kernel reads their FP32
+// mirrors.  The projection is repeated `nproj` times, each on the divergence
+// residual of the FP64 velocity (iterative refinement), so the final
+// divergence is at FP64 round-off.  MLS inversions, the Stefan front and the
+// geometry stay FP64.  Mirrors: T is written by the z solve and the
+// temperature forcing, u, v, w by the last velocity update, p by the last
+// pressure update of the substep.
 static void tschem_f32(Ctx* c, const double* gam, const double* rom, const double bd[3][2][3]) {
   const Grid& g = c->g;
   if (!ensure_f32(c)) return;
@@ -89,6 +107,8 @@ static void tschem_f32(Ctx* c, const double* gam, const double* rom, const doubl
   const float* tf = nullptr;
   if (!tri_step_prepare(c, bd, &tlen, &tf)) return;
   static const int fid[4] = {MIBM_F_VX, MIBM_F_VY, MIBM_F_VZ, MIBM_F_TEMP};
+  float* t_mirror = c->q32 + 3 * g.cells;
+  c->q32_valid = false;   // until the step has completed
   for (int ns = 0; ns < 3; ++ns) {
     *c->hs[MIBM_S_AL] = gam[ns] + rom[ns];
     *c->hs[MIBM_S_GA] = gam[ns];
@@ -102,18 +122,20 @@ static void tschem_f32(Ctx* c, const double* gam, const double* rom, const doubl
       float* r = c->rhs32 + (size_t)q * g.cells;
       k_solve_x_f32(c, r, T);
       k_solve_y_f32(c, r, T + tlen);
-      k_solve_z_f32(c, r, T + 2 * tlen, c->df[fid[q]]);
+      k_solve_z_f32(c, r, T + 2 * tlen, c->df[fid[q]], q == 3 ? t_mirror : nullptr);
     }
-    const double* mean3 = lagr_particle_fused(c, dp);
+    const double* mean3 = lagr_particle_fused(c, dp, t_mirror);
     if (c->status != MIBM_OK) return;
     for (int it = 0; it < c->nproj; ++it) {
-      k_divg(c, dp);                                   // FP64 residual
-      k_phcalc_f32(c, c->df[MIBM_F_DPH], c->phi32);    // FP32 Poisson solve
-      k_updvp_f32(c, dp, c->phi32, it == 0 ? mean3 : nullptr);
-      k_prcalc_f32(c, dp, c->phi32);
+      bool last = it + 1 == c->nproj;
+      k_divg_f32(c, dp, c->res32);                     // FP64 residual, rounded once
+      k_phcalc_f32(c, c->res32, c->phi32);             // FP32 Poisson solve
+      k_updvp_f32(c, dp, c->phi32, it == 0 ? mean3 : nullptr, last);
+      k_prcalc_f32(c, dp, c->phi32, last);
     }
     if (c->status != MIBM_OK) return;
   }
+  c->q32_valid = true;
   lagr_step_finish(c);
 }
 
@@ -141,6 +163,7 @@ static void tschem(Ctx* c) {
     }
   }
   if (c->precision == 1) { tschem_f32(c, gam, rom, bd); return; }
+  c->q32_valid = false;
   int tlen = 0;
   const double* tables = tri_step_prepare(c, bd, &tlen, nullptr);
   if (!tables) return;
@@ -159,7 +182,7 @@ static void tschem(Ctx* c) {
       k_solve_y_T(c, r, T + tlen);
       k_solve_z_T(c, r, T + 2 * tlen, c->df[fid[q]], 0);
     }
-    const double* mean3 = lagr_particle_fused(c, dp);
+    const double* mean3 = lagr_particle_fused(c, dp, nullptr);
     if (c->status != MIBM_OK) return;
     k_divg(c, dp);
     k_phcalc(c);
@@ -177,6 +200,11 @@ using namespace mibm;
 #define DROPIN_BEGIN          \
   Ctx* c = current();         \
   if (!ready(c)) return;
+// drop-in routines that write u, v, w, T or p: the FP32 mirrors of the
+// precision form are rebuilt before its next step
+#define DROPIN_WRITES         \
+  DROPIN_BEGIN                \
+  c->q32_valid = false;
 #define DROPIN_END cuda_ok(c, cudaGetLastError(), __func__);
 
 extern "C" {
@@ -186,14 +214,14 @@ void hdnl1_(void) { DROPIN_BEGIN k_hdnl(c, 0, push_params(c, 3)); DROPIN_END }
 void hdnl2_(void) { DROPIN_BEGIN k_hdnl(c, 1, push_params(c, 3)); DROPIN_END }
 void hdnl3_(void) { DROPIN_BEGIN k_hdnl(c, 2, push_params(c, 3)); DROPIN_END }
 void hdnlte_(void) { DROPIN_BEGIN k_hdnl(c, 3, push_params(c, 3)); DROPIN_END }
-void invtr1_(void) { DROPIN_BEGIN invtr(c, 0); DROPIN_END }
-void invtr2_(void) { DROPIN_BEGIN invtr(c, 1); DROPIN_END }
-void invtr3_(void) { DROPIN_BEGIN invtr(c, 2); DROPIN_END }
-void invtrte_(void) { DROPIN_BEGIN invtr(c, 3); DROPIN_END }
+void invtr1_(void) { DROPIN_WRITES invtr(c, 0); DROPIN_END }
+void invtr2_(void) { DROPIN_WRITES invtr(c, 1); DROPIN_END }
+void invtr3_(void) { DROPIN_WRITES invtr(c, 2); DROPIN_END }
+void invtrte_(void) { DROPIN_WRITES invtr(c, 3); DROPIN_END }
 void solxi_(const double* betadx) { DROPIN_BEGIN k_solve_x(c, c->df[MIBM_F_RHS], *betadx); DROPIN_END }
 void solxj_(const double* betadx) { DROPIN_BEGIN k_solve_y(c, c->df[MIBM_F_RHS], *betadx); DROPIN_END }
 void solxk_(double* q, const double* betadx) {
-  DROPIN_BEGIN
+  DROPIN_WRITES
   int id = field_of_plane1(c, q);
   if (id < 0) { fail(c, MIBM_EINVAL, "solxk_: q is not element (1,1,kstart) of a registered field"); return; }
   k_solve_z(c, c->df[MIBM_F_RHS], *betadx, c->df[id]);
@@ -201,19 +229,19 @@ void solxk_(double* q, const double* betadx) {
 }
 void divg_(void) { DROPIN_BEGIN k_divg(c, push_params(c, 3)); DROPIN_END }
 void phcalc_(void) { DROPIN_BEGIN k_phcalc(c); DROPIN_END }
-void updvp_(void) { DROPIN_BEGIN k_updvp(c, push_params(c, 3)); DROPIN_END }
-void prcalc_(void) { DROPIN_BEGIN k_prcalc(c, push_params(c, 3)); DROPIN_END }
+void updvp_(void) { DROPIN_WRITES k_updvp(c, push_params(c, 3)); DROPIN_END }
+void prcalc_(void) { DROPIN_WRITES k_prcalc(c, push_params(c, 3)); DROPIN_END }
 void findcentroidindices_(void) { DROPIN_BEGIN lagr_find_centroid_indices(c); DROPIN_END }
 void mlsweight_(void) { DROPIN_BEGIN lagr_mls_weight(c); DROPIN_END }
-void mlsforce_(void) { DROPIN_BEGIN lagr_mls_force(c, push_params(c, 3), true); DROPIN_END }
-void velforce_(void) { DROPIN_BEGIN lagr_velforce(c); DROPIN_END }
-void tempforce_(void) { DROPIN_BEGIN lagr_tempforce(c); DROPIN_END }
+void mlsforce_(void) { DROPIN_WRITES lagr_mls_force(c, push_params(c, 3), true); DROPIN_END }
+void velforce_(void) { DROPIN_WRITES lagr_velforce(c); DROPIN_END }
+void tempforce_(void) { DROPIN_WRITES lagr_tempforce(c); DROPIN_END }
 void findprobeindices_(void) { DROPIN_BEGIN lagr_find_probe_indices(c); DROPIN_END }
 void mls_heatflux_(void) { DROPIN_BEGIN lagr_heat_flux(c); DROPIN_END }
-void apply_stefancondition_(void) { DROPIN_BEGIN lagr_stefan(c, push_params(c, 3)); DROPIN_END }
+void apply_stefancondition_(void) { DROPIN_WRITES lagr_stefan(c, push_params(c, 3)); DROPIN_END }
 void tagcells_(void) { DROPIN_BEGIN lagr_tag_narrow_band(c); DROPIN_END }
 void tagcells_initial_(void) { DROPIN_BEGIN lagr_tag_initial(c); DROPIN_END }
-void particle_(void) { DROPIN_BEGIN lagr_particle(c, push_params(c, 3)); DROPIN_END }
+void particle_(void) { DROPIN_WRITES lagr_particle(c, push_params(c, 3)); DROPIN_END }
 
 void cfl_(void) {
   DROPIN_BEGIN
@@ -235,13 +263,13 @@ void get_dt_(void) {
 void mibm_set_precision_(const int* mode, const int* nproj) {
   Ctx* c = current(); if (!ready(c)) return;
   if (*mode < 0 || *mode > 1 || *nproj < 1 || *nproj > 8) { fail(c, MIBM_EINVAL, "set_precision: mode 0|1, nproj 1..8"); return; }
-  if (*mode == 1 && c->precision == 0 && c->ru32) {
-    static const int ru[4] = {MIBM_F_RU1, MIBM_F_RU2, MIBM_F_RU3, MIBM_F_RUT};
-    for (int q = 0; q < 4; ++q) {
-      cast_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g.cells, c->df[ru[q]], c->ru32 + (size_t)q * c->g.cells);
-      ++c->launches;
-    }
-  }
+  // the explicit-term histories live in ru32 while the precision form runs:
+  // hand them over in the direction of the switch
+  if (*mode == 1 && c->precision == 0 && c->ru32)
+    for (int q = 0; q < 4; ++q) k_cast_d2f(c, c->g.cells, c->df[kRuFields[q]], c->ru32 + (size_t)q * c->g.cells);
+  if (*mode == 0 && c->precision == 1 && c->ru32)
+    for (int q = 0; q < 4; ++q) k_cast_f2d(c, c->g.cells, c->ru32 + (size_t)q * c->g.cells, c->df[kRuFields[q]]);
+  c->q32_valid = false;
   c->precision = *mode;
   c->nproj = *nproj;
 }

@@ -23,6 +23,27 @@ namespace mibm {
 
 constexpr int kMaxCtx = 4096;
 
+// Per-substep products of grid and step scalars used by the stencils.  Each
+// is one IEEE operation (or the left-to-right product the reference writes)
+// evaluated on the host in FP64, so the FP64 kernels read the same value they
+// would compute per cell; `cf` holds the same values rounded once to FP32.
+// Taking them off the device matters because FP64 multiplies, divisions and
+// FP64<->FP32 conversions all issue at the low FP64 rate.
+enum Coef {
+  kQ1, kQ2, kQ3,          // dx1*0.25, dx2*0.25, dx3*0.25   (hdnl1-3 udx)
+  kH1, kH2, kH3,          // dx1*0.5,  dx2*0.5,  dx3*0.5    (hdnlte udx)
+  kDQ1, kDQ2, kDQ3,       // dx1q, dx2q, dx3q
+  kGA, kRO, kALRE, kDT,
+  kPX1, kPX2, kPX3,       // dx1*al, dx2*al, al*dx3          (invtr pressure gradient)
+  kALPEC,                 // al/pec                          (invtrte)
+  kBETAGZ, kTLIQ,
+  kXLEN, kYLEN, kZLEN,
+  kUP1, kUP2, kUP3,       // al*dt*dx1, al*dt*dx2, al*dt*dx3 (updvp)
+  kBE,                    // al*beta                         (prcalc)
+  kUSDTAL,                // 1/(dt*al)                       (divg)
+  kNCoef
+};
+
 // Per-substep scalars read by the kernels.  The fused RK3 path keeps one
 // copy per substep on the device so that a captured graph reads the values
 // of the current step (dt changes every step in CFL mode).
@@ -32,7 +53,13 @@ struct StepParams {
   double pec, ren;
   double betagz, tliq, tmelt;
   double pos[3], vel[3], om[3];
+  double cd[kNCoef];
+  float cf[kNCoef];
 };
+
+template <typename R> __host__ __device__ __forceinline__ R coef(const StepParams& p, int i);
+template <> __host__ __device__ __forceinline__ double coef<double>(const StepParams& p, int i) { return p.cd[i]; }
+template <> __host__ __device__ __forceinline__ float coef<float>(const StepParams& p, int i) { return p.cf[i]; }
 
 struct Grid {
   int n1m, n2m, n3m;         // cells per direction
@@ -93,6 +120,14 @@ struct Ctx {
   float* ru32 = nullptr;                  // 4 explicit-term histories (FP32)
   float* rhs32 = nullptr;                 // 4 RHS / line-solve fields (FP32)
   float* phi32 = nullptr;                 // FP32 pressure correction
+  float* res32 = nullptr;                 // FP32 copy of the FP64 divergence residual
+  // FP32 mirrors of u, v, w, T, p (5 fields, field order of the Stencil
+  // kernels) read by the FP32 stencils.  The kernels that write the FP64
+  // fields in the precision form also write the mirror; anything else that
+  // writes a field (drop-in routines, mibm_sync_from_host_, the FP64 form)
+  // clears q32_valid and the next precision step rebuilds the mirrors.
+  float* q32 = nullptr;
+  bool q32_valid = false;
   unsigned long long* divmax = nullptr;   // device max|div u| (IEEE bits)
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -177,8 +212,16 @@ void k_hdnl(Ctx* c, int which, const StepParams* dp);
 void k_invtr_rhs(Ctx* c, int which, const StepParams* dp, double* rhs_out);
 void k_fused_rhs(Ctx* c, const StepParams* dp);
 void k_fused_rhs_f32(Ctx* c, const StepParams* dp, float* ru4, float* rhs4);
-void k_updvp_f32(Ctx* c, const StepParams* dp, const float* phi, const double* mean3);
-void k_prcalc_f32(Ctx* c, const StepParams* dp, const float* phi);
+void k_updvp_f32(Ctx* c, const StepParams* dp, const float* phi, const double* mean3, bool mirror);
+void k_prcalc_f32(Ctx* c, const StepParams* dp, const float* phi, bool mirror);
+void k_divg_f32(Ctx* c, const StepParams* dp, float* res);
+void k_mirror_fields(Ctx* c);
+// precision form around host transfers: the explicit-term histories ru* are
+// carried in FP32 on the device; uploads of u, v, w, T, p invalidate the mirrors
+void precision_before_download(Ctx* c, unsigned long long mask);
+void precision_after_upload(Ctx* c, unsigned long long mask);
+void k_cast_f2d(Ctx* c, size_t n, const float* a, double* b);
+void k_cast_d2f(Ctx* c, size_t n, const double* a, float* b);
 void k_divmax(Ctx* c, unsigned long long* out);
 void k_divg(Ctx* c, const StepParams* dp);
 void k_updvp(Ctx* c, const StepParams* dp, const double* mean3 = nullptr);
@@ -199,10 +242,10 @@ void k_solve_z_T(Ctx* c, double* rhs, const double* T, double* q, int write_rhs)
 const double* tri_step_prepare(Ctx* c, const double betadx[3][2][3], int* len_out, const float** f32_out);
 void k_solve_x_f32(Ctx* c, float* rhs, const float* T);
 void k_solve_y_f32(Ctx* c, float* rhs, const float* T);
-void k_solve_z_f32(Ctx* c, float* rhs, const float* T, double* q);
+void k_solve_z_f32(Ctx* c, float* rhs, const float* T, double* q, float* mirror);
 // fft.cu
 void k_phcalc(Ctx* c);
-void k_phcalc_f32(Ctx* c, const double* src, float* phi);
+void k_phcalc_f32(Ctx* c, const float* src, float* phi);
 // lagr.cu
 void lagr_find_centroid_indices(Ctx* c);
 void lagr_mls_weight(Ctx* c);
@@ -216,7 +259,7 @@ void lagr_geometry_refresh(Ctx* c, bool imelt);
 void lagr_tag_narrow_band(Ctx* c);
 void lagr_tag_initial(Ctx* c);
 void lagr_particle(Ctx* c, const StepParams* dp);
-const double* lagr_particle_fused(Ctx* c, const StepParams* dp);
+const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror);
 void lagr_step_finish(Ctx* c);
 void lagr_geometry_to_host(Ctx* c);
 void lagr_invalidate(Ctx* c);

@@ -58,6 +58,20 @@ StepParams host_params(Ctx* c) {
     p.vel[d] = c->hs[MIBM_S_VEL_CM][d];
     p.om[d] = c->hs[MIBM_S_OMEGA_C][d];
   }
+  const Grid& g = c->g;
+  double* q = p.cd;
+  q[kQ1] = g.dx1 * 0.25; q[kQ2] = g.dx2 * 0.25; q[kQ3] = g.dx3 * 0.25;
+  q[kH1] = g.dx1 * 0.5; q[kH2] = g.dx2 * 0.5; q[kH3] = g.dx3 * 0.5;
+  q[kDQ1] = g.dx1q; q[kDQ2] = g.dx2q; q[kDQ3] = g.dx3q;
+  q[kGA] = p.ga; q[kRO] = p.ro; q[kALRE] = p.alre; q[kDT] = p.dt;
+  q[kPX1] = g.dx1 * p.al; q[kPX2] = g.dx2 * p.al; q[kPX3] = p.al * g.dx3;
+  q[kALPEC] = p.al / p.pec;
+  q[kBETAGZ] = p.betagz; q[kTLIQ] = p.tliq;
+  q[kXLEN] = g.xlen; q[kYLEN] = g.ylen; q[kZLEN] = g.zlen;
+  q[kUP1] = p.al * p.dt * g.dx1; q[kUP2] = p.al * p.dt * g.dx2; q[kUP3] = p.al * p.dt * g.dx3;
+  q[kBE] = p.al * p.beta;
+  q[kUSDTAL] = 1.0 / (p.dt * p.al);
+  for (int i = 0; i < kNCoef; ++i) p.cf[i] = (float)q[i];
   return p;
 }
 
@@ -230,6 +244,7 @@ void release(Ctx* c) {
   cudaFree(c->xc); cudaFree(c->xm); cudaFree(c->yc); cudaFree(c->ym); cudaFree(c->zc); cudaFree(c->zm);
   cudaFree(c->red); cudaFree(c->dflag); cudaFree(c->dparams); cudaFree(c->rhs4);
   cudaFree(c->ru32); cudaFree(c->rhs32); cudaFree(c->phi32); cudaFree(c->divmax);
+  cudaFree(c->res32); cudaFree(c->q32);
   cudaFree(c->tri_coef); cudaFree(c->lag_red);
   if (c->red_host) cudaFreeHost(c->red_host);
   if (c->hflag) cudaFreeHost(c->hflag);
@@ -389,6 +404,7 @@ void mibm_sync_from_host_(const long long* mask) {
   unsigned long long m = (unsigned long long)*mask;
   for (int i = 0; i < MIBM_NFIELDS; ++i)
     if (m & (1ull << i)) sync_field_from_host(c, i);
+  precision_after_upload(c, m);
   for (int i = 0; i < MIBM_NMESH && c->maxnf > 0; ++i)
     if ((m >> 32) & (1ull << i))
       cuda_ok(c, cudaMemcpyAsync(c->dm[i], c->hm[i], mesh_bytes(c, i), cudaMemcpyHostToDevice, c->stream), "H2D mesh");
@@ -401,6 +417,7 @@ void mibm_sync_from_host_(const long long* mask) {
 void mibm_sync_to_host_(const long long* mask) {
   Ctx* c = current(); if (!ready(c)) return;
   unsigned long long m = (unsigned long long)*mask;
+  precision_before_download(c, m);
   for (int i = 0; i < MIBM_NFIELDS; ++i)
     if (m & (1ull << i)) sync_field_to_host(c, i);
   for (int i = 0; i < MIBM_NMESH && c->maxnf > 0; ++i)

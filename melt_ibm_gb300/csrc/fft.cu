@@ -129,9 +129,9 @@ __device__ __forceinline__ void load_tw(C* s, const C* tw, int n) {
 constexpr int kRowPairs = 4;   // X passes: 4 complex lines (8 real rows) per CTA
 constexpr int kCols = 8;       // Y/Z passes: 8 adjacent kx columns per CTA
 
-// X forward: real rows (j, j+1) of plane k (FP64 input) -> half spectra
-template <typename C>
-__global__ void fft_x_fwd(FftArgs<C> F, const double* __restrict__ src, C* __restrict__ spec) {
+// X forward: real rows (j, j+1) of plane k (source type S) -> half spectra
+template <typename C, typename S>
+__global__ void fft_x_fwd(FftArgs<C> F, const S* __restrict__ src, C* __restrict__ spec) {
   typedef typename Real<C>::T R;
   extern __shared__ __align__(16) unsigned char shraw[];
   C* sh = (C*)shraw;
@@ -335,14 +335,14 @@ void fft_free(Ctx* c) {
     }
 }
 
-template <typename C>
-static void phcalc_launch(Ctx* c, FftArgs<C> F, const double* src, typename Real<C>::T* dst, const char* tag) {
+template <typename C, typename S>
+static void phcalc_launch(Ctx* c, FftArgs<C> F, const S* src, typename Real<C>::T* dst, const char* tag) {
   const Grid& g = c->g;
   C* spec = (C*)c->spec;
   size_t smx = sizeof(C) * (g.n1m + 2 * kRowPairs * g.n1m);
   size_t smy = sizeof(C) * (g.n2m + 2 * kCols * g.n2m);
   size_t smz = sizeof(C) * (g.n3m + 2 * kCols * g.n3m);
-  cudaFuncSetAttribute((const void*)fft_x_fwd<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  cudaFuncSetAttribute((const void*)fft_x_fwd<C, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   cudaFuncSetAttribute((const void*)fft_x_inv<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   cudaFuncSetAttribute((const void*)fft_y<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   cudaFuncSetAttribute((const void*)fft_z_solve<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
@@ -350,7 +350,7 @@ static void phcalc_launch(Ctx* c, FftArgs<C> F, const double* src, typename Real
   dim3 gy(div_up(g.H, kCols), g.n3m);
   dim3 gz(div_up(g.H, kCols), g.n2m);
   bool f32 = sizeof(C) == sizeof(float2);
-  { MIBM_PROF(c, f32 ? "fft_x_fwd_f32" : "fft_x_fwd"); fft_x_fwd<C><<<gx, 256, smx, c->stream>>>(F, src, spec); }
+  { MIBM_PROF(c, f32 ? "fft_x_fwd_f32" : "fft_x_fwd"); fft_x_fwd<C, S><<<gx, 256, smx, c->stream>>>(F, src, spec); }
   { MIBM_PROF(c, f32 ? "fft_y_f32" : "fft_y"); fft_y<C><<<gy, 256, smy, c->stream>>>(F, spec, -1); }
   { MIBM_PROF(c, f32 ? "fft_z_solve_f32" : "fft_z_solve"); fft_z_solve<C><<<gz, 256, smz, c->stream>>>(F, spec); }
   { MIBM_PROF(c, f32 ? "fft_y_f32" : "fft_y"); fft_y<C><<<gy, 256, smy, c->stream>>>(F, spec, +1); }
@@ -369,12 +369,12 @@ void k_phcalc(Ctx* c) {
   F.twx = fc->twx; F.twy = fc->twy; F.twz = fc->twz;
   F.ak1 = c->ak1; F.ak2 = c->ak2; F.ak3 = c->ak3;
   F.inv_nn = 1.0 / ((double)g.n1m * (double)g.n2m * (double)g.n3m);
-  phcalc_launch<double2>(c, F, c->df[MIBM_F_DPH], c->df[MIBM_F_DPH], "phcalc");
+  phcalc_launch<double2, double>(c, F, c->df[MIBM_F_DPH], c->df[MIBM_F_DPH], "phcalc");
 }
 
-// Precision form: the same solve in FP32 on the FP64 right-hand side
-// `src`, result phi in FP32.
-void k_phcalc_f32(Ctx* c, const double* src, float* phi) {
+// Precision form: the same solve in FP32 on the FP32 right-hand side
+// `src` (the rounded FP64 residual), result phi in FP32.
+void k_phcalc_f32(Ctx* c, const float* src, float* phi) {
   const Grid& g = c->g;
   FftCache* fc = fft_of(c);
   if (!fc->ftwx || !fc->fak1) return;
@@ -384,7 +384,7 @@ void k_phcalc_f32(Ctx* c, const double* src, float* phi) {
   F.twx = fc->ftwx; F.twy = fc->ftwy; F.twz = fc->ftwz;
   F.ak1 = fc->fak1; F.ak2 = fc->fak2; F.ak3 = fc->fak3;
   F.inv_nn = (float)(1.0 / ((double)g.n1m * (double)g.n2m * (double)g.n3m));
-  phcalc_launch<float2>(c, F, src, phi, "phcalc_f32");
+  phcalc_launch<float2, float>(c, F, src, phi, "phcalc_f32");
 }
 
 }  // namespace mibm

@@ -420,6 +420,7 @@ __global__ void radix_scatter_kernel(const int* __restrict__ kin, const int* __r
 struct ScatterOut {
   double* f[4];
   const double* phi[4];
+  float* m32[4];   // FP32 mirrors of f (precision form), null where none
 };
 
 __device__ __forceinline__ int key_comp(int k, size_t cells) {
@@ -447,7 +448,9 @@ __global__ void scatter_apply_kernel(int n, int nf, size_t cells, const int* __r
     int t = sr / 27;
     sum = sum + coef[(size_t)comp * nf + t] * O.phi[comp][sr];
   }
-  O.f[comp][cell] = O.f[comp][cell] + sum;
+  double q = O.f[comp][cell] + sum;
+  O.f[comp][cell] = q;
+  if (O.m32[comp]) O.m32[comp][cell] = (float)q;
   if (segval) segval[e] = sum;
 }
 
@@ -1145,8 +1148,10 @@ static void update_plan(Ctx* c) {
   MIBM_LAUNCH_CHECK(c, "scatter plan");
 }
 
-static ScatterOut scatter_out(Ctx* c, bool into_fields) {
+static ScatterOut scatter_out(Ctx* c, bool into_fields, float* t_mirror) {
   ScatterOut O;
+  O.m32[0] = O.m32[1] = O.m32[2] = nullptr;
+  O.m32[3] = into_fields ? t_mirror : nullptr;
   static const int fo[4] = {MIBM_F_FORXC, MIBM_F_FORYC, MIBM_F_FORZC, MIBM_F_FORTEMP};
   static const int fq[4] = {MIBM_F_VX, MIBM_F_VY, MIBM_F_VZ, MIBM_F_TEMP};
   for (int q = 0; q < 4; ++q) O.f[q] = c->df[into_fields ? fq[q] : fo[q]];
@@ -1168,11 +1173,11 @@ static void force_coefficients(Ctx* c) {
   ++c->launches;
 }
 
-static void scatter(Ctx* c, bool into_fields, int lo, int hi, bool record) {
+static void scatter(Ctx* c, bool into_fields, int lo, int hi, bool record, float* t_mirror = nullptr) {
   LagState* s = lag_of(c);
   { MIBM_PROF(c, "scatter_apply");
     scatter_apply_kernel<<<div_up(s->plan_n, 256), 256, 0, c->stream>>>(
-        s->plan_n, c->maxnf, c->g.cells, s->res_key, s->res_src, c->tri_coef, scatter_out(c, into_fields), lo, hi,
+        s->plan_n, c->maxnf, c->g.cells, s->res_key, s->res_src, c->tri_coef, scatter_out(c, into_fields, t_mirror), lo, hi,
         record ? s->segval : nullptr); }
   ++c->launches;
 }
@@ -1424,7 +1429,7 @@ void lagr_particle(Ctx* c, const StepParams* dp) {
 // has read the unforced temperature, into T.  MLS weights of a stationary
 // cage are reused.  Flags and geometry scalars are read by the caller at the
 // end of the step.
-const double* lagr_particle_fused(Ctx* c, const StepParams* dp) {
+const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror) {
   if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0) return nullptr;
   if (!ensure_adjacency(c) || !ensure_lag_buffers(c)) return nullptr;
   LagState* s = lag_of(c);
@@ -1448,7 +1453,7 @@ const double* lagr_particle_fused(Ctx* c, const StepParams* dp) {
     lagr_find_probe_indices(c);
     heat_flux_launch(c);
   }
-  scatter(c, true, 3, 4, false);
+  scatter(c, true, 3, 4, false, t_mirror);
   if (imelt) lagr_stefan(c, dp);
   geometry_launch(c, imelt);
   MIBM_LAUNCH_CHECK(c, "particle");

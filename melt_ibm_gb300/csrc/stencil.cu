@@ -35,9 +35,28 @@ struct StencilArgs {
   const double* __restrict__ ym;
   const double* __restrict__ zc;
   const double* __restrict__ zm;
+  const float* __restrict__ u32;   // FP32 mirrors (precision form only)
+  const float* __restrict__ v32;
+  const float* __restrict__ w32;
+  const float* __restrict__ t32;
+  const float* __restrict__ p32;
   int coff;
   int forcing;
 };
+
+// the five prognostic fields as read by the stencils of compute type R: the
+// FP64 fields themselves, or their FP32 mirrors in the precision form
+template <typename R>
+struct Prog {
+  const R* u; const R* v; const R* w; const R* t; const R* p;
+};
+template <typename R> __device__ __forceinline__ Prog<R> prog(const StencilArgs& A);
+template <> __device__ __forceinline__ Prog<double> prog<double>(const StencilArgs& A) {
+  return Prog<double>{A.vx, A.vy, A.vz, A.temp, A.pr};
+}
+template <> __device__ __forceinline__ Prog<float> prog<float>(const StencilArgs& A) {
+  return Prog<float>{A.u32, A.v32, A.w32, A.t32, A.p32};
+}
 
 static StencilArgs make_args(Ctx* c) {
   StencilArgs a;
@@ -47,6 +66,10 @@ static StencilArgs make_args(Ctx* c) {
   a.vofx = c->df[MIBM_F_VOFX]; a.vofy = c->df[MIBM_F_VOFY]; a.vofz = c->df[MIBM_F_VOFZ]; a.vofp = c->df[MIBM_F_VOFP];
   a.forcx = c->df[MIBM_F_FORCX]; a.forcy = c->df[MIBM_F_FORCY]; a.forcz = c->df[MIBM_F_FORCZ];
   a.xc = c->xc; a.xm = c->xm; a.yc = c->yc; a.ym = c->ym; a.zc = c->zc; a.zm = c->zm;
+  const float* m = c->q32;
+  size_t n = c->g.cells;
+  a.u32 = m; a.v32 = m ? m + n : nullptr; a.w32 = m ? m + 2 * n : nullptr;
+  a.t32 = m ? m + 3 * n : nullptr; a.p32 = m ? m + 4 * n : nullptr;
   a.coff = c->coord_off;
   a.forcing = c->I(MIBM_I_FORCING);
   return a;
@@ -73,63 +96,65 @@ static StencilArgs make_args(Ctx* c) {
 // ---------------------------------------------------------------------
 // explicit terms, templated on the compute type R: R = double is the plain
 // FP64 form (bit-identical to a double-only build), R = float the precision
-// form (fields stay FP64 in memory and are rounded once on load).
+// form, which reads the FP32 mirrors of the fields and the FP32 coefficients
+// so that no FP64 operation is left in the cell loop (on this part FP64
+// arithmetic and FP64<->FP32 conversions share the low FP64 issue rate).
 // ---------------------------------------------------------------------
 template <typename R>
 __device__ __forceinline__ R h_x(const StencilArgs& A, size_t c0, ptrdiff_t dip, ptrdiff_t dim, ptrdiff_t djp,
-                                 ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm) {
-  const Grid& g = A.g;
-  const double* vx = A.vx; const double* vy = A.vy; const double* vz = A.vz;
-  R udx1 = R(g.dx1 * 0.25), udx2 = R(g.dx2 * 0.25), udx3 = R(g.dx3 * 0.25);
-  R vxc = R(vx[c0]);
-  R a = R(vx[c0 + dip]) + vxc, b = R(vx[c0 + dim]) + vxc;
+                                 ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm, const StepParams& p) {
+  const Prog<R> F = prog<R>(A);
+  const R* vx = F.u; const R* vy = F.v; const R* vz = F.w;
+  R udx1 = coef<R>(p, kQ1), udx2 = coef<R>(p, kQ2), udx3 = coef<R>(p, kQ3);
+  R vxc = vx[c0];
+  R a = vx[c0 + dip] + vxc, b = vx[c0 + dim] + vxc;
   R h11 = (a * a - b * b) * udx1;
-  R h12 = ((R(vy[c0 + djp]) + R(vy[c0 + dim + djp])) * (R(vx[c0 + djp]) + vxc) -
-           (R(vy[c0]) + R(vy[c0 + dim])) * (vxc + R(vx[c0 + djm]))) * udx2;
-  R h13 = ((R(vz[c0 + dkp]) + R(vz[c0 + dim + dkp])) * (R(vx[c0 + dkp]) + vxc) -
-           (R(vz[c0]) + R(vz[c0 + dim])) * (vxc + R(vx[c0 + dkm]))) * udx3;
+  R h12 = ((vy[c0 + djp] + vy[c0 + dim + djp]) * (vx[c0 + djp] + vxc) -
+           (vy[c0] + vy[c0 + dim]) * (vxc + vx[c0 + djm])) * udx2;
+  R h13 = ((vz[c0 + dkp] + vz[c0 + dim + dkp]) * (vx[c0 + dkp] + vxc) -
+           (vz[c0] + vz[c0 + dim]) * (vxc + vx[c0 + dkm])) * udx3;
   R h = -(h11 + h12 + h13);
-  if (A.forcing) h = h + R(A.vofx[c0]) * R(A.forcx[c0]) / R(g.xlen);
+  if (A.forcing) h = h + R(A.vofx[c0]) * R(A.forcx[c0]) / coef<R>(p, kXLEN);
   return h;
 }
 
 template <typename R>
 __device__ __forceinline__ R h_y(const StencilArgs& A, size_t c0, ptrdiff_t dip, ptrdiff_t dim, ptrdiff_t djp,
-                                 ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm) {
-  const Grid& g = A.g;
-  const double* vx = A.vx; const double* vy = A.vy; const double* vz = A.vz;
-  R udx1 = R(g.dx1 * 0.25), udx2 = R(g.dx2 * 0.25), udx3 = R(g.dx3 * 0.25);
-  R vyc = R(vy[c0]);
-  R h21 = ((R(vy[c0 + dip]) + vyc) * (R(vx[c0 + dip]) + R(vx[c0 + dip + djm])) -
-           (vyc + R(vy[c0 + dim])) * (R(vx[c0]) + R(vx[c0 + djm]))) * udx1;
-  R a = R(vy[c0 + djp]) + vyc, b = R(vy[c0 + djm]) + vyc;
+                                 ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm, const StepParams& p) {
+  const Prog<R> F = prog<R>(A);
+  const R* vx = F.u; const R* vy = F.v; const R* vz = F.w;
+  R udx1 = coef<R>(p, kQ1), udx2 = coef<R>(p, kQ2), udx3 = coef<R>(p, kQ3);
+  R vyc = vy[c0];
+  R h21 = ((vy[c0 + dip] + vyc) * (vx[c0 + dip] + vx[c0 + dip + djm]) -
+           (vyc + vy[c0 + dim]) * (vx[c0] + vx[c0 + djm])) * udx1;
+  R a = vy[c0 + djp] + vyc, b = vy[c0 + djm] + vyc;
   R h22 = (a * a - b * b) * udx2;
-  R h23 = ((R(vz[c0 + dkp]) + R(vz[c0 + djm + dkp])) * (R(vy[c0 + dkp]) + vyc) -
-           (R(vz[c0]) + R(vz[c0 + djm])) * (vyc + R(vy[c0 + dkm]))) * udx3;
+  R h23 = ((vz[c0 + dkp] + vz[c0 + djm + dkp]) * (vy[c0 + dkp] + vyc) -
+           (vz[c0] + vz[c0 + djm]) * (vyc + vy[c0 + dkm])) * udx3;
   R h = -(h21 + h22 + h23);
-  if (A.forcing) h = h + R(A.vofy[c0]) * R(A.forcy[c0]) / R(g.ylen);
+  if (A.forcing) h = h + R(A.vofy[c0]) * R(A.forcy[c0]) / coef<R>(p, kYLEN);
   return h;
 }
 
 template <typename R>
 __device__ __forceinline__ R h_z(const StencilArgs& A, size_t c0, ptrdiff_t dip, ptrdiff_t dim, ptrdiff_t djp,
                                  ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm, const StepParams& p) {
-  const Grid& g = A.g;
-  const double* vx = A.vx; const double* vy = A.vy; const double* vz = A.vz;
-  R udx1 = R(g.dx1 * 0.25), udx2 = R(g.dx2 * 0.25), udx3 = R(g.dx3 * 0.25);
-  R vzc = R(vz[c0]);
-  R h31 = ((R(vx[c0 + dip]) + R(vx[c0 + dip + dkm])) * (R(vz[c0 + dip]) + vzc) -
-           (R(vx[c0]) + R(vx[c0 + dkm])) * (vzc + R(vz[c0 + dim]))) * udx1;
-  R h32 = ((R(vy[c0 + djp]) + R(vy[c0 + djp + dkm])) * (R(vz[c0 + djp]) + vzc) -
-           (R(vy[c0]) + R(vy[c0 + dkm])) * (vzc + R(vz[c0 + djm]))) * udx2;
-  R a = R(vz[c0 + dkp]) + vzc, b = vzc + R(vz[c0 + dkm]);
+  const Prog<R> F = prog<R>(A);
+  const R* vx = F.u; const R* vy = F.v; const R* vz = F.w;
+  R udx1 = coef<R>(p, kQ1), udx2 = coef<R>(p, kQ2), udx3 = coef<R>(p, kQ3);
+  R vzc = vz[c0];
+  R h31 = ((vx[c0 + dip] + vx[c0 + dip + dkm]) * (vz[c0 + dip] + vzc) -
+           (vx[c0] + vx[c0 + dkm]) * (vzc + vz[c0 + dim])) * udx1;
+  R h32 = ((vy[c0 + djp] + vy[c0 + djp + dkm]) * (vz[c0 + djp] + vzc) -
+           (vy[c0] + vy[c0 + dkm]) * (vzc + vz[c0 + djm])) * udx2;
+  R a = vz[c0 + dkp] + vzc, b = vzc + vz[c0 + dkm];
   R h33 = (a * a - b * b) * udx3;
   R h = -(h31 + h32 + h33);
   if (p.betagz != 0.0) {
-    R T_interp = (R(A.temp[c0]) + R(A.temp[c0 + dkm])) * R(0.5);
-    h = h + R(p.betagz) * (T_interp - R(p.tliq));
+    R T_interp = (F.t[c0] + F.t[c0 + dkm]) * R(0.5);
+    h = h + coef<R>(p, kBETAGZ) * (T_interp - coef<R>(p, kTLIQ));
   }
-  if (A.forcing) h = h + R(A.vofz[c0]) * R(A.forcz[c0]) / R(g.zlen);
+  if (A.forcing) h = h + R(A.vofz[c0]) * R(A.forcz[c0]) / coef<R>(p, kZLEN);
   return h;
 }
 
@@ -139,13 +164,14 @@ template <typename R>
 __device__ __forceinline__ R h_t(const StencilArgs& A, int i, int j, int k, size_t c0, ptrdiff_t dip, ptrdiff_t dim,
                                  ptrdiff_t djp, ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm, const StepParams& p) {
   const Grid& g = A.g;
-  const double* vx = A.vx; const double* vy = A.vy; const double* vz = A.vz; const double* T = A.temp;
-  R udx1 = R(g.dx1 * 0.5), udx2 = R(g.dx2 * 0.5), udx3 = R(g.dx3 * 0.5);
-  R tc = R(T[c0]), tip = R(T[c0 + dip]), tim = R(T[c0 + dim]), tjp = R(T[c0 + djp]), tjm = R(T[c0 + djm]);
-  R tkp = R(T[c0 + dkp]), tkm = R(T[c0 + dkm]);
-  R h31 = (R(vx[c0 + dip]) * (tip + tc) - R(vx[c0]) * (tc + tim)) * udx1;
-  R h32 = (R(vy[c0 + djp]) * (tjp + tc) - R(vy[c0]) * (tc + tjm)) * udx2;
-  R h33 = (R(vz[c0 + dkp]) * (tkp + tc) - R(vz[c0]) * (tc + tkm)) * udx3;
+  const Prog<R> F = prog<R>(A);
+  const R* vx = F.u; const R* vy = F.v; const R* vz = F.w; const R* T = F.t;
+  R udx1 = coef<R>(p, kH1), udx2 = coef<R>(p, kH2), udx3 = coef<R>(p, kH3);
+  R tc = T[c0], tip = T[c0 + dip], tim = T[c0 + dim], tjp = T[c0 + djp], tjm = T[c0 + djm];
+  R tkp = T[c0 + dkp], tkm = T[c0 + dkm];
+  R h31 = (vx[c0 + dip] * (tip + tc) - vx[c0] * (tc + tim)) * udx1;
+  R h32 = (vy[c0 + djp] * (tjp + tc) - vy[c0] * (tc + tjm)) * udx2;
+  R h33 = (vz[c0 + dkp] * (tkp + tc) - vz[c0] * (tc + tkm)) * udx3;
   R vp = R(A.vofp[c0]);
   R ht = -(h31 + h32 + h33) * vp;
   R sv = R(1.0) - vp;
@@ -173,8 +199,8 @@ __global__ void hdnl_kernel(StencilArgs A, int which, const StepParams* __restri
   CELL_INDEX
   StepParams p = *pp;
   double h;
-  if (which == 0) h = h_x<double>(A, c0, dip, dim, djp, djm, dkp, dkm);
-  else if (which == 1) h = h_y<double>(A, c0, dip, dim, djp, djm, dkp, dkm);
+  if (which == 0) h = h_x<double>(A, c0, dip, dim, djp, djm, dkp, dkm, p);
+  else if (which == 1) h = h_y<double>(A, c0, dip, dim, djp, djm, dkp, dkm, p);
   else if (which == 2) h = h_z<double>(A, c0, dip, dim, djp, djm, dkp, dkm, p);
   else h = h_t<double>(A, i, j, k, c0, dip, dim, djp, djm, dkp, dkm, p);
   out[c0] = h;
@@ -184,12 +210,12 @@ __global__ void hdnl_kernel(StencilArgs A, int which, const StepParams* __restri
 // RHS of the factored implicit step
 // ---------------------------------------------------------------------
 template <typename R>
-__device__ __forceinline__ R lap(const double* q, size_t c0, ptrdiff_t dip, ptrdiff_t dim, ptrdiff_t djp,
-                                 ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm, const Grid& g, bool fortran_order_t) {
-  R qc = R(q[c0]);
-  R d1 = (R(q[c0 + dip]) - R(2.0) * qc + R(q[c0 + dim])) * R(g.dx1q);
-  R d2 = (R(q[c0 + djp]) - R(2.0) * qc + R(q[c0 + djm])) * R(g.dx2q);
-  R d3 = (R(q[c0 + dkp]) - R(2.0) * qc + R(q[c0 + dkm])) * R(g.dx3q);
+__device__ __forceinline__ R lap(const R* q, size_t c0, ptrdiff_t dip, ptrdiff_t dim, ptrdiff_t djp, ptrdiff_t djm,
+                                 ptrdiff_t dkp, ptrdiff_t dkm, const StepParams& p, bool fortran_order_t) {
+  R qc = q[c0];
+  R d1 = (q[c0 + dip] - R(2.0) * qc + q[c0 + dim]) * coef<R>(p, kDQ1);
+  R d2 = (q[c0 + djp] - R(2.0) * qc + q[c0 + djm]) * coef<R>(p, kDQ2);
+  R d3 = (q[c0 + dkp] - R(2.0) * qc + q[c0 + dkm]) * coef<R>(p, kDQ3);
   // invtr1/2: d11+d22+d33 ; invtr3/invtrte: d22+d33+d11
   return fortran_order_t ? (d2 + d3) + d1 : (d1 + d2) + d3;
 }
@@ -198,23 +224,23 @@ template <typename R>
 __device__ __forceinline__ R rhs_value(const StencilArgs& A, int which, R h, R ru, size_t c0, ptrdiff_t dip,
                                        ptrdiff_t dim, ptrdiff_t djp, ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm,
                                        const StepParams& p) {
-  const Grid& g = A.g;
-  R ga = R(p.ga), ro = R(p.ro), alre = R(p.alre), dt = R(p.dt);
+  const Prog<R> F = prog<R>(A);
+  R ga = coef<R>(p, kGA), ro = coef<R>(p, kRO), alre = coef<R>(p, kALRE), dt = coef<R>(p, kDT);
   if (which == 0) {
-    R dcvx = lap<R>(A.vx, c0, dip, dim, djp, djm, dkp, dkm, g, false);
-    R dpx11 = (R(A.pr[c0]) - R(A.pr[c0 + dim])) * R(g.dx1 * p.al);
+    R dcvx = lap<R>(F.u, c0, dip, dim, djp, djm, dkp, dkm, p, false);
+    R dpx11 = (F.p[c0] - F.p[c0 + dim]) * coef<R>(p, kPX1);
     return (ga * h + ro * ru + alre * dcvx - dpx11) * dt;
   } else if (which == 1) {
-    R dcvy = lap<R>(A.vy, c0, dip, dim, djp, djm, dkp, dkm, g, false);
-    R dpx22 = (R(A.pr[c0]) - R(A.pr[c0 + djm])) * R(g.dx2 * p.al);
+    R dcvy = lap<R>(F.v, c0, dip, dim, djp, djm, dkp, dkm, p, false);
+    R dpx22 = (F.p[c0] - F.p[c0 + djm]) * coef<R>(p, kPX2);
     return (ga * h + ro * ru + alre * dcvy - dpx22) * dt;
   } else if (which == 2) {
-    R dcvz = lap<R>(A.vz, c0, dip, dim, djp, djm, dkp, dkm, g, true);
-    R dpx33 = (R(A.pr[c0]) - R(A.pr[c0 + dkm])) * R(p.al * g.dx3);
+    R dcvz = lap<R>(F.w, c0, dip, dim, djp, djm, dkp, dkm, p, true);
+    R dpx33 = (F.p[c0] - F.p[c0 + dkm]) * coef<R>(p, kPX3);
     return (ga * h + ro * ru + alre * dcvz - dpx33) * dt;
   }
-  R dcte = lap<R>(A.temp, c0, dip, dim, djp, djm, dkp, dkm, g, true);
-  return dt * (ga * h + ro * ru) + R(p.al / p.pec) * dcte * dt;
+  R dcte = lap<R>(F.t, c0, dip, dim, djp, djm, dkp, dkm, p, true);
+  return dt * (ga * h + ro * ru) + coef<R>(p, kALPEC) * dcte * dt;
 }
 
 // invtr drop-in: reads H from the explicit-term array, writes rhs, ru = H
@@ -235,8 +261,8 @@ __global__ void fused_rhs_kernel(StencilArgs A, int which, const StepParams* __r
   CELL_INDEX
   StepParams p = *pp;
   R h;
-  if (which == 0) h = h_x<R>(A, c0, dip, dim, djp, djm, dkp, dkm);
-  else if (which == 1) h = h_y<R>(A, c0, dip, dim, djp, djm, dkp, dkm);
+  if (which == 0) h = h_x<R>(A, c0, dip, dim, djp, djm, dkp, dkm, p);
+  else if (which == 1) h = h_y<R>(A, c0, dip, dim, djp, djm, dkp, dkm, p);
   else if (which == 2) h = h_z<R>(A, c0, dip, dim, djp, djm, dkp, dkm, p);
   else h = h_t<R>(A, i, j, k, c0, dip, dim, djp, djm, dkp, dkm, p);
   rhs[c0] = rhs_value<R>(A, which, h, ru[c0], c0, dip, dim, djp, djm, dkp, dkm, p);
@@ -248,10 +274,20 @@ __global__ void fused_rhs_kernel(StencilArgs A, int which, const StepParams* __r
 // ---------------------------------------------------------------------
 __global__ void divg_kernel(StencilArgs A, const StepParams* __restrict__ pp, double* __restrict__ dph) {
   CELL_INDEX
-  double usdtal = 1.0 / (pp->dt * pp->al);
+  double usdtal = pp->cd[kUSDTAL];
   double dq = (A.vx[c0 + dip] - A.vx[c0]) * g.dx1 + (A.vy[c0 + djp] - A.vy[c0]) * g.dx2 +
               (A.vz[c0 + dkp] - A.vz[c0]) * g.dx3;
   dph[c0] = dq * usdtal;
+}
+
+// precision form: the divergence residual of the FP64 velocity, formed in
+// FP64 (the face differences cancel to round-off of u), then rounded once to
+// FP32 as the right-hand side of the FP32 Poisson solve
+__global__ void divg_f32_kernel(StencilArgs A, const StepParams* __restrict__ pp, float* __restrict__ res) {
+  CELL_INDEX
+  double du = A.vx[c0 + dip] - A.vx[c0], dv = A.vy[c0 + djp] - A.vy[c0], dw = A.vz[c0 + dkp] - A.vz[c0];
+  double dq = fma(dw, g.dx3, fma(dv, g.dx2, du * g.dx1));
+  res[c0] = (float)dq * pp->cf[kUSDTAL];
 }
 
 // mean3 (fused step only): the mean IBM force of velforce.f90:21-50, removed
@@ -260,8 +296,7 @@ __global__ void updvp_kernel(StencilArgs A, const StepParams* __restrict__ pp, c
                              double* __restrict__ vx, double* __restrict__ vy, double* __restrict__ vz,
                              const double* __restrict__ mean3) {
   CELL_INDEX
-  double al = pp->al, dt = pp->dt;
-  double udx1 = al * dt * g.dx1, udx2 = al * dt * g.dx2, udx3 = al * dt * g.dx3;
+  double udx1 = pp->cd[kUP1], udx2 = pp->cd[kUP2], udx3 = pp->cd[kUP3];
   double loc = dph[c0];
   double mx = 0.0, my = 0.0, mz = 0.0;
   if (mean3) { mx = mean3[0]; my = mean3[1]; mz = mean3[2]; }
@@ -270,32 +305,57 @@ __global__ void updvp_kernel(StencilArgs A, const StepParams* __restrict__ pp, c
   vz[c0] = (vz[c0] - mz) - (loc - dph[c0 + dkm]) * udx3;
 }
 
-// precision form: u -= al dt grad(phi) with phi from the FP32 Poisson solve
-// (FP64 update of the FP64 velocity), optional mean-force removal
+// precision form: u -= al dt grad(phi) with phi from the FP32 Poisson solve;
+// the increment is formed in FP32 and added to the FP64 velocity, optional
+// mean-force removal, optional FP32 mirror m32 (u, v, w at 0, cells, 2 cells)
 __global__ void updvp_f32_kernel(StencilArgs A, const StepParams* __restrict__ pp, const float* __restrict__ phi,
                                  double* __restrict__ vx, double* __restrict__ vy, double* __restrict__ vz,
-                                 const double* __restrict__ mean3) {
+                                 const double* __restrict__ mean3, float* __restrict__ m32) {
   CELL_INDEX
-  double al = pp->al, dt = pp->dt;
-  double udx1 = al * dt * g.dx1, udx2 = al * dt * g.dx2, udx3 = al * dt * g.dx3;
-  double loc = phi[c0];
-  double mx = 0.0, my = 0.0, mz = 0.0;
-  if (mean3) { mx = mean3[0]; my = mean3[1]; mz = mean3[2]; }
-  vx[c0] = (vx[c0] - mx) - (loc - (double)phi[c0 + dim]) * udx1;
-  vy[c0] = (vy[c0] - my) - (loc - (double)phi[c0 + djm]) * udx2;
-  vz[c0] = (vz[c0] - mz) - (loc - (double)phi[c0 + dkm]) * udx3;
+  float loc = phi[c0];
+  float ix = (loc - phi[c0 + dim]) * pp->cf[kUP1];
+  float iy = (loc - phi[c0 + djm]) * pp->cf[kUP2];
+  float iz = (loc - phi[c0 + dkm]) * pp->cf[kUP3];
+  double x = vx[c0], y = vy[c0], z = vz[c0];
+  if (mean3) { x = x - mean3[0]; y = y - mean3[1]; z = z - mean3[2]; }
+  x = x - (double)ix; y = y - (double)iy; z = z - (double)iz;
+  vx[c0] = x; vy[c0] = y; vz[c0] = z;
+  if (m32) { m32[c0] = (float)x; m32[c0 + g.cells] = (float)y; m32[c0 + 2 * g.cells] = (float)z; }
 }
 
-// precision form: p += phi - al beta lap(phi), increment in FP32
+// precision form: p += phi - al beta lap(phi), increment in FP32, optional
+// FP32 mirror of p
 __global__ void prcalc_f32_kernel(StencilArgs A, const StepParams* __restrict__ pp, const float* __restrict__ phi,
-                                  double* __restrict__ pr) {
+                                  double* __restrict__ pr, float* __restrict__ m32) {
   CELL_INDEX
-  float be = (float)(pp->al * pp->beta);
+  float be = pp->cf[kBE];
   float d = phi[c0];
-  float inc = d - be * ((phi[c0 + dip] - 2.0f * d + phi[c0 + dim]) * (float)g.dx1q +
-                        (phi[c0 + djp] - 2.0f * d + phi[c0 + djm]) * (float)g.dx2q +
-                        (phi[c0 + dkp] - 2.0f * d + phi[c0 + dkm]) * (float)g.dx3q);
-  pr[c0] = pr[c0] + (double)inc;
+  float inc = d - be * ((phi[c0 + dip] - 2.0f * d + phi[c0 + dim]) * pp->cf[kDQ1] +
+                        (phi[c0 + djp] - 2.0f * d + phi[c0 + djm]) * pp->cf[kDQ2] +
+                        (phi[c0 + dkp] - 2.0f * d + phi[c0 + dkm]) * pp->cf[kDQ3]);
+  double q = pr[c0] + (double)inc;
+  pr[c0] = q;
+  if (m32) m32[c0] = (float)q;
+}
+
+// FP32 mirrors of u, v, w, T, p (field f at m32 + f*cells)
+__global__ void mirror_kernel(size_t n, const double* __restrict__ u, const double* __restrict__ v,
+                              const double* __restrict__ w, const double* __restrict__ t,
+                              const double* __restrict__ p, float* __restrict__ m32) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  m32[e] = (float)u[e]; m32[e + n] = (float)v[e]; m32[e + 2 * n] = (float)w[e];
+  m32[e + 3 * n] = (float)t[e]; m32[e + 4 * n] = (float)p[e];
+}
+
+__global__ void cast_d2f_kernel(size_t n, const double* __restrict__ a, float* __restrict__ b) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) b[e] = (float)a[e];
+}
+
+__global__ void cast_f2d_kernel(size_t n, const float* __restrict__ a, double* __restrict__ b) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) b[e] = (double)a[e];
 }
 
 // max |div u| (divgck semantics, divg.f90:26-56) into bits of `out`
@@ -311,7 +371,7 @@ __global__ void divmax_kernel(StencilArgs A, unsigned long long* __restrict__ ou
 __global__ void prcalc_kernel(StencilArgs A, const StepParams* __restrict__ pp, const double* __restrict__ dph,
                               double* __restrict__ pr) {
   CELL_INDEX
-  double be = pp->al * pp->beta;
+  double be = pp->cd[kBE];
   double d = dph[c0];
   pr[c0] = pr[c0] + d - be * ((dph[c0 + dip] - 2.0 * d + dph[c0 + dim]) * g.dx1q +
                               (dph[c0 + djp] - 2.0 * d + dph[c0 + djm]) * g.dx2q +
@@ -490,19 +550,48 @@ void k_updvp(Ctx* c, const StepParams* dp, const double* mean3) {
   MIBM_LAUNCH_CHECK(c, "updvp");
 }
 
-void k_updvp_f32(Ctx* c, const StepParams* dp, const float* phi, const double* mean3) {
+void k_updvp_f32(Ctx* c, const StepParams* dp, const float* phi, const double* mean3, bool mirror) {
   { MIBM_PROF(c, "updvp_f32");
     updvp_f32_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, phi, c->df[MIBM_F_VX],
-                                                                     c->df[MIBM_F_VY], c->df[MIBM_F_VZ], mean3); }
+                                                                     c->df[MIBM_F_VY], c->df[MIBM_F_VZ], mean3,
+                                                                     mirror ? c->q32 : nullptr); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "updvp_f32");
 }
 
-void k_prcalc_f32(Ctx* c, const StepParams* dp, const float* phi) {
+void k_prcalc_f32(Ctx* c, const StepParams* dp, const float* phi, bool mirror) {
   { MIBM_PROF(c, "prcalc_f32");
-    prcalc_f32_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, phi, c->df[MIBM_F_PR]); }
+    prcalc_f32_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, phi, c->df[MIBM_F_PR],
+                                                                      mirror ? c->q32 + 4 * c->g.cells : nullptr); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "prcalc_f32");
+}
+
+void k_divg_f32(Ctx* c, const StepParams* dp, float* res) {
+  { MIBM_PROF(c, "divg_f32"); divg_f32_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, res); }
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "divg_f32");
+}
+
+void k_mirror_fields(Ctx* c) {
+  { MIBM_PROF(c, "mirror");
+    mirror_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g.cells, c->df[MIBM_F_VX], c->df[MIBM_F_VY],
+                                                                  c->df[MIBM_F_VZ], c->df[MIBM_F_TEMP],
+                                                                  c->df[MIBM_F_PR], c->q32); }
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "mirror");
+}
+
+void k_cast_d2f(Ctx* c, size_t n, const double* a, float* b) {
+  cast_d2f_kernel<<<div_up(n, 256), 256, 0, c->stream>>>(n, a, b);
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "cast");
+}
+
+void k_cast_f2d(Ctx* c, size_t n, const float* a, double* b) {
+  cast_f2d_kernel<<<div_up(n, 256), 256, 0, c->stream>>>(n, a, b);
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "cast");
 }
 
 // max |div u| over the owned cells (device), cleared first

@@ -249,10 +249,11 @@ __global__ void solve_y_kernel(Grid g, V* __restrict__ rhs, const V* __restrict_
 }
 
 // z-lines: tile = up to 32 adjacent i of one row j; smem[k][l]; then q += x
-// (solxk.f90:44-50), optionally leaving rhs holding the increment.
+// (solxk.f90:44-50), optionally leaving rhs holding the increment and, in
+// the precision form, writing the FP32 mirror m32 of the updated q.
 template <typename V>
 __global__ void solve_z_kernel(Grid g, V* __restrict__ rhs, const V* __restrict__ T, double* __restrict__ q,
-                               int write_rhs) {
+                               int write_rhs, float* __restrict__ m32) {
   extern __shared__ __align__(16) unsigned char smraw[];
   V* sm = (V*)smraw;
   int n = g.n3m;
@@ -282,7 +283,9 @@ __global__ void solve_z_kernel(Grid g, V* __restrict__ rhs, const V* __restrict_
       size_t c0 = cidx(g, i0 + l, j, k);
       V x = sm[t];
       if (write_rhs) rhs[c0] = x;
-      q[c0] = q[c0] + (double)x;
+      double qn = q[c0] + (double)x;
+      q[c0] = qn;
+      if (m32) m32[c0] = (float)qn;
     }
   }
 }
@@ -387,11 +390,11 @@ static void solve_y_launch(Ctx* c, V* rhs, const V* T, const char* name) {
 }
 
 template <typename V>
-static void solve_z_launch(Ctx* c, V* rhs, const V* T, double* q, int write_rhs, const char* name) {
+static void solve_z_launch(Ctx* c, V* rhs, const V* T, double* q, int write_rhs, float* m32, const char* name) {
   size_t sm = ((size_t)kLines * c->g.n3m + 4 * (size_t)c->g.n3m + 4) * sizeof(V);
   if (!smem_ok(c, (const void*)solve_z_kernel<V>, sm)) return;
   dim3 grid(div_up(c->g.n1m, kLines), c->g.n2m);
-  { MIBM_PROF(c, name); solve_z_kernel<V><<<grid, 128, sm, c->stream>>>(c->g, rhs, T, q, write_rhs); }
+  { MIBM_PROF(c, name); solve_z_kernel<V><<<grid, 128, sm, c->stream>>>(c->g, rhs, T, q, write_rhs, m32); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, name);
 }
@@ -399,11 +402,13 @@ static void solve_z_launch(Ctx* c, V* rhs, const V* T, double* q, int write_rhs,
 void k_solve_x_T(Ctx* c, double* rhs, const double* T) { solve_x_launch<double>(c, rhs, T, "solve_x"); }
 void k_solve_y_T(Ctx* c, double* rhs, const double* T) { solve_y_launch<double>(c, rhs, T, "solve_y"); }
 void k_solve_z_T(Ctx* c, double* rhs, const double* T, double* q, int write_rhs) {
-  solve_z_launch<double>(c, rhs, T, q, write_rhs, "solve_z");
+  solve_z_launch<double>(c, rhs, T, q, write_rhs, nullptr, "solve_z");
 }
 void k_solve_x_f32(Ctx* c, float* rhs, const float* T) { solve_x_launch<float>(c, rhs, T, "solve_x_f32"); }
 void k_solve_y_f32(Ctx* c, float* rhs, const float* T) { solve_y_launch<float>(c, rhs, T, "solve_y_f32"); }
-void k_solve_z_f32(Ctx* c, float* rhs, const float* T, double* q) { solve_z_launch<float>(c, rhs, T, q, 0, "solve_z_f32"); }
+void k_solve_z_f32(Ctx* c, float* rhs, const float* T, double* q, float* mirror) {
+  solve_z_launch<float>(c, rhs, T, q, 0, mirror, "solve_z_f32");
+}
 
 void k_solve_x(Ctx* c, double* rhs, double betadx) {
   const double* T = table_for(c, c->g.n1m, betadx);
