@@ -337,8 +337,51 @@ __global__ void radix_hist_kernel(const int* __restrict__ key, int n, int shift,
   for (int d = threadIdx.x; d < 256; d += blockDim.x) hist[d * nblk + b] = h[d];
 }
 
+// exclusive scan of one tile of 1024 ints in place (warp-shuffle scans,
+// then a scan of the 32 warp totals); the tile total goes to tsum[tile]
+__device__ __forceinline__ int block_exclusive_scan(int v, int* wsum, int& total) {
+  const unsigned FULL = 0xffffffffu;
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int x = v;
+  for (int off = 1; off < 32; off <<= 1) {
+    int u = __shfl_up_sync(FULL, x, off);
+    if (lane >= off) x += u;
+  }
+  if (lane == 31) wsum[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    int y = (lane < (int)(blockDim.x >> 5)) ? wsum[lane] : 0;
+    for (int off = 1; off < 32; off <<= 1) {
+      int u = __shfl_up_sync(FULL, y, off);
+      if (lane >= off) y += u;
+    }
+    wsum[lane] = y;                         // inclusive warp totals
+  }
+  __syncthreads();
+  total = wsum[(blockDim.x >> 5) - 1];
+  return x - v + (w > 0 ? wsum[w - 1] : 0);
+}
+
+__global__ void scan_tile_kernel(int* __restrict__ a, int m, int* __restrict__ tsum, const int* __restrict__ dirty) {
+  if (!*dirty) return;
+  __shared__ int wsum[32];
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  int v = (idx < m) ? a[idx] : 0;
+  int total;
+  int ex = block_exclusive_scan(v, wsum, total);
+  if (idx < m) a[idx] = ex;
+  if (threadIdx.x == 0) tsum[blockIdx.x] = total;
+}
+
+__global__ void scan_add_kernel(int* __restrict__ a, int m, const int* __restrict__ tsum, const int* __restrict__ dirty) {
+  if (!*dirty) return;
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < m && blockIdx.x > 0) a[idx] += tsum[blockIdx.x];
+}
+
 // exclusive scan of m ints by one block of 1024 threads: coalesced tiles
 // of 1024, warp-shuffle scans inside a tile, a running carry across tiles
+// (used on the tile totals of the multi-block scan)
 __global__ void scan_kernel(int* __restrict__ a, int m, const int* __restrict__ dirty) {
   if (!*dirty) return;
   __shared__ int wsum[32];
@@ -1007,6 +1050,7 @@ struct LagState {
   // merged scatter plan
   int plan_n = 0, plan_cap = 0, nblk = 0;
   int *key = nullptr, *src = nullptr, *tmp_key = nullptr, *tmp_src = nullptr, *hist = nullptr;
+  int* tsum = nullptr;   // tile totals of the histogram scan
   int *res_key = nullptr, *res_src = nullptr;   // buffers holding the sorted result
   int* saved = nullptr;                          // 7 ints per face: pind(1:6), ghost
   int* dirty = nullptr;
@@ -1079,6 +1123,7 @@ static bool ensure_lag_buffers(Ctx* c) {
               cuda_ok(c, cudaMalloc(&s->tmp_key, sizeof(int) * n), "plan") &&
               cuda_ok(c, cudaMalloc(&s->tmp_src, sizeof(int) * n), "plan") &&
               cuda_ok(c, cudaMalloc(&s->hist, sizeof(int) * 256 * (size_t)s->nblk), "plan") &&
+              cuda_ok(c, cudaMalloc(&s->tsum, sizeof(int) * (size_t)div_up(256 * (size_t)s->nblk, 1024)), "plan") &&
               cuda_ok(c, cudaMalloc(&s->saved, sizeof(int) * 7 * (size_t)std::max(1, c->maxnf)), "plan") &&
               cuda_ok(c, cudaMalloc(&s->dirty, sizeof(int)), "plan") &&
               cuda_ok(c, cudaMalloc(&s->segval, sizeof(double) * n), "plan");
@@ -1136,7 +1181,11 @@ static void update_plan(Ctx* c) {
     { MIBM_PROF(c, "radix_hist");
       radix_hist_kernel<<<s->nblk, 256, 0, c->stream>>>(kin, n, shift, s->nblk, s->dirty, s->hist); }
     { MIBM_PROF(c, "radix_scan");
-      scan_kernel<<<1, 1024, 0, c->stream>>>(s->hist, 256 * s->nblk, s->dirty); }
+      int m = 256 * s->nblk;
+      unsigned tiles = div_up(m, 1024);
+      scan_tile_kernel<<<tiles, 1024, 0, c->stream>>>(s->hist, m, s->tsum, s->dirty);
+      scan_kernel<<<1, 1024, 0, c->stream>>>(s->tsum, (int)tiles, s->dirty);
+      scan_add_kernel<<<tiles, 1024, 0, c->stream>>>(s->hist, m, s->tsum, s->dirty); }
     { MIBM_PROF(c, "radix_scatter");
       radix_scatter_kernel<<<s->nblk, 256, 0, c->stream>>>(kin, vin, kout, vout, n, shift, s->nblk, s->hist, s->dirty); }
     std::swap(kin, kout); std::swap(vin, vout);
@@ -1144,7 +1193,7 @@ static void update_plan(Ctx* c) {
   s->res_key = kin; s->res_src = vin;         // fixed per grid: the buffers of the last pass
   { MIBM_PROF(c, "plan_commit");
     plan_commit_kernel<<<div_up(nf, 256), 256, 0, c->stream>>>(nf, pind, ghost, s->saved, s->dirty); }
-  c->launches += 3 + 3 * passes;
+  c->launches += 3 + 5 * passes;
   MIBM_LAUNCH_CHECK(c, "scatter plan");
 }
 
@@ -1475,6 +1524,7 @@ void lagr_free(Ctx* c) {
       cudaFree(s->adj_off); cudaFree(s->adj_face); cudaFree(s->face_part); cudaFree(s->geom_out);
       cudaFree(s->mean3); cudaFree(s->sdf_bits); cudaFree(s->winner); cudaFree(s->dist_buf);
       cudaFree(s->key); cudaFree(s->src); cudaFree(s->tmp_key); cudaFree(s->tmp_src); cudaFree(s->hist);
+      cudaFree(s->tsum);
       cudaFree(s->saved); cudaFree(s->dirty); cudaFree(s->segval);
       delete s;
       g_lag.erase(g_lag.begin() + q);

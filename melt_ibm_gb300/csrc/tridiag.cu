@@ -15,11 +15,25 @@
 //             x_i = x_n s_i + f_i
 // = 4 FP64 operations per element, one read and one write of the line.
 //
-// Lines are staged through shared memory in tiles of up to 32 lines that are
-// contiguous in the fastest address direction, so global loads and stores
-// are coalesced in every direction: x-lines are rows (tile = 32 rows of one
-// k-plane, row pitch n+1 in shared memory), y- and z-lines are columns
-// (tile = 32 adjacent i).  One thread runs one line's recurrences.
+// Main path (chunked solves): a line of n cells is cut into G chunks of M
+// cells and each thread keeps one chunk in registers.  The two recurrences
+// are linear, so a chunk runs them from a zero entry value and corrects
+// afterwards with its true entry value times a factor that depends on the
+// table only (prefix products of -b, suffix products of q):
+//   forward   C_e = a_e r_e - b_e C_{e-1}          y_e = C_e + P_e y_in
+//   backward  D_e = C_e + q_e D_{e+1}              f_e = D_e + DP_e y_in + Q_e f_in
+// with P_e = prod(-b) from the chunk start to e, Q_e = prod(q) from e to the
+// chunk end and DP_e = P_e + q_e DP_{e+1}.  The entry values y_in, f_in of
+// the chunks are a scan over the chunk end values: warp shuffles for
+// x-lines (one warp per line, lane = chunk, contiguous vector loads), shared
+// memory for y- and z-lines (lane = adjacent i, warp = chunk, coalesced
+// rows).  The last cell of the line joins the last chunk through zero
+// coefficients (a = b = q = 0, s = 1), so every chunk is alike.  Rounding
+// differs from the sequential sweep only in summation order.
+//
+// Fallback (line lengths the chunking does not split, and the allocation-
+// free entry point): lines staged through shared memory in tiles of 32
+// lines, one thread running one line's sequential sweep.
 #include <cmath>
 #include <mutex>
 #include <vector>
@@ -63,6 +77,9 @@ static void build_table(int n, double betadx, std::vector<double>& t) {
   t[4 * n + 3] = 1.0 / den;
 }
 
+static size_t slot_len(int nmax);
+static void fill_slot(int n, double betadx, double* out);
+
 // Device table cache: small ring of slots, refilled when (n, betadx) changes.
 struct TriCache {
   double* dev = nullptr;
@@ -94,7 +111,7 @@ static const double* table_for(Ctx* c, int n, double betadx) {
   int nmax = std::max(c->g.n1m, c->g.n3m);
   if (!tc.dev) {
     tc.slots = 64;
-    tc.len = 4 * nmax + 4;
+    tc.len = (int)slot_len(nmax);
     if (!cuda_ok(c, cudaMalloc(&tc.dev, sizeof(double) * tc.len * tc.slots), "tri table")) return nullptr;
     if (!cuda_ok(c, cudaMallocHost(&tc.pinned, sizeof(double) * tc.len * tc.slots), "tri table")) return nullptr;
     tc.n.assign(tc.slots, -1);
@@ -104,12 +121,10 @@ static const double* table_for(Ctx* c, int n, double betadx) {
     if (tc.n[s] == n && tc.bd[s] == betadx) return tc.dev + (size_t)s * tc.len;
   int s = tc.next;
   tc.next = (tc.next + 1) % tc.slots;
-  std::vector<double> t;
-  build_table(n, betadx, t);
   // a slot may still be read by an in-flight kernel: order the refill on the stream
   cudaStreamSynchronize(c->stream);
-  std::copy(t.begin(), t.end(), tc.pinned + (size_t)s * tc.len);
-  cudaMemcpyAsync(tc.dev + (size_t)s * tc.len, tc.pinned + (size_t)s * tc.len, sizeof(double) * t.size(),
+  fill_slot(n, betadx, tc.pinned + (size_t)s * tc.len);
+  cudaMemcpyAsync(tc.dev + (size_t)s * tc.len, tc.pinned + (size_t)s * tc.len, sizeof(double) * tc.len,
                   cudaMemcpyHostToDevice, c->stream);
   tc.n[s] = n;
   tc.bd[s] = betadx;
@@ -291,6 +306,279 @@ __global__ void solve_z_kernel(Grid g, V* __restrict__ rhs, const V* __restrict_
 }
 
 
+// ---------------------------------------------------------------------
+// chunked solves
+// ---------------------------------------------------------------------
+// Chunk lengths with a kernel instance.  x-lines: G = n/M lanes of one warp
+// (largest G <= 32); y/z-lines: G = n/M warps of one block (M as large as
+// possible, G <= 32).  0 = not split, use the tile kernels.
+static const int kChunkM[] = {2, 3, 4, 6, 8, 12, 16};
+
+static bool chunk_ok(int m) {
+  for (int v : kChunkM)
+    if (v == m) return true;
+  return false;
+}
+
+int tri_chunk_line(int n) {
+  for (int G = 32; G >= 1; --G)
+    if (n % G == 0 && chunk_ok(n / G)) return n / G;
+  return 0;
+}
+
+constexpr int kColMaxChunks = 16;   // y/z blocks of at most 32 x 16 threads (register budget)
+
+int tri_chunk_col(int n) {
+  static const int pref[] = {16, 12, 8, 6, 4, 3, 2};
+  for (int m : pref)
+    if (n % m == 0 && n / m <= kColMaxChunks) return m;
+  return 0;
+}
+
+// extended table of (n, M): element arrays a, b, q, s, P, Q, DP at offsets
+// 0, n, .., 6n, element e stored at (e % M) * G + e / M (a warp reads one
+// word per lane, or one broadcast word); then PL (P at each chunk end), QF (Q
+// at each chunk start), DPF (DP at each chunk start), then the four scalars
+// ackl_b, api, ami, 1/den of the base table.
+static size_t ext_len(int n, int m) { return m ? 7 * (size_t)n + 3 * (size_t)(n / m) + 4 : 0; }
+
+static void build_ext(const std::vector<double>& t, int n, int m, double* out) {
+  int G = n / m;
+  std::vector<double> a(t.begin(), t.begin() + n), b(t.begin() + n, t.begin() + 2 * n);
+  std::vector<double> q(t.begin() + 2 * n, t.begin() + 3 * n), s(t.begin() + 3 * n, t.begin() + 4 * n);
+  a[n - 1] = 0.0; b[n - 1] = 0.0; q[n - 1] = 0.0; b[0] = 0.0; s[n - 1] = 1.0;
+  auto pos = [&](int e) { return (size_t)(e % m) * G + e / m; };
+  std::vector<double> P(n);
+  for (int e = 0; e < n; ++e) {
+    out[pos(e)] = a[e];
+    out[n + pos(e)] = b[e];
+    out[2 * (size_t)n + pos(e)] = q[e];
+    out[3 * (size_t)n + pos(e)] = s[e];
+  }
+  for (int h = 0; h < G; ++h) {
+    int st = h * m, en = st + m - 1;
+    double pv = 1.0;
+    for (int e = st; e <= en; ++e) { pv = -b[e] * pv; P[e] = pv; out[4 * (size_t)n + pos(e)] = pv; }
+    out[7 * (size_t)n + h] = pv;
+    double qv = 1.0, dv = 0.0;
+    for (int e = en; e >= st; --e) {
+      qv = q[e] * qv;
+      dv = P[e] + q[e] * dv;
+      out[5 * (size_t)n + pos(e)] = qv;
+      out[6 * (size_t)n + pos(e)] = dv;
+    }
+    out[7 * (size_t)n + G + h] = qv;
+    out[7 * (size_t)n + 2 * G + h] = dv;
+  }
+  for (int w = 0; w < 4; ++w) out[7 * (size_t)n + 3 * G + w] = t[4 * (size_t)n + w];
+}
+
+// one table slot: base table (tile kernels), extended table for x-lines,
+// extended table for y/z-lines
+struct TriLayout {
+  int n, m_line, m_col;
+  size_t off_line, off_col, len;
+};
+
+static TriLayout tri_layout(int n) {
+  TriLayout L;
+  L.n = n;
+  L.m_line = tri_chunk_line(n);
+  L.m_col = tri_chunk_col(n);
+  L.off_line = 4 * (size_t)n + 4;
+  L.off_col = L.off_line + ext_len(n, L.m_line);
+  L.len = L.off_col + ext_len(n, L.m_col);
+  return L;
+}
+
+// fills one slot (base + both extended tables) for (n, betadx)
+static void fill_slot(int n, double betadx, double* out) {
+  std::vector<double> t;
+  build_table(n, betadx, t);
+  TriLayout L = tri_layout(n);
+  std::copy(t.begin(), t.end(), out);
+  if (L.m_line) build_ext(t, n, L.m_line, out + L.off_line);
+  if (L.m_col) build_ext(t, n, L.m_col, out + L.off_col);
+}
+
+static size_t slot_len(int nmax) {
+  size_t len = 0;
+  for (int n = 1; n <= nmax; ++n) len = std::max(len, tri_layout(n).len);
+  return len;
+}
+
+template <typename V, int M>
+__device__ __forceinline__ void load_chunk(const V* __restrict__ p, V (&r)[M]) {
+  if constexpr (sizeof(V) == 4 && M % 4 == 0) {
+#pragma unroll
+    for (int v = 0; v < M / 4; ++v) {
+      float4 t = reinterpret_cast<const float4*>(p)[v];
+      r[4 * v] = t.x; r[4 * v + 1] = t.y; r[4 * v + 2] = t.z; r[4 * v + 3] = t.w;
+    }
+  } else if constexpr (sizeof(V) == 8 && M % 2 == 0) {
+#pragma unroll
+    for (int v = 0; v < M / 2; ++v) {
+      double2 t = reinterpret_cast<const double2*>(p)[v];
+      r[2 * v] = t.x; r[2 * v + 1] = t.y;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < M; ++i) r[i] = p[i];
+  }
+}
+
+template <typename V, int M>
+__device__ __forceinline__ void store_chunk(V* __restrict__ p, const V (&r)[M]) {
+  if constexpr (sizeof(V) == 4 && M % 4 == 0) {
+#pragma unroll
+    for (int v = 0; v < M / 4; ++v)
+      reinterpret_cast<float4*>(p)[v] = make_float4(r[4 * v], r[4 * v + 1], r[4 * v + 2], r[4 * v + 3]);
+  } else if constexpr (sizeof(V) == 8 && M % 2 == 0) {
+#pragma unroll
+    for (int v = 0; v < M / 2; ++v) reinterpret_cast<double2*>(p)[v] = make_double2(r[2 * v], r[2 * v + 1]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < M; ++i) p[i] = r[i];
+  }
+}
+
+// x-lines: one warp per line (row j of plane k), lane h < G holds cells
+// [h*M, h*M + M).  Rows start on 16-byte boundaries (pitch multiple of 4).
+template <typename V, int M>
+__global__ void __launch_bounds__(256) solve_xc_kernel(Grid g, V* __restrict__ rhs, const V* __restrict__ X) {
+  const unsigned FULL = 0xffffffffu;
+  const int n = g.n1m, G = n / M;
+  const int lane = threadIdx.x & 31;
+  const int line = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (line >= g.n2m * g.n3m) return;                 // whole warp
+  const int j = line % g.n2m, k = line / g.n2m;
+  const bool act = lane < G;
+  V* row = rhs + cidx(g, 0, j, k) + (size_t)(act ? lane : 0) * M;
+  V r[M];
+  if (act) load_chunk<V, M>(row, r);
+  else {
+#pragma unroll
+    for (int i = 0; i < M; ++i) r[i] = V(0);
+  }
+  const V rlast = r[M - 1];
+  const int h = act ? lane : 0;
+  // forward, zero entry
+  V C = V(0);
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
+    int t = i * G + h;
+    C = X[t] * r[i] - X[n + t] * C;
+    r[i] = C;
+  }
+  // y_in: exclusive scan of the affine chunk maps y -> C + PL y
+  V Cv = act ? C : V(0), Pv = act ? X[7 * n + h] : V(1);
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    V Co = __shfl_up_sync(FULL, Cv, off), Po = __shfl_up_sync(FULL, Pv, off);
+    if (lane >= off) { Cv = Cv + Pv * Co; Pv = Pv * Po; }
+  }
+  V y_in = __shfl_up_sync(FULL, Cv, 1);
+  if (lane == 0) y_in = V(0);
+  // backward, zero entry
+  V D = V(0);
+#pragma unroll
+  for (int i = M - 1; i >= 0; --i) {
+    D = r[i] + X[2 * n + i * G + h] * D;
+    r[i] = D;
+  }
+  // f_in: exclusive suffix scan of f -> u + QF f, u = D_first + DPF y_in
+  V Uv = act ? r[0] + X[7 * n + 2 * G + h] * y_in : V(0), Qv = act ? X[7 * n + G + h] : V(1);
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    V Uo = __shfl_down_sync(FULL, Uv, off), Qo = __shfl_down_sync(FULL, Qv, off);
+    if (lane + off < G) { Uv = Uv + Qv * Uo; Qv = Qv * Qo; }
+  }
+  V f_in = __shfl_down_sync(FULL, Uv, 1);
+  if (lane + 1 >= G) f_in = V(0);
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
+    int t = i * G + h;
+    r[i] = r[i] + X[6 * n + t] * y_in + X[5 * n + t] * f_in;
+  }
+  // periodic closure
+  const V* S = X + 7 * n + 3 * G;
+  V f1 = __shfl_sync(FULL, r[0], 0);
+  V fnm1 = __shfl_sync(FULL, r[M - 2], G - 1);
+  V rn = __shfl_sync(FULL, rlast, G - 1);
+  V xn = (rn * S[0] - S[1] * f1 - S[2] * fnm1) * S[3];
+#pragma unroll
+  for (int i = 0; i < M; ++i) r[i] = xn * X[3 * n + i * G + h] + r[i];
+  if (act) store_chunk<V, M>(row, r);
+}
+
+// y- and z-lines: block = 32 adjacent i (lanes) x G chunks (warps) of one
+// plane k (y-lines) or one row j (z-lines).  For z-lines the result is added
+// to q (solxk.f90:44-50), optionally also left in rhs, and in the precision
+// form copied to the FP32 mirror m32.
+template <typename V, int M, bool ZL>
+__global__ void __launch_bounds__(32 * kColMaxChunks) solve_cc_kernel(Grid g, V* __restrict__ rhs, const V* __restrict__ X,
+                                                        double* __restrict__ q, int write_rhs, float* __restrict__ m32) {
+  __shared__ V sC[kColMaxChunks][32];
+  __shared__ V sU[kColMaxChunks][32];
+  __shared__ V sF[3][32];
+  const int n = ZL ? g.n3m : g.n2m, G = n / M;
+  const int lane = threadIdx.x, w = threadIdx.y;
+  const int x = blockIdx.x * 32 + lane;
+  const bool act = x < g.n1m;
+  const size_t stride = ZL ? g.plane : (size_t)g.P;
+  const size_t base = ZL ? cidx(g, act ? x : 0, blockIdx.y, 0) : cidx(g, act ? x : 0, 0, blockIdx.y);
+  const int e0 = w * M;
+  V r[M];
+#pragma unroll
+  for (int i = 0; i < M; ++i) r[i] = act ? rhs[base + (size_t)(e0 + i) * stride] : V(0);
+  const V rlast = r[M - 1];
+  V C = V(0);
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
+    int t = i * G + w;
+    C = X[t] * r[i] - X[n + t] * C;
+    r[i] = C;
+  }
+  sC[w][lane] = C;
+  __syncthreads();
+  V y_in = V(0);
+  for (int hh = 0; hh < w; ++hh) y_in = sC[hh][lane] + X[7 * n + hh] * y_in;
+  V D = V(0);
+#pragma unroll
+  for (int i = M - 1; i >= 0; --i) {
+    D = r[i] + X[2 * n + i * G + w] * D;
+    r[i] = D;
+  }
+  sU[w][lane] = r[0] + X[7 * n + 2 * G + w] * y_in;
+  __syncthreads();
+  V f_in = V(0);
+  for (int hh = G - 1; hh > w; --hh) f_in = sU[hh][lane] + X[7 * n + G + hh] * f_in;
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
+    int t = i * G + w;
+    r[i] = r[i] + X[6 * n + t] * y_in + X[5 * n + t] * f_in;
+  }
+  if (w == 0) sF[0][lane] = r[0];
+  if (w == G - 1) { sF[1][lane] = r[M - 2]; sF[2][lane] = rlast; }
+  __syncthreads();
+  const V* S = X + 7 * n + 3 * G;
+  V xn = (sF[2][lane] * S[0] - S[1] * sF[0][lane] - S[2] * sF[1][lane]) * S[3];
+  if (!act) return;
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
+    V xv = xn * X[3 * n + i * G + w] + r[i];
+    size_t c0 = base + (size_t)(e0 + i) * stride;
+    if (ZL) {
+      if (write_rhs) rhs[c0] = xv;
+      double qn = q[c0] + (double)xv;
+      q[c0] = qn;
+      if (m32) m32[c0] = (float)qn;
+    } else {
+      rhs[c0] = xv;
+    }
+  }
+}
+
 // Tables of one fused RK3 step: [substep][velocity|temperature][x|y|z].
 // Built on the host once per step into one of two pinned buffers (the one
 // not read by the previous step's copy) and copied in stream order.
@@ -315,7 +603,7 @@ const double* tri_step_prepare(Ctx* c, const double betadx[3][2][3], int* len_ou
   StepTables* st = steptab_of(c);
   int nmax = std::max(c->g.n1m, c->g.n3m);
   if (!st->dev) {
-    st->len = 4 * nmax + 4;
+    st->len = (int)slot_len(nmax);
     size_t bytes = sizeof(double) * 18 * (size_t)st->len;
     if (!cuda_ok(c, cudaMalloc(&st->dev, bytes), "step tables")) return nullptr;
     if (!cuda_ok(c, cudaMalloc(&st->devf, bytes / 2), "step tables")) return nullptr;
@@ -328,13 +616,10 @@ const double* tri_step_prepare(Ctx* c, const double betadx[3][2][3], int* len_ou
   st->parity ^= 1;
   cudaEventSynchronize(st->copied[p]);            // the copy that last read pinned[p]
   const int n[3] = {c->g.n1m, c->g.n2m, c->g.n3m};
-  std::vector<double> t;
   for (int ns = 0; ns < 3; ++ns)
     for (int f = 0; f < 2; ++f)
-      for (int d = 0; d < 3; ++d) {
-        build_table(n[d], betadx[ns][f][d], t);
-        std::copy(t.begin(), t.end(), st->pinned[p] + (size_t)((ns * 2 + f) * 3 + d) * st->len);
-      }
+      for (int d = 0; d < 3; ++d)
+        fill_slot(n[d], betadx[ns][f][d], st->pinned[p] + (size_t)((ns * 2 + f) * 3 + d) * st->len);
   cudaMemcpyAsync(st->dev, st->pinned[p], sizeof(double) * 18 * (size_t)st->len, cudaMemcpyHostToDevice, c->stream);
   if (f32_out) {
     float* hf = (float*)(st->pinned[p] + 18 * (size_t)st->len);
@@ -369,8 +654,55 @@ static bool smem_ok(Ctx* c, const void* fn, size_t bytes) {
   return true;
 }
 
+#define MIBM_CHUNK_CASES(M_, CALL) \
+  switch (M_) {                       \
+    case 2: CALL(2); break;           \
+    case 3: CALL(3); break;           \
+    case 4: CALL(4); break;           \
+    case 6: CALL(6); break;           \
+    case 8: CALL(8); break;           \
+    case 12: CALL(12); break;         \
+    case 16: CALL(16); break;         \
+  }
+
+template <typename V>
+static bool solve_xc_launch(Ctx* c, V* rhs, const V* T, const char* name) {
+  TriLayout L = tri_layout(c->g.n1m);
+  if (!L.m_line) return false;
+  const V* X = T + L.off_line;
+  dim3 grid(div_up((size_t)c->g.n2m * c->g.n3m, 8));
+  {
+    MIBM_PROF(c, name);
+#define XC(M) solve_xc_kernel<V, M><<<grid, 256, 0, c->stream>>>(c->g, rhs, X)
+    MIBM_CHUNK_CASES(L.m_line, XC)
+#undef XC
+  }
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, name);
+  return true;
+}
+
+template <typename V, bool ZL>
+static bool solve_cc_launch(Ctx* c, V* rhs, const V* T, double* q, int write_rhs, float* m32, const char* name) {
+  TriLayout L = tri_layout(ZL ? c->g.n3m : c->g.n2m);
+  if (!L.m_col) return false;
+  const V* X = T + L.off_col;
+  dim3 block(32, L.n / L.m_col);
+  dim3 grid(div_up(c->g.n1m, 32), ZL ? c->g.n2m : c->g.n3m);
+  {
+    MIBM_PROF(c, name);
+#define CC(M) solve_cc_kernel<V, M, ZL><<<grid, block, 0, c->stream>>>(c->g, rhs, X, q, write_rhs, m32)
+    MIBM_CHUNK_CASES(L.m_col, CC)
+#undef CC
+  }
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, name);
+  return true;
+}
+
 template <typename V>
 static void solve_x_launch(Ctx* c, V* rhs, const V* T, const char* name) {
+  if (solve_xc_launch<V>(c, rhs, T, name)) return;
   size_t sm = ((size_t)kLines * (c->g.n1m + 1) + 4 * (size_t)c->g.n1m + 4) * sizeof(V);
   if (!smem_ok(c, (const void*)solve_x_kernel<V>, sm)) return;
   dim3 grid(div_up(c->g.n2m, kLines), c->g.n3m);
@@ -381,6 +713,7 @@ static void solve_x_launch(Ctx* c, V* rhs, const V* T, const char* name) {
 
 template <typename V>
 static void solve_y_launch(Ctx* c, V* rhs, const V* T, const char* name) {
+  if (solve_cc_launch<V, false>(c, rhs, T, nullptr, 0, nullptr, name)) return;
   size_t sm = ((size_t)kLines * c->g.n2m + 4 * (size_t)c->g.n2m + 4) * sizeof(V);
   if (!smem_ok(c, (const void*)solve_y_kernel<V>, sm)) return;
   dim3 grid(div_up(c->g.n1m, kLines), c->g.n3m);
@@ -391,6 +724,7 @@ static void solve_y_launch(Ctx* c, V* rhs, const V* T, const char* name) {
 
 template <typename V>
 static void solve_z_launch(Ctx* c, V* rhs, const V* T, double* q, int write_rhs, float* m32, const char* name) {
+  if (solve_cc_launch<V, true>(c, rhs, T, q, write_rhs, m32, name)) return;
   size_t sm = ((size_t)kLines * c->g.n3m + 4 * (size_t)c->g.n3m + 4) * sizeof(V);
   if (!smem_ok(c, (const void*)solve_z_kernel<V>, sm)) return;
   dim3 grid(div_up(c->g.n1m, kLines), c->g.n2m);
