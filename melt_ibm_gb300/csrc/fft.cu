@@ -14,41 +14,17 @@
 //   X' c2r along x   two Hermitian half-rows packed as one complex line
 // Line FFTs are Stockham autosort transforms with radix-4/2/3 stages
 // (n = 2^a 3^b), twiddles e^{-2 pi i m/n} tabulated on the host in FP64 and
-// staged in shared memory.  Unnormalised, FFTW sign convention
+// staged in shared memory.  Each pass runs the kernel of fft_fast.cuh
+// specialised for its line length when the length has one; the kernels
+// below take any length (run-time plan).  Unnormalised, FFTW sign convention
 // (forward = e^{-i...}).  The c2r pass drops the imaginary parts of the
 // kx = 0 and kx = n1m/2 bins, as a Hermitian c2r transform does.
 #include <cmath>
 #include <vector>
 
-#include "common.cuh"
+#include "fft_common.cuh"
 
 namespace mibm {
-
-struct Plan1D {
-  int n = 0;
-  int nst = 0;
-  int radix[16];
-};
-
-static Plan1D make_plan(int n) {
-  Plan1D p;
-  p.n = n;
-  int m = n;
-  while (m % 4 == 0) { p.radix[p.nst++] = 4; m /= 4; }
-  while (m % 2 == 0) { p.radix[p.nst++] = 2; m /= 2; }
-  while (m % 3 == 0) { p.radix[p.nst++] = 3; m /= 3; }
-  return p;
-}
-
-// complex helpers for double2 / float2
-template <typename C> struct Real;
-template <> struct Real<double2> { typedef double T; };
-template <> struct Real<float2> { typedef float T; };
-template <typename C> __device__ __forceinline__ C mk(typename Real<C>::T x, typename Real<C>::T y) { C r; r.x = x; r.y = y; return r; }
-template <typename C> __device__ __forceinline__ C cmul(C a, C b) { return mk<C>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
-template <typename C> __device__ __forceinline__ C cadd(C a, C b) { return mk<C>(a.x + b.x, a.y + b.y); }
-template <typename C> __device__ __forceinline__ C csub(C a, C b) { return mk<C>(a.x - b.x, a.y - b.y); }
-template <typename C> __device__ __forceinline__ C conjc(C a) { return mk<C>(a.x, -a.y); }
 
 // Batched Stockham FFT of `nl` lines of length n held in shared memory.
 // Element e of line l lives at buf[l*LS + e*ES].  Ping-pong between A and B;
@@ -106,28 +82,6 @@ __device__ C* fft_lines(C* A, C* B, int n, int nl, int LS, int ES, const Plan1D&
   }
   return A;
 }
-
-template <typename C>
-struct FftArgs {
-  typedef typename Real<C>::T R;
-  Grid g;
-  Plan1D px, py, pz;
-  const C* twx;
-  const C* twy;
-  const C* twz;
-  const R* ak1;
-  const R* ak2;
-  const R* ak3;
-  R inv_nn;
-};
-
-template <typename C>
-__device__ __forceinline__ void load_tw(C* s, const C* tw, int n) {
-  for (int m = threadIdx.x; m < n; m += blockDim.x) s[m] = tw[m];
-}
-
-constexpr int kRowPairs = 4;   // X passes: 4 complex lines (8 real rows) per CTA
-constexpr int kCols = 8;       // Y/Z passes: 8 adjacent kx columns per CTA
 
 // X forward: real rows (j, j+1) of plane k (source type S) -> half spectra
 template <typename C, typename S>
@@ -350,11 +304,17 @@ static void phcalc_launch(Ctx* c, FftArgs<C> F, const S* src, typename Real<C>::
   dim3 gy(div_up(g.H, kCols), g.n3m);
   dim3 gz(div_up(g.H, kCols), g.n2m);
   bool f32 = sizeof(C) == sizeof(float2);
-  { MIBM_PROF(c, f32 ? "fft_x_fwd_f32" : "fft_x_fwd"); fft_x_fwd<C, S><<<gx, 256, smx, c->stream>>>(F, src, spec); }
-  { MIBM_PROF(c, f32 ? "fft_y_f32" : "fft_y"); fft_y<C><<<gy, 256, smy, c->stream>>>(F, spec, -1); }
-  { MIBM_PROF(c, f32 ? "fft_z_solve_f32" : "fft_z_solve"); fft_z_solve<C><<<gz, 256, smz, c->stream>>>(F, spec); }
-  { MIBM_PROF(c, f32 ? "fft_y_f32" : "fft_y"); fft_y<C><<<gy, 256, smy, c->stream>>>(F, spec, +1); }
-  { MIBM_PROF(c, f32 ? "fft_x_inv_f32" : "fft_x_inv"); fft_x_inv<C><<<gx, 256, smx, c->stream>>>(F, spec, dst); }
+  // each pass: the kernel specialised for its line length where one exists
+  { MIBM_PROF(c, f32 ? "fft_x_fwd_f32" : "fft_x_fwd");
+    if (!fastfft_x_fwd<C, S>(c, F, src, spec)) fft_x_fwd<C, S><<<gx, 256, smx, c->stream>>>(F, src, spec); }
+  { MIBM_PROF(c, f32 ? "fft_y_f32" : "fft_y");
+    if (!fastfft_y<C>(c, F, spec, -1)) fft_y<C><<<gy, 256, smy, c->stream>>>(F, spec, -1); }
+  { MIBM_PROF(c, f32 ? "fft_z_solve_f32" : "fft_z_solve");
+    if (!fastfft_z_solve<C>(c, F, spec)) fft_z_solve<C><<<gz, 256, smz, c->stream>>>(F, spec); }
+  { MIBM_PROF(c, f32 ? "fft_y_f32" : "fft_y");
+    if (!fastfft_y<C>(c, F, spec, +1)) fft_y<C><<<gy, 256, smy, c->stream>>>(F, spec, +1); }
+  { MIBM_PROF(c, f32 ? "fft_x_inv_f32" : "fft_x_inv");
+    if (!fastfft_x_inv<C>(c, F, spec, dst)) fft_x_inv<C><<<gx, 256, smx, c->stream>>>(F, spec, dst); }
   c->launches += 5;
   MIBM_LAUNCH_CHECK(c, tag);
 }

@@ -1,0 +1,363 @@
+// fft_fast.cuh -- Poisson-solve FFT passes specialised for one line length N
+// at compile time (phcalc.f90:11-97, same chain and conventions as fft.cu).
+//
+// A block transforms L lines of length N held in one shared buffer, element
+// e of line l at buf[e*(L+1) + l] (the padding keeps both the column loads
+// of the y/z passes and the row loads of the x passes free of bank
+// conflicts).  Each Stockham stage reads every butterfly's inputs into
+// registers, synchronises, applies the twiddles and the radix-4/2/3
+// butterfly and writes the outputs in place; stage radices, strides and
+// twiddle steps are compile-time constants, so no index division is left
+// at run time.  Twiddles e^{-2 pi i m/N} are the FP64-tabulated table of
+// fft.cu, staged in shared memory.  L is chosen so that a block moves 128
+// contiguous bytes per spectrum row and a thread holds 16 (FP32) or 8
+// (FP64) complex values per stage.
+#pragma once
+
+#include "fft_common.cuh"
+
+namespace mibm {
+namespace fastfft {
+
+__host__ __device__ constexpr int nstages(int n) {
+  int s = 0;
+  while (n % 4 == 0) { n /= 4; ++s; }
+  while (n % 2 == 0) { n /= 2; ++s; }
+  while (n % 3 == 0) { n /= 3; ++s; }
+  return s;
+}
+
+__host__ __device__ constexpr int radix_at(int n, int st) {
+  int s = 0;
+  while (n % 4 == 0) { if (s == st) return 4; n /= 4; ++s; }
+  while (n % 2 == 0) { if (s == st) return 2; n /= 2; ++s; }
+  while (n % 3 == 0) { if (s == st) return 3; n /= 3; ++s; }
+  return 1;
+}
+
+// lines per block and threads per block for length N and complex type C
+template <typename C, int N>
+struct Shape {
+  static constexpr int kWork = sizeof(C) == 8 ? 4096 : 2048;   // values per block
+  static constexpr int L = (kWork / N) < 1 ? 1 : ((kWork / N) > 32 ? 32 : kWork / N);
+  static constexpr int T = 256;
+  static constexpr int ES = L + 1;
+  static constexpr size_t smem = sizeof(C) * ((size_t)N + (size_t)N * ES);
+};
+
+template <typename C, int R, bool INV>
+__device__ __forceinline__ void butterfly(C (&v)[R]) {
+  typedef typename Real<C>::T Rt;
+  if constexpr (R == 4) {
+    C a02p = cadd(v[0], v[2]), a02m = csub(v[0], v[2]);
+    C a13p = cadd(v[1], v[3]), a13m = csub(v[1], v[3]);
+    // -i*(a1-a3) for the forward sign, +i*(a1-a3) for the inverse
+    C rot = INV ? mk<C>(-a13m.y, a13m.x) : mk<C>(a13m.y, -a13m.x);
+    v[0] = cadd(a02p, a13p);
+    v[2] = csub(a02p, a13p);
+    v[1] = cadd(a02m, rot);
+    v[3] = csub(a02m, rot);
+  } else if constexpr (R == 2) {
+    C a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+  } else {
+    const Rt s3 = Rt(0.86602540378443864676);   // sqrt(3)/2
+    C t1 = cadd(v[1], v[2]), t2 = csub(v[1], v[2]);
+    C m = mk<C>(v[0].x - Rt(0.5) * t1.x, v[0].y - Rt(0.5) * t1.y);
+    // forward: -i*s3*t2 ; inverse: +i*s3*t2
+    C sv = INV ? mk<C>(-s3 * t2.y, s3 * t2.x) : mk<C>(s3 * t2.y, -s3 * t2.x);
+    v[0] = cadd(v[0], t1);
+    v[1] = cadd(m, sv);
+    v[2] = csub(m, sv);
+  }
+}
+
+// one Stockham stage of radix R after NS points have been combined
+template <typename C, int N, int L, int T, int R, int NS, bool INV>
+__device__ __forceinline__ void stage(C* buf, const C* tw) {
+  constexpr int ES = L + 1, NB = N / R, TOT = NB * L, PER = (TOT + T - 1) / T, TS = N / (NS * R);
+  C v[PER][R];
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int b = threadIdx.x + p * T;
+    if (TOT % T == 0 || b < TOT) {
+      const int l = b % L, j = b / L;
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[p][r] = buf[(j + r * NB) * ES + l];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int b = threadIdx.x + p * T;
+    if (TOT % T == 0 || b < TOT) {
+      const int l = b % L, j = b / L, kk = j % NS;
+      if constexpr (NS > 1) {
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+          C w = tw[kk * r * TS];
+          if (INV) w.y = -w.y;
+          v[p][r] = cmul(v[p][r], w);
+        }
+      }
+      butterfly<C, R, INV>(v[p]);
+      const int o = (j / NS) * NS * R + kk;
+#pragma unroll
+      for (int r = 0; r < R; ++r) buf[(o + r * NS) * ES + l] = v[p][r];
+    }
+  }
+  __syncthreads();
+}
+
+template <typename C, int N, int L, int T, bool INV, int S = 0, int NS = 1>
+__device__ __forceinline__ void run(C* buf, const C* tw) {
+  if constexpr (S < nstages(N)) {
+    constexpr int R = radix_at(N, S);
+    stage<C, N, L, T, R, NS, INV>(buf, tw);
+    run<C, N, L, T, INV, S + 1, NS * R>(buf, tw);
+  }
+}
+
+template <typename C, int N, int T>
+__device__ __forceinline__ void stage_twiddles(C* s, const C* __restrict__ tw) {
+  for (int m = threadIdx.x; m < N; m += T) s[m] = tw[m];
+}
+
+// X forward: rows (j, j+1) of plane k packed as one complex line, r2c split
+template <typename C, typename S, int N>
+__global__ void __launch_bounds__(Shape<C, N>::T) x_fwd(FftArgs<C> F, const S* __restrict__ src, C* __restrict__ spec) {
+  typedef typename Real<C>::T R;
+  constexpr int L = Shape<C, N>::L, T = Shape<C, N>::T, ES = Shape<C, N>::ES, PER = (N * L + T - 1) / T;
+  extern __shared__ __align__(16) unsigned char shraw[];
+  C* tw = (C*)shraw;
+  C* buf = tw + N;
+  stage_twiddles<C, N, T>(tw, F.twx);
+  const Grid& g = F.g;
+  const int k = blockIdx.y, jp0 = blockIdx.x * L;
+  const int npairs = min(L, g.n2m / 2 - jp0);
+  C v[PER];
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int t = threadIdx.x + p * T;
+    const int e = t % N, l = t / N;
+    if ((N * L) % T == 0 || t < N * L) {
+      if (l < npairs) {
+        const int j = 2 * (jp0 + l);
+        v[p] = mk<C>(R(src[cidx(g, e, j, k)]), R(src[cidx(g, e, j + 1, k)]));
+      } else {
+        v[p] = mk<C>(R(0), R(0));
+      }
+    }
+  }
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int t = threadIdx.x + p * T;
+    if ((N * L) % T == 0 || t < N * L) buf[(t % N) * ES + t / N] = v[p];
+  }
+  __syncthreads();
+  run<C, N, L, T, false>(buf, tw);
+  const int H = g.H;
+  for (int t = threadIdx.x; t < H * L; t += T) {
+    const int l = t / H, kx = t - l * H;
+    if (l >= npairs) continue;
+    C z = buf[kx * ES + l];
+    C zc = conjc(buf[((N - kx) % N) * ES + l]);
+    // X_a = (Z + conj Z_-)/2 ; X_b = (Z - conj Z_-)/(2i)
+    C xa = mk<C>(R(0.5) * (z.x + zc.x), R(0.5) * (z.y + zc.y));
+    C d = csub(z, zc);
+    C xb = mk<C>(R(0.5) * d.y, R(-0.5) * d.x);
+    const int j = 2 * (jp0 + l);
+    spec[(size_t)kx + (size_t)g.HP * ((size_t)j + (size_t)g.n2m * k)] = xa;
+    spec[(size_t)kx + (size_t)g.HP * ((size_t)(j + 1) + (size_t)g.n2m * k)] = xb;
+  }
+}
+
+// X inverse (c2r): half spectra of rows (j, j+1) -> real rows
+template <typename C, int N>
+__global__ void __launch_bounds__(Shape<C, N>::T) x_inv(FftArgs<C> F, const C* __restrict__ spec,
+                                                       typename Real<C>::T* __restrict__ dst) {
+  typedef typename Real<C>::T R;
+  constexpr int L = Shape<C, N>::L, T = Shape<C, N>::T, ES = Shape<C, N>::ES, PER = (N * L + T - 1) / T;
+  extern __shared__ __align__(16) unsigned char shraw[];
+  C* tw = (C*)shraw;
+  C* buf = tw + N;
+  stage_twiddles<C, N, T>(tw, F.twx);
+  const Grid& g = F.g;
+  const int H = g.H;
+  const int k = blockIdx.y, jp0 = blockIdx.x * L;
+  const int npairs = min(L, g.n2m / 2 - jp0);
+  C v[PER];
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int t = threadIdx.x + p * T;
+    const int kx = t % N, l = t / N;
+    if ((N * L) % T == 0 || t < N * L) {
+      if (l < npairs) {
+        const int j = 2 * (jp0 + l);
+        const int sk = (kx < H) ? kx : N - kx;
+        C xa = spec[(size_t)sk + (size_t)g.HP * ((size_t)j + (size_t)g.n2m * k)];
+        C xb = spec[(size_t)sk + (size_t)g.HP * ((size_t)(j + 1) + (size_t)g.n2m * k)];
+        if (sk == 0 || 2 * sk == N) { xa.y = R(0); xb.y = R(0); }
+        if (kx >= H) { xa.y = -xa.y; xb.y = -xb.y; }
+        v[p] = mk<C>(xa.x - xb.y, xa.y + xb.x);   // Z = Xa + i Xb
+      } else {
+        v[p] = mk<C>(R(0), R(0));
+      }
+    }
+  }
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int t = threadIdx.x + p * T;
+    if ((N * L) % T == 0 || t < N * L) buf[(t % N) * ES + t / N] = v[p];
+  }
+  __syncthreads();
+  run<C, N, L, T, true>(buf, tw);
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int t = threadIdx.x + p * T;
+    const int i = t % N, l = t / N;
+    if (((N * L) % T == 0 || t < N * L) && l < npairs) {
+      const int j = 2 * (jp0 + l);
+      C z = buf[i * ES + l];
+      dst[cidx(g, i, j, k)] = z.x;
+      dst[cidx(g, i, j + 1, k)] = z.y;
+    }
+  }
+}
+
+// tile of L adjacent kx columns, line elements `step` apart in the spectrum
+template <typename C, int N>
+__device__ __forceinline__ void load_cols(C* buf, const C* __restrict__ spec, size_t base, size_t step, int nc) {
+  constexpr int L = Shape<C, N>::L, T = Shape<C, N>::T, ES = Shape<C, N>::ES, PER = (N * L + T - 1) / T;
+  C v[PER];
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int t = threadIdx.x + p * T;
+    const int l = t % L, e = t / L;
+    if ((N * L) % T == 0 || t < N * L) v[p] = (l < nc) ? spec[base + l + step * e] : C{};
+  }
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int t = threadIdx.x + p * T;
+    if ((N * L) % T == 0 || t < N * L) buf[(t / L) * ES + t % L] = v[p];
+  }
+}
+
+template <typename C, int N>
+__device__ __forceinline__ void store_cols(const C* buf, C* __restrict__ spec, size_t base, size_t step, int nc) {
+  constexpr int L = Shape<C, N>::L, T = Shape<C, N>::T, ES = Shape<C, N>::ES, PER = (N * L + T - 1) / T;
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int t = threadIdx.x + p * T;
+    const int l = t % L, e = t / L;
+    if (((N * L) % T == 0 || t < N * L) && l < nc) spec[base + l + step * e] = buf[e * ES + l];
+  }
+}
+
+// Y pass (forward or inverse) on L kx columns of plane k
+template <typename C, int N, bool INV>
+__global__ void __launch_bounds__(Shape<C, N>::T) y_pass(FftArgs<C> F, C* __restrict__ spec) {
+  constexpr int L = Shape<C, N>::L, T = Shape<C, N>::T;
+  extern __shared__ __align__(16) unsigned char shraw[];
+  C* tw = (C*)shraw;
+  C* buf = tw + N;
+  stage_twiddles<C, N, T>(tw, F.twy);
+  const Grid& g = F.g;
+  const int kx0 = blockIdx.x * L, k = blockIdx.y;
+  const int nc = min(L, g.H - kx0);
+  const size_t base = (size_t)kx0 + (size_t)g.HP * (size_t)g.n2m * k;
+  load_cols<C, N>(buf, spec, base, (size_t)g.HP, nc);
+  __syncthreads();
+  run<C, N, L, T, INV>(buf, tw);
+  store_cols<C, N>(buf, spec, base, (size_t)g.HP, nc);
+}
+
+// Z pass: forward, scale, eigenvalue division, zero mode, inverse
+template <typename C, int N>
+__global__ void __launch_bounds__(Shape<C, N>::T) z_solve(FftArgs<C> F, C* __restrict__ spec) {
+  typedef typename Real<C>::T R;
+  constexpr int L = Shape<C, N>::L, T = Shape<C, N>::T, ES = Shape<C, N>::ES;
+  extern __shared__ __align__(16) unsigned char shraw[];
+  C* tw = (C*)shraw;
+  C* buf = tw + N;
+  stage_twiddles<C, N, T>(tw, F.twz);
+  const Grid& g = F.g;
+  const int kx0 = blockIdx.x * L, j = blockIdx.y;
+  const int nc = min(L, g.H - kx0);
+  const size_t zstride = (size_t)g.HP * g.n2m;
+  const size_t base = (size_t)kx0 + (size_t)g.HP * j;
+  load_cols<C, N>(buf, spec, base, zstride, nc);
+  __syncthreads();
+  run<C, N, L, T, false>(buf, tw);
+  const R a2 = F.ak2[j];
+  for (int t = threadIdx.x; t < N * L; t += T) {
+    const int l = t % L, k = t / L;
+    C v = buf[k * ES + l];
+    if (l < nc) {
+      v.x *= F.inv_nn; v.y *= F.inv_nn;                 // buft / float(n1m*n2m*n3m)
+      R d = -F.ak3[k] - F.ak1[kx0 + l] - a2;            // -ak3(k)-ak1(i)-ak2(j)
+      if (k == 0 && kx0 + l == 0 && j == 0) v = mk<C>(R(0), R(0));
+      else { R rd = R(1) / d; v.x *= rd; v.y *= rd; }
+    } else {
+      v = mk<C>(R(0), R(0));
+    }
+    buf[k * ES + l] = v;
+  }
+  __syncthreads();
+  run<C, N, L, T, true>(buf, tw);
+  store_cols<C, N>(buf, spec, base, zstride, nc);
+}
+
+// shared-memory opt-in for the instances above the default 48 KB
+template <typename K>
+inline bool smem_attr(Ctx* c, K kern, size_t bytes) {
+  if (bytes <= 48 * 1024) return true;
+  return cuda_ok(c, cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes),
+                 "fft smem");
+}
+
+template <typename C, typename S, int N>
+void launch_x_fwd(Ctx* c, const FftArgs<C>& F, const S* src, C* spec) {
+  typedef Shape<C, N> Sh;
+  auto k = x_fwd<C, S, N>;
+  if (!smem_attr(c, k, Sh::smem)) return;
+  dim3 grid(div_up(c->g.n2m / 2, Sh::L), c->g.n3m);
+  k<<<grid, Sh::T, Sh::smem, c->stream>>>(F, src, spec);
+}
+
+template <typename C, int N>
+void launch_x_inv(Ctx* c, const FftArgs<C>& F, const C* spec, typename Real<C>::T* dst) {
+  typedef Shape<C, N> Sh;
+  auto k = x_inv<C, N>;
+  if (!smem_attr(c, k, Sh::smem)) return;
+  dim3 grid(div_up(c->g.n2m / 2, Sh::L), c->g.n3m);
+  k<<<grid, Sh::T, Sh::smem, c->stream>>>(F, spec, dst);
+}
+
+template <typename C, int N>
+void launch_y(Ctx* c, const FftArgs<C>& F, C* spec, int sign) {
+  typedef Shape<C, N> Sh;
+  auto kf = y_pass<C, N, false>;
+  auto ki = y_pass<C, N, true>;
+  if (!smem_attr(c, kf, Sh::smem) || !smem_attr(c, ki, Sh::smem)) return;
+  dim3 grid(div_up(c->g.H, Sh::L), c->g.n3m);
+  if (sign < 0) kf<<<grid, Sh::T, Sh::smem, c->stream>>>(F, spec);
+  else ki<<<grid, Sh::T, Sh::smem, c->stream>>>(F, spec);
+}
+
+template <typename C, int N>
+void launch_z(Ctx* c, const FftArgs<C>& F, C* spec) {
+  typedef Shape<C, N> Sh;
+  auto k = z_solve<C, N>;
+  if (!smem_attr(c, k, Sh::smem)) return;
+  dim3 grid(div_up(c->g.H, Sh::L), c->g.n2m);
+  k<<<grid, Sh::T, Sh::smem, c->stream>>>(F, spec);
+}
+
+}  // namespace fastfft
+
+// line lengths with an instance
+#define MIBM_FFT_SIZES(X) X(16) X(24) X(32) X(48) X(64) X(96) X(128) X(192) X(256) X(384) X(512)
+
+}  // namespace mibm

@@ -531,7 +531,11 @@ __global__ void seg_final_kernel(const double* __restrict__ part, double ncell, 
     __syncthreads();
   }
   if (threadIdx.x == 0)
-    for (int q = 0; q < 3; ++q) mean3[q] = sm[q][0] / ncell;
+    for (int q = 0; q < 3; ++q) {
+      double m = sm[q][0] / ncell;
+      mean3[q] = m;
+      reinterpret_cast<float*>(mean3 + 4)[q] = (float)m;   // FP32 copy for the precision form
+    }
 }
 
 // ---------------------------------------------------------------------
@@ -1110,8 +1114,9 @@ static bool ensure_lag_buffers(Ctx* c) {
   if (!s->face_part) {
     if (!cuda_ok(c, cudaMalloc(&s->face_part, sizeof(double) * 11 * std::max(1, c->maxnf)), "lag")) return false;
     if (!cuda_ok(c, cudaMalloc(&s->geom_out, sizeof(double) * 8), "lag")) return false;
-    if (!cuda_ok(c, cudaMalloc(&s->mean3, sizeof(double) * 4), "lag")) return false;
-    cudaMemsetAsync(s->mean3, 0, sizeof(double) * 4, c->stream);
+    // [0..3) FP64 mean force, [4..6) the same rounded to FP32 (3 floats)
+    if (!cuda_ok(c, cudaMalloc(&s->mean3, sizeof(double) * 8), "lag")) return false;
+    cudaMemsetAsync(s->mean3, 0, sizeof(double) * 8, c->stream);
   }
   if (!c->tri_coef)
     if (!cuda_ok(c, cudaMalloc(&c->tri_coef, sizeof(double) * 4 * std::max(1, c->maxnf)), "lag")) return false;

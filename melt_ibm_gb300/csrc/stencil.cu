@@ -11,6 +11,8 @@
 // the FP64 FMA rate of the part, not by HBM, so the code avoids divisions
 // (reciprocals are taken once on the host) and skips terms that are zero by
 // configuration (HIT forcing off).
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace mibm {
@@ -306,19 +308,19 @@ __global__ void updvp_kernel(StencilArgs A, const StepParams* __restrict__ pp, c
 }
 
 // precision form: u -= al dt grad(phi) with phi from the FP32 Poisson solve;
-// the increment is formed in FP32 and added to the FP64 velocity, optional
-// mean-force removal, optional FP32 mirror m32 (u, v, w at 0, cells, 2 cells)
+// the increment is formed in FP32 (with the FP32 mean force mean3f folded
+// in when given) and added to the FP64 velocity; optional FP32 mirror m32
+// (u, v, w at 0, cells, 2 cells)
 __global__ void updvp_f32_kernel(StencilArgs A, const StepParams* __restrict__ pp, const float* __restrict__ phi,
                                  double* __restrict__ vx, double* __restrict__ vy, double* __restrict__ vz,
-                                 const double* __restrict__ mean3, float* __restrict__ m32) {
+                                 const float* __restrict__ mean3f, float* __restrict__ m32) {
   CELL_INDEX
   float loc = phi[c0];
   float ix = (loc - phi[c0 + dim]) * pp->cf[kUP1];
   float iy = (loc - phi[c0 + djm]) * pp->cf[kUP2];
   float iz = (loc - phi[c0 + dkm]) * pp->cf[kUP3];
-  double x = vx[c0], y = vy[c0], z = vz[c0];
-  if (mean3) { x = x - mean3[0]; y = y - mean3[1]; z = z - mean3[2]; }
-  x = x - (double)ix; y = y - (double)iy; z = z - (double)iz;
+  if (mean3f) { ix += mean3f[0]; iy += mean3f[1]; iz += mean3f[2]; }
+  double x = vx[c0] - (double)ix, y = vy[c0] - (double)iy, z = vz[c0] - (double)iz;
   vx[c0] = x; vy[c0] = y; vz[c0] = z;
   if (m32) { m32[c0] = (float)x; m32[c0 + g.cells] = (float)y; m32[c0 + 2 * g.cells] = (float)z; }
 }
@@ -419,49 +421,68 @@ __device__ __forceinline__ double warp_max(double v) {
 
 // cfl.f90:11-26: i+1, j+1, k+1 are not wrapped -- column n1 / row n2 are the
 // stored padding values, plane n3m+1 is the periodic ghost.
+// R = float: the precision form on the FP32 mirrors (dt only sets the step
+// size; the FP32 maximum is rounded up to double unchanged)
+template <typename R>
 __global__ void cfl_kernel(StencilArgs A, const double* __restrict__ padx, const double* __restrict__ pady,
                            double* __restrict__ part) {
   const Grid& g = A.g;
-  int j = blockIdx.y, k = blockIdx.z;
-  double m = 0.0;
-  for (int i = threadIdx.x; i < g.n1m; i += blockDim.x) {
+  const Prog<R> F = prog<R>(A);
+  const R h1 = R(0.5 * g.dx1), h2 = R(0.5 * g.dx2), h3 = R(0.5 * g.dx3);
+  R mr = R(0);
+  const int rows = g.n2m * g.n3m;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < rows * g.n1m; t += gridDim.x * blockDim.x) {
+    int i = t % g.n1m, row = t / g.n1m;
+    int j = row % g.n2m, k = row / g.n2m;
     size_t c0 = cidx(g, i, j, k);
-    double vxp = (i + 1 < g.n1m) ? A.vx[c0 + 1] : padx[j + (size_t)g.n2m * k];
-    double vyp = (j + 1 < g.n2m) ? A.vy[c0 + g.P] : pady[i + (size_t)g.n1m * k];
-    double vzp = A.vz[cidx(g, i, j, (k + 1 == g.n3m) ? 0 : k + 1)];
-    double qcf = fabs((A.vx[c0] + vxp) * 0.5 * g.dx1) + fabs((A.vy[c0] + vyp) * 0.5 * g.dx2) +
-                 fabs((A.vz[c0] + vzp) * 0.5 * g.dx3);
-    m = fmax(m, qcf);
+    R vxp = (i + 1 < g.n1m) ? F.u[c0 + 1] : R(padx[j + (size_t)g.n2m * k]);
+    R vyp = (j + 1 < g.n2m) ? F.v[c0 + g.P] : R(pady[i + (size_t)g.n1m * k]);
+    R vzp = F.w[cidx(g, i, j, (k + 1 == g.n3m) ? 0 : k + 1)];
+    R qcf;
+    if (sizeof(R) == 8)   // FP64 form: the reference's operation order (x*0.5*dx)
+      qcf = fabs((F.u[c0] + vxp) * R(0.5) * R(g.dx1)) + fabs((F.v[c0] + vyp) * R(0.5) * R(g.dx2)) +
+            fabs((F.w[c0] + vzp) * R(0.5) * R(g.dx3));
+    else
+      qcf = fabs((F.u[c0] + vxp) * h1) + fabs((F.v[c0] + vyp) * h2) + fabs((F.w[c0] + vzp) * h3);
+    mr = fmax(mr, qcf);
   }
-  m = warp_max(m);
+  double m = warp_max((double)mr);
   __shared__ double sm[32];
   if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
   __syncthreads();
   if (threadIdx.x < 32) {
     double v = (threadIdx.x < (blockDim.x >> 5)) ? sm[threadIdx.x] : 0.0;
     v = warp_max(v);
-    if (threadIdx.x == 0) part[j + (size_t)g.n2m * k] = v;
+    if (threadIdx.x == 0) part[blockIdx.x] = v;
   }
 }
 
 // get_dt advective term: max(|u| dt dx1 + |v| dt dx2 + |w| dt dx3)
+template <typename R>
 __global__ void getdt_kernel(StencilArgs A, double dt, double* __restrict__ part) {
   const Grid& g = A.g;
-  int j = blockIdx.y, k = blockIdx.z;
-  double m = 0.0;
-  for (int i = threadIdx.x; i < g.n1m; i += blockDim.x) {
-    size_t c0 = cidx(g, i, j, k);
-    double v = fabs(A.vx[c0]) * dt * g.dx1 + fabs(A.vy[c0]) * dt * g.dx2 + fabs(A.vz[c0]) * dt * g.dx3;
-    m = fmax(m, v);
+  const Prog<R> F = prog<R>(A);
+  const R d1 = R(dt * g.dx1), d2 = R(dt * g.dx2), d3 = R(dt * g.dx3);
+  R mr = R(0);
+  const int rows = g.n2m * g.n3m;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < rows * g.n1m; t += gridDim.x * blockDim.x) {
+    int i = t % g.n1m, row = t / g.n1m;
+    size_t c0 = cidx(g, i, row % g.n2m, row / g.n2m);
+    R v;
+    if (sizeof(R) == 8)   // FP64 form: the reference's operation order
+      v = fabs(F.u[c0]) * R(dt) * R(g.dx1) + fabs(F.v[c0]) * R(dt) * R(g.dx2) + fabs(F.w[c0]) * R(dt) * R(g.dx3);
+    else
+      v = fabs(F.u[c0]) * d1 + fabs(F.v[c0]) * d2 + fabs(F.w[c0]) * d3;
+    mr = fmax(mr, v);
   }
-  m = warp_max(m);
+  double m = warp_max((double)mr);
   __shared__ double sm[32];
   if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
   __syncthreads();
   if (threadIdx.x < 32) {
     double v = (threadIdx.x < (blockDim.x >> 5)) ? sm[threadIdx.x] : 0.0;
     v = warp_max(v);
-    if (threadIdx.x == 0) part[j + (size_t)g.n2m * k] = v;
+    if (threadIdx.x == 0) part[blockIdx.x] = v;
   }
 }
 
@@ -552,8 +573,9 @@ void k_updvp(Ctx* c, const StepParams* dp, const double* mean3) {
 
 void k_updvp_f32(Ctx* c, const StepParams* dp, const float* phi, const double* mean3, bool mirror) {
   { MIBM_PROF(c, "updvp_f32");
+    const float* mean3f = mean3 ? reinterpret_cast<const float*>(mean3 + 4) : nullptr;
     updvp_f32_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, phi, c->df[MIBM_F_VX],
-                                                                     c->df[MIBM_F_VY], c->df[MIBM_F_VZ], mean3,
+                                                                     c->df[MIBM_F_VY], c->df[MIBM_F_VZ], mean3f,
                                                                      mirror ? c->q32 : nullptr); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "updvp_f32");
@@ -637,10 +659,23 @@ void k_tempforce_apply(Ctx* c) {
   MIBM_LAUNCH_CHECK(c, "tempforce");
 }
 
+// blocks of the two max reductions: a few waves over the SMs, never more
+// than the rows (the partials area of the reduction buffer holds one per row)
+static unsigned reduce_blocks(const Grid& g) {
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  size_t want = (size_t)std::max(1, sms) * 8;
+  return (unsigned)std::min(want, (size_t)g.n2m * g.n3m);
+}
+
 double k_cfl(Ctx* c) {
-  dim3 grid(1, c->g.n2m, c->g.n3m);
-  { MIBM_PROF(c, "cfl"); cfl_kernel<<<grid, 128, 0, c->stream>>>(make_args(c), c->pad_vx, c->pad_vy, c->red + kRedPart); }
-  max_reduce_kernel<<<1, 1024, 0, c->stream>>>(c->red + kRedPart, (size_t)c->g.n2m * c->g.n3m, c->red + kRedOut);
+  unsigned nb = reduce_blocks(c->g);
+  bool f32 = c->precision == 1 && c->q32_valid;
+  { MIBM_PROF(c, "cfl");
+    if (f32) cfl_kernel<float><<<nb, 256, 0, c->stream>>>(make_args(c), c->pad_vx, c->pad_vy, c->red + kRedPart);
+    else cfl_kernel<double><<<nb, 256, 0, c->stream>>>(make_args(c), c->pad_vx, c->pad_vy, c->red + kRedPart); }
+  max_reduce_kernel<<<1, 1024, 0, c->stream>>>(c->red + kRedPart, nb, c->red + kRedOut);
   c->launches += 2;
   cudaMemcpyAsync(c->red_host, c->red + kRedOut, 8, cudaMemcpyDeviceToHost, c->stream);
   if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "cfl")) return 0.0;
@@ -649,9 +684,12 @@ double k_cfl(Ctx* c) {
 }
 
 double k_get_dt_buffer(Ctx* c, double dt, double ren) {
-  dim3 grid(1, c->g.n2m, c->g.n3m);
-  { MIBM_PROF(c, "getdt"); getdt_kernel<<<grid, 128, 0, c->stream>>>(make_args(c), dt, c->red + kRedPart); }
-  max_reduce_kernel<<<1, 1024, 0, c->stream>>>(c->red + kRedPart, (size_t)c->g.n2m * c->g.n3m, c->red + kRedOut);
+  unsigned nb = reduce_blocks(c->g);
+  bool f32 = c->precision == 1 && c->q32_valid;
+  { MIBM_PROF(c, "getdt");
+    if (f32) getdt_kernel<float><<<nb, 256, 0, c->stream>>>(make_args(c), dt, c->red + kRedPart);
+    else getdt_kernel<double><<<nb, 256, 0, c->stream>>>(make_args(c), dt, c->red + kRedPart); }
+  max_reduce_kernel<<<1, 1024, 0, c->stream>>>(c->red + kRedPart, nb, c->red + kRedOut);
   c->launches += 2;
   cudaMemcpyAsync(c->red_host, c->red + kRedOut, 8, cudaMemcpyDeviceToHost, c->stream);
   if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "get_dt")) return 0.0;

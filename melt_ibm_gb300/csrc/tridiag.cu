@@ -326,12 +326,15 @@ int tri_chunk_line(int n) {
   return 0;
 }
 
-constexpr int kColMaxChunks = 16;   // y/z blocks of at most 32 x 16 threads (register budget)
+// y/z blocks: up to 32 chunks (warps) of M <= 8 cells, or 16 chunks of the
+// longer M (register budget of a 1024- or 512-thread block)
+constexpr int kColMaxChunks = 32;
+__host__ __device__ constexpr int col_max_chunks(int m) { return m >= 12 ? 16 : 32; }
 
 int tri_chunk_col(int n) {
   static const int pref[] = {16, 12, 8, 6, 4, 3, 2};
   for (int m : pref)
-    if (n % m == 0 && n / m <= kColMaxChunks) return m;
+    if (n % m == 0 && n / m <= col_max_chunks(m)) return m;
   return 0;
 }
 
@@ -516,7 +519,7 @@ __global__ void __launch_bounds__(256) solve_xc_kernel(Grid g, V* __restrict__ r
 // to q (solxk.f90:44-50), optionally also left in rhs, and in the precision
 // form copied to the FP32 mirror m32.
 template <typename V, int M, bool ZL>
-__global__ void __launch_bounds__(32 * kColMaxChunks) solve_cc_kernel(Grid g, V* __restrict__ rhs, const V* __restrict__ X,
+__global__ void __launch_bounds__(32 * col_max_chunks(M)) solve_cc_kernel(Grid g, V* __restrict__ rhs, const V* __restrict__ X,
                                                         double* __restrict__ q, int write_rhs, float* __restrict__ m32) {
   __shared__ V sC[kColMaxChunks][32];
   __shared__ V sU[kColMaxChunks][32];
@@ -525,12 +528,22 @@ __global__ void __launch_bounds__(32 * kColMaxChunks) solve_cc_kernel(Grid g, V*
   const int lane = threadIdx.x, w = threadIdx.y;
   const int x = blockIdx.x * 32 + lane;
   const bool act = x < g.n1m;
-  const size_t stride = ZL ? g.plane : (size_t)g.P;
-  const size_t base = ZL ? cidx(g, act ? x : 0, blockIdx.y, 0) : cidx(g, act ? x : 0, 0, blockIdx.y);
+  // element stride of the line (< 2^31 for every supported grid) and the
+  // first cell of this thread's chunk
+  const int stride = ZL ? (int)g.plane : g.P;
   const int e0 = w * M;
+  const size_t first = (ZL ? cidx(g, act ? x : 0, blockIdx.y, 0) : cidx(g, act ? x : 0, 0, blockIdx.y)) +
+                       (size_t)e0 * stride;
+  V* __restrict__ rp = rhs + first;
   V r[M];
+  double qv[ZL ? M : 1];
 #pragma unroll
-  for (int i = 0; i < M; ++i) r[i] = act ? rhs[base + (size_t)(e0 + i) * stride] : V(0);
+  for (int i = 0; i < M; ++i) r[i] = act ? rp[i * stride] : V(0);
+  if (ZL) {   // the field the increment is added to, fetched with the line (more loads in flight)
+    const double* __restrict__ qp = q + first;
+#pragma unroll
+    for (int i = 0; i < M; ++i) qv[ZL ? i : 0] = act ? qp[i * stride] : 0.0;
+  }
   const V rlast = r[M - 1];
   V C = V(0);
 #pragma unroll
@@ -567,14 +580,14 @@ __global__ void __launch_bounds__(32 * kColMaxChunks) solve_cc_kernel(Grid g, V*
 #pragma unroll
   for (int i = 0; i < M; ++i) {
     V xv = xn * X[3 * n + i * G + w] + r[i];
-    size_t c0 = base + (size_t)(e0 + i) * stride;
+    int o = i * stride;
     if (ZL) {
-      if (write_rhs) rhs[c0] = xv;
-      double qn = q[c0] + (double)xv;
-      q[c0] = qn;
-      if (m32) m32[c0] = (float)qn;
+      if (write_rhs) rp[o] = xv;
+      double qn = qv[ZL ? i : 0] + (double)xv;
+      q[first + o] = qn;
+      if (m32) m32[first + o] = (float)qn;
     } else {
-      rhs[c0] = xv;
+      rp[o] = xv;
     }
   }
 }
