@@ -892,26 +892,127 @@ __device__ __forceinline__ void tri_verts(const TagArgs& T, int f, double V0[3],
   for (int d = 0; d < 3; ++d) { V0[d] = T.x[3 * a + d]; V1[d] = T.x[3 * b + d]; V2[d] = T.x[3 * c + d]; }
 }
 
-__global__ void sdf_reset_kernel(Grid g, unsigned long long* __restrict__ sdf_bits, int* __restrict__ winner) {
+__global__ void sdf_reset_kernel(Grid g, unsigned long long* __restrict__ sdf_bits, int* __restrict__ winner,
+                                 unsigned* __restrict__ band_ub) {
   size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= g.cells) return;
   sdf_bits[t] = (unsigned long long)__double_as_longlong(999.0);   // genSDF.f90:138
   winner[t] = INT_MAX;
+  if (band_ub) band_ub[t] = 0x7f800000u;                           // +inf
 }
 
-// one thread per (triangle, band cell); pass 0: distance (stored) and the
-// minimum per cell, pass 1: the earliest triangle at that distance, pass 2:
-// the winner writes the signed distance and the VOF
-__global__ void band_kernel(TagArgs T, int pass, unsigned long long* __restrict__ sdf_bits, int* __restrict__ winner,
-                            double* __restrict__ vofp, double* __restrict__ dist_buf) {
+// Culling of the narrow-band distance pass.  With c the face centroid and
+// R >= the largest centroid-vertex distance, every point of the face lies
+// within R of c, so for a cell centre P
+//   |P - c| - R  <=  dist(P, face)  <=  |P - c|.
+// Pass U takes the minimum of the upper bounds over the candidate faces of a
+// cell; the exact pass skips a face whose lower bound exceeds that minimum:
+// such a face is strictly farther than the nearest one, so the minimum, the
+// set of faces tied at it and hence the earliest-face winner are unchanged.
+// The bounds are evaluated in FP32 from FP32 copies of the coordinates
+// (|x| < 13, rounding error < 1e-6 per coordinate, < 3e-6 on |P - c|), and
+// kBandMargin covers that error on both sides.
+constexpr float kBandMargin = 8e-6f;
+
+__global__ void cm32_kernel(LagArgs A, float* __restrict__ cm32) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= A.clen) return;
+  cm32[t] = (float)A.xm[t];
+  cm32[A.clen + t] = (float)A.ym[t];
+  cm32[2 * A.clen + t] = (float)A.zm[t];
+}
+
+__global__ void band_prep_kernel(TagArgs T, float4* __restrict__ face4, int4* __restrict__ face_cell) {
+  int f = blockIdx.x * blockDim.x + threadIdx.x;
+  const LagArgs& A = T.L;
+  if (f >= A.nf) return;
+  const Grid& g = A.g;
+  double pos[3] = {T.bar[3 * f], T.bar[3 * f + 1], T.bar[3 * f + 2]};
+  double V[3][3];
+  tri_verts(T, f, V[0], V[1], V[2]);
+  double r2 = 0.0;
+  for (int v = 0; v < 3; ++v) {
+    double dx = V[v][0] - pos[0], dy = V[v][1] - pos[1], dz = V[v][2] - pos[2];
+    r2 = fmax(r2, dx * dx + dy * dy + dz * dz);
+  }
+  float R = (float)sqrt(r2);
+  R = R * 1.000001f + 1e-30f;                                        // round the radius up
+  face4[f] = make_float4((float)pos[0], (float)pos[1], (float)pos[2], R);
+  // base cell of the band, as band_kernel derives it (genSDF.f90:151-153)
+  face_cell[f] = make_int4(ffloor(pos[0] * g.dx1) + 1, ffloor(pos[1] * g.dx2) + 1, ffloor(pos[2] * g.dx3) + 1, 0);
+}
+
+__device__ __forceinline__ float band_center_dist(const float* __restrict__ cm32, int clen, int coff, int ii, int jj,
+                                                  int kk, float4 c) {
+  float px = cm32[min(max(ii + coff, 0), clen - 1)];
+  float py = cm32[clen + min(max(jj + coff, 0), clen - 1)];
+  float pz = cm32[2 * clen + min(max(kk + coff, 0), clen - 1)];
+  float dx = px - c.x, dy = py - c.y, dz = pz - c.z;
+  return sqrtf(dx * dx + dy * dy + dz * dz);
+}
+
+// after pass U: pairs whose lower bound does not exceed the cell's bound go
+// to a compact list (warp-aggregated append), the others get the "far"
+// distance 1e300 so that they never match the cell minimum
+__global__ void band_select_kernel(TagArgs T, const float4* __restrict__ face4, const int4* __restrict__ face_cell,
+                                   const float* __restrict__ cm32, const unsigned* __restrict__ band_ub,
+                                   double* __restrict__ dist_buf, int* __restrict__ list, int* __restrict__ count) {
+  long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  int f = (int)(gid / 125), q = (int)(gid % 125);
+  const LagArgs& A = T.L;
+  bool keep = false;
+  if (f < A.nf && !T.ghost[f]) {
+    const Grid& g = A.g;
+    int4 b = face_cell[f];
+    int ii = b.x - 2 + q % 5, jj = b.y - 2 + (q / 5) % 5, kk = b.z - 2 + q / 25;
+    int im = fmod_pos(ii - 1, g.n1m), jm = fmod_pos(jj - 1, g.n1m), km = fmod_pos(kk - 1, g.n3m);
+    float4 fc = face4[f];
+    float lb = band_center_dist(cm32, A.clen, A.coff, ii, jj, kk, fc) - fc.w - kBandMargin;
+    keep = !(lb > __uint_as_float(band_ub[cidx(g, im, jm, km)]));
+    if (!keep) dist_buf[gid] = 1e300;
+  }
+  unsigned m = __ballot_sync(0xffffffffu, keep);
+  if (!m) return;
+  int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(count, __popc(m));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (keep) list[base + __popc(m & ((1u << lane) - 1u))] = (int)gid;
+}
+
+// pass U: per (face, band cell) the upper bound |P - c| + margin, min per cell
+__global__ void band_ub_kernel(TagArgs T, const float4* __restrict__ face4, const int4* __restrict__ face_cell,
+                               const float* __restrict__ cm32, unsigned* __restrict__ band_ub) {
   long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   int f = (int)(gid / 125), q = (int)(gid % 125);
   const LagArgs& A = T.L;
   if (f >= A.nf || T.ghost[f]) return;
   const Grid& g = A.g;
-  double pos[3] = {T.bar[3 * f], T.bar[3 * f + 1], T.bar[3 * f + 2]};
-  int i = ffloor(pos[0] * g.dx1) + 1, j = ffloor(pos[1] * g.dx2) + 1, k = ffloor(pos[2] * g.dx3) + 1;
-  int ii = i - 2 + q % 5, jj = j - 2 + (q / 5) % 5, kk = k - 2 + q / 25;
+  int4 b = face_cell[f];
+  int ii = b.x - 2 + q % 5, jj = b.y - 2 + (q / 5) % 5, kk = b.z - 2 + q / 25;
+  int im = fmod_pos(ii - 1, g.n1m), jm = fmod_pos(jj - 1, g.n1m), km = fmod_pos(kk - 1, g.n3m);
+  float ub = band_center_dist(cm32, A.clen, A.coff, ii, jj, kk, face4[f]) + kBandMargin;
+  atomicMin(&band_ub[cidx(g, im, jm, km)], __float_as_uint(ub));
+}
+
+// one thread per (triangle, band cell); pass 0: distance (stored) and the
+// minimum per cell, pass 1: the earliest triangle at that distance, pass 2:
+// the winner writes the signed distance and the VOF
+// pass 0 runs over the compact list of band_select_kernel (entry t < *count)
+__global__ void band_kernel(TagArgs T, int pass, unsigned long long* __restrict__ sdf_bits, int* __restrict__ winner,
+                            double* __restrict__ vofp, double* __restrict__ dist_buf, const int4* __restrict__ face_cell,
+                            const int* __restrict__ list, const int* __restrict__ count) {
+  long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (pass == 0) {
+    if (gid >= *count) return;
+    gid = list[gid];
+  }
+  int f = (int)(gid / 125), q = (int)(gid % 125);
+  const LagArgs& A = T.L;
+  if (f >= A.nf || T.ghost[f]) return;
+  const Grid& g = A.g;
+  int4 b = face_cell[f];
+  int ii = b.x - 2 + q % 5, jj = b.y - 2 + (q / 5) % 5, kk = b.z - 2 + q / 25;
   int im = fmod_pos(ii - 1, g.n1m), jm = fmod_pos(jj - 1, g.n1m), km = fmod_pos(kk - 1, g.n3m);
   size_t c0 = cidx(g, im, jm, km);
   double dist;
@@ -931,6 +1032,7 @@ __global__ void band_kernel(TagArgs T, int pass, unsigned long long* __restrict_
     return;
   }
   if (winner[c0] != f || sdf_bits[c0] != bits) return;
+  double pos[3] = {T.bar[3 * f], T.bar[3 * f + 1], T.bar[3 * f + 2]};
   double P[3] = {coord(A, 0, 1, ii), coord(A, 1, 1, jj), coord(A, 2, 1, kk)};
   double Q0 = pos[0] - P[0], Q1 = pos[1] - P[1], Q2 = pos[2] - P[2];
   double dotval = T.nor[3 * f] * Q0 + T.nor[3 * f + 1] * Q1 + T.nor[3 * f + 2] * Q2;
@@ -1051,6 +1153,15 @@ struct LagState {
   unsigned long long* sdf_bits = nullptr;
   int* winner = nullptr;
   double* dist_buf = nullptr;
+  // narrow-band culling: per cell an FP32 upper bound of the nearest face
+  // distance (float bits), per face its FP32 centroid and circumradius and
+  // the base cell of its 5^3 band, FP32 cell-centre coordinates
+  unsigned* band_ub = nullptr;
+  int* band_list = nullptr;      // (face, cell) pairs that survive the bound, and their count
+  int* band_count = nullptr;
+  float4* face4 = nullptr;
+  int4* face_cell = nullptr;
+  float* cm32 = nullptr;
   // merged scatter plan
   int plan_n = 0, plan_cap = 0, nblk = 0;
   int *key = nullptr, *src = nullptr, *tmp_key = nullptr, *tmp_src = nullptr, *hist = nullptr;
@@ -1386,23 +1497,39 @@ void lagr_tag_narrow_band(Ctx* c) {
     if (!cuda_ok(c, cudaMalloc(&s->sdf_bits, sizeof(unsigned long long) * c->g.cells), "band")) return;
     if (!cuda_ok(c, cudaMalloc(&s->winner, sizeof(int) * c->g.cells), "band")) return;
   }
-  if (!s->dist_buf)
-    if (!cuda_ok(c, cudaMalloc(&s->dist_buf, sizeof(double) * 125 * (size_t)c->maxnf), "band")) return;
   TagArgs T;
   T.L = lag_args(c);
+  if (!s->dist_buf) {
+    bool ok = cuda_ok(c, cudaMalloc(&s->dist_buf, sizeof(double) * 125 * (size_t)c->maxnf), "band") &&
+              cuda_ok(c, cudaMalloc(&s->band_ub, sizeof(unsigned) * c->g.cells), "band") &&
+              cuda_ok(c, cudaMalloc(&s->band_list, sizeof(int) * 125 * (size_t)c->maxnf), "band") &&
+              cuda_ok(c, cudaMalloc(&s->band_count, sizeof(int)), "band") &&
+              cuda_ok(c, cudaMalloc(&s->face4, sizeof(float4) * (size_t)c->maxnf), "band") &&
+              cuda_ok(c, cudaMalloc(&s->face_cell, sizeof(int4) * (size_t)c->maxnf), "band") &&
+              cuda_ok(c, cudaMalloc(&s->cm32, sizeof(float) * 3 * (size_t)T.L.clen), "band");
+    if (!ok) return;
+    cm32_kernel<<<div_up(T.L.clen, 256), 256, 0, c->stream>>>(T.L, s->cm32);
+    ++c->launches;
+  }
   T.x = M<double>(c, MIBM_M_XYZV); T.vof = M<int>(c, MIBM_M_VERT_OF_FACE); T.ghost = M<int>(c, MIBM_M_GHOST_FACE);
   T.bar = M<double>(c, MIBM_M_TRI_BAR); T.nor = M<double>(c, MIBM_M_TRI_NOR);
   { MIBM_PROF(c, "sdf_reset");
-    sdf_reset_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, s->sdf_bits, s->winner); }
+    sdf_reset_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, s->sdf_bits, s->winner, s->band_ub); }
   size_t nthr = (size_t)c->maxnf * 125;
+  { MIBM_PROF(c, "band_bound");
+    band_prep_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(T, s->face4, s->face_cell);
+    band_ub_kernel<<<div_up(nthr, 128), 128, 0, c->stream>>>(T, s->face4, s->face_cell, s->cm32, s->band_ub);
+    cudaMemsetAsync(s->band_count, 0, sizeof(int), c->stream);
+    band_select_kernel<<<div_up(nthr, 128), 128, 0, c->stream>>>(T, s->face4, s->face_cell, s->cm32, s->band_ub,
+                                                                  s->dist_buf, s->band_list, s->band_count); }
   for (int pass = 0; pass < 3; ++pass) {
     MIBM_PROF(c, "band");
     band_kernel<<<div_up(nthr, 128), 128, 0, c->stream>>>(T, pass, s->sdf_bits, s->winner, c->df[MIBM_F_VOFP],
-                                                           s->dist_buf);
+                                                           s->dist_buf, s->face_cell, s->band_list, s->band_count);
   }
   { MIBM_PROF(c, "sdf_finish");
     sdf_finish_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, s->sdf_bits, c->df[MIBM_F_SDF]); }
-  c->launches += 5;
+  c->launches += 8;
   k_interp_vof(c);
   MIBM_LAUNCH_CHECK(c, "narrowBandTagging");
 }
@@ -1442,7 +1569,7 @@ void lagr_tag_initial(Ctx* c) {
   }
   double* tmp = nullptr;
   if (!cuda_ok(c, cudaMalloc(&tmp, sizeof(double) * std::max<size_t>(1, ncell)), "initial tag")) return;
-  sdf_reset_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, s->sdf_bits, s->winner);
+  sdf_reset_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, s->sdf_bits, s->winner, nullptr);
   initial_tag_kernel<<<div_up(ncell, 128), 128, 0, c->stream>>>(T, b0[0], b0[1], b0[2], nb[0], nb[1], nb[2], tmp);
   for (int pass = 0; pass < 2; ++pass)
     initial_claim_kernel<<<div_up(ncell, 256), 256, 0, c->stream>>>(c->g, b0[0], b0[1], b0[2], nb[0], nb[1], nb[2], tmp,
@@ -1528,6 +1655,8 @@ void lagr_free(Ctx* c) {
       LagState* s = g_lag[q];
       cudaFree(s->adj_off); cudaFree(s->adj_face); cudaFree(s->face_part); cudaFree(s->geom_out);
       cudaFree(s->mean3); cudaFree(s->sdf_bits); cudaFree(s->winner); cudaFree(s->dist_buf);
+      cudaFree(s->band_ub); cudaFree(s->face4); cudaFree(s->face_cell); cudaFree(s->cm32);
+      cudaFree(s->band_list); cudaFree(s->band_count);
       cudaFree(s->key); cudaFree(s->src); cudaFree(s->tmp_key); cudaFree(s->tmp_src); cudaFree(s->hist);
       cudaFree(s->tsum);
       cudaFree(s->saved); cudaFree(s->dirty); cudaFree(s->segval);
