@@ -9,9 +9,9 @@
 // butterfly and writes the outputs in place; stage radices, strides and
 // twiddle steps are compile-time constants, so no index division is left
 // at run time.  Twiddles e^{-2 pi i m/N} are the FP64-tabulated table of
-// fft.cu, staged in shared memory.  L is chosen so that a block moves 128
-// contiguous bytes per spectrum row and a thread holds 16 (FP32) or 8
-// (FP64) complex values per stage.
+// fft.cu, staged in shared memory.  L (a power of two) is chosen so that a
+// block moves at least 128 contiguous bytes per spectrum row and a thread
+// holds at most 16 (FP32) or 8 (FP64) complex values per stage.
 #pragma once
 
 #include "fft_common.cuh"
@@ -39,8 +39,11 @@ __host__ __device__ constexpr int radix_at(int n, int st) {
 template <typename C, int N>
 struct Shape {
   static constexpr int kWork = sizeof(C) == 8 ? 4096 : 2048;   // values per block
-  static constexpr int L = (kWork / N) < 1 ? 1 : ((kWork / N) > 32 ? 32 : kWork / N);
+  // lines per block: the largest power of two <= min(32, kWork / N)
+  static constexpr int pow2_floor(int v) { int p = 1; while (2 * p <= v) p *= 2; return p; }
+  static constexpr int L = pow2_floor((kWork / N) < 1 ? 1 : ((kWork / N) > 32 ? 32 : kWork / N));
   static constexpr int T = 256;
+  static constexpr int kMinBlocks = sizeof(C) == 8 ? 3 : 2;   // resident blocks per SM asked of ptxas
   static constexpr int ES = L + 1;
   static constexpr size_t smem = sizeof(C) * ((size_t)N + (size_t)N * ES);
 };
@@ -126,7 +129,7 @@ __device__ __forceinline__ void stage_twiddles(C* s, const C* __restrict__ tw) {
 
 // X forward: rows (j, j+1) of plane k packed as one complex line, r2c split
 template <typename C, typename S, int N>
-__global__ void __launch_bounds__(Shape<C, N>::T) x_fwd(FftArgs<C> F, const S* __restrict__ src, C* __restrict__ spec) {
+__global__ void __launch_bounds__(Shape<C, N>::T, Shape<C, N>::kMinBlocks) x_fwd(FftArgs<C> F, const S* __restrict__ src, C* __restrict__ spec) {
   typedef typename Real<C>::T R;
   constexpr int L = Shape<C, N>::L, T = Shape<C, N>::T, ES = Shape<C, N>::ES, PER = (N * L + T - 1) / T;
   extern __shared__ __align__(16) unsigned char shraw[];
@@ -175,7 +178,7 @@ __global__ void __launch_bounds__(Shape<C, N>::T) x_fwd(FftArgs<C> F, const S* _
 
 // X inverse (c2r): half spectra of rows (j, j+1) -> real rows
 template <typename C, int N>
-__global__ void __launch_bounds__(Shape<C, N>::T) x_inv(FftArgs<C> F, const C* __restrict__ spec,
+__global__ void __launch_bounds__(Shape<C, N>::T, Shape<C, N>::kMinBlocks) x_inv(FftArgs<C> F, const C* __restrict__ spec,
                                                        typename Real<C>::T* __restrict__ dst) {
   typedef typename Real<C>::T R;
   constexpr int L = Shape<C, N>::L, T = Shape<C, N>::T, ES = Shape<C, N>::ES, PER = (N * L + T - 1) / T;
@@ -257,7 +260,7 @@ __device__ __forceinline__ void store_cols(const C* buf, C* __restrict__ spec, s
 
 // Y pass (forward or inverse) on L kx columns of plane k
 template <typename C, int N, bool INV>
-__global__ void __launch_bounds__(Shape<C, N>::T) y_pass(FftArgs<C> F, C* __restrict__ spec) {
+__global__ void __launch_bounds__(Shape<C, N>::T, Shape<C, N>::kMinBlocks) y_pass(FftArgs<C> F, C* __restrict__ spec) {
   constexpr int L = Shape<C, N>::L, T = Shape<C, N>::T;
   extern __shared__ __align__(16) unsigned char shraw[];
   C* tw = (C*)shraw;
@@ -275,7 +278,7 @@ __global__ void __launch_bounds__(Shape<C, N>::T) y_pass(FftArgs<C> F, C* __rest
 
 // Z pass: forward, scale, eigenvalue division, zero mode, inverse
 template <typename C, int N>
-__global__ void __launch_bounds__(Shape<C, N>::T) z_solve(FftArgs<C> F, C* __restrict__ spec) {
+__global__ void __launch_bounds__(Shape<C, N>::T, Shape<C, N>::kMinBlocks) z_solve(FftArgs<C> F, C* __restrict__ spec) {
   typedef typename Real<C>::T R;
   constexpr int L = Shape<C, N>::L, T = Shape<C, N>::T, ES = Shape<C, N>::ES;
   extern __shared__ __align__(16) unsigned char shraw[];

@@ -702,6 +702,161 @@ __global__ void heat_flux_kernel(LagArgs A, const double* __restrict__ temp, con
   qout[t] = qv / pec;
 }
 
+// ---------------------------------------------------------------------
+// Precision form of mlsWeight and mls_heatFlux.  MLS with the complete
+// linear basis is invariant under an affine change of basis, so the shape
+// functions (and their gradients) can be built from the basis
+// p = (1, x - x0, y - y0, z - z0) shifted to the interpolation point x0,
+// where p(x0) = e0.  With separable Gaussian weights w_n = wx_i wy_j wz_k
+// every moment sum factorises into 1-D moments S_m = sum_q w_q d_q^m
+// (m = 0, 1, 2) and the derivative weights likewise (D_m), so the 4x4
+// moment matrix and its three derivatives take a few dozen FP64 operations
+// instead of 27 rank-one updates each, and are far better conditioned than
+// with absolute coordinates.  The 4x4 inversion is the FP64 LU of the plain
+// form.  The values agree with the reference construction to its round-off
+// (amplified by its conditioning), not bit for bit.
+// ---------------------------------------------------------------------
+__device__ __forceinline__ void moments3(const double w[3], const double d[3], double S[3]) {
+  S[0] = w[0] + w[1] + w[2];
+  S[1] = fma(w[0], d[0], fma(w[1], d[1], w[2] * d[2]));
+  S[2] = fma(w[0] * d[0], d[0], fma(w[1] * d[1], d[1], (w[2] * d[2]) * d[2]));
+}
+
+// symmetric moment matrix (column-major) of the shifted linear basis from
+// 1-D moments X, Y, Z (each S0, S1, S2)
+__device__ __forceinline__ void moment_matrix(const double X[3], const double Y[3], const double Z[3], double M[16]) {
+  double a00 = X[0] * Y[0] * Z[0];
+  double a01 = X[1] * Y[0] * Z[0], a02 = X[0] * Y[1] * Z[0], a03 = X[0] * Y[0] * Z[1];
+  double a11 = X[2] * Y[0] * Z[0], a22 = X[0] * Y[2] * Z[0], a33 = X[0] * Y[0] * Z[2];
+  double a12 = X[1] * Y[1] * Z[0], a13 = X[1] * Y[0] * Z[1], a23 = X[0] * Y[1] * Z[1];
+  M[0] = a00; M[1] = a01; M[2] = a02; M[3] = a03;
+  M[4] = a01; M[5] = a11; M[6] = a12; M[7] = a13;
+  M[8] = a02; M[9] = a12; M[10] = a22; M[11] = a23;
+  M[12] = a03; M[13] = a13; M[14] = a23; M[15] = a33;
+}
+
+__global__ void mls_weight_sep_kernel(LagArgs A, const double* __restrict__ tri_bar, const int* __restrict__ ghost,
+                                      const int* __restrict__ pind, double* __restrict__ p1, double* __restrict__ p2,
+                                      double* __restrict__ p3, double* __restrict__ pt, int* __restrict__ flag) {
+  int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  int t = gid >> 2, comp = gid & 3;
+  if (t >= A.nf || ghost[t]) return;
+  const Grid& g = A.g;
+  double pos[3] = {tri_bar[3 * t], tri_bar[3 * t + 1], tri_bar[3 * t + 2]};
+  CageSpec cs = cage_spec(comp);
+  int i0 = pind[6 * t + cs.ix], j0 = pind[6 * t + cs.iy];
+  int k0 = cs.znint ? fnint(pos[2] * g.dx3) + 1 : ffloor(pos[2] * g.dx3) + 1;
+  double wx[3], wy[3], wz[3], dx[3], dy[3], dz[3];
+  for (int q = 0; q < 3; ++q) {
+    double cz = coord(A, 2, cs.sz, k0 - 1 + q), cy = coord(A, 1, cs.sy, j0 - 1 + q), cx = coord(A, 0, cs.sx, i0 - 1 + q);
+    wz[q] = mls_gaussian(fabs(cz - pos[2]) / (A.wscl / g.dx3), A.wcon);
+    wy[q] = mls_gaussian(fabs(cy - pos[1]) / (A.wscl / g.dx2), A.wcon);
+    wx[q] = mls_gaussian(fabs(cx - pos[0]) / (A.wscl / g.dx1), A.wcon);
+    dx[q] = cx - pos[0]; dy[q] = cy - pos[1]; dz[q] = cz - pos[2];
+  }
+  double X[3], Y[3], Z[3], M[16];
+  moments3(wx, dx, X); moments3(wy, dy, Y); moments3(wz, dz, Z);
+  moment_matrix(X, Y, Z, M);
+  if (!inv4(M)) { atomicOr(flag, 1); return; }
+  const double c0 = M[0], c1 = M[1], c2 = M[2], c3 = M[3];   // A^{-1} e0
+  double* out = (comp == 0) ? p1 : (comp == 1) ? p2 : (comp == 2) ? p3 : pt;
+  out += 27 * (size_t)t;
+  for (int kk = 0; kk < 3; ++kk)
+    for (int jj = 0; jj < 3; ++jj) {
+      double wyz = wy[jj] * wz[kk], base = fma(c2, dy[jj], fma(c3, dz[kk], c0));
+      for (int ii = 0; ii < 3; ++ii) out[ii + 3 * jj + 9 * kk] = (wx[ii] * wyz) * fma(c1, dx[ii], base);
+    }
+}
+
+__global__ void heat_flux_sep_kernel(LagArgs A, const double* __restrict__ temp, const double* __restrict__ tri_bar,
+                                     const double* __restrict__ tri_nor, const int* __restrict__ ghost,
+                                     const int* __restrict__ pind, double h, double pec, double* __restrict__ qw_o,
+                                     double* __restrict__ qw_i, int* __restrict__ flag) {
+  int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  int t = gid >> 1, side = gid & 1;
+  if (t >= A.nf) return;
+  double* qout = side == 0 ? qw_o : qw_i;
+  if (ghost[t]) { qout[t] = 0.0; return; }
+  const Grid& g = A.g;
+  double n0 = tri_nor[3 * t], n1 = tri_nor[3 * t + 1], n2 = tri_nor[3 * t + 2];
+  double s = sqrt(n0 * n0 + n1 * n1 + n2 * n2);
+  double pos[3];
+  for (int d = 0; d < 3; ++d) {
+    double nd = tri_nor[3 * t + d];
+    pos[d] = side == 0 ? tri_bar[3 * t + d] + h * nd / s : tri_bar[3 * t + d] - h * nd / s;
+  }
+  int pi1 = pind[6 * t + 3 * side + 0], pi2 = pind[6 * t + 3 * side + 1];
+  const double eps = 2.220446049250313e-16;
+  int k1 = ffloor(pos[2] * g.dx3) + 1;
+  int kin[3] = {k1 - 1, k1, k1};                  // mls_heatFlux.f90:213 (third layer repeats k1)
+  int k1w = fmod_pos(k1 - 1, g.n3m) + 1;
+  int keul[3] = {k1w - 1, k1w, k1w + 1};
+  double w[3][3], dw[3][3], dd[3][3];             // [axis][point]
+  for (int q = 0; q < 3; ++q) {
+    double pc[3] = {coord(A, 0, 1, pi1 - 1 + q), coord(A, 1, 1, pi2 - 1 + q), coord(A, 2, 1, kin[q])};
+    const double dxs[3] = {g.dx1, g.dx2, g.dx3};
+    for (int a = 0; a < 3; ++a) {
+      double r = pos[a] - pc[a];
+      double np = fabs(r) / (A.wscl / dxs[a]);
+      w[a][q] = mls_gaussian(np, A.wcon);
+      dw[a][q] = (np < eps) ? 0.0 : mls_gauss_deriv(np, A.wcon) * (r / fabs(r) / (A.wscl / dxs[a]));
+      dd[a][q] = pc[a] - pos[a];
+    }
+  }
+  double S[3][3], D[3][3];
+  for (int a = 0; a < 3; ++a) { moments3(w[a], dd[a], S[a]); moments3(dw[a], dd[a], D[a]); }
+  double Ai[16];
+  moment_matrix(S[0], S[1], S[2], Ai);
+  if (!inv4(Ai)) { atomicOr(flag, 1); qout[t] = 0.0; return; }
+  const double gam[4] = {Ai[0], Ai[1], Ai[2], Ai[3]};     // A^{-1} p(x0), p(x0) = e0
+  // sums over the cage of T times the weighted basis: MT (weights), MD[d]
+  // (derivative of the weights along d)
+  double MT[4] = {0, 0, 0, 0}, MD[3][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}};
+  for (int kk = 0; kk < 3; ++kk)
+    for (int jj = 0; jj < 3; ++jj) {
+      int jj_ = fmod_pos(pi2 - 1 + jj - 1, g.n2m), kk_ = wrap(keul[kk] - 1, g.n3m);
+      double wyz = w[1][jj] * w[2][kk], dyz = dw[1][jj] * w[2][kk], ydz = w[1][jj] * dw[2][kk];
+      for (int ii = 0; ii < 3; ++ii) {
+        int ii_ = fmod_pos(pi1 - 1 + ii - 1, g.n1m);
+        double T = temp[cidx(g, ii_, jj_, kk_)];
+        double pb[4] = {1.0, dd[0][ii], dd[1][jj], dd[2][kk]};
+        double a0 = w[0][ii] * wyz * T, a1 = dw[0][ii] * wyz * T, a2 = w[0][ii] * dyz * T, a3 = w[0][ii] * ydz * T;
+        for (int r = 0; r < 4; ++r) {
+          MT[r] = fma(a0, pb[r], MT[r]);
+          MD[0][r] = fma(a1, pb[r], MD[0][r]);
+          MD[1][r] = fma(a2, pb[r], MD[1][r]);
+          MD[2][r] = fma(a3, pb[r], MD[2][r]);
+        }
+      }
+    }
+  double grad[3];
+  for (int d = 0; d < 3; ++d) {
+    double dA[16];
+    double X[3], Y[3], Z[3];
+    for (int m = 0; m < 3; ++m) {
+      X[m] = d == 0 ? D[0][m] : S[0][m];
+      Y[m] = d == 1 ? D[1][m] : S[1][m];
+      Z[m] = d == 2 ? D[2][m] : S[2][m];
+    }
+    moment_matrix(X, Y, Z, dA);
+    double pk[4];
+    for (int r = 0; r < 4; ++r) {
+      double a = 0;
+      for (int cc = 0; cc < 4; ++cc) a = fma(dA[r + 4 * cc], gam[cc], a);
+      pk[r] = (r == d + 1 ? 1.0 : 0.0) - a;
+    }
+    double acc = 0;
+    for (int r = 0; r < 4; ++r) {
+      double dg = 0;
+      for (int cc = 0; cc < 4; ++cc) dg = fma(Ai[r + 4 * cc], pk[cc], dg);
+      acc = fma(dg, MT[r], fma(gam[r], MD[d][r], acc));
+    }
+    grad[d] = acc;
+  }
+  double qv = n0 * grad[0] + n1 * grad[1] + n2 * grad[2];
+  qout[t] = qv / pec;
+}
+
 // face -> vertex: qw_v(v) = sum over adjacent faces (ascending) of q_f*(A_f/3/A_v)
 __global__ void face_to_vert_kernel(int nv, const int* __restrict__ adj_off, const int* __restrict__ adj_face,
                                     const double* __restrict__ sur, const double* __restrict__ avert,
@@ -1360,6 +1515,15 @@ void lagr_find_centroid_indices(Ctx* c) {
 }
 
 static void mls_weight_launch(Ctx* c) {
+  if (c->precision == 1) {
+    { MIBM_PROF(c, "mls_weight_sep");
+      mls_weight_sep_kernel<<<div_up(4 * (size_t)c->maxnf, 128), 128, 0, c->stream>>>(
+          lag_args(c), M<double>(c, MIBM_M_TRI_BAR), M<int>(c, MIBM_M_GHOST_FACE), M<int>(c, MIBM_M_PIND),
+          M<double>(c, MIBM_M_PTXAB_Q1), M<double>(c, MIBM_M_PTXAB_Q2), M<double>(c, MIBM_M_PTXAB_Q3),
+          M<double>(c, MIBM_M_PTXAB_TEMP), c->dflag); }
+    ++c->launches;
+    return;
+  }
   { MIBM_PROF(c, "mls_weight");
     mls_weight_kernel<<<div_up(4 * (size_t)c->maxnf, 64), 64, 0, c->stream>>>(
         lag_args(c), M<double>(c, MIBM_M_TRI_BAR), M<int>(c, MIBM_M_GHOST_FACE), M<int>(c, MIBM_M_PIND),
@@ -1412,11 +1576,19 @@ void lagr_find_probe_indices(Ctx* c) {
 
 static void heat_flux_launch(Ctx* c) {
   LagState* s = lag_of(c);
-  { MIBM_PROF(c, "heat_flux");
+  if (c->precision == 1) {
+    MIBM_PROF(c, "heat_flux_sep");
+    heat_flux_sep_kernel<<<div_up(2 * (size_t)c->maxnf, 128), 128, 0, c->stream>>>(
+        lag_args(c), c->df[MIBM_F_TEMP], M<double>(c, MIBM_M_TRI_BAR), M<double>(c, MIBM_M_TRI_NOR),
+        M<int>(c, MIBM_M_GHOST_FACE), M<int>(c, MIBM_M_PIND), c->S(MIBM_S_H_EULERIAN), c->S(MIBM_S_PEC),
+        M<double>(c, MIBM_M_QW_O), M<double>(c, MIBM_M_QW_I), c->dflag);
+  } else {
+    MIBM_PROF(c, "heat_flux");
     heat_flux_kernel<<<div_up(2 * (size_t)c->maxnf, 64), 64, 0, c->stream>>>(
         lag_args(c), c->df[MIBM_F_TEMP], M<double>(c, MIBM_M_TRI_BAR), M<double>(c, MIBM_M_TRI_NOR),
         M<int>(c, MIBM_M_GHOST_FACE), M<int>(c, MIBM_M_PIND), c->S(MIBM_S_H_EULERIAN), c->S(MIBM_S_PEC),
-        M<double>(c, MIBM_M_QW_O), M<double>(c, MIBM_M_QW_I), c->dflag); }
+        M<double>(c, MIBM_M_QW_O), M<double>(c, MIBM_M_QW_I), c->dflag);
+  }
   { MIBM_PROF(c, "face_to_vert");
     face_to_vert_kernel<<<div_up(c->maxnv, 128), 128, 0, c->stream>>>(
         c->maxnv, s->adj_off, s->adj_face, M<double>(c, MIBM_M_SUR), M<double>(c, MIBM_M_AVERT),

@@ -17,6 +17,8 @@
 
 namespace mibm {
 
+typedef int idx_t;
+
 struct StencilArgs {
   Grid g;
   const double* __restrict__ vx;
@@ -77,22 +79,23 @@ static StencilArgs make_args(Ctx* c) {
   return a;
 }
 
+// Cell index and the six periodic neighbour offsets in 32-bit arithmetic
+// (the largest supported grid, 512^3 with pitch 512, has < 2^31 cells).
 #define CELL_INDEX                                                   \
   const Grid& g = A.g;                                               \
   int i = blockIdx.x * blockDim.x + threadIdx.x;                     \
   int j = blockIdx.y * blockDim.y + threadIdx.y;                     \
   int k = blockIdx.z;                                                \
   if (i >= g.n1m || j >= g.n2m) return;                              \
-  const int ip = (i + 1 == g.n1m) ? 0 : i + 1;                       \
-  const int im = (i == 0) ? g.n1m - 1 : i - 1;                       \
-  const size_t P = g.P;                                              \
-  const size_t PL = g.plane;                                         \
-  const size_t c0 = cidx(g, i, j, k);                                \
-  const ptrdiff_t dip = (ptrdiff_t)ip - i, dim = (ptrdiff_t)im - i;   \
-  const ptrdiff_t djp = (j + 1 == g.n2m) ? -(ptrdiff_t)(g.n2m - 1) * (ptrdiff_t)P : (ptrdiff_t)P; \
-  const ptrdiff_t djm = (j == 0) ? (ptrdiff_t)(g.n2m - 1) * (ptrdiff_t)P : -(ptrdiff_t)P;         \
-  const ptrdiff_t dkp = (k + 1 == g.n3m) ? -(ptrdiff_t)(g.n3m - 1) * (ptrdiff_t)PL : (ptrdiff_t)PL; \
-  const ptrdiff_t dkm = (k == 0) ? (ptrdiff_t)(g.n3m - 1) * (ptrdiff_t)PL : -(ptrdiff_t)PL;         \
+  const int P = g.P;                                                 \
+  const int PL = (int)g.plane;                                       \
+  const idx_t c0 = i + P * (j + g.n2m * k);                          \
+  const idx_t dip = (i + 1 == g.n1m) ? 1 - g.n1m : 1;                \
+  const idx_t dim = (i == 0) ? g.n1m - 1 : -1;                       \
+  const idx_t djp = (j + 1 == g.n2m) ? -(g.n2m - 1) * P : P;         \
+  const idx_t djm = (j == 0) ? (g.n2m - 1) * P : -P;                 \
+  const idx_t dkp = (k + 1 == g.n3m) ? -(g.n3m - 1) * PL : PL;       \
+  const idx_t dkm = (k == 0) ? (g.n3m - 1) * PL : -PL;               \
   (void)dip; (void)dim; (void)djp; (void)djm; (void)dkp; (void)dkm; (void)P;
 
 // ---------------------------------------------------------------------
@@ -103,8 +106,8 @@ static StencilArgs make_args(Ctx* c) {
 // arithmetic and FP64<->FP32 conversions share the low FP64 issue rate).
 // ---------------------------------------------------------------------
 template <typename R>
-__device__ __forceinline__ R h_x(const StencilArgs& A, size_t c0, ptrdiff_t dip, ptrdiff_t dim, ptrdiff_t djp,
-                                 ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm, const StepParams& p) {
+__device__ __forceinline__ R h_x(const StencilArgs& A, idx_t c0, idx_t dip, idx_t dim, idx_t djp,
+                                 idx_t djm, idx_t dkp, idx_t dkm, const StepParams& p) {
   const Prog<R> F = prog<R>(A);
   const R* vx = F.u; const R* vy = F.v; const R* vz = F.w;
   R udx1 = coef<R>(p, kQ1), udx2 = coef<R>(p, kQ2), udx3 = coef<R>(p, kQ3);
@@ -121,8 +124,8 @@ __device__ __forceinline__ R h_x(const StencilArgs& A, size_t c0, ptrdiff_t dip,
 }
 
 template <typename R>
-__device__ __forceinline__ R h_y(const StencilArgs& A, size_t c0, ptrdiff_t dip, ptrdiff_t dim, ptrdiff_t djp,
-                                 ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm, const StepParams& p) {
+__device__ __forceinline__ R h_y(const StencilArgs& A, idx_t c0, idx_t dip, idx_t dim, idx_t djp,
+                                 idx_t djm, idx_t dkp, idx_t dkm, const StepParams& p) {
   const Prog<R> F = prog<R>(A);
   const R* vx = F.u; const R* vy = F.v; const R* vz = F.w;
   R udx1 = coef<R>(p, kQ1), udx2 = coef<R>(p, kQ2), udx3 = coef<R>(p, kQ3);
@@ -139,8 +142,8 @@ __device__ __forceinline__ R h_y(const StencilArgs& A, size_t c0, ptrdiff_t dip,
 }
 
 template <typename R>
-__device__ __forceinline__ R h_z(const StencilArgs& A, size_t c0, ptrdiff_t dip, ptrdiff_t dim, ptrdiff_t djp,
-                                 ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm, const StepParams& p) {
+__device__ __forceinline__ R h_z(const StencilArgs& A, idx_t c0, idx_t dip, idx_t dim, idx_t djp,
+                                 idx_t djm, idx_t dkp, idx_t dkm, const StepParams& p) {
   const Prog<R> F = prog<R>(A);
   const R* vx = F.u; const R* vy = F.v; const R* vz = F.w;
   R udx1 = coef<R>(p, kQ1), udx2 = coef<R>(p, kQ2), udx3 = coef<R>(p, kQ3);
@@ -163,8 +166,8 @@ __device__ __forceinline__ R h_z(const StencilArgs& A, size_t c0, ptrdiff_t dip,
 __device__ __forceinline__ double nint_d(double x) { return round(x); }   // Fortran NINT semantics
 
 template <typename R>
-__device__ __forceinline__ R h_t(const StencilArgs& A, int i, int j, int k, size_t c0, ptrdiff_t dip, ptrdiff_t dim,
-                                 ptrdiff_t djp, ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm, const StepParams& p) {
+__device__ __forceinline__ R h_t(const StencilArgs& A, int i, int j, int k, idx_t c0, idx_t dip, idx_t dim,
+                                 idx_t djp, idx_t djm, idx_t dkp, idx_t dkm, const StepParams& p) {
   const Grid& g = A.g;
   const Prog<R> F = prog<R>(A);
   const R* vx = F.u; const R* vy = F.v; const R* vz = F.w; const R* T = F.t;
@@ -212,8 +215,8 @@ __global__ void hdnl_kernel(StencilArgs A, int which, const StepParams* __restri
 // RHS of the factored implicit step
 // ---------------------------------------------------------------------
 template <typename R>
-__device__ __forceinline__ R lap(const R* q, size_t c0, ptrdiff_t dip, ptrdiff_t dim, ptrdiff_t djp, ptrdiff_t djm,
-                                 ptrdiff_t dkp, ptrdiff_t dkm, const StepParams& p, bool fortran_order_t) {
+__device__ __forceinline__ R lap(const R* q, idx_t c0, idx_t dip, idx_t dim, idx_t djp, idx_t djm,
+                                 idx_t dkp, idx_t dkm, const StepParams& p, bool fortran_order_t) {
   R qc = q[c0];
   R d1 = (q[c0 + dip] - R(2.0) * qc + q[c0 + dim]) * coef<R>(p, kDQ1);
   R d2 = (q[c0 + djp] - R(2.0) * qc + q[c0 + djm]) * coef<R>(p, kDQ2);
@@ -223,8 +226,8 @@ __device__ __forceinline__ R lap(const R* q, size_t c0, ptrdiff_t dip, ptrdiff_t
 }
 
 template <typename R>
-__device__ __forceinline__ R rhs_value(const StencilArgs& A, int which, R h, R ru, size_t c0, ptrdiff_t dip,
-                                       ptrdiff_t dim, ptrdiff_t djp, ptrdiff_t djm, ptrdiff_t dkp, ptrdiff_t dkm,
+__device__ __forceinline__ R rhs_value(const StencilArgs& A, int which, R h, R ru, idx_t c0, idx_t dip,
+                                       idx_t dim, idx_t djp, idx_t djm, idx_t dkp, idx_t dkm,
                                        const StepParams& p) {
   const Prog<R> F = prog<R>(A);
   R ga = coef<R>(p, kGA), ro = coef<R>(p, kRO), alre = coef<R>(p, kALRE), dt = coef<R>(p, kDT);
@@ -257,18 +260,31 @@ __global__ void invtr_rhs_kernel(StencilArgs A, int which, const StepParams* __r
 
 // fused path: explicit term computed in registers (hdnl + invtr RHS); R is
 // the compute type, ru and rhs are stored in R
-template <typename R>
-__global__ void fused_rhs_kernel(StencilArgs A, int which, const StepParams* __restrict__ pp, R* __restrict__ ru,
-                                 R* __restrict__ rhs) {
+// (one instance per component W, so each carries only its own stencil)
+template <typename R, int W>
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 3)
+fused_rhs_kernel(StencilArgs A, const StepParams* __restrict__ pp, R* __restrict__ ru, R* __restrict__ rhs) {
   CELL_INDEX
-  StepParams p = *pp;
+  const StepParams& p = *pp;
   R h;
-  if (which == 0) h = h_x<R>(A, c0, dip, dim, djp, djm, dkp, dkm, p);
-  else if (which == 1) h = h_y<R>(A, c0, dip, dim, djp, djm, dkp, dkm, p);
-  else if (which == 2) h = h_z<R>(A, c0, dip, dim, djp, djm, dkp, dkm, p);
+  if (W == 0) h = h_x<R>(A, c0, dip, dim, djp, djm, dkp, dkm, p);
+  else if (W == 1) h = h_y<R>(A, c0, dip, dim, djp, djm, dkp, dkm, p);
+  else if (W == 2) h = h_z<R>(A, c0, dip, dim, djp, djm, dkp, dkm, p);
   else h = h_t<R>(A, i, j, k, c0, dip, dim, djp, djm, dkp, dkm, p);
-  rhs[c0] = rhs_value<R>(A, which, h, ru[c0], c0, dip, dim, djp, djm, dkp, dkm, p);
+  rhs[c0] = rhs_value<R>(A, W, h, ru[c0], c0, dip, dim, djp, djm, dkp, dkm, p);
   ru[c0] = h;
+}
+
+template <typename R>
+static void fused_rhs_launch(Ctx* c, const StepParams* dp, int w, R* ru, R* rhs) {
+  dim3 grid(div_up(c->g.n1m, 32), div_up(c->g.n2m, 8), c->g.n3m), block(32, 8);
+  StencilArgs a = make_args(c);
+  switch (w) {
+    case 0: fused_rhs_kernel<R, 0><<<grid, block, 0, c->stream>>>(a, dp, ru, rhs); break;
+    case 1: fused_rhs_kernel<R, 1><<<grid, block, 0, c->stream>>>(a, dp, ru, rhs); break;
+    case 2: fused_rhs_kernel<R, 2><<<grid, block, 0, c->stream>>>(a, dp, ru, rhs); break;
+    default: fused_rhs_kernel<R, 3><<<grid, block, 0, c->stream>>>(a, dp, ru, rhs); break;
+  }
 }
 
 // ---------------------------------------------------------------------
@@ -390,9 +406,19 @@ __global__ void interp_vof_kernel(StencilArgs A, double* __restrict__ vofx, doub
   CELL_INDEX
   const double* vp = A.vofp;
   double c = vp[c0];
-  vofx[c0] = 0.5 * (vp[c0 + dim] + c);
-  vofy[c0] = 0.5 * (vp[c0 + djm] + c);
-  vofz[c0] = 0.5 * (vp[c0 + dkm] + c);
+  // 0.5*(a + c) == c exactly when a and c are the same double (a + c = 2c
+  // and the halving are exact), which holds everywhere but at the
+  // interface; testing the bits keeps those cells off the FP64 pipe
+  const long long cb = __double_as_longlong(c);
+  double a = vp[c0 + dim], b = vp[c0 + djm], d = vp[c0 + dkm];
+  bool same = __double_as_longlong(a) == cb && __double_as_longlong(b) == cb && __double_as_longlong(d) == cb;
+  if (__all_sync(__activemask(), same)) {   // warp-uniform branch: no FP64 issue at all
+    vofx[c0] = c; vofy[c0] = c; vofz[c0] = c;
+    return;
+  }
+  vofx[c0] = 0.5 * (a + c);
+  vofy[c0] = 0.5 * (b + c);
+  vofz[c0] = 0.5 * (d + c);
 }
 
 __global__ void velforce_apply_kernel(Grid g, const double* __restrict__ mean3, const double* __restrict__ fx,
@@ -539,8 +565,7 @@ void k_invtr_rhs(Ctx* c, int which, const StepParams* dp, double* rhs_out) {
 void k_fused_rhs(Ctx* c, const StepParams* dp) {
   for (int w = 0; w < 4; ++w) {
     { MIBM_PROF(c, "fused_rhs");
-      fused_rhs_kernel<double><<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), w, dp, ru_of(c, w),
-                                                                             c->rhs4 + (size_t)w * c->g.cells); }
+      fused_rhs_launch<double>(c, dp, w, ru_of(c, w), c->rhs4 + (size_t)w * c->g.cells); }
     ++c->launches;
   }
   MIBM_LAUNCH_CHECK(c, "fused_rhs");
@@ -550,9 +575,7 @@ void k_fused_rhs(Ctx* c, const StepParams* dp) {
 void k_fused_rhs_f32(Ctx* c, const StepParams* dp, float* ru4, float* rhs4) {
   for (int w = 0; w < 4; ++w) {
     { MIBM_PROF(c, "fused_rhs_f32");
-      fused_rhs_kernel<float><<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), w, dp,
-                                                                            ru4 + (size_t)w * c->g.cells,
-                                                                            rhs4 + (size_t)w * c->g.cells); }
+      fused_rhs_launch<float>(c, dp, w, ru4 + (size_t)w * c->g.cells, rhs4 + (size_t)w * c->g.cells); }
     ++c->launches;
   }
   MIBM_LAUNCH_CHECK(c, "fused_rhs_f32");

@@ -12,7 +12,7 @@ import pytest
 
 from melt_ibm_gb300 import abi
 from melt_ibm_gb300.case import Case, CaseConfig, CONFIG0
-from tests.helpers import FIELDS_OUT, rel_l2, small_config
+from tests.helpers import FIELDS_OUT, pair, rel_l2, set_substep, small_config
 
 pytestmark = pytest.mark.gpu
 TOL_FIELD = 1e-6
@@ -63,3 +63,41 @@ def test_precision_form_deterministic(gpu_lib):
     b, _ = _run(case, gpu_lib, 2, 1)
     for k in FIELDS_OUT:
         assert np.array_equal(a[k], b[k]), k
+
+
+def _mls_pair(oracle_lib, gpu_lib):
+    case = Case(small_config(n=24, level=2))
+    co, cg = pair(case, oracle_lib, gpu_lib, initial_tag=True)
+    cg.bind(gpu_lib)
+    gpu_lib.mibm_set_precision_(C.byref(C.c_int(1)), C.byref(C.c_int(2)))
+    gpu_lib.check("set_precision")
+    return co, cg
+
+
+def test_precision_mls_weights_match_oracle(oracle_lib, gpu_lib):
+    """Shifted-basis, separable-moment MLS weights (precision form) against the
+    reference construction: equal up to the reference's own conditioning error."""
+    co, cg = _mls_pair(oracle_lib, gpu_lib)
+    for c, lib in ((co, oracle_lib), (cg, gpu_lib)):
+        c.bind(lib)
+        lib.findcentroidindices_()
+        lib.mlsweight_()
+        lib.check("mlsweight")
+    cg.sync_to_host(gpu_lib, -1)
+    for mid in (abi.MIBM_M_PTXAB_Q1, abi.MIBM_M_PTXAB_Q2, abi.MIBM_M_PTXAB_Q3, abi.MIBM_M_PTXAB_TEMP):
+        e = rel_l2(cg.mesh_arrays[mid], co.mesh_arrays[mid])
+        assert e <= 1e-8, (mid, e)
+
+
+def test_precision_heat_flux_matches_oracle(oracle_lib, gpu_lib):
+    co, cg = _mls_pair(oracle_lib, gpu_lib)
+    for c, lib in ((co, oracle_lib), (cg, gpu_lib)):
+        c.bind(lib)
+        set_substep(c, 0, dt=0.01)
+        lib.findprobeindices_()
+        lib.mls_heatflux_()
+        lib.check("heat")
+    cg.sync_to_host(gpu_lib, -1)
+    for mid in (abi.MIBM_M_QW_O, abi.MIBM_M_QW_I, abi.MIBM_M_QW_OVERT, abi.MIBM_M_QW_IVERT):
+        e = rel_l2(cg.mesh_arrays[mid], co.mesh_arrays[mid])
+        assert e <= 1e-7, (mid, e)
