@@ -78,6 +78,14 @@ ALGO_PASSES = {
     "divg": 4.0, "updvp": 7.0, "prcalc": 3.0, "hdnl": 6.0,
 }
 
+# DRAM bytes per launch measured with ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum, one pass) for the kernel that dominates the FP64
+# step, at the size given, per cell: profiles/fused_rhs_melt128_fp64_dram.md.
+# Other sizes scale by the cell count (the traffic is per-cell compulsory).
+NCU_TRAFFIC = {
+    "fused_rhs": {"bytes_per_cell": 96.4e6 / 128 ** 3, "measured_at": "128^3 (melt128_fixed)"},
+}
+
 FIELDS = {"u": abi.MIBM_F_VX, "v": abi.MIBM_F_VY, "w": abi.MIBM_F_VZ, "T": abi.MIBM_F_TEMP, "p": abi.MIBM_F_PR}
 FIELD_MASK = sum(1 << f for f in FIELDS.values())
 MESH_MASK = 1 << (32 + abi.MIBM_M_XYZV)
@@ -285,8 +293,12 @@ def run_gpu(args):
     if passes is not None:
         algo_bytes = passes * 8.0 * n3
         achieved = algo_bytes / (avg_ms * 1e-3) / 1e9
+        tr = NCU_TRAFFIC.get(dname)
+        traffic = tr["bytes_per_cell"] * n3 if tr else None
         roofline = {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peaks["hbm_gbs"],
-                    "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                    "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
+                    "traffic_source": (f"ncu dram bytes per launch measured at {tr['measured_at']}, "
+                                       f"scaled by cells") if tr else None,
                     "algo_bytes_per_launch": algo_bytes, "avg_launch_ms": avg_ms,
                     "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs)",
                     "note": "FP64 stencils are bounded by the FP64 FMA rate (about 1.2 TFLOP/s measured), "
