@@ -113,6 +113,9 @@ enum {
   MIBM_S_CFLM, MIBM_S_H_EULERIAN, MIBM_S_CELVOL, MIBM_S_VOLUME, MIBM_S_SURFACE,
   MIBM_S_POS_CM, MIBM_S_VEL_CM, MIBM_S_OMEGA_C, MIBM_S_WCON, MIBM_S_WSCL,
   MIBM_S_E_THRESH, MIBM_S_V_THRESH, MIBM_S_DENS_RATIO, MIBM_S_TIME,
+  /* HIT forcing parameters (param.f90:16, read from HITForcing.in at    */
+  /* papero.f90:52-56): tl, epsstar, kf_on_kmin, C_HIT                   */
+  MIBM_S_TL, MIBM_S_EPSSTAR, MIBM_S_KF_ON_KMIN, MIBM_S_C_HIT,
   MIBM_NSCALARS
 };
 
@@ -121,6 +124,8 @@ enum {
   MIBM_I_IMLSFOR = 0, MIBM_I_IMLSSTR, MIBM_I_IMELT, MIBM_I_IREMESH,
   MIBM_I_TAGTYPE, MIBM_I_FORCING, MIBM_I_IDTV, MIBM_I_NTIME,
   MIBM_I_STATIONARY, MIBM_I_NSST,
+  MIBM_I_WHICH_HIT,   /* param.f90:17: 1 Eswaran-Pope, 2 ABC                  */
+  MIBM_I_HIT_SEED,    /* seed of the forcing's random stream (see below)       */
   MIBM_NINTS
 };
 
@@ -212,6 +217,33 @@ double mibm_divergence_max_(void);
 /* Initial full cell tagging at t = 0 (pencil_rayTag.f90:37-165 with the  */
 /* narrow band, tagCells.f90:17-23 with initial_tag = .true.).            */
 void tagcells_initial_(void);
+
+/* HIT forcing into forcx, forcy, forcz (called once per step before      */
+/* tschem_ when forcing = 1, gcurv.f90:164-170).                          */
+/* calchitrandomforce_: Eswaran & Pope stochastic forcing, hit.f90:1-126.  */
+/*   The Ornstein-Uhlenbeck update of bhat(3,nmodes,nmodes,nmodes) and    */
+/*   the solenoidal projection run on the host in the reference's loop    */
+/*   order; the DFT sums run on the device.  gfortran's random_number      */
+/*   cannot be reproduced, so the Gaussian increments come from this       */
+/*   library's stream: splitmix64 seeded with the HIT_SEED integer at the */
+/*   first call, u = ((x >> 11) + 1) * 2^-53 in (0, 1], Box-Muller as in   */
+/*   hit.f90:40-42 (two draws per direction, modes in l, m, n order).      */
+/*   bhat lives in the context; nmodes = 2*floor(kf_on_kmin) + 1.         */
+void calchitrandomforce_(void);
+/* calcabc_hitforce_: ABC forcing, hit.f90:224-254 (CalcABC_HITForce).    */
+void calcabc_hitforce_(void);
+/* mibm_hit_modes_: nmodes of the current parameters (InitRandomForce,    */
+/* hit.f90:128-150).  mibm_hit_bhat_: copy bhat out of (dir = 0) or into  */
+/* (dir = 1) the context, as 2*3*nmodes^3 doubles (re, im) in Fortran     */
+/* order bhat(ndir,l,m,n) -- the state WriteRandForcCoef / hdf_read_bhat  */
+/* save and restore (hit.f90:256-356).                                    */
+int  mibm_hit_modes_(void);
+void mibm_hit_bhat_(double* bhat, const int* dir);
+/* Linear forcing (no counterpart in the reference, which offers only the */
+/* two forcings above): forc = C_HIT * u at each velocity's own staggered */
+/* position, stored as xlen * C_HIT * u so that the reference's explicit  */
+/* term adds VOF * C_HIT * u (hdnl1.f90:74 divides forcx by xlen).         */
+void mibm_linear_hit_force_(void);
 
 /* ------------------------------------------------------------------ */
 /* Allocation-free x-line solve.  No counterpart in the reference: it is  */

@@ -73,13 +73,15 @@ SIGNATURES: dict[str, tuple] = {
     "solxj_": (None, [_D]),
     "solxk_": (None, [C.c_void_p, _D]),
     "interp_": (None, [C.c_void_p, C.c_void_p, _I, _I, _I, _I, _I, _I]),
+    "mibm_hit_modes_": (C.c_int, []),
+    "mibm_hit_bhat_": (None, [C.c_void_p, _I]),
 }
 VOID_ROUTINES = [
     "tschem_", "hdnl1_", "hdnl2_", "hdnl3_", "hdnlte_", "invtr1_", "invtr2_", "invtr3_",
     "invtrte_", "divg_", "phcalc_", "updvp_", "prcalc_", "findcentroidindices_",
     "mlsweight_", "mlsforce_", "velforce_", "tempforce_", "findprobeindices_",
     "mls_heatflux_", "apply_stefancondition_", "tagcells_", "particle_", "cfl_", "get_dt_",
-    "tagcells_initial_",
+    "tagcells_initial_", "calchitrandomforce_", "calcabc_hitforce_", "mibm_linear_hit_force_",
 ]
 for _n in VOID_ROUTINES:
     SIGNATURES[_n] = (None, [])

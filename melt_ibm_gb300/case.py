@@ -89,6 +89,12 @@ class CaseConfig:
     iremesh: int = 0
     tagtype: int = 1
     forcing: int = 0
+    which_hit: int = 1            # 1 Eswaran-Pope, 2 ABC (HITForcing.in); 3 = linear forcing (extension)
+    tl: float = 0.5               # HITForcing.in: TL, EPSSTAR, KF/KMIN, C
+    epsstar: float = 0.05
+    kf_on_kmin: float = 2.3
+    c_hit: float = 0.1
+    hit_seed: int = 0
     dens_ratio: float = 1.0
     mesh_level: int = 3
     rad_p: float = 0.5
@@ -167,6 +173,10 @@ class Case:
         self.set_S(A.MIBM_S_WCON, 0.3)                          # initmls.f90:12
         self.set_S(A.MIBM_S_WSCL, 1.5)                          # initmls.f90:13
         self.set_S(A.MIBM_S_DENS_RATIO, c.dens_ratio)
+        self.set_S(A.MIBM_S_TL, c.tl)
+        self.set_S(A.MIBM_S_EPSSTAR, c.epsstar)
+        self.set_S(A.MIBM_S_KF_ON_KMIN, c.kf_on_kmin)
+        self.set_S(A.MIBM_S_C_HIT, c.c_hit)
         h = (1.0 / self.dx1 + 1.0 / self.dx2 + 1.0 / self.dx3) / 3.0
         celvol = 1.0 / (self.dx1 * self.dx2 * self.dx3)
         self.set_S(A.MIBM_S_H_EULERIAN, h)
@@ -177,6 +187,7 @@ class Case:
         iv[A.MIBM_I_IMLSFOR], iv[A.MIBM_I_IMLSSTR], iv[A.MIBM_I_IMELT] = c.imlsfor, c.imlsstr, c.imelt
         iv[A.MIBM_I_IREMESH], iv[A.MIBM_I_TAGTYPE], iv[A.MIBM_I_FORCING] = c.iremesh, c.tagtype, c.forcing
         iv[A.MIBM_I_IDTV], iv[A.MIBM_I_NSST] = c.idtv, 3
+        iv[A.MIBM_I_WHICH_HIT], iv[A.MIBM_I_HIT_SEED] = c.which_hit, c.hit_seed
         stationary = not (c.imlsfor == 1 and (c.imlsstr == 1 or c.imelt == 1))   # papero.f90:353-358
         iv[A.MIBM_I_STATIONARY] = 1 if stationary else 0
 
@@ -314,6 +325,15 @@ class Case:
             if ntime != 1:
                 self.set_S(A.MIBM_S_DT, self.S(A.MIBM_S_DTMAX))
             lib.get_dt_()
+        if self.iv[A.MIBM_I_FORCING] == 1:        # gcurv.f90:164-170
+            which = self.iv[A.MIBM_I_WHICH_HIT]
+            if which == 1:
+                lib.calchitrandomforce_()
+            elif which == 2:
+                lib.calcabc_hitforce_()
+            elif which == 3:
+                lib.mibm_linear_hit_force_()
+            lib.check("forcing")
         lib.tschem_()
         lib.check("tschem")
         self.set_S(A.MIBM_S_TIME, self.S(A.MIBM_S_TIME) + self.S(A.MIBM_S_DT))

@@ -243,6 +243,21 @@ void tagcells_(void) { DROPIN_BEGIN lagr_tag_narrow_band(c); DROPIN_END }
 void tagcells_initial_(void) { DROPIN_BEGIN lagr_tag_initial(c); DROPIN_END }
 void particle_(void) { DROPIN_WRITES lagr_particle(c, push_params(c, 3)); DROPIN_END }
 
+// forcx, forcy, forcz are read by the stencils as FP64 in both forms (no
+// FP32 mirror), so the HIT drop-ins leave the mirrors valid
+void calchitrandomforce_(void) { DROPIN_BEGIN k_hit_random_force(c); DROPIN_END }
+void calcabc_hitforce_(void) { DROPIN_BEGIN k_hit_abc_force(c); DROPIN_END }
+void mibm_linear_hit_force_(void) { DROPIN_BEGIN k_hit_linear_force(c); DROPIN_END }
+int mibm_hit_modes_(void) {
+  Ctx* c = current(); if (!ready(c)) return 0;
+  return hit_modes(c);
+}
+void mibm_hit_bhat_(double* bhat, const int* dir) {
+  Ctx* c = current(); if (!ready(c)) return;
+  if (!bhat || (*dir != 0 && *dir != 1)) { fail(c, MIBM_EINVAL, "hit_bhat: dir 0 (get) or 1 (set)"); return; }
+  hit_bhat(c, bhat, *dir);
+}
+
 void cfl_(void) {
   DROPIN_BEGIN
   *c->hs[MIBM_S_CFLM] = k_cfl(c);
@@ -287,9 +302,11 @@ double mibm_divergence_max_(void) {
   return v;
 }
 
-void interp_(double*, double*, const int*, const int*, const int*, const int*, const int*, const int*) {
+void interp_(double* arrold, double* arrnew, const int* n1o, const int* n2o, const int* n3o, const int* intvar,
+             const int* kstarto, const int* kendo) {
   DROPIN_BEGIN
-  fail(c, MIBM_EINVAL, "interp_: not available in this build");
+  if (!arrold || !arrnew) { fail(c, MIBM_EINVAL, "interp_: null array"); return; }
+  k_interp_restart(c, arrold, arrnew, *n1o, *n2o, *n3o, *intvar, *kstarto, *kendo);
   DROPIN_END
 }
 

@@ -216,6 +216,16 @@ void k_updvp_f32(Ctx* c, const StepParams* dp, const float* phi, const double* m
 void k_prcalc_f32(Ctx* c, const StepParams* dp, const float* phi, bool mirror);
 void k_divg_f32(Ctx* c, const StepParams* dp, float* res);
 void k_mirror_fields(Ctx* c);
+// HIT forcing (hit.cu)
+void k_hit_random_force(Ctx* c);
+void k_hit_abc_force(Ctx* c);
+void k_hit_linear_force(Ctx* c);
+int hit_modes(Ctx* c);
+void hit_bhat(Ctx* c, double* buf, int dir);
+void hit_free(Ctx* c);
+// restart regrid (interp.cu): host arrays in, host array out
+void k_interp_restart(Ctx* c, double* arrold, double* arrnew, int n1o, int n2o, int n3o, int intvar, int kstarto,
+                      int kendo);
 // precision form around host transfers: the explicit-term histories ru* are
 // carried in FP32 on the device; uploads of u, v, w, T, p invalidate the mirrors
 void precision_before_download(Ctx* c, unsigned long long mask);

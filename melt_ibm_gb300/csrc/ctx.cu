@@ -255,6 +255,7 @@ void release(Ctx* c) {
   lagr_free(c);
   tri_free(c);
   fft_free(c);
+  hit_free(c);
   if (c->stream) cudaStreamDestroy(c->stream);
 }
 

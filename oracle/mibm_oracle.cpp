@@ -80,6 +80,11 @@ struct Ctx {
   int* iv[MIBM_NINTS] = {nullptr};
   int maxnv = 0, maxne = 0, maxnf = 0;
   bool inited = false;
+  // HIT forcing state (hit.f90: bhat and the module's random stream)
+  int hit_nmodes = 0;
+  std::vector<cd> hit_bhat;      // bhat(3, nmodes, nmodes, nmodes)
+  bool hit_seeded = false;
+  uint64_t hit_rng = 0;
   // coordinate accessors with the reference's extended ranges (cordin.f90:55-61)
   double xc(int i) const { return xc_[i + n1]; }
   double yc(int j) const { return yc_[j + n2]; }
@@ -1593,6 +1598,144 @@ void tagCells_initial(Ctx& c) {
 // ==========================================================================
 // C-ABI (include/mibm.h)
 // ==========================================================================
+// ---------------------------------------------------------------------------
+// HIT forcing, hit.f90.  InitRandomForce (hit.f90:128-202) is redone at every
+// call (its tables depend on the grid and kf_on_kmin only).  The Gaussian
+// increments come from the library's documented stream (splitmix64 seeded
+// with HIT_SEED, u = ((x >> 11) + 1) * 2^-53, Box-Muller of hit.f90:40-42),
+// since gfortran's random_number cannot be reproduced.
+// ---------------------------------------------------------------------------
+static int hit_modes_of(double kf_on_kmin) {
+  int nbuffer = (int)std::floor(kf_on_kmin) + 1;
+  return (nbuffer - 1) * 2 + 1;
+}
+
+static double hit_uniform(Ctx& c) {
+  uint64_t z = (c.hit_rng += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return (double)((z >> 11) + 1) * (1.0 / 9007199254740992.0);
+}
+
+static void hit_state(Ctx& c) {
+  int nm = hit_modes_of(c.S(MIBM_S_KF_ON_KMIN));
+  if (nm != c.hit_nmodes || c.hit_bhat.size() != 3 * (size_t)nm * nm * nm) {
+    c.hit_nmodes = nm;
+    c.hit_bhat.assign(3 * (size_t)nm * nm * nm, cd(0.0, 0.0));
+  }
+}
+
+void CalcHITRandomForce(Ctx& c) {
+  hit_state(c);
+  const int nmodes = c.hit_nmodes, nbuffer = (nmodes - 1) / 2 + 1;
+  const double pi = c.pi, xlen = c.xlen, ylen = c.ylen, zlen = c.zlen;
+  const double dt = c.S(MIBM_S_DT), TL = c.S(MIBM_S_TL), epsstar = c.S(MIBM_S_EPSSTAR);
+  std::vector<int> waveN(nmodes + 1);
+  for (int i = 1; i <= nbuffer - 1; ++i) waveN[i] = -(nbuffer - i);
+  for (int i = 0; i <= nbuffer - 1; ++i) waveN[nbuffer + i] = i;
+  // exponential tables (1-based)
+  const int n1m = c.n1m, n2m = c.n2m, n3m = c.n3m;
+  auto E = [&](int n, int nn) { return (size_t)(nn - 1) * n; };
+  std::vector<cd> exi(n1m * nmodes), exsi(n1m * nmodes), eyj(n2m * nmodes), eysj(n2m * nmodes),
+      ezk(n3m * nmodes), ezsk(n3m * nmodes);
+  const cd im(0.0, 1.0);
+  for (int i = 1; i <= n1m; ++i)
+    for (int nn = 1; nn <= nmodes; ++nn) {
+      double kappa = (double)waveN[nn] * 2.0 * pi / xlen;
+      exi[E(n1m, nn) + i - 1] = std::exp(im * kappa * c.xm(i));
+      exsi[E(n1m, nn) + i - 1] = std::exp(im * kappa * c.xc(i));
+    }
+  for (int j = 1; j <= n2m; ++j)
+    for (int nn = 1; nn <= nmodes; ++nn) {
+      double kappa = (double)waveN[nn] * 2.0 * pi / ylen;
+      eyj[E(n2m, nn) + j - 1] = std::exp(im * kappa * c.ym(j));
+      eysj[E(n2m, nn) + j - 1] = std::exp(im * kappa * c.yc(j));
+    }
+  for (int k = 1; k <= n3m; ++k)
+    for (int nn = 1; nn <= nmodes; ++nn) {
+      double kappa = (double)waveN[nn] * 2.0 * pi / zlen;
+      ezk[E(n3m, nn) + k - 1] = std::exp(im * kappa * c.zm(k));
+      ezsk[E(n3m, nn) + k - 1] = std::exp(im * kappa * c.zc(k));
+    }
+  // hit.f90:20-60
+  double kf = c.S(MIBM_S_KF_ON_KMIN) * 2.0 * pi / xlen;
+  auto B = [&](int d, int l, int m, int nn) -> cd& {
+    return c.hit_bhat[(size_t)(d - 1) + 3 * ((size_t)(l - 1) + nmodes * ((size_t)(m - 1) + (size_t)nmodes * (nn - 1)))];
+  };
+  std::vector<cd> Fhat(3 * (size_t)nmodes * nmodes * nmodes, cd(0.0, 0.0));
+  auto FH = [&](int d, int l, int m, int nn) -> cd& {
+    return Fhat[(size_t)(d - 1) + 3 * ((size_t)(l - 1) + nmodes * ((size_t)(m - 1) + (size_t)nmodes * (nn - 1)))];
+  };
+  if (!c.hit_seeded) { c.hit_rng = (uint64_t)(int64_t)c.I(MIBM_I_HIT_SEED); c.hit_seeded = true; }
+  for (int l = 1; l <= nmodes; ++l) {
+    double kl = (double)waveN[l] * 2.0 * pi / xlen;
+    for (int m = 1; m <= nmodes; ++m) {
+      double km = (double)waveN[m] * 2.0 * pi / ylen;
+      for (int nn = 1; nn <= nmodes; ++nn) {
+        double kn = (double)waveN[nn] * 2.0 * pi / zlen;
+        double kmag = std::sqrt(kl * kl + km * km + kn * kn);
+        if (kmag > 0.0 && kmag < kf) {
+          for (int ndir = 1; ndir <= 3; ++ndir) {
+            double u1 = hit_uniform(c), u2 = hit_uniform(c);
+            cd rand_complex(std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * pi * u2),
+                            std::sqrt(-2.0 * std::log(u1)) * std::sin(2.0 * pi * u2));
+            B(ndir, l, m, nn) = B(ndir, l, m, nn) * (1.0 - dt / TL) + rand_complex * std::sqrt(2.0 * epsstar * dt / (TL * TL));
+          }
+          double kvec[3] = {kl, km, kn};
+          cd dot = kvec[0] * B(1, l, m, nn) + kvec[1] * B(2, l, m, nn) + kvec[2] * B(3, l, m, nn);
+          for (int d = 1; d <= 3; ++d) FH(d, l, m, nn) = B(d, l, m, nn) - kvec[d - 1] * dot / (kmag * kmag);
+        }
+      }
+    }
+  }
+  F3 &forcx = c.f[MIBM_F_FORCX], &forcy = c.f[MIBM_F_FORCY], &forcz = c.f[MIBM_F_FORCZ];
+  for (F3* q : {&forcx, &forcy, &forcz})
+    std::fill(q->p, q->p + (size_t)q->n1 * q->ny * (q->khi - q->klo + 1), 0.0);
+  // hit.f90:72-124 (loops nn, m, l, k, j, i)
+  for (int nn = 1; nn <= nmodes; ++nn)
+    for (int m = 1; m <= nmodes; ++m)
+      for (int l = 1; l <= nmodes; ++l)
+        for (int k = 1; k <= n3m; ++k)
+          for (int j = 1; j <= n2m; ++j) {
+            cd b1 = eyj[E(n2m, m) + j - 1] * ezk[E(n3m, nn) + k - 1];
+            cd b2 = eysj[E(n2m, m) + j - 1] * ezk[E(n3m, nn) + k - 1];
+            cd b3 = eyj[E(n2m, m) + j - 1] * ezsk[E(n3m, nn) + k - 1];
+            for (int i = 1; i <= n1m; ++i) {
+              forcx(i, j, k) = forcx(i, j, k) + std::real(FH(1, l, m, nn) * exsi[E(n1m, l) + i - 1] * b1);
+              forcy(i, j, k) = forcy(i, j, k) + std::real(FH(2, l, m, nn) * exi[E(n1m, l) + i - 1] * b2);
+              forcz(i, j, k) = forcz(i, j, k) + std::real(FH(3, l, m, nn) * exi[E(n1m, l) + i - 1] * b3);
+            }
+          }
+}
+
+void CalcABC_HITForce(Ctx& c) {   // hit.f90:224-254
+  const double pi = c.pi;
+  double C = c.S(MIBM_S_C_HIT) * ((2.0 * pi / c.xlen) * (2.0 * pi / c.xlen));
+  F3 &forcx = c.f[MIBM_F_FORCX], &forcy = c.f[MIBM_F_FORCY], &forcz = c.f[MIBM_F_FORCZ];
+  for (int k = 1; k <= c.n3m; ++k)
+    for (int j = 1; j <= c.n2m; ++j)
+      for (int i = 1; i <= c.n1m; ++i) {
+        forcx(i, j, k) = C * std::sin(2.0 * pi * c.zm(k) / c.zlen) + C * std::cos(2.0 * pi * c.ym(j) / c.ylen);
+        forcy(i, j, k) = C * std::sin(2.0 * pi * c.xm(i) / c.xlen) + C * std::cos(2.0 * pi * c.zm(k) / c.zlen);
+        forcz(i, j, k) = C * std::sin(2.0 * pi * c.ym(j) / c.ylen) + C * std::cos(2.0 * pi * c.xm(i) / c.xlen);
+      }
+}
+
+// linear forcing (library extension): forc = xlen * C_HIT * u
+void LinearHITForce(Ctx& c) {
+  double a = c.xlen * c.S(MIBM_S_C_HIT);
+  F3 &forcx = c.f[MIBM_F_FORCX], &forcy = c.f[MIBM_F_FORCY], &forcz = c.f[MIBM_F_FORCZ];
+  const F3 &vx = c.f[MIBM_F_VX], &vy = c.f[MIBM_F_VY], &vz = c.f[MIBM_F_VZ];
+  for (int k = 1; k <= c.n3m; ++k)
+    for (int j = 1; j <= c.n2m; ++j)
+      for (int i = 1; i <= c.n1m; ++i) {
+        forcx(i, j, k) = a * vx(i, j, k);
+        forcy(i, j, k) = a * vy(i, j, k);
+        forcz(i, j, k) = a * vz(i, j, k);
+      }
+}
+
 extern "C" {
 
 int mibm_context_create_(void) {
@@ -1726,6 +1869,19 @@ DROPIN(particle_, particle)
 DROPIN(cfl_, cfl)
 DROPIN(get_dt_, get_dt)
 DROPIN(tagcells_initial_, tagCells_initial)
+DROPIN(calchitrandomforce_, CalcHITRandomForce)
+DROPIN(calcabc_hitforce_, CalcABC_HITForce)
+DROPIN(mibm_linear_hit_force_, LinearHITForce)
+int mibm_hit_modes_(void) { Ctx* c = cur(); return ready(c) ? hit_modes_of(c->S(MIBM_S_KF_ON_KMIN)) : 0; }
+void mibm_hit_bhat_(double* bhat, const int* dir) {
+  Ctx* c = cur(); if (!ready(c)) return;
+  if (!bhat || (*dir != 0 && *dir != 1)) { fail(c, MIBM_EINVAL, "hit_bhat: dir 0 (get) or 1 (set)"); return; }
+  hit_state(*c);
+  for (size_t q = 0; q < c->hit_bhat.size(); ++q) {
+    if (*dir == 0) { bhat[2 * q] = c->hit_bhat[q].real(); bhat[2 * q + 1] = c->hit_bhat[q].imag(); }
+    else c->hit_bhat[q] = cd(bhat[2 * q], bhat[2 * q + 1]);
+  }
+}
 
 void solxi_(const double* betadx) { Ctx* c = cur(); if (ready(c)) solxi(*c, *betadx); }
 void solxj_(const double* betadx) { Ctx* c = cur(); if (ready(c)) solxj(*c, *betadx); }

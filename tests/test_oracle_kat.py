@@ -237,3 +237,95 @@ def test_oracle_golden_checksums(oracle_lib):
         assert abs(float(np.sqrt(np.sum(a * a))) - gold[name]["l2"]) <= 1e-12 * gold[name]["l2"]
     assert abs(c.S(abi.MIBM_S_DT) - gold["dt"]) <= 1e-15
     assert abs(c.S(abi.MIBM_S_VOLUME) - gold["volume"]) <= 1e-14
+
+
+# ---------------------------------------------------------------------------
+# HIT forcing (hit.f90): the oracle against a numpy restatement of the
+# documented random stream, the Ornstein-Uhlenbeck update, the solenoidal
+# projection and the DFT sums at the staggered positions
+# ---------------------------------------------------------------------------
+_M64 = (1 << 64) - 1
+
+
+def _splitmix_uniforms(seed, count):
+    state, out = seed & _M64, []
+    for _ in range(count):
+        state = (state + 0x9E3779B97F4A7C15) & _M64
+        z = state
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & _M64
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & _M64
+        z ^= z >> 31
+        out.append(((z >> 11) + 1) * 2.0 ** -53)
+    return out
+
+
+def _hit_numpy(case, nsteps, seed):
+    A = abi
+    L, n = case.xlen, case.n1m
+    kf_on_kmin, tl, eps, dt = (case.S(A.MIBM_S_KF_ON_KMIN), case.S(A.MIBM_S_TL), case.S(A.MIBM_S_EPSSTAR),
+                               case.S(A.MIBM_S_DT))
+    nb = int(np.floor(kf_on_kmin)) + 1
+    nm = 2 * (nb - 1) + 1
+    waven = np.arange(nm) - (nb - 1)
+    k = waven * 2.0 * np.pi / L
+    kf = kf_on_kmin * 2.0 * np.pi / L
+    modes = [(l, m, q) for l in range(nm) for m in range(nm) for q in range(nm)
+             if 0.0 < np.sqrt(k[l] ** 2 + k[m] ** 2 + k[q] ** 2) < kf]
+    u = iter(_splitmix_uniforms(seed, 6 * len(modes) * nsteps))
+    bhat = np.zeros((3, nm, nm, nm), dtype=complex)
+    for _ in range(nsteps):
+        fhat = np.zeros_like(bhat)
+        for (l, m, q) in modes:
+            for d in range(3):
+                u1, u2 = next(u), next(u)
+                r = np.sqrt(-2.0 * np.log(u1))
+                bhat[d, l, m, q] = bhat[d, l, m, q] * (1.0 - dt / tl) + \
+                    complex(r * np.cos(2 * np.pi * u2), r * np.sin(2 * np.pi * u2)) * np.sqrt(2.0 * eps * dt / tl ** 2)
+            kv = np.array([k[l], k[m], k[q]])
+            fhat[:, l, m, q] = bhat[:, l, m, q] - kv * (kv @ bhat[:, l, m, q]) / (kv @ kv)
+    xc = L * np.arange(n) / n
+    xm = xc + 0.5 * L / n
+    def field(c, xs, ys, zs):
+        ex, ey, ez = np.exp(1j * np.outer(k, xs)), np.exp(1j * np.outer(k, ys)), np.exp(1j * np.outer(k, zs))
+        return np.real(np.einsum("lmq,li,mj,qk->ijk", fhat[c], ex, ey, ez))
+    return bhat, [field(0, xc, xm, xm), field(1, xm, xc, xm), field(2, xm, xm, xc)]
+
+
+def test_hit_forcing_matches_numpy(oracle_lib):
+    case = Case(small_config(n=16, level=2, forcing=1, which_hit=1, hit_seed=11, kf_on_kmin=2.3))
+    case.attach(oracle_lib, initial_tag=False)
+    case.bind(oracle_lib)
+    for _ in range(3):
+        oracle_lib.calchitrandomforce_()
+        oracle_lib.check("hit")
+    nm = oracle_lib.mibm_hit_modes_()
+    assert nm == 5
+    got = np.zeros(2 * 3 * nm ** 3)
+    oracle_lib.mibm_hit_bhat_(got.ctypes.data, abi.ref_int(0))
+    bhat, forc = _hit_numpy(case, 3, 11)
+    want = np.stack([bhat.real, bhat.imag], axis=-1).transpose(4, 0, 1, 2, 3)   # (re/im, d, l, m, q)
+    got = got.reshape(nm, nm, nm, 3, 2)          # Fortran bhat(d,l,m,q): q slowest ... d, then re/im fastest
+    got = np.moveaxis(got, [4, 3, 2, 1, 0], [0, 1, 2, 3, 4])
+    assert np.allclose(got, want, rtol=1e-13, atol=1e-15)
+    for c, fid in enumerate((abi.MIBM_F_FORCX, abi.MIBM_F_FORCY, abi.MIBM_F_FORCZ)):
+        a = case.interior(fid)
+        assert np.max(np.abs(a - forc[c])) <= 1e-12 * max(1.0, np.max(np.abs(forc[c]))), fid
+    case.detach(oracle_lib)
+
+
+def test_abc_forcing_closed_form(oracle_lib):
+    case = Case(small_config(n=16, level=2, forcing=1, which_hit=2, c_hit=0.3))
+    case.attach(oracle_lib, initial_tag=False)
+    case.bind(oracle_lib)
+    oracle_lib.calcabc_hitforce_()
+    oracle_lib.check("abc")
+    L, n = case.xlen, case.n1m
+    xm = L * (np.arange(n) + 0.5) / n
+    C = 0.3 * (2 * np.pi / L) ** 2
+    X, Y, Z = np.meshgrid(xm, xm, xm, indexing="ij")
+    s, co = np.sin, np.cos
+    want = [C * s(2 * np.pi * Z / L) + C * co(2 * np.pi * Y / L), C * s(2 * np.pi * X / L) + C * co(2 * np.pi * Z / L),
+            C * s(2 * np.pi * Y / L) + C * co(2 * np.pi * X / L)]
+    for c, fid in enumerate((abi.MIBM_F_FORCX, abi.MIBM_F_FORCY, abi.MIBM_F_FORCZ)):
+        assert np.max(np.abs(case.interior(fid) - want[c])) <= 1e-14
+    case.detach(oracle_lib)
