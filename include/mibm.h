@@ -211,6 +211,12 @@ void interp_(double* arrold, double* arrnew, const int* n1o, const int* n2o,
  * terms, RHS, line solves and FFTs on FP64 fields, with the pressure
  * projection repeated `nproj` times on the FP64 divergence residual. */
 void mibm_set_precision_(const int* mode, const int* nproj);
+/* Step graphs (no counterpart in the reference): from its second call on,  */
+/* tschem_ captures its device work into a CUDA graph and replays it while */
+/* nothing it reads by value from the host changes (flags, constants, the */
+/* form, the mesh's launch sequence); on = 0 launches every kernel         */
+/* directly instead.  Results are identical either way.                    */
+void mibm_set_graphs_(const int* on);
 /* max over the owned cells of |div u| as divgck computes it
  * (divg.f90:26-56); synchronises with the device. */
 double mibm_divergence_max_(void);

@@ -92,28 +92,62 @@ void precision_after_upload(Ctx* c, unsigned long long mask) {
     if (mask & (1ull << kRuFields[q])) k_cast_d2f(c, c->g.cells, c->df[kRuFields[q]], c->ru32 + (size_t)q * c->g.cells);
 }
 
-// Precision form of tsch.f90:18-97: FP32 explicit terms, RHS, line solves
-// and FFTs; u, v, w, T, p stay FP64 and every FP32 kernel reads their FP32
-// mirrors.  The projection is repeated `nproj` times, each on the divergence
-// residual of the FP64 velocity (iterative refinement), so the final
-// divergence is at FP64 round-off.  MLS inversions, the Stefan front and the
-// geometry stay FP64.  Mirrors: T is written by the z solve and the
-// temperature forcing, u, v, w by the last velocity update, p by the last
-// pressure update of the substep.
-static void tschem_f32(Ctx* c, const double* gam, const double* rom, const double bd[3][2][3]) {
+static const double kGam[3] = {8.0 / 15.0, 5.0 / 12.0, 3.0 / 4.0};     // papero.f90:118-137
+static const double kRom[3] = {0.0, -17.0 / 60.0, -5.0 / 12.0};
+static const int kStepFid[4] = {MIBM_F_VX, MIBM_F_VY, MIBM_F_VZ, MIBM_F_TEMP};
+
+// tsch.f90:18-97 in three phases.  step_prepare (host): beta, the factor
+// tables of the 18 line solves (invtr*.f90 betadx) and the three substeps'
+// scalars, written to pinned buffers; buffers the form needs.  step_enqueue
+// (device, no host synchronisation): every copy and kernel of the step --
+// this is what a step graph captures.  step_finish (host): wait, then the
+// MLS / geometry checks.
+static bool step_prepare(Ctx* c) {
   const Grid& g = c->g;
-  if (!ensure_f32(c)) return;
+  *c->hs[MIBM_S_BETA] = c->S(MIBM_S_DT) / c->S(MIBM_S_REN) * 0.5;
+  double bd[3][2][3];
+  double dt = c->S(MIBM_S_DT), beta = c->S(MIBM_S_BETA), pec = c->S(MIBM_S_PEC);
+  const double dq[3] = {g.dx1q, g.dx2q, g.dx3q};
+  for (int ns = 0; ns < 3; ++ns) {
+    double al = kGam[ns] + kRom[ns];
+    for (int d = 0; d < 3; ++d) {
+      bd[ns][0][d] = beta * al * dq[d];
+      bd[ns][1][d] = dt / pec * 0.5 * al * dq[d];
+    }
+  }
+  bool f32 = c->precision == 1;
+  if (f32) {
+    if (!ensure_f32(c)) return false;
+  } else {
+    c->q32_valid = false;
+    if (!c->rhs4 && !cuda_ok(c, cudaMalloc(&c->rhs4, 4 * g.cells * sizeof(double)), "rhs4")) return false;
+  }
+  if (!tri_step_fill(c, bd, f32)) return false;
+  for (int ns = 0; ns < 3; ++ns) {
+    *c->hs[MIBM_S_AL] = kGam[ns] + kRom[ns];
+    *c->hs[MIBM_S_GA] = kGam[ns];
+    *c->hs[MIBM_S_RO] = kRom[ns];
+    c->hparams[ns] = host_params(c);
+  }
+  return c->status == MIBM_OK;
+}
+
+// Precision form: FP32 explicit terms, RHS, line solves and FFTs; u, v, w,
+// T, p stay FP64 and every FP32 kernel reads their FP32 mirrors.  The
+// projection is repeated `nproj` times, each on the divergence residual of
+// the FP64 velocity (iterative refinement), so the final divergence is at
+// FP64 round-off.  MLS inversions, the Stefan front and the geometry stay
+// FP64.  Mirrors: T is written by the z solve and the temperature forcing,
+// u, v, w by the last velocity update, p by the last pressure update of the
+// substep.
+static void step_enqueue_f32(Ctx* c) {
+  const Grid& g = c->g;
   int tlen = 0;
   const float* tf = nullptr;
-  if (!tri_step_prepare(c, bd, &tlen, &tf)) return;
-  static const int fid[4] = {MIBM_F_VX, MIBM_F_VY, MIBM_F_VZ, MIBM_F_TEMP};
+  if (!tri_step_enqueue(c, true, &tlen, &tf)) return;
   float* t_mirror = c->q32 + 3 * g.cells;
-  c->q32_valid = false;   // until the step has completed
   for (int ns = 0; ns < 3; ++ns) {
-    *c->hs[MIBM_S_AL] = gam[ns] + rom[ns];
-    *c->hs[MIBM_S_GA] = gam[ns];
-    *c->hs[MIBM_S_RO] = rom[ns];
-    const StepParams* dp = push_params(c, ns);
+    const StepParams* dp = c->dparams + ns;
     if (!c->I(MIBM_I_STATIONARY) && c->I(MIBM_I_IMLSFOR) == 1) lagr_tag_narrow_band(c);
     k_fused_rhs_f32(c, dp, c->ru32, c->rhs32);
     for (int q = 0; q < 4; ++q) {
@@ -122,7 +156,7 @@ static void tschem_f32(Ctx* c, const double* gam, const double* rom, const doubl
       float* r = c->rhs32 + (size_t)q * g.cells;
       k_solve_x_f32(c, r, T);
       k_solve_y_f32(c, r, T + tlen);
-      k_solve_z_f32(c, r, T + 2 * tlen, c->df[fid[q]], q == 3 ? t_mirror : nullptr);
+      k_solve_z_f32(c, r, T + 2 * tlen, c->df[kStepFid[q]], q == 3 ? t_mirror : nullptr);
     }
     const double* mean3 = lagr_particle_fused(c, dp, t_mirror);
     if (c->status != MIBM_OK) return;
@@ -135,43 +169,15 @@ static void tschem_f32(Ctx* c, const double* gam, const double* rom, const doubl
     }
     if (c->status != MIBM_OK) return;
   }
-  c->q32_valid = true;
-  lagr_step_finish(c);
 }
 
-// tsch.f90:18-97 on the device
-static void tschem(Ctx* c) {
-  static const double gam[3] = {8.0 / 15.0, 5.0 / 12.0, 3.0 / 4.0};
-  static const double rom[3] = {0.0, -17.0 / 60.0, -5.0 / 12.0};
+static void step_enqueue_f64(Ctx* c) {
   const Grid& g = c->g;
-  if (!c->rhs4) {
-    if (!cuda_ok(c, cudaMalloc(&c->rhs4, 4 * g.cells * sizeof(double)), "rhs4")) return;
-  }
-  *c->hs[MIBM_S_BETA] = c->S(MIBM_S_DT) / c->S(MIBM_S_REN) * 0.5;
-  static const int fid[4] = {MIBM_F_VX, MIBM_F_VY, MIBM_F_VZ, MIBM_F_TEMP};
-  // factor tables of all 18 line solves of the step (invtr*.f90 betadx)
-  double bd[3][2][3];
-  {
-    double dt = c->S(MIBM_S_DT), beta = c->S(MIBM_S_BETA), pec = c->S(MIBM_S_PEC);
-    const double dq[3] = {g.dx1q, g.dx2q, g.dx3q};
-    for (int ns = 0; ns < 3; ++ns) {
-      double al = gam[ns] + rom[ns];
-      for (int d = 0; d < 3; ++d) {
-        bd[ns][0][d] = beta * al * dq[d];
-        bd[ns][1][d] = dt / pec * 0.5 * al * dq[d];
-      }
-    }
-  }
-  if (c->precision == 1) { tschem_f32(c, gam, rom, bd); return; }
-  c->q32_valid = false;
   int tlen = 0;
-  const double* tables = tri_step_prepare(c, bd, &tlen, nullptr);
+  const double* tables = tri_step_enqueue(c, false, &tlen, nullptr);
   if (!tables) return;
   for (int ns = 0; ns < 3; ++ns) {
-    *c->hs[MIBM_S_AL] = gam[ns] + rom[ns];
-    *c->hs[MIBM_S_GA] = gam[ns];
-    *c->hs[MIBM_S_RO] = rom[ns];
-    const StepParams* dp = push_params(c, ns);
+    const StepParams* dp = c->dparams + ns;
     if (!c->I(MIBM_I_STATIONARY) && c->I(MIBM_I_IMLSFOR) == 1) lagr_tag_narrow_band(c);
     k_fused_rhs(c, dp);
     for (int q = 0; q < 4; ++q) {
@@ -180,7 +186,7 @@ static void tschem(Ctx* c) {
       double* r = c->rhs4 + (size_t)q * g.cells;
       k_solve_x_T(c, r, T);
       k_solve_y_T(c, r, T + tlen);
-      k_solve_z_T(c, r, T + 2 * tlen, c->df[fid[q]], 0);
+      k_solve_z_T(c, r, T + 2 * tlen, c->df[kStepFid[q]], 0);
     }
     const double* mean3 = lagr_particle_fused(c, dp, nullptr);
     if (c->status != MIBM_OK) return;
@@ -190,7 +196,107 @@ static void tschem(Ctx* c) {
     k_prcalc(c, dp);
     if (c->status != MIBM_OK) return;
   }
-  lagr_step_finish(c);
+}
+
+static void step_enqueue(Ctx* c) {
+  cudaMemcpyAsync(c->dparams, c->hparams, 3 * sizeof(StepParams), cudaMemcpyHostToDevice, c->stream);
+  if (c->precision == 1) step_enqueue_f32(c);
+  else step_enqueue_f64(c);
+  if (c->status == MIBM_OK) lagr_step_readback(c);
+}
+
+static void step_finish(Ctx* c) {
+  if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "tschem")) return;
+  if (c->status != MIBM_OK) return;
+  lagr_step_host_finish(c);
+  if (c->precision == 1 && c->status == MIBM_OK) c->q32_valid = true;
+  ++c->steps_done;
+}
+
+// Everything a step reads by value from the host besides the per-step
+// scalars (dt, al, ga, ro, beta, the rigid-body state: those go through the
+// pinned parameter block): the integer flags, the constant scalars passed to
+// kernels, the form, and the Lagrangian launch sequence generation.
+static uint64_t step_key(Ctx* c) {
+  uint64_t h = 1469598103934665603ull;
+  auto mix = [&](uint64_t v) { h ^= v; h *= 1099511628211ull; };
+  for (int i = 0; i < MIBM_NINTS; ++i)
+    if (i != MIBM_I_NTIME) mix((uint64_t)(uint32_t)c->I(i));
+  static const int per_step[] = {MIBM_S_DT, MIBM_S_AL, MIBM_S_GA, MIBM_S_RO, MIBM_S_BETA, MIBM_S_TIME,
+                                 MIBM_S_CFLM, MIBM_S_VOLUME, MIBM_S_SURFACE, MIBM_S_POS_CM, MIBM_S_VEL_CM,
+                                 MIBM_S_OMEGA_C, MIBM_S_DTMAX};
+  for (int i = 0; i < MIBM_NSCALARS; ++i) {
+    bool skip = false;
+    for (int p : per_step) skip |= (p == i);
+    if (skip) continue;
+    uint64_t b;
+    double v = c->S(i);
+    memcpy(&b, &v, 8);
+    mix(b);
+  }
+  mix((uint64_t)c->precision); mix((uint64_t)c->nproj); mix(c->lag_gen); mix(c->q32 ? 1 : 0);
+  return h;
+}
+
+static void drop_graph(Ctx* c) {
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  c->graph_exec = nullptr;
+  c->graph = nullptr;
+  c->graph_key = 0;
+}
+
+// Capture step_enqueue into a graph; false (and graphs off for this
+// context) if the capture or the instantiation fails.
+static bool capture_step(Ctx* c, uint64_t key) {
+  drop_graph(c);
+  uint64_t gen = c->lag_gen, before = c->launches;
+  if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+    cudaGetLastError();
+    c->use_graph = false;
+    return false;
+  }
+  step_enqueue(c);
+  cudaGraph_t gr = nullptr;
+  cudaError_t e = cudaStreamEndCapture(c->stream, &gr);
+  uint64_t kernels = c->launches - before;
+  c->launches = before;                         // counted again at every replay
+  if (e != cudaSuccess || !gr || c->status != MIBM_OK || gen != c->lag_gen) {
+    if (gr) cudaGraphDestroy(gr);
+    cudaGetLastError();
+    if (e != cudaSuccess) c->use_graph = false;
+    return false;
+  }
+  cudaGraphExec_t ex = nullptr;
+  if (cudaGraphInstantiate(&ex, gr, 0) != cudaSuccess) {
+    cudaGraphDestroy(gr);
+    cudaGetLastError();
+    c->use_graph = false;
+    return false;
+  }
+  c->graph = gr;
+  c->graph_exec = ex;
+  c->graph_key = key;
+  c->graph_kernels = kernels;
+  return true;
+}
+
+// tsch.f90:18-97 on the device.  From the second call on, the device part
+// runs as a captured graph (one launch per step) while its key holds.
+static void tschem(Ctx* c) {
+  if (!step_prepare(c)) return;
+  bool graph = c->use_graph && c->steps_done >= 1 && !c->profiling;
+  if (graph) {
+    uint64_t key = step_key(c);
+    if (!c->graph_exec || key != c->graph_key) graph = capture_step(c, key);
+  }
+  if (graph) {
+    if (!cuda_ok(c, cudaGraphLaunch(c->graph_exec, c->stream), "step graph")) return;
+    c->launches += c->graph_kernels;
+  } else {
+    step_enqueue(c);
+  }
+  step_finish(c);
 }
 
 }  // namespace mibm
@@ -287,6 +393,12 @@ void mibm_set_precision_(const int* mode, const int* nproj) {
   c->q32_valid = false;
   c->precision = *mode;
   c->nproj = *nproj;
+}
+
+void mibm_set_graphs_(const int* on) {
+  Ctx* c = current(); if (!ready(c)) return;
+  c->use_graph = *on != 0;
+  if (!c->use_graph) drop_graph(c);
 }
 
 // max over owned cells of |div u| (divgck, divg.f90:26-56); synchronises

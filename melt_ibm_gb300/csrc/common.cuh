@@ -129,9 +129,17 @@ struct Ctx {
   float* q32 = nullptr;
   bool q32_valid = false;
   unsigned long long* divmax = nullptr;   // device max|div u| (IEEE bits)
+  // captured step graph (tschem_ from its second call): replayed while the
+  // key of everything a step reads by value from the host is unchanged
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   bool use_graph = true;
+  uint64_t graph_key = 0;
+  uint64_t graph_kernels = 0;             // kernel launches recorded in the graph
+  uint64_t steps_done = 0;
+  uint64_t lag_gen = 0;                   // bumped when the Lagrangian launch sequence changes
+  bool profiling = false;                 // per-kernel event profiling on (no graphs then)
+  double* step_host = nullptr;            // pinned: geometry scalars read back at step end
   uint64_t launches = 0;                  // kernels launched through this context
   cudaEvent_t timers[64] = {nullptr};
 
@@ -249,7 +257,8 @@ void k_solve_z(Ctx* c, double* rhs, double betadx, double* q);
 void k_solve_x_T(Ctx* c, double* rhs, const double* T);
 void k_solve_y_T(Ctx* c, double* rhs, const double* T);
 void k_solve_z_T(Ctx* c, double* rhs, const double* T, double* q, int write_rhs);
-const double* tri_step_prepare(Ctx* c, const double betadx[3][2][3], int* len_out, const float** f32_out);
+bool tri_step_fill(Ctx* c, const double betadx[3][2][3], bool f32);
+const double* tri_step_enqueue(Ctx* c, bool f32, int* len_out, const float** f32_out);
 void k_solve_x_f32(Ctx* c, float* rhs, const float* T);
 void k_solve_y_f32(Ctx* c, float* rhs, const float* T);
 void k_solve_z_f32(Ctx* c, float* rhs, const float* T, double* q, float* mirror);
@@ -270,7 +279,8 @@ void lagr_tag_narrow_band(Ctx* c);
 void lagr_tag_initial(Ctx* c);
 void lagr_particle(Ctx* c, const StepParams* dp);
 const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror);
-void lagr_step_finish(Ctx* c);
+void lagr_step_readback(Ctx* c);
+void lagr_step_host_finish(Ctx* c);
 void lagr_geometry_to_host(Ctx* c);
 void lagr_invalidate(Ctx* c);
 void lagr_free(Ctx* c);

@@ -248,6 +248,7 @@ void release(Ctx* c) {
   cudaFree(c->tri_coef); cudaFree(c->lag_red);
   if (c->red_host) cudaFreeHost(c->red_host);
   if (c->hflag) cudaFreeHost(c->hflag);
+  if (c->step_host) cudaFreeHost(c->step_host);
   if (c->hparams) cudaFreeHost(c->hparams);
   for (int q = 0; q < 64; ++q)
     if (c->timers[q]) cudaEventDestroy(c->timers[q]);
@@ -384,6 +385,8 @@ void mibm_init_(void) {
   if (!cuda_ok(c, cudaMallocHost((void**)&c->red_host, 4096), "pinned")) return;
   if (!dev_alloc(c, (void**)&c->dflag, 64, "flags")) return;
   if (!cuda_ok(c, cudaMallocHost((void**)&c->hflag, 64), "pinned")) return;
+  if (!cuda_ok(c, cudaMallocHost((void**)&c->step_host, 16 * sizeof(double)), "pinned")) return;
+  c->hflag[0] = 0;
   for (int i = 0; i < MIBM_NMESH; ++i) {
     size_t b = mesh_bytes(c, i);
     if (b == 0) continue;

@@ -1343,6 +1343,7 @@ void lagr_invalidate(Ctx* c) {
   LagState* s = lag_of(c);
   s->force_rebuild = true;
   s->weights_valid = false;
+  ++c->lag_gen;
 }
 
 static bool ensure_adjacency(Ctx* c) {
@@ -1431,9 +1432,9 @@ static void update_plan(Ctx* c) {
   LagState* s = lag_of(c);
   int nf = c->maxnf, n = s->plan_n;
   if (s->force_rebuild) {
-    int one = 1;
-    cudaMemcpyAsync(s->dirty, &one, sizeof(int), cudaMemcpyHostToDevice, c->stream);
+    cudaMemsetAsync(s->dirty, 1, sizeof(int), c->stream);   // any non-zero value marks the plan dirty
     s->force_rebuild = false;
+    ++c->lag_gen;                                              // the next step has the other shape
   } else {
     cudaMemsetAsync(s->dirty, 0, sizeof(int), c->stream);
   }
@@ -1791,6 +1792,7 @@ const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror)
   if (!(stationary && s->weights_valid)) {
     mls_weight_launch(c);
     s->weights_valid = stationary;
+    if (stationary) ++c->lag_gen;     // later steps skip the weights: another launch sequence
   }
   force_coefficients(c);
   update_plan(c);
@@ -1813,11 +1815,32 @@ const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror)
   return s->mean3;
 }
 
-// end-of-step checks of the fused path: MLS flags, geometry scalars, volume
-void lagr_step_finish(Ctx* c) {
+// End of the fused step, in two halves so that the device half can sit in
+// a captured step graph: lagr_step_readback enqueues the copies of the MLS
+// flag and the geometry scalars into pinned host memory; after the stream
+// has completed, lagr_step_host_finish reads them (MLS failure status,
+// Surface, Volume, centre of mass, V_thresh abort of particle.f90:218-224).
+void lagr_step_readback(Ctx* c) {
   if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0) return;
-  if (!check_flag(c, "particle")) return;
-  lagr_geometry_to_host(c);
+  LagState* s = lag_of(c);
+  cudaMemcpyAsync(c->hflag, c->dflag, 4, cudaMemcpyDeviceToHost, c->stream);
+  if (s->geom_out) cudaMemcpyAsync(c->step_host, s->geom_out, sizeof(double) * 6, cudaMemcpyDeviceToHost, c->stream);
+}
+
+void lagr_step_host_finish(Ctx* c) {
+  if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0) return;
+  if (c->hflag[0]) {
+    fail(c, MIBM_ENUMERIC, "particle: singular MLS moment matrix (dgetrf info /= 0)");
+    c->hflag[0] = 0;
+    cudaMemsetAsync(c->dflag, 0, 4, c->stream);
+    return;
+  }
+  if (!lag_of(c)->geom_out) return;
+  *c->hs[MIBM_S_SURFACE] = c->step_host[0];
+  *c->hs[MIBM_S_VOLUME] = c->step_host[2];
+  c->hs[MIBM_S_POS_CM][0] = c->step_host[3];
+  c->hs[MIBM_S_POS_CM][1] = c->step_host[4];
+  c->hs[MIBM_S_POS_CM][2] = c->step_host[5];
   if (c->S(MIBM_S_VOLUME) < c->S(MIBM_S_V_THRESH)) fail(c, MIBM_EABORT, "Geometry V/VE smaller than threshold");
 }
 

@@ -89,6 +89,7 @@ void mibm_profile_(const int* on) {
   ProfState& s = g_prof[c];
   if (*on) { collect(c); s.table.clear(); s.on = true; }
   else { collect(c); s.on = false; }
+  c->profiling = s.on;
 }
 
 // Number of distinct kernel names recorded so far (collects pending events).

@@ -593,14 +593,16 @@ __global__ void __launch_bounds__(32 * col_max_chunks(M)) solve_cc_kernel(Grid g
 }
 
 // Tables of one fused RK3 step: [substep][velocity|temperature][x|y|z].
-// Built on the host once per step into one of two pinned buffers (the one
-// not read by the previous step's copy) and copied in stream order.
+// Built on the host into one pinned buffer (`tri_step_fill`) and copied in
+// stream order (`tri_step_enqueue`); the copy is part of a captured step
+// graph, so the buffer address is fixed.  The step ends with a stream
+// synchronisation (tschem_ reads the geometry back), so the host never
+// refills the buffer while a copy from it is pending.
 struct StepTables {
   double* dev = nullptr;
   float* devf = nullptr;                 // FP32 copy for the precision form
-  double* pinned[2] = {nullptr, nullptr};
-  cudaEvent_t copied[2] = {nullptr, nullptr};
-  int parity = 0, len = 0;
+  double* pinned = nullptr;              // 18 double tables, then 18 float tables
+  int len = 0;
 };
 static std::vector<std::pair<Ctx*, StepTables*>> g_steptab;
 
@@ -612,35 +614,39 @@ static StepTables* steptab_of(Ctx* c) {
   return t;
 }
 
-const double* tri_step_prepare(Ctx* c, const double betadx[3][2][3], int* len_out, const float** f32_out) {
+bool tri_step_fill(Ctx* c, const double betadx[3][2][3], bool f32) {
   StepTables* st = steptab_of(c);
   int nmax = std::max(c->g.n1m, c->g.n3m);
   if (!st->dev) {
     st->len = (int)slot_len(nmax);
     size_t bytes = sizeof(double) * 18 * (size_t)st->len;
-    if (!cuda_ok(c, cudaMalloc(&st->dev, bytes), "step tables")) return nullptr;
-    if (!cuda_ok(c, cudaMalloc(&st->devf, bytes / 2), "step tables")) return nullptr;
-    for (int q = 0; q < 2; ++q) {
-      if (!cuda_ok(c, cudaMallocHost(&st->pinned[q], bytes + bytes / 2), "step tables")) return nullptr;
-      if (!cuda_ok(c, cudaEventCreateWithFlags(&st->copied[q], cudaEventDisableTiming), "step tables")) return nullptr;
-    }
+    if (!cuda_ok(c, cudaMalloc(&st->dev, bytes), "step tables")) return false;
+    if (!cuda_ok(c, cudaMalloc(&st->devf, bytes / 2), "step tables")) return false;
+    if (!cuda_ok(c, cudaMallocHost(&st->pinned, bytes + bytes / 2), "step tables")) return false;
   }
-  int p = st->parity;
-  st->parity ^= 1;
-  cudaEventSynchronize(st->copied[p]);            // the copy that last read pinned[p]
   const int n[3] = {c->g.n1m, c->g.n2m, c->g.n3m};
   for (int ns = 0; ns < 3; ++ns)
     for (int f = 0; f < 2; ++f)
       for (int d = 0; d < 3; ++d)
-        fill_slot(n[d], betadx[ns][f][d], st->pinned[p] + (size_t)((ns * 2 + f) * 3 + d) * st->len);
-  cudaMemcpyAsync(st->dev, st->pinned[p], sizeof(double) * 18 * (size_t)st->len, cudaMemcpyHostToDevice, c->stream);
-  if (f32_out) {
-    float* hf = (float*)(st->pinned[p] + 18 * (size_t)st->len);
-    for (size_t q = 0; q < 18 * (size_t)st->len; ++q) hf[q] = (float)st->pinned[p][q];
-    cudaMemcpyAsync(st->devf, hf, sizeof(float) * 18 * (size_t)st->len, cudaMemcpyHostToDevice, c->stream);
-    *f32_out = st->devf;
+        fill_slot(n[d], betadx[ns][f][d], st->pinned + (size_t)((ns * 2 + f) * 3 + d) * st->len);
+  if (f32) {
+    float* hf = (float*)(st->pinned + 18 * (size_t)st->len);
+    for (size_t q = 0; q < 18 * (size_t)st->len; ++q) hf[q] = (float)st->pinned[q];
   }
-  cudaEventRecord(st->copied[p], c->stream);
+  return true;
+}
+
+// device tables of the step (FP64, and FP32 when f32) after tri_step_fill
+const double* tri_step_enqueue(Ctx* c, bool f32, int* len_out, const float** f32_out) {
+  StepTables* st = steptab_of(c);
+  if (!st->dev) return nullptr;
+  if (f32) {
+    float* hf = (float*)(st->pinned + 18 * (size_t)st->len);
+    cudaMemcpyAsync(st->devf, hf, sizeof(float) * 18 * (size_t)st->len, cudaMemcpyHostToDevice, c->stream);
+    if (f32_out) *f32_out = st->devf;
+  } else {
+    cudaMemcpyAsync(st->dev, st->pinned, sizeof(double) * 18 * (size_t)st->len, cudaMemcpyHostToDevice, c->stream);
+  }
   *len_out = st->len;
   return st->dev;
 }
@@ -651,10 +657,7 @@ static void steptab_free(Ctx* c) {
       StepTables* t = g_steptab[q].second;
       cudaFree(t->dev);
       cudaFree(t->devf);
-      for (int p = 0; p < 2; ++p) {
-        if (t->pinned[p]) cudaFreeHost(t->pinned[p]);
-        if (t->copied[p]) cudaEventDestroy(t->copied[p]);
-      }
+      if (t->pinned) cudaFreeHost(t->pinned);
       delete t;
       g_steptab.erase(g_steptab.begin() + q);
       return;

@@ -1772,6 +1772,7 @@ void mibm_timer_mark_(const int* slot) {
 double mibm_timer_ms_(const int* a, const int* b) { return g_marks[*b] - g_marks[*a]; }
 void mibm_profile_(const int*) {}
 void mibm_set_precision_(const int*, const int*) {}
+void mibm_set_graphs_(const int*) {}
 double mibm_divergence_max_(void) {
   Ctx* c = cur();
   if (!ready(c)) return -1.0;

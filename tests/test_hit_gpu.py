@@ -53,8 +53,9 @@ def test_bhat_round_trip(gpu_lib):
     gpu_lib.calchitrandomforce_()
     b = _bhat(c, gpu_lib)
     assert np.any(b != 0.0)
-    gpu_lib.mibm_hit_bhat_((2.0 * b).ctypes.data, abi.ref_int(1))
-    assert np.array_equal(_bhat(c, gpu_lib), 2.0 * b)
+    b2 = 2.0 * b                       # keep the array alive across the call
+    gpu_lib.mibm_hit_bhat_(b2.ctypes.data, abi.ref_int(1))
+    assert np.array_equal(_bhat(c, gpu_lib), b2)
     c.detach(gpu_lib)
 
 

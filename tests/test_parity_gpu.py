@@ -240,3 +240,30 @@ def test_gpu_determinism(gpu_lib):
         c.detach(gpu_lib)
     for k in FIELDS_OUT:
         assert np.array_equal(runs[0][k], runs[1][k]), k
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_step_graph_replay_is_bitwise_identical(gpu_lib, precision):
+    """From the second step on tschem_ replays a captured CUDA graph; the
+    result must equal launching every kernel directly, bit for bit."""
+    case = Case(small_config(n=32, level=3))
+    runs = []
+    for graphs in (0, 1):
+        c = case.clone()
+        c.attach(gpu_lib)
+        c.bind(gpu_lib)
+        gpu_lib.mibm_set_graphs_(C.byref(C.c_int(graphs)))
+        gpu_lib.mibm_set_precision_(C.byref(C.c_int(precision)), C.byref(C.c_int(2)))
+        gpu_lib.check("setup")
+        launches0 = gpu_lib.mibm_launch_count_()
+        c.run(gpu_lib, 4)
+        c.sync_to_host(gpu_lib, ALL)
+        runs.append(({k: c.interior(f).copy() for k, f in FIELDS_OUT.items()},
+                     c.mesh_arrays[A.MIBM_M_XYZV].copy(), c.S(A.MIBM_S_VOLUME),
+                     gpu_lib.mibm_launch_count_() - launches0))
+        c.detach(gpu_lib)
+    (f0, x0, v0, n0), (f1, x1, v1, n1) = runs
+    for k in FIELDS_OUT:
+        assert np.array_equal(f0[k], f1[k]), k
+    assert np.array_equal(x0, x1) and v0 == v1
+    assert n0 == n1            # the graph's kernels are counted at every replay
