@@ -217,6 +217,18 @@ void mibm_set_precision_(const int* mode, const int* nproj);
 /* form, the mesh's launch sequence); on = 0 launches every kernel         */
 /* directly instead.  Results are identical either way.                    */
 void mibm_set_graphs_(const int* on);
+/* Batched form (no counterpart in the reference, which runs one case per  */
+/* MPI job): independent cases -- each its own context after mibm_init_,   */
+/* any grid size, either form -- advanced by one iteration of the time     */
+/* loop (cfl, get_dt, forcing, tschem; gcurv.f90:151-172) together.  Their  */
+/* reductions overlap, their step graphs run as one batch graph (one child */
+/* node per case, no edges: the device interleaves them), and each case    */
+/* gets exactly the result of stepping it alone.  create returns a handle  */
+/* > 0 (0 on error); step returns a status; destroy the batch before its   */
+/* contexts.                                                               */
+int mibm_batch_create_(const int* ids, const int* n);
+int mibm_batch_step_(const int* handle, const int* ntime);
+int mibm_batch_destroy_(const int* handle);
 /* max over the owned cells of |div u| as divgck computes it
  * (divg.f90:26-56); synchronises with the device. */
 double mibm_divergence_max_(void);

@@ -11,6 +11,10 @@
 //     orders them (every invtr only advances its own component).
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
 
 #include "common.cuh"
 
@@ -299,6 +303,130 @@ static void tschem(Ctx* c) {
   step_finish(c);
 }
 
+// ---------------------------------------------------------------------
+// Batched form: many independent cases (contexts, any grid size, either
+// form) advanced by one reference time-loop iteration together
+// (gcurv.f90:151-172 for each case).  Per batch step: every case's CFL and
+// dt reductions are enqueued on its own stream and read back with one wait
+// per case; dt, forcing and the step's host preparation follow; then the
+// step graphs of all cases run as one batch graph (one child-graph node per
+// case, no edges between them, so the device overlaps the cases), or, for
+// cases without a graph yet, as direct launches on their own streams.  The
+// per-case host checks close the step.  Each case computes exactly what
+// stepping it alone computes.
+// ---------------------------------------------------------------------
+struct Batch {
+  std::vector<int> ids;
+  cudaStream_t stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<cudaGraphExec_t> built_from;   // the case graphs the batch graph holds
+};
+static std::mutex g_batch_mu;
+static std::map<int, Batch*> g_batch;
+static int g_batch_next = 1;
+
+static Batch* batch_of(int h) {
+  std::lock_guard<std::mutex> g(g_batch_mu);
+  auto it = g_batch.find(h);
+  return it == g_batch.end() ? nullptr : it->second;
+}
+
+static void batch_drop_graph(Batch* b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+  b->built_from.clear();
+}
+
+static int batch_step(Batch* b, int ntime) {
+  std::vector<Ctx*> cs;
+  for (int id : b->ids) {
+    Ctx* c = context_by_id(id);
+    if (!c || !ready(c)) { fail(c, MIBM_ESTATE, "batch: context " + std::to_string(id) + " is gone or not initialised"); return MIBM_ESTATE; }
+    if (c->status != MIBM_OK) return c->status;
+    cs.push_back(c);
+  }
+  // (A) CFL and dt reductions of every case, gcurv.f90:153-160
+  for (Ctx* c : cs) {
+    *c->hi[MIBM_I_NTIME] = ntime;
+    if (c->I(MIBM_I_IDTV) == 1 && ntime != 1) *c->hs[MIBM_S_DT] = c->S(MIBM_S_DTMAX);
+    k_cfl_async(c, c->red_host);
+    if (c->I(MIBM_I_IDTV) == 1) k_getdt_async(c, c->S(MIBM_S_DT), c->red_host + 1);
+  }
+  for (Ctx* c : cs) {
+    if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "batch cfl")) return c->status;
+    *c->hs[MIBM_S_CFLM] = cfl_value(c->red_host[0]);
+    if (c->I(MIBM_I_IDTV) == 1) {
+      double dt = c->S(MIBM_S_DT);
+      double buf = getdt_buffer(c->g, c->red_host[1], dt, c->S(MIBM_S_REN));
+      if (buf > 0.0) *c->hs[MIBM_S_DT] = dt * c->S(MIBM_S_CFLFIX) / buf;
+    }
+  }
+  // (B) forcing (gcurv.f90:164-170) and the host part of each step
+  for (Ctx* c : cs) {
+    if (c->I(MIBM_I_FORCING) == 1) {
+      int which = c->I(MIBM_I_WHICH_HIT);
+      if (which == 1) k_hit_random_force(c);
+      else if (which == 2) k_hit_abc_force(c);
+      else if (which == 3) k_hit_linear_force(c);
+    }
+    if (c->status != MIBM_OK || !step_prepare(c)) return c->status != MIBM_OK ? c->status : MIBM_ESTATE;
+  }
+  // (C) device work: step graphs (captured where missing or stale)
+  bool all_graphs = true;
+  for (Ctx* c : cs) {
+    bool graph = c->use_graph && c->steps_done >= 1 && !c->profiling;
+    if (graph) {
+      uint64_t key = step_key(c);
+      if (!c->graph_exec || key != c->graph_key) graph = capture_step(c, key);
+    }
+    all_graphs = all_graphs && graph;
+    if (c->status != MIBM_OK) return c->status;
+  }
+  if (all_graphs) {
+    std::vector<cudaGraphExec_t> now;
+    for (Ctx* c : cs) now.push_back(c->graph_exec);
+    if (!b->exec || now != b->built_from) {
+      batch_drop_graph(b);
+      bool ok = cudaGraphCreate(&b->graph, 0) == cudaSuccess;
+      for (size_t q = 0; ok && q < cs.size(); ++q) {
+        cudaGraphNode_t node;
+        ok = cudaGraphAddChildGraphNode(&node, b->graph, nullptr, 0, cs[q]->graph) == cudaSuccess;
+      }
+      ok = ok && cudaGraphInstantiate(&b->exec, b->graph, 0) == cudaSuccess;
+      if (!ok) { cudaGetLastError(); batch_drop_graph(b); all_graphs = false; }
+      else b->built_from = now;
+    }
+  }
+  if (all_graphs) {
+    for (Ctx* c : cs)   // forcing and buffer work enqueued on the case streams comes first
+      if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "batch")) return c->status;
+    if (!cuda_ok(cs[0], cudaGraphLaunch(b->exec, b->stream), "batch graph")) return cs[0]->status;
+    for (Ctx* c : cs) c->launches += c->graph_kernels;
+    if (!cuda_ok(cs[0], cudaStreamSynchronize(b->stream), "batch graph")) return cs[0]->status;
+  } else {
+    for (Ctx* c : cs) {
+      if (c->use_graph && c->graph_exec && c->steps_done >= 1 && !c->profiling) {
+        if (!cuda_ok(c, cudaGraphLaunch(c->graph_exec, c->stream), "step graph")) return c->status;
+        c->launches += c->graph_kernels;
+      } else {
+        step_enqueue(c);
+      }
+      if (c->status != MIBM_OK) return c->status;
+    }
+  }
+  // (D) per-case host checks, time
+  int st = MIBM_OK;
+  for (Ctx* c : cs) {
+    step_finish(c);
+    if (c->status != MIBM_OK && st == MIBM_OK) st = c->status;
+    *c->hs[MIBM_S_TIME] = c->S(MIBM_S_TIME) + c->S(MIBM_S_DT);
+  }
+  return st;
+}
+
 }  // namespace mibm
 
 using namespace mibm;
@@ -393,6 +521,54 @@ void mibm_set_precision_(const int* mode, const int* nproj) {
   c->q32_valid = false;
   c->precision = *mode;
   c->nproj = *nproj;
+}
+
+// Batched form (see Batch above).  ids: contexts after mibm_init_ (and the
+// initial tagging); returns a handle > 0, or 0 with the status in
+// mibm_last_status_.
+int mibm_batch_create_(const int* ids, const int* n) {
+  if (!ids || *n < 1) { fail(nullptr, MIBM_EINVAL, "batch_create: empty batch"); return 0; }
+  Batch* b = new Batch();
+  for (int q = 0; q < *n; ++q) {
+    Ctx* c = context_by_id(ids[q]);
+    if (!c || !ready(c)) { delete b; fail(nullptr, MIBM_EINVAL, "batch_create: context not initialised"); return 0; }
+    for (int id : b->ids)
+      if (id == ids[q]) { delete b; fail(nullptr, MIBM_EINVAL, "batch_create: context listed twice"); return 0; }
+    b->ids.push_back(ids[q]);
+  }
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    delete b;
+    fail(nullptr, MIBM_ECUDA, "batch_create: stream");
+    return 0;
+  }
+  std::lock_guard<std::mutex> g(g_batch_mu);
+  int h = g_batch_next++;
+  g_batch[h] = b;
+  return h;
+}
+
+// One iteration of the time loop (cfl, dt, forcing, tschem) for every case
+// of the batch; ntime as in gcurv.f90:151.  Returns a status.
+int mibm_batch_step_(const int* handle, const int* ntime) {
+  Batch* b = batch_of(*handle);
+  if (!b) { fail(nullptr, MIBM_EINVAL, "batch_step: unknown batch"); return MIBM_EINVAL; }
+  return batch_step(b, *ntime);
+}
+
+int mibm_batch_destroy_(const int* handle) {
+  Batch* b = nullptr;
+  {
+    std::lock_guard<std::mutex> g(g_batch_mu);
+    auto it = g_batch.find(*handle);
+    if (it == g_batch.end()) return MIBM_EINVAL;
+    b = it->second;
+    g_batch.erase(it);
+  }
+  batch_drop_graph(b);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return MIBM_OK;
 }
 
 void mibm_set_graphs_(const int* on) {

@@ -149,6 +149,7 @@ struct Ctx {
 
 Ctx* current();
 void fail(Ctx* c, int st, const std::string& m);
+Ctx* context_by_id(int id);
 bool cuda_ok(Ctx* c, cudaError_t e, const char* what);
 bool ready(Ctx* c);
 StepParams host_params(Ctx* c);
@@ -246,6 +247,10 @@ void k_updvp(Ctx* c, const StepParams* dp, const double* mean3 = nullptr);
 void k_prcalc(Ctx* c, const StepParams* dp);
 void k_add_field(Ctx* c, double* q, const double* r);
 double k_cfl(Ctx* c);
+void k_cfl_async(Ctx* c, double* out);
+void k_getdt_async(Ctx* c, double dt, double* out);
+double cfl_value(double reduced);
+double getdt_buffer(const Grid& g, double reduced, double dt, double ren);
 double k_get_dt_buffer(Ctx* c, double dt, double ren);
 void k_interp_vof(Ctx* c);
 void k_velforce_apply(Ctx* c, const double* mean3);

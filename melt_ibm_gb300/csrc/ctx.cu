@@ -28,6 +28,15 @@ Ctx* current() {
   return t_cur;
 }
 
+// registered context of an id, or null (also for destroyed contexts)
+Ctx* context_by_id(int id) {
+  std::lock_guard<std::mutex> g(g_mu);
+  auto it = g_ctx.find(id);
+  return it == g_ctx.end() ? nullptr : it->second;
+}
+
+int last_status_of_thread() { return t_status; }
+
 void fail(Ctx* c, int st, const std::string& m) {
   t_status = st; t_msg = m;
   if (c && c->status == MIBM_OK) { c->status = st; c->msg = m; }

@@ -692,7 +692,9 @@ static unsigned reduce_blocks(const Grid& g) {
   return (unsigned)std::min(want, (size_t)g.n2m * g.n3m);
 }
 
-double k_cfl(Ctx* c) {
+// CFL maximum (cfl.f90:11-26) reduced on the device and copied to the
+// pinned host slot `out`; read it after the stream has completed.
+void k_cfl_async(Ctx* c, double* out) {
   unsigned nb = reduce_blocks(c->g);
   bool f32 = c->precision == 1 && c->q32_valid;
   { MIBM_PROF(c, "cfl");
@@ -700,24 +702,39 @@ double k_cfl(Ctx* c) {
     else cfl_kernel<double><<<nb, 256, 0, c->stream>>>(make_args(c), c->pad_vx, c->pad_vy, c->red + kRedPart); }
   max_reduce_kernel<<<1, 1024, 0, c->stream>>>(c->red + kRedPart, nb, c->red + kRedOut);
   c->launches += 2;
-  cudaMemcpyAsync(c->red_host, c->red + kRedOut, 8, cudaMemcpyDeviceToHost, c->stream);
-  if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "cfl")) return 0.0;
-  // cfl.f90:448 starts the max at 1e-8
-  return fmax(0.00000001, c->red_host[0]);
+  cudaMemcpyAsync(out, c->red + kRedOut, 8, cudaMemcpyDeviceToHost, c->stream);
 }
 
-double k_get_dt_buffer(Ctx* c, double dt, double ren) {
+// get_dt advective maximum for time step dt (cfl.f90:33-77), as k_cfl_async
+void k_getdt_async(Ctx* c, double dt, double* out) {
   unsigned nb = reduce_blocks(c->g);
   bool f32 = c->precision == 1 && c->q32_valid;
   { MIBM_PROF(c, "getdt");
-    if (f32) getdt_kernel<float><<<nb, 256, 0, c->stream>>>(make_args(c), dt, c->red + kRedPart);
-    else getdt_kernel<double><<<nb, 256, 0, c->stream>>>(make_args(c), dt, c->red + kRedPart); }
-  max_reduce_kernel<<<1, 1024, 0, c->stream>>>(c->red + kRedPart, nb, c->red + kRedOut);
+    if (f32) getdt_kernel<float><<<nb, 256, 0, c->stream>>>(make_args(c), dt, c->red + kRedPart + c->red_elems / 2);
+    else getdt_kernel<double><<<nb, 256, 0, c->stream>>>(make_args(c), dt, c->red + kRedPart + c->red_elems / 2); }
+  max_reduce_kernel<<<1, 1024, 0, c->stream>>>(c->red + kRedPart + c->red_elems / 2, nb, c->red + kRedOut + 1);
   c->launches += 2;
-  cudaMemcpyAsync(c->red_host, c->red + kRedOut, 8, cudaMemcpyDeviceToHost, c->stream);
+  cudaMemcpyAsync(out, c->red + kRedOut + 1, 8, cudaMemcpyDeviceToHost, c->stream);
+}
+
+// cfl.f90:448 starts the max at 1e-8
+double cfl_value(double reduced) { return fmax(0.00000001, reduced); }
+
+// viscous restriction 6/ren*dt*dx1**2 (cfl.f90:499), the same for every cell
+double getdt_buffer(const Grid& g, double reduced, double dt, double ren) {
+  return fmax(reduced, 6.0 / ren * dt * (g.dx1 * g.dx1));
+}
+
+double k_cfl(Ctx* c) {
+  k_cfl_async(c, c->red_host);
+  if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "cfl")) return 0.0;
+  return cfl_value(c->red_host[0]);
+}
+
+double k_get_dt_buffer(Ctx* c, double dt, double ren) {
+  k_getdt_async(c, dt, c->red_host + 1);
   if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "get_dt")) return 0.0;
-  // viscous restriction 6/ren*dt*dx1**2 (cfl.f90:499), the same for every cell
-  return fmax(c->red_host[0], 6.0 / ren * dt * (c->g.dx1 * c->g.dx1));
+  return getdt_buffer(c->g, c->red_host[1], dt, ren);
 }
 
 }  // namespace mibm

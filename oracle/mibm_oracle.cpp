@@ -1773,6 +1773,41 @@ double mibm_timer_ms_(const int* a, const int* b) { return g_marks[*b] - g_marks
 void mibm_profile_(const int*) {}
 void mibm_set_precision_(const int*, const int*) {}
 void mibm_set_graphs_(const int*) {}
+// the oracle runs cases one after another: a batch is its list of contexts
+static std::map<int, std::vector<int>> g_obatch;
+static int g_obatch_next = 1;
+int mibm_batch_create_(const int* ids, const int* n) {
+  if (!ids || *n < 1) return 0;
+  int h = g_obatch_next++;
+  g_obatch[h] = std::vector<int>(ids, ids + *n);
+  return h;
+}
+int mibm_batch_step_(const int* handle, const int* ntime) {
+  auto it = g_obatch.find(*handle);
+  if (it == g_obatch.end()) return MIBM_EINVAL;
+  for (int id : it->second) {
+    if (mibm_context_bind_(&id) != MIBM_OK) return MIBM_EINVAL;
+    Ctx* c = cur();
+    if (!ready(c)) return MIBM_ESTATE;
+    c->I(MIBM_I_NTIME) = *ntime;
+    cfl(*c);
+    if (c->I(MIBM_I_IDTV) == 1) {
+      if (*ntime != 1) c->S(MIBM_S_DT) = c->S(MIBM_S_DTMAX);
+      get_dt(*c);
+    }
+    if (c->I(MIBM_I_FORCING) == 1) {
+      int which = c->I(MIBM_I_WHICH_HIT);
+      if (which == 1) CalcHITRandomForce(*c);
+      else if (which == 2) CalcABC_HITForce(*c);
+      else if (which == 3) LinearHITForce(*c);
+    }
+    tschem(*c);
+    if (c->status != MIBM_OK) return c->status;
+    c->S(MIBM_S_TIME) = c->S(MIBM_S_TIME) + c->S(MIBM_S_DT);
+  }
+  return MIBM_OK;
+}
+int mibm_batch_destroy_(const int* handle) { return g_obatch.erase(*handle) ? MIBM_OK : MIBM_EINVAL; }
 double mibm_divergence_max_(void) {
   Ctx* c = cur();
   if (!ready(c)) return -1.0;
