@@ -226,6 +226,16 @@ void mibm_set_graphs_(const int* on);
 /* gets exactly the result of stepping it alone.  create returns a handle  */
 /* > 0 (0 on error); step returns a status; destroy the batch before its   */
 /* contexts.                                                               */
+/* Autotuner (no counterpart in the reference): times the feasible chunk    */
+/* lengths of the x-, y- and z-line solves and the block heights of the    */
+/* explicit-term kernel on the bound context (scratch data; its state is   */
+/* unchanged) and keeps the fastest; results are cached per (grid, form)   */
+/* for the process and can be saved to / loaded from a text file.  get     */
+/* writes the chunk lengths (x, y, z) and block height in use to out[0..3]. */
+int  mibm_autotune_(void);
+int  mibm_autotune_get_(int* out);
+int  mibm_autotune_save_(const char* path);
+int  mibm_autotune_load_(const char* path);
 int mibm_batch_create_(const int* ids, const int* n);
 int mibm_batch_step_(const int* handle, const int* ntime);
 int mibm_batch_destroy_(const int* handle);

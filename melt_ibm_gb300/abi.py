@@ -69,6 +69,10 @@ SIGNATURES: dict[str, tuple] = {
     "mibm_solxi_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_void_p]),
     "mibm_set_precision_": (None, [_I, _I]),
     "mibm_set_graphs_": (None, [_I]),
+    "mibm_autotune_": (C.c_int, []),
+    "mibm_autotune_get_": (C.c_int, [C.c_void_p]),
+    "mibm_autotune_save_": (C.c_int, [C.c_char_p]),
+    "mibm_autotune_load_": (C.c_int, [C.c_char_p]),
     "mibm_batch_create_": (C.c_int, [C.c_void_p, _I]),
     "mibm_batch_step_": (C.c_int, [_I, _I]),
     "mibm_batch_destroy_": (C.c_int, [_I]),

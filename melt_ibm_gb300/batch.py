@@ -18,9 +18,15 @@ from .case import Case
 
 
 class BatchRunner:
-    def __init__(self, lib: abi.Lib, cases: list[Case]):
+    def __init__(self, lib: abi.Lib, cases: list[Case], autotune: bool = False):
         self.lib = lib
         self.cases = list(cases)
+        if autotune:                  # shapes per (grid, form); repeated shapes hit the cache
+            for c in self.cases:
+                c.bind(lib)
+                st = int(lib.mibm_autotune_())
+                if st != 0:
+                    raise RuntimeError(f"mibm_autotune_ failed ({st}): {lib.mibm_last_message().decode()}")
         ids = np.array([c.ctx[lib.path] for c in self.cases], dtype=np.int32)
         self._ids = ids
         self.handle = int(lib.mibm_batch_create_(ids.ctypes.data, abi.ref_int(len(ids))))

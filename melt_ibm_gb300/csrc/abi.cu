@@ -239,6 +239,7 @@ static uint64_t step_key(Ctx* c) {
     mix(b);
   }
   mix((uint64_t)c->precision); mix((uint64_t)c->nproj); mix(c->lag_gen); mix(c->q32 ? 1 : 0);
+  mix(c->tune_gen);
   return h;
 }
 
@@ -301,6 +302,72 @@ static void tschem(Ctx* c) {
     step_enqueue(c);
   }
   step_finish(c);
+}
+
+// ---------------------------------------------------------------------
+// Autotuner.  Per shape (grid n1m x n2m x n3m, form) it times, with CUDA
+// events on the case's own stream, every feasible chunk length of the x-,
+// y- and z-line solves (scratch lines) and the block heights 2, 4, 8 of the
+// explicit-term kernel (RK history saved and restored), and keeps the
+// fastest of each.  Results live in a process-wide table, so every later
+// case of the same shape reuses them, and can be saved to / loaded from a
+// text file.  A context picks them up by mibm_autotune_; its step graph is
+// re-captured (the tuning generation is part of the step key).
+// ---------------------------------------------------------------------
+struct TuneResult {
+  int m[3] = {0, 0, 0};
+  int by = 8;
+  float ms_m[3] = {0, 0, 0};
+  float ms_by = 0;
+};
+static std::mutex g_tune_mu;
+static std::map<std::vector<int>, TuneResult> g_tune;
+
+static std::vector<int> tune_key(Ctx* c) { return {c->g.n1m, c->g.n2m, c->g.n3m, c->precision}; }
+
+static void tune_apply(Ctx* c, const TuneResult& r) {
+  for (int d = 0; d < 3; ++d) c->tune_m[d] = r.m[d];
+  c->tune_by = r.by;
+  ++c->tune_gen;
+}
+
+static int autotune(Ctx* c) {
+  {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    auto it = g_tune.find(tune_key(c));
+    if (it != g_tune.end()) { tune_apply(c, it->second); return MIBM_OK; }
+  }
+  // the form's buffers and parameters must exist for the explicit-term timing
+  if (!step_prepare(c)) return c->status;
+  cudaMemcpyAsync(c->dparams, c->hparams, 3 * sizeof(StepParams), cudaMemcpyHostToDevice, c->stream);
+  const bool f32 = c->precision == 1;
+  TuneResult r;
+  for (int d = 0; d < 3; ++d) {
+    std::vector<int> cand = tri_chunk_candidates(c, d);
+    r.m[d] = tri_chunk(c, d);
+    r.ms_m[d] = -1.f;
+    for (int m : cand) {
+      float ms = tri_time_direction(c, d, m, f32, 5);
+      if (c->status != MIBM_OK) return c->status;
+      if (ms >= 0.f && (r.ms_m[d] < 0.f || ms < r.ms_m[d])) { r.ms_m[d] = ms; r.m[d] = m; }
+    }
+  }
+  r.ms_by = -1.f;
+  for (int by : {2, 4, 8}) {
+    float ms = stencil_time_by(c, c->dparams, by, 5);
+    if (c->status != MIBM_OK) return c->status;
+    if (ms >= 0.f && (r.ms_by < 0.f || ms < r.ms_by)) { r.ms_by = ms; r.by = by; }
+  }
+  {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    g_tune[tune_key(c)] = r;
+  }
+  tune_apply(c, r);
+  // the preparation above built the FP32 mirrors ahead of the case's first
+  // step; leave them stale so that the case's own sequence (CFL of step 1
+  // from the FP64 fields) is exactly that of an untuned case
+  c->q32_valid = false;
+  return MIBM_OK;
 }
 
 // ---------------------------------------------------------------------
@@ -568,6 +635,51 @@ int mibm_batch_destroy_(const int* handle) {
   batch_drop_graph(b);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
+  return MIBM_OK;
+}
+
+// Autotune the bound context's shapes (cached per grid and form); returns a
+// status.  get: out[0..3] = x, y, z chunk lengths and the block height in
+// use.  save / load: the process-wide table as text, one shape per line.
+int mibm_autotune_(void) {
+  Ctx* c = current(); if (!ready(c)) return MIBM_ESTATE;
+  return autotune(c);
+}
+
+int mibm_autotune_get_(int* out) {
+  Ctx* c = current(); if (!ready(c)) return MIBM_ESTATE;
+  for (int d = 0; d < 3; ++d) out[d] = tri_chunk(c, d);
+  out[3] = c->tune_by;
+  return MIBM_OK;
+}
+
+int mibm_autotune_save_(const char* path) {
+  FILE* f = fopen(path, "w");
+  if (!f) return MIBM_EINVAL;
+  std::lock_guard<std::mutex> g(g_tune_mu);
+  fprintf(f, "# n1m n2m n3m form  m_x m_y m_z by  ms_x ms_y ms_z ms_by\n");
+  for (auto& e : g_tune)
+    fprintf(f, "%d %d %d %d  %d %d %d %d  %.5f %.5f %.5f %.5f\n", e.first[0], e.first[1], e.first[2], e.first[3],
+            e.second.m[0], e.second.m[1], e.second.m[2], e.second.by, e.second.ms_m[0], e.second.ms_m[1],
+            e.second.ms_m[2], e.second.ms_by);
+  fclose(f);
+  return MIBM_OK;
+}
+
+int mibm_autotune_load_(const char* path) {
+  FILE* f = fopen(path, "r");
+  if (!f) return MIBM_EINVAL;
+  char line[512];
+  std::lock_guard<std::mutex> g(g_tune_mu);
+  while (fgets(line, sizeof(line), f)) {
+    if (line[0] == '#') continue;
+    int k[4];
+    TuneResult r;
+    if (sscanf(line, "%d %d %d %d %d %d %d %d %f %f %f %f", &k[0], &k[1], &k[2], &k[3], &r.m[0], &r.m[1], &r.m[2],
+               &r.by, &r.ms_m[0], &r.ms_m[1], &r.ms_m[2], &r.ms_by) == 12)
+      g_tune[{k[0], k[1], k[2], k[3]}] = r;
+  }
+  fclose(f);
   return MIBM_OK;
 }
 

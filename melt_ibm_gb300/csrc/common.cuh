@@ -139,6 +139,10 @@ struct Ctx {
   uint64_t steps_done = 0;
   uint64_t lag_gen = 0;                   // bumped when the Lagrangian launch sequence changes
   bool profiling = false;                 // per-kernel event profiling on (no graphs then)
+  // shapes chosen by the autotuner (tune.cu); -1 / 8 = the default rules
+  int tune_m[3] = {-1, -1, -1};           // line-solve chunk length per direction
+  int tune_by = 8;                        // block height of the explicit-term kernel
+  uint64_t tune_gen = 0;
   double* step_host = nullptr;            // pinned: geometry scalars read back at step end
   uint64_t launches = 0;                  // kernels launched through this context
   cudaEvent_t timers[64] = {nullptr};
@@ -232,6 +236,11 @@ void k_hit_linear_force(Ctx* c);
 int hit_modes(Ctx* c);
 void hit_bhat(Ctx* c, double* buf, int dir);
 void hit_free(Ctx* c);
+// autotuner support (tridiag.cu, stencil.cu)
+float tri_time_direction(Ctx* c, int dir, int m, bool f32, int reps);
+std::vector<int> tri_chunk_candidates(Ctx* c, int dir);
+int tri_chunk(Ctx* c, int dir);
+float stencil_time_by(Ctx* c, const StepParams* dp, int by, int reps);
 // restart regrid (interp.cu): host arrays in, host array out
 void k_interp_restart(Ctx* c, double* arrold, double* arrnew, int n1o, int n2o, int n3o, int intvar, int kstarto,
                       int kendo);

@@ -277,7 +277,8 @@ fused_rhs_kernel(StencilArgs A, const StepParams* __restrict__ pp, R* __restrict
 
 template <typename R>
 static void fused_rhs_launch(Ctx* c, const StepParams* dp, int w, R* ru, R* rhs) {
-  dim3 grid(div_up(c->g.n1m, 32), div_up(c->g.n2m, 8), c->g.n3m), block(32, 8);
+  const int by = (c->tune_by == 2 || c->tune_by == 4) ? c->tune_by : 8;   // autotuned block height
+  dim3 grid(div_up(c->g.n1m, 32), div_up(c->g.n2m, by), c->g.n3m), block(32, by);
   StencilArgs a = make_args(c);
   switch (w) {
     case 0: fused_rhs_kernel<R, 0><<<grid, block, 0, c->stream>>>(a, dp, ru, rhs); break;
@@ -569,6 +570,59 @@ void k_fused_rhs(Ctx* c, const StepParams* dp) {
     ++c->launches;
   }
   MIBM_LAUNCH_CHECK(c, "fused_rhs");
+}
+
+// Autotuner support: time the explicit-term kernel (components u and T) with
+// block height `by`, best of `reps` runs after one warm-up, in ms.  The RK
+// history it overwrites is saved first and restored, so the context's state
+// is unchanged.  ru4/rhs4: the form's history and RHS buffers.
+template <typename R>
+static float time_fused_by(Ctx* c, const StepParams* dp, int by, int reps, R* ru4, R* rhs4, R* const* ru_fields) {
+  const size_t n = c->g.cells;
+  R* save = nullptr;
+  if (!cuda_ok(c, cudaMalloc(&save, 4 * n * sizeof(R)), "tune")) return -1.f;
+  for (int w = 0; w < 4; ++w)
+    cudaMemcpyAsync(save + (size_t)w * n, ru_fields[w], n * sizeof(R), cudaMemcpyDeviceToDevice, c->stream);
+  const int old = c->tune_by;
+  c->tune_by = by;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  auto run = [&]() {
+    fused_rhs_launch<R>(c, dp, 0, ru_fields[0], rhs4);
+    fused_rhs_launch<R>(c, dp, 3, ru_fields[3], rhs4 + 3 * n);
+  };
+  float best = -1.f;
+  run();
+  for (int r = 0; r < reps; ++r) {
+    cudaEventRecord(e0, c->stream);
+    run();
+    cudaEventRecord(e1, c->stream);
+    if (!cuda_ok(c, cudaEventSynchronize(e1), "tune")) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (best < 0.f || ms < best) best = ms;
+  }
+  for (int w = 0; w < 4; ++w)
+    cudaMemcpyAsync(ru_fields[w], save + (size_t)w * n, n * sizeof(R), cudaMemcpyDeviceToDevice, c->stream);
+  cudaStreamSynchronize(c->stream);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(save);
+  c->tune_by = old;
+  (void)ru4;
+  return best;
+}
+
+float stencil_time_by(Ctx* c, const StepParams* dp, int by, int reps) {
+  if (c->precision == 1) {
+    float* ru[4];
+    for (int w = 0; w < 4; ++w) ru[w] = c->ru32 + (size_t)w * c->g.cells;
+    return time_fused_by<float>(c, dp, by, reps, c->ru32, c->rhs32, ru);
+  }
+  double* ru[4];
+  for (int w = 0; w < 4; ++w) ru[w] = ru_of(c, w);
+  return time_fused_by<double>(c, dp, by, reps, nullptr, c->rhs4, ru);
 }
 
 // precision form: FP32 explicit terms and RHS into FP32 ru / rhs buffers

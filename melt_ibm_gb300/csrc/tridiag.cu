@@ -78,14 +78,15 @@ static void build_table(int n, double betadx, std::vector<double>& t) {
 }
 
 static size_t slot_len(int nmax);
-static void fill_slot(int n, double betadx, double* out);
+static void fill_slot(int n, int m, double betadx, double* out);
+int tri_chunk(Ctx* c, int dir);
 
 // Device table cache: small ring of slots, refilled when (n, betadx) changes.
 struct TriCache {
   double* dev = nullptr;
   double* pinned = nullptr;
   int slots = 0, len = 0, next = 0;
-  std::vector<int> n;
+  std::vector<int> n, m;
   std::vector<double> bd;
 };
 
@@ -106,7 +107,9 @@ static CtxTri* tri_of(Ctx* c) {
 // Returns a device pointer to the table of (n, betadx).  The table is
 // written to a pinned slot and copied on the context stream, so the value is
 // stream-ordered with the solve that uses it.
-static const double* table_for(Ctx* c, int n, double betadx) {
+static const double* table_for(Ctx* c, int dir, double betadx) {
+  const int n = dir == 0 ? c->g.n1m : (dir == 1 ? c->g.n2m : c->g.n3m);
+  const int m = tri_chunk(c, dir);
   TriCache& tc = tri_of(c)->cache;
   int nmax = std::max(c->g.n1m, c->g.n3m);
   if (!tc.dev) {
@@ -115,18 +118,20 @@ static const double* table_for(Ctx* c, int n, double betadx) {
     if (!cuda_ok(c, cudaMalloc(&tc.dev, sizeof(double) * tc.len * tc.slots), "tri table")) return nullptr;
     if (!cuda_ok(c, cudaMallocHost(&tc.pinned, sizeof(double) * tc.len * tc.slots), "tri table")) return nullptr;
     tc.n.assign(tc.slots, -1);
+    tc.m.assign(tc.slots, -1);
     tc.bd.assign(tc.slots, -1.0);
   }
   for (int s = 0; s < tc.slots; ++s)
-    if (tc.n[s] == n && tc.bd[s] == betadx) return tc.dev + (size_t)s * tc.len;
+    if (tc.n[s] == n && tc.m[s] == m && tc.bd[s] == betadx) return tc.dev + (size_t)s * tc.len;
   int s = tc.next;
   tc.next = (tc.next + 1) % tc.slots;
   // a slot may still be read by an in-flight kernel: order the refill on the stream
   cudaStreamSynchronize(c->stream);
-  fill_slot(n, betadx, tc.pinned + (size_t)s * tc.len);
+  fill_slot(n, m, betadx, tc.pinned + (size_t)s * tc.len);
   cudaMemcpyAsync(tc.dev + (size_t)s * tc.len, tc.pinned + (size_t)s * tc.len, sizeof(double) * tc.len,
                   cudaMemcpyHostToDevice, c->stream);
   tc.n[s] = n;
+  tc.m[s] = m;
   tc.bd[s] = betadx;
   return tc.dev + (size_t)s * tc.len;
 }
@@ -376,39 +381,56 @@ static void build_ext(const std::vector<double>& t, int n, int m, double* out) {
   for (int w = 0; w < 4; ++w) out[7 * (size_t)n + 3 * G + w] = t[4 * (size_t)n + w];
 }
 
-// one table slot: base table (tile kernels), extended table for x-lines,
-// extended table for y/z-lines
+// one table slot: base table (tile kernels) and the extended table of the
+// chunk length M chosen for the direction the slot serves (0 = none)
 struct TriLayout {
-  int n, m_line, m_col;
-  size_t off_line, off_col, len;
+  int n, m;
+  size_t off_ext, len;
 };
 
-static TriLayout tri_layout(int n) {
+static TriLayout tri_layout(int n, int m) {
   TriLayout L;
   L.n = n;
-  L.m_line = tri_chunk_line(n);
-  L.m_col = tri_chunk_col(n);
-  L.off_line = 4 * (size_t)n + 4;
-  L.off_col = L.off_line + ext_len(n, L.m_line);
-  L.len = L.off_col + ext_len(n, L.m_col);
+  L.m = m;
+  L.off_ext = 4 * (size_t)n + 4;
+  L.len = L.off_ext + ext_len(n, m);
   return L;
 }
 
-// fills one slot (base + both extended tables) for (n, betadx)
-static void fill_slot(int n, double betadx, double* out) {
-  std::vector<double> t;
-  build_table(n, betadx, t);
-  TriLayout L = tri_layout(n);
-  std::copy(t.begin(), t.end(), out);
-  if (L.m_line) build_ext(t, n, L.m_line, out + L.off_line);
-  if (L.m_col) build_ext(t, n, L.m_col, out + L.off_col);
+static bool chunk_feasible(int n, int m, bool line) {
+  if (!chunk_ok(m) || n % m != 0) return false;
+  return line ? n / m <= 32 : n / m <= col_max_chunks(m);
 }
 
-static size_t slot_len(int nmax) {
-  size_t len = 0;
-  for (int n = 1; n <= nmax; ++n) len = std::max(len, tri_layout(n).len);
-  return len;
+// chunk length of direction dir (0 x, 1 y, 2 z) for context c: the
+// autotuner's choice when one is set and feasible, else the default rule
+int tri_chunk(Ctx* c, int dir) {
+  const int n = dir == 0 ? c->g.n1m : (dir == 1 ? c->g.n2m : c->g.n3m);
+  int m = c->tune_m[dir];
+  if (m > 0 && chunk_feasible(n, m, dir == 0)) return m;
+  return dir == 0 ? tri_chunk_line(n) : tri_chunk_col(n);
 }
+
+// candidate chunk lengths of direction dir (for the autotuner)
+std::vector<int> tri_chunk_candidates(Ctx* c, int dir) {
+  const int n = dir == 0 ? c->g.n1m : (dir == 1 ? c->g.n2m : c->g.n3m);
+  std::vector<int> out;
+  for (int m : kChunkM)
+    if (chunk_feasible(n, m, dir == 0)) out.push_back(m);
+  return out;
+}
+
+// fills one slot (base + the extended table of chunk m) for (n, betadx)
+static void fill_slot(int n, int m, double betadx, double* out) {
+  std::vector<double> t;
+  build_table(n, betadx, t);
+  TriLayout L = tri_layout(n, m);
+  std::copy(t.begin(), t.end(), out);
+  if (m) build_ext(t, n, m, out + L.off_ext);
+}
+
+// slot length for lines up to nmax and any chunk (ext_len <= 7n + 3*32 + 4)
+static size_t slot_len(int nmax) { return 4 * (size_t)nmax + 4 + 7 * (size_t)nmax + 3 * 32 + 4; }
 
 template <typename V, int M>
 __device__ __forceinline__ void load_chunk(const V* __restrict__ p, V (&r)[M]) {
@@ -628,7 +650,7 @@ bool tri_step_fill(Ctx* c, const double betadx[3][2][3], bool f32) {
   for (int ns = 0; ns < 3; ++ns)
     for (int f = 0; f < 2; ++f)
       for (int d = 0; d < 3; ++d)
-        fill_slot(n[d], betadx[ns][f][d], st->pinned + (size_t)((ns * 2 + f) * 3 + d) * st->len);
+        fill_slot(n[d], tri_chunk(c, d), betadx[ns][f][d], st->pinned + (size_t)((ns * 2 + f) * 3 + d) * st->len);
   if (f32) {
     float* hf = (float*)(st->pinned + 18 * (size_t)st->len);
     for (size_t q = 0; q < 18 * (size_t)st->len; ++q) hf[q] = (float)st->pinned[q];
@@ -683,14 +705,14 @@ static bool smem_ok(Ctx* c, const void* fn, size_t bytes) {
 
 template <typename V>
 static bool solve_xc_launch(Ctx* c, V* rhs, const V* T, const char* name) {
-  TriLayout L = tri_layout(c->g.n1m);
-  if (!L.m_line) return false;
-  const V* X = T + L.off_line;
+  TriLayout L = tri_layout(c->g.n1m, tri_chunk(c, 0));
+  if (!L.m) return false;
+  const V* X = T + L.off_ext;
   dim3 grid(div_up((size_t)c->g.n2m * c->g.n3m, 8));
   {
     MIBM_PROF(c, name);
 #define XC(M) solve_xc_kernel<V, M><<<grid, 256, 0, c->stream>>>(c->g, rhs, X)
-    MIBM_CHUNK_CASES(L.m_line, XC)
+    MIBM_CHUNK_CASES(L.m, XC)
 #undef XC
   }
   ++c->launches;
@@ -700,15 +722,15 @@ static bool solve_xc_launch(Ctx* c, V* rhs, const V* T, const char* name) {
 
 template <typename V, bool ZL>
 static bool solve_cc_launch(Ctx* c, V* rhs, const V* T, double* q, int write_rhs, float* m32, const char* name) {
-  TriLayout L = tri_layout(ZL ? c->g.n3m : c->g.n2m);
-  if (!L.m_col) return false;
-  const V* X = T + L.off_col;
-  dim3 block(32, L.n / L.m_col);
+  TriLayout L = tri_layout(ZL ? c->g.n3m : c->g.n2m, tri_chunk(c, ZL ? 2 : 1));
+  if (!L.m) return false;
+  const V* X = T + L.off_ext;
+  dim3 block(32, L.n / L.m);
   dim3 grid(div_up(c->g.n1m, 32), ZL ? c->g.n2m : c->g.n3m);
   {
     MIBM_PROF(c, name);
 #define CC(M) solve_cc_kernel<V, M, ZL><<<grid, block, 0, c->stream>>>(c->g, rhs, X, q, write_rhs, m32)
-    MIBM_CHUNK_CASES(L.m_col, CC)
+    MIBM_CHUNK_CASES(L.m, CC)
 #undef CC
   }
   ++c->launches;
@@ -761,18 +783,79 @@ void k_solve_z_f32(Ctx* c, float* rhs, const float* T, double* q, float* mirror)
 }
 
 void k_solve_x(Ctx* c, double* rhs, double betadx) {
-  const double* T = table_for(c, c->g.n1m, betadx);
+  const double* T = table_for(c, 0, betadx);
   if (T) k_solve_x_T(c, rhs, T);
 }
 
 void k_solve_y(Ctx* c, double* rhs, double betadx) {
-  const double* T = table_for(c, c->g.n2m, betadx);
+  const double* T = table_for(c, 1, betadx);
   if (T) k_solve_y_T(c, rhs, T);
 }
 
 void k_solve_z(Ctx* c, double* rhs, double betadx, double* q) {
-  const double* T = table_for(c, c->g.n3m, betadx);
+  const double* T = table_for(c, 2, betadx);
   if (T) k_solve_z_T(c, rhs, T, q, 1);
+}
+
+// ---------------------------------------------------------------------
+// Autotuner support: time the solve of direction dir with chunk length m
+// (0 = tile kernel) on scratch lines (betadx 0.9), best of `reps` runs after
+// one warm-up, in ms.  The context's own state is not touched.
+// ---------------------------------------------------------------------
+float tri_time_direction(Ctx* c, int dir, int m, bool f32, int reps) {
+  const int n = dir == 0 ? c->g.n1m : (dir == 1 ? c->g.n2m : c->g.n3m);
+  const int saved = c->tune_m[dir];
+  c->tune_m[dir] = m;
+  std::vector<double> slot(slot_len(std::max(c->g.n1m, c->g.n3m)), 0.0);
+  fill_slot(n, m, 0.9, slot.data());
+  std::vector<float> slotf(slot.begin(), slot.end());
+  void* tab = nullptr;
+  void* rhs = nullptr;
+  double* q = nullptr;
+  float best = -1.f;
+  size_t vs = f32 ? sizeof(float) : sizeof(double);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  bool ok = cuda_ok(c, cudaMalloc(&tab, sizeof(double) * slot.size()), "tune") &&
+            cuda_ok(c, cudaMalloc(&rhs, vs * c->g.cells), "tune") &&
+            cuda_ok(c, cudaMalloc((void**)&q, sizeof(double) * c->g.cells), "tune") &&
+            cuda_ok(c, cudaEventCreate(&e0), "tune") && cuda_ok(c, cudaEventCreate(&e1), "tune");
+  if (ok) {
+    if (f32) cudaMemcpyAsync(tab, slotf.data(), sizeof(float) * slotf.size(), cudaMemcpyHostToDevice, c->stream);
+    else cudaMemcpyAsync(tab, slot.data(), sizeof(double) * slot.size(), cudaMemcpyHostToDevice, c->stream);
+    cudaMemsetAsync(rhs, 0, vs * c->g.cells, c->stream);
+    cudaMemsetAsync(q, 0, sizeof(double) * c->g.cells, c->stream);
+    auto run = [&]() {
+      if (f32) {
+        float* r = (float*)rhs;
+        const float* T = (const float*)tab;
+        if (dir == 0) solve_x_launch<float>(c, r, T, "tune");
+        else if (dir == 1) solve_y_launch<float>(c, r, T, "tune");
+        else solve_z_launch<float>(c, r, T, q, 0, nullptr, "tune");
+      } else {
+        double* r = (double*)rhs;
+        const double* T = (const double*)tab;
+        if (dir == 0) solve_x_launch<double>(c, r, T, "tune");
+        else if (dir == 1) solve_y_launch<double>(c, r, T, "tune");
+        else solve_z_launch<double>(c, r, T, q, 0, nullptr, "tune");
+      }
+    };
+    run();
+    for (int r = 0; r < reps && c->status == MIBM_OK; ++r) {
+      cudaEventRecord(e0, c->stream);
+      run();
+      cudaEventRecord(e1, c->stream);
+      if (!cuda_ok(c, cudaEventSynchronize(e1), "tune")) break;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (best < 0.f || ms < best) best = ms;
+    }
+  }
+  cudaStreamSynchronize(c->stream);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(tab); cudaFree(rhs); cudaFree(q);
+  c->tune_m[dir] = saved;
+  return best;
 }
 
 // ---------------------------------------------------------------------

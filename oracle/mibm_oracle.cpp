@@ -1773,6 +1773,10 @@ double mibm_timer_ms_(const int* a, const int* b) { return g_marks[*b] - g_marks
 void mibm_profile_(const int*) {}
 void mibm_set_precision_(const int*, const int*) {}
 void mibm_set_graphs_(const int*) {}
+int mibm_autotune_(void) { return MIBM_OK; }
+int mibm_autotune_get_(int* out) { for (int q = 0; q < 4; ++q) out[q] = 0; return MIBM_OK; }
+int mibm_autotune_save_(const char*) { return MIBM_OK; }
+int mibm_autotune_load_(const char*) { return MIBM_OK; }
 // the oracle runs cases one after another: a batch is its list of contexts
 static std::map<int, std::vector<int>> g_obatch;
 static int g_obatch_next = 1;

@@ -75,3 +75,49 @@ def test_batch_matches_oracle(oracle_lib, gpu_lib):
         for k in FIELDS_OUT:
             assert rel_l2(fg[k], fo[k]) <= 1e-10, k
         assert dtg == pytest.approx(dto, rel=1e-12)
+
+
+def test_autotune_keeps_state_and_parity(oracle_lib, gpu_lib, tmp_path):
+    case = Case(small_config(n=32, level=3, seed=7))
+    cg = case.clone()
+    cg.attach(gpu_lib)
+    before, *_ = _state(cg, gpu_lib)
+    cg.bind(gpu_lib)
+    assert gpu_lib.mibm_autotune_() == 0
+    shapes = np.zeros(4, dtype=np.int32)
+    gpu_lib.mibm_autotune_get_(shapes.ctypes.data)
+    assert all(32 % m == 0 for m in shapes[:3]) and shapes[3] in (2, 4, 8)
+    after, *_ = _state(cg, gpu_lib)
+    for k in FIELDS_OUT:
+        assert np.array_equal(before[k], after[k]), k        # tuning ran on scratch data
+    path = str(tmp_path / "tune.txt").encode()
+    assert gpu_lib.mibm_autotune_save_(path) == 0 and gpu_lib.mibm_autotune_load_(path) == 0
+    co = case.clone()
+    co.attach(oracle_lib)
+    co.run(oracle_lib, 3)
+    cg.run(gpu_lib, 3)
+    got, *_ = _state(cg, gpu_lib)
+    for k, f in FIELDS_OUT.items():
+        assert rel_l2(got[k], co.interior(f)) <= 1e-10, k
+    cg.detach(gpu_lib)
+    co.detach(oracle_lib)
+
+
+def test_autotuned_batch_equals_cases_alone(gpu_lib):
+    nsteps = 3
+    cases = _cases()
+    alone = []
+    for case in cases:
+        c = _attach(case, gpu_lib, 1)
+        assert gpu_lib.mibm_autotune_() == 0
+        c.run(gpu_lib, nsteps)
+        alone.append(_state(c, gpu_lib))
+        c.detach(gpu_lib)
+    bc = [_attach(case, gpu_lib, 1) for case in cases]
+    with BatchRunner(gpu_lib, bc, autotune=True) as b:
+        b.run(nsteps)
+    for q, c in enumerate(bc):
+        f, x, dt, t = _state(c, gpu_lib)
+        for k in FIELDS_OUT:
+            assert np.array_equal(f[k], alone[q][0][k]), (q, k)
+        c.detach(gpu_lib)
