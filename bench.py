@@ -386,6 +386,10 @@ def run_gpu(args):
                     "d2h_bytes_per_step": d2h},
             "roofline": roofline, "gpu_launches": launches, "clocks": clocks, "fp32_refined": fp32,
             "host_wall_ms_per_step": 1e3 * wall / args.steps, "kernels": kernels}
+    if dist.ws == 1 and not args.no_batch:
+        line["batched"] = batched_measurement(lib, args.batch_steps, args.warmup)
+    if dist.ws == 1 and not args.no_serve:
+        line["serving"] = serving_measurement(lib, args.serve_seconds, args.serve_steps, args.serve_budget_gb)
     if dist.ws == 1 and not args.no_cpu:
         try:
             line["cpu_baseline"] = cpu_baseline(args.workload, args.cpu_steps)
@@ -393,6 +397,96 @@ def run_gpu(args):
             line["cpu_baseline"] = {"value": None, "error": str(e)}
     print(json.dumps(line), flush=True)
     dist.close()
+
+
+def batched_measurement(lib, steps: int, warmup: int, seed: int = 100) -> dict:
+    """Batched form on the batched configuration's mix: 32 cases (12 x 48^3,
+    10 x 64^3, 6 x 96^3, 4 x 128^3), icosphere level 2-4 and radius 0.3-0.6
+    uniform, St log-uniform in [0.5, 4], nu uniform in [0.005, 0.02], seeds
+    100-131, precision form, shapes autotuned; timed against stepping the
+    same cases one after another.  Host wall clock around whole batch steps
+    (each ends with a device synchronisation)."""
+    from melt_ibm_gb300.batch import BatchRunner
+    rng = np.random.default_rng(seed)
+    sizes = [48] * 12 + [64] * 10 + [96] * 6 + [128] * 4
+    cfgs = [CaseConfig(n=n, mesh_level=int(rng.integers(2, 5)), rad_p=float(rng.uniform(0.3, 0.6)),
+                       ren=float(1.0 / rng.uniform(0.005, 0.02)),
+                       latheat=float(1.0 / np.exp(rng.uniform(np.log(0.5), np.log(4.0)))), seed=seed + q,
+                       v_on_ve=0.0) for q, n in enumerate(sizes)]
+    t0 = time.perf_counter()
+    proto = [Case(c) for c in cfgs]
+    setup_s = time.perf_counter() - t0
+    cells = sum(n ** 3 for n in sizes)
+
+    def attached():
+        out = []
+        for p in proto:
+            c = p.clone()
+            c.attach(lib)
+            c.bind(lib)
+            lib.mibm_set_precision_(abi.ref_int(1), abi.ref_int(2))
+            lib.check("precision")
+            out.append(c)
+        return out
+
+    cs = attached()
+    with BatchRunner(lib, cs, autotune=True) as b:
+        b.run(warmup)
+        t0 = time.perf_counter()
+        b.run(steps)
+        t_batch = time.perf_counter() - t0
+    launches = lib.mibm_launch_count_()
+    for c in cs:
+        c.detach(lib)
+    cs = attached()
+    for c in cs:
+        c.run(lib, warmup)
+    t0 = time.perf_counter()
+    for s in range(steps):
+        for c in cs:
+            c.step(lib, warmup + 1 + s)
+    t_seq = time.perf_counter() - t0
+    for c in cs:
+        c.detach(lib)
+    shapes = {}
+    for n in sorted(set(sizes)):
+        c = proto[sizes.index(n)].clone()
+        c.attach(lib)
+        c.bind(lib)
+        lib.mibm_set_precision_(abi.ref_int(1), abi.ref_int(2))
+        lib.mibm_autotune_()
+        got = np.zeros(4, dtype=np.int32)
+        lib.mibm_autotune_get_(got.ctypes.data)
+        shapes[f"{n}^3"] = {"chunk_x": int(got[0]), "chunk_y": int(got[1]), "chunk_z": int(got[2]),
+                            "rhs_block_y": int(got[3])}
+        c.detach(lib)
+    return {"value": cells * steps / t_batch / 1e6, "unit": "Mcell-steps/s", "cases": len(sizes),
+            "cells": cells, "steps": steps, "warmup": warmup, "ms_per_step": 1e3 * t_batch / steps,
+            "sequential_value": cells * steps / t_seq / 1e6, "speedup_vs_sequential": t_seq / t_batch,
+            "autotuned_shapes": shapes, "host_setup_s": setup_s, "form": "precision (f32 compute, f64 fields)",
+            "config": "32 cases: 12x48^3, 10x64^3, 6x96^3, 4x128^3; level 2-4, r 0.3-0.6, St log-U[0.5,4], "
+                      "nu U[0.005,0.02], seeds 100-131",
+            "timing": "host wall clock around batch steps (each ends synchronised)"}
+
+
+def serving_measurement(lib, seconds: float, steps: int, budget_gb: float, seed: int = 7) -> dict:
+    """Serving form: Poisson arrivals at 2 cases/s for `seconds`, grids
+    {64, 96, 128, 192}^3 with probabilities {0.4, 0.3, 0.2, 0.1}, the batched
+    configuration's parameter laws, `steps` steps per case in the precision
+    form, admission against an HBM budget of `budget_gb` GB; the run lasts
+    until every request has completed."""
+    from melt_ibm_gb300.serve import DeviceExecutor, Server, serving_requests
+    reqs = serving_requests(seconds, rate=2.0, seed=seed, steps=steps)
+    ex = DeviceExecutor(lib)
+    try:
+        stats = Server(ex, int(budget_gb * 1e9), prepare_workers=4).run(reqs)
+    finally:
+        ex.close()
+    out = stats.summary()
+    out.update({"requests": len(reqs), "arrival_window_s": seconds, "rate_per_s": 2.0, "steps_per_case": steps,
+                "hbm_budget_gb": budget_gb, "seed": seed, "form": "precision (f32 compute, f64 fields)",
+                "unit_cell_steps": "cell-steps/s over the whole run (first arrival to last completion)"})
+    return out
 
 
 def main():
@@ -406,6 +500,14 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp32", action="store_true", help="skip the precision-form measurement")
     ap.add_argument("--nproj", type=int, default=2, help="Poisson solves per substep in the precision form")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-form measurement")
+    ap.add_argument("--batch-steps", type=int, default=10)
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--serve-seconds", type=float, default=20.0,
+                    help="arrival window of the serving run (the serving configuration uses 600)")
+    ap.add_argument("--serve-steps", type=int, default=30,
+                    help="steps per served case (the serving configuration uses 300)")
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     args = ap.parse_args()
     if args.warmup < 3:
         log("bench: warm-up raised to 3 steps")

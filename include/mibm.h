@@ -224,8 +224,8 @@ void mibm_set_graphs_(const int* on);
 /* reductions overlap, their step graphs run as one batch graph (one child */
 /* node per case, no edges: the device interleaves them), and each case    */
 /* gets exactly the result of stepping it alone.  create returns a handle  */
-/* > 0 (0 on error); step returns a status; destroy the batch before its   */
-/* contexts.                                                               */
+/* > 0 (0 on error); step returns a status (ntime <= 0: each case uses its */
+/* own completed-step count + 1); destroy the batch before its contexts.   */
 /* Autotuner (no counterpart in the reference): times the feasible chunk    */
 /* lengths of the x-, y- and z-line solves and the block heights of the    */
 /* explicit-term kernel on the bound context (scratch data; its state is   */

@@ -415,10 +415,12 @@ static int batch_step(Batch* b, int ntime) {
     if (c->status != MIBM_OK) return c->status;
     cs.push_back(c);
   }
-  // (A) CFL and dt reductions of every case, gcurv.f90:153-160
+  // (A) CFL and dt reductions of every case, gcurv.f90:153-160; ntime <= 0:
+  // every case counts its own steps (cases that joined at different times)
   for (Ctx* c : cs) {
-    *c->hi[MIBM_I_NTIME] = ntime;
-    if (c->I(MIBM_I_IDTV) == 1 && ntime != 1) *c->hs[MIBM_S_DT] = c->S(MIBM_S_DTMAX);
+    const int nt = ntime > 0 ? ntime : (int)c->steps_done + 1;
+    *c->hi[MIBM_I_NTIME] = nt;
+    if (c->I(MIBM_I_IDTV) == 1 && nt != 1) *c->hs[MIBM_S_DT] = c->S(MIBM_S_DTMAX);
     k_cfl_async(c, c->red_host);
     if (c->I(MIBM_I_IDTV) == 1) k_getdt_async(c, c->S(MIBM_S_DT), c->red_host + 1);
   }
@@ -616,7 +618,8 @@ int mibm_batch_create_(const int* ids, const int* n) {
 }
 
 // One iteration of the time loop (cfl, dt, forcing, tschem) for every case
-// of the batch; ntime as in gcurv.f90:151.  Returns a status.
+// of the batch; ntime as in gcurv.f90:151, or <= 0 for each case's own step
+// count + 1.  Returns a status.
 int mibm_batch_step_(const int* handle, const int* ntime) {
   Batch* b = batch_of(*handle);
   if (!b) { fail(nullptr, MIBM_EINVAL, "batch_step: unknown batch"); return MIBM_EINVAL; }

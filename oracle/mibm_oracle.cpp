@@ -85,6 +85,7 @@ struct Ctx {
   std::vector<cd> hit_bhat;      // bhat(3, nmodes, nmodes, nmodes)
   bool hit_seeded = false;
   uint64_t hit_rng = 0;
+  int steps_done = 0;   // batch steps completed (per-case step counter)
   // coordinate accessors with the reference's extended ranges (cordin.f90:55-61)
   double xc(int i) const { return xc_[i + n1]; }
   double yc(int j) const { return yc_[j + n2]; }
@@ -1793,10 +1794,11 @@ int mibm_batch_step_(const int* handle, const int* ntime) {
     if (mibm_context_bind_(&id) != MIBM_OK) return MIBM_EINVAL;
     Ctx* c = cur();
     if (!ready(c)) return MIBM_ESTATE;
-    c->I(MIBM_I_NTIME) = *ntime;
+    const int nt = *ntime > 0 ? *ntime : c->steps_done + 1;
+    c->I(MIBM_I_NTIME) = nt;
     cfl(*c);
     if (c->I(MIBM_I_IDTV) == 1) {
-      if (*ntime != 1) c->S(MIBM_S_DT) = c->S(MIBM_S_DTMAX);
+      if (nt != 1) c->S(MIBM_S_DT) = c->S(MIBM_S_DTMAX);
       get_dt(*c);
     }
     if (c->I(MIBM_I_FORCING) == 1) {
@@ -1807,6 +1809,7 @@ int mibm_batch_step_(const int* handle, const int* ntime) {
     }
     tschem(*c);
     if (c->status != MIBM_OK) return c->status;
+    ++c->steps_done;
     c->S(MIBM_S_TIME) = c->S(MIBM_S_TIME) + c->S(MIBM_S_DT);
   }
   return MIBM_OK;
