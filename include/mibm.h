@@ -105,7 +105,8 @@ enum {
 };
 
 /* Scalars (double), registered by address.  Vectors take 3 consecutive  */
-/* doubles at the registered address.                                    */
+/* doubles at the registered address; QUAT takes 4 and INERT_TENSOR 9    */
+/* (InertTensor(3,3), column-major).                                     */
 enum {
   MIBM_S_DT = 0, MIBM_S_AL, MIBM_S_GA, MIBM_S_RO, MIBM_S_BETA,
   MIBM_S_REN, MIBM_S_PEC, MIBM_S_BETAGZ, MIBM_S_TMELT, MIBM_S_TLIQ,
@@ -116,6 +117,15 @@ enum {
   /* HIT forcing parameters (param.f90:16, read from HITForcing.in at    */
   /* papero.f90:52-56): tl, epsstar, kf_on_kmin, C_HIT                   */
   MIBM_S_TL, MIBM_S_EPSSTAR, MIBM_S_KF_ON_KMIN, MIBM_S_C_HIT,
+  /* Moving body (imlsstr = 1; param.f90:229-257, allotri.f90:62-83):    */
+  /* orientation quaternion, inertia tensor, the surface-integrated       */
+  /* pressure / viscous forces and torques of mls_structLoads and their   */
+  /* values one substep back, and the load sums kept for output           */
+  /* (Fp, Ftau, Torq_p, Torq_tau).                                        */
+  MIBM_S_QUAT, MIBM_S_INERT_TENSOR,
+  MIBM_S_INT_PRN_DA, MIBM_S_INT_TAU_DA, MIBM_S_INT_R_X_PRN_DA, MIBM_S_INT_R_X_TAU_DA,
+  MIBM_S_INT_PRN_DA_M1, MIBM_S_INT_TAU_DA_M1, MIBM_S_INT_R_X_PRN_DA_M1, MIBM_S_INT_R_X_TAU_DA_M1,
+  MIBM_S_FP, MIBM_S_FTAU, MIBM_S_TORQ_P, MIBM_S_TORQ_TAU,
   MIBM_NSCALARS
 };
 
@@ -200,7 +210,12 @@ void findprobeindices_(void);     /* findProbeIndices.f90:9-76              */
 void mls_heatflux_(void); /* mls_heatFlux.f90:1-158 (wght_gradT, faceToVert) */
 void apply_stefancondition_(void);/* stefanCondition.f90:1-61               */
 void tagcells_(void);     /* tagCells.f90:4-27 (narrow band + interp_vof)   */
-void particle_(void);     /* particle.f90:1-230 (forcing, melt, geometry)   */
+void particle_(void);     /* particle.f90:1-230 (forcing, melt, motion,
+                             geometry)                                     */
+void mls_structloads_(void);  /* mls_structLoads.f90:1-269 (wght_press,
+                             wght_gradP/U/V/W): pressure and viscous loads */
+void update_part_pos_(void);  /* RigidAuxRoutines.f90:1-54 (newton_euler,
+                             calc_rot_matrix, update_xyz; no collisions)   */
 void cfl_(void);          /* cfl.f90:1-31                                   */
 void get_dt_(void);       /* cfl.f90:33-77                                  */
 void interp_(double* arrold, double* arrnew, const int* n1o, const int* n2o,

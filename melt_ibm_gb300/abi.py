@@ -90,6 +90,7 @@ VOID_ROUTINES = [
     "mlsweight_", "mlsforce_", "velforce_", "tempforce_", "findprobeindices_",
     "mls_heatflux_", "apply_stefancondition_", "tagcells_", "particle_", "cfl_", "get_dt_",
     "tagcells_initial_", "calchitrandomforce_", "calcabc_hitforce_", "mibm_linear_hit_force_",
+    "mls_structloads_", "update_part_pos_",
 ]
 for _n in VOID_ROUTINES:
     SIGNATURES[_n] = (None, [])

@@ -31,7 +31,7 @@ FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", 
 # The Lagrangian kernels make discrete decisions (floor/nint of positions,
 # signs of distances) from geometry; compiling them without FMA contraction
 # keeps that arithmetic bit-identical to an IEEE evaluation in source order.
-PER_FILE = {"lagr.cu": ["--fmad=false"], "interp.cu": ["--fmad=false"]}
+PER_FILE = {"lagr.cu": ["--fmad=false"], "interp.cu": ["--fmad=false"], "rigid.cu": ["--fmad=false"]}
 
 
 def _nvcc() -> str:

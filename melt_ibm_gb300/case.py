@@ -31,7 +31,13 @@ GHOSTED = {abi.MIBM_F_VX, abi.MIBM_F_VY, abi.MIBM_F_VZ, abi.MIBM_F_TEMP, abi.MIB
            abi.MIBM_F_FORCX, abi.MIBM_F_FORCY, abi.MIBM_F_FORCZ,
            abi.MIBM_F_VOFX, abi.MIBM_F_VOFY, abi.MIBM_F_VOFZ, abi.MIBM_F_VOFP,
            abi.MIBM_F_FORXC, abi.MIBM_F_FORYC, abi.MIBM_F_FORZC, abi.MIBM_F_FORTEMP}
-VECTOR_SCALARS = {abi.MIBM_S_POS_CM, abi.MIBM_S_VEL_CM, abi.MIBM_S_OMEGA_C}
+VECTOR_SCALARS = {abi.MIBM_S_POS_CM, abi.MIBM_S_VEL_CM, abi.MIBM_S_OMEGA_C, abi.MIBM_S_QUAT,
+                  abi.MIBM_S_INERT_TENSOR, abi.MIBM_S_INT_PRN_DA, abi.MIBM_S_INT_TAU_DA,
+                  abi.MIBM_S_INT_R_X_PRN_DA, abi.MIBM_S_INT_R_X_TAU_DA, abi.MIBM_S_INT_PRN_DA_M1,
+                  abi.MIBM_S_INT_TAU_DA_M1, abi.MIBM_S_INT_R_X_PRN_DA_M1, abi.MIBM_S_INT_R_X_TAU_DA_M1,
+                  abi.MIBM_S_FP, abi.MIBM_S_FTAU, abi.MIBM_S_TORQ_P, abi.MIBM_S_TORQ_TAU}
+#: doubles per registered scalar slot (InertTensor(3,3) is the widest)
+SCALAR_WIDTH = 9
 
 
 def field_shape(fid: int, n1m: int, n2m: int, n3m: int) -> tuple[int, int, int]:
@@ -63,6 +69,23 @@ def mesh_spec(mid: int, nv: int, ne: int, nf: int):
         abi.MIBM_M_SKEWNESS: ((nf,), d),
     }
     return spec[mid]
+
+
+def inertia_tensor(p1: np.ndarray, p2: np.ndarray, p3: np.ndarray, dens_ratio: float) -> np.ndarray:
+    """Inertia tensor about the centroid of the closed mesh with faces
+    (p1, p2, p3), scaled by the density ratio: the signed-tetrahedron sums of
+    calc_rigidBody_params (RigidAuxRoutines.f90:653-780, Kallay 2006), used
+    at set-up as create_geo.f90:42 does."""
+    v = np.einsum("ij,ij->i", p1, np.cross(p2, p3))
+    s4 = p1 + p2 + p3
+    vol = v.sum()
+    com = (v[:, None] * s4).sum(0) / (4.0 * vol)
+    vol = vol / 6.0
+    mono = lambda a, b: (v * (p1[:, a] * p1[:, b] + p2[:, a] * p2[:, b] + p3[:, a] * p3[:, b]
+                              + s4[:, a] * s4[:, b])).sum() / 120.0 - vol * com[a] * com[b]
+    xx, yy, zz = mono(0, 0), mono(1, 1), mono(2, 2)
+    ixy, ixz, iyz = mono(0, 1), mono(0, 2), mono(1, 2)
+    return dens_ratio * np.array([[yy + zz, -ixy, -ixz], [-ixy, zz + xx, -iyz], [-ixz, -iyz, xx + yy]])
 
 
 @dataclass
@@ -128,7 +151,7 @@ class Case:
                        for fid in range(abi.MIBM_NFIELDS)}
         for fid in (abi.MIBM_F_VOFX, abi.MIBM_F_VOFY, abi.MIBM_F_VOFZ, abi.MIBM_F_VOFP):
             self.fields[fid][...] = 1.0                       # init.f90:30-33
-        self.sc = np.zeros((abi.MIBM_NSCALARS, 3), dtype=np.float64)
+        self.sc = np.zeros((abi.MIBM_NSCALARS, SCALAR_WIDTH), dtype=np.float64)
         self.iv = np.zeros(abi.MIBM_NINTS, dtype=np.int32)
         self.mesh_arrays: dict[int, np.ndarray] = {}
         self._grid()
@@ -207,7 +230,7 @@ class Case:
         M[A.MIBM_M_VERT_OF_FACE][...] = mesh.vert_of_face.T
         M[A.MIBM_M_VERT_OF_EDGE][...] = mesh.vert_of_edge.T
         M[A.MIBM_M_EDGE_OF_FACE][...] = mesh.edge_of_face.T
-        self.sc[A.MIBM_S_POS_CM, :] = pos
+        self.sc[A.MIBM_S_POS_CM, :3] = pos
         self._geometry_refresh(initial=True)
         h, cv = self.S(A.MIBM_S_H_EULERIAN), self.S(A.MIBM_S_CELVOL)
         M[A.MIBM_M_CFAC][...] = (M[A.MIBM_M_SUR] * h) / cv            # initmls.f90:25
@@ -240,6 +263,7 @@ class Case:
                + x[f[:, 2], 0] * (x[f[:, 0], 1] * x[f[:, 1], 2] - x[f[:, 0], 2] * x[f[:, 1], 1]))
         self.set_S(A.MIBM_S_VOLUME, vol.sum() / 6.0)
         self.set_S(A.MIBM_S_SURFACE, sur.sum())
+        self.sc[A.MIBM_S_INERT_TENSOR, :9] = inertia_tensor(p1, p2, p3, self.cfg.dens_ratio).ravel(order="F")
         e = M[A.MIBM_M_VERT_OF_EDGE].T - 1
         M[A.MIBM_M_ELENGTHS][...] = np.sqrt(((x[e[:, 0]] - x[e[:, 1]]) ** 2).sum(1))
 
@@ -254,7 +278,7 @@ class Case:
             F[A.MIBM_F_VX][:n1m, :n2m, 1:n3m + 1] = u
             F[A.MIBM_F_VY][:n1m, :n2m, 1:n3m + 1] = v
             F[A.MIBM_F_VZ][:n1m, :n2m, 1:n3m + 1] = w
-        pos = self.sc[A.MIBM_S_POS_CM]
+        pos = self.sc[A.MIBM_S_POS_CM, :3]
         T = tanh_temperature(self.xm, self.ym, self.zm, pos, c.rad_p, c.tliq, c.tsol, self.dx1)
         F[A.MIBM_F_TEMP][...] = c.tsol
         F[A.MIBM_F_TEMP][:n1m, :n2m, 1:n3m + 1] = T

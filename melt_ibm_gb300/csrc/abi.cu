@@ -9,6 +9,7 @@
 //   * the four RHS fields are separate buffers, so all explicit terms are
 //     formed from the substep's initial fields exactly as tsch.f90:49-57
 //     orders them (every invtr only advances its own component).
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -97,6 +98,10 @@ void precision_after_upload(Ctx* c, unsigned long long mask) {
 }
 
 static const double kGam[3] = {8.0 / 15.0, 5.0 / 12.0, 3.0 / 4.0};     // papero.f90:118-137
+// the body moves (particle.f90:108-129): its state rides with the step
+static bool moving_body(Ctx* c) {
+  return c->I(MIBM_I_IMLSFOR) == 1 && c->I(MIBM_I_IMLSSTR) == 1 && c->maxnf > 0;
+}
 static const double kRom[3] = {0.0, -17.0 / 60.0, -5.0 / 12.0};
 static const int kStepFid[4] = {MIBM_F_VX, MIBM_F_VY, MIBM_F_VZ, MIBM_F_TEMP};
 
@@ -127,6 +132,10 @@ static bool step_prepare(Ctx* c) {
     if (!c->rhs4 && !cuda_ok(c, cudaMalloc(&c->rhs4, 4 * g.cells * sizeof(double)), "rhs4")) return false;
   }
   if (!tri_step_fill(c, bd, f32)) return false;
+  if (moving_body(c)) {
+    if (!rigid_ensure(c)) return false;
+    rigid_pack(c, c->hrigid_in, false);
+  }
   for (int ns = 0; ns < 3; ++ns) {
     *c->hs[MIBM_S_AL] = kGam[ns] + kRom[ns];
     *c->hs[MIBM_S_GA] = kGam[ns];
@@ -162,7 +171,7 @@ static void step_enqueue_f32(Ctx* c) {
       k_solve_y_f32(c, r, T + tlen);
       k_solve_z_f32(c, r, T + 2 * tlen, c->df[kStepFid[q]], q == 3 ? t_mirror : nullptr);
     }
-    const double* mean3 = lagr_particle_fused(c, dp, t_mirror);
+    const double* mean3 = lagr_particle_fused(c, dp, t_mirror, ns < 2 ? c->dparams + ns + 1 : nullptr);
     if (c->status != MIBM_OK) return;
     for (int it = 0; it < c->nproj; ++it) {
       bool last = it + 1 == c->nproj;
@@ -192,7 +201,7 @@ static void step_enqueue_f64(Ctx* c) {
       k_solve_y_T(c, r, T + tlen);
       k_solve_z_T(c, r, T + 2 * tlen, c->df[kStepFid[q]], 0);
     }
-    const double* mean3 = lagr_particle_fused(c, dp, nullptr);
+    const double* mean3 = lagr_particle_fused(c, dp, nullptr, ns < 2 ? c->dparams + ns + 1 : nullptr);
     if (c->status != MIBM_OK) return;
     k_divg(c, dp);
     k_phcalc(c);
@@ -204,6 +213,7 @@ static void step_enqueue_f64(Ctx* c) {
 
 static void step_enqueue(Ctx* c) {
   cudaMemcpyAsync(c->dparams, c->hparams, 3 * sizeof(StepParams), cudaMemcpyHostToDevice, c->stream);
+  if (moving_body(c)) rigid_upload(c);
   if (c->precision == 1) step_enqueue_f32(c);
   else step_enqueue_f64(c);
   if (c->status == MIBM_OK) lagr_step_readback(c);
@@ -219,8 +229,9 @@ static void step_finish(Ctx* c) {
 
 // Everything a step reads by value from the host besides the per-step
 // scalars (dt, al, ga, ro, beta, the rigid-body state: those go through the
-// pinned parameter block): the integer flags, the constant scalars passed to
-// kernels, the form, and the Lagrangian launch sequence generation.
+// pinned parameter and rigid-body blocks): the integer flags, the constant
+// scalars passed to kernels, the form, and the Lagrangian launch sequence
+// generation.
 static uint64_t step_key(Ctx* c) {
   uint64_t h = 1469598103934665603ull;
   auto mix = [&](uint64_t v) { h ^= v; h *= 1099511628211ull; };
@@ -228,7 +239,11 @@ static uint64_t step_key(Ctx* c) {
     if (i != MIBM_I_NTIME) mix((uint64_t)(uint32_t)c->I(i));
   static const int per_step[] = {MIBM_S_DT, MIBM_S_AL, MIBM_S_GA, MIBM_S_RO, MIBM_S_BETA, MIBM_S_TIME,
                                  MIBM_S_CFLM, MIBM_S_VOLUME, MIBM_S_SURFACE, MIBM_S_POS_CM, MIBM_S_VEL_CM,
-                                 MIBM_S_OMEGA_C, MIBM_S_DTMAX};
+                                 MIBM_S_OMEGA_C, MIBM_S_DTMAX, MIBM_S_QUAT, MIBM_S_INERT_TENSOR,
+                                 MIBM_S_INT_PRN_DA, MIBM_S_INT_TAU_DA, MIBM_S_INT_R_X_PRN_DA,
+                                 MIBM_S_INT_R_X_TAU_DA, MIBM_S_INT_PRN_DA_M1, MIBM_S_INT_TAU_DA_M1,
+                                 MIBM_S_INT_R_X_PRN_DA_M1, MIBM_S_INT_R_X_TAU_DA_M1, MIBM_S_FP, MIBM_S_FTAU,
+                                 MIBM_S_TORQ_P, MIBM_S_TORQ_TAU};
   for (int i = 0; i < MIBM_NSCALARS; ++i) {
     bool skip = false;
     for (int p : per_step) skip |= (p == i);
@@ -545,6 +560,46 @@ void apply_stefancondition_(void) { DROPIN_WRITES lagr_stefan(c, push_params(c, 
 void tagcells_(void) { DROPIN_BEGIN lagr_tag_narrow_band(c); DROPIN_END }
 void tagcells_initial_(void) { DROPIN_BEGIN lagr_tag_initial(c); DROPIN_END }
 void particle_(void) { DROPIN_WRITES lagr_particle(c, push_params(c, 3)); DROPIN_END }
+
+// mls_structLoads: the loads of the registered fields and mesh into the
+// registered int_*_dA (previous values to the _m1 slots, sums to Fp, ...).
+void mls_structloads_(void) {
+  DROPIN_BEGIN
+  if (c->maxnf == 0 || !rigid_ensure(c)) return;
+  rigid_pack(c, c->hrigid_in, false);
+  rigid_upload(c);
+  lagr_struct_loads(c, push_params(c, 3));
+  if (c->status != MIBM_OK) return;
+  rigid_download(c);
+  if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "mls_structloads")) return;
+  rigid_unpack(c, c->hrigid_out, false);
+  DROPIN_END
+}
+
+// update_part_pos: Newton-Euler from the registered loads, Volume, pos_CM
+// and InertTensor; moves the device mesh (xyzv, tri_bar, vel_tri) and
+// updates pos_CM, vel_CM, omega_c, quat and InertTensor.
+void update_part_pos_(void) {
+  DROPIN_BEGIN
+  if (c->maxnf == 0 || !rigid_ensure(c)) return;
+  rigid_pack(c, c->hrigid_in, true);
+  rigid_upload(c);
+  const double* geom = (const double*)((const char*)c->drigid + offsetof(RigidDev, geom_in));
+  k_newton_euler(c, push_params(c, 3), geom);
+  k_update_xyz(c, true);
+  rigid_download(c);
+  cudaMemcpyAsync(c->hflag, c->dflag, 4, cudaMemcpyDeviceToHost, c->stream);
+  if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "update_part_pos")) return;
+  if (c->hflag[0]) {
+    fail(c, MIBM_ENUMERIC, "update_part_pos: singular inertia tensor (dgetrf info /= 0)");
+    c->hflag[0] = 0;
+    cudaMemsetAsync(c->dflag, 0, 4, c->stream);
+    return;
+  }
+  rigid_unpack(c, c->hrigid_out, true);
+  lagr_invalidate(c);
+  DROPIN_END
+}
 
 // forcx, forcy, forcz are read by the stencils as FP64 in both forms (no
 // FP32 mirror), so the HIT drop-ins leave the mirrors valid

@@ -61,6 +61,23 @@ template <typename R> __host__ __device__ __forceinline__ R coef(const StepParam
 template <> __host__ __device__ __forceinline__ double coef<double>(const StepParams& p, int i) { return p.cd[i]; }
 template <> __host__ __device__ __forceinline__ float coef<float>(const StepParams& p, int i) { return p.cf[i]; }
 
+// Moving-body state (imlsstr = 1) kept on the device while a step runs:
+// rigid velocities, orientation, the structural loads of this and the
+// previous substep (mls_structLoads.f90:21-24), their running sums, and the
+// products of the Newton-Euler update that update_xyz applies.  Loads are
+// packed [int_prn_dA, int_tau_dA, int_r_x_prn_dA, int_r_x_tau_dA] and the
+// sums [Fp, Ftau, Torq_p, Torq_tau].  `geom_in` mirrors the geometry buffer
+// layout [Surface, Volume1, Volume, pos_CM(3), InertTensor(9)] for the
+// drop-in update_part_pos_, which takes them from the registered scalars.
+struct RigidDev {
+  double vel[3], om[3], quat[4];
+  double load[12], load1[12], acc[12];
+  double inert[9];
+  double xf[15];        // AA (column-major), new pos_CM, pos_CM before the move
+  double geom_in[16];
+  int iters, pad;
+};
+
 struct Grid {
   int n1m, n2m, n3m;         // cells per direction
   int P;                     // row pitch (elements)
@@ -144,6 +161,9 @@ struct Ctx {
   int tune_by = 8;                        // block height of the explicit-term kernel
   uint64_t tune_gen = 0;
   double* step_host = nullptr;            // pinned: geometry scalars read back at step end
+  RigidDev* drigid = nullptr;             // moving-body state (device)
+  RigidDev* hrigid_in = nullptr;          // pinned: uploaded at the start of a step
+  RigidDev* hrigid_out = nullptr;         // pinned: read back at its end
   uint64_t launches = 0;                  // kernels launched through this context
   cudaEvent_t timers[64] = {nullptr};
 
@@ -292,7 +312,18 @@ void lagr_geometry_refresh(Ctx* c, bool imelt);
 void lagr_tag_narrow_band(Ctx* c);
 void lagr_tag_initial(Ctx* c);
 void lagr_particle(Ctx* c, const StepParams* dp);
-const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror);
+const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror, StepParams* next);
+void lagr_struct_loads(Ctx* c, const StepParams* dp);
+// rigid.cu (moving body)
+bool rigid_ensure(Ctx* c);
+void rigid_pack(Ctx* c, RigidDev* h, bool geom_from_scalars);
+void rigid_unpack(Ctx* c, const RigidDev* h, bool pos_from_motion);
+void rigid_upload(Ctx* c);
+void rigid_download(Ctx* c);
+void k_newton_euler(Ctx* c, const StepParams* dp, const double* geom);
+void k_update_xyz(Ctx* c, bool centroids);
+void k_rigid_publish(Ctx* c, const double* geom, StepParams* next);
+void rigid_free(Ctx* c);
 void lagr_step_readback(Ctx* c);
 void lagr_step_host_finish(Ctx* c);
 void lagr_geometry_to_host(Ctx* c);

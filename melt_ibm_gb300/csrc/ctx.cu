@@ -266,6 +266,7 @@ void release(Ctx* c) {
   tri_free(c);
   fft_free(c);
   hit_free(c);
+  rigid_free(c);
   if (c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -394,7 +395,7 @@ void mibm_init_(void) {
   if (!cuda_ok(c, cudaMallocHost((void**)&c->red_host, 4096), "pinned")) return;
   if (!dev_alloc(c, (void**)&c->dflag, 64, "flags")) return;
   if (!cuda_ok(c, cudaMallocHost((void**)&c->hflag, 64), "pinned")) return;
-  if (!cuda_ok(c, cudaMallocHost((void**)&c->step_host, 16 * sizeof(double)), "pinned")) return;
+  if (!cuda_ok(c, cudaMallocHost((void**)&c->step_host, 32 * sizeof(double)), "pinned")) return;
   c->hflag[0] = 0;
   for (int i = 0; i < MIBM_NMESH; ++i) {
     size_t b = mesh_bytes(c, i);

@@ -589,56 +589,45 @@ __global__ void mean3_kernel(const double* __restrict__ part, int m, double ncel
 }
 
 // ---------------------------------------------------------------------
-// heat flux (wght_gradT, mls_heatFlux.f90:161-376): one thread per
-// (triangle, side); result qw_o / qw_i per face
-// ---------------------------------------------------------------------
-__global__ void heat_flux_kernel(LagArgs A, const double* __restrict__ temp, const double* __restrict__ tri_bar,
-                                 const double* __restrict__ tri_nor, const int* __restrict__ ghost,
-                                 const int* __restrict__ pind, double h, double pec, double* __restrict__ qw_o,
-                                 double* __restrict__ qw_i, int* __restrict__ flag) {
-  int gid = blockIdx.x * blockDim.x + threadIdx.x;
-  int t = gid >> 1, side = gid & 1;
-  if (t >= A.nf) return;
-  double* qout = side == 0 ? qw_o : qw_i;
-  if (ghost[t]) { qout[t] = 0.0; return; }
+// MLS gradient at a probe: the common body of wght_gradT (mls_heatFlux.f90:
+// 161-376) and wght_gradP/U/V/W (mls_structLoads.f90:406-1298).  Cage i, j
+// centred on (pi1, pi2); z layers [k1-1, k1, k1] (the repeated layer of the
+// reference) with k1 = floor(z*dx3)+1, or nint for the w-velocity;
+// coordinates per axis from the field's staggering (sel 0 = face, 1 =
+// centre); field values at the wrapped cage, z from [k1w-1, k1w, k1w+1].
+// Returns false on a singular moment matrix.
+__device__ bool probe_grad(const LagArgs& A, const double pos[3], int pi1, int pi2, int sx, int sy, int sz,
+                           bool knint, const double* __restrict__ q, double grad[3]) {
   const Grid& g = A.g;
-  double n0 = tri_nor[3 * t], n1 = tri_nor[3 * t + 1], n2 = tri_nor[3 * t + 2];
-  double s = sqrt(n0 * n0 + n1 * n1 + n2 * n2);
-  double pos[3];
-  for (int d = 0; d < 3; ++d) {
-    double nd = tri_nor[3 * t + d];
-    pos[d] = side == 0 ? tri_bar[3 * t + d] + h * nd / s : tri_bar[3 * t + d] - h * nd / s;
-  }
   double ptx[4] = {1.0, pos[0], pos[1], pos[2]};
-  int pi1 = pind[6 * t + 3 * side + 0], pi2 = pind[6 * t + 3 * side + 1];
   const double eps = 2.220446049250313e-16;
-  int k1 = ffloor(pos[2] * g.dx3) + 1;
-  int kin[3] = {k1 - 1, k1, k1};                  // mls_heatFlux.f90:213 (third layer repeats k1)
+  int k1 = knint ? fnint(pos[2] * g.dx3) + 1 : ffloor(pos[2] * g.dx3) + 1;
+  int kin[3] = {k1 - 1, k1, k1};
   int k1w = fmod_pos(k1 - 1, g.n3m) + 1;
   int keul[3] = {k1w - 1, k1w, k1w + 1};
   double Am[16], dA[3][16];
-  for (int q = 0; q < 16; ++q) { Am[q] = 0; dA[0][q] = 0; dA[1][q] = 0; dA[2][q] = 0; }
+  for (int r = 0; r < 16; ++r) { Am[r] = 0; dA[0][r] = 0; dA[1][r] = 0; dA[2][r] = 0; }
   double W[27], dW[3][27], Tn[27], px[3], py[3], pzv[3];
   double wx[3], wy[3], wz[3], dwx[3], dwy[3], dwz[3];
-  for (int q = 0; q < 3; ++q) {
-    int k = kin[q];
-    pzv[q] = coord(A, 2, 1, k);
-    double np3 = fabs(pos[2] - pzv[q]) / (A.wscl / g.dx3);
-    wz[q] = mls_gaussian(np3, A.wcon);
-    if (np3 < eps) dwz[q] = 0.0;
-    else dwz[q] = mls_gauss_deriv(np3, A.wcon) * ((pos[2] - pzv[q]) / fabs(pos[2] - pzv[q]) / (A.wscl / g.dx3));
-    int j = pi2 - 1 + q;
-    py[q] = coord(A, 1, 1, j);
-    double np2 = fabs(pos[1] - py[q]) / (A.wscl / g.dx2);
-    wy[q] = mls_gaussian(np2, A.wcon);
-    if (np2 < eps) dwy[q] = 0.0;
-    else dwy[q] = mls_gauss_deriv(np2, A.wcon) * ((pos[1] - py[q]) / fabs(pos[1] - py[q]) / (A.wscl / g.dx2));
-    int i = pi1 - 1 + q;
-    px[q] = coord(A, 0, 1, i);
-    double np1 = fabs(pos[0] - px[q]) / (A.wscl / g.dx1);
-    wx[q] = mls_gaussian(np1, A.wcon);
-    if (np1 < eps) dwx[q] = 0.0;
-    else dwx[q] = mls_gauss_deriv(np1, A.wcon) * ((pos[0] - px[q]) / fabs(pos[0] - px[q]) / (A.wscl / g.dx1));
+  for (int r = 0; r < 3; ++r) {
+    int k = kin[r];
+    pzv[r] = coord(A, 2, sz, k);
+    double np3 = fabs(pos[2] - pzv[r]) / (A.wscl / g.dx3);
+    wz[r] = mls_gaussian(np3, A.wcon);
+    if (np3 < eps) dwz[r] = 0.0;
+    else dwz[r] = mls_gauss_deriv(np3, A.wcon) * ((pos[2] - pzv[r]) / fabs(pos[2] - pzv[r]) / (A.wscl / g.dx3));
+    int j = pi2 - 1 + r;
+    py[r] = coord(A, 1, sy, j);
+    double np2 = fabs(pos[1] - py[r]) / (A.wscl / g.dx2);
+    wy[r] = mls_gaussian(np2, A.wcon);
+    if (np2 < eps) dwy[r] = 0.0;
+    else dwy[r] = mls_gauss_deriv(np2, A.wcon) * ((pos[1] - py[r]) / fabs(pos[1] - py[r]) / (A.wscl / g.dx2));
+    int i = pi1 - 1 + r;
+    px[r] = coord(A, 0, sx, i);
+    double np1 = fabs(pos[0] - px[r]) / (A.wscl / g.dx1);
+    wx[r] = mls_gaussian(np1, A.wcon);
+    if (np1 < eps) dwx[r] = 0.0;
+    else dwx[r] = mls_gauss_deriv(np1, A.wcon) * ((pos[0] - px[r]) / fabs(pos[0] - px[r]) / (A.wscl / g.dx1));
   }
   for (int kk = 0; kk < 3; ++kk)
     for (int jj = 0; jj < 3; ++jj)
@@ -661,16 +650,15 @@ __global__ void heat_flux_kernel(LagArgs A, const double* __restrict__ temp, con
         }
         int ii_ = fmod_pos(pi1 - 1 + ii - 1, g.n1m), jj_ = fmod_pos(pi2 - 1 + jj - 1, g.n2m);
         int kk_ = wrap(keul[kk] - 1, g.n3m);
-        Tn[n] = temp[cidx(g, ii_, jj_, kk_)];
+        Tn[n] = q[cidx(g, ii_, jj_, kk_)];
       }
-  if (!inv4(Am)) { atomicOr(flag, 1); qout[t] = 0.0; return; }
+  if (!inv4(Am)) return false;
   double gam[4];
   for (int r = 0; r < 4; ++r) {
     double a = 0;
     for (int cc = 0; cc < 4; ++cc) a += Am[r + 4 * cc] * ptx[cc];
     gam[r] = a;
   }
-  double grad[3];
   for (int d = 0; d < 3; ++d) {
     double pk[4] = {0, 0, 0, 0};
     pk[d + 1] = 1.0;
@@ -698,8 +686,217 @@ __global__ void heat_flux_kernel(LagArgs A, const double* __restrict__ temp, con
         }
     grad[d] = acc;
   }
+  return true;
+}
+
+// ---------------------------------------------------------------------
+// heat flux (wght_gradT, mls_heatFlux.f90:161-376): one thread per
+// (triangle, side); result qw_o / qw_i per face
+// ---------------------------------------------------------------------
+__global__ void heat_flux_kernel(LagArgs A, const double* __restrict__ temp, const double* __restrict__ tri_bar,
+                                 const double* __restrict__ tri_nor, const int* __restrict__ ghost,
+                                 const int* __restrict__ pind, double h, double pec, double* __restrict__ qw_o,
+                                 double* __restrict__ qw_i, int* __restrict__ flag) {
+  int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  int t = gid >> 1, side = gid & 1;
+  if (t >= A.nf) return;
+  double* qout = side == 0 ? qw_o : qw_i;
+  if (ghost[t]) { qout[t] = 0.0; return; }
+  double n0 = tri_nor[3 * t], n1 = tri_nor[3 * t + 1], n2 = tri_nor[3 * t + 2];
+  double s = sqrt(n0 * n0 + n1 * n1 + n2 * n2);
+  double pos[3];
+  for (int d = 0; d < 3; ++d) {
+    double nd = tri_nor[3 * t + d];
+    pos[d] = side == 0 ? tri_bar[3 * t + d] + h * nd / s : tri_bar[3 * t + d] - h * nd / s;
+  }
+  int pi1 = pind[6 * t + 3 * side + 0], pi2 = pind[6 * t + 3 * side + 1];
+  double grad[3];
+  if (!probe_grad(A, pos, pi1, pi2, 1, 1, 1, false, temp, grad)) { atomicOr(flag, 1); qout[t] = 0.0; return; }
   double qv = n0 * grad[0] + n1 * grad[1] + n2 * grad[2];
   qout[t] = qv / pec;
+}
+
+// ---------------------------------------------------------------------
+// Structural loads (mls_structLoads.f90:1-269).  Stage 1: one thread per
+// (face, evaluation) at the face's positive probe x_p = X + h n/|n|:
+//   e = 0  pressure value (wght_press: cell-centred cage, z layers
+//          k1-1..k1+1 without the repeated layer, mls_structLoads.f90:271-404)
+//   e = 1  grad p   (wght_gradP, cage (icent, jcent))
+//   e = 2  grad u   (wght_gradU, x at faces, cage (istag, jcent))
+//   e = 3  grad v   (wght_gradV, y at faces, cage (icent, jstag))
+//   e = 4  grad w   (wght_gradW, z at faces with nint, cage (icent, jcent))
+// written to 13 doubles per face [p, gradP, gradU, gradV, gradW].
+// Stage 2: one block forms the per-face pressure force, viscous normal
+// stress and their moments about pos_CM in the reference's operation
+// order and sums them over the faces in a fixed order.
+// ---------------------------------------------------------------------
+__device__ bool probe_value(const LagArgs& A, const double pos[3], int i0, int j0, const double* __restrict__ q,
+                            double& val) {
+  const Grid& g = A.g;
+  double ptx[4] = {1.0, pos[0], pos[1], pos[2]};
+  int k1 = ffloor(pos[2] * g.dx3) + 1;
+  double wz[3], wy[3], wx[3], cz[3], cy[3], cx[3];
+  for (int r = 0; r < 3; ++r) {
+    cz[r] = coord(A, 2, 1, k1 - 1 + r);
+    cy[r] = coord(A, 1, 1, j0 - 1 + r);
+    cx[r] = coord(A, 0, 1, i0 - 1 + r);
+    wz[r] = mls_gaussian(fabs(cz[r] - pos[2]) / (A.wscl / g.dx3), A.wcon);
+    wy[r] = mls_gaussian(fabs(cy[r] - pos[1]) / (A.wscl / g.dx2), A.wcon);
+    wx[r] = mls_gaussian(fabs(cx[r] - pos[0]) / (A.wscl / g.dx1), A.wcon);
+  }
+  double Am[16];
+  for (int r = 0; r < 16; ++r) Am[r] = 0.0;
+  for (int kk = 0; kk < 3; ++kk)
+    for (int jj = 0; jj < 3; ++jj) {
+      double w23 = wy[jj] * wz[kk];
+      for (int ii = 0; ii < 3; ++ii) {
+        double wtx = wx[ii] * w23;
+        double pk[4] = {1.0, cx[ii], cy[jj], cz[kk]};
+        for (int cc = 0; cc < 4; ++cc) {
+          double tt = wtx * pk[cc];
+          for (int r = 0; r < 4; ++r) Am[r + 4 * cc] = Am[r + 4 * cc] + tt * pk[r];
+        }
+      }
+    }
+  if (!inv4(Am)) return false;
+  double ptxA[4];
+  for (int cc = 0; cc < 4; ++cc) {
+    double sum = 0;
+    for (int r = 0; r < 4; ++r) sum += ptx[r] * Am[r + 4 * cc];
+    ptxA[cc] = sum;
+  }
+  int k1w = fmod_pos(k1 - 1, g.n3m) + 1;
+  double acc = 0.0;
+  for (int kk = 0; kk < 3; ++kk) {
+    int kc = wrap(k1w - 1 + kk - 1, g.n3m);        // keul = k1w-1, k1w, k1w+1 (1-based)
+    for (int jj = 0; jj < 3; ++jj) {
+      int jc = fmod_pos(j0 - 1 + jj - 1, g.n2m);
+      double w23 = wy[jj] * wz[kk];
+      for (int ii = 0; ii < 3; ++ii) {
+        int ic = fmod_pos(i0 - 1 + ii - 1, g.n1m);
+        double wtx = wx[ii] * w23;
+        double phi = ptxA[0] * (wtx * 1.0) + ptxA[1] * (wtx * cx[ii]) + ptxA[2] * (wtx * cy[jj]) +
+                     ptxA[3] * (wtx * cz[kk]);
+        acc = acc + q[cidx(g, ic, jc, kc)] * phi;
+      }
+    }
+  }
+  val = acc;
+  return true;
+}
+
+__device__ __forceinline__ void struct_probe(const LagArgs& A, const double* __restrict__ tri_bar,
+                                             const double* __restrict__ tri_nor, int t, double h, double pos[3],
+                                             double nrm[3]) {
+  for (int d = 0; d < 3; ++d) nrm[d] = tri_nor[3 * t + d];
+  double s = sqrt(nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2]);
+  for (int d = 0; d < 3; ++d) pos[d] = tri_bar[3 * t + d] + h * nrm[d] / s;
+}
+
+__global__ void loads_eval_kernel(LagArgs A, const double* __restrict__ pr, const double* __restrict__ vx,
+                                  const double* __restrict__ vy, const double* __restrict__ vz,
+                                  const double* __restrict__ tri_bar, const double* __restrict__ tri_nor,
+                                  const int* __restrict__ ghost, double h, double* __restrict__ ev,
+                                  int* __restrict__ flag) {
+  int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  int t = gid / 5, e = gid - 5 * t;
+  if (t >= A.nf) return;
+  double* out = ev + 13 * (size_t)t;
+  if (ghost[t]) {
+    if (e == 0) out[0] = 0.0;
+    else for (int d = 0; d < 3; ++d) out[1 + 3 * (e - 1) + d] = 0.0;
+    return;
+  }
+  const Grid& g = A.g;
+  double pos[3], nrm[3];
+  struct_probe(A, tri_bar, tri_nor, t, h, pos, nrm);
+  int icent = ffloor(pos[0] * g.dx1) + 1, istag = fnint(pos[0] * g.dx1) + 1;
+  int jcent = ffloor(pos[1] * g.dx2) + 1, jstag = fnint(pos[1] * g.dx2) + 1;
+  bool ok;
+  if (e == 0) {
+    double v = 0.0;
+    ok = probe_value(A, pos, icent, jcent, pr, v);
+    out[0] = ok ? v : 0.0;
+  } else {
+    double gr[3] = {0, 0, 0};
+    if (e == 1) ok = probe_grad(A, pos, icent, jcent, 1, 1, 1, false, pr, gr);
+    else if (e == 2) ok = probe_grad(A, pos, istag, jcent, 0, 1, 1, false, vx, gr);
+    else if (e == 3) ok = probe_grad(A, pos, icent, jstag, 1, 0, 1, false, vy, gr);
+    else ok = probe_grad(A, pos, icent, jcent, 1, 1, 0, true, vz, gr);
+    for (int d = 0; d < 3; ++d) out[1 + 3 * (e - 1) + d] = ok ? gr[d] : 0.0;
+  }
+  if (!ok) atomicOr(flag, 1);
+}
+
+__device__ __forceinline__ void cross3(double r[3], const double x[3], const double y[3]) {
+  r[0] = x[1] * y[2] - y[1] * x[2];
+  r[1] = x[2] * y[0] - y[2] * x[0];
+  r[2] = x[0] * y[1] - y[0] * x[1];
+}
+
+// Per-face loads in the reference's order (mls_structLoads.f90:52-202):
+// c[0..3) pressure force, [3..6) viscous force, [6..9) pressure torque,
+// [9..12) viscous torque.
+__device__ void face_loads(const double* __restrict__ e, const double nrm[3], const double rad[3], double sur,
+                           double h, double ren, double c[12]) {
+  double press_tri = e[0] - h * (e[1] * nrm[0] + e[2] * nrm[1] + e[3] * nrm[2]);
+  double pn[3], buf[3];
+  for (int d = 0; d < 3; ++d) { c[d] = press_tri * sur * nrm[d]; pn[d] = press_tri * nrm[d]; }
+  cross3(buf, rad, pn);
+  for (int d = 0; d < 3; ++d) c[6 + d] = buf[d] * sur;
+  double S11 = e[4], S12 = e[5], S13 = e[6], S21 = e[7], S22 = e[8], S23 = e[9];
+  double S31 = e[10], S32 = e[11], S33 = e[12];
+  double sr = sur / ren;
+  double tv[3];
+  tv[0] = sr * (2.0 * S11 * nrm[0] + (S12 + S21) * nrm[1] + S13 * nrm[2]);
+  tv[1] = sr * ((S21 + S12) * nrm[0] + 2.0 * S22 * nrm[1] + S23 * nrm[2]);
+  tv[2] = sr * (S13 * nrm[0] + S23 * nrm[1]);
+  double tn[3], rt[3];
+  for (int d = 0; d < 3; ++d) tn[d] = 0.0 + tv[d];
+  cross3(buf, rad, tv);
+  for (int d = 0; d < 3; ++d) rt[d] = 0.0 + buf[d];
+  tv[0] = sr * (S31 * nrm[2]);
+  tv[1] = sr * (S32 * nrm[2]);
+  tv[2] = sr * (S31 * nrm[0] + S32 * nrm[1] + 2.0 * S33 * nrm[2]);
+  for (int d = 0; d < 3; ++d) tn[d] = tn[d] + tv[d];
+  cross3(buf, rad, tv);
+  for (int d = 0; d < 3; ++d) rt[d] = rt[d] + buf[d];
+  for (int d = 0; d < 3; ++d) { c[3 + d] = tn[d]; c[9 + d] = rt[d]; }
+}
+
+// One block: fixed-order sums of the per-face loads; thread 0 moves the
+// previous loads to the _m1 slots, stores the new ones and adds them to the
+// running sums (mls_structLoads.f90:21-24, 207-262).
+__global__ void loads_reduce_kernel(int nf, const double* __restrict__ ev, const double* __restrict__ tri_bar,
+                                    const double* __restrict__ tri_nor, const double* __restrict__ sur,
+                                    const int* __restrict__ ghost, const StepParams* __restrict__ pp, double h,
+                                    double ren, RigidDev* r) {
+  __shared__ double sm[12][256];
+  double acc[12];
+  for (int q = 0; q < 12; ++q) acc[q] = 0.0;
+  double pcm[3] = {pp->pos[0], pp->pos[1], pp->pos[2]};
+  for (int t = threadIdx.x; t < nf; t += blockDim.x) {
+    if (ghost[t]) continue;
+    double nrm[3], rad[3], cf[12];
+    for (int d = 0; d < 3; ++d) { nrm[d] = tri_nor[3 * t + d]; rad[d] = tri_bar[3 * t + d] - pcm[d]; }
+    face_loads(ev + 13 * (size_t)t, nrm, rad, sur[t], h, ren, cf);
+    for (int q = 0; q < 12; ++q) acc[q] += cf[q];
+  }
+  for (int q = 0; q < 12; ++q) sm[q][threadIdx.x] = acc[q];
+  __syncthreads();
+  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off)
+      for (int q = 0; q < 12; ++q) sm[q][threadIdx.x] += sm[q][threadIdx.x + off];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    // packed [prn, tau, rprn, rtau]; face_loads gives [prn, tau, rprn, rtau]
+    for (int q = 0; q < 12; ++q) {
+      r->load1[q] = r->load[q];
+      r->load[q] = sm[q][0];
+      r->acc[q] = r->acc[q] + sm[q][0];
+    }
+  }
 }
 
 // ---------------------------------------------------------------------
@@ -897,11 +1094,11 @@ __global__ void stefan_kernel(int nv, const int* __restrict__ ghostv, const doub
 // ---------------------------------------------------------------------
 __global__ void face_geom_kernel(int nf, const int* __restrict__ vof, const int* __restrict__ ghost,
                                  const double* __restrict__ x, double* __restrict__ sur, double* __restrict__ nor,
-                                 double* __restrict__ bar, double* __restrict__ part /* 11 per face */) {
+                                 double* __restrict__ bar, double* __restrict__ part /* 12 per face */) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nf) return;
-  double* pp = part + 11 * (size_t)t;
-  if (ghost[t]) { for (int q = 0; q < 11; ++q) pp[q] = 0.0; return; }
+  double* pp = part + 12 * (size_t)t;
+  if (ghost[t]) { for (int q = 0; q < 12; ++q) pp[q] = 0.0; return; }
   int a = vof[3 * t] - 1, b = vof[3 * t + 1] - 1, d = vof[3 * t + 2] - 1;
   double x1 = x[3 * a], y1 = x[3 * a + 1], z1 = x[3 * a + 2];
   double x2 = x[3 * b], y2 = x[3 * b + 1], z2 = x[3 * b + 2];
@@ -931,6 +1128,7 @@ __global__ void face_geom_kernel(int nf, const int* __restrict__ vof, const int*
   pp[8] = v * (z1 * z1 + z2 * z2 + z3 * z3 + z4 * z4);
   pp[9] = v * (y1 * x1 + y2 * x2 + y3 * x3 + y4 * x4);
   pp[10] = v * (z1 * x1 + z2 * x2 + z3 * x3 + z4 * x4);
+  pp[11] = v * (z1 * y1 + z2 * y2 + z3 * y3 + z4 * y4);
 }
 
 __global__ void vert_geom_kernel(int nv, const int* __restrict__ adj_off, const int* __restrict__ adj_face,
@@ -952,19 +1150,21 @@ __global__ void vert_geom_kernel(int nv, const int* __restrict__ adj_off, const 
   vnor[3 * v] = a0 / m; vnor[3 * v + 1] = a1 / m; vnor[3 * v + 2] = a2 / m;
 }
 
-// fixed-order reduction of the 11 per-face sums by one block; writes
-// [Surface, Volume, pos_CM(3), ...] into out
-__global__ void geom_reduce_kernel(int nf, const double* __restrict__ part, double* __restrict__ out) {
-  __shared__ double sm[11][256];
-  double s[11];
-  for (int q = 0; q < 11; ++q) s[q] = 0.0;
+// fixed-order reduction of the 12 per-face sums by one block; writes
+// [Surface, Volume1, Volume, pos_CM(3), InertTensor(9)] into out (the
+// post-processing of calc_rigidBody_params, RigidAuxRoutines.f90:736-775)
+__global__ void geom_reduce_kernel(int nf, const double* __restrict__ part, double dens_ratio,
+                                   double* __restrict__ out) {
+  __shared__ double sm[12][256];
+  double s[12];
+  for (int q = 0; q < 12; ++q) s[q] = 0.0;
   for (int t = threadIdx.x; t < nf; t += blockDim.x)
-    for (int q = 0; q < 11; ++q) s[q] += part[11 * (size_t)t + q];
-  for (int q = 0; q < 11; ++q) sm[q][threadIdx.x] = s[q];
+    for (int q = 0; q < 12; ++q) s[q] += part[12 * (size_t)t + q];
+  for (int q = 0; q < 12; ++q) sm[q][threadIdx.x] = s[q];
   __syncthreads();
   for (int off = blockDim.x / 2; off > 0; off >>= 1) {
     if (threadIdx.x < off)
-      for (int q = 0; q < 11; ++q) sm[q][threadIdx.x] += sm[q][threadIdx.x + off];
+      for (int q = 0; q < 12; ++q) sm[q][threadIdx.x] += sm[q][threadIdx.x + off];
     __syncthreads();
   }
   if (threadIdx.x == 0) {
@@ -975,6 +1175,14 @@ __global__ void geom_reduce_kernel(int nf, const double* __restrict__ part, doub
     Vol = Vol / 6.0;
     out[0] = Surface; out[1] = Volume1; out[2] = Vol;
     out[3] = Cx; out[4] = Cy; out[5] = Cz;
+    r = 1.0 / 120.0;
+    double Ixy = sm[9][0] * r - Vol * Cy * Cx;
+    double Ixz = sm[10][0] * r - Vol * Cz * Cx;
+    double Iyz = sm[11][0] * r - Vol * Cz * Cy;
+    double xx = sm[6][0] * r - Vol * Cx * Cx, yy = sm[7][0] * r - Vol * Cy * Cy, zz = sm[8][0] * r - Vol * Cz * Cz;
+    double Ixx = yy + zz, Iyy = zz + xx, Izz = xx + yy;
+    double I[9] = {Ixx, -Ixy, -Ixz, -Ixy, Iyy, -Iyz, -Ixz, -Iyz, Izz};
+    for (int q = 0; q < 9; ++q) out[6 + q] = I[q] * dens_ratio;
   }
 }
 
@@ -1303,7 +1511,8 @@ struct LagState {
   int* adj_face = nullptr;
   int adj_nf = -1, adj_nv = -1;
   double* face_part = nullptr;
-  double* geom_out = nullptr;   // device [Surface, Volume1, Vol, Cx, Cy, Cz]
+  double* geom_out = nullptr;   // device [Surface, Volume1, Vol, Cx, Cy, Cz, InertTensor(9)]
+  double* loads_ev = nullptr;   // structural loads: 13 probe evaluations per face
   double* mean3 = nullptr;
   unsigned long long* sdf_bits = nullptr;
   int* winner = nullptr;
@@ -1379,8 +1588,9 @@ static bool ensure_adjacency(Ctx* c) {
 static bool ensure_lag_buffers(Ctx* c) {
   LagState* s = lag_of(c);
   if (!s->face_part) {
-    if (!cuda_ok(c, cudaMalloc(&s->face_part, sizeof(double) * 11 * std::max(1, c->maxnf)), "lag")) return false;
-    if (!cuda_ok(c, cudaMalloc(&s->geom_out, sizeof(double) * 8), "lag")) return false;
+    if (!cuda_ok(c, cudaMalloc(&s->face_part, sizeof(double) * 12 * std::max(1, c->maxnf)), "lag")) return false;
+    if (!cuda_ok(c, cudaMalloc(&s->geom_out, sizeof(double) * 16), "lag")) return false;
+    cudaMemsetAsync(s->geom_out, 0, sizeof(double) * 16, c->stream);
     // [0..3) FP64 mean force, [4..6) the same rounded to FP32 (3 floats)
     if (!cuda_ok(c, cudaMalloc(&s->mean3, sizeof(double) * 8), "lag")) return false;
     cudaMemsetAsync(s->mean3, 0, sizeof(double) * 8, c->stream);
@@ -1412,7 +1622,8 @@ static bool check_flag(Ctx* c, const char* what) {
   cudaMemcpyAsync(c->hflag, c->dflag, 4, cudaMemcpyDeviceToHost, c->stream);
   if (!cuda_ok(c, cudaStreamSynchronize(c->stream), what)) return false;
   if (c->hflag[0]) {
-    fail(c, MIBM_ENUMERIC, std::string(what) + ": singular MLS moment matrix (dgetrf info /= 0)");
+    fail(c, MIBM_ENUMERIC, std::string(what) + ((c->hflag[0] & 2) ? ": singular inertia tensor (dgetrf info /= 0)"
+                                                                  : ": singular MLS moment matrix (dgetrf info /= 0)"));
     cudaMemsetAsync(c->dflag, 0, 4, c->stream);
     return false;
   }
@@ -1618,19 +1829,28 @@ void lagr_stefan(Ctx* c, const StepParams* dp) {
 }
 
 // Geometry refresh (particle.f90:165-193): kernels only; the scalars stay
-// in the device buffer until geometry_to_host.
-static void geometry_launch(Ctx* c, bool imelt) {
+// in the device buffer until geometry_to_host.  body_only: the pass before
+// the Newton-Euler update (particle.f90:108-117: centroids, normals,
+// volume, centre of mass and inertia tensor of the melted body); it also
+// rewrites `sur`, which nothing reads before the full refresh recomputes it.
+static void geometry_launch(Ctx* c, bool imelt, bool body_only = false) {
   LagState* s = lag_of(c);
   { MIBM_PROF(c, "face_geom");
     face_geom_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(
         c->maxnf, M<int>(c, MIBM_M_VERT_OF_FACE), M<int>(c, MIBM_M_GHOST_FACE), M<double>(c, MIBM_M_XYZV),
         M<double>(c, MIBM_M_SUR), M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_TRI_BAR), s->face_part); }
+  if (body_only) {
+    { MIBM_PROF(c, "geom_reduce");
+      geom_reduce_kernel<<<1, 256, 0, c->stream>>>(c->maxnf, s->face_part, c->S(MIBM_S_DENS_RATIO), s->geom_out); }
+    c->launches += 2;
+    return;
+  }
   { MIBM_PROF(c, "vert_geom");
     vert_geom_kernel<<<div_up(c->maxnv, 128), 128, 0, c->stream>>>(
         c->maxnv, s->adj_off, s->adj_face, M<int>(c, MIBM_M_GHOST_VERT), M<double>(c, MIBM_M_SUR),
         M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_AVERT), M<double>(c, MIBM_M_VERT_NOR)); }
   { MIBM_PROF(c, "geom_reduce");
-    geom_reduce_kernel<<<1, 256, 0, c->stream>>>(c->maxnf, s->face_part, s->geom_out); }
+    geom_reduce_kernel<<<1, 256, 0, c->stream>>>(c->maxnf, s->face_part, c->S(MIBM_S_DENS_RATIO), s->geom_out); }
   c->launches += 3;
   if (imelt) {
     { MIBM_PROF(c, "cfac");
@@ -1647,13 +1867,48 @@ void lagr_geometry_to_host(Ctx* c) {
   if (c->maxnf == 0) return;
   LagState* s = lag_of(c);
   if (!s->geom_out) return;
-  cudaMemcpyAsync(c->red_host, s->geom_out, sizeof(double) * 6, cudaMemcpyDeviceToHost, c->stream);
+  cudaMemcpyAsync(c->red_host, s->geom_out, sizeof(double) * 15, cudaMemcpyDeviceToHost, c->stream);
   if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "geometry")) return;
   *c->hs[MIBM_S_SURFACE] = c->red_host[0];
   *c->hs[MIBM_S_VOLUME] = c->red_host[2];
-  c->hs[MIBM_S_POS_CM][0] = c->red_host[3];
-  c->hs[MIBM_S_POS_CM][1] = c->red_host[4];
-  c->hs[MIBM_S_POS_CM][2] = c->red_host[5];
+  for (int d = 0; d < 3; ++d) c->hs[MIBM_S_POS_CM][d] = c->red_host[3 + d];
+  for (int q = 0; q < 9; ++q) c->hs[MIBM_S_INERT_TENSOR][q] = c->red_host[6 + q];
+}
+
+static void struct_loads_launch(Ctx* c, const StepParams* dp) {
+  LagState* s = lag_of(c);
+  if (!s->loads_ev &&
+      !cuda_ok(c, cudaMalloc(&s->loads_ev, sizeof(double) * 13 * std::max(1, c->maxnf)), "structLoads"))
+    return;
+  double h = c->S(MIBM_S_H_EULERIAN);
+  { MIBM_PROF(c, "loads_eval");
+    loads_eval_kernel<<<div_up(5 * (size_t)c->maxnf, 128), 128, 0, c->stream>>>(
+        lag_args(c), c->df[MIBM_F_PR], c->df[MIBM_F_VX], c->df[MIBM_F_VY], c->df[MIBM_F_VZ],
+        M<double>(c, MIBM_M_TRI_BAR), M<double>(c, MIBM_M_TRI_NOR), M<int>(c, MIBM_M_GHOST_FACE), h, s->loads_ev,
+        c->dflag); }
+  { MIBM_PROF(c, "loads_reduce");
+    loads_reduce_kernel<<<1, 256, 0, c->stream>>>(c->maxnf, s->loads_ev, M<double>(c, MIBM_M_TRI_BAR),
+                                                  M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_SUR),
+                                                  M<int>(c, MIBM_M_GHOST_FACE), dp, h, c->S(MIBM_S_REN),
+                                                  c->drigid); }
+  c->launches += 2;
+}
+
+// mls_structLoads on the device state; the loads stay in c->drigid.
+void lagr_struct_loads(Ctx* c, const StepParams* dp) {
+  if (c->maxnf == 0) return;
+  if (!ensure_lag_buffers(c) || !rigid_ensure(c)) return;
+  struct_loads_launch(c, dp);
+  if (MIBM_LAUNCH_CHECK(c, "mls_structLoads")) check_flag(c, "mls_structLoads");
+}
+
+// particle.f90:108-129: geometry of the melted body, then update_part_pos
+// (newton_euler, update_xyz) on the device.
+static void motion_launch(Ctx* c, const StepParams* dp) {
+  LagState* s = lag_of(c);
+  geometry_launch(c, false, true);
+  k_newton_euler(c, dp, s->geom_out);
+  k_update_xyz(c, false);
 }
 
 void lagr_geometry_refresh(Ctx* c, bool imelt) {
@@ -1770,10 +2025,29 @@ void lagr_particle(Ctx* c, const StepParams* dp) {
     lagr_heat_flux(c);
     if (c->status != MIBM_OK) return;
   }
+  bool str = c->I(MIBM_I_IMLSSTR) == 1;
+  if (str) {
+    if (!ensure_lag_buffers(c) || !rigid_ensure(c)) return;
+    rigid_pack(c, c->hrigid_in, false);
+    rigid_upload(c);
+    lagr_struct_loads(c, dp);
+    if (c->status != MIBM_OK) return;
+  }
   lagr_velforce(c);
   lagr_tempforce(c);
   if (imelt) lagr_stefan(c, dp);
-  lagr_geometry_refresh(c, imelt);
+  if (!ensure_adjacency(c) || !ensure_lag_buffers(c)) return;
+  if (str) motion_launch(c, dp);
+  geometry_launch(c, imelt);
+  if (str) {
+    k_rigid_publish(c, lag_of(c)->geom_out, nullptr);
+    rigid_download(c);
+  }
+  lagr_geometry_to_host(c);
+  if (str) {
+    if (!check_flag(c, "update_part_pos")) return;
+    rigid_unpack(c, c->hrigid_out, false);
+  }
   if (c->S(MIBM_S_VOLUME) < c->S(MIBM_S_V_THRESH)) fail(c, MIBM_EABORT, "Geometry V/VE smaller than threshold");
 }
 
@@ -1783,7 +2057,7 @@ void lagr_particle(Ctx* c, const StepParams* dp) {
 // has read the unforced temperature, into T.  MLS weights of a stationary
 // cage are reused.  Flags and geometry scalars are read by the caller at the
 // end of the step.
-const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror) {
+const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror, StepParams* next) {
   if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0) return nullptr;
   if (!ensure_adjacency(c) || !ensure_lag_buffers(c)) return nullptr;
   LagState* s = lag_of(c);
@@ -1796,6 +2070,8 @@ const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror)
   }
   force_coefficients(c);
   update_plan(c);
+  bool str = c->I(MIBM_I_IMLSSTR) == 1;
+  if (str) struct_loads_launch(c, dp);      // reads the unforced u, v, w and p
   scatter(c, true, 0, 3, true);
   double ncell = (double)c->g.n1m * (double)c->g.n2m * (double)c->g.n3m;
   { MIBM_PROF(c, "seg_mean");
@@ -1810,7 +2086,9 @@ const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror)
   }
   scatter(c, true, 3, 4, false, t_mirror);
   if (imelt) lagr_stefan(c, dp);
+  if (str) motion_launch(c, dp);
   geometry_launch(c, imelt);
+  if (str) k_rigid_publish(c, s->geom_out, next);
   MIBM_LAUNCH_CHECK(c, "particle");
   return s->mean3;
 }
@@ -1824,23 +2102,25 @@ void lagr_step_readback(Ctx* c) {
   if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0) return;
   LagState* s = lag_of(c);
   cudaMemcpyAsync(c->hflag, c->dflag, 4, cudaMemcpyDeviceToHost, c->stream);
-  if (s->geom_out) cudaMemcpyAsync(c->step_host, s->geom_out, sizeof(double) * 6, cudaMemcpyDeviceToHost, c->stream);
+  if (s->geom_out) cudaMemcpyAsync(c->step_host, s->geom_out, sizeof(double) * 15, cudaMemcpyDeviceToHost, c->stream);
+  if (c->I(MIBM_I_IMLSSTR) == 1 && c->drigid) rigid_download(c);
 }
 
 void lagr_step_host_finish(Ctx* c) {
   if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0) return;
   if (c->hflag[0]) {
-    fail(c, MIBM_ENUMERIC, "particle: singular MLS moment matrix (dgetrf info /= 0)");
+    fail(c, MIBM_ENUMERIC, (c->hflag[0] & 2) ? "particle: singular inertia tensor (dgetrf info /= 0)"
+                                             : "particle: singular MLS moment matrix (dgetrf info /= 0)");
     c->hflag[0] = 0;
     cudaMemsetAsync(c->dflag, 0, 4, c->stream);
     return;
   }
   if (!lag_of(c)->geom_out) return;
+  if (c->I(MIBM_I_IMLSSTR) == 1 && c->drigid) rigid_unpack(c, c->hrigid_out, false);
   *c->hs[MIBM_S_SURFACE] = c->step_host[0];
   *c->hs[MIBM_S_VOLUME] = c->step_host[2];
-  c->hs[MIBM_S_POS_CM][0] = c->step_host[3];
-  c->hs[MIBM_S_POS_CM][1] = c->step_host[4];
-  c->hs[MIBM_S_POS_CM][2] = c->step_host[5];
+  for (int d = 0; d < 3; ++d) c->hs[MIBM_S_POS_CM][d] = c->step_host[3 + d];
+  for (int q = 0; q < 9; ++q) c->hs[MIBM_S_INERT_TENSOR][q] = c->step_host[6 + q];
   if (c->S(MIBM_S_VOLUME) < c->S(MIBM_S_V_THRESH)) fail(c, MIBM_EABORT, "Geometry V/VE smaller than threshold");
 }
 
@@ -1849,6 +2129,7 @@ void lagr_free(Ctx* c) {
     if (g_lag[q]->c == c) {
       LagState* s = g_lag[q];
       cudaFree(s->adj_off); cudaFree(s->adj_face); cudaFree(s->face_part); cudaFree(s->geom_out);
+      cudaFree(s->loads_ev);
       cudaFree(s->mean3); cudaFree(s->sdf_bits); cudaFree(s->winner); cudaFree(s->dist_buf);
       cudaFree(s->band_ub); cudaFree(s->face4); cudaFree(s->face_cell); cudaFree(s->cm32);
       cudaFree(s->band_list); cudaFree(s->band_count);

@@ -1,0 +1,334 @@
+// rigid.cu -- moving body: newton_euler, calc_rot_matrix, update_part_pos /
+// update_xyz (RigidAuxRoutines.f90:1-306, 556-582, 818-868).
+//
+// The rigid-body state is a few dozen doubles, so the Newton-Euler update is
+// one device thread: it stays in the stream between the structural loads
+// and the geometry refresh of the same substep, and in a captured step graph,
+// with no host round trip.  Its inputs are the loads summed on the device
+// (lagr.cu), the geometry of the melted body (volume, centre of mass,
+// inertia tensor) and the state of the previous substep; its outputs feed
+// update_xyz (one thread per vertex / face) and the next substep's explicit
+// terms (pos_CM, vel_CM, omega_c in the substep parameters).
+//
+// Single particle and no collisions: update_substepping (RigidAuxRoutines.
+// f90:310-418) moves nothing unless `collision` flags a pair, which needs two
+// particles.  Compiled without FMA contraction, like the oracle.
+#include <cmath>
+#include <cstring>
+
+#include "common.cuh"
+
+namespace mibm {
+
+// In-place inverse of a 3x3 column-major matrix: LU with partial pivoting
+// (first maximal pivot, dgetrf) and inversion from the factors (dgetri).
+__device__ bool inv3(double* a) {
+  const int n = 3;
+  int ipiv[3];
+  for (int j = 0; j < n; ++j) {
+    int p = j;
+    double amax = fabs(a[j + n * j]);
+    for (int i = j + 1; i < n; ++i)
+      if (fabs(a[i + n * j]) > amax) { amax = fabs(a[i + n * j]); p = i; }
+    ipiv[j] = p;
+    if (a[p + n * j] == 0.0) return false;
+    if (p != j)
+      for (int cc = 0; cc < n; ++cc) { double t = a[j + n * cc]; a[j + n * cc] = a[p + n * cc]; a[p + n * cc] = t; }
+    double r = 1.0 / a[j + n * j];
+    for (int i = j + 1; i < n; ++i) a[i + n * j] *= r;
+    for (int cc = j + 1; cc < n; ++cc) {
+      double t = a[j + n * cc];
+      for (int i = j + 1; i < n; ++i) a[i + n * cc] -= t * a[i + n * j];
+    }
+  }
+  for (int j = 0; j < n; ++j) {
+    a[j + n * j] = 1.0 / a[j + n * j];
+    double ajj = -a[j + n * j];
+    for (int i = 0; i < j; ++i) {
+      double s = 0;
+      for (int k = i; k < j; ++k) s += a[i + n * k] * a[k + n * j];
+      a[i + n * j] = s;
+    }
+    for (int i = 0; i < j; ++i) a[i + n * j] *= ajj;
+  }
+  double work[3];
+  for (int j = n - 1; j >= 0; --j) {
+    for (int i = j + 1; i < n; ++i) { work[i] = a[i + n * j]; a[i + n * j] = 0.0; }
+    if (j < n - 1)
+      for (int i = 0; i < n; ++i) {
+        double s = 0;
+        for (int k = j + 1; k < n; ++k) s += a[i + n * k] * work[k];
+        a[i + n * j] -= s;
+      }
+  }
+  for (int j = n - 2; j >= 0; --j) {
+    int jp = ipiv[j];
+    if (jp != j)
+      for (int i = 0; i < n; ++i) { double t = a[i + n * j]; a[i + n * j] = a[i + n * jp]; a[i + n * jp] = t; }
+  }
+  return true;
+}
+
+// calc_rot_matrix (RigidAuxRoutines.f90:556-582): normalises q, AA column-major
+__device__ void rot_matrix(double q[4], double AA[9]) {
+  double norm = sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  for (int i = 0; i < 4; ++i) q[i] = q[i] / norm;
+  AA[0] = q[0] * q[0] + q[1] * q[1] - q[2] * q[2] - q[3] * q[3];
+  AA[3] = 2.0 * (q[1] * q[2] + q[0] * q[3]);
+  AA[6] = 2.0 * (q[1] * q[3] - q[0] * q[2]);
+  AA[1] = 2.0 * (q[1] * q[2] - q[0] * q[3]);
+  AA[4] = q[0] * q[0] - q[1] * q[1] + q[2] * q[2] - q[3] * q[3];
+  AA[7] = 2.0 * (q[2] * q[3] + q[0] * q[1]);
+  AA[2] = 2.0 * (q[1] * q[3] + q[0] * q[2]);
+  AA[5] = 2.0 * (q[2] * q[3] - q[0] * q[1]);
+  AA[8] = q[0] * q[0] - q[1] * q[1] - q[2] * q[2] + q[3] * q[3];
+}
+
+// newton_euler + the periodic wrap of update_part_pos.  geom: [.., .., Volume,
+// pos_CM(3), InertTensor(9)] of the body before the move.
+__global__ void newton_euler_kernel(const StepParams* __restrict__ pp, const double* __restrict__ geom,
+                                    double dens_ratio, double xlen, double ylen, double zlen, RigidDev* r,
+                                    int* __restrict__ flag) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double al = pp->al, ga = pp->ga, ro = pp->ro, dt = pp->dt;
+  const double Volume = geom[2];
+  double pos1[3] = {geom[3], geom[4], geom[5]};
+  double I[9];
+  for (int q = 0; q < 9; ++q) I[q] = geom[6 + q];
+  const double* prn = r->load; const double* tau = r->load + 3;
+  const double* rprn = r->load + 6; const double* rtau = r->load + 9;
+  const double* prn1 = r->load1; const double* tau1 = r->load1 + 3;
+  const double* rprn1 = r->load1 + 6; const double* rtau1 = r->load1 + 9;
+  const double e_z[3] = {0.0, 0.0, -1.0};
+  double vel1[3], om1[3], vel[3], pos[3], om[3] = {0, 0, 0}, quat[4] = {0, 0, 0, 0};
+  for (int d = 0; d < 3; ++d) { vel1[d] = r->vel[d]; om1[d] = r->om[d]; }
+  // translation, RigidAuxRoutines.f90:218-225
+  double pre_fac = 1.0 / Volume / dens_ratio;
+  for (int i = 0; i < 3; ++i)
+    vel[i] = vel1[i] + ga * dt * pre_fac * (-prn[i] + tau[i]) + ro * dt * pre_fac * (-prn1[i] + tau1[i]) +
+             al * dt * (1.0 - (1.0 / dens_ratio)) * e_z[i];
+  for (int i = 0; i < 3; ++i) pos[i] = pos1[i] + 0.5 * al * dt * (vel[i] + vel1[i]);
+  // rotation: iterative inertia-tensor update, RigidAuxRoutines.f90:243-296
+  const double tolerance = 1.e-15;
+  const int max_iter = 10000;
+  double I_LHS[9], I_prev[9], I_inv[9], AA[9], buf[9];
+  for (int q = 0; q < 9; ++q) I_LHS[q] = I[q];
+  double Iresidual = 1.0;
+  int n_iter = 1;
+  while (n_iter <= max_iter && Iresidual > tolerance) {
+    for (int q = 0; q < 9; ++q) I_inv[q] = I_LHS[q];
+    if (!inv3(I_inv)) { atomicOr(flag, 2); return; }
+    double rhs[3];
+    for (int i = 0; i < 3; ++i) {
+      double m = 0.0;
+      for (int j = 0; j < 3; ++j) m += I[i + 3 * j] * om1[j];
+      rhs[i] = m + ga * dt * (-rprn[i] + rtau[i]) + ro * dt * (-rprn1[i] + rtau1[i]);
+    }
+    for (int i = 0; i < 3; ++i) {
+      double m = 0.0;
+      for (int j = 0; j < 3; ++j) m += I_inv[i + 3 * j] * rhs[j];
+      om[i] = m;
+    }
+    double ob[3];
+    for (int i = 0; i < 3; ++i) ob[i] = 0.5 * (om[i] + om1[i]);
+    double magOM = sqrt(ob[0] * ob[0] + ob[1] * ob[1] + ob[2] * ob[2]);
+    double angle = magOM * al * dt;
+    if (magOM < tolerance) { ob[0] = 0.0; ob[1] = 0.0; ob[2] = 0.0; }
+    else for (int i = 0; i < 3; ++i) ob[i] = ob[i] / magOM;
+    double ch = cos(0.5 * angle), sh = sin(0.5 * angle);
+    quat[0] = ch; quat[1] = sh * ob[0]; quat[2] = sh * ob[1]; quat[3] = sh * ob[2];
+    double qn = sqrt(quat[0] * quat[0] + quat[1] * quat[1] + quat[2] * quat[2] + quat[3] * quat[3]);
+    for (int i = 0; i < 4; ++i) quat[i] = quat[i] / qn;
+    rot_matrix(quat, AA);
+    for (int q = 0; q < 9; ++q) I_prev[q] = I_LHS[q];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        double m = 0.0;
+        for (int k = 0; k < 3; ++k) m += I[i + 3 * k] * AA[j + 3 * k];
+        buf[i + 3 * j] = m;
+      }
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        double m = 0.0;
+        for (int k = 0; k < 3; ++k) m += AA[i + 3 * k] * buf[k + 3 * j];
+        I_LHS[i + 3 * j] = m;
+      }
+    Iresidual = 0.0;
+    for (int q = 0; q < 9; ++q) Iresidual = fmax(Iresidual, fabs(I_LHS[q] - I_prev[q]));
+    ++n_iter;
+  }
+  // periodicity corrections, RigidAuxRoutines.f90:40-51
+  const double L[3] = {xlen, ylen, zlen};
+  for (int d = 0; d < 3; ++d) {
+    if (pos[d] < 0.) pos[d] = pos[d] + L[d];
+    if (pos[d] > L[d]) pos[d] = pos[d] - L[d];
+  }
+  // update_xyz re-derives AA from the stored quaternion
+  rot_matrix(quat, AA);
+  for (int d = 0; d < 3; ++d) { r->vel[d] = vel[d]; r->om[d] = om[d]; }
+  for (int q = 0; q < 4; ++q) r->quat[q] = quat[q];
+  for (int q = 0; q < 9; ++q) { r->inert[q] = I_LHS[q]; r->xf[q] = AA[q]; }
+  for (int d = 0; d < 3; ++d) { r->xf[9 + d] = pos[d]; r->xf[12 + d] = pos1[d]; }
+  r->iters = n_iter - 1;
+}
+
+// update_xyz (RigidAuxRoutines.f90:818-868): vertices turned by AA^T about
+// the old centre and moved to the new one; face velocities vel_CM +
+// omega x (centroid - old centre) from the centroids before the move.
+__global__ void update_xyz_kernel(int nv, int nf, const int* __restrict__ ghostv, const int* __restrict__ ghostf,
+                                  const RigidDev* __restrict__ r, double* __restrict__ x,
+                                  const double* __restrict__ bar, double* __restrict__ vel_tri) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const double* AA = r->xf;
+  const double* pos = r->xf + 9;
+  const double* pos1 = r->xf + 12;
+  if (t < nv && !ghostv[t]) {
+    double d[3];
+    for (int k = 0; k < 3; ++k) d[k] = x[3 * t + k] - pos1[k];
+    for (int q = 0; q < 3; ++q) {
+      double m = 0.0;
+      for (int k = 0; k < 3; ++k) m += AA[k + 3 * q] * d[k];
+      x[3 * t + q] = m + pos[q];
+    }
+  }
+  if (t < nf && !ghostf[t]) {
+    double ds[3];
+    for (int k = 0; k < 3; ++k) ds[k] = bar[3 * t + k] - pos1[k];
+    const double* om = r->om;
+    double c0 = om[1] * ds[2] - ds[1] * om[2];
+    double c1 = om[2] * ds[0] - ds[2] * om[0];
+    double c2 = om[0] * ds[1] - ds[0] * om[1];
+    vel_tri[3 * t] = r->vel[0] + c0;
+    vel_tri[3 * t + 1] = r->vel[1] + c1;
+    vel_tri[3 * t + 2] = r->vel[2] + c2;
+  }
+}
+
+// calc_centroids_from_vert (triaux.f90:308-323)
+__global__ void centroid_kernel(int nf, const int* __restrict__ vof, const int* __restrict__ ghost,
+                                const double* __restrict__ x, double* __restrict__ bar) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nf || ghost[t]) return;
+  int a = vof[3 * t] - 1, b = vof[3 * t + 1] - 1, d = vof[3 * t + 2] - 1;
+  for (int k = 0; k < 3; ++k) bar[3 * t + k] = (x[3 * a + k] + x[3 * b + k] + x[3 * d + k]) / 3.0;
+}
+
+// After the geometry refresh: the inertia tensor of the moved body
+// (calc_rigidBody_params of the primitive geometry, particle.f90:189) and
+// the centre of mass / velocities the next substep's explicit terms read.
+__global__ void publish_kernel(const double* __restrict__ geom, RigidDev* r, StepParams* next) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  for (int q = 0; q < 9; ++q) r->inert[q] = geom[6 + q];
+  if (next) {
+    for (int d = 0; d < 3; ++d) {
+      next->pos[d] = geom[3 + d];
+      next->vel[d] = r->vel[d];
+      next->om[d] = r->om[d];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------
+bool rigid_ensure(Ctx* c) {
+  if (c->drigid) return true;
+  if (!cuda_ok(c, cudaMalloc(&c->drigid, sizeof(RigidDev)), "rigid")) return false;
+  if (!cuda_ok(c, cudaMallocHost((void**)&c->hrigid_in, sizeof(RigidDev)), "rigid")) return false;
+  if (!cuda_ok(c, cudaMallocHost((void**)&c->hrigid_out, sizeof(RigidDev)), "rigid")) return false;
+  memset(c->hrigid_in, 0, sizeof(RigidDev));
+  memset(c->hrigid_out, 0, sizeof(RigidDev));
+  return true;
+}
+
+static const int kLoadIds[4] = {MIBM_S_INT_PRN_DA, MIBM_S_INT_TAU_DA, MIBM_S_INT_R_X_PRN_DA, MIBM_S_INT_R_X_TAU_DA};
+static const int kLoad1Ids[4] = {MIBM_S_INT_PRN_DA_M1, MIBM_S_INT_TAU_DA_M1, MIBM_S_INT_R_X_PRN_DA_M1,
+                                 MIBM_S_INT_R_X_TAU_DA_M1};
+static const int kAccIds[4] = {MIBM_S_FP, MIBM_S_FTAU, MIBM_S_TORQ_P, MIBM_S_TORQ_TAU};
+
+// registered module state -> h.  geom_from_scalars: Volume, pos_CM and
+// InertTensor as the drop-in update_part_pos_ reads them.
+void rigid_pack(Ctx* c, RigidDev* h, bool geom_from_scalars) {
+  for (int d = 0; d < 3; ++d) { h->vel[d] = c->hs[MIBM_S_VEL_CM][d]; h->om[d] = c->hs[MIBM_S_OMEGA_C][d]; }
+  for (int q = 0; q < 4; ++q) h->quat[q] = c->hs[MIBM_S_QUAT][q];
+  for (int b = 0; b < 4; ++b)
+    for (int d = 0; d < 3; ++d) {
+      h->load[3 * b + d] = c->hs[kLoadIds[b]][d];
+      h->load1[3 * b + d] = c->hs[kLoad1Ids[b]][d];
+      h->acc[3 * b + d] = c->hs[kAccIds[b]][d];
+    }
+  for (int q = 0; q < 9; ++q) h->inert[q] = c->hs[MIBM_S_INERT_TENSOR][q];
+  if (geom_from_scalars) {
+    for (int q = 0; q < 16; ++q) h->geom_in[q] = 0.0;
+    h->geom_in[2] = c->S(MIBM_S_VOLUME);
+    for (int d = 0; d < 3; ++d) h->geom_in[3 + d] = c->hs[MIBM_S_POS_CM][d];
+    for (int q = 0; q < 9; ++q) h->geom_in[6 + q] = c->hs[MIBM_S_INERT_TENSOR][q];
+  }
+}
+
+// h -> registered module state.  pos_from_motion: pos_CM is the
+// Newton-Euler result (the drop-in update_part_pos_); otherwise the caller
+// sets it from the refreshed geometry.
+void rigid_unpack(Ctx* c, const RigidDev* h, bool pos_from_motion) {
+  for (int d = 0; d < 3; ++d) { c->hs[MIBM_S_VEL_CM][d] = h->vel[d]; c->hs[MIBM_S_OMEGA_C][d] = h->om[d]; }
+  for (int q = 0; q < 4; ++q) c->hs[MIBM_S_QUAT][q] = h->quat[q];
+  for (int b = 0; b < 4; ++b)
+    for (int d = 0; d < 3; ++d) {
+      c->hs[kLoadIds[b]][d] = h->load[3 * b + d];
+      c->hs[kLoad1Ids[b]][d] = h->load1[3 * b + d];
+      c->hs[kAccIds[b]][d] = h->acc[3 * b + d];
+    }
+  for (int q = 0; q < 9; ++q) c->hs[MIBM_S_INERT_TENSOR][q] = h->inert[q];
+  if (pos_from_motion)
+    for (int d = 0; d < 3; ++d) c->hs[MIBM_S_POS_CM][d] = h->xf[9 + d];
+}
+
+// stream-ordered copies through the pinned blocks (captured into step graphs)
+void rigid_upload(Ctx* c) {
+  cudaMemcpyAsync(c->drigid, c->hrigid_in, sizeof(RigidDev), cudaMemcpyHostToDevice, c->stream);
+}
+void rigid_download(Ctx* c) {
+  cudaMemcpyAsync(c->hrigid_out, c->drigid, sizeof(RigidDev), cudaMemcpyDeviceToHost, c->stream);
+}
+
+void k_newton_euler(Ctx* c, const StepParams* dp, const double* geom) {
+  { MIBM_PROF(c, "newton_euler");
+    newton_euler_kernel<<<1, 32, 0, c->stream>>>(dp, geom, c->S(MIBM_S_DENS_RATIO), c->g.xlen, c->g.ylen,
+                                                 c->g.zlen, c->drigid, c->dflag); }
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "newton_euler");
+}
+
+void k_update_xyz(Ctx* c, bool centroids) {
+  int n = std::max(c->maxnv, c->maxnf);
+  if (n == 0) return;
+  { MIBM_PROF(c, "update_xyz");
+    update_xyz_kernel<<<div_up(n, 128), 128, 0, c->stream>>>(
+        c->maxnv, c->maxnf, (const int*)c->dm[MIBM_M_GHOST_VERT], (const int*)c->dm[MIBM_M_GHOST_FACE], c->drigid,
+        (double*)c->dm[MIBM_M_XYZV], (const double*)c->dm[MIBM_M_TRI_BAR], (double*)c->dm[MIBM_M_VEL_TRI]); }
+  ++c->launches;
+  if (centroids && c->maxnf > 0) {
+    MIBM_PROF(c, "centroids");
+    centroid_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(
+        c->maxnf, (const int*)c->dm[MIBM_M_VERT_OF_FACE], (const int*)c->dm[MIBM_M_GHOST_FACE],
+        (const double*)c->dm[MIBM_M_XYZV], (double*)c->dm[MIBM_M_TRI_BAR]);
+    ++c->launches;
+  }
+  MIBM_LAUNCH_CHECK(c, "update_xyz");
+}
+
+void k_rigid_publish(Ctx* c, const double* geom, StepParams* next) {
+  { MIBM_PROF(c, "rigid_publish");
+    publish_kernel<<<1, 32, 0, c->stream>>>(geom, c->drigid, next); }
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "rigid_publish");
+}
+
+void rigid_free(Ctx* c) {
+  cudaFree(c->drigid);
+  if (c->hrigid_in) cudaFreeHost(c->hrigid_in);
+  if (c->hrigid_out) cudaFreeHost(c->hrigid_out);
+  c->drigid = nullptr; c->hrigid_in = nullptr; c->hrigid_out = nullptr;
+}
+
+}  // namespace mibm

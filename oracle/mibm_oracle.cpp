@@ -125,7 +125,10 @@ thread_local std::string t_msg;
 
 void fail(Ctx* c, int st, const std::string& m) {
   t_status = st; t_msg = m;
-  if (c) { c->status = st; c->msg = m; }
+  if (c) {
+#pragma omp critical(mibm_oracle_fail)
+    { c->status = st; c->msg = m; }
+  }
 }
 
 Ctx* cur() {
@@ -955,15 +958,25 @@ void findProbeIndices(Ctx& c) {
   }
 }
 
-// wght_gradT, mls_heatFlux.f90:161-376
-void wght_gradT(Ctx& c, const double pos[3], const double ptx[4], double gradT[3], const int probe_inds[3]) {
-  const F3& temp = c.f[MIBM_F_TEMP];
+// MLS gradient at a probe, the common body of wght_gradT
+// (mls_heatFlux.f90:161-376) and wght_gradP/U/V/W (mls_structLoads.f90:406-
+// 1298): cage i, j around probe_inds(1:2); z layers k_inds = [k1-1,k1,k1]
+// (the repeated layer of mls_heatFlux.f90:213 / mls_structLoads.f90:459) with
+// k1 = floor(pos3*dx3)+1, or nint for the w-velocity (mls_structLoads.f90:
+// 1127); coordinates per axis from the field's staggering (cx/cy/cz: true =
+// face coordinates xc/yc/zc, false = centres xm/ym/zm); field values at the
+// wrapped cage, z from keul = [k1w-1,k1w,k1w+1] (ghost planes of the field).
+void wght_grad_field(Ctx& c, const double pos[3], const double ptx[4], double grad[3], const int probe_inds[3],
+                     const F3& field, bool cx, bool cy, bool cz, bool knint) {
   double wcon = c.S(MIBM_S_WCON), wscl = c.S(MIBM_S_WSCL);
   const double eps = 2.220446049250313e-16;   // EPSILON(1.0d0)
+  auto X = [&](int i) { return cx ? c.xc(i) : c.xm(i); };
+  auto Y = [&](int j) { return cy ? c.yc(j) : c.ym(j); };
+  auto Z = [&](int k) { return cz ? c.zc(k) : c.zm(k); };
   int pi1 = probe_inds[0] - 1, po1 = probe_inds[0] + 1;
   int pi2 = probe_inds[1] - 1, po2 = probe_inds[1] + 1;
-  int k1 = f_floor(pos[2] * c.dx3) + 1;
-  int k_inds[3] = {k1 - 1, k1, k1};           // spatial-grid quirk (mls_heatFlux.f90:213)
+  int k1 = knint ? f_nint(pos[2] * c.dx3) + 1 : f_floor(pos[2] * c.dx3) + 1;
+  int k_inds[3] = {k1 - 1, k1, k1};
   int k1w = f_modulo(k1 - 1, c.n3m) + 1;
   int keul[3] = {k1w - 1, k1w, k1w + 1};
   double A[16] = {0}, dAdx[16] = {0}, dAdy[16] = {0}, dAdz[16] = {0};
@@ -971,33 +984,33 @@ void wght_gradT(Ctx& c, const double pos[3], const double ptx[4], double gradT[3
   int inw = 0;
   for (int nk = 0; nk < 3; ++nk) {
     int k = k_inds[nk];
-    double norp3 = std::fabs(pos[2] - c.zm(k)) / (wscl / c.dx3);
+    double norp3 = std::fabs(pos[2] - Z(k)) / (wscl / c.dx3);
     double Wt3 = mls_gaussian(norp3, wcon), dWz_dz;
     if (norp3 < eps) dWz_dz = 0.0;
     else {
       dWz_dz = mls_gauss_deriv(norp3, wcon);
-      dWz_dz = dWz_dz * ((pos[2] - c.zm(k)) / std::fabs(pos[2] - c.zm(k)) / (wscl / c.dx3));
+      dWz_dz = dWz_dz * ((pos[2] - Z(k)) / std::fabs(pos[2] - Z(k)) / (wscl / c.dx3));
     }
     for (int j = pi2; j <= po2; ++j) {
-      double norp2 = std::fabs(pos[1] - c.ym(j)) / (wscl / c.dx2);
+      double norp2 = std::fabs(pos[1] - Y(j)) / (wscl / c.dx2);
       double Wt2 = mls_gaussian(norp2, wcon);
       double Wt23 = Wt2 * Wt3, dWy_dy;
       (void)Wt23;
       if (norp2 < eps) dWy_dy = 0.0;
       else {
         dWy_dy = mls_gauss_deriv(norp2, wcon);
-        dWy_dy = dWy_dy * ((pos[1] - c.ym(j)) / std::fabs(pos[1] - c.ym(j)) / (wscl / c.dx2));
+        dWy_dy = dWy_dy * ((pos[1] - Y(j)) / std::fabs(pos[1] - Y(j)) / (wscl / c.dx2));
       }
       for (int i = pi1; i <= po1; ++i) {
-        double norp1 = std::fabs(pos[0] - c.xm(i)) / (wscl / c.dx1);
+        double norp1 = std::fabs(pos[0] - X(i)) / (wscl / c.dx1);
         double Wt1 = mls_gaussian(norp1, wcon);
         double Wtx = Wt1 * Wt23, dWx_dx;
         if (norp1 < eps) dWx_dx = 0.0;
         else {
           dWx_dx = mls_gauss_deriv(norp1, wcon);
-          dWx_dx = dWx_dx * ((pos[0] - c.xm(i)) / std::fabs(pos[0] - c.xm(i)) / (wscl / c.dx1));
+          dWx_dx = dWx_dx * ((pos[0] - X(i)) / std::fabs(pos[0] - X(i)) / (wscl / c.dx1));
         }
-        double pxk[4] = {1.0, c.xm(i), c.ym(j), c.zm(k)};
+        double pxk[4] = {1.0, X(i), Y(j), Z(k)};
         for (int cc = 0; cc < 4; ++cc) {
           double t = Wtx * pxk[cc];
           for (int r = 0; r < 4; ++r) A[r + 4 * cc] = A[r + 4 * cc] + t * pxk[r];
@@ -1022,12 +1035,12 @@ void wght_gradT(Ctx& c, const double pos[3], const double ptx[4], double gradT[3
         int ii = f_modulo(i - 1, c.n1m) + 1;
         int jj = f_modulo(j - 1, c.n2m) + 1;
         int kk = keul[nk];
-        Tnel[inw] = temp(ii, jj, kk);
+        Tnel[inw] = field(ii, jj, kk);
         ++inw;
       }
     }
   }
-  if (lu_inverse(A, 4) != 0) { fail(&c, MIBM_ENUMERIC, "Error in dgetrf (wght_gradT)"); return; }
+  if (lu_inverse(A, 4) != 0) { fail(&c, MIBM_ENUMERIC, "Error in dgetrf (MLS gradient)"); return; }
   double gam[4];
   for (int r = 0; r < 4; ++r) {                  // DGEMV('N', invA, ptx)
     double t = 0;
@@ -1057,8 +1070,13 @@ void wght_gradT(Ctx& c, const double pos[3], const double ptx[4], double gradT[3
       for (int r = 0; r < 4; ++r) t2 += gam[r] * dB[d][r + 4 * n];
       g += (t1 + t2) * Tnel[n];
     }
-    gradT[d] = g;
+    grad[d] = g;
   }
+}
+
+// wght_gradT, mls_heatFlux.f90:161-376
+void wght_gradT(Ctx& c, const double pos[3], const double ptx[4], double gradT[3], const int probe_inds[3]) {
+  wght_grad_field(c, pos, ptx, gradT, probe_inds, c.f[MIBM_F_TEMP], false, false, false, false);
 }
 
 void mls_heatFlux(Ctx& c) {   // mls_heatFlux.f90:77-158
@@ -1341,8 +1359,270 @@ void tagCells(Ctx& c) {   // tagCells.f90:4-27 with tagType = 1, initial_tag = .
 }
 
 // ------------------------------------------------------------------------
-// particle.f90:1-230 (single particle; remeshing and Newton-Euler are
-// outside this build's scope and are skipped when their flags are off)
+// Moving body: mls_structLoads.f90:1-1298, RigidAuxRoutines.f90:1-640
+// ------------------------------------------------------------------------
+// wght_press, mls_structLoads.f90:271-404: MLS value of pr at the probe.  The
+// z cage is k1-1..k1+1 (no repeated layer) at zm, x/y at xm/ym around
+// probe_inds(1:2); values from the wrapped cage, z from keul.
+double wght_press(Ctx& c, const double pos[3], const double ptx[4], const int probe_inds[3]) {
+  int k1 = f_floor(pos[2] * c.dx3) + 1;
+  double ptxAB[27];
+  if (!mls_shape(c, pos, ptx, probe_inds[0], probe_inds[1], k1, GX_M, GX_M, GX_M, ptxAB)) {
+    fail(&c, MIBM_ENUMERIC, "Error in dgetrf (wght_press)");
+    return 0.0;
+  }
+  int k1w = f_modulo(k1 - 1, c.n3m) + 1;
+  int keul[3] = {k1w - 1, k1w, k1w + 1};
+  const F3& pr = c.f[MIBM_F_PR];
+  double press_probe = 0.0;
+  int inw = 0;
+  for (int kk = 0; kk < 3; ++kk)
+    for (int j = probe_inds[1] - 1; j <= probe_inds[1] + 1; ++j) {
+      int jj = f_modulo(j - 1, c.n2m) + 1;
+      for (int i = probe_inds[0] - 1; i <= probe_inds[0] + 1; ++i) {
+        int ii = f_modulo(i - 1, c.n1m) + 1;
+        press_probe = press_probe + pr(ii, jj, keul[kk]) * ptxAB[inw];
+        ++inw;
+      }
+    }
+  return press_probe;
+}
+
+inline void cross3(double r[3], const double x[3], const double y[3]) {   // triaux.f90:385-393
+  r[0] = x[1] * y[2] - y[1] * x[2];
+  r[1] = x[2] * y[0] - y[2] * x[0];
+  r[2] = x[0] * y[1] - y[0] * x[1];
+}
+
+// mls_structLoads, mls_structLoads.f90:1-269 (one particle, one rank).
+// Per face: the positive probe, pressure extrapolated back to the face
+// (P(X) = P(x_p) - h dP/dn), the normal viscous stress from the velocity
+// gradients (U, V at the cell-centred z layer; W at the staggered one), and
+// their moments about pos_CM; summed over all faces in face order.
+void mls_structLoads(Ctx& c) {
+  double* prn = c.s[MIBM_S_INT_PRN_DA];
+  double* tau = c.s[MIBM_S_INT_TAU_DA];
+  double* rprn = c.s[MIBM_S_INT_R_X_PRN_DA];
+  double* rtau = c.s[MIBM_S_INT_R_X_TAU_DA];
+  for (int d = 0; d < 3; ++d) {
+    c.s[MIBM_S_INT_PRN_DA_M1][d] = prn[d];
+    c.s[MIBM_S_INT_TAU_DA_M1][d] = tau[d];
+    c.s[MIBM_S_INT_R_X_PRN_DA_M1][d] = rprn[d];
+    c.s[MIBM_S_INT_R_X_TAU_DA_M1][d] = rtau[d];
+  }
+  const int nf_ = c.maxnf;
+  std::vector<double> press_n(3 * (size_t)nf_, 0.0), r_x_prn(3 * (size_t)nf_, 0.0);
+  std::vector<double> tau_n(3 * (size_t)nf_, 0.0), r_x_tau(3 * (size_t)nf_, 0.0);
+  double h = c.S(MIBM_S_H_EULERIAN), ren = c.S(MIBM_S_REN);
+  const double* pcm = c.s[MIBM_S_POS_CM];
+#pragma omp parallel for schedule(static)
+  for (int nf = 1; nf <= nf_; ++nf) {
+    if (c.ghostf(nf)) continue;
+    double nrm[3] = {c.tri_nor(1, nf), c.tri_nor(2, nf), c.tri_nor(3, nf)};
+    double s = norm3(nrm[0], nrm[1], nrm[2]);
+    double pos[3], rad[3];
+    for (int d = 0; d < 3; ++d) {
+      pos[d] = c.tri_bar(d + 1, nf) + h * nrm[d] / s;
+      rad[d] = c.tri_bar(d + 1, nf) - pcm[d];
+    }
+    int kcent = f_floor(pos[2] * c.dx3) + 1, kstag = f_nint(pos[2] * c.dx3) + 1;
+    kcent = f_modulo(kcent - 1, c.n3m) + 1;
+    kstag = f_modulo(kstag - 1, c.n3m) + 1;
+    double ptx[4] = {1.0, pos[0], pos[1], pos[2]};
+    int jcent = f_floor(pos[1] * c.dx2) + 1, jstag = f_nint(pos[1] * c.dx2) + 1;
+    int icent = f_floor(pos[0] * c.dx1) + 1, istag = f_nint(pos[0] * c.dx1) + 1;
+    double sur = c.sur(nf);
+    // pressure: cell-centred cage
+    int pc[3] = {icent, jcent, kcent};
+    double press_probe = wght_press(c, pos, ptx, pc);
+    double gradP[3] = {0, 0, 0};
+    wght_grad_field(c, pos, ptx, gradP, pc, c.f[MIBM_F_PR], false, false, false, false);
+    double press_tri = press_probe - h * (gradP[0] * nrm[0] + gradP[1] * nrm[1] + gradP[2] * nrm[2]);
+    double pn[3], buf[3];
+    for (int d = 0; d < 3; ++d) {
+      press_n[3 * (size_t)(nf - 1) + d] = press_tri * sur * nrm[d];
+      pn[d] = press_tri * nrm[d];
+    }
+    cross3(buf, rad, pn);
+    for (int d = 0; d < 3; ++d) r_x_prn[3 * (size_t)(nf - 1) + d] = buf[d] * sur;
+    // U and V gradients
+    double gU[3] = {0, 0, 0}, gV[3] = {0, 0, 0}, gW[3] = {0, 0, 0};
+    int pu[3] = {istag, jcent, kcent}, pv[3] = {icent, jstag, kcent}, pw[3] = {icent, jcent, kstag};
+    wght_grad_field(c, pos, ptx, gU, pu, c.f[MIBM_F_VX], true, false, false, false);
+    wght_grad_field(c, pos, ptx, gV, pv, c.f[MIBM_F_VY], false, true, false, false);
+    double S11 = gU[0], S12 = gU[1], S13 = gU[2], S21 = gV[0], S22 = gV[1], S23 = gV[2];
+    double sr = sur / ren;
+    double t1 = sr * (2.0 * S11 * nrm[0] + (S12 + S21) * nrm[1] + S13 * nrm[2]);
+    double t2 = sr * ((S21 + S12) * nrm[0] + 2.0 * S22 * nrm[1] + S23 * nrm[2]);
+    double t3 = sr * (S13 * nrm[0] + S23 * nrm[1]);
+    double* tn = &tau_n[3 * (size_t)(nf - 1)];
+    double* rt = &r_x_tau[3 * (size_t)(nf - 1)];
+    double tv[3] = {t1, t2, t3};
+    for (int d = 0; d < 3; ++d) tn[d] = tn[d] + tv[d];
+    cross3(buf, rad, tv);
+    for (int d = 0; d < 3; ++d) rt[d] = rt[d] + buf[d];
+    // W gradients: staggered z layer
+    wght_grad_field(c, pos, ptx, gW, pw, c.f[MIBM_F_VZ], false, false, true, true);
+    double S31 = gW[0], S32 = gW[1], S33 = gW[2];
+    tv[0] = sr * (S31 * nrm[2]);
+    tv[1] = sr * (S32 * nrm[2]);
+    tv[2] = sr * (S31 * nrm[0] + S32 * nrm[1] + 2.0 * S33 * nrm[2]);
+    for (int d = 0; d < 3; ++d) tn[d] = tn[d] + tv[d];
+    cross3(buf, rad, tv);
+    for (int d = 0; d < 3; ++d) rt[d] = rt[d] + buf[d];
+  }
+  if (c.status != MIBM_OK) return;
+  for (int d = 0; d < 3; ++d) {
+    double a = 0, b = 0, e = 0, f = 0;
+    for (int nf = 0; nf < nf_; ++nf) {
+      a += press_n[3 * (size_t)nf + d]; b += r_x_prn[3 * (size_t)nf + d];
+      e += tau_n[3 * (size_t)nf + d]; f += r_x_tau[3 * (size_t)nf + d];
+    }
+    prn[d] = a; rprn[d] = b; tau[d] = e; rtau[d] = f;
+    c.s[MIBM_S_FP][d] = c.s[MIBM_S_FP][d] + prn[d];
+    c.s[MIBM_S_FTAU][d] = c.s[MIBM_S_FTAU][d] + tau[d];
+    c.s[MIBM_S_TORQ_P][d] = c.s[MIBM_S_TORQ_P][d] + rprn[d];
+    c.s[MIBM_S_TORQ_TAU][d] = c.s[MIBM_S_TORQ_TAU][d] + rtau[d];
+  }
+}
+
+// calc_rot_matrix, RigidAuxRoutines.f90:556-582 (normalises quat in place;
+// AA column-major: body = AA space)
+void calc_rot_matrix(double q[4], double AA[9]) {
+  double norm = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  for (int i = 0; i < 4; ++i) q[i] = q[i] / norm;
+  auto A = [&](int r, int cc) -> double& { return AA[(r - 1) + 3 * (cc - 1)]; };
+  A(1, 1) = q[0] * q[0] + q[1] * q[1] - q[2] * q[2] - q[3] * q[3];
+  A(1, 2) = 2.0 * (q[1] * q[2] + q[0] * q[3]);
+  A(1, 3) = 2.0 * (q[1] * q[3] - q[0] * q[2]);
+  A(2, 1) = 2.0 * (q[1] * q[2] - q[0] * q[3]);
+  A(2, 2) = q[0] * q[0] - q[1] * q[1] + q[2] * q[2] - q[3] * q[3];
+  A(2, 3) = 2.0 * (q[2] * q[3] + q[0] * q[1]);
+  A(3, 1) = 2.0 * (q[1] * q[3] + q[0] * q[2]);
+  A(3, 2) = 2.0 * (q[2] * q[3] - q[0] * q[1]);
+  A(3, 3) = q[0] * q[0] - q[1] * q[1] - q[2] * q[2] + q[3] * q[3];
+}
+
+// newton_euler, RigidAuxRoutines.f90:128-306: translation with the RK3
+// weights on the surface loads plus buoyancy along -z; rotation by the
+// iterative inertia-tensor update of Ardekani et al. (2016): omega from the
+// current estimate of the rotated tensor, quaternion of the axis-angle
+// rotation 0.5 (omega + omega_m1) al dt, tensor rotated by that quaternion,
+// until the tensor changes by at most 1e-15 (10000 iterations at most).
+// I_ij (column-major) is replaced by the rotated tensor.
+void newton_euler(Ctx& c, const double prn[3], const double tau[3], const double prn1[3], const double tau1[3],
+                  const double rprn[3], const double rtau[3], const double rprn1[3], const double rtau1[3],
+                  double vel[3], const double vel1[3], double pos[3], const double pos1[3], double om[3],
+                  const double om1[3], double I[9], double quat[4], double Volume) {
+  double al = c.S(MIBM_S_AL), ga = c.S(MIBM_S_GA), ro = c.S(MIBM_S_RO), dt = c.S(MIBM_S_DT);
+  double dens_ratio = c.S(MIBM_S_DENS_RATIO);
+  const double e_z[3] = {0.0, 0.0, -1.0};
+  double pre_fac = 1.0 / Volume / dens_ratio;
+  for (int i = 0; i < 3; ++i)
+    vel[i] = vel1[i] + ga * dt * pre_fac * (-prn[i] + tau[i]) + ro * dt * pre_fac * (-prn1[i] + tau1[i]) +
+             al * dt * (1.0 - (1.0 / dens_ratio)) * e_z[i];
+  for (int i = 0; i < 3; ++i) pos[i] = pos1[i] + 0.5 * al * dt * (vel[i] + vel1[i]);
+  const double tolerance = 1.e-15;
+  const int max_iter = 10000;
+  double I_LHS[9], I_prev[9], I_inv[9], AA[9], buf[9];
+  for (int q = 0; q < 9; ++q) I_LHS[q] = I[q];
+  double Iresidual = 1.0;
+  int n_iter = 1;
+  while (n_iter <= max_iter && Iresidual > tolerance) {
+    for (int q = 0; q < 9; ++q) I_inv[q] = I_LHS[q];
+    if (lu_inverse(I_inv, 3) != 0) { fail(&c, MIBM_ENUMERIC, "Error in dgetrf for I_inv calculation"); return; }
+    double rhs[3];
+    for (int i = 0; i < 3; ++i) {
+      double m = 0.0;
+      for (int j = 0; j < 3; ++j) m += I[i + 3 * j] * om1[j];
+      rhs[i] = m + ga * dt * (-rprn[i] + rtau[i]) + ro * dt * (-rprn1[i] + rtau1[i]);
+    }
+    for (int i = 0; i < 3; ++i) {
+      double m = 0.0;
+      for (int j = 0; j < 3; ++j) m += I_inv[i + 3 * j] * rhs[j];
+      om[i] = m;
+    }
+    double ob[3];
+    for (int i = 0; i < 3; ++i) ob[i] = 0.5 * (om[i] + om1[i]);
+    double magOM = norm3(ob[0], ob[1], ob[2]);
+    double angle = magOM * al * dt;
+    if (magOM < tolerance) ob[0] = ob[1] = ob[2] = 0.0;
+    else for (int i = 0; i < 3; ++i) ob[i] = ob[i] / magOM;
+    double ch = std::cos(0.5 * angle), sh = std::sin(0.5 * angle);
+    quat[0] = ch; quat[1] = sh * ob[0]; quat[2] = sh * ob[1]; quat[3] = sh * ob[2];
+    double qn = std::sqrt(quat[0] * quat[0] + quat[1] * quat[1] + quat[2] * quat[2] + quat[3] * quat[3]);
+    for (int i = 0; i < 4; ++i) quat[i] = quat[i] / qn;
+    calc_rot_matrix(quat, AA);
+    for (int q = 0; q < 9; ++q) I_prev[q] = I_LHS[q];
+    for (int i = 0; i < 3; ++i)             // buffer = I_ij AA^T
+      for (int j = 0; j < 3; ++j) {
+        double m = 0.0;
+        for (int k = 0; k < 3; ++k) m += I[i + 3 * k] * AA[j + 3 * k];
+        buf[i + 3 * j] = m;
+      }
+    for (int i = 0; i < 3; ++i)             // I_LHS = AA buffer
+      for (int j = 0; j < 3; ++j) {
+        double m = 0.0;
+        for (int k = 0; k < 3; ++k) m += AA[i + 3 * k] * buf[k + 3 * j];
+        I_LHS[i + 3 * j] = m;
+      }
+    Iresidual = 0.0;
+    for (int q = 0; q < 9; ++q) Iresidual = std::max(Iresidual, std::fabs(I_LHS[q] - I_prev[q]));
+    ++n_iter;
+  }
+  for (int q = 0; q < 9; ++q) I[q] = I_LHS[q];
+}
+
+// update_part_pos + update_regular + update_xyz, RigidAuxRoutines.f90:1-126
+// and 818-868.  Collisions (coll.f90) never fire for one particle and
+// update_substepping then leaves the state unchanged.
+void update_part_pos(Ctx& c) {
+  double* pos = c.s[MIBM_S_POS_CM];
+  double* vel = c.s[MIBM_S_VEL_CM];
+  double* om = c.s[MIBM_S_OMEGA_C];
+  std::vector<double> dxyzv(3 * (size_t)c.maxnv, 0.0), dxyz(3 * (size_t)c.maxnf, 0.0);
+  for (int i = 1; i <= c.maxnv; ++i)
+    if (!c.ghostv(i))
+      for (int d = 0; d < 3; ++d) dxyzv[3 * (size_t)(i - 1) + d] = c.xyzv(d + 1, i) - pos[d];
+  for (int i = 1; i <= c.maxnf; ++i)
+    if (!c.ghostf(i))
+      for (int d = 0; d < 3; ++d) dxyz[3 * (size_t)(i - 1) + d] = c.tri_bar(d + 1, i) - pos[d];
+  double vel1[3], pos1[3], om1[3];
+  for (int d = 0; d < 3; ++d) { vel1[d] = vel[d]; pos1[d] = pos[d]; om1[d] = om[d]; }
+  newton_euler(c, c.s[MIBM_S_INT_PRN_DA], c.s[MIBM_S_INT_TAU_DA], c.s[MIBM_S_INT_PRN_DA_M1],
+               c.s[MIBM_S_INT_TAU_DA_M1], c.s[MIBM_S_INT_R_X_PRN_DA], c.s[MIBM_S_INT_R_X_TAU_DA],
+               c.s[MIBM_S_INT_R_X_PRN_DA_M1], c.s[MIBM_S_INT_R_X_TAU_DA_M1], vel, vel1, pos, pos1, om, om1,
+               c.s[MIBM_S_INERT_TENSOR], c.s[MIBM_S_QUAT], c.S(MIBM_S_VOLUME));
+  if (c.status != MIBM_OK) return;
+  const double L[3] = {c.xlen, c.ylen, c.zlen};
+  for (int d = 0; d < 3; ++d) {
+    if (pos[d] < 0.) pos[d] = pos[d] + L[d];
+    if (pos[d] > L[d]) pos[d] = pos[d] - L[d];
+  }
+  // update_xyz
+  double AA[9];
+  calc_rot_matrix(c.s[MIBM_S_QUAT], AA);
+  for (int i = 1; i <= c.maxnv; ++i) {
+    if (c.ghostv(i)) continue;
+    const double* dv = &dxyzv[3 * (size_t)(i - 1)];
+    for (int r = 0; r < 3; ++r) {
+      double m = 0.0;
+      for (int k = 0; k < 3; ++k) m += AA[k + 3 * r] * dv[k];   // AA^T dxyzv_s
+      c.xyzv(r + 1, i) = m + pos[r];
+    }
+  }
+  calc_centroids_from_vert(c);
+  for (int i = 1; i <= c.maxnf; ++i) {
+    if (c.ghostf(i)) continue;
+    double omd[3];
+    cross3(omd, om, &dxyz[3 * (size_t)(i - 1)]);
+    for (int d = 0; d < 3; ++d) c.vel_tri(d + 1, i) = vel[d] + omd[d];
+  }
+}
+
+// ------------------------------------------------------------------------
+// particle.f90:1-230 (single particle; remeshing is outside this build's
+// scope and is skipped when its flag is off)
 // ------------------------------------------------------------------------
 void geometry_refresh(Ctx& c) {   // particle.f90:165-193
   c.S(MIBM_S_SURFACE) = calculate_area(c);
@@ -1351,8 +1631,7 @@ void geometry_refresh(Ctx& c) {   // particle.f90:165-193
   calculate_vert_area(c);
   c.S(MIBM_S_VOLUME) = calculate_volume(c);
   calculate_areaWeighted_vert_normal(c);
-  double I[9];
-  calc_rigidBody_params(c, c.s[MIBM_S_POS_CM], c.S(MIBM_S_VOLUME), I);
+  calc_rigidBody_params(c, c.s[MIBM_S_POS_CM], c.S(MIBM_S_VOLUME), c.s[MIBM_S_INERT_TENSOR]);
   if (c.I(MIBM_I_IMELT) == 1) {
     double h = c.S(MIBM_S_H_EULERIAN), cv = c.S(MIBM_S_CELVOL);
     for (int t = 1; t <= c.maxnf; ++t) c.cfac(t) = (c.sur(t) * h) / cv;
@@ -1370,6 +1649,7 @@ void particle(Ctx& c) {
   }
   mlsForce(c);
   if (c.I(MIBM_I_IMELT) == 1) { findProbeIndices(c); mls_heatFlux(c); }
+  if (c.I(MIBM_I_IMLSSTR) == 1) { mls_structLoads(c); if (c.status != MIBM_OK) return; }
   velforce(c);
   tempforce(c);
   update_both_ghosts(c, c.f[MIBM_F_VX], c.n2);
@@ -1379,6 +1659,13 @@ void particle(Ctx& c) {
   if (c.I(MIBM_I_IMELT) == 1) {
     apply_StefanCondition(c);
     c.S(MIBM_S_VOLUME) = calculate_volume(c);
+  }
+  if (c.I(MIBM_I_IMLSSTR) == 1) {          // particle.f90:108-129
+    calc_centroids_from_vert(c);
+    update_tri_normal(c);
+    calc_rigidBody_params(c, c.s[MIBM_S_POS_CM], c.S(MIBM_S_VOLUME), c.s[MIBM_S_INERT_TENSOR]);
+    update_part_pos(c);
+    if (c.status != MIBM_OK) return;
   }
   geometry_refresh(c);
   if (c.S(MIBM_S_VOLUME) < c.S(MIBM_S_V_THRESH)) fail(&c, MIBM_EABORT, "Geometry V/VE smaller than threshold");
@@ -1909,6 +2196,8 @@ DROPIN(mls_heatflux_, mls_heatFlux)
 DROPIN(apply_stefancondition_, apply_StefanCondition)
 DROPIN(tagcells_, tagCells)
 DROPIN(particle_, particle)
+DROPIN(mls_structloads_, mls_structLoads)
+DROPIN(update_part_pos_, update_part_pos)
 DROPIN(cfl_, cfl)
 DROPIN(get_dt_, get_dt)
 DROPIN(tagcells_initial_, tagCells_initial)

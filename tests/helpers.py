@@ -45,9 +45,9 @@ def randomize(case: Case, seed: int = 7, forcing: bool = True) -> None:
                 A.MIBM_F_FORCX, A.MIBM_F_FORCY, A.MIBM_F_FORCZ):
         case.fill_ghosts(fid)
     case.set_S(A.MIBM_S_BETAGZ, 0.3)
-    case.sc[A.MIBM_S_VEL_CM, :] = [0.1, -0.2, 0.05]
-    case.sc[A.MIBM_S_OMEGA_C, :] = [0.3, 0.1, -0.4]
-    case.sc[A.MIBM_S_POS_CM, :] += [0.01, -0.02, 0.03]
+    case.sc[A.MIBM_S_VEL_CM, :3] = [0.1, -0.2, 0.05]
+    case.sc[A.MIBM_S_OMEGA_C, :3] = [0.3, 0.1, -0.4]
+    case.sc[A.MIBM_S_POS_CM, :3] += [0.01, -0.02, 0.03]
     set_substep(case, 1)
 
 
