@@ -716,118 +716,6 @@ __global__ void heat_flux_kernel(LagArgs A, const double* __restrict__ temp, con
   qout[t] = qv / pec;
 }
 
-// ---------------------------------------------------------------------
-// Structural loads (mls_structLoads.f90:1-269).  Stage 1: one thread per
-// (face, evaluation) at the face's positive probe x_p = X + h n/|n|:
-//   e = 0  pressure value (wght_press: cell-centred cage, z layers
-//          k1-1..k1+1 without the repeated layer, mls_structLoads.f90:271-404)
-//   e = 1  grad p   (wght_gradP, cage (icent, jcent))
-//   e = 2  grad u   (wght_gradU, x at faces, cage (istag, jcent))
-//   e = 3  grad v   (wght_gradV, y at faces, cage (icent, jstag))
-//   e = 4  grad w   (wght_gradW, z at faces with nint, cage (icent, jcent))
-// written to 13 doubles per face [p, gradP, gradU, gradV, gradW].
-// Stage 2: one block forms the per-face pressure force, viscous normal
-// stress and their moments about pos_CM in the reference's operation
-// order and sums them over the faces in a fixed order.
-// ---------------------------------------------------------------------
-__device__ bool probe_value(const LagArgs& A, const double pos[3], int i0, int j0, const double* __restrict__ q,
-                            double& val) {
-  const Grid& g = A.g;
-  double ptx[4] = {1.0, pos[0], pos[1], pos[2]};
-  int k1 = ffloor(pos[2] * g.dx3) + 1;
-  double wz[3], wy[3], wx[3], cz[3], cy[3], cx[3];
-  for (int r = 0; r < 3; ++r) {
-    cz[r] = coord(A, 2, 1, k1 - 1 + r);
-    cy[r] = coord(A, 1, 1, j0 - 1 + r);
-    cx[r] = coord(A, 0, 1, i0 - 1 + r);
-    wz[r] = mls_gaussian(fabs(cz[r] - pos[2]) / (A.wscl / g.dx3), A.wcon);
-    wy[r] = mls_gaussian(fabs(cy[r] - pos[1]) / (A.wscl / g.dx2), A.wcon);
-    wx[r] = mls_gaussian(fabs(cx[r] - pos[0]) / (A.wscl / g.dx1), A.wcon);
-  }
-  double Am[16];
-  for (int r = 0; r < 16; ++r) Am[r] = 0.0;
-  for (int kk = 0; kk < 3; ++kk)
-    for (int jj = 0; jj < 3; ++jj) {
-      double w23 = wy[jj] * wz[kk];
-      for (int ii = 0; ii < 3; ++ii) {
-        double wtx = wx[ii] * w23;
-        double pk[4] = {1.0, cx[ii], cy[jj], cz[kk]};
-        for (int cc = 0; cc < 4; ++cc) {
-          double tt = wtx * pk[cc];
-          for (int r = 0; r < 4; ++r) Am[r + 4 * cc] = Am[r + 4 * cc] + tt * pk[r];
-        }
-      }
-    }
-  if (!inv4(Am)) return false;
-  double ptxA[4];
-  for (int cc = 0; cc < 4; ++cc) {
-    double sum = 0;
-    for (int r = 0; r < 4; ++r) sum += ptx[r] * Am[r + 4 * cc];
-    ptxA[cc] = sum;
-  }
-  int k1w = fmod_pos(k1 - 1, g.n3m) + 1;
-  double acc = 0.0;
-  for (int kk = 0; kk < 3; ++kk) {
-    int kc = wrap(k1w - 1 + kk - 1, g.n3m);        // keul = k1w-1, k1w, k1w+1 (1-based)
-    for (int jj = 0; jj < 3; ++jj) {
-      int jc = fmod_pos(j0 - 1 + jj - 1, g.n2m);
-      double w23 = wy[jj] * wz[kk];
-      for (int ii = 0; ii < 3; ++ii) {
-        int ic = fmod_pos(i0 - 1 + ii - 1, g.n1m);
-        double wtx = wx[ii] * w23;
-        double phi = ptxA[0] * (wtx * 1.0) + ptxA[1] * (wtx * cx[ii]) + ptxA[2] * (wtx * cy[jj]) +
-                     ptxA[3] * (wtx * cz[kk]);
-        acc = acc + q[cidx(g, ic, jc, kc)] * phi;
-      }
-    }
-  }
-  val = acc;
-  return true;
-}
-
-__device__ __forceinline__ void struct_probe(const LagArgs& A, const double* __restrict__ tri_bar,
-                                             const double* __restrict__ tri_nor, int t, double h, double pos[3],
-                                             double nrm[3]) {
-  for (int d = 0; d < 3; ++d) nrm[d] = tri_nor[3 * t + d];
-  double s = sqrt(nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2]);
-  for (int d = 0; d < 3; ++d) pos[d] = tri_bar[3 * t + d] + h * nrm[d] / s;
-}
-
-__global__ void loads_eval_kernel(LagArgs A, const double* __restrict__ pr, const double* __restrict__ vx,
-                                  const double* __restrict__ vy, const double* __restrict__ vz,
-                                  const double* __restrict__ tri_bar, const double* __restrict__ tri_nor,
-                                  const int* __restrict__ ghost, double h, double* __restrict__ ev,
-                                  int* __restrict__ flag) {
-  int gid = blockIdx.x * blockDim.x + threadIdx.x;
-  int t = gid / 5, e = gid - 5 * t;
-  if (t >= A.nf) return;
-  double* out = ev + 13 * (size_t)t;
-  if (ghost[t]) {
-    if (e == 0) out[0] = 0.0;
-    else for (int d = 0; d < 3; ++d) out[1 + 3 * (e - 1) + d] = 0.0;
-    return;
-  }
-  const Grid& g = A.g;
-  double pos[3], nrm[3];
-  struct_probe(A, tri_bar, tri_nor, t, h, pos, nrm);
-  int icent = ffloor(pos[0] * g.dx1) + 1, istag = fnint(pos[0] * g.dx1) + 1;
-  int jcent = ffloor(pos[1] * g.dx2) + 1, jstag = fnint(pos[1] * g.dx2) + 1;
-  bool ok;
-  if (e == 0) {
-    double v = 0.0;
-    ok = probe_value(A, pos, icent, jcent, pr, v);
-    out[0] = ok ? v : 0.0;
-  } else {
-    double gr[3] = {0, 0, 0};
-    if (e == 1) ok = probe_grad(A, pos, icent, jcent, 1, 1, 1, false, pr, gr);
-    else if (e == 2) ok = probe_grad(A, pos, istag, jcent, 0, 1, 1, false, vx, gr);
-    else if (e == 3) ok = probe_grad(A, pos, icent, jstag, 1, 0, 1, false, vy, gr);
-    else ok = probe_grad(A, pos, icent, jcent, 1, 1, 0, true, vz, gr);
-    for (int d = 0; d < 3; ++d) out[1 + 3 * (e - 1) + d] = ok ? gr[d] : 0.0;
-  }
-  if (!ok) atomicOr(flag, 1);
-}
-
 __device__ __forceinline__ void cross3(double r[3], const double x[3], const double y[3]) {
   r[0] = x[1] * y[2] - y[1] * x[2];
   r[1] = x[2] * y[0] - y[2] * x[0];
@@ -862,41 +750,6 @@ __device__ void face_loads(const double* __restrict__ e, const double nrm[3], co
   cross3(buf, rad, tv);
   for (int d = 0; d < 3; ++d) rt[d] = rt[d] + buf[d];
   for (int d = 0; d < 3; ++d) { c[3 + d] = tn[d]; c[9 + d] = rt[d]; }
-}
-
-// One block: fixed-order sums of the per-face loads; thread 0 moves the
-// previous loads to the _m1 slots, stores the new ones and adds them to the
-// running sums (mls_structLoads.f90:21-24, 207-262).
-__global__ void loads_reduce_kernel(int nf, const double* __restrict__ ev, const double* __restrict__ tri_bar,
-                                    const double* __restrict__ tri_nor, const double* __restrict__ sur,
-                                    const int* __restrict__ ghost, const StepParams* __restrict__ pp, double h,
-                                    double ren, RigidDev* r) {
-  __shared__ double sm[12][256];
-  double acc[12];
-  for (int q = 0; q < 12; ++q) acc[q] = 0.0;
-  double pcm[3] = {pp->pos[0], pp->pos[1], pp->pos[2]};
-  for (int t = threadIdx.x; t < nf; t += blockDim.x) {
-    if (ghost[t]) continue;
-    double nrm[3], rad[3], cf[12];
-    for (int d = 0; d < 3; ++d) { nrm[d] = tri_nor[3 * t + d]; rad[d] = tri_bar[3 * t + d] - pcm[d]; }
-    face_loads(ev + 13 * (size_t)t, nrm, rad, sur[t], h, ren, cf);
-    for (int q = 0; q < 12; ++q) acc[q] += cf[q];
-  }
-  for (int q = 0; q < 12; ++q) sm[q][threadIdx.x] = acc[q];
-  __syncthreads();
-  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
-    if (threadIdx.x < off)
-      for (int q = 0; q < 12; ++q) sm[q][threadIdx.x] += sm[q][threadIdx.x + off];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    // packed [prn, tau, rprn, rtau]; face_loads gives [prn, tau, rprn, rtau]
-    for (int q = 0; q < 12; ++q) {
-      r->load1[q] = r->load[q];
-      r->load[q] = sm[q][0];
-      r->acc[q] = r->acc[q] + sm[q][0];
-    }
-  }
 }
 
 // ---------------------------------------------------------------------
@@ -965,49 +818,39 @@ __global__ void mls_weight_sep_kernel(LagArgs A, const double* __restrict__ tri_
     }
 }
 
-__global__ void heat_flux_sep_kernel(LagArgs A, const double* __restrict__ temp, const double* __restrict__ tri_bar,
-                                     const double* __restrict__ tri_nor, const int* __restrict__ ghost,
-                                     const int* __restrict__ pind, double h, double pec, double* __restrict__ qw_o,
-                                     double* __restrict__ qw_i, int* __restrict__ flag) {
-  int gid = blockIdx.x * blockDim.x + threadIdx.x;
-  int t = gid >> 1, side = gid & 1;
-  if (t >= A.nf) return;
-  double* qout = side == 0 ? qw_o : qw_i;
-  if (ghost[t]) { qout[t] = 0.0; return; }
+// Separable MLS gradient at a probe, parameterised like probe_grad (cage
+// centre, staggering per axis, floor or nint z base with the repeated
+// layer); field values at the wrapped cage.  Returns false on a singular
+// moment matrix.
+__device__ bool probe_grad_sep(const LagArgs& A, const double pos[3], int pi1, int pi2, int sx, int sy, int sz,
+                               bool knint, const double* __restrict__ q, double grad[3]) {
   const Grid& g = A.g;
-  double n0 = tri_nor[3 * t], n1 = tri_nor[3 * t + 1], n2 = tri_nor[3 * t + 2];
-  double s = sqrt(n0 * n0 + n1 * n1 + n2 * n2);
-  double pos[3];
-  for (int d = 0; d < 3; ++d) {
-    double nd = tri_nor[3 * t + d];
-    pos[d] = side == 0 ? tri_bar[3 * t + d] + h * nd / s : tri_bar[3 * t + d] - h * nd / s;
-  }
-  int pi1 = pind[6 * t + 3 * side + 0], pi2 = pind[6 * t + 3 * side + 1];
   const double eps = 2.220446049250313e-16;
-  int k1 = ffloor(pos[2] * g.dx3) + 1;
+  int k1 = knint ? fnint(pos[2] * g.dx3) + 1 : ffloor(pos[2] * g.dx3) + 1;
   int kin[3] = {k1 - 1, k1, k1};                  // mls_heatFlux.f90:213 (third layer repeats k1)
   int k1w = fmod_pos(k1 - 1, g.n3m) + 1;
   int keul[3] = {k1w - 1, k1w, k1w + 1};
+  const int sel[3] = {sx, sy, sz};
   double w[3][3], dw[3][3], dd[3][3];             // [axis][point]
-  for (int q = 0; q < 3; ++q) {
-    double pc[3] = {coord(A, 0, 1, pi1 - 1 + q), coord(A, 1, 1, pi2 - 1 + q), coord(A, 2, 1, kin[q])};
+  for (int r = 0; r < 3; ++r) {
+    double pc[3] = {coord(A, 0, sel[0], pi1 - 1 + r), coord(A, 1, sel[1], pi2 - 1 + r), coord(A, 2, sel[2], kin[r])};
     const double dxs[3] = {g.dx1, g.dx2, g.dx3};
     for (int a = 0; a < 3; ++a) {
-      double r = pos[a] - pc[a];
-      double np = fabs(r) / (A.wscl / dxs[a]);
-      w[a][q] = mls_gaussian(np, A.wcon);
-      dw[a][q] = (np < eps) ? 0.0 : mls_gauss_deriv(np, A.wcon) * (r / fabs(r) / (A.wscl / dxs[a]));
-      dd[a][q] = pc[a] - pos[a];
+      double rr = pos[a] - pc[a];
+      double np = fabs(rr) / (A.wscl / dxs[a]);
+      w[a][r] = mls_gaussian(np, A.wcon);
+      dw[a][r] = (np < eps) ? 0.0 : mls_gauss_deriv(np, A.wcon) * (rr / fabs(rr) / (A.wscl / dxs[a]));
+      dd[a][r] = pc[a] - pos[a];
     }
   }
   double S[3][3], D[3][3];
   for (int a = 0; a < 3; ++a) { moments3(w[a], dd[a], S[a]); moments3(dw[a], dd[a], D[a]); }
   double Ai[16];
   moment_matrix(S[0], S[1], S[2], Ai);
-  if (!inv4(Ai)) { atomicOr(flag, 1); qout[t] = 0.0; return; }
+  if (!inv4(Ai)) return false;
   const double gam[4] = {Ai[0], Ai[1], Ai[2], Ai[3]};     // A^{-1} p(x0), p(x0) = e0
-  // sums over the cage of T times the weighted basis: MT (weights), MD[d]
-  // (derivative of the weights along d)
+  // sums over the cage of the field times the weighted basis: MT (weights),
+  // MD[d] (derivative of the weights along d)
   double MT[4] = {0, 0, 0, 0}, MD[3][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}};
   for (int kk = 0; kk < 3; ++kk)
     for (int jj = 0; jj < 3; ++jj) {
@@ -1015,7 +858,7 @@ __global__ void heat_flux_sep_kernel(LagArgs A, const double* __restrict__ temp,
       double wyz = w[1][jj] * w[2][kk], dyz = dw[1][jj] * w[2][kk], ydz = w[1][jj] * dw[2][kk];
       for (int ii = 0; ii < 3; ++ii) {
         int ii_ = fmod_pos(pi1 - 1 + ii - 1, g.n1m);
-        double T = temp[cidx(g, ii_, jj_, kk_)];
+        double T = q[cidx(g, ii_, jj_, kk_)];
         double pb[4] = {1.0, dd[0][ii], dd[1][jj], dd[2][kk]};
         double a0 = w[0][ii] * wyz * T, a1 = dw[0][ii] * wyz * T, a2 = w[0][ii] * dyz * T, a3 = w[0][ii] * ydz * T;
         for (int r = 0; r < 4; ++r) {
@@ -1026,7 +869,6 @@ __global__ void heat_flux_sep_kernel(LagArgs A, const double* __restrict__ temp,
         }
       }
     }
-  double grad[3];
   for (int d = 0; d < 3; ++d) {
     double dA[16];
     double X[3], Y[3], Z[3];
@@ -1050,8 +892,170 @@ __global__ void heat_flux_sep_kernel(LagArgs A, const double* __restrict__ temp,
     }
     grad[d] = acc;
   }
+  return true;
+}
+
+// Separable MLS value at a probe (wght_press, mls_structLoads.f90:271-404):
+// cell-centred cage around (i0, j0), z layers k1-1, k1, k1+1 (no repeated
+// layer).  value = A^{-1} e0 . sum_n w_n p_n q_n in the shifted basis.
+__device__ bool probe_value_sep(const LagArgs& A, const double pos[3], int i0, int j0, const double* __restrict__ q,
+                                double& val) {
+  const Grid& g = A.g;
+  int k1 = ffloor(pos[2] * g.dx3) + 1;
+  int k1w = fmod_pos(k1 - 1, g.n3m) + 1;
+  double w[3][3], dd[3][3];
+  for (int r = 0; r < 3; ++r) {
+    double pc[3] = {coord(A, 0, 1, i0 - 1 + r), coord(A, 1, 1, j0 - 1 + r), coord(A, 2, 1, k1 - 1 + r)};
+    const double dxs[3] = {g.dx1, g.dx2, g.dx3};
+    for (int a = 0; a < 3; ++a) {
+      w[a][r] = mls_gaussian(fabs(pc[a] - pos[a]) / (A.wscl / dxs[a]), A.wcon);
+      dd[a][r] = pc[a] - pos[a];
+    }
+  }
+  double S[3][3];
+  for (int a = 0; a < 3; ++a) moments3(w[a], dd[a], S[a]);
+  double Ai[16];
+  moment_matrix(S[0], S[1], S[2], Ai);
+  if (!inv4(Ai)) return false;
+  double MT[4] = {0, 0, 0, 0};
+  for (int kk = 0; kk < 3; ++kk)
+    for (int jj = 0; jj < 3; ++jj) {
+      int jj_ = fmod_pos(j0 - 1 + jj - 1, g.n2m), kk_ = wrap(k1w - 1 + kk - 1, g.n3m);
+      double wyz = w[1][jj] * w[2][kk];
+      for (int ii = 0; ii < 3; ++ii) {
+        int ii_ = fmod_pos(i0 - 1 + ii - 1, g.n1m);
+        double a0 = w[0][ii] * wyz * q[cidx(g, ii_, jj_, kk_)];
+        double pb[4] = {1.0, dd[0][ii], dd[1][jj], dd[2][kk]};
+        for (int r = 0; r < 4; ++r) MT[r] = fma(a0, pb[r], MT[r]);
+      }
+    }
+  double v = 0;
+  for (int r = 0; r < 4; ++r) v = fma(Ai[r], MT[r], v);
+  val = v;
+  return true;
+}
+
+__global__ void heat_flux_sep_kernel(LagArgs A, const double* __restrict__ temp, const double* __restrict__ tri_bar,
+                                     const double* __restrict__ tri_nor, const int* __restrict__ ghost,
+                                     const int* __restrict__ pind, double h, double pec, double* __restrict__ qw_o,
+                                     double* __restrict__ qw_i, int* __restrict__ flag) {
+  int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  int t = gid >> 1, side = gid & 1;
+  if (t >= A.nf) return;
+  double* qout = side == 0 ? qw_o : qw_i;
+  if (ghost[t]) { qout[t] = 0.0; return; }
+  double n0 = tri_nor[3 * t], n1 = tri_nor[3 * t + 1], n2 = tri_nor[3 * t + 2];
+  double s = sqrt(n0 * n0 + n1 * n1 + n2 * n2);
+  double pos[3];
+  for (int d = 0; d < 3; ++d) {
+    double nd = tri_nor[3 * t + d];
+    pos[d] = side == 0 ? tri_bar[3 * t + d] + h * nd / s : tri_bar[3 * t + d] - h * nd / s;
+  }
+  int pi1 = pind[6 * t + 3 * side + 0], pi2 = pind[6 * t + 3 * side + 1];
+  double grad[3];
+  if (!probe_grad_sep(A, pos, pi1, pi2, 1, 1, 1, false, temp, grad)) { atomicOr(flag, 1); qout[t] = 0.0; return; }
   double qv = n0 * grad[0] + n1 * grad[1] + n2 * grad[2];
   qout[t] = qv / pec;
+}
+
+// ---------------------------------------------------------------------
+// Structural loads (mls_structLoads.f90:1-269).  A block takes 32 faces;
+// warp e of the block evaluates, at each face's positive probe
+// x_p = X + h n/|n|,
+//   e = 0  the pressure (wght_press: cell-centred cage, z layers k1-1..k1+1
+//          without the repeated layer, mls_structLoads.f90:271-404)
+//   e = 1  grad p   (wght_gradP, cage (icent, jcent))
+//   e = 2  grad u   (wght_gradU, x at faces, cage (istag, jcent))
+//   e = 3  grad v   (wght_gradV, y at faces, cage (icent, jstag))
+//   e = 4  grad w   (wght_gradW, z at faces with nint, cage (icent, jcent))
+// so every warp runs one kind of evaluation.  Warp 0 then forms each face's
+// pressure force, viscous normal stress and their moments about pos_CM in
+// the reference's operation order (face_loads) and sums its 32 faces with a
+// fixed shuffle tree; loads_final_kernel adds the block sums in block order.
+// The MLS uses the separable construction of the precision form: it agrees
+// with the reference's rank-one accumulation in absolute coordinates to
+// that construction's round-off (amplified by its ~1e8 conditioning), and
+// keeps the 5 evaluations in registers.
+// ---------------------------------------------------------------------
+constexpr int kLoadFaces = 32;
+
+__device__ __forceinline__ void struct_probe(const double* __restrict__ tri_bar, const double* __restrict__ tri_nor,
+                                             int t, double h, double pos[3], double nrm[3]) {
+  for (int d = 0; d < 3; ++d) nrm[d] = tri_nor[3 * t + d];
+  double s = sqrt(nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2]);
+  for (int d = 0; d < 3; ++d) pos[d] = tri_bar[3 * t + d] + h * nrm[d] / s;
+}
+
+__global__ void __launch_bounds__(kLoadFaces * 5)
+loads_face_kernel(LagArgs A, const double* __restrict__ pr, const double* __restrict__ vx,
+                  const double* __restrict__ vy, const double* __restrict__ vz, const double* __restrict__ tri_bar,
+                  const double* __restrict__ tri_nor, const double* __restrict__ sur, const int* __restrict__ ghost,
+                  const StepParams* __restrict__ pp, double h, double ren, double* __restrict__ part,
+                  int* __restrict__ flag) {
+  __shared__ double ev[13][kLoadFaces];
+  const int lf = threadIdx.x, e = threadIdx.y;
+  const int t = blockIdx.x * kLoadFaces + lf;
+  const bool live = t < A.nf && !ghost[t];
+  const Grid& g = A.g;
+  double pos[3], nrm[3];
+  if (live) {
+    struct_probe(tri_bar, tri_nor, t, h, pos, nrm);
+    int icent = ffloor(pos[0] * g.dx1) + 1, istag = fnint(pos[0] * g.dx1) + 1;
+    int jcent = ffloor(pos[1] * g.dx2) + 1, jstag = fnint(pos[1] * g.dx2) + 1;
+    bool ok;
+    if (e == 0) {
+      double v = 0.0;
+      ok = probe_value_sep(A, pos, icent, jcent, pr, v);
+      ev[0][lf] = ok ? v : 0.0;
+    } else {
+      double gr[3] = {0, 0, 0};
+      if (e == 1) ok = probe_grad_sep(A, pos, icent, jcent, 1, 1, 1, false, pr, gr);
+      else if (e == 2) ok = probe_grad_sep(A, pos, istag, jcent, 0, 1, 1, false, vx, gr);
+      else if (e == 3) ok = probe_grad_sep(A, pos, icent, jstag, 1, 0, 1, false, vy, gr);
+      else ok = probe_grad_sep(A, pos, icent, jcent, 1, 1, 0, true, vz, gr);
+      for (int d = 0; d < 3; ++d) ev[1 + 3 * (e - 1) + d][lf] = ok ? gr[d] : 0.0;
+    }
+    if (!ok) atomicOr(flag, 1);
+  }
+  __syncthreads();
+  if (e != 0) return;
+  double cf[12];
+  for (int q = 0; q < 12; ++q) cf[q] = 0.0;
+  if (live) {
+    double e13[13], rad[3];
+    for (int q = 0; q < 13; ++q) e13[q] = ev[q][lf];
+    for (int d = 0; d < 3; ++d) rad[d] = tri_bar[3 * t + d] - pp->pos[d];
+    face_loads(e13, nrm, rad, sur[t], h, ren, cf);
+  }
+  for (int q = 0; q < 12; ++q) {
+    double v = cf[q];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if (lf == 0) part[12 * (size_t)blockIdx.x + q] = v;
+  }
+}
+
+// Sum of the block sums in block order; thread 0 moves the previous loads
+// to the _m1 slots, stores the new ones and adds them to the running sums
+// (mls_structLoads.f90:21-24, 207-262).
+__global__ void loads_final_kernel(int nb, const double* __restrict__ part, RigidDev* r) {
+  __shared__ double sm[12][256];
+  double acc[12];
+  for (int q = 0; q < 12; ++q) acc[q] = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x)
+    for (int q = 0; q < 12; ++q) acc[q] += part[12 * (size_t)b + q];
+  for (int q = 0; q < 12; ++q) sm[q][threadIdx.x] = acc[q];
+  __syncthreads();
+  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off)
+      for (int q = 0; q < 12; ++q) sm[q][threadIdx.x] += sm[q][threadIdx.x + off];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int q = 0; q < 12; ++q) {        // packed [prn, tau, rprn, rtau]
+      r->load1[q] = r->load[q];
+      r->load[q] = sm[q][0];
+      r->acc[q] = r->acc[q] + sm[q][0];
+    }
 }
 
 // face -> vertex: qw_v(v) = sum over adjacent faces (ascending) of q_f*(A_f/3/A_v)
@@ -1092,13 +1096,11 @@ __global__ void stefan_kernel(int nv, const int* __restrict__ ghostv, const doub
 // ---------------------------------------------------------------------
 // geometry refresh (particle.f90:165-193)
 // ---------------------------------------------------------------------
-__global__ void face_geom_kernel(int nf, const int* __restrict__ vof, const int* __restrict__ ghost,
-                                 const double* __restrict__ x, double* __restrict__ sur, double* __restrict__ nor,
-                                 double* __restrict__ bar, double* __restrict__ part /* 12 per face */) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nf) return;
-  double* pp = part + 12 * (size_t)t;
-  if (ghost[t]) { for (int q = 0; q < 12; ++q) pp[q] = 0.0; return; }
+// calculate_area, update_tri_normal, calc_centroids_from_vert of face t and
+// its summands of calculate_volume and calc_rigidBody_params
+__device__ __forceinline__ void face_geom_one(int t, const int* __restrict__ vof, const double* __restrict__ x,
+                                              double* __restrict__ sur, double* __restrict__ nor,
+                                              double* __restrict__ bar, double pp[12]) {
   int a = vof[3 * t] - 1, b = vof[3 * t + 1] - 1, d = vof[3 * t + 2] - 1;
   double x1 = x[3 * a], y1 = x[3 * a + 1], z1 = x[3 * a + 2];
   double x2 = x[3 * b], y2 = x[3 * b + 1], z2 = x[3 * b + 2];
@@ -1131,6 +1133,33 @@ __global__ void face_geom_kernel(int nf, const int* __restrict__ vof, const int*
   pp[11] = v * (z1 * y1 + z2 * y2 + z3 * y3 + z4 * y4);
 }
 
+// One thread per face; the 12 per-face sums are added over the block (warp
+// shuffle tree, then the 4 warps in order) into part[12 * block + q].
+constexpr int kGeomBlock = 128;
+__global__ void __launch_bounds__(kGeomBlock)
+face_geom_kernel(int nf, const int* __restrict__ vof, const int* __restrict__ ghost, const double* __restrict__ x,
+                 double* __restrict__ sur, double* __restrict__ nor, double* __restrict__ bar,
+                 double* __restrict__ part /* 12 per block */) {
+  __shared__ double ws[kGeomBlock / 32][12];
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  double pp[12];
+  for (int q = 0; q < 12; ++q) pp[q] = 0.0;
+  if (t < nf && !ghost[t]) face_geom_one(t, vof, x, sur, nor, bar, pp);
+  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int q = 0; q < 12; ++q) {
+    double v = pp[q];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if (lane == 0) ws[warp][q] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 12) {
+    double v = ws[0][threadIdx.x];
+    for (int w = 1; w < kGeomBlock / 32; ++w) v += ws[w][threadIdx.x];
+    part[12 * (size_t)blockIdx.x + threadIdx.x] = v;
+  }
+}
+
+
 __global__ void vert_geom_kernel(int nv, const int* __restrict__ adj_off, const int* __restrict__ adj_face,
                                  const int* __restrict__ ghostv, const double* __restrict__ sur,
                                  const double* __restrict__ nor, double* __restrict__ avert,
@@ -1150,15 +1179,15 @@ __global__ void vert_geom_kernel(int nv, const int* __restrict__ adj_off, const 
   vnor[3 * v] = a0 / m; vnor[3 * v + 1] = a1 / m; vnor[3 * v + 2] = a2 / m;
 }
 
-// fixed-order reduction of the 12 per-face sums by one block; writes
+// fixed-order reduction of the 12 block sums by one block; writes
 // [Surface, Volume1, Volume, pos_CM(3), InertTensor(9)] into out (the
 // post-processing of calc_rigidBody_params, RigidAuxRoutines.f90:736-775)
-__global__ void geom_reduce_kernel(int nf, const double* __restrict__ part, double dens_ratio,
+__global__ void geom_reduce_kernel(int nb, const double* __restrict__ part, double dens_ratio,
                                    double* __restrict__ out) {
   __shared__ double sm[12][256];
   double s[12];
   for (int q = 0; q < 12; ++q) s[q] = 0.0;
-  for (int t = threadIdx.x; t < nf; t += blockDim.x)
+  for (int t = threadIdx.x; t < nb; t += blockDim.x)
     for (int q = 0; q < 12; ++q) s[q] += part[12 * (size_t)t + q];
   for (int q = 0; q < 12; ++q) sm[q][threadIdx.x] = s[q];
   __syncthreads();
@@ -1512,7 +1541,7 @@ struct LagState {
   int adj_nf = -1, adj_nv = -1;
   double* face_part = nullptr;
   double* geom_out = nullptr;   // device [Surface, Volume1, Vol, Cx, Cy, Cz, InertTensor(9)]
-  double* loads_ev = nullptr;   // structural loads: 13 probe evaluations per face
+  double* loads_ev = nullptr;   // structural loads: 12 block sums per 32 faces
   double* mean3 = nullptr;
   unsigned long long* sdf_bits = nullptr;
   int* winner = nullptr;
@@ -1836,12 +1865,13 @@ void lagr_stefan(Ctx* c, const StepParams* dp) {
 static void geometry_launch(Ctx* c, bool imelt, bool body_only = false) {
   LagState* s = lag_of(c);
   { MIBM_PROF(c, "face_geom");
-    face_geom_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(
+    face_geom_kernel<<<div_up(c->maxnf, kGeomBlock), kGeomBlock, 0, c->stream>>>(
         c->maxnf, M<int>(c, MIBM_M_VERT_OF_FACE), M<int>(c, MIBM_M_GHOST_FACE), M<double>(c, MIBM_M_XYZV),
         M<double>(c, MIBM_M_SUR), M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_TRI_BAR), s->face_part); }
+  const int gnb = (int)div_up(c->maxnf, kGeomBlock);
   if (body_only) {
     { MIBM_PROF(c, "geom_reduce");
-      geom_reduce_kernel<<<1, 256, 0, c->stream>>>(c->maxnf, s->face_part, c->S(MIBM_S_DENS_RATIO), s->geom_out); }
+      geom_reduce_kernel<<<1, 256, 0, c->stream>>>(gnb, s->face_part, c->S(MIBM_S_DENS_RATIO), s->geom_out); }
     c->launches += 2;
     return;
   }
@@ -1850,7 +1880,7 @@ static void geometry_launch(Ctx* c, bool imelt, bool body_only = false) {
         c->maxnv, s->adj_off, s->adj_face, M<int>(c, MIBM_M_GHOST_VERT), M<double>(c, MIBM_M_SUR),
         M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_AVERT), M<double>(c, MIBM_M_VERT_NOR)); }
   { MIBM_PROF(c, "geom_reduce");
-    geom_reduce_kernel<<<1, 256, 0, c->stream>>>(c->maxnf, s->face_part, c->S(MIBM_S_DENS_RATIO), s->geom_out); }
+    geom_reduce_kernel<<<1, 256, 0, c->stream>>>(gnb, s->face_part, c->S(MIBM_S_DENS_RATIO), s->geom_out); }
   c->launches += 3;
   if (imelt) {
     { MIBM_PROF(c, "cfac");
@@ -1881,16 +1911,14 @@ static void struct_loads_launch(Ctx* c, const StepParams* dp) {
       !cuda_ok(c, cudaMalloc(&s->loads_ev, sizeof(double) * 13 * std::max(1, c->maxnf)), "structLoads"))
     return;
   double h = c->S(MIBM_S_H_EULERIAN);
-  { MIBM_PROF(c, "loads_eval");
-    loads_eval_kernel<<<div_up(5 * (size_t)c->maxnf, 128), 128, 0, c->stream>>>(
+  int nb = (int)div_up(c->maxnf, kLoadFaces);
+  { MIBM_PROF(c, "loads_face");
+    loads_face_kernel<<<nb, dim3(kLoadFaces, 5), 0, c->stream>>>(
         lag_args(c), c->df[MIBM_F_PR], c->df[MIBM_F_VX], c->df[MIBM_F_VY], c->df[MIBM_F_VZ],
-        M<double>(c, MIBM_M_TRI_BAR), M<double>(c, MIBM_M_TRI_NOR), M<int>(c, MIBM_M_GHOST_FACE), h, s->loads_ev,
-        c->dflag); }
-  { MIBM_PROF(c, "loads_reduce");
-    loads_reduce_kernel<<<1, 256, 0, c->stream>>>(c->maxnf, s->loads_ev, M<double>(c, MIBM_M_TRI_BAR),
-                                                  M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_SUR),
-                                                  M<int>(c, MIBM_M_GHOST_FACE), dp, h, c->S(MIBM_S_REN),
-                                                  c->drigid); }
+        M<double>(c, MIBM_M_TRI_BAR), M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_SUR),
+        M<int>(c, MIBM_M_GHOST_FACE), dp, h, c->S(MIBM_S_REN), s->loads_ev, c->dflag); }
+  { MIBM_PROF(c, "loads_final");
+    loads_final_kernel<<<1, 256, 0, c->stream>>>(nb, s->loads_ev, c->drigid); }
   c->launches += 2;
 }
 
