@@ -818,6 +818,32 @@ __global__ void mls_weight_sep_kernel(LagArgs A, const double* __restrict__ tri_
     }
 }
 
+// Gaussian weight of one cage coordinate and its derivative along the axis
+// (geom.f90:24-53 with the chain-rule factor of mls_heatFlux.f90:176-180).
+// The cut-off decision r > 1 uses r = |x - x_c| / (wscl/dx) rounded as the
+// reference rounds it; the rest uses precomputed reciprocals (the separable
+// construction is insensitive to last-ulp changes of the weights).
+struct AxisScale {
+  double c, inv_c, inv_wcon, dcoef;   // wscl/dx, its reciprocal, 1/wcon, -2/wcon^2
+};
+__device__ __forceinline__ AxisScale axis_scale(const LagArgs& A, double dx) {
+  AxisScale a;
+  a.c = A.wscl / dx;
+  a.inv_c = 1.0 / a.c;
+  a.inv_wcon = 1.0 / A.wcon;
+  a.dcoef = -2.0 / (A.wcon * A.wcon);
+  return a;
+}
+__device__ __forceinline__ void axis_weight(const AxisScale& a, double pos, double pc, double& w, double& dw) {
+  const double eps = 2.220446049250313e-16;
+  double rr = pos - pc;
+  double np = fabs(rr) / a.c;
+  if (np > 1.0) { w = 0.0; dw = 0.0; return; }
+  double e = exp(-sqd(np * a.inv_wcon));
+  w = e;
+  dw = (np < eps) ? 0.0 : (a.dcoef * np) * e * copysign(a.inv_c, rr);
+}
+
 // Separable MLS gradient at a probe, parameterised like probe_grad (cage
 // centre, staggering per axis, floor or nint z base with the repeated
 // layer); field values at the wrapped cage.  Returns false on a singular
@@ -825,21 +851,17 @@ __global__ void mls_weight_sep_kernel(LagArgs A, const double* __restrict__ tri_
 __device__ bool probe_grad_sep(const LagArgs& A, const double pos[3], int pi1, int pi2, int sx, int sy, int sz,
                                bool knint, const double* __restrict__ q, double grad[3]) {
   const Grid& g = A.g;
-  const double eps = 2.220446049250313e-16;
   int k1 = knint ? fnint(pos[2] * g.dx3) + 1 : ffloor(pos[2] * g.dx3) + 1;
   int kin[3] = {k1 - 1, k1, k1};                  // mls_heatFlux.f90:213 (third layer repeats k1)
   int k1w = fmod_pos(k1 - 1, g.n3m) + 1;
   int keul[3] = {k1w - 1, k1w, k1w + 1};
   const int sel[3] = {sx, sy, sz};
+  const AxisScale sc[3] = {axis_scale(A, g.dx1), axis_scale(A, g.dx2), axis_scale(A, g.dx3)};
   double w[3][3], dw[3][3], dd[3][3];             // [axis][point]
   for (int r = 0; r < 3; ++r) {
     double pc[3] = {coord(A, 0, sel[0], pi1 - 1 + r), coord(A, 1, sel[1], pi2 - 1 + r), coord(A, 2, sel[2], kin[r])};
-    const double dxs[3] = {g.dx1, g.dx2, g.dx3};
     for (int a = 0; a < 3; ++a) {
-      double rr = pos[a] - pc[a];
-      double np = fabs(rr) / (A.wscl / dxs[a]);
-      w[a][r] = mls_gaussian(np, A.wcon);
-      dw[a][r] = (np < eps) ? 0.0 : mls_gauss_deriv(np, A.wcon) * (rr / fabs(rr) / (A.wscl / dxs[a]));
+      axis_weight(sc[a], pos[a], pc[a], w[a][r], dw[a][r]);
       dd[a][r] = pc[a] - pos[a];
     }
   }
@@ -903,12 +925,13 @@ __device__ bool probe_value_sep(const LagArgs& A, const double pos[3], int i0, i
   const Grid& g = A.g;
   int k1 = ffloor(pos[2] * g.dx3) + 1;
   int k1w = fmod_pos(k1 - 1, g.n3m) + 1;
+  const AxisScale sc[3] = {axis_scale(A, g.dx1), axis_scale(A, g.dx2), axis_scale(A, g.dx3)};
   double w[3][3], dd[3][3];
   for (int r = 0; r < 3; ++r) {
     double pc[3] = {coord(A, 0, 1, i0 - 1 + r), coord(A, 1, 1, j0 - 1 + r), coord(A, 2, 1, k1 - 1 + r)};
-    const double dxs[3] = {g.dx1, g.dx2, g.dx3};
     for (int a = 0; a < 3; ++a) {
-      w[a][r] = mls_gaussian(fabs(pc[a] - pos[a]) / (A.wscl / dxs[a]), A.wcon);
+      double dwu;
+      axis_weight(sc[a], pos[a], pc[a], w[a][r], dwu);
       dd[a][r] = pc[a] - pos[a];
     }
   }
