@@ -288,6 +288,35 @@ void mibm_hit_bhat_(double* bhat, const int* dir);
 /* term adds VOF * C_HIT * u (hdnl1.f90:74 divides forcx by xlen).         */
 void mibm_linear_hit_force_(void);
 
+/* Per-step diagnostics.  The reference's CalcDissipation (diss.f90:11-201), */
+/* vorticity (vorticity.f90:1-109) and calcFluidVelAvgs (calcSlipVels.f90:   */
+/* 17-181), called after every tschem (gcurv.f90:194-203), sum over the     */
+/* fully fluid cells (VOFp = 1) and append the results to text files; here  */
+/* they return the same numbers in out[MIBM_NDIAG] (layout below, the       */
+/* files' columns after `time`).  As CalcDissipation does, a body that is   */
+/* not stationary is re-tagged first (tagCells).                            */
+/*   mibm_diagnostics_: computes them now (synchronises with the device).   */
+/*   mibm_set_diagnostics_(on): with on = 1 every tschem_ appends the same   */
+/*   computation to its device work (and step graph) and reads the results  */
+/*   back with the step's own end-of-step copies: no extra synchronisation. */
+/*   mibm_diagnostics_get_: the values of the last such step (or of the     */
+/*   last mibm_diagnostics_ call).  Status codes returned; MIBM_ESTATE if     */
+/*   nothing has computed them yet.                                         */
+enum {
+  MIBM_D_DISS = 0, MIBM_D_KENERG, MIBM_D_URMS, MIBM_D_ETA, MIBM_D_LAMBDA_T,
+  MIBM_D_RE_L, MIBM_D_RE_LAMBDA, MIBM_D_L_INT, MIBM_D_CHI,   /* diss.txt        */
+  MIBM_D_ENSTROPHY,                                           /* enstrophy.txt   */
+  MIBM_D_NFLUID, MIBM_D_U, MIBM_D_V, MIBM_D_W,
+  MIBM_D_UU, MIBM_D_VV, MIBM_D_WW,                            /* fluidAvgVels    */
+  MIBM_D_UREL, MIBM_D_VREL, MIBM_D_WREL,
+  MIBM_D_UUREL, MIBM_D_VVREL, MIBM_D_WWREL,                   /* rel_velBox.txt  */
+  MIBM_D_T, MIBM_D_DT, MIBM_D_DT2,                            /* fluidAvgTemps   */
+  MIBM_NDIAG
+};
+int  mibm_diagnostics_(double* out);
+void mibm_set_diagnostics_(const int* on);
+int  mibm_diagnostics_get_(double* out);
+
 /* ------------------------------------------------------------------ */
 /* Allocation-free x-line solve.  No counterpart in the reference: it is  */
 /* for callers whose device memory belongs to someone else -- a CUDA      */

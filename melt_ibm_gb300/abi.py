@@ -77,6 +77,9 @@ SIGNATURES: dict[str, tuple] = {
     "mibm_batch_step_": (C.c_int, [_I, _I]),
     "mibm_batch_destroy_": (C.c_int, [_I]),
     "mibm_divergence_max_": (C.c_double, []),
+    "mibm_diagnostics_": (C.c_int, [C.c_void_p]),
+    "mibm_set_diagnostics_": (None, [_I]),
+    "mibm_diagnostics_get_": (C.c_int, [C.c_void_p]),
     "solxi_": (None, [_D]),
     "solxj_": (None, [_D]),
     "solxk_": (None, [C.c_void_p, _D]),

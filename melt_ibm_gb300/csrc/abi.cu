@@ -211,11 +211,19 @@ static void step_enqueue_f64(Ctx* c) {
   }
 }
 
+// device address of vel_CM at the end of a step: the moving body's state,
+// else the value the step was given
+static const double* step_vel_cm(Ctx* c) {
+  if (moving_body(c)) return (const double*)((const char*)c->drigid + offsetof(RigidDev, vel));
+  return (const double*)((const char*)(c->dparams + 2) + offsetof(StepParams, vel));
+}
+
 static void step_enqueue(Ctx* c) {
   cudaMemcpyAsync(c->dparams, c->hparams, 3 * sizeof(StepParams), cudaMemcpyHostToDevice, c->stream);
   if (moving_body(c)) rigid_upload(c);
   if (c->precision == 1) step_enqueue_f32(c);
   else step_enqueue_f64(c);
+  if (c->status == MIBM_OK && c->diag_on) diag_enqueue(c, step_vel_cm(c));
   if (c->status == MIBM_OK) lagr_step_readback(c);
 }
 
@@ -223,6 +231,7 @@ static void step_finish(Ctx* c) {
   if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "tschem")) return;
   if (c->status != MIBM_OK) return;
   lagr_step_host_finish(c);
+  if (c->diag_on && c->status == MIBM_OK) diag_finish(c);
   if (c->precision == 1 && c->status == MIBM_OK) c->q32_valid = true;
   ++c->steps_done;
 }
@@ -254,7 +263,7 @@ static uint64_t step_key(Ctx* c) {
     mix(b);
   }
   mix((uint64_t)c->precision); mix((uint64_t)c->nproj); mix(c->lag_gen); mix(c->q32 ? 1 : 0);
-  mix(c->tune_gen);
+  mix(c->tune_gen); mix(c->diag_on ? 1 : 0);
   return h;
 }
 
@@ -745,6 +754,31 @@ void mibm_set_graphs_(const int* on) {
   Ctx* c = current(); if (!ready(c)) return;
   c->use_graph = *on != 0;
   if (!c->use_graph) drop_graph(c);
+}
+
+// Diagnostics (diag.cu): computed now, or per step inside tschem_.
+int mibm_diagnostics_(double* out) {
+  Ctx* c = current(); if (!ready(c)) return c ? c->status : MIBM_ESTATE;
+  if (!out) { fail(c, MIBM_EINVAL, "diagnostics: null output"); return MIBM_EINVAL; }
+  const StepParams* dp = push_params(c, 3);
+  diag_enqueue(c, (const double*)((const char*)dp + offsetof(StepParams, vel)));
+  if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "diagnostics")) return c->status;
+  if (c->status != MIBM_OK) return c->status;
+  diag_finish(c);
+  memcpy(out, c->diag_last, sizeof(double) * MIBM_NDIAG);
+  return MIBM_OK;
+}
+
+void mibm_set_diagnostics_(const int* on) {
+  Ctx* c = current(); if (!ready(c)) return;
+  c->diag_on = *on != 0;
+}
+
+int mibm_diagnostics_get_(double* out) {
+  Ctx* c = current(); if (!ready(c)) return c ? c->status : MIBM_ESTATE;
+  if (!c->diag_valid) { fail(c, MIBM_ESTATE, "diagnostics: no step computed them"); return MIBM_ESTATE; }
+  memcpy(out, c->diag_last, sizeof(double) * MIBM_NDIAG);
+  return MIBM_OK;
 }
 
 // max over owned cells of |div u| (divgck, divg.f90:26-56); synchronises

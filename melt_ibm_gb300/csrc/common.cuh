@@ -161,6 +161,10 @@ struct Ctx {
   int tune_by = 8;                        // block height of the explicit-term kernel
   uint64_t tune_gen = 0;
   double* step_host = nullptr;            // pinned: geometry scalars read back at step end
+  // per-step diagnostics (diag.cu): requested, last values, device state
+  bool diag_on = false, diag_valid = false;
+  double diag_last[MIBM_NDIAG] = {0};
+  void* diag = nullptr;
   RigidDev* drigid = nullptr;             // moving-body state (device)
   RigidDev* hrigid_in = nullptr;          // pinned: uploaded at the start of a step
   RigidDev* hrigid_out = nullptr;         // pinned: read back at its end
@@ -314,6 +318,10 @@ void lagr_tag_initial(Ctx* c);
 void lagr_particle(Ctx* c, const StepParams* dp);
 const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror, StepParams* next);
 void lagr_struct_loads(Ctx* c, const StepParams* dp);
+// diag.cu (CalcDissipation, vorticity, calcFluidVelAvgs)
+void diag_enqueue(Ctx* c, const double* vcm);
+void diag_finish(Ctx* c);
+void diag_free(Ctx* c);
 // rigid.cu (moving body)
 bool rigid_ensure(Ctx* c);
 void rigid_pack(Ctx* c, RigidDev* h, bool geom_from_scalars);

@@ -267,6 +267,7 @@ void release(Ctx* c) {
   fft_free(c);
   hit_free(c);
   rigid_free(c);
+  diag_free(c);
   if (c->stream) cudaStreamDestroy(c->stream);
 }
 

@@ -86,6 +86,7 @@ struct Ctx {
   bool hit_seeded = false;
   uint64_t hit_rng = 0;
   int steps_done = 0;   // batch steps completed (per-case step counter)
+  bool diag_on = false, diag_stepped = false;   // per-step diagnostics requested / computed
   // coordinate accessors with the reference's extended ranges (cordin.f90:55-61)
   double xc(int i) const { return xc_[i + n1]; }
   double yc(int j) const { return yc_[j + n2]; }
@@ -1672,6 +1673,96 @@ void particle(Ctx& c) {
 }
 
 // ------------------------------------------------------------------------
+// Diagnostics: CalcDissipation diss.f90:11-201, vorticity vorticity.f90:
+// 1-109, calcFluidVelAvgs calcSlipVels.f90:17-181 -- the sums over fully
+// fluid cells (VOFp = 1) in the reference's loop order; the numbers the
+// reference writes to diss.txt, enstrophy.txt, fluidAvgVels.txt,
+// rel_velBox.txt and fluidAvgTemps.txt (include/mibm.h MIBM_D_*).
+// ------------------------------------------------------------------------
+void diagnostics(Ctx& c, double* out) {
+  update_both_ghosts(c, c.f[MIBM_F_VX], c.n2);
+  update_both_ghosts(c, c.f[MIBM_F_VY], c.n2);
+  update_both_ghosts(c, c.f[MIBM_F_VZ], c.n2);
+  update_both_ghosts(c, c.f[MIBM_F_TEMP], c.n2);
+  if (!c.I(MIBM_I_STATIONARY)) tagCells(c);           // diss.f90:47-50
+  const F3 &vx = c.f[MIBM_F_VX], &vy = c.f[MIBM_F_VY], &vz = c.f[MIBM_F_VZ], &temp = c.f[MIBM_F_TEMP];
+  const F3& VOFp = c.f[MIBM_F_VOFP];
+  const double ren = c.S(MIBM_S_REN), pec = c.S(MIBM_S_PEC), tliq = c.S(MIBM_S_TLIQ);
+  const double* vcm = c.s[MIBM_S_VEL_CM];
+  const double udx1 = c.dx1, udx2 = c.dx2, udx3 = c.dx3;
+  double sumvof = 0, kenerg = 0, diss_volAvg = 0, chi_volAvg = 0, enstrophy = 0;
+  double uf[3] = {0, 0, 0}, uvar[3] = {0, 0, 0}, urel[3] = {0, 0, 0}, uurel[3] = {0, 0, 0};
+  double Tfluid = 0, DT_fluid = 0, DT2_fluid = 0;
+  long long counter = 0;
+  for (int kc = 1; kc <= c.n3m; ++kc) {
+    int kp = kc + 1, km = kc - 1;
+    for (int jc = 1; jc <= c.n2m; ++jc) {
+      int jm = c.jmv[jc], jp = c.jpv[jc];
+      for (int ic = 1; ic <= c.n1m; ++ic) {
+        int im = c.imv[ic], ip = c.ipv[ic];
+        double h11 = (vx(ip, jc, kc) - vx(ic, jc, kc)) * udx1;
+        double h12 = ((vx(ic, jp, kc) + vx(ip, jp, kc)) - (vx(ic, jm, kc) + vx(ip, jm, kc))) * 0.25 * udx2;
+        double h13 = ((vx(ic, jc, kp) + vx(ip, jc, kp)) - (vx(ic, jc, km) + vx(ip, jc, km))) * 0.25 * udx3;
+        double h21 = ((vy(ip, jc, kc) + vy(ip, jp, kc)) - (vy(im, jc, kc) + vy(im, jp, kc))) * 0.25 * udx1;
+        double h22 = (vy(ic, jp, kc) - vy(ic, jc, kc)) * udx2;
+        double h23 = ((vy(ic, jc, kp) + vy(ic, jp, kp)) - (vy(ic, jc, km) + vy(ic, jp, km))) * 0.25 * udx3;
+        double h31 = ((vz(ip, jc, kc) + vz(ip, jc, kp)) - (vz(im, jc, kc) + vz(im, jc, kp))) * 0.25 * udx1;
+        double h32 = ((vz(ic, jp, kc) + vz(ic, jp, kp)) - (vz(ic, jm, kc) + vz(ic, jm, kp))) * 0.25 * udx2;
+        double h33 = (vz(ic, jc, kp) - vz(ic, jc, kc)) * udx3;
+        double tke = (sq(vx(ic, jc, kc)) + sq(vx(ip, jc, kc)) + sq(vy(ic, jc, kc)) + sq(vy(ic, jp, kc)) +
+                      sq(vz(ic, jc, kc)) + sq(vz(ic, jc, kp))) * 0.5;
+        tke = tke * 0.5;
+        double diss = sq(h11) + sq(h22) + sq(h33) + 0.5 * sq(h21 + h12) + 0.5 * sq(h31 + h13) + 0.5 * sq(h32 + h23);
+        diss = diss * 2.0 / ren;
+        double chi = sq(0.5 * c.dx1 * (temp(ip, jc, kc) - temp(im, jc, kc))) +
+                     sq(0.5 * c.dx2 * (temp(ic, jp, kc) - temp(ic, jm, kc))) +
+                     sq(0.5 * c.dx3 * (temp(ic, jc, kp) - temp(ic, jc, km)));
+        chi = chi / pec;
+        // vorticity.f90:45-77: the same differences, scaled after the 0.25
+        double vorx = h32 - h23, vory = h13 - h31, vorz = h21 - h12;
+        if (VOFp(ic, jc, kc) == 1.0) {
+          sumvof = sumvof + VOFp(ic, jc, kc);
+          kenerg = kenerg + tke;
+          diss_volAvg = diss_volAvg + diss;
+          chi_volAvg = chi_volAvg + chi;
+          enstrophy = enstrophy + (sq(vorx) + sq(vory) + sq(vorz));
+          ++counter;
+          double q[3] = {vx(ic, jc, kc), vy(ic, jc, kc), vz(ic, jc, kc)};
+          for (int d = 0; d < 3; ++d) {
+            uf[d] = uf[d] + q[d];
+            uvar[d] = uvar[d] + sq(q[d]);
+            urel[d] = urel[d] + (q[d] - vcm[d]);
+            uurel[d] = uurel[d] + sq(q[d] - vcm[d]);
+          }
+          double T = temp(ic, jc, kc);
+          Tfluid = Tfluid + T;
+          DT_fluid = DT_fluid + (T - tliq);
+          DT2_fluid = DT2_fluid + sq(T - tliq);
+        }
+      }
+    }
+  }
+  // diss.f90:160-186, vorticity.f90:93-95, calcSlipVels.f90:134-168
+  double nu = 1.0 / ren;
+  kenerg = kenerg / sumvof;
+  diss_volAvg = diss_volAvg / sumvof;
+  chi_volAvg = chi_volAvg / sumvof;
+  double urms = std::sqrt(2.0 / 3.0 * kenerg);
+  double eta = std::pow(nu * nu * nu / diss_volAvg, 0.25);
+  double Re_L = kenerg * kenerg / (nu * diss_volAvg);
+  double lambda_t = std::sqrt(15.0 * nu * urms * urms / diss_volAvg);
+  double re_lam = urms * lambda_t / nu;
+  double L_int = std::sqrt(kenerg * kenerg * kenerg) / diss_volAvg;
+  double n = (double)counter;
+  double o[MIBM_NDIAG] = {diss_volAvg, kenerg, urms, eta, lambda_t, Re_L, re_lam, L_int, chi_volAvg,
+                          enstrophy / sumvof, n,
+                          uf[0] / n, uf[1] / n, uf[2] / n, uvar[0] / n, uvar[1] / n, uvar[2] / n,
+                          urel[0] / n, urel[1] / n, urel[2] / n, uurel[0] / n, uurel[1] / n, uurel[2] / n,
+                          Tfluid / n, DT_fluid / n, DT2_fluid / n};
+  for (int q = 0; q < MIBM_NDIAG; ++q) out[q] = o[q];
+}
+
+// ------------------------------------------------------------------------
 // tsch.f90:1-99
 // ------------------------------------------------------------------------
 void tschem(Ctx& c) {
@@ -1702,6 +1793,7 @@ void tschem(Ctx& c) {
     update_both_ghosts(c, c.f[MIBM_F_PR], c.n2);
     update_both_ghosts(c, c.f[MIBM_F_TEMP], c.n2);
   }
+  if (c.diag_on) c.diag_stepped = true;
 }
 
 // cfl.f90:1-31 (ip, jp, kp are not wrapped: column n1, row n2 and ghost
@@ -2196,6 +2288,20 @@ DROPIN(mls_heatflux_, mls_heatFlux)
 DROPIN(apply_stefancondition_, apply_StefanCondition)
 DROPIN(tagcells_, tagCells)
 DROPIN(particle_, particle)
+int mibm_diagnostics_(double* out) {
+  Ctx* c = cur(); if (!ready(c)) return t_status;
+  diagnostics(*c, out);
+  c->diag_stepped = true;
+  return c->status;
+}
+// the oracle computes on request: the state has not changed since the step
+void mibm_set_diagnostics_(const int* on) { Ctx* c = cur(); if (c) c->diag_on = *on != 0; }
+int mibm_diagnostics_get_(double* out) {
+  Ctx* c = cur(); if (!ready(c)) return t_status;
+  if (!c->diag_stepped) { fail(c, MIBM_ESTATE, "diagnostics: no step computed them"); return MIBM_ESTATE; }
+  diagnostics(*c, out);
+  return c->status;
+}
 DROPIN(mls_structloads_, mls_structLoads)
 DROPIN(update_part_pos_, update_part_pos)
 DROPIN(cfl_, cfl)

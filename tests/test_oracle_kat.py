@@ -329,3 +329,35 @@ def test_abc_forcing_closed_form(oracle_lib):
     for c, fid in enumerate((abi.MIBM_F_FORCX, abi.MIBM_F_FORCY, abi.MIBM_F_FORCZ)):
         assert np.max(np.abs(case.interior(fid) - want[c])) <= 1e-14
     case.detach(oracle_lib)
+
+
+def test_diagnostics_shear_flow_kat(oracle_lib):
+    """CalcDissipation / vorticity / calcFluidVelAvgs on u = A sin(k y), no
+    body (every cell fluid): the central difference du/dy = A k' cos(ky) with
+    k' = sin(k dy)/dy gives mean dissipation (A k')^2 / (2 Re), enstrophy
+    (A k')^2 / 2, kinetic energy A^2/4 (diss.f90:69-141, vorticity.f90:45-83)."""
+    cfg = small_config(n=16, level=2, imlsfor=0, imelt=0, velocity="rest")
+    c = Case(cfg)
+    A_, k = 0.7, 3
+    dy = c.ylen / c.n2m
+    u = A_ * np.sin(k * c.ym)
+    c.fields[abi.MIBM_F_VX][:c.n1m, :c.n2m, :] = u[None, :, None]
+    c.fields[abi.MIBM_F_TEMP][...] = 0.25
+    c.attach(oracle_lib, initial_tag=False)
+    out = np.zeros(abi.MIBM_NDIAG)
+    assert oracle_lib.mibm_diagnostics_(out.ctypes.data) == 0
+    kp = np.sin(k * dy) / dy
+    ren = c.S(abi.MIBM_S_REN)
+    D = abi
+    assert out[D.MIBM_D_NFLUID] == c.n1m * c.n2m * c.n3m
+    assert abs(out[D.MIBM_D_DISS] - (A_ * kp) ** 2 / (2 * ren)) < 1e-14
+    assert abs(out[D.MIBM_D_ENSTROPHY] - (A_ * kp) ** 2 / 2) < 1e-13
+    # sums over 16^3 cells in the reference's order: round-off ~1e-14
+    assert abs(out[D.MIBM_D_KENERG] - A_ ** 2 / 4) < 1e-13
+    assert abs(out[D.MIBM_D_URMS] - np.sqrt(2.0 / 3.0 * A_ ** 2 / 4)) < 1e-13
+    assert abs(out[D.MIBM_D_U]) < 1e-14 and abs(out[D.MIBM_D_UU] - A_ ** 2 / 2) < 1e-13
+    assert out[D.MIBM_D_CHI] == 0.0 and out[D.MIBM_D_T] == 0.25
+    nu = 1.0 / ren
+    eps = out[D.MIBM_D_DISS]
+    lam = np.sqrt(15 * nu * out[D.MIBM_D_URMS] ** 2 / eps)
+    assert abs(out[D.MIBM_D_RE_LAMBDA] - out[D.MIBM_D_URMS] * lam / nu) < 1e-10
