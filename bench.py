@@ -283,6 +283,12 @@ def run_gpu(args):
     launches = int(lib.mibm_launch_count_() - l0)
     lib.check("timed steps")
     div64 = lib.mibm_divergence_max_()
+    diag = np.zeros(abi.MIBM_NDIAG)
+    diagnostics = None
+    if lib.mibm_diagnostics_(diag.ctypes.data) == 0:
+        diagnostics = {"re_lambda": float(diag[abi.MIBM_D_RE_LAMBDA]), "dissipation": float(diag[abi.MIBM_D_DISS]),
+                       "kinetic_energy": float(diag[abi.MIBM_D_KENERG]), "eta": float(diag[abi.MIBM_D_ETA]),
+                       "after_steps": nt - 1}
     case.sync_to_host(lib, FIELD_MASK)
     snap64 = {k: case.interior(f).copy() for k, f in FIELDS.items()}
     dist.barrier()
@@ -398,6 +404,7 @@ def run_gpu(args):
             "e2e": {"value": e2e_value, "unit": "Mcell-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "roofline": roofline, "gpu_launches": launches, "clocks": clocks, "fp32_refined": fp32,
+            "diagnostics": diagnostics,
             "host_wall_ms_per_step": 1e3 * wall / args.steps, "kernels": kernels}
     if dist.ws == 1 and not args.no_batch:
         line["batched"] = batched_measurement(lib, args.batch_steps, args.warmup)
