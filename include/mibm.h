@@ -288,6 +288,27 @@ void mibm_hit_bhat_(double* bhat, const int* dir);
 /* term adds VOF * C_HIT * u (hdnl1.f90:74 divides forcx by xlen).         */
 void mibm_linear_hit_force_(void);
 
+/* Remeshing hand-off (particle.f90:119-160, 196-200).  The remesher edits  */
+/* the mesh topology (edge collapses, vertex smoothing: remesh_coarsen.f90,  */
+/* remesh_smooth.f90) and stays with the host.  With iremesh = 1 the device  */
+/* computes the edge lengths every substep after the body has moved        */
+/* (calculate_eLengths, triaux.f90:277-306); when a live edge is shorter    */
+/* than E_thresh the library writes the current mesh to the registered     */
+/* host arrays (every mesh array; tri_nor from update_tri_normal, and the   */
+/* registered Volume set to calculate_volume of that mesh) and calls the    */
+/* host's remesher `fn(user)`, which edits those arrays in place and        */
+/* returns 0, or nonzero to abort the run (the volume-residual check of     */
+/* particle.f90:205-216) -- the library then reports MIBM_EABORT.  The       */
+/* library uploads the mesh, rebuilds what depends on its topology, and     */
+/* continues the substep: primitive geometry, then update_tri_velocity      */
+/* (RigidAuxRoutines.f90:902-928).  A step with iremesh = 1 runs without a  */
+/* step graph and reads the trigger once per substep (one host              */
+/* synchronisation).  A trigger with no remesher set stops the step with    */
+/* MIBM_ESTATE.  mibm_remesh_count_: hand-offs done by the bound context.   */
+typedef int (*mibm_remesh_fn)(void* user);
+void mibm_set_remesh_callback_(mibm_remesh_fn fn, void* user);
+int  mibm_remesh_count_(void);
+
 /* Per-step diagnostics.  The reference's CalcDissipation (diss.f90:11-201), */
 /* vorticity (vorticity.f90:1-109) and calcFluidVelAvgs (calcSlipVels.f90:   */
 /* 17-181), called after every tschem (gcurv.f90:194-203), sum over the     */

@@ -77,6 +77,8 @@ SIGNATURES: dict[str, tuple] = {
     "mibm_batch_step_": (C.c_int, [_I, _I]),
     "mibm_batch_destroy_": (C.c_int, [_I]),
     "mibm_divergence_max_": (C.c_double, []),
+    "mibm_set_remesh_callback_": (None, [C.c_void_p, C.c_void_p]),
+    "mibm_remesh_count_": (C.c_int, []),
     "mibm_diagnostics_": (C.c_int, [C.c_void_p]),
     "mibm_set_diagnostics_": (None, [_I]),
     "mibm_diagnostics_get_": (C.c_int, [C.c_void_p]),
@@ -99,9 +101,14 @@ for _n in VOID_ROUTINES:
     SIGNATURES[_n] = (None, [])
 
 
+#: C type of the host remesher passed to mibm_set_remesh_callback_
+REMESH_FN = C.CFUNCTYPE(C.c_int, C.c_void_p)
+
+
 def header_symbols() -> list[str]:
     """Every function name declared in include/mibm.h."""
     text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    text = re.sub(r"typedef[^;]*;", "", text)
     return re.findall(r"\b([a-z_][a-z0-9_]*)\s*\((?:[^;{]*?)\)\s*;", text)
 
 

@@ -267,6 +267,12 @@ static uint64_t step_key(Ctx* c) {
   return h;
 }
 
+// A step becomes a graph from its second call, unless kernels are being
+// profiled one by one or the step may stop for the host's remesher.
+static bool graphs_allowed(Ctx* c) {
+  return c->use_graph && c->steps_done >= 1 && !c->profiling && !lagr_remesh_active(c);
+}
+
 static void drop_graph(Ctx* c) {
   if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
   if (c->graph) cudaGraphDestroy(c->graph);
@@ -314,7 +320,7 @@ static bool capture_step(Ctx* c, uint64_t key) {
 // runs as a captured graph (one launch per step) while its key holds.
 static void tschem(Ctx* c) {
   if (!step_prepare(c)) return;
-  bool graph = c->use_graph && c->steps_done >= 1 && !c->profiling;
+  bool graph = graphs_allowed(c);
   if (graph) {
     uint64_t key = step_key(c);
     if (!c->graph_exec || key != c->graph_key) graph = capture_step(c, key);
@@ -470,7 +476,7 @@ static int batch_step(Batch* b, int ntime) {
   // (C) device work: step graphs (captured where missing or stale)
   bool all_graphs = true;
   for (Ctx* c : cs) {
-    bool graph = c->use_graph && c->steps_done >= 1 && !c->profiling;
+    bool graph = graphs_allowed(c);
     if (graph) {
       uint64_t key = step_key(c);
       if (!c->graph_exec || key != c->graph_key) graph = capture_step(c, key);
@@ -501,7 +507,7 @@ static int batch_step(Batch* b, int ntime) {
     if (!cuda_ok(cs[0], cudaStreamSynchronize(b->stream), "batch graph")) return cs[0]->status;
   } else {
     for (Ctx* c : cs) {
-      if (c->use_graph && c->graph_exec && c->steps_done >= 1 && !c->profiling) {
+      if (c->graph_exec && graphs_allowed(c)) {
         if (!cuda_ok(c, cudaGraphLaunch(c->graph_exec, c->stream), "step graph")) return c->status;
         c->launches += c->graph_kernels;
       } else {
@@ -754,6 +760,18 @@ void mibm_set_graphs_(const int* on) {
   Ctx* c = current(); if (!ready(c)) return;
   c->use_graph = *on != 0;
   if (!c->use_graph) drop_graph(c);
+}
+
+// The host's remesher (see include/mibm.h); fn = NULL removes it.
+void mibm_set_remesh_callback_(mibm_remesh_fn fn, void* user) {
+  Ctx* c = current(); if (!ready(c)) return;
+  c->remesh_fn = fn;
+  c->remesh_user = user;
+}
+
+int mibm_remesh_count_(void) {
+  Ctx* c = current(); if (!c) return 0;
+  return c->remesh_count;
 }
 
 // Diagnostics (diag.cu): computed now, or per step inside tschem_.

@@ -161,6 +161,10 @@ struct Ctx {
   int tune_by = 8;                        // block height of the explicit-term kernel
   uint64_t tune_gen = 0;
   double* step_host = nullptr;            // pinned: geometry scalars read back at step end
+  // remeshing hand-off: the host's remesher and the hand-offs done
+  mibm_remesh_fn remesh_fn = nullptr;
+  void* remesh_user = nullptr;
+  int remesh_count = 0;
   // per-step diagnostics (diag.cu): requested, last values, device state
   bool diag_on = false, diag_valid = false;
   double diag_last[MIBM_NDIAG] = {0};
@@ -336,6 +340,8 @@ void lagr_step_readback(Ctx* c);
 void lagr_step_host_finish(Ctx* c);
 void lagr_geometry_to_host(Ctx* c);
 void lagr_invalidate(Ctx* c);
+void lagr_topology_changed(Ctx* c);
+bool lagr_remesh_active(Ctx* c);
 void lagr_free(Ctx* c);
 // ctx.cu
 bool ensure_params(Ctx* c);

@@ -423,8 +423,11 @@ void mibm_sync_from_host_(const long long* mask) {
   for (int i = 0; i < MIBM_NMESH && c->maxnf > 0; ++i)
     if ((m >> 32) & (1ull << i))
       cuda_ok(c, cudaMemcpyAsync(c->dm[i], c->hm[i], mesh_bytes(c, i), cudaMemcpyHostToDevice, c->stream), "H2D mesh");
-  // the scatter plan and the MLS weights depend on the mesh
-  if ((m >> 32) != 0) lagr_invalidate(c);
+  // the scatter plan and the MLS weights depend on the mesh, the
+  // vertex->face lists on its connectivity
+  const unsigned long long topo = (1ull << MIBM_M_VERT_OF_FACE) | (1ull << MIBM_M_GHOST_FACE);
+  if ((m >> 32) & topo) lagr_topology_changed(c);
+  else if ((m >> 32) != 0) lagr_invalidate(c);
   cuda_ok(c, cudaStreamSynchronize(c->stream), "sync_from_host");
   if (c->maxnf > 0 && ((m >> 32) & ((1ull << MIBM_M_VERT_OF_FACE) | (1ull << MIBM_M_GHOST_FACE)))) validate_mesh(c);
 }

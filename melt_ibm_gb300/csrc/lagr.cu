@@ -22,6 +22,8 @@
 // (non-negative) IEEE bit pattern and the earliest triangle among equal
 // distances, exactly the strict "<" update rule of genSDF.f90:167.
 #include <climits>
+#include <string>
+#include <cstddef>
 #include <cmath>
 #include <vector>
 
@@ -1238,6 +1240,48 @@ __global__ void geom_reduce_kernel(int nb, const double* __restrict__ part, doub
   }
 }
 
+// calculate_eLengths (triaux.f90:277-306); flag bit 0 set when a live edge
+// is shorter than thresh (the remesh trigger rm_flag)
+__global__ void elength_kernel(int ne, const int* __restrict__ voe, const int* __restrict__ ghoste,
+                               const double* __restrict__ x, double thresh, double* __restrict__ el,
+                               int* __restrict__ flag) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne || ghoste[e]) return;
+  int v1 = voe[2 * e] - 1, v2 = voe[2 * e + 1] - 1;
+  double len = sqrt(sqd(x[3 * v1] - x[3 * v2]) + sqd(x[3 * v1 + 1] - x[3 * v2 + 1]) + sqd(x[3 * v1 + 2] - x[3 * v2 + 2]));
+  el[e] = len;
+  if (flag && len < thresh) atomicOr(flag, 1);
+}
+
+// calculate_skewness (triaux.f90:325-358)
+__global__ void skewness_kernel(int nf, const int* __restrict__ eof, const int* __restrict__ ghost,
+                                const double* __restrict__ el, const double* __restrict__ sur,
+                                double* __restrict__ skew) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nf || ghost[t]) return;
+  double perim = el[eof[3 * t] - 1] + el[eof[3 * t + 1] - 1] + el[eof[3 * t + 2] - 1];
+  double sur_opt = sqrt(3.0) / 4.0 * sqd(perim / 3.0);
+  skew[t] = (sur_opt - sur[t]) / sur_opt;
+}
+
+// update_tri_velocity (RigidAuxRoutines.f90:902-928) after a remesh:
+// vel_tri = vel_CM + omega x (tri_bar - pos_CM), pos_CM of the refreshed
+// geometry (geom + 3)
+__global__ void tri_velocity_kernel(int nf, const int* __restrict__ ghost, const double* __restrict__ bar,
+                                    const double* __restrict__ geom, const double* __restrict__ vel,
+                                    const double* __restrict__ om, double* __restrict__ vel_tri) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nf || ghost[t]) return;
+  double r[3];
+  for (int d = 0; d < 3; ++d) r[d] = bar[3 * t + d] - geom[3 + d];
+  double c0 = om[1] * r[2] - r[1] * om[2];
+  double c1 = om[2] * r[0] - r[2] * om[0];
+  double c2 = om[0] * r[1] - r[0] * om[1];
+  vel_tri[3 * t] = vel[0] + c0;
+  vel_tri[3 * t + 1] = vel[1] + c1;
+  vel_tri[3 * t + 2] = vel[2] + c2;
+}
+
 __global__ void cfac_kernel(int nf, const double* __restrict__ sur, double h, double celvol, double* __restrict__ cfac) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t < nf) cfac[t] = (sur[t] * h) / celvol;
@@ -1565,6 +1609,7 @@ struct LagState {
   double* face_part = nullptr;
   double* geom_out = nullptr;   // device [Surface, Volume1, Vol, Cx, Cy, Cz, InertTensor(9)]
   double* loads_ev = nullptr;   // structural loads: 12 block sums per 32 faces
+  int* rm_flag = nullptr;       // remesh trigger (device)
   double* mean3 = nullptr;
   unsigned long long* sdf_bits = nullptr;
   int* winner = nullptr;
@@ -1605,6 +1650,13 @@ void lagr_invalidate(Ctx* c) {
   s->force_rebuild = true;
   s->weights_valid = false;
   ++c->lag_gen;
+}
+
+// the face/vertex/edge relations changed (a remesh or a host upload of the
+// connectivity): rebuild the vertex->face lists too
+void lagr_topology_changed(Ctx* c) {
+  lagr_invalidate(c);
+  lag_of(c)->adj_nf = -1;
 }
 
 static bool ensure_adjacency(Ctx* c) {
@@ -1905,6 +1957,16 @@ static void geometry_launch(Ctx* c, bool imelt, bool body_only = false) {
   { MIBM_PROF(c, "geom_reduce");
     geom_reduce_kernel<<<1, 256, 0, c->stream>>>(gnb, s->face_part, c->S(MIBM_S_DENS_RATIO), s->geom_out); }
   c->launches += 3;
+  if (c->maxne > 0) {           // calculate_eLengths, calculate_skewness (particle.f90:173-176)
+    MIBM_PROF(c, "edges");
+    elength_kernel<<<div_up(c->maxne, 128), 128, 0, c->stream>>>(
+        c->maxne, M<int>(c, MIBM_M_VERT_OF_EDGE), M<int>(c, MIBM_M_GHOST_EDGE), M<double>(c, MIBM_M_XYZV), 0.0,
+        M<double>(c, MIBM_M_ELENGTHS), nullptr);
+    skewness_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(
+        c->maxnf, M<int>(c, MIBM_M_EDGE_OF_FACE), M<int>(c, MIBM_M_GHOST_FACE), M<double>(c, MIBM_M_ELENGTHS),
+        M<double>(c, MIBM_M_SUR), M<double>(c, MIBM_M_SKEWNESS));
+    c->launches += 2;
+  }
   if (imelt) {
     { MIBM_PROF(c, "cfac");
       cfac_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(c->maxnf, M<double>(c, MIBM_M_SUR),
@@ -2061,6 +2123,71 @@ void lagr_tag_initial(Ctx* c) {
   lagr_tag_narrow_band(c);
 }
 
+bool lagr_remesh_active(Ctx* c) {
+  return c->I(MIBM_I_IREMESH) == 1 && c->I(MIBM_I_IMLSFOR) == 1 && c->maxnf > 0 && c->maxne > 0;
+}
+
+// particle.f90:119-160: the trigger (calculate_eLengths of the moved mesh)
+// read on the host, and when it fires the hand-off to the host's remesher.
+// Returns true if the mesh was remeshed.  Synchronises the stream.
+static bool remesh_check(Ctx* c) {
+  LagState* s = lag_of(c);
+  if (!s->rm_flag && !cuda_ok(c, cudaMalloc(&s->rm_flag, sizeof(int)), "remesh")) return false;
+  cudaMemsetAsync(s->rm_flag, 0, sizeof(int), c->stream);
+  { MIBM_PROF(c, "edges");
+    elength_kernel<<<div_up(c->maxne, 128), 128, 0, c->stream>>>(
+        c->maxne, M<int>(c, MIBM_M_VERT_OF_EDGE), M<int>(c, MIBM_M_GHOST_EDGE), M<double>(c, MIBM_M_XYZV),
+        c->S(MIBM_S_E_THRESH), M<double>(c, MIBM_M_ELENGTHS), s->rm_flag); }
+  ++c->launches;
+  cudaMemcpyAsync(c->hflag + 1, s->rm_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "remesh trigger")) return false;
+  if (!c->hflag[1]) return false;
+  if (!c->remesh_fn) {
+    fail(c, MIBM_ESTATE, "remeshing triggered (an edge is shorter than E_thresh) but no remesher is set "
+                         "(mibm_set_remesh_callback_)");
+    return false;
+  }
+  // update_tri_normal of the moved mesh and its volume, then every mesh
+  // array to the host
+  geometry_launch(c, false, true);
+  cudaMemcpyAsync(c->red_host, s->geom_out, sizeof(double) * 2, cudaMemcpyDeviceToHost, c->stream);
+  for (int i = 0; i < MIBM_NMESH; ++i)
+    cudaMemcpyAsync(c->hm[i], c->dm[i], mesh_bytes(c, i), cudaMemcpyDeviceToHost, c->stream);
+  if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "remesh download")) return false;
+  *c->hs[MIBM_S_VOLUME] = c->red_host[1];          // calculate_volume
+  int st = c->remesh_fn(c->remesh_user);
+  if (st != 0) {
+    fail(c, MIBM_EABORT, "remesher returned " + std::to_string(st));
+    return false;
+  }
+  for (int i = 0; i < MIBM_NMESH; ++i)
+    cudaMemcpyAsync(c->dm[i], c->hm[i], mesh_bytes(c, i), cudaMemcpyHostToDevice, c->stream);
+  if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "remesh upload")) return false;
+  lagr_topology_changed(c);
+  ++c->remesh_count;
+  return ensure_adjacency(c);
+}
+
+static void tri_velocity_launch(Ctx* c, const double* vel, const double* om) {
+  MIBM_PROF(c, "tri_velocity");
+  tri_velocity_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(
+      c->maxnf, M<int>(c, MIBM_M_GHOST_FACE), M<double>(c, MIBM_M_TRI_BAR), lag_of(c)->geom_out, vel, om,
+      M<double>(c, MIBM_M_VEL_TRI));
+  ++c->launches;
+}
+
+// device addresses of vel_CM and omega_c for update_tri_velocity: the moving
+// body's state, else the values the substep was given
+static void body_velocity(Ctx* c, const StepParams* dp, const double** vel, const double** om) {
+  if (c->I(MIBM_I_IMLSSTR) == 1 && c->drigid) {
+    *vel = (const double*)((const char*)c->drigid + offsetof(RigidDev, vel));
+    *om = (const double*)((const char*)c->drigid + offsetof(RigidDev, om));
+  } else {
+    *vel = (const double*)((const char*)dp + offsetof(StepParams, vel));
+    *om = (const double*)((const char*)dp + offsetof(StepParams, om));
+  }
+}
+
 // particle.f90:38-193 (drop-in particle_): dense force fields, host checks
 void lagr_particle(Ctx* c, const StepParams* dp) {
   if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0) return;
@@ -2089,7 +2216,14 @@ void lagr_particle(Ctx* c, const StepParams* dp) {
   if (imelt) lagr_stefan(c, dp);
   if (!ensure_adjacency(c) || !ensure_lag_buffers(c)) return;
   if (str) motion_launch(c, dp);
+  bool remeshed = lagr_remesh_active(c) && remesh_check(c);
+  if (c->status != MIBM_OK) return;
   geometry_launch(c, imelt);
+  if (remeshed) {
+    const double *vel, *om;
+    body_velocity(c, dp, &vel, &om);
+    tri_velocity_launch(c, vel, om);
+  }
   if (str) {
     k_rigid_publish(c, lag_of(c)->geom_out, nullptr);
     rigid_download(c);
@@ -2138,7 +2272,14 @@ const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror,
   scatter(c, true, 3, 4, false, t_mirror);
   if (imelt) lagr_stefan(c, dp);
   if (str) motion_launch(c, dp);
+  bool remeshed = lagr_remesh_active(c) && remesh_check(c);
+  if (c->status != MIBM_OK) return nullptr;
   geometry_launch(c, imelt);
+  if (remeshed) {
+    const double *vel, *om;
+    body_velocity(c, dp, &vel, &om);
+    tri_velocity_launch(c, vel, om);
+  }
   if (str) k_rigid_publish(c, s->geom_out, next);
   MIBM_LAUNCH_CHECK(c, "particle");
   return s->mean3;
@@ -2180,7 +2321,7 @@ void lagr_free(Ctx* c) {
     if (g_lag[q]->c == c) {
       LagState* s = g_lag[q];
       cudaFree(s->adj_off); cudaFree(s->adj_face); cudaFree(s->face_part); cudaFree(s->geom_out);
-      cudaFree(s->loads_ev);
+      cudaFree(s->loads_ev); cudaFree(s->rm_flag);
       cudaFree(s->mean3); cudaFree(s->sdf_bits); cudaFree(s->winner); cudaFree(s->dist_buf);
       cudaFree(s->band_ub); cudaFree(s->face4); cudaFree(s->face_cell); cudaFree(s->cm32);
       cudaFree(s->band_list); cudaFree(s->band_count);

@@ -87,6 +87,9 @@ struct Ctx {
   uint64_t hit_rng = 0;
   int steps_done = 0;   // batch steps completed (per-case step counter)
   bool diag_on = false, diag_stepped = false;   // per-step diagnostics requested / computed
+  mibm_remesh_fn remesh_fn = nullptr;           // the host's remesher
+  void* remesh_user = nullptr;
+  int remesh_count = 0;
   // coordinate accessors with the reference's extended ranges (cordin.f90:55-61)
   double xc(int i) const { return xc_[i + n1]; }
   double yc(int j) const { return yc_[j + n2]; }
@@ -109,6 +112,11 @@ struct Ctx {
   double& avert(int v) { return md(MIBM_M_AVERT)[v - 1]; }
   double& vel_tri(int c, int t) { return md(MIBM_M_VEL_TRI)[(size_t)(t - 1) * 3 + (c - 1)]; }
   double& cfac(int t) { return md(MIBM_M_CFAC)[t - 1]; }
+  int voe(int c, int e) { return mi(MIBM_M_VERT_OF_EDGE)[(size_t)(e - 1) * 2 + (c - 1)]; }
+  int eof(int c, int f) { return mi(MIBM_M_EDGE_OF_FACE)[(size_t)(f - 1) * 3 + (c - 1)]; }
+  bool ghoste(int e) { return mi(MIBM_M_GHOST_EDGE)[e - 1] != 0; }
+  double& elen(int e) { return md(MIBM_M_ELENGTHS)[e - 1]; }
+  double& skew(int t) { return md(MIBM_M_SKEWNESS)[t - 1]; }
   bool ghostf(int t) { return mi(MIBM_M_GHOST_FACE)[t - 1] != 0; }
   bool ghostv(int v) { return mi(MIBM_M_GHOST_VERT)[v - 1] != 0; }
   int& pind(int c, int t) { return mi(MIBM_M_PIND)[(size_t)(t - 1) * 6 + (c - 1)]; }
@@ -1200,6 +1208,29 @@ void calculate_areaWeighted_vert_normal(Ctx& c) {
   }
 }
 
+// calculate_eLengths triaux.f90:277-306: returns rm_flag
+bool calculate_eLengths(Ctx& c, double edge_thresh) {
+  bool rm_flag = false;
+  for (int i = 1; i <= c.maxne; ++i) {
+    if (c.ghoste(i)) continue;
+    int v1 = c.voe(1, i), v2 = c.voe(2, i);
+    c.elen(i) = std::sqrt(sq(c.xyzv(1, v1) - c.xyzv(1, v2)) + sq(c.xyzv(2, v1) - c.xyzv(2, v2)) +
+                          sq(c.xyzv(3, v1) - c.xyzv(3, v2)));
+    if (c.elen(i) < edge_thresh) rm_flag = true;
+  }
+  return rm_flag;
+}
+
+// calculate_skewness triaux.f90:325-358
+void calculate_skewness(Ctx& c) {
+  for (int i = 1; i <= c.maxnf; ++i) {
+    if (c.ghostf(i)) continue;
+    double perim = c.elen(c.eof(1, i)) + c.elen(c.eof(2, i)) + c.elen(c.eof(3, i));
+    double sur_opt = std::sqrt(3.0) / 4.0 * sq(perim / 3.0);
+    c.skew(i) = (sur_opt - c.sur(i)) / sur_opt;
+  }
+}
+
 // calc_rigidBody_params RigidAuxRoutines.f90:653-780 (COM, volume; the
 // inertia tensor is returned through I[9] column-major)
 void calc_rigidBody_params(Ctx& c, double COM[3], double& Vol, double I[9]) {
@@ -1574,6 +1605,20 @@ void newton_euler(Ctx& c, const double prn[3], const double tau[3], const double
   for (int q = 0; q < 9; ++q) I[q] = I_LHS[q];
 }
 
+// update_tri_velocity RigidAuxRoutines.f90:902-928
+void update_tri_velocity(Ctx& c) {
+  const double* pos = c.s[MIBM_S_POS_CM];
+  const double* vel = c.s[MIBM_S_VEL_CM];
+  const double* om = c.s[MIBM_S_OMEGA_C];
+  for (int i = 1; i <= c.maxnf; ++i) {
+    if (c.ghostf(i)) continue;
+    double rad[3], omd[3];
+    for (int d = 0; d < 3; ++d) rad[d] = c.tri_bar(d + 1, i) - pos[d];
+    cross3(omd, om, rad);
+    for (int d = 0; d < 3; ++d) c.vel_tri(d + 1, i) = vel[d] + omd[d];
+  }
+}
+
 // update_part_pos + update_regular + update_xyz, RigidAuxRoutines.f90:1-126
 // and 818-868.  Collisions (coll.f90) never fire for one particle and
 // update_substepping then leaves the state unchanged.
@@ -1627,7 +1672,9 @@ void update_part_pos(Ctx& c) {
 // ------------------------------------------------------------------------
 void geometry_refresh(Ctx& c) {   // particle.f90:165-193
   c.S(MIBM_S_SURFACE) = calculate_area(c);
+  calculate_eLengths(c, 0.0);
   update_tri_normal(c);
+  calculate_skewness(c);
   calc_centroids_from_vert(c);
   calculate_vert_area(c);
   c.S(MIBM_S_VOLUME) = calculate_volume(c);
@@ -1668,7 +1715,22 @@ void particle(Ctx& c) {
     update_part_pos(c);
     if (c.status != MIBM_OK) return;
   }
+  // particle.f90:119-160: the remesher itself is the host's (see mibm.h)
+  bool did_remesh = false;
+  if (c.I(MIBM_I_IREMESH) == 1 && c.maxne > 0 && calculate_eLengths(c, c.S(MIBM_S_E_THRESH))) {
+    if (!c.remesh_fn) {
+      fail(&c, MIBM_ESTATE, "remeshing triggered (an edge is shorter than E_thresh) but no remesher is set");
+      return;
+    }
+    did_remesh = true;
+    update_tri_normal(c);
+    c.S(MIBM_S_VOLUME) = calculate_volume(c);
+    int st = c.remesh_fn(c.remesh_user);
+    if (st != 0) { fail(&c, MIBM_EABORT, "remesher returned " + std::to_string(st)); return; }
+    ++c.remesh_count;
+  }
   geometry_refresh(c);
+  if (did_remesh) update_tri_velocity(c);
   if (c.S(MIBM_S_VOLUME) < c.S(MIBM_S_V_THRESH)) fail(&c, MIBM_EABORT, "Geometry V/VE smaller than threshold");
 }
 
@@ -2294,6 +2356,11 @@ int mibm_diagnostics_(double* out) {
   c->diag_stepped = true;
   return c->status;
 }
+void mibm_set_remesh_callback_(mibm_remesh_fn fn, void* user) {
+  Ctx* c = cur(); if (!c) return;
+  c->remesh_fn = fn; c->remesh_user = user;
+}
+int mibm_remesh_count_(void) { Ctx* c = cur(); return c ? c->remesh_count : 0; }
 // the oracle computes on request: the state has not changed since the step
 void mibm_set_diagnostics_(const int* on) { Ctx* c = cur(); if (c) c->diag_on = *on != 0; }
 int mibm_diagnostics_get_(double* out) {

@@ -1,6 +1,8 @@
 """Test helpers: seeded cases, paired oracle/GPU runs, error norms."""
 from __future__ import annotations
 
+import ctypes as C
+
 import numpy as np
 
 from melt_ibm_gb300 import abi
@@ -68,3 +70,50 @@ def pair(case: Case, oracle_lib, gpu_lib, initial_tag: bool = True):
     co.attach(oracle_lib, initial_tag=initial_tag)
     cg.attach(gpu_lib, initial_tag=initial_tag)
     return co, cg
+
+
+def elength_range(mesh, scale):
+    """Shortest and longest edge of `mesh` scaled by `scale`."""
+    e = mesh.vert_of_edge - 1
+    d = np.linalg.norm(mesh.xyz[e[:, 0]] - mesh.xyz[e[:, 1]], axis=1) * scale
+    return float(d.min()), float(d.max())
+
+
+class CoarseningRemesher:
+    """A stand-in for the host's remesher in tests: it replaces the live mesh
+    by an icosphere of a coarser level, scaled to the body's mean radius and
+    centred on its vertex mean, in the same (larger) arrays -- the unused
+    vertices, edges and faces become ghosts, as after the reference's edge
+    collapses.  The melt velocities are reset.  A topology change as drastic
+    as a remesh can make, with a known result."""
+
+    def __init__(self, case, level):
+        from melt_ibm_gb300.mesh import icosphere
+        self.case, self.mesh, self.calls = case, icosphere(level), 0
+        self.fn = abi.REMESH_FN(self._call)
+
+    def _call(self, user):
+        A, M, m = abi, self.case.mesh_arrays, self.mesh
+        live = M[A.MIBM_M_GHOST_VERT] == 0
+        x = M[A.MIBM_M_XYZV][:, live].T
+        centre = x.mean(0)
+        radius = float(np.linalg.norm(x - centre, axis=1).mean())
+        nv, ne, nf = m.nv, m.ne, m.nf
+        M[A.MIBM_M_XYZV][:, :nv] = (m.xyz * radius + centre).T
+        M[A.MIBM_M_VERT_OF_FACE][:, :nf] = m.vert_of_face.T
+        M[A.MIBM_M_VERT_OF_FACE][:, nf:] = 1
+        M[A.MIBM_M_EDGE_OF_FACE][:, :nf] = m.edge_of_face.T
+        M[A.MIBM_M_EDGE_OF_FACE][:, nf:] = 1
+        M[A.MIBM_M_VERT_OF_EDGE][:, :ne] = m.vert_of_edge.T
+        M[A.MIBM_M_VERT_OF_EDGE][:, ne:] = 1
+        for mid, n in ((A.MIBM_M_GHOST_VERT, nv), (A.MIBM_M_GHOST_EDGE, ne), (A.MIBM_M_GHOST_FACE, nf)):
+            M[mid][:n] = 0
+            M[mid][n:] = 1
+        M[A.MIBM_M_VMELT][...] = 0.0
+        M[A.MIBM_M_VMELT_M1][...] = 0.0
+        self.calls += 1
+        return 0
+
+    def install(self, lib):
+        self.case.bind(lib)
+        lib.mibm_set_remesh_callback_(C.cast(self.fn, C.c_void_p), None)
