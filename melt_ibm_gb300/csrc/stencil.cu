@@ -44,6 +44,9 @@ struct StencilArgs {
   const float* __restrict__ w32;
   const float* __restrict__ t32;
   const float* __restrict__ p32;
+  // forcx/xlen, forcy/ylen, forcz/zlen (3 fields) formed once per step by
+  // the fused step; nullptr elsewhere
+  const double* __restrict__ fq;
   int coff;
   int forcing;
 };
@@ -74,9 +77,26 @@ static StencilArgs make_args(Ctx* c) {
   size_t n = c->g.cells;
   a.u32 = m; a.v32 = m ? m + n : nullptr; a.w32 = m ? m + 2 * n : nullptr;
   a.t32 = m ? m + 3 * n : nullptr; a.p32 = m ? m + 4 * n : nullptr;
+  a.fq = nullptr;
   a.coff = c->coord_off;
   a.forcing = c->I(MIBM_I_FORCING);
   return a;
+}
+
+// The forcing term VOF*forc/len of hdnl1/2/3 (hdnl1.f90:74): where VOF = 1
+// (every fluid cell) it equals forc/len, which the fused step forms once per
+// step (fq); the division stays for the interface cells, so the FP64 value is
+// the reference's bit for bit.
+template <typename R>
+__device__ __forceinline__ R forcing_term(const StencilArgs& A, const double* __restrict__ vof,
+                                          const double* __restrict__ forc, int comp, idx_t c0, R len) {
+  if constexpr (sizeof(R) == 8) {
+    double v = vof[c0];
+    if (A.fq && v == 1.0) return A.fq[(size_t)comp * A.g.cells + c0];
+    return (v * forc[c0]) / len;
+  } else {
+    return R(vof[c0]) * R(forc[c0]) / len;
+  }
 }
 
 // Cell index and the six periodic neighbour offsets in 32-bit arithmetic
@@ -119,7 +139,7 @@ __device__ __forceinline__ R h_x(const StencilArgs& A, idx_t c0, idx_t dip, idx_
   R h13 = ((vz[c0 + dkp] + vz[c0 + dim + dkp]) * (vx[c0 + dkp] + vxc) -
            (vz[c0] + vz[c0 + dim]) * (vxc + vx[c0 + dkm])) * udx3;
   R h = -(h11 + h12 + h13);
-  if (A.forcing) h = h + R(A.vofx[c0]) * R(A.forcx[c0]) / coef<R>(p, kXLEN);
+  if (A.forcing) h = h + forcing_term<R>(A, A.vofx, A.forcx, 0, c0, coef<R>(p, kXLEN));
   return h;
 }
 
@@ -137,7 +157,7 @@ __device__ __forceinline__ R h_y(const StencilArgs& A, idx_t c0, idx_t dip, idx_
   R h23 = ((vz[c0 + dkp] + vz[c0 + djm + dkp]) * (vy[c0 + dkp] + vyc) -
            (vz[c0] + vz[c0 + djm]) * (vyc + vy[c0 + dkm])) * udx3;
   R h = -(h21 + h22 + h23);
-  if (A.forcing) h = h + R(A.vofy[c0]) * R(A.forcy[c0]) / coef<R>(p, kYLEN);
+  if (A.forcing) h = h + forcing_term<R>(A, A.vofy, A.forcy, 1, c0, coef<R>(p, kYLEN));
   return h;
 }
 
@@ -159,7 +179,7 @@ __device__ __forceinline__ R h_z(const StencilArgs& A, idx_t c0, idx_t dip, idx_
     R T_interp = (F.t[c0] + F.t[c0 + dkm]) * R(0.5);
     h = h + coef<R>(p, kBETAGZ) * (T_interp - coef<R>(p, kTLIQ));
   }
-  if (A.forcing) h = h + R(A.vofz[c0]) * R(A.forcz[c0]) / coef<R>(p, kZLEN);
+  if (A.forcing) h = h + forcing_term<R>(A, A.vofz, A.forcz, 2, c0, coef<R>(p, kZLEN));
   return h;
 }
 
@@ -280,6 +300,7 @@ static void fused_rhs_launch(Ctx* c, const StepParams* dp, int w, R* ru, R* rhs)
   const int by = (c->tune_by == 2 || c->tune_by == 4) ? c->tune_by : 8;   // autotuned block height
   dim3 grid(div_up(c->g.n1m, 32), div_up(c->g.n2m, by), c->g.n3m), block(32, by);
   StencilArgs a = make_args(c);
+  if (c->forc_q_ready) a.fq = c->forc_q;
   switch (w) {
     case 0: fused_rhs_kernel<R, 0><<<grid, block, 0, c->stream>>>(a, dp, ru, rhs); break;
     case 1: fused_rhs_kernel<R, 1><<<grid, block, 0, c->stream>>>(a, dp, ru, rhs); break;
@@ -561,6 +582,28 @@ void k_invtr_rhs(Ctx* c, int which, const StepParams* dp, double* rhs_out) {
                                                                    ru_of(c, which), rhs_out); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "invtr_rhs");
+}
+
+__global__ void forc_quotient_kernel(size_t n, const double* __restrict__ fx, const double* __restrict__ fy,
+                                     const double* __restrict__ fz, double xlen, double ylen, double zlen,
+                                     double* __restrict__ q) {
+  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  q[t] = fx[t] / xlen;
+  q[n + t] = fy[t] / ylen;
+  q[2 * n + t] = fz[t] / zlen;
+}
+
+// forcx/xlen, forcy/ylen, forcz/zlen for the explicit terms of this step
+// (the forcing fields change once per step, before tschem)
+void k_forcing_quotient(Ctx* c) {
+  const size_t n = c->g.cells;
+  { MIBM_PROF(c, "forcing_quotient");
+    forc_quotient_kernel<<<div_up(n, 256), 256, 0, c->stream>>>(n, c->df[MIBM_F_FORCX], c->df[MIBM_F_FORCY],
+                                                               c->df[MIBM_F_FORCZ], c->g.xlen, c->g.ylen,
+                                                               c->g.zlen, c->forc_q); }
+  ++c->launches;
+  if (MIBM_LAUNCH_CHECK(c, "forcing quotient")) c->forc_q_ready = true;
 }
 
 void k_fused_rhs(Ctx* c, const StepParams* dp) {
