@@ -164,6 +164,7 @@ static void step_enqueue_f32(Ctx* c) {
   float* t_mirror = c->q32 + 3 * g.cells;
   for (int ns = 0; ns < 3; ++ns) {
     const StepParams* dp = c->dparams + ns;
+    lagr_join(c);
     if (!c->I(MIBM_I_STATIONARY) && c->I(MIBM_I_IMLSFOR) == 1) lagr_tag_narrow_band(c);
     k_fused_rhs_f32(c, dp, c->ru32, c->rhs32);
     for (int q = 0; q < 4; ++q) {
@@ -194,6 +195,7 @@ static void step_enqueue_f64(Ctx* c) {
   if (!tables) return;
   for (int ns = 0; ns < 3; ++ns) {
     const StepParams* dp = c->dparams + ns;
+    lagr_join(c);
     if (!c->I(MIBM_I_STATIONARY) && c->I(MIBM_I_IMLSFOR) == 1) lagr_tag_narrow_band(c);
     k_fused_rhs(c, dp);
     for (int q = 0; q < 4; ++q) {
@@ -227,11 +229,13 @@ static void step_enqueue(Ctx* c) {
   if (c->I(MIBM_I_FORCING) == 1 && c->precision == 0) k_forcing_quotient(c);
   if (c->precision == 1) step_enqueue_f32(c);
   else step_enqueue_f64(c);
+  lagr_join(c);
   if (c->status == MIBM_OK && c->diag_on) diag_enqueue(c, step_vel_cm(c));
   if (c->status == MIBM_OK) lagr_step_readback(c);
 }
 
 static void step_finish(Ctx* c) {
+  lagr_join(c);
   if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "tschem")) return;
   if (c->status != MIBM_OK) return;
   lagr_step_host_finish(c);

@@ -127,6 +127,11 @@ struct Ctx {
   double* tri_coef = nullptr;             // per triangle & component: cfac*(target-Um)
   double* lag_red = nullptr;              // per-triangle partial sums
   cudaStream_t stream = nullptr;
+  // second stream of the fused step: the Lagrangian work after the velocity
+  // forcing runs on it beside the pressure projection (fork / join events)
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  bool join_pending = false;
   // fused-step state
   StepParams* dparams = nullptr;          // [3] device copies (one per substep)
   StepParams* hparams = nullptr;          // pinned
@@ -340,6 +345,7 @@ void k_update_xyz(Ctx* c, bool centroids);
 void k_rigid_publish(Ctx* c, const double* geom, StepParams* next);
 void rigid_free(Ctx* c);
 void lagr_step_readback(Ctx* c);
+void lagr_join(Ctx* c);
 void lagr_step_host_finish(Ctx* c);
 void lagr_geometry_to_host(Ctx* c);
 void lagr_invalidate(Ctx* c);

@@ -268,6 +268,9 @@ void release(Ctx* c) {
   hit_free(c);
   rigid_free(c);
   diag_free(c);
+  if (c->side) { cudaStreamSynchronize(c->side); cudaStreamDestroy(c->side); }
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
   if (c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -285,7 +288,10 @@ int mibm_context_create_(void) {
     g_ctx[c->id] = c;
   }
   cudaGetDevice(&c->device);
-  if (!cuda_ok(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream")) {
+  if (!cuda_ok(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream") ||
+      !cuda_ok(c, cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking), "stream") ||
+      !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "event") ||
+      !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming), "event")) {
     t_cur = c;
     return -MIBM_ECUDA;
   }

@@ -25,6 +25,7 @@
 #include <string>
 #include <cstddef>
 #include <cmath>
+#include <utility>
 #include <vector>
 
 #include "common.cuh"
@@ -2135,6 +2136,17 @@ const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror,
                                                            c->red + kRedPart);
     seg_final_kernel<<<1, kMeanBlocks, 0, c->stream>>>(c->red + kRedPart, ncell, s->mean3); }
   c->launches += 2;
+  // Fork: the rest of particle (heat flux, temperature forcing, Stefan
+  // front, motion, geometry) reads and writes none of the buffers of the
+  // pressure projection that the caller enqueues next, so it runs on the
+  // side stream; lagr_join makes the main stream wait for it before the next
+  // substep.  Not when a remesh may need the host mid-way.
+  const bool fork = c->side && !lagr_remesh_active(c);
+  if (fork) {
+    cudaEventRecord(c->ev_fork, c->stream);
+    cudaStreamWaitEvent(c->side, c->ev_fork, 0);
+    std::swap(c->stream, c->side);
+  }
   bool imelt = c->I(MIBM_I_IMELT) == 1;
   if (imelt) {
     lagr_find_probe_indices(c);
@@ -2143,17 +2155,30 @@ const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror,
   scatter(c, true, 3, 4, false, t_mirror);
   if (imelt) lagr_stefan(c, dp);
   if (str) motion_launch(c, dp);
-  bool remeshed = lagr_remesh_active(c) && remesh_check(c);
-  if (c->status != MIBM_OK) return nullptr;
-  geometry_launch(c, imelt);
-  if (remeshed) {
-    const double *vel, *om;
-    body_velocity(c, dp, &vel, &om);
-    tri_velocity_launch(c, vel, om);
+  bool remeshed = !fork && lagr_remesh_active(c) && remesh_check(c);
+  if (c->status == MIBM_OK) {
+    geometry_launch(c, imelt);
+    if (remeshed) {
+      const double *vel, *om;
+      body_velocity(c, dp, &vel, &om);
+      tri_velocity_launch(c, vel, om);
+    }
+    if (str) k_rigid_publish(c, s->geom_out, next);
+    MIBM_LAUNCH_CHECK(c, "particle");
   }
-  if (str) k_rigid_publish(c, s->geom_out, next);
-  MIBM_LAUNCH_CHECK(c, "particle");
-  return s->mean3;
+  if (fork) {
+    cudaEventRecord(c->ev_join, c->stream);
+    std::swap(c->stream, c->side);
+    c->join_pending = true;
+  }
+  return c->status == MIBM_OK ? s->mean3 : nullptr;
+}
+
+// the main stream waits for the side-stream half of the last particle
+void lagr_join(Ctx* c) {
+  if (!c->join_pending) return;
+  cudaStreamWaitEvent(c->stream, c->ev_join, 0);
+  c->join_pending = false;
 }
 
 // End of the fused step, in two halves so that the device half can sit in
