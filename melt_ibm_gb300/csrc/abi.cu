@@ -165,7 +165,8 @@ static void step_enqueue_f32(Ctx* c) {
   for (int ns = 0; ns < 3; ++ns) {
     const StepParams* dp = c->dparams + ns;
     lagr_join(c);
-    if (!c->I(MIBM_I_STATIONARY) && c->I(MIBM_I_IMLSFOR) == 1) lagr_tag_narrow_band(c);
+    if (!c->prologue_done) lagr_substep_prologue(c);
+    c->prologue_done = false;
     k_fused_rhs_f32(c, dp, c->ru32, c->rhs32);
     for (int q = 0; q < 4; ++q) {
       int f = (q < 3) ? 0 : 1;
@@ -175,7 +176,7 @@ static void step_enqueue_f32(Ctx* c) {
       k_solve_y_f32(c, r, T + tlen);
       k_solve_z_f32(c, r, T + 2 * tlen, c->df[kStepFid[q]], q == 3 ? t_mirror : nullptr);
     }
-    const double* mean3 = lagr_particle_fused(c, dp, t_mirror, ns < 2 ? c->dparams + ns + 1 : nullptr);
+    const double* mean3 = lagr_particle_fused(c, dp, t_mirror, ns < 2 ? c->dparams + ns + 1 : nullptr, ns < 2);
     if (c->status != MIBM_OK) return;
     for (int it = 0; it < c->nproj; ++it) {
       bool last = it + 1 == c->nproj;
@@ -196,7 +197,8 @@ static void step_enqueue_f64(Ctx* c) {
   for (int ns = 0; ns < 3; ++ns) {
     const StepParams* dp = c->dparams + ns;
     lagr_join(c);
-    if (!c->I(MIBM_I_STATIONARY) && c->I(MIBM_I_IMLSFOR) == 1) lagr_tag_narrow_band(c);
+    if (!c->prologue_done) lagr_substep_prologue(c);
+    c->prologue_done = false;
     k_fused_rhs(c, dp);
     for (int q = 0; q < 4; ++q) {
       int f = (q < 3) ? 0 : 1;
@@ -206,7 +208,7 @@ static void step_enqueue_f64(Ctx* c) {
       k_solve_y_T(c, r, T + tlen);
       k_solve_z_T(c, r, T + 2 * tlen, c->df[kStepFid[q]], 0);
     }
-    const double* mean3 = lagr_particle_fused(c, dp, nullptr, ns < 2 ? c->dparams + ns + 1 : nullptr);
+    const double* mean3 = lagr_particle_fused(c, dp, nullptr, ns < 2 ? c->dparams + ns + 1 : nullptr, ns < 2);
     if (c->status != MIBM_OK) return;
     k_divg(c, dp);
     k_phcalc(c);
@@ -225,6 +227,7 @@ static const double* step_vel_cm(Ctx* c) {
 
 static void step_enqueue(Ctx* c) {
   cudaMemcpyAsync(c->dparams, c->hparams, 3 * sizeof(StepParams), cudaMemcpyHostToDevice, c->stream);
+  c->prologue_done = false;
   if (moving_body(c)) rigid_upload(c);
   if (c->I(MIBM_I_FORCING) == 1 && c->precision == 0) k_forcing_quotient(c);
   if (c->precision == 1) step_enqueue_f32(c);

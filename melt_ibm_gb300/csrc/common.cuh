@@ -132,6 +132,7 @@ struct Ctx {
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   bool join_pending = false;
+  bool prologue_done = false;             // the next substep's geometry-only work is enqueued
   // fused-step state
   StepParams* dparams = nullptr;          // [3] device copies (one per substep)
   StepParams* hparams = nullptr;          // pinned
@@ -328,7 +329,9 @@ void lagr_geometry_refresh(Ctx* c, bool imelt);
 void lagr_tag_narrow_band(Ctx* c);
 void lagr_tag_initial(Ctx* c);
 void lagr_particle(Ctx* c, const StepParams* dp);
-const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror, StepParams* next);
+const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror, StepParams* next,
+                                  bool next_prologue);
+void lagr_substep_prologue(Ctx* c);
 void lagr_struct_loads(Ctx* c, const StepParams* dp);
 // diag.cu (CalcDissipation, vorticity, calcFluidVelAvgs)
 void diag_enqueue(Ctx* c, const double* vcm);

@@ -2114,9 +2114,15 @@ void lagr_particle(Ctx* c, const StepParams* dp) {
 // has read the unforced temperature, into T.  MLS weights of a stationary
 // cage are reused.  Flags and geometry scalars are read by the caller at the
 // end of the step.
-const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror, StepParams* next) {
-  if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0) return nullptr;
-  if (!ensure_adjacency(c) || !ensure_lag_buffers(c)) return nullptr;
+// The work of a substep that depends on the geometry alone: narrow-band
+// tagging (tagCells at the start of the substep, tsch.f90:45-47) and, from
+// particle, the cage indices, the MLS weights and the scatter plan.  The fused
+// step runs it for substeps 1 and 2 on the side stream of the substep before
+// (the geometry is final once that substep's particle is done).
+void lagr_substep_prologue(Ctx* c) {
+  if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0) return;
+  if (!c->I(MIBM_I_STATIONARY)) lagr_tag_narrow_band(c);
+  if (!ensure_adjacency(c) || !ensure_lag_buffers(c)) return;
   LagState* s = lag_of(c);
   bool stationary = c->I(MIBM_I_STATIONARY) != 0;
   lagr_find_centroid_indices(c);
@@ -2125,8 +2131,15 @@ const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror,
     s->weights_valid = stationary;
     if (stationary) ++c->lag_gen;     // later steps skip the weights: another launch sequence
   }
-  force_coefficients(c);
   update_plan(c);
+}
+
+const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror, StepParams* next,
+                                  bool next_prologue) {
+  if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0) return nullptr;
+  if (!ensure_adjacency(c) || !ensure_lag_buffers(c)) return nullptr;
+  LagState* s = lag_of(c);
+  force_coefficients(c);
   bool str = c->I(MIBM_I_IMLSSTR) == 1;
   if (str) struct_loads_launch(c, dp);      // reads the unforced u, v, w and p
   scatter(c, true, 0, 3, true);
@@ -2164,6 +2177,10 @@ const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror,
       tri_velocity_launch(c, vel, om);
     }
     if (str) k_rigid_publish(c, s->geom_out, next);
+    if (fork && next_prologue) {
+      lagr_substep_prologue(c);
+      c->prologue_done = true;
+    }
     MIBM_LAUNCH_CHECK(c, "particle");
   }
   if (fork) {
