@@ -336,6 +336,7 @@ def run_gpu(args):
     h2d += case.mesh_arrays[abi.MIBM_M_XYZV].nbytes
     d2h += case.mesh_arrays[abi.MIBM_M_XYZV].nbytes
     case.sync_to_host(lib, FIELD_MASK | MESH_MASK)
+    pinned = lib.mibm_pin_host_(abi.ref_int(1)) == 0      # page-locked host arrays: DMA copies
     dist.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
@@ -402,7 +403,7 @@ def run_gpu(args):
                        "parallelism": f"replicas x{dist.ws}" if dist.ws > 1 else "single GPU",
                        "l2": "inputs larger than L2 (>30 fields of N^3 doubles resident)"},
             "e2e": {"value": e2e_value, "unit": "Mcell-steps/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
+                    "d2h_bytes_per_step": d2h, "host_arrays_pinned": pinned},
             "roofline": roofline, "gpu_launches": launches, "clocks": clocks, "fp32_refined": fp32,
             "diagnostics": diagnostics,
             "host_wall_ms_per_step": 1e3 * wall / args.steps, "kernels": kernels}

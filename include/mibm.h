@@ -163,6 +163,14 @@ void mibm_init_(void);
 /* mask bit b (0..25) selects field b; bit 32+m selects mesh array m. */
 void mibm_sync_from_host_(const long long* mask);
 void mibm_sync_to_host_(const long long* mask);
+/* Page-lock (on = 1) or release (on = 0) the registered host arrays of   */
+/* the bound context with cudaHostRegister, so that mibm_sync_*_ copy them  */
+/* by DMA at the host link's speed instead of through the driver's bounce   */
+/* buffers (no counterpart in the reference).  While pinned, the arrays     */
+/* must outlive the context or be released first; destroying the context   */
+/* releases them.  Arrays the host has already page-locked are left as they */
+/* are.  Returns a status.                                                  */
+int  mibm_pin_host_(const int* on);
 /* Visible CUDA devices (0 without a GPU); kernels launched by the bound
  * context so far (libmibm.so only). */
 int  mibm_device_count_(void);

@@ -78,6 +78,7 @@ SIGNATURES: dict[str, tuple] = {
     "mibm_batch_destroy_": (C.c_int, [_I]),
     "mibm_divergence_max_": (C.c_double, []),
     "mibm_set_remesh_callback_": (None, [C.c_void_p, C.c_void_p]),
+    "mibm_pin_host_": (C.c_int, [_I]),
     "mibm_remesh_count_": (C.c_int, []),
     "mibm_diagnostics_": (C.c_int, [C.c_void_p]),
     "mibm_set_diagnostics_": (None, [_I]),

@@ -132,6 +132,7 @@ struct Ctx {
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   bool join_pending = false;
+  std::vector<void*> pinned;              // host arrays page-locked by mibm_pin_host_
   bool prologue_done = false;             // the next substep's geometry-only work is enqueued
   // fused-step state
   StepParams* dparams = nullptr;          // [3] device copies (one per substep)

@@ -241,8 +241,15 @@ bool ensure_params(Ctx* c) {
   return true;
 }
 
+static void unpin_host(Ctx* c) {
+  for (void* p : c->pinned) cudaHostUnregister(p);
+  c->pinned.clear();
+  cudaGetLastError();
+}
+
 void release(Ctx* c) {
   cudaSetDevice(c->device);
+  unpin_host(c);
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
   if (c->graph) cudaGraphDestroy(c->graph);
@@ -448,6 +455,25 @@ void mibm_sync_to_host_(const long long* mask) {
     if ((m >> 32) & (1ull << i))
       cuda_ok(c, cudaMemcpyAsync(c->hm[i], c->dm[i], mesh_bytes(c, i), cudaMemcpyDeviceToHost, c->stream), "D2H mesh");
   cuda_ok(c, cudaStreamSynchronize(c->stream), "sync_to_host");
+}
+
+int mibm_pin_host_(const int* on) {
+  Ctx* c = current(); if (!ready(c)) return c ? c->status : MIBM_ESTATE;
+  if (!*on) { unpin_host(c); return MIBM_OK; }
+  if (!c->pinned.empty()) return MIBM_OK;
+  auto pin = [&](void* p, size_t bytes) {
+    if (!p || bytes == 0) return;
+    cudaError_t e = cudaHostRegister(p, bytes, cudaHostRegisterDefault);
+    if (e == cudaSuccess) c->pinned.push_back(p);
+    else cudaGetLastError();               // already page-locked, or not registrable: copies stay pageable
+  };
+  for (int id = 0; id < MIBM_NFIELDS; ++id) {
+    int ny, klo, nk;
+    field_host_shape(c, id, ny, klo, nk);
+    pin(c->hf[id], (size_t)(c->g.n1m + 1) * ny * nk * sizeof(double));
+  }
+  for (int i = 0; i < MIBM_NMESH && c->maxnf > 0; ++i) pin(c->hm[i], mesh_bytes(c, i));
+  return MIBM_OK;
 }
 
 // Number of CUDA devices visible to this process (0 on a host without a

@@ -2361,6 +2361,7 @@ void mibm_set_remesh_callback_(mibm_remesh_fn fn, void* user) {
   c->remesh_fn = fn; c->remesh_user = user;
 }
 int mibm_remesh_count_(void) { Ctx* c = cur(); return c ? c->remesh_count : 0; }
+int mibm_pin_host_(const int*) { return MIBM_OK; }   // the oracle works on the host arrays themselves
 // the oracle computes on request: the state has not changed since the step
 void mibm_set_diagnostics_(const int* on) { Ctx* c = cur(); if (c) c->diag_on = *on != 0; }
 int mibm_diagnostics_get_(double* out) {
