@@ -132,6 +132,7 @@ static bool step_prepare(Ctx* c) {
     if (!c->rhs4 && !cuda_ok(c, cudaMalloc(&c->rhs4, 4 * g.cells * sizeof(double)), "rhs4")) return false;
   }
   if (!tri_step_fill(c, bd, f32)) return false;
+  if (!lagr_step_prepare(c)) return false;
   if (c->I(MIBM_I_FORCING) == 1 && !c->forc_q &&
       !cuda_ok(c, cudaMalloc(&c->forc_q, 3 * g.cells * sizeof(double)), "forcing quotient"))
     return false;
@@ -165,7 +166,7 @@ static void step_enqueue_f32(Ctx* c) {
   for (int ns = 0; ns < 3; ++ns) {
     const StepParams* dp = c->dparams + ns;
     lagr_join(c);
-    if (!c->prologue_done) lagr_substep_prologue(c);
+    if (!c->prologue_done) lagr_substep_prologue(c, ns);
     c->prologue_done = false;
     k_fused_rhs_f32(c, dp, c->ru32, c->rhs32);
     for (int q = 0; q < 4; ++q) {
@@ -176,7 +177,7 @@ static void step_enqueue_f32(Ctx* c) {
       k_solve_y_f32(c, r, T + tlen);
       k_solve_z_f32(c, r, T + 2 * tlen, c->df[kStepFid[q]], q == 3 ? t_mirror : nullptr);
     }
-    const double* mean3 = lagr_particle_fused(c, dp, t_mirror, ns < 2 ? c->dparams + ns + 1 : nullptr, ns < 2);
+    const double* mean3 = lagr_particle_fused(c, dp, t_mirror, ns < 2 ? c->dparams + ns + 1 : nullptr, ns < 2 ? ns + 1 : -1);
     if (c->status != MIBM_OK) return;
     for (int it = 0; it < c->nproj; ++it) {
       bool last = it + 1 == c->nproj;
@@ -197,7 +198,7 @@ static void step_enqueue_f64(Ctx* c) {
   for (int ns = 0; ns < 3; ++ns) {
     const StepParams* dp = c->dparams + ns;
     lagr_join(c);
-    if (!c->prologue_done) lagr_substep_prologue(c);
+    if (!c->prologue_done) lagr_substep_prologue(c, ns);
     c->prologue_done = false;
     k_fused_rhs(c, dp);
     for (int q = 0; q < 4; ++q) {
@@ -208,7 +209,7 @@ static void step_enqueue_f64(Ctx* c) {
       k_solve_y_T(c, r, T + tlen);
       k_solve_z_T(c, r, T + 2 * tlen, c->df[kStepFid[q]], 0);
     }
-    const double* mean3 = lagr_particle_fused(c, dp, nullptr, ns < 2 ? c->dparams + ns + 1 : nullptr, ns < 2);
+    const double* mean3 = lagr_particle_fused(c, dp, nullptr, ns < 2 ? c->dparams + ns + 1 : nullptr, ns < 2 ? ns + 1 : -1);
     if (c->status != MIBM_OK) return;
     k_divg(c, dp);
     k_phcalc(c);

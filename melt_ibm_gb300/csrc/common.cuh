@@ -331,8 +331,9 @@ void lagr_tag_narrow_band(Ctx* c);
 void lagr_tag_initial(Ctx* c);
 void lagr_particle(Ctx* c, const StepParams* dp);
 const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror, StepParams* next,
-                                  bool next_prologue);
-void lagr_substep_prologue(Ctx* c);
+                                  int next_prologue);
+void lagr_substep_prologue(Ctx* c, int slot);
+bool lagr_step_prepare(Ctx* c);
 void lagr_struct_loads(Ctx* c, const StepParams* dp);
 // diag.cu (CalcDissipation, vorticity, calcFluidVelAvgs)
 void diag_enqueue(Ctx* c, const double* vcm);

@@ -1508,6 +1508,7 @@ struct LagState {
   int* dirty = nullptr;
   double* segval = nullptr;
   bool force_rebuild = true;
+  int* force_pinned = nullptr;                   // per-substep rebuild requests read by the step (pinned)
   bool weights_valid = false;                    // stationary cages: weights kept
 };
 static std::vector<LagState*> g_lag;
@@ -1521,11 +1522,29 @@ static LagState* lag_of(Ctx* c) {
   return s;
 }
 
+// The mesh changed on the host side: the scatter plan is rebuilt from
+// scratch and the MLS weights recomputed.  The step graph stays valid (the
+// rebuild is requested through pinned memory read at replay) unless the
+// weights of a stationary body were being reused, which changes the launch
+// sequence.
 void lagr_invalidate(Ctx* c) {
   LagState* s = lag_of(c);
   s->force_rebuild = true;
+  if (c->I(MIBM_I_STATIONARY) && s->weights_valid) ++c->lag_gen;
   s->weights_valid = false;
-  ++c->lag_gen;
+}
+
+// Per step, before the step's device work is enqueued or replayed: the
+// plan-rebuild request of each substep into the pinned block the step's
+// plan updates read (substep 0 takes a pending request).
+bool lagr_step_prepare(Ctx* c) {
+  if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0) return true;
+  LagState* s = lag_of(c);
+  if (!s->force_pinned && !cuda_ok(c, cudaMallocHost((void**)&s->force_pinned, 4 * sizeof(int)), "plan")) return false;
+  s->force_pinned[0] = s->force_rebuild ? 1 : 0;
+  s->force_pinned[1] = s->force_pinned[2] = s->force_pinned[3] = 0;
+  s->force_rebuild = false;
+  return true;
 }
 
 // the face/vertex/edge relations changed (a remesh or a host upload of the
@@ -1619,15 +1638,19 @@ bool validate_mesh(Ctx* c) {
 }
 
 // (Re)build the merged scatter plan when the cage centres changed.
-static void update_plan(Ctx* c) {
+// slot >= 0: inside the fused step, the rebuild request comes from the
+// step's pinned block (lagr_step_prepare); slot < 0 (drop-ins): now.
+static void update_plan(Ctx* c, int slot) {
   LagState* s = lag_of(c);
   int nf = c->maxnf, n = s->plan_n;
-  if (s->force_rebuild) {
-    cudaMemsetAsync(s->dirty, 1, sizeof(int), c->stream);   // any non-zero value marks the plan dirty
-    s->force_rebuild = false;
-    ++c->lag_gen;                                              // the next step has the other shape
+  if (slot >= 0 && s->force_pinned) {
+    // a request raised inside the step (a remesh, which runs without a
+    // step graph) goes into this substep's slot
+    if (s->force_rebuild) { s->force_pinned[slot] = 1; s->force_rebuild = false; }
+    cudaMemcpyAsync(s->dirty, s->force_pinned + slot, sizeof(int), cudaMemcpyHostToDevice, c->stream);
   } else {
-    cudaMemsetAsync(s->dirty, 0, sizeof(int), c->stream);
+    cudaMemsetAsync(s->dirty, s->force_rebuild ? 1 : 0, sizeof(int), c->stream);   // non-zero: dirty
+    s->force_rebuild = false;
   }
   const int* pind = M<int>(c, MIBM_M_PIND);
   const int* ghost = M<int>(c, MIBM_M_GHOST_FACE);
@@ -1735,7 +1758,7 @@ void lagr_mls_force(Ctx* c, const StepParams*, bool) {
   if (c->maxnf == 0) return;
   if (!ensure_lag_buffers(c)) return;
   force_coefficients(c);
-  update_plan(c);
+  update_plan(c, -1);
   scatter(c, false, 0, 4, false);
   MIBM_LAUNCH_CHECK(c, "mlsForce");
 }
@@ -2119,7 +2142,7 @@ void lagr_particle(Ctx* c, const StepParams* dp) {
 // particle, the cage indices, the MLS weights and the scatter plan.  The fused
 // step runs it for substeps 1 and 2 on the side stream of the substep before
 // (the geometry is final once that substep's particle is done).
-void lagr_substep_prologue(Ctx* c) {
+void lagr_substep_prologue(Ctx* c, int slot) {
   if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0) return;
   if (!c->I(MIBM_I_STATIONARY)) lagr_tag_narrow_band(c);
   if (!ensure_adjacency(c) || !ensure_lag_buffers(c)) return;
@@ -2131,11 +2154,11 @@ void lagr_substep_prologue(Ctx* c) {
     s->weights_valid = stationary;
     if (stationary) ++c->lag_gen;     // later steps skip the weights: another launch sequence
   }
-  update_plan(c);
+  update_plan(c, slot);
 }
 
 const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror, StepParams* next,
-                                  bool next_prologue) {
+                                  int next_prologue) {
   if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0) return nullptr;
   if (!ensure_adjacency(c) || !ensure_lag_buffers(c)) return nullptr;
   LagState* s = lag_of(c);
@@ -2177,8 +2200,8 @@ const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror,
       tri_velocity_launch(c, vel, om);
     }
     if (str) k_rigid_publish(c, s->geom_out, next);
-    if (fork && next_prologue) {
-      lagr_substep_prologue(c);
+    if (fork && next_prologue >= 0) {
+      lagr_substep_prologue(c, next_prologue);
       c->prologue_done = true;
     }
     MIBM_LAUNCH_CHECK(c, "particle");
@@ -2235,6 +2258,7 @@ void lagr_free(Ctx* c) {
       LagState* s = g_lag[q];
       cudaFree(s->adj_off); cudaFree(s->adj_face); cudaFree(s->face_part); cudaFree(s->geom_out);
       cudaFree(s->loads_ev); cudaFree(s->rm_flag);
+      if (s->force_pinned) cudaFreeHost(s->force_pinned);
       cudaFree(s->mean3); cudaFree(s->sdf_bits); cudaFree(s->winner); cudaFree(s->dist_buf);
       cudaFree(s->band_ub); cudaFree(s->face4); cudaFree(s->face_cell); cudaFree(s->cm32);
       cudaFree(s->band_list); cudaFree(s->band_count);
