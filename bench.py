@@ -70,6 +70,9 @@ WORKLOADS = {
                           imelt=1, imlsstr=0, seed=1, v_on_ve=0.0),
     "melt64_c0": dict(n=64, mesh_level=3, rad_p=0.5, ren=100.0, prandtl=1.0, latheat=1.0, cpliquid=1.0,
                       imelt=1, imlsstr=0, seed=0, v_on_ve=0.0),
+    "melt256_c2": dict(n=256, mesh_level=5, rad_p=1.0, axes=(0.6, 0.3, 0.3), ren=400.0, prandtl=1.0,
+                       latheat=0.5, cpliquid=1.0, betagz=0.1, forcing=1, which_hit=1, imelt=1, imlsstr=0,
+                       seed=2, v_on_ve=0.0),
     "melt256_fixed": dict(n=256, mesh_level=5, rad_p=0.4, ren=400.0, prandtl=1.0, latheat=2.0, cpliquid=1.0,
                           imelt=1, imlsstr=0, seed=2, v_on_ve=0.0),
 }
@@ -79,6 +82,9 @@ WORKLOAD_TEXT = {
     "melt128_fixed": "128^3 FP64, icosphere level 4 (5120 tri) r=0.4 melting (St=1), nu=0.005, body fixed "
                      "(Newton-Euler, linear HIT forcing and remeshing of the 128^3 configuration not built)",
     "melt64_c0": "64^3 FP64 plain configuration: icosphere level 3 r=0.5, nu=kappa=0.01, St=1",
+    "melt256_c2": "256^3, prolate spheroid (0.6, 0.3, 0.3) from a level-5 icosphere (20480 tri), "
+                  "Eswaran-Pope forcing, Boussinesq (betagz = Ri = 0.1), St=2, Pr=1, nu=0.0025, body fixed; "
+                  "the configuration of the precision form (its FP64 run is the error reference)",
     "melt256_fixed": "256^3 FP64, icosphere level 5 r=0.4 melting (St=2), nu=0.0025, body fixed",
 }
 

@@ -279,7 +279,7 @@ class Case:
             F[A.MIBM_F_VY][:n1m, :n2m, 1:n3m + 1] = v
             F[A.MIBM_F_VZ][:n1m, :n2m, 1:n3m + 1] = w
         pos = self.sc[A.MIBM_S_POS_CM, :3]
-        T = tanh_temperature(self.xm, self.ym, self.zm, pos, c.rad_p, c.tliq, c.tsol, self.dx1)
+        T = tanh_temperature(self.xm, self.ym, self.zm, pos, c.rad_p, c.tliq, c.tsol, self.dx1, c.axes)
         F[A.MIBM_F_TEMP][...] = c.tsol
         F[A.MIBM_F_TEMP][:n1m, :n2m, 1:n3m + 1] = T
         for fid in (A.MIBM_F_VX, A.MIBM_F_VY, A.MIBM_F_VZ, A.MIBM_F_TEMP, A.MIBM_F_PR):

@@ -96,8 +96,17 @@ def random_velocity(n: int, length: float, seed: int, kmax: int = 8):
     return u / rms, v / rms, w / rms
 
 
-def tanh_temperature(xm, ym, zm, pos_cm, rad, tliq, tsol, dx1):
-    """inqpr.f90:18-28: T = Tliq - (Tliq-Tsol)/2 (1 - tanh((r-rad) dx1/2))."""
+def tanh_temperature(xm, ym, zm, pos_cm, rad, tliq, tsol, dx1, axes=(1.0, 1.0, 1.0)):
+    """inqpr.f90:18-28: T = Tliq - (Tliq-Tsol)/2 (1 - tanh((r-rad) dx1/2)).
+
+    For a body scaled by `axes` (a spheroid) r is the scaled radius
+    |(x - x_c) / axes| times the smallest axis, so that the profile is
+    centred on the body's surface; axes = (1, 1, 1) is the reference's sphere.
+    """
     X, Y, Z = np.meshgrid(xm, ym, zm, indexing="ij")
-    rr = np.sqrt((X - pos_cm[0]) ** 2 + (Y - pos_cm[1]) ** 2 + (Z - pos_cm[2]) ** 2)
-    return tliq - (tliq - tsol) * 0.5 * (1.0 - np.tanh((rr - rad) * dx1 / 2.0))
+    a = np.asarray(axes, dtype=np.float64)
+    if np.all(a == 1.0):
+        rr = np.sqrt((X - pos_cm[0]) ** 2 + (Y - pos_cm[1]) ** 2 + (Z - pos_cm[2]) ** 2)
+        return tliq - (tliq - tsol) * 0.5 * (1.0 - np.tanh((rr - rad) * dx1 / 2.0))
+    rho = np.sqrt(((X - pos_cm[0]) / a[0]) ** 2 + ((Y - pos_cm[1]) / a[1]) ** 2 + ((Z - pos_cm[2]) / a[2]) ** 2)
+    return tliq - (tliq - tsol) * 0.5 * (1.0 - np.tanh((rho - rad) * a.min() * dx1 / 2.0))
