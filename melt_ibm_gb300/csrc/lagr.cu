@@ -2176,8 +2176,10 @@ const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror,
   // front, motion, geometry) reads and writes none of the buffers of the
   // pressure projection that the caller enqueues next, so it runs on the
   // side stream; lagr_join makes the main stream wait for it before the next
-  // substep.  Not when a remesh may need the host mid-way.
-  const bool fork = c->side && !lagr_remesh_active(c);
+  // substep.  Not when a remesh may need the host mid-way, nor while kernels
+  // are timed one by one (mibm_profile_: serial, so each time is the
+  // kernel's own).
+  const bool fork = c->side && !lagr_remesh_active(c) && !c->profiling;
   if (fork) {
     cudaEventRecord(c->ev_fork, c->stream);
     cudaStreamWaitEvent(c->side, c->ev_fork, 0);
