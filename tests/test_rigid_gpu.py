@@ -129,6 +129,21 @@ def test_moving_body_step_parity(oracle_lib, gpu_lib, imelt):
     assert np.abs(co.sc[A.MIBM_S_VEL_CM, :3]).max() > 1e-4
 
 
+def test_free_body_forced_ten_steps(oracle_lib, gpu_lib):
+    """The free-body configuration's physics (free melting body, density
+    ratio 2, linear forcing) at 24^3: rel L2 <= 1e-10 on u, v, w, T, p after
+    1 and 10 steps, the rigid state alike."""
+    case = Case(_cfg(n=24, level=2, dens_ratio=2.0, forcing=1, which_hit=3, c_hit=0.2, ren=200.0))
+    co, cg = pair(case, oracle_lib, gpu_lib)
+    for nsteps, start in ((1, 1), (9, 2)):
+        _steps(co, oracle_lib, nsteps, start)
+        _steps(cg, gpu_lib, nsteps, start)
+        for name, fid in FIELDS_OUT.items():
+            err = rel_l2(cg.interior(fid), co.interior(fid))
+            assert err <= 1e-10, f"{name} after {start + nsteps - 1} steps: {err:.3e}"
+        _cmp_rigid(co, cg, 1e-10)
+
+
 def test_moving_body_precision_form(oracle_lib, gpu_lib):
     case = Case(_cfg(n=24, level=2))
     co, cg = pair(case, oracle_lib, gpu_lib)
