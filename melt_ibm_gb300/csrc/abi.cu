@@ -132,7 +132,6 @@ static bool step_prepare(Ctx* c) {
     if (!c->rhs4 && !cuda_ok(c, cudaMalloc(&c->rhs4, 4 * g.cells * sizeof(double)), "rhs4")) return false;
   }
   if (!tri_step_fill(c, bd, f32)) return false;
-  if (!lagr_step_prepare(c)) return false;
   if (c->I(MIBM_I_FORCING) == 1 && !c->forc_q &&
       !cuda_ok(c, cudaMalloc(&c->forc_q, 3 * g.cells * sizeof(double)), "forcing quotient"))
     return false;
@@ -146,6 +145,7 @@ static bool step_prepare(Ctx* c) {
     *c->hs[MIBM_S_RO] = kRom[ns];
     c->hparams[ns] = host_params(c);
   }
+  c->hparams[0].force_plan = lagr_take_plan_request(c);
   return c->status == MIBM_OK;
 }
 

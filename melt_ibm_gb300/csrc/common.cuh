@@ -55,6 +55,7 @@ struct StepParams {
   double pos[3], vel[3], om[3];
   double cd[kNCoef];
   float cf[kNCoef];
+  int force_plan;   // rebuild the scatter plan from scratch this substep (a host mesh upload)
 };
 
 template <typename R> __host__ __device__ __forceinline__ R coef(const StepParams& p, int i);
@@ -333,7 +334,7 @@ void lagr_particle(Ctx* c, const StepParams* dp);
 const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror, StepParams* next,
                                   int next_prologue);
 void lagr_substep_prologue(Ctx* c, int slot);
-bool lagr_step_prepare(Ctx* c);
+int lagr_take_plan_request(Ctx* c);
 void lagr_struct_loads(Ctx* c, const StepParams* dp);
 // diag.cu (CalcDissipation, vorticity, calcFluidVelAvgs)
 void diag_enqueue(Ctx* c, const double* vcm);

@@ -294,8 +294,10 @@ constexpr int kSortChunk = 4096;
 // plan was built from and every kernel of the rebuild returns at once when
 // nothing changed, so a rebuild costs nothing on a stationary cage.
 __global__ void plan_check_kernel(int nf, const int* __restrict__ pind, const int* __restrict__ ghost,
-                                  const int* __restrict__ saved, int* __restrict__ dirty) {
+                                  const int* __restrict__ saved, int* __restrict__ dirty,
+                                  const StepParams* __restrict__ pp) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t == 0 && pp && pp->force_plan) atomicOr(dirty, 1);   // rebuild requested by the host
   if (t >= nf) return;
   const int* sv = saved + 7 * (size_t)t;
   bool diff = (sv[6] != ghost[t]);
@@ -1508,7 +1510,6 @@ struct LagState {
   int* dirty = nullptr;
   double* segval = nullptr;
   bool force_rebuild = true;
-  int* force_pinned = nullptr;                   // per-substep rebuild requests read by the step (pinned)
   bool weights_valid = false;                    // stationary cages: weights kept
 };
 static std::vector<LagState*> g_lag;
@@ -1534,17 +1535,15 @@ void lagr_invalidate(Ctx* c) {
   s->weights_valid = false;
 }
 
-// Per step, before the step's device work is enqueued or replayed: the
-// plan-rebuild request of each substep into the pinned block the step's
-// plan updates read (substep 0 takes a pending request).
-bool lagr_step_prepare(Ctx* c) {
-  if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0) return true;
+// Per step, while its parameter blocks are filled: a pending request to
+// rebuild the scatter plan from scratch goes into substep 0's block, which
+// the step reads on the device (so a step graph stays valid across uploads).
+int lagr_take_plan_request(Ctx* c) {
+  if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0) return 0;
   LagState* s = lag_of(c);
-  if (!s->force_pinned && !cuda_ok(c, cudaMallocHost((void**)&s->force_pinned, 4 * sizeof(int)), "plan")) return false;
-  s->force_pinned[0] = s->force_rebuild ? 1 : 0;
-  s->force_pinned[1] = s->force_pinned[2] = s->force_pinned[3] = 0;
+  int r = s->force_rebuild ? 1 : 0;
   s->force_rebuild = false;
-  return true;
+  return r;
 }
 
 // the face/vertex/edge relations changed (a remesh or a host upload of the
@@ -1638,24 +1637,19 @@ bool validate_mesh(Ctx* c) {
 }
 
 // (Re)build the merged scatter plan when the cage centres changed.
-// slot >= 0: inside the fused step, the rebuild request comes from the
-// step's pinned block (lagr_step_prepare); slot < 0 (drop-ins): now.
-static void update_plan(Ctx* c, int slot) {
+// dp: inside the fused step, the substep's parameter block, whose
+// force_plan carries a rebuild request (lagr_take_plan_request); nullptr
+// (drop-ins): the pending request is applied now.  A request raised inside
+// a step (a remesh, which runs without a step graph) is applied now too.
+static void update_plan(Ctx* c, const StepParams* dp) {
   LagState* s = lag_of(c);
   int nf = c->maxnf, n = s->plan_n;
-  if (slot >= 0 && s->force_pinned) {
-    // a request raised inside the step (a remesh, which runs without a
-    // step graph) goes into this substep's slot
-    if (s->force_rebuild) { s->force_pinned[slot] = 1; s->force_rebuild = false; }
-    cudaMemcpyAsync(s->dirty, s->force_pinned + slot, sizeof(int), cudaMemcpyHostToDevice, c->stream);
-  } else {
-    cudaMemsetAsync(s->dirty, s->force_rebuild ? 1 : 0, sizeof(int), c->stream);   // non-zero: dirty
-    s->force_rebuild = false;
-  }
+  cudaMemsetAsync(s->dirty, s->force_rebuild ? 1 : 0, sizeof(int), c->stream);   // non-zero: dirty
+  s->force_rebuild = false;
   const int* pind = M<int>(c, MIBM_M_PIND);
   const int* ghost = M<int>(c, MIBM_M_GHOST_FACE);
   { MIBM_PROF(c, "plan_check");
-    plan_check_kernel<<<div_up(nf, 256), 256, 0, c->stream>>>(nf, pind, ghost, s->saved, s->dirty); }
+    plan_check_kernel<<<div_up(nf, 256), 256, 0, c->stream>>>(nf, pind, ghost, s->saved, s->dirty, dp); }
   { MIBM_PROF(c, "plan_keys");
     plan_keys_kernel<<<div_up(n, 256), 256, 0, c->stream>>>(c->g, nf, pind, ghost, s->dirty, s->tmp_key, s->tmp_src); }
   int* kin = s->tmp_key; int* vin = s->tmp_src; int* kout = s->key; int* vout = s->src;
@@ -1758,7 +1752,7 @@ void lagr_mls_force(Ctx* c, const StepParams*, bool) {
   if (c->maxnf == 0) return;
   if (!ensure_lag_buffers(c)) return;
   force_coefficients(c);
-  update_plan(c, -1);
+  update_plan(c, nullptr);
   scatter(c, false, 0, 4, false);
   MIBM_LAUNCH_CHECK(c, "mlsForce");
 }
@@ -2154,7 +2148,7 @@ void lagr_substep_prologue(Ctx* c, int slot) {
     s->weights_valid = stationary;
     if (stationary) ++c->lag_gen;     // later steps skip the weights: another launch sequence
   }
-  update_plan(c, slot);
+  update_plan(c, c->dparams + slot);
 }
 
 const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror, StepParams* next,
@@ -2260,7 +2254,6 @@ void lagr_free(Ctx* c) {
       LagState* s = g_lag[q];
       cudaFree(s->adj_off); cudaFree(s->adj_face); cudaFree(s->face_part); cudaFree(s->geom_out);
       cudaFree(s->loads_ev); cudaFree(s->rm_flag);
-      if (s->force_pinned) cudaFreeHost(s->force_pinned);
       cudaFree(s->mean3); cudaFree(s->sdf_bits); cudaFree(s->winner); cudaFree(s->dist_buf);
       cudaFree(s->band_ub); cudaFree(s->face4); cudaFree(s->face_cell); cudaFree(s->cm32);
       cudaFree(s->band_list); cudaFree(s->band_count);
