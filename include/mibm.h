@@ -23,7 +23,10 @@
  * void signatures; failures are recorded and read with mibm_last_status_()
  * and mibm_last_message().  No device trap is ever raised: device-side
  * failures (singular MLS matrix, non-finite field, wait limit) set a flag
- * that the host reads after the launch sequence.
+ * that the host reads after the launch sequence.  The non-finite guard is
+ * the library's own: cfl_ (and mibm_batch_step_, which runs it) reports
+ * MIBM_ENONFINITE when an owned cell's velocity or temperature is NaN or
+ * Inf, where the reference's max would drop the NaN.
  *
  * Threading: one context per case.  A context is bound to the calling host
  * thread (mibm_context_bind_); every drop-in acts on the bound context.
@@ -48,7 +51,8 @@ enum {
   MIBM_ETIMEOUT = 6,   /* bounded device wait ran out                     */
   MIBM_ENUMERIC = 7,   /* singular MLS matrix (the reference `stop`s)     */
   MIBM_EBUDGET = 8,    /* serving layer: HBM budget refused the case      */
-  MIBM_EABORT = 9      /* body volume below threshold (particle.f90:218)  */
+  MIBM_EABORT = 9,     /* body volume below threshold (particle.f90:218)  */
+  MIBM_ENONFINITE = 10 /* cfl_ met a non-finite velocity or temperature   */
 };
 
 /* ------------------------------------------------------------------ */

@@ -345,6 +345,7 @@ class Case:
         self.bind(lib)
         self.iv[A.MIBM_I_NTIME] = ntime
         lib.cfl_()
+        lib.check("cfl")
         if self.iv[A.MIBM_I_IDTV] == 1:
             if ntime != 1:
                 self.set_S(A.MIBM_S_DT, self.S(A.MIBM_S_DTMAX))

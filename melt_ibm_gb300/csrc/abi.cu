@@ -468,6 +468,7 @@ static int batch_step(Batch* b, int ntime) {
   }
   for (Ctx* c : cs) {
     if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "batch cfl")) return c->status;
+    if (!cfl_finite(c)) return c->status;
     *c->hs[MIBM_S_CFLM] = cfl_value(c->red_host[0]);
     if (c->I(MIBM_I_IDTV) == 1) {
       double dt = c->S(MIBM_S_DT);

@@ -296,6 +296,7 @@ void k_prcalc(Ctx* c, const StepParams* dp);
 void k_add_field(Ctx* c, double* q, const double* r);
 double k_cfl(Ctx* c);
 void k_cfl_async(Ctx* c, double* out);
+bool cfl_finite(Ctx* c);
 void k_getdt_async(Ctx* c, double dt, double* out);
 double cfl_value(double reduced);
 double getdt_buffer(const Grid& g, double reduced, double dt, double ren);

@@ -410,7 +410,7 @@ void mibm_init_(void) {
   if (!dev_alloc(c, (void**)&c->dflag, 64, "flags")) return;
   if (!cuda_ok(c, cudaMallocHost((void**)&c->hflag, 64), "pinned")) return;
   if (!cuda_ok(c, cudaMallocHost((void**)&c->step_host, 32 * sizeof(double)), "pinned")) return;
-  c->hflag[0] = 0;
+  memset(c->hflag, 0, 64);
   for (int i = 0; i < MIBM_NMESH; ++i) {
     size_t b = mesh_bytes(c, i);
     if (b == 0) continue;

@@ -473,7 +473,7 @@ __device__ __forceinline__ double warp_max(double v) {
 // size; the FP32 maximum is rounded up to double unchanged)
 template <typename R>
 __global__ void cfl_kernel(StencilArgs A, const double* __restrict__ padx, const double* __restrict__ pady,
-                           double* __restrict__ part) {
+                           double* __restrict__ part, int* __restrict__ nonfinite) {
   const Grid& g = A.g;
   const Prog<R> F = prog<R>(A);
   const R h1 = R(0.5 * g.dx1), h2 = R(0.5 * g.dx2), h3 = R(0.5 * g.dx3);
@@ -492,6 +492,8 @@ __global__ void cfl_kernel(StencilArgs A, const double* __restrict__ padx, const
             fabs((F.w[c0] + vzp) * R(0.5) * R(g.dx3));
     else
       qcf = fabs((F.u[c0] + vxp) * h1) + fabs((F.v[c0] + vyp) * h2) + fabs((F.w[c0] + vzp) * h3);
+    // fmax drops NaN: a non-finite velocity or temperature raises the guard
+    if (!isfinite(qcf) || !isfinite(F.t[c0])) atomicOr(nonfinite, 1);
     mr = fmax(mr, qcf);
   }
   double m = warp_max((double)mr);
@@ -795,11 +797,21 @@ void k_cfl_async(Ctx* c, double* out) {
   unsigned nb = reduce_blocks(c->g);
   bool f32 = c->precision == 1 && c->q32_valid;
   { MIBM_PROF(c, "cfl");
-    if (f32) cfl_kernel<float><<<nb, 256, 0, c->stream>>>(make_args(c), c->pad_vx, c->pad_vy, c->red + kRedPart);
-    else cfl_kernel<double><<<nb, 256, 0, c->stream>>>(make_args(c), c->pad_vx, c->pad_vy, c->red + kRedPart); }
+    if (f32) cfl_kernel<float><<<nb, 256, 0, c->stream>>>(make_args(c), c->pad_vx, c->pad_vy, c->red + kRedPart, c->dflag + 2);
+    else cfl_kernel<double><<<nb, 256, 0, c->stream>>>(make_args(c), c->pad_vx, c->pad_vy, c->red + kRedPart, c->dflag + 2); }
   max_reduce_kernel<<<1, 1024, 0, c->stream>>>(c->red + kRedPart, nb, c->red + kRedOut);
   c->launches += 2;
   cudaMemcpyAsync(out, c->red + kRedOut, 8, cudaMemcpyDeviceToHost, c->stream);
+  cudaMemcpyAsync(c->hflag + 2, c->dflag + 2, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+}
+
+// After the stream has completed a k_cfl_async: the non-finite guard.
+bool cfl_finite(Ctx* c) {
+  if (!c->hflag[2]) return true;
+  c->hflag[2] = 0;
+  cudaMemsetAsync(c->dflag + 2, 0, sizeof(int), c->stream);
+  fail(c, MIBM_ENONFINITE, "cfl: non-finite velocity or temperature");
+  return false;
 }
 
 // get_dt advective maximum for time step dt (cfl.f90:33-77), as k_cfl_async
@@ -825,6 +837,7 @@ double getdt_buffer(const Grid& g, double reduced, double dt, double ren) {
 double k_cfl(Ctx* c) {
   k_cfl_async(c, c->red_host);
   if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "cfl")) return 0.0;
+  cfl_finite(c);
   return cfl_value(c->red_host[0]);
 }
 

@@ -1859,19 +1859,24 @@ void tschem(Ctx& c) {
 }
 
 // cfl.f90:1-31 (ip, jp, kp are not wrapped: column n1, row n2 and ghost
-// plane n3m+1 are read as stored)
+// plane n3m+1 are read as stored).  The reference's max silently drops a
+// NaN; here a non-finite velocity sum or cell temperature is reported as
+// MIBM_ENONFINITE (the library's own guard, not a reference behaviour).
 void cfl(Ctx& c) {
-  const F3 &vx = c.f[MIBM_F_VX], &vy = c.f[MIBM_F_VY], &vz = c.f[MIBM_F_VZ];
+  const F3 &vx = c.f[MIBM_F_VX], &vy = c.f[MIBM_F_VY], &vz = c.f[MIBM_F_VZ], &te = c.f[MIBM_F_TEMP];
   double cflm = 0.00000001;
+  bool finite = true;
   for (int k = 1; k <= c.n3m; ++k)
     for (int j = 1; j <= c.n2m; ++j)
       for (int i = 1; i <= c.n1m; ++i) {
         double qcf = std::fabs((vx(i, j, k) + vx(i + 1, j, k)) * 0.5 * c.dx1) +
                      std::fabs((vy(i, j, k) + vy(i, j + 1, k)) * 0.5 * c.dx2) +
                      std::fabs((vz(i, j, k) + vz(i, j, k + 1)) * 0.5 * c.dx3);
+        if (!std::isfinite(qcf) || !std::isfinite(te(i, j, k))) finite = false;
         cflm = std::max(cflm, qcf);
       }
   c.S(MIBM_S_CFLM) = cflm;
+  if (!finite) fail(&c, MIBM_ENONFINITE, "cfl: non-finite velocity or temperature");
 }
 
 void get_dt(Ctx& c) {   // cfl.f90:33-77
@@ -2238,6 +2243,7 @@ int mibm_batch_step_(const int* handle, const int* ntime) {
     const int nt = *ntime > 0 ? *ntime : c->steps_done + 1;
     c->I(MIBM_I_NTIME) = nt;
     cfl(*c);
+    if (c->status != MIBM_OK) return c->status;
     if (c->I(MIBM_I_IDTV) == 1) {
       if (nt != 1) c->S(MIBM_S_DT) = c->S(MIBM_S_DTMAX);
       get_dt(*c);
