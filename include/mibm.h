@@ -294,6 +294,13 @@ void calcabc_hitforce_(void);
 /* save and restore (hit.f90:256-356).                                    */
 int  mibm_hit_modes_(void);
 void mibm_hit_bhat_(double* bhat, const int* dir);
+/* mibm_hit_rng_: position of the Gaussian-increment stream (the splitmix64 */
+/* counter), read (dir = 0; before the first draw: the seed it would take)  */
+/* or set (dir = 1).  Saved beside bhat in a continuation so that a        */
+/* restarted run draws the increments the uninterrupted run would (the      */
+/* reference reseeds at restart, hit.f90:39-42; exact continuation needs    */
+/* the stream position).                                                    */
+void mibm_hit_rng_(unsigned long long* state, const int* dir);
 /* Linear forcing (no counterpart in the reference, which offers only the */
 /* two forcings above): forc = C_HIT * u at each velocity's own staggered */
 /* position, stored as xlen * C_HIT * u so that the reference's explicit  */

@@ -643,6 +643,11 @@ void mibm_hit_bhat_(double* bhat, const int* dir) {
   if (!bhat || (*dir != 0 && *dir != 1)) { fail(c, MIBM_EINVAL, "hit_bhat: dir 0 (get) or 1 (set)"); return; }
   hit_bhat(c, bhat, *dir);
 }
+void mibm_hit_rng_(unsigned long long* state, const int* dir) {
+  Ctx* c = current(); if (!ready(c)) return;
+  if (!state || (*dir != 0 && *dir != 1)) { fail(c, MIBM_EINVAL, "hit_rng: dir 0 (get) or 1 (set)"); return; }
+  hit_rng(c, state, *dir);
+}
 
 void cfl_(void) {
   DROPIN_BEGIN

@@ -274,6 +274,7 @@ void k_hit_abc_force(Ctx* c);
 void k_hit_linear_force(Ctx* c);
 int hit_modes(Ctx* c);
 void hit_bhat(Ctx* c, double* buf, int dir);
+void hit_rng(Ctx* c, unsigned long long* state, int dir);
 void hit_free(Ctx* c);
 // autotuner support (tridiag.cu, stencil.cu)
 float tri_time_direction(Ctx* c, int dir, int m, bool f32, int reps);

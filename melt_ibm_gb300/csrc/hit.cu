@@ -324,4 +324,13 @@ void hit_bhat(Ctx* c, double* buf, int dir) {
   else std::copy(buf, buf + n, h->bhat.begin());
 }
 
+// Position of the Gaussian-increment stream (the splitmix64 counter): read
+// (dir 0; before the first draw, the seed the first call would take) or
+// set (dir 1), so that a continued run draws what the uninterrupted one would.
+void hit_rng(Ctx* c, unsigned long long* state, int dir) {
+  HitState* h = hit_of(c);
+  if (dir == 0) *state = h->rng_seeded ? h->rng : (uint64_t)(int64_t)c->I(MIBM_I_HIT_SEED);
+  else { h->rng = *state; h->rng_seeded = true; }
+}
+
 }  // namespace mibm

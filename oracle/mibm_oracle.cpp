@@ -2395,6 +2395,13 @@ void mibm_hit_bhat_(double* bhat, const int* dir) {
   }
 }
 
+void mibm_hit_rng_(unsigned long long* state, const int* dir) {
+  Ctx* c = cur(); if (!ready(c)) return;
+  if (!state || (*dir != 0 && *dir != 1)) { fail(c, MIBM_EINVAL, "hit_rng: dir 0 (get) or 1 (set)"); return; }
+  if (*dir == 0) *state = c->hit_seeded ? c->hit_rng : (uint64_t)(int64_t)c->I(MIBM_I_HIT_SEED);
+  else { c->hit_rng = *state; c->hit_seeded = true; }
+}
+
 void solxi_(const double* betadx) { Ctx* c = cur(); if (ready(c)) solxi(*c, *betadx); }
 void solxj_(const double* betadx) { Ctx* c = cur(); if (ready(c)) solxj(*c, *betadx); }
 void solxk_(double* q, const double* betadx) { Ctx* c = cur(); if (ready(c)) solxk(*c, q, *betadx); }
