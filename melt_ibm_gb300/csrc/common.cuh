@@ -41,6 +41,11 @@ enum Coef {
   kUP1, kUP2, kUP3,       // al*dt*dx1, al*dt*dx2, al*dt*dx3 (updvp)
   kBE,                    // al*beta                         (prcalc)
   kUSDTAL,                // 1/(dt*al)                       (divg)
+  // the RHS of invtr1-3 / invtrte with dt folded in (one multiply per term)
+  kGDT, kRDT,             // ga*dt, ro*dt
+  kLV1, kLV2, kLV3, kLVC, // al/ren*dt*dxq (per direction), 2*(kLV1+kLV2+kLV3)
+  kLT1, kLT2, kLT3, kLTC, // al/pec*dt*dxq, 2*(kLT1+kLT2+kLT3)
+  kPD1, kPD2, kPD3,       // dt*kPX1, dt*kPX2, dt*kPX3
   kNCoef
 };
 

@@ -80,6 +80,13 @@ StepParams host_params(Ctx* c) {
   q[kUP1] = p.al * p.dt * g.dx1; q[kUP2] = p.al * p.dt * g.dx2; q[kUP3] = p.al * p.dt * g.dx3;
   q[kBE] = p.al * p.beta;
   q[kUSDTAL] = 1.0 / (p.dt * p.al);
+  q[kGDT] = p.ga * p.dt; q[kRDT] = p.ro * p.dt;
+  q[kLV1] = p.alre * p.dt * g.dx1q; q[kLV2] = p.alre * p.dt * g.dx2q; q[kLV3] = p.alre * p.dt * g.dx3q;
+  q[kLVC] = 2.0 * (q[kLV1] + q[kLV2] + q[kLV3]);
+  const double alpec = p.al / p.pec;
+  q[kLT1] = alpec * p.dt * g.dx1q; q[kLT2] = alpec * p.dt * g.dx2q; q[kLT3] = alpec * p.dt * g.dx3q;
+  q[kLTC] = 2.0 * (q[kLT1] + q[kLT2] + q[kLT3]);
+  q[kPD1] = p.dt * q[kPX1]; q[kPD2] = p.dt * q[kPX2]; q[kPD3] = p.dt * q[kPX3];
   for (int i = 0; i < kNCoef; ++i) p.cf[i] = (float)q[i];
   return p;
 }
