@@ -132,6 +132,7 @@ static bool step_prepare(Ctx* c) {
     if (!c->rhs4 && !cuda_ok(c, cudaMalloc(&c->rhs4, 4 * g.cells * sizeof(double)), "rhs4")) return false;
   }
   if (!tri_step_fill(c, bd, f32)) return false;
+  if (!fft_prepare(c, false) || (f32 && !fft_prepare(c, true))) return false;
   if (c->I(MIBM_I_FORCING) == 1 && !c->forc_q &&
       !cuda_ok(c, cudaMalloc(&c->forc_q, 3 * g.cells * sizeof(double)), "forcing quotient"))
     return false;

@@ -204,15 +204,15 @@ __global__ void fft_z_solve(FftArgs<C> F, C* __restrict__ spec) {
   __syncthreads();
   C* Rr = fft_lines(A, B, n, kCols, 1, kCols, F.pz, tws, -1);
   C* O = (Rr == A) ? B : A;
-  R a2 = F.ak2[j];
+  const R* __restrict__ eig = F.eig + (size_t)g.H * j;
+  const size_t eig_k = (size_t)g.H * g.n2m;
   for (int t = threadIdx.x; t < kCols * n; t += blockDim.x) {
     int k = t / kCols, l = t % kCols;
     C v = Rr[t];
     if (l < nc) {
-      v.x *= F.inv_nn; v.y *= F.inv_nn;                 // buft / float(n1m*n2m*n3m)
-      R d = -F.ak3[k] - F.ak1[kx0 + l] - a2;            // -ak3(k)-ak1(i)-ak2(j)
+      // buft / float(n1m*n2m*n3m) / (-ak3(k)-ak1(i)-ak2(j)), zero mode := 0
       if (k == 0 && kx0 + l == 0 && j == 0) v = mk<C>(0, 0);
-      else { R rd = R(1) / d; v.x *= rd; v.y *= rd; }
+      else { const R f = eig[(size_t)(kx0 + l) + eig_k * k]; v.x *= f; v.y *= f; }
     } else {
       v = mk<C>(0, 0);
     }
@@ -232,8 +232,41 @@ struct FftCache {
   double2 *twx = nullptr, *twy = nullptr, *twz = nullptr;
   float2 *ftwx = nullptr, *ftwy = nullptr, *ftwz = nullptr;
   float *fak1 = nullptr, *fak2 = nullptr, *fak3 = nullptr;
+  double* eig = nullptr;    // FftArgs::eig, FP64 (built at the first FP64 solve)
+  float* feig = nullptr;    // the same rounded to FP32 (first FP32 solve)
 };
 static std::vector<FftCache> g_fft;
+
+// inv_nn * (1 / (-ak3(k) - ak1(kx) - ak2(j))) for kx < H, 0 at the zero mode
+__global__ void eig_kernel(Grid g, const double* __restrict__ ak1, const double* __restrict__ ak2,
+                           const double* __restrict__ ak3, double inv_nn, double* __restrict__ out,
+                           float* __restrict__ fout) {
+  const size_t n = (size_t)g.H * g.n2m * g.n3m;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const int kx = (int)(t % g.H);
+    const size_t r = t / g.H;
+    const int j = (int)(r % g.n2m), k = (int)(r / g.n2m);
+    double f = 0.0;
+    if (kx != 0 || j != 0 || k != 0) f = inv_nn * (1.0 / (-ak3[k] - ak1[kx] - ak2[j]));
+    if (out) out[t] = f;
+    if (fout) fout[t] = (float)f;
+  }
+}
+
+static bool make_eig(Ctx* c, FftCache* f, bool f32) {
+  if (f32 ? f->feig != nullptr : f->eig != nullptr) return true;
+  const Grid& g = c->g;
+  const size_t n = (size_t)g.H * g.n2m * g.n3m;
+  void* p = nullptr;
+  if (!cuda_ok(c, cudaMalloc(&p, n * (f32 ? sizeof(float) : sizeof(double))), "eigenvalue table")) return false;
+  const double inv_nn = 1.0 / ((double)g.n1m * (double)g.n2m * (double)g.n3m);
+  eig_kernel<<<(unsigned)std::min<size_t>(div_up(n, 256), 4096), 256, 0, c->stream>>>(
+      g, c->ak1, c->ak2, c->ak3, inv_nn, f32 ? nullptr : (double*)p, f32 ? (float*)p : nullptr);
+  ++c->launches;
+  if (f32) f->feig = (float*)p;
+  else f->eig = (double*)p;
+  return true;
+}
 
 template <typename C>
 static C* make_tw(Ctx* c, int n) {
@@ -284,9 +317,17 @@ void fft_free(Ctx* c) {
       cudaFree(f.twx); cudaFree(f.twy); cudaFree(f.twz);
       cudaFree(f.ftwx); cudaFree(f.ftwy); cudaFree(f.ftwz);
       cudaFree(f.fak1); cudaFree(f.fak2); cudaFree(f.fak3);
+      cudaFree(f.eig); cudaFree(f.feig);
       g_fft.erase(g_fft.begin() + q);
       return;
     }
+}
+
+// Builds the tables the solve of the given form needs before a step is
+// launched (and possibly captured into a graph).
+bool fft_prepare(Ctx* c, bool f32) {
+  FftCache* fc = fft_of(c);
+  return make_eig(c, fc, f32);
 }
 
 template <typename C, typename S>
@@ -329,6 +370,8 @@ void k_phcalc(Ctx* c) {
   F.twx = fc->twx; F.twy = fc->twy; F.twz = fc->twz;
   F.ak1 = c->ak1; F.ak2 = c->ak2; F.ak3 = c->ak3;
   F.inv_nn = 1.0 / ((double)g.n1m * (double)g.n2m * (double)g.n3m);
+  if (!make_eig(c, fc, false)) return;
+  F.eig = fc->eig;
   phcalc_launch<double2, double>(c, F, c->df[MIBM_F_DPH], c->df[MIBM_F_DPH], "phcalc");
 }
 
@@ -344,6 +387,8 @@ void k_phcalc_f32(Ctx* c, const float* src, float* phi) {
   F.twx = fc->ftwx; F.twy = fc->ftwy; F.twz = fc->ftwz;
   F.ak1 = fc->fak1; F.ak2 = fc->fak2; F.ak3 = fc->fak3;
   F.inv_nn = (float)(1.0 / ((double)g.n1m * (double)g.n2m * (double)g.n3m));
+  if (!make_eig(c, fc, true)) return;
+  F.eig = fc->feig;
   phcalc_launch<float2, float>(c, F, src, phi, "phcalc_f32");
 }
 

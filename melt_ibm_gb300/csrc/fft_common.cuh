@@ -45,6 +45,10 @@ struct FftArgs {
   const R* ak2;
   const R* ak3;
   R inv_nn;
+  // inv_nn / (-ak3(k) - ak1(kx) - ak2(j)) at kx + H*(j + n2m*k), 0 at the
+  // zero mode: the scale and the eigenvalue division of the z pass as one
+  // multiply (an FP64 division is a long sequence of FP64 operations)
+  const R* eig;
 };
 
 template <typename C>

@@ -293,15 +293,15 @@ __global__ void __launch_bounds__(Shape<C, N>::T, Shape<C, N>::kMinBlocks) z_sol
   load_cols<C, N>(buf, spec, base, zstride, nc);
   __syncthreads();
   run<C, N, L, T, false>(buf, tw);
-  const R a2 = F.ak2[j];
+  const R* __restrict__ eig = F.eig + (size_t)g.H * j;
+  const size_t eig_k = (size_t)g.H * g.n2m;
   for (int t = threadIdx.x; t < N * L; t += T) {
     const int l = t % L, k = t / L;
     C v = buf[k * ES + l];
     if (l < nc) {
-      v.x *= F.inv_nn; v.y *= F.inv_nn;                 // buft / float(n1m*n2m*n3m)
-      R d = -F.ak3[k] - F.ak1[kx0 + l] - a2;            // -ak3(k)-ak1(i)-ak2(j)
+      // buft / float(n1m*n2m*n3m) / (-ak3(k)-ak1(i)-ak2(j)), zero mode := 0
       if (k == 0 && kx0 + l == 0 && j == 0) v = mk<C>(R(0), R(0));
-      else { R rd = R(1) / d; v.x *= rd; v.y *= rd; }
+      else { const R f = eig[(size_t)(kx0 + l) + eig_k * k]; v.x *= f; v.y *= f; }
     } else {
       v = mk<C>(R(0), R(0));
     }

@@ -325,10 +325,33 @@ static bool chunk_ok(int m) {
   return false;
 }
 
+// lanes a line occupies in the x-line kernel: G = n/M rounded up to a power
+// of two (shuffle segments); a warp solves 32/that lines
+__host__ __device__ constexpr int line_lanes(int G) {
+  return G <= 1 ? 1 : (G <= 2 ? 2 : (G <= 4 ? 4 : (G <= 8 ? 8 : (G <= 16 ? 16 : 32))));
+}
+static int ilog2(int v) { int l = 0; while ((1 << l) < v) ++l; return l; }
+
+// x-lines: the chunk length with the fewest FP64 warp instructions per line.
+// A warp instruction costs the same however many of its lanes are active,
+// and on this part FP64 ones issue at a small fraction of the FP32 rate: per
+// line, 6 per element of a chunk (forward, backward, fix-up, closure) plus 4
+// per round of the two shuffle scans, shared by the 32/Gp lines of a warp.
+// Segments of at least 16 lanes are preferred: with 8 (M = 16 at 128) the
+// longer per-thread chains and fewer warps lose what the model saves
+// (measured at 128^3: M = 8 0.475 ms, M = 16 0.523 ms per step of x-solves;
+// at 256^3 M = 16 with 16 lanes is the best).
 int tri_chunk_line(int n) {
-  for (int G = 32; G >= 1; --G)
-    if (n % G == 0 && chunk_ok(n / G)) return n / G;
-  return 0;
+  int best = 0, best_wide = 0;
+  double best_cost = 1e300, best_wide_cost = 1e300;
+  for (int m : kChunkM) {
+    if (n % m != 0 || n / m > 32) continue;
+    const int gp = line_lanes(n / m);
+    const double cost = (6.0 * m + 4.0 * ilog2(gp) + 8.0) * gp / 32.0;
+    if (cost < best_cost) { best_cost = cost; best = m; }
+    if (gp >= 16 && cost < best_wide_cost) { best_wide_cost = cost; best_wide = m; }
+  }
+  return best_wide ? best_wide : best;
 }
 
 // y/z blocks: up to 32 chunks (warps) of M <= 8 cells, or 16 chunks of the
@@ -467,18 +490,21 @@ __device__ __forceinline__ void store_chunk(V* __restrict__ p, const V (&r)[M]) 
   }
 }
 
-// x-lines: one warp per line (row j of plane k), lane h < G holds cells
-// [h*M, h*M + M).  Rows start on 16-byte boundaries (pitch multiple of 4).
+// x-lines: a line (row j of plane k) occupies a segment of GP = line_lanes(G)
+// lanes, lane h < G of it holding cells [h*M, h*M + M); a warp solves 32/GP
+// lines.  Rows start on 16-byte boundaries (pitch multiple of 4).
 template <typename V, int M>
 __global__ void __launch_bounds__(256) solve_xc_kernel(Grid g, V* __restrict__ rhs, const V* __restrict__ X) {
   const unsigned FULL = 0xffffffffu;
-  const int n = g.n1m, G = n / M;
-  const int lane = threadIdx.x & 31;
-  const int line = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (line >= g.n2m * g.n3m) return;                 // whole warp
+  const int n = g.n1m, G = n / M, GP = line_lanes(G), LPW = 32 / GP;
+  const int lane = threadIdx.x & 31, hl = lane % GP;
+  const int warp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lines = g.n2m * g.n3m;
+  if (warp * LPW >= lines) return;                   // whole warp
+  const int line = warp * LPW + lane / GP;
+  const bool act = line < lines && hl < G;
   const int j = line % g.n2m, k = line / g.n2m;
-  const bool act = lane < G;
-  V* row = rhs + cidx(g, 0, j, k) + (size_t)(act ? lane : 0) * M;
+  V* row = act ? rhs + cidx(g, 0, j, k) + (size_t)hl * M : rhs;
   V r[M];
   if (act) load_chunk<V, M>(row, r);
   else {
@@ -486,7 +512,7 @@ __global__ void __launch_bounds__(256) solve_xc_kernel(Grid g, V* __restrict__ r
     for (int i = 0; i < M; ++i) r[i] = V(0);
   }
   const V rlast = r[M - 1];
-  const int h = act ? lane : 0;
+  const int h = hl < G ? hl : 0;
   // forward, zero entry
   V C = V(0);
 #pragma unroll
@@ -497,13 +523,12 @@ __global__ void __launch_bounds__(256) solve_xc_kernel(Grid g, V* __restrict__ r
   }
   // y_in: exclusive scan of the affine chunk maps y -> C + PL y
   V Cv = act ? C : V(0), Pv = act ? X[7 * n + h] : V(1);
-#pragma unroll
-  for (int off = 1; off < 32; off <<= 1) {
-    V Co = __shfl_up_sync(FULL, Cv, off), Po = __shfl_up_sync(FULL, Pv, off);
-    if (lane >= off) { Cv = Cv + Pv * Co; Pv = Pv * Po; }
+  for (int off = 1; off < GP; off <<= 1) {
+    V Co = __shfl_up_sync(FULL, Cv, off, GP), Po = __shfl_up_sync(FULL, Pv, off, GP);
+    if (hl >= off) { Cv = Cv + Pv * Co; Pv = Pv * Po; }
   }
-  V y_in = __shfl_up_sync(FULL, Cv, 1);
-  if (lane == 0) y_in = V(0);
+  V y_in = __shfl_up_sync(FULL, Cv, 1, GP);
+  if (hl == 0) y_in = V(0);
   // backward, zero entry
   V D = V(0);
 #pragma unroll
@@ -513,13 +538,12 @@ __global__ void __launch_bounds__(256) solve_xc_kernel(Grid g, V* __restrict__ r
   }
   // f_in: exclusive suffix scan of f -> u + QF f, u = D_first + DPF y_in
   V Uv = act ? r[0] + X[7 * n + 2 * G + h] * y_in : V(0), Qv = act ? X[7 * n + G + h] : V(1);
-#pragma unroll
-  for (int off = 1; off < 32; off <<= 1) {
-    V Uo = __shfl_down_sync(FULL, Uv, off), Qo = __shfl_down_sync(FULL, Qv, off);
-    if (lane + off < G) { Uv = Uv + Qv * Uo; Qv = Qv * Qo; }
+  for (int off = 1; off < GP; off <<= 1) {
+    V Uo = __shfl_down_sync(FULL, Uv, off, GP), Qo = __shfl_down_sync(FULL, Qv, off, GP);
+    if (hl + off < G) { Uv = Uv + Qv * Uo; Qv = Qv * Qo; }
   }
-  V f_in = __shfl_down_sync(FULL, Uv, 1);
-  if (lane + 1 >= G) f_in = V(0);
+  V f_in = __shfl_down_sync(FULL, Uv, 1, GP);
+  if (hl + 1 >= G) f_in = V(0);
 #pragma unroll
   for (int i = 0; i < M; ++i) {
     int t = i * G + h;
@@ -527,9 +551,9 @@ __global__ void __launch_bounds__(256) solve_xc_kernel(Grid g, V* __restrict__ r
   }
   // periodic closure
   const V* S = X + 7 * n + 3 * G;
-  V f1 = __shfl_sync(FULL, r[0], 0);
-  V fnm1 = __shfl_sync(FULL, r[M - 2], G - 1);
-  V rn = __shfl_sync(FULL, rlast, G - 1);
+  V f1 = __shfl_sync(FULL, r[0], 0, GP);
+  V fnm1 = __shfl_sync(FULL, r[M - 2], G - 1, GP);
+  V rn = __shfl_sync(FULL, rlast, G - 1, GP);
   V xn = (rn * S[0] - S[1] * f1 - S[2] * fnm1) * S[3];
 #pragma unroll
   for (int i = 0; i < M; ++i) r[i] = xn * X[3 * n + i * G + h] + r[i];
@@ -708,7 +732,8 @@ static bool solve_xc_launch(Ctx* c, V* rhs, const V* T, const char* name) {
   TriLayout L = tri_layout(c->g.n1m, tri_chunk(c, 0));
   if (!L.m) return false;
   const V* X = T + L.off_ext;
-  dim3 grid(div_up((size_t)c->g.n2m * c->g.n3m, 8));
+  const int lpw = 32 / line_lanes(c->g.n1m / L.m);           // lines per warp
+  dim3 grid(div_up((size_t)c->g.n2m * c->g.n3m, 8 * (size_t)lpw));
   {
     MIBM_PROF(c, name);
 #define XC(M) solve_xc_kernel<V, M><<<grid, 256, 0, c->stream>>>(c->g, rhs, X)
