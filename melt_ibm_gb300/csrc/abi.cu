@@ -171,6 +171,7 @@ static void step_enqueue_f32(Ctx* c) {
     c->prologue_done = false;
     k_fused_rhs_f32(c, dp, c->ru32, c->rhs32);
     for (int q = 0; q < 4; ++q) {
+      if (q == 3) lagr_loads_early(c, dp);   // u, v, w solved: loads beside the T solves
       int f = (q < 3) ? 0 : 1;
       const float* T = tf + (size_t)((ns * 2 + f) * 3) * tlen;
       float* r = c->rhs32 + (size_t)q * g.cells;
@@ -203,6 +204,7 @@ static void step_enqueue_f64(Ctx* c) {
     c->prologue_done = false;
     k_fused_rhs(c, dp);
     for (int q = 0; q < 4; ++q) {
+      if (q == 3) lagr_loads_early(c, dp);   // u, v, w solved: loads beside the T solves
       int f = (q < 3) ? 0 : 1;
       const double* T = tables + (size_t)((ns * 2 + f) * 3) * tlen;
       double* r = c->rhs4 + (size_t)q * g.cells;

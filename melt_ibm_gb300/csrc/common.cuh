@@ -138,6 +138,8 @@ struct Ctx {
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   bool join_pending = false;
+  cudaEvent_t ev_lfork = nullptr, ev_ldone = nullptr;   // structural loads on the side stream
+  bool loads_pending = false;
   std::vector<void*> pinned;              // host arrays page-locked by mibm_pin_host_
   bool prologue_done = false;             // the next substep's geometry-only work is enqueued
   // fused-step state
@@ -360,6 +362,7 @@ void k_rigid_publish(Ctx* c, const double* geom, StepParams* next);
 void rigid_free(Ctx* c);
 void lagr_step_readback(Ctx* c);
 void lagr_join(Ctx* c);
+void lagr_loads_early(Ctx* c, const StepParams* dp);
 void lagr_step_host_finish(Ctx* c);
 void lagr_geometry_to_host(Ctx* c);
 void lagr_invalidate(Ctx* c);

@@ -285,6 +285,8 @@ void release(Ctx* c) {
   if (c->side) { cudaStreamSynchronize(c->side); cudaStreamDestroy(c->side); }
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
+  if (c->ev_lfork) cudaEventDestroy(c->ev_lfork);
+  if (c->ev_ldone) cudaEventDestroy(c->ev_ldone);
   if (c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -305,7 +307,9 @@ int mibm_context_create_(void) {
   if (!cuda_ok(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream") ||
       !cuda_ok(c, cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking), "stream") ||
       !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "event") ||
-      !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming), "event")) {
+      !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming), "event") ||
+      !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_lfork, cudaEventDisableTiming), "event") ||
+      !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_ldone, cudaEventDisableTiming), "event")) {
     t_cur = c;
     return -MIBM_ECUDA;
   }

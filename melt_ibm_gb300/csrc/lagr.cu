@@ -2151,6 +2151,25 @@ void lagr_substep_prologue(Ctx* c, int slot) {
   update_plan(c, c->dparams + slot);
 }
 
+// The structural loads read u, v, w after their line solves, p, and the
+// geometry, nothing that the temperature's line solves write: the fused step
+// starts them on the side stream once w is solved, so that they run beside
+// the temperature solves; the velocity scatter, which changes u, v, w, waits
+// for them (lagr_particle_fused).  Same conditions as the particle fork.
+void lagr_loads_early(Ctx* c, const StepParams* dp) {
+  c->loads_pending = false;
+  if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0 || c->I(MIBM_I_IMLSSTR) != 1) return;
+  if (!c->side || lagr_remesh_active(c) || c->profiling) return;
+  if (!ensure_adjacency(c) || !ensure_lag_buffers(c)) return;
+  cudaEventRecord(c->ev_lfork, c->stream);
+  cudaStreamWaitEvent(c->side, c->ev_lfork, 0);
+  std::swap(c->stream, c->side);
+  struct_loads_launch(c, dp);
+  cudaEventRecord(c->ev_ldone, c->stream);
+  std::swap(c->stream, c->side);
+  c->loads_pending = true;
+}
+
 const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror, StepParams* next,
                                   int next_prologue) {
   if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0) return nullptr;
@@ -2158,7 +2177,14 @@ const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror,
   LagState* s = lag_of(c);
   force_coefficients(c);
   bool str = c->I(MIBM_I_IMLSSTR) == 1;
-  if (str) struct_loads_launch(c, dp);      // reads the unforced u, v, w and p
+  if (str) {                                 // reads the unforced u, v, w and p
+    if (c->loads_pending) {
+      cudaStreamWaitEvent(c->stream, c->ev_ldone, 0);
+      c->loads_pending = false;
+    } else {
+      struct_loads_launch(c, dp);
+    }
+  }
   scatter(c, true, 0, 3, true);
   double ncell = (double)c->g.n1m * (double)c->g.n2m * (double)c->g.n3m;
   { MIBM_PROF(c, "seg_mean");
