@@ -476,44 +476,85 @@ __device__ __forceinline__ int key_comp(int k, size_t cells) {
   return (u >= cells) + (u >= 2 * cells) + (u >= 3 * cells) + (u >= 4 * cells);   // 4 = ghost face
 }
 
-__global__ void scatter_apply_kernel(int n, int nf, size_t cells, const int* __restrict__ key,
-                                     const int* __restrict__ src, const double* __restrict__ coef, ScatterOut O,
-                                     int comp_lo, int comp_hi, double* __restrict__ segval) {
+// Heads of the sorted plan (the first entry of each run of one real key),
+// in key order, built with the plan: flag, exclusive scan, compaction.
+__device__ __forceinline__ bool plan_head(const int* __restrict__ key, int e, size_t cells) {
+  const int k = key[e];
+  return key_comp(k, cells) < 4 && (e == 0 || key[e - 1] != k);
+}
+
+__global__ void head_flag_kernel(int n, size_t cells, const int* __restrict__ key, const int* __restrict__ dirty,
+                                 int* __restrict__ hidx) {
+  if (!*dirty) return;
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) hidx[e] = plan_head(key, e, cells) ? 1 : 0;
+}
+
+__global__ void head_compact_kernel(int n, size_t cells, const int* __restrict__ key, const int* __restrict__ hidx,
+                                    const int* __restrict__ dirty, int* __restrict__ heads, int* __restrict__ nheads) {
+  if (!*dirty) return;
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n) return;
-  int k = key[e];
-  int comp = key_comp(k, cells);
-  bool head = (comp < 4) && (e == 0 || key[e - 1] != k);
-  if (!head || comp < comp_lo || comp >= comp_hi) {
-    if (segval && comp >= comp_lo && comp < comp_hi) segval[e] = 0.0;
-    return;
+  const bool head = plan_head(key, e, cells);
+  if (head) heads[hidx[e]] = e;
+  if (e == n - 1) *nheads = hidx[e] + (head ? 1 : 0);
+}
+
+// One warp per run (a cell of one component): the lanes take every 32nd
+// entry of the run (face order), a fixed shuffle tree adds the 32 partial
+// sums, lane 0 adds the total to the target field.  A warp instruction costs
+// the same with 1 or 32 active lanes, and FP64 ones issue at a small fraction
+// of the FP32 rate, so the runs (tens of entries each) are not summed by one
+// thread.  With `segval` the run sum is also recorded at the run's index
+// (for the mean force).
+constexpr int kScatterBlocks = 1216;     // 8 blocks of 8 warps per SM on 152 SMs; the warps loop over runs
+__global__ void __launch_bounds__(256) scatter_apply_kernel(int n, int nf, size_t cells, const int* __restrict__ key,
+                                     const int* __restrict__ src, const double* __restrict__ coef, ScatterOut O,
+                                     int comp_lo, int comp_hi, const int* __restrict__ heads,
+                                     const int* __restrict__ nheads, double* __restrict__ segval) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  const int nh = *nheads;
+  const int per = 27 * nf;
+  for (int h = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); h < nh; h += nw) {
+    const int e0 = heads[h];
+    const int k = key[e0];
+    const int comp = key_comp(k, cells);
+    if (comp < comp_lo || comp >= comp_hi) continue;            // uniform over the warp
+    const int e1 = h + 1 < nh ? heads[h + 1] : n;               // the last run ends before the ghost entries
+    const double* __restrict__ phi = O.phi[comp];
+    const double* __restrict__ cf = coef + (size_t)comp * nf;
+    double sum = 0.0;
+    for (int q = e0 + lane; q < e1 && key[q] == k; q += 32) {
+      const int sr = src[q] - comp * per;
+      sum = fma(cf[sr / 27], phi[sr], sum);
+    }
+    for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(FULL, sum, off);
+    if (lane == 0) {
+      const size_t cell = (size_t)k - (size_t)comp * cells;
+      const double v = O.f[comp][cell] + sum;
+      O.f[comp][cell] = v;
+      if (O.m32[comp]) O.m32[comp][cell] = (float)v;
+      if (segval) segval[h] = sum;
+    }
   }
-  size_t cell = (size_t)k - (size_t)comp * cells;
-  int per = 27 * nf;
-  double sum = 0.0;
-  for (int q = e; q < n && key[q] == k; ++q) {
-    int sr = src[q] - comp * per;
-    int t = sr / 27;
-    sum = sum + coef[(size_t)comp * nf + t] * O.phi[comp][sr];
-  }
-  double q = O.f[comp][cell] + sum;
-  O.f[comp][cell] = q;
-  if (O.m32[comp]) O.m32[comp][cell] = (float)q;
-  if (segval) segval[e] = sum;
 }
 
 // fixed-order sum of the recorded run sums per velocity component: 256
-// blocks over contiguous ranges, then one block over the 256 partials
+// blocks over contiguous ranges of runs, then one block over the 256 partials
 constexpr int kMeanBlocks = 256;
-__global__ void seg_partial_kernel(int n, size_t cells, const int* __restrict__ key, const double* __restrict__ segval,
+__global__ void seg_partial_kernel(const int* __restrict__ nheads, const int* __restrict__ heads, size_t cells,
+                                   const int* __restrict__ key, const double* __restrict__ segval,
                                    double* __restrict__ part) {
   __shared__ double sm[3][256];
+  const int n = *nheads;
   int per = (n + gridDim.x - 1) / gridDim.x;
   int lo = blockIdx.x * per, hi = min(n, lo + per);
   double s[3] = {0, 0, 0};
-  for (int e = lo + threadIdx.x; e < hi; e += blockDim.x) {
-    int comp = key_comp(key[e], cells);
-    if (comp < 3) s[comp] += segval[e];
+  for (int h = lo + threadIdx.x; h < hi; h += blockDim.x) {
+    int comp = key_comp(key[heads[h]], cells);
+    if (comp < 3) s[comp] += segval[h];
   }
   for (int q = 0; q < 3; ++q) sm[q][threadIdx.x] = s[q];
   __syncthreads();
@@ -1505,6 +1546,7 @@ struct LagState {
   int plan_n = 0, plan_cap = 0, nblk = 0;
   int *key = nullptr, *src = nullptr, *tmp_key = nullptr, *tmp_src = nullptr, *hist = nullptr;
   int* tsum = nullptr;   // tile totals of the histogram scan
+  int *hidx = nullptr, *heads = nullptr, *nheads = nullptr, *htsum = nullptr;   // run heads of the plan
   int *res_key = nullptr, *res_src = nullptr;   // buffers holding the sorted result
   int* saved = nullptr;                          // 7 ints per face: pind(1:6), ghost
   int* dirty = nullptr;
@@ -1606,10 +1648,15 @@ static bool ensure_lag_buffers(Ctx* c) {
               cuda_ok(c, cudaMalloc(&s->tsum, sizeof(int) * (size_t)div_up(256 * (size_t)s->nblk, 1024)), "plan") &&
               cuda_ok(c, cudaMalloc(&s->saved, sizeof(int) * 7 * (size_t)std::max(1, c->maxnf)), "plan") &&
               cuda_ok(c, cudaMalloc(&s->dirty, sizeof(int)), "plan") &&
-              cuda_ok(c, cudaMalloc(&s->segval, sizeof(double) * n), "plan");
+              cuda_ok(c, cudaMalloc(&s->segval, sizeof(double) * n), "plan") &&
+              cuda_ok(c, cudaMalloc(&s->hidx, sizeof(int) * n), "plan") &&
+              cuda_ok(c, cudaMalloc(&s->heads, sizeof(int) * n), "plan") &&
+              cuda_ok(c, cudaMalloc(&s->nheads, sizeof(int)), "plan") &&
+              cuda_ok(c, cudaMalloc(&s->htsum, sizeof(int) * (size_t)div_up(n, 1024)), "plan");
     if (!ok) return false;
     s->plan_n = n;
     cudaMemsetAsync(s->saved, 0xff, sizeof(int) * 7 * (size_t)std::max(1, c->maxnf), c->stream);
+    cudaMemsetAsync(s->nheads, 0, sizeof(int), c->stream);
   }
   return true;
 }
@@ -1671,6 +1718,15 @@ static void update_plan(Ctx* c, const StepParams* dp) {
     std::swap(kin, kout); std::swap(vin, vout);
   }
   s->res_key = kin; s->res_src = vin;         // fixed per grid: the buffers of the last pass
+  { MIBM_PROF(c, "plan_heads");
+    const unsigned tiles = div_up(n, 1024);
+    head_flag_kernel<<<tiles, 1024, 0, c->stream>>>(n, c->g.cells, s->res_key, s->dirty, s->hidx);
+    scan_tile_kernel<<<tiles, 1024, 0, c->stream>>>(s->hidx, n, s->htsum, s->dirty);
+    scan_kernel<<<1, 1024, 0, c->stream>>>(s->htsum, (int)tiles, s->dirty);
+    scan_add_kernel<<<tiles, 1024, 0, c->stream>>>(s->hidx, n, s->htsum, s->dirty);
+    head_compact_kernel<<<tiles, 1024, 0, c->stream>>>(n, c->g.cells, s->res_key, s->hidx, s->dirty, s->heads,
+                                                       s->nheads); }
+  c->launches += 5;
   { MIBM_PROF(c, "plan_commit");
     plan_commit_kernel<<<div_up(nf, 256), 256, 0, c->stream>>>(nf, pind, ghost, s->saved, s->dirty); }
   c->launches += 3 + 5 * passes;
@@ -1705,9 +1761,9 @@ static void force_coefficients(Ctx* c) {
 static void scatter(Ctx* c, bool into_fields, int lo, int hi, bool record, float* t_mirror = nullptr) {
   LagState* s = lag_of(c);
   { MIBM_PROF(c, "scatter_apply");
-    scatter_apply_kernel<<<div_up(s->plan_n, 256), 256, 0, c->stream>>>(
+    scatter_apply_kernel<<<(unsigned)std::min<size_t>(kScatterBlocks, div_up(s->plan_n, 256)), 256, 0, c->stream>>>(
         s->plan_n, c->maxnf, c->g.cells, s->res_key, s->res_src, c->tri_coef, scatter_out(c, into_fields, t_mirror), lo, hi,
-        record ? s->segval : nullptr); }
+        s->heads, s->nheads, record ? s->segval : nullptr); }
   ++c->launches;
 }
 
@@ -2188,7 +2244,7 @@ const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror,
   scatter(c, true, 0, 3, true);
   double ncell = (double)c->g.n1m * (double)c->g.n2m * (double)c->g.n3m;
   { MIBM_PROF(c, "seg_mean");
-    seg_partial_kernel<<<kMeanBlocks, 256, 0, c->stream>>>(s->plan_n, c->g.cells, s->res_key, s->segval,
+    seg_partial_kernel<<<kMeanBlocks, 256, 0, c->stream>>>(s->nheads, s->heads, c->g.cells, s->res_key, s->segval,
                                                            c->red + kRedPart);
     seg_final_kernel<<<1, kMeanBlocks, 0, c->stream>>>(c->red + kRedPart, ncell, s->mean3); }
   c->launches += 2;
@@ -2286,6 +2342,7 @@ void lagr_free(Ctx* c) {
       cudaFree(s->key); cudaFree(s->src); cudaFree(s->tmp_key); cudaFree(s->tmp_src); cudaFree(s->hist);
       cudaFree(s->tsum);
       cudaFree(s->saved); cudaFree(s->dirty); cudaFree(s->segval);
+      cudaFree(s->hidx); cudaFree(s->heads); cudaFree(s->nheads); cudaFree(s->htsum);
       delete s;
       g_lag.erase(g_lag.begin() + q);
       break;
