@@ -179,7 +179,7 @@ static void step_enqueue_f32(Ctx* c) {
       k_solve_y_f32(c, r, T + tlen);
       k_solve_z_f32(c, r, T + 2 * tlen, c->df[kStepFid[q]], q == 3 ? t_mirror : nullptr);
     }
-    const double* mean3 = lagr_particle_fused(c, dp, t_mirror, ns < 2 ? c->dparams + ns + 1 : nullptr, ns < 2 ? ns + 1 : -1);
+    const double* mean3 = lagr_particle_fused(c, dp, t_mirror, ns < 2 ? c->dparams + ns + 1 : nullptr, ns + 1);
     if (c->status != MIBM_OK) return;
     for (int it = 0; it < c->nproj; ++it) {
       bool last = it + 1 == c->nproj;
@@ -212,7 +212,7 @@ static void step_enqueue_f64(Ctx* c) {
       k_solve_y_T(c, r, T + tlen);
       k_solve_z_T(c, r, T + 2 * tlen, c->df[kStepFid[q]], 0);
     }
-    const double* mean3 = lagr_particle_fused(c, dp, nullptr, ns < 2 ? c->dparams + ns + 1 : nullptr, ns < 2 ? ns + 1 : -1);
+    const double* mean3 = lagr_particle_fused(c, dp, nullptr, ns < 2 ? c->dparams + ns + 1 : nullptr, ns + 1);
     if (c->status != MIBM_OK) return;
     k_divg(c, dp);
     k_phcalc(c);
@@ -231,7 +231,6 @@ static const double* step_vel_cm(Ctx* c) {
 
 static void step_enqueue(Ctx* c) {
   cudaMemcpyAsync(c->dparams, c->hparams, 3 * sizeof(StepParams), cudaMemcpyHostToDevice, c->stream);
-  c->prologue_done = false;
   if (moving_body(c)) rigid_upload(c);
   if (c->I(MIBM_I_FORCING) == 1 && c->precision == 0) k_forcing_quotient(c);
   if (c->precision == 1) step_enqueue_f32(c);
@@ -241,14 +240,39 @@ static void step_enqueue(Ctx* c) {
   if (c->status == MIBM_OK) lagr_step_readback(c);
 }
 
+static uint64_t step_key(Ctx* c);
+
 static void step_finish(Ctx* c) {
   lagr_join(c);
+  c->early_prologue = false;
   if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "tschem")) return;
   if (c->status != MIBM_OK) return;
   lagr_step_host_finish(c);
   if (c->diag_on && c->status == MIBM_OK) diag_finish(c);
   if (c->precision == 1 && c->status == MIBM_OK) c->q32_valid = true;
   ++c->steps_done;
+  // the last substep enqueued the next step's substep-0 geometry work
+  if (c->status == MIBM_OK && lagr_fork_enabled(c)) {
+    c->early_prologue = true;
+    c->early_gen = c->geom_gen;
+    c->early_key = step_key(c);
+  }
+}
+
+// Substep 0's geometry-only work (tagging, cage indices, MLS weights,
+// scatter plan): the previous step enqueued it at the end of its last
+// substep, on the side stream, unless a host call since may have changed its
+// inputs (geom_gen) or the step's configuration changed (step key); then it
+// runs here, ahead of the step and outside any step graph, after the
+// parameter blocks (substep 0's carries the host's plan rebuild request).
+static void step_head(Ctx* c) {
+  const bool early = c->early_prologue && c->early_gen == c->geom_gen && c->early_key == step_key(c);
+  c->early_prologue = false;
+  if (!early) {
+    cudaMemcpyAsync(c->dparams, c->hparams, 3 * sizeof(StepParams), cudaMemcpyHostToDevice, c->stream);
+    lagr_substep_prologue(c, 0);
+  }
+  c->prologue_done = true;
 }
 
 // Everything a step reads by value from the host besides the per-step
@@ -335,6 +359,8 @@ static bool capture_step(Ctx* c, uint64_t key) {
 // runs as a captured graph (one launch per step) while its key holds.
 static void tschem(Ctx* c) {
   if (!step_prepare(c)) return;
+  step_head(c);
+  if (c->status != MIBM_OK) return;
   bool graph = graphs_allowed(c);
   if (graph) {
     uint64_t key = step_key(c);
@@ -488,6 +514,8 @@ static int batch_step(Batch* b, int ntime) {
       else if (which == 3) k_hit_linear_force(c);
     }
     if (c->status != MIBM_OK || !step_prepare(c)) return c->status != MIBM_OK ? c->status : MIBM_ESTATE;
+    step_head(c);
+    if (c->status != MIBM_OK) return c->status;
   }
   // (C) device work: step graphs (captured where missing or stale)
   bool all_graphs = true;
@@ -555,6 +583,12 @@ using namespace mibm;
   DROPIN_BEGIN                \
   c->q32_valid = false;
 #define DROPIN_END cuda_ok(c, cudaGetLastError(), __func__);
+// drop-in routines that write the geometry, the VOF fields, the cage
+// indices, the MLS weights or the scatter plan: the next step redoes its
+// substep-0 geometry work instead of taking the one its predecessor enqueued
+#define DROPIN_GEOM           \
+  DROPIN_BEGIN                \
+  ++c->geom_gen;
 
 extern "C" {
 
@@ -580,17 +614,17 @@ void divg_(void) { DROPIN_BEGIN k_divg(c, push_params(c, 3)); DROPIN_END }
 void phcalc_(void) { DROPIN_BEGIN k_phcalc(c); DROPIN_END }
 void updvp_(void) { DROPIN_WRITES k_updvp(c, push_params(c, 3)); DROPIN_END }
 void prcalc_(void) { DROPIN_WRITES k_prcalc(c, push_params(c, 3)); DROPIN_END }
-void findcentroidindices_(void) { DROPIN_BEGIN lagr_find_centroid_indices(c); DROPIN_END }
-void mlsweight_(void) { DROPIN_BEGIN lagr_mls_weight(c); DROPIN_END }
-void mlsforce_(void) { DROPIN_WRITES lagr_mls_force(c, push_params(c, 3), true); DROPIN_END }
+void findcentroidindices_(void) { DROPIN_GEOM lagr_find_centroid_indices(c); DROPIN_END }
+void mlsweight_(void) { DROPIN_GEOM lagr_mls_weight(c); DROPIN_END }
+void mlsforce_(void) { DROPIN_WRITES ++c->geom_gen; lagr_mls_force(c, push_params(c, 3), true); DROPIN_END }
 void velforce_(void) { DROPIN_WRITES lagr_velforce(c); DROPIN_END }
 void tempforce_(void) { DROPIN_WRITES lagr_tempforce(c); DROPIN_END }
-void findprobeindices_(void) { DROPIN_BEGIN lagr_find_probe_indices(c); DROPIN_END }
-void mls_heatflux_(void) { DROPIN_BEGIN lagr_heat_flux(c); DROPIN_END }
-void apply_stefancondition_(void) { DROPIN_WRITES lagr_stefan(c, push_params(c, 3)); DROPIN_END }
-void tagcells_(void) { DROPIN_BEGIN lagr_tag_narrow_band(c); DROPIN_END }
-void tagcells_initial_(void) { DROPIN_BEGIN lagr_tag_initial(c); DROPIN_END }
-void particle_(void) { DROPIN_WRITES lagr_particle(c, push_params(c, 3)); DROPIN_END }
+void findprobeindices_(void) { DROPIN_GEOM lagr_find_probe_indices(c); DROPIN_END }
+void mls_heatflux_(void) { DROPIN_GEOM lagr_heat_flux(c); DROPIN_END }
+void apply_stefancondition_(void) { DROPIN_WRITES ++c->geom_gen; lagr_stefan(c, push_params(c, 3)); DROPIN_END }
+void tagcells_(void) { DROPIN_GEOM lagr_tag_narrow_band(c); DROPIN_END }
+void tagcells_initial_(void) { DROPIN_GEOM lagr_tag_initial(c); DROPIN_END }
+void particle_(void) { DROPIN_WRITES ++c->geom_gen; lagr_particle(c, push_params(c, 3)); DROPIN_END }
 
 // mls_structLoads: the loads of the registered fields and mesh into the
 // registered int_*_dA (previous values to the _m1 slots, sums to Fp, ...).
@@ -681,6 +715,7 @@ void mibm_set_precision_(const int* mode, const int* nproj) {
   c->q32_valid = false;
   c->precision = *mode;
   c->nproj = *nproj;
+  ++c->geom_gen;                       // the MLS weights of the two forms differ
 }
 
 // Batched form (see Batch above).  ids: contexts after mibm_init_ (and the

@@ -142,6 +142,11 @@ struct Ctx {
   bool loads_pending = false;
   std::vector<void*> pinned;              // host arrays page-locked by mibm_pin_host_
   bool prologue_done = false;             // the next substep's geometry-only work is enqueued
+  // substep 0's geometry-only work, enqueued by the previous step's last
+  // substep: valid while geom_gen (bumped by every host call that may change
+  // the geometry, the VOF fields or the MLS state) and the step key hold
+  bool early_prologue = false;
+  uint64_t geom_gen = 0, early_gen = 0, early_key = 0;
   // fused-step state
   StepParams* dparams = nullptr;          // [3] device copies (one per substep)
   StepParams* hparams = nullptr;          // pinned
@@ -363,6 +368,7 @@ void rigid_free(Ctx* c);
 void lagr_step_readback(Ctx* c);
 void lagr_join(Ctx* c);
 void lagr_loads_early(Ctx* c, const StepParams* dp);
+bool lagr_fork_enabled(Ctx* c);
 void lagr_step_host_finish(Ctx* c);
 void lagr_geometry_to_host(Ctx* c);
 void lagr_invalidate(Ctx* c);

@@ -450,6 +450,7 @@ void mibm_sync_from_host_(const long long* mask) {
   // the scatter plan and the MLS weights depend on the mesh, the
   // vertex->face lists on its connectivity
   const unsigned long long topo = (1ull << MIBM_M_VERT_OF_FACE) | (1ull << MIBM_M_GHOST_FACE);
+  ++c->geom_gen;                       // fields (VOF) or mesh from the host
   if ((m >> 32) & topo) lagr_topology_changed(c);
   else if ((m >> 32) != 0) lagr_invalidate(c);
   cuda_ok(c, cudaStreamSynchronize(c->stream), "sync_from_host");

@@ -1571,6 +1571,7 @@ static LagState* lag_of(Ctx* c) {
 // weights of a stationary body were being reused, which changes the launch
 // sequence.
 void lagr_invalidate(Ctx* c) {
+  ++c->geom_gen;
   LagState* s = lag_of(c);
   s->force_rebuild = true;
   if (c->I(MIBM_I_STATIONARY) && s->weights_valid) ++c->lag_gen;
@@ -2190,8 +2191,10 @@ void lagr_particle(Ctx* c, const StepParams* dp) {
 // The work of a substep that depends on the geometry alone: narrow-band
 // tagging (tagCells at the start of the substep, tsch.f90:45-47) and, from
 // particle, the cage indices, the MLS weights and the scatter plan.  The fused
-// step runs it for substeps 1 and 2 on the side stream of the substep before
-// (the geometry is final once that substep's particle is done).
+// step runs it on the side stream of the substep before (the geometry is
+// final once that substep's particle is done): for substeps 1 and 2, and for
+// substep 0 of the next step (slot 3: no parameter block, the host's plan
+// rebuild requests invalidate it instead).
 void lagr_substep_prologue(Ctx* c, int slot) {
   if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0) return;
   if (!c->I(MIBM_I_STATIONARY)) lagr_tag_narrow_band(c);
@@ -2204,7 +2207,14 @@ void lagr_substep_prologue(Ctx* c, int slot) {
     s->weights_valid = stationary;
     if (stationary) ++c->lag_gen;     // later steps skip the weights: another launch sequence
   }
-  update_plan(c, c->dparams + slot);
+  update_plan(c, slot < 3 ? c->dparams + slot : nullptr);
+}
+
+// The side stream takes the second half of particle (and the work that
+// follows it) unless the host's remesher may be needed mid-way or kernels
+// are timed one by one (mibm_profile_: serial, so each time is its own).
+bool lagr_fork_enabled(Ctx* c) {
+  return c->side && !lagr_remesh_active(c) && !c->profiling && c->I(MIBM_I_IMLSFOR) == 1 && c->maxnf > 0;
 }
 
 // The structural loads read u, v, w after their line solves, p, and the
@@ -2215,7 +2225,7 @@ void lagr_substep_prologue(Ctx* c, int slot) {
 void lagr_loads_early(Ctx* c, const StepParams* dp) {
   c->loads_pending = false;
   if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0 || c->I(MIBM_I_IMLSSTR) != 1) return;
-  if (!c->side || lagr_remesh_active(c) || c->profiling) return;
+  if (!lagr_fork_enabled(c)) return;
   if (!ensure_adjacency(c) || !ensure_lag_buffers(c)) return;
   cudaEventRecord(c->ev_lfork, c->stream);
   cudaStreamWaitEvent(c->side, c->ev_lfork, 0);
@@ -2252,10 +2262,8 @@ const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror,
   // front, motion, geometry) reads and writes none of the buffers of the
   // pressure projection that the caller enqueues next, so it runs on the
   // side stream; lagr_join makes the main stream wait for it before the next
-  // substep.  Not when a remesh may need the host mid-way, nor while kernels
-  // are timed one by one (mibm_profile_: serial, so each time is the
-  // kernel's own).
-  const bool fork = c->side && !lagr_remesh_active(c) && !c->profiling;
+  // substep.
+  const bool fork = lagr_fork_enabled(c);
   if (fork) {
     cudaEventRecord(c->ev_fork, c->stream);
     cudaStreamWaitEvent(c->side, c->ev_fork, 0);
