@@ -283,6 +283,9 @@ void release(Ctx* c) {
   rigid_free(c);
   diag_free(c);
   if (c->side) { cudaStreamSynchronize(c->side); cudaStreamDestroy(c->side); }
+  if (c->side2) { cudaStreamSynchronize(c->side2); cudaStreamDestroy(c->side2); }
+  if (c->ev_tfork) cudaEventDestroy(c->ev_tfork);
+  if (c->ev_tjoin) cudaEventDestroy(c->ev_tjoin);
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
   if (c->ev_lfork) cudaEventDestroy(c->ev_lfork);
@@ -306,6 +309,9 @@ int mibm_context_create_(void) {
   cudaGetDevice(&c->device);
   if (!cuda_ok(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream") ||
       !cuda_ok(c, cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking), "stream") ||
+      !cuda_ok(c, cudaStreamCreateWithFlags(&c->side2, cudaStreamNonBlocking), "stream") ||
+      !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_tfork, cudaEventDisableTiming), "event") ||
+      !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_tjoin, cudaEventDisableTiming), "event") ||
       !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "event") ||
       !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming), "event") ||
       !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_lfork, cudaEventDisableTiming), "event") ||

@@ -2197,8 +2197,24 @@ void lagr_particle(Ctx* c, const StepParams* dp) {
 // rebuild requests invalidate it instead).
 void lagr_substep_prologue(Ctx* c, int slot) {
   if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0) return;
-  if (!c->I(MIBM_I_STATIONARY)) lagr_tag_narrow_band(c);
-  if (!ensure_adjacency(c) || !ensure_lag_buffers(c)) return;
+  // the tagging (VOF fields) and the cage indices, weights and plan read the
+  // same geometry and write disjoint buffers: the tagging goes to a stream of
+  // its own and is joined back before the prologue ends
+  const bool split = !c->I(MIBM_I_STATIONARY) && c->side2 && lagr_fork_enabled(c);
+  if (split) {
+    cudaEventRecord(c->ev_tfork, c->stream);
+    cudaStreamWaitEvent(c->side2, c->ev_tfork, 0);
+    std::swap(c->stream, c->side2);
+    lagr_tag_narrow_band(c);
+    cudaEventRecord(c->ev_tjoin, c->stream);
+    std::swap(c->stream, c->side2);
+  } else if (!c->I(MIBM_I_STATIONARY)) {
+    lagr_tag_narrow_band(c);
+  }
+  if (!ensure_adjacency(c) || !ensure_lag_buffers(c)) {
+    if (split) cudaStreamWaitEvent(c->stream, c->ev_tjoin, 0);
+    return;
+  }
   LagState* s = lag_of(c);
   bool stationary = c->I(MIBM_I_STATIONARY) != 0;
   lagr_find_centroid_indices(c);
@@ -2208,6 +2224,7 @@ void lagr_substep_prologue(Ctx* c, int slot) {
     if (stationary) ++c->lag_gen;     // later steps skip the weights: another launch sequence
   }
   update_plan(c, slot < 3 ? c->dparams + slot : nullptr);
+  if (split) cudaStreamWaitEvent(c->stream, c->ev_tjoin, 0);
 }
 
 // The side stream takes the second half of particle (and the work that
