@@ -133,9 +133,6 @@ static bool step_prepare(Ctx* c) {
   }
   if (!tri_step_fill(c, bd, f32)) return false;
   if (!fft_prepare(c, false) || (f32 && !fft_prepare(c, true))) return false;
-  if (c->I(MIBM_I_FORCING) == 1 && !c->forc_q &&
-      !cuda_ok(c, cudaMalloc(&c->forc_q, 3 * g.cells * sizeof(double)), "forcing quotient"))
-    return false;
   if (moving_body(c)) {
     if (!rigid_ensure(c)) return false;
     rigid_pack(c, c->hrigid_in, false);
@@ -232,7 +229,6 @@ static const double* step_vel_cm(Ctx* c) {
 static void step_enqueue(Ctx* c) {
   cudaMemcpyAsync(c->dparams, c->hparams, 3 * sizeof(StepParams), cudaMemcpyHostToDevice, c->stream);
   if (moving_body(c)) rigid_upload(c);
-  if (c->I(MIBM_I_FORCING) == 1 && c->precision == 0) k_forcing_quotient(c);
   if (c->precision == 1) step_enqueue_f32(c);
   else step_enqueue_f64(c);
   lagr_join(c);

@@ -46,6 +46,7 @@ enum Coef {
   kLV1, kLV2, kLV3, kLVC, // al/ren*dt*dxq (per direction), 2*(kLV1+kLV2+kLV3)
   kLT1, kLT2, kLT3, kLTC, // al/pec*dt*dxq, 2*(kLT1+kLT2+kLT3)
   kPD1, kPD2, kPD3,       // dt*kPX1, dt*kPX2, dt*kPX3
+  kRXLEN, kRYLEN, kRZLEN, // 1/xlen, 1/ylen, 1/zlen           (hdnl1-3 forcing term)
   kNCoef
 };
 
@@ -183,8 +184,6 @@ struct Ctx {
   int tune_by = 8;                        // block height of the explicit-term kernel
   uint64_t tune_gen = 0;
   double* step_host = nullptr;            // pinned: geometry scalars read back at step end
-  double* forc_q = nullptr;               // forc/len per component (fused step, forcing on)
-  bool forc_q_ready = false;
   // remeshing hand-off: the host's remesher and the hand-offs done
   mibm_remesh_fn remesh_fn = nullptr;
   void* remesh_user = nullptr;
@@ -276,7 +275,6 @@ inline void field_host_shape(const Ctx* c, int id, int& ny, int& klo, int& nk) {
 void k_hdnl(Ctx* c, int which, const StepParams* dp);
 void k_invtr_rhs(Ctx* c, int which, const StepParams* dp, double* rhs_out);
 void k_fused_rhs(Ctx* c, const StepParams* dp);
-void k_forcing_quotient(Ctx* c);
 void k_fused_rhs_f32(Ctx* c, const StepParams* dp, float* ru4, float* rhs4);
 void k_updvp_f32(Ctx* c, const StepParams* dp, const float* phi, const double* mean3, bool mirror);
 void k_prcalc_f32(Ctx* c, const StepParams* dp, const float* phi, bool mirror);

@@ -87,6 +87,7 @@ StepParams host_params(Ctx* c) {
   q[kLT1] = alpec * p.dt * g.dx1q; q[kLT2] = alpec * p.dt * g.dx2q; q[kLT3] = alpec * p.dt * g.dx3q;
   q[kLTC] = 2.0 * (q[kLT1] + q[kLT2] + q[kLT3]);
   q[kPD1] = p.dt * q[kPX1]; q[kPD2] = p.dt * q[kPX2]; q[kPD3] = p.dt * q[kPX3];
+  q[kRXLEN] = 1.0 / g.xlen; q[kRYLEN] = 1.0 / g.ylen; q[kRZLEN] = 1.0 / g.zlen;
   for (int i = 0; i < kNCoef; ++i) p.cf[i] = (float)q[i];
   return p;
 }
@@ -267,7 +268,7 @@ void release(Ctx* c) {
   cudaFree(c->xc); cudaFree(c->xm); cudaFree(c->yc); cudaFree(c->ym); cudaFree(c->zc); cudaFree(c->zm);
   cudaFree(c->red); cudaFree(c->dflag); cudaFree(c->dparams); cudaFree(c->rhs4);
   cudaFree(c->ru32); cudaFree(c->rhs32); cudaFree(c->phi32); cudaFree(c->divmax);
-  cudaFree(c->res32); cudaFree(c->q32); cudaFree(c->forc_q);
+  cudaFree(c->res32); cudaFree(c->q32);
   cudaFree(c->tri_coef); cudaFree(c->lag_red);
   if (c->red_host) cudaFreeHost(c->red_host);
   if (c->hflag) cudaFreeHost(c->hflag);

@@ -46,7 +46,6 @@ struct StencilArgs {
   const float* __restrict__ p32;
   // forcx/xlen, forcy/ylen, forcz/zlen (3 fields) formed once per step by
   // the fused step; nullptr elsewhere
-  const double* __restrict__ fq;
   int coff;
   int forcing;
 };
@@ -77,31 +76,45 @@ static StencilArgs make_args(Ctx* c) {
   size_t n = c->g.cells;
   a.u32 = m; a.v32 = m ? m + n : nullptr; a.w32 = m ? m + 2 * n : nullptr;
   a.t32 = m ? m + 3 * n : nullptr; a.p32 = m ? m + 4 * n : nullptr;
-  a.fq = nullptr;
   a.coff = c->coord_off;
   a.forcing = c->I(MIBM_I_FORCING);
   return a;
 }
 
-// The forcing term VOF*forc/len of hdnl1/2/3 (hdnl1.f90:74): where VOF = 1
-// (every fluid cell) it equals forc/len, which the fused step forms once per
-// step (fq); the division stays for the interface cells, so the FP64 value is
-// the reference's bit for bit.
+// NaN or +-Inf, and the max of two non-negative values, on the bit patterns:
+// integer operations instead of FP64 ones (which issue at the FP64 rate)
+__device__ __forceinline__ bool bits_nonfinite(double x) {
+  return ((__double_as_longlong(x) >> 52) & 0x7ff) == 0x7ff;
+}
+__device__ __forceinline__ bool bits_nonfinite(float x) { return ((__float_as_int(x) >> 23) & 0xff) == 0xff; }
+__device__ __forceinline__ double max_nonneg(double a, double b) {
+  return __longlong_as_double(max(__double_as_longlong(a), __double_as_longlong(b)));
+}
+__device__ __forceinline__ float max_nonneg(float a, float b) {
+  return __int_as_float(max(__float_as_int(a), __float_as_int(b)));
+}
+
 // VOF == 1 (a fully fluid cell) tested on the bit pattern: an integer
 // compare instead of an FP64 one (FP64 compares issue at the FP64 rate).
 __device__ __forceinline__ bool vof_is_one(double v) {
   return __double_as_longlong(v) == 0x3FF0000000000000LL;
 }
 
+// The forcing term VOF*forc/len of hdnl1/2/3 (hdnl1.f90:74) added to h, as
+// (VOF*forc)*(1/len) with 1/len formed once on the host: a multiply instead
+// of an FP64 division (a long sequence of FP64 operations), the value within
+// one rounding of the quotient.  In a fluid cell (VOF = 1) it is one FMA, and
+// the precision form converts a single FP64 value there.
 template <typename R>
-__device__ __forceinline__ R forcing_term(const StencilArgs& A, const double* __restrict__ vof,
-                                          const double* __restrict__ forc, int comp, idx_t c0, R len) {
+__device__ __forceinline__ R add_forcing(R h, const double* __restrict__ vof, const double* __restrict__ forc,
+                                         idx_t c0, R rlen) {
+  const double v = vof[c0];
   if constexpr (sizeof(R) == 8) {
-    double v = vof[c0];
-    if (A.fq && vof_is_one(v)) return A.fq[(size_t)comp * A.g.cells + c0];
-    return (v * forc[c0]) / len;
+    if (vof_is_one(v)) return forc[c0] * rlen + h;
+    return (v * forc[c0]) * rlen + h;
   } else {
-    return R(vof[c0]) * R(forc[c0]) / len;
+    if (vof_is_one(v)) return R(forc[c0]) * rlen + h;
+    return R(v * forc[c0]) * rlen + h;
   }
 }
 
@@ -145,7 +158,7 @@ __device__ __forceinline__ R h_x(const StencilArgs& A, idx_t c0, idx_t dip, idx_
   R x13 = (vz[c0 + dkp] + vz[c0 + dim + dkp]) * (vx[c0 + dkp] + vxc) -
           (vz[c0] + vz[c0 + dim]) * (vxc + vx[c0 + dkm]);
   R h = -(udx1 * x11 + udx2 * x12 + udx3 * x13);   // -(h11 + h12 + h13), each h1d = x1d * udx_d
-  if (A.forcing) h = h + forcing_term<R>(A, A.vofx, A.forcx, 0, c0, coef<R>(p, kXLEN));
+  if (A.forcing) h = add_forcing<R>(h, A.vofx, A.forcx, c0, coef<R>(p, kRXLEN));
   return h;
 }
 
@@ -163,7 +176,7 @@ __device__ __forceinline__ R h_y(const StencilArgs& A, idx_t c0, idx_t dip, idx_
   R x23 = (vz[c0 + dkp] + vz[c0 + djm + dkp]) * (vy[c0 + dkp] + vyc) -
           (vz[c0] + vz[c0 + djm]) * (vyc + vy[c0 + dkm]);
   R h = -(udx1 * x21 + udx2 * x22 + udx3 * x23);
-  if (A.forcing) h = h + forcing_term<R>(A, A.vofy, A.forcy, 1, c0, coef<R>(p, kYLEN));
+  if (A.forcing) h = add_forcing<R>(h, A.vofy, A.forcy, c0, coef<R>(p, kRYLEN));
   return h;
 }
 
@@ -185,7 +198,7 @@ __device__ __forceinline__ R h_z(const StencilArgs& A, idx_t c0, idx_t dip, idx_
     R T_interp = (F.t[c0] + F.t[c0 + dkm]) * R(0.5);
     h = h + coef<R>(p, kBETAGZ) * (T_interp - coef<R>(p, kTLIQ));
   }
-  if (A.forcing) h = h + forcing_term<R>(A, A.vofz, A.forcz, 2, c0, coef<R>(p, kZLEN));
+  if (A.forcing) h = add_forcing<R>(h, A.vofz, A.forcz, c0, coef<R>(p, kRZLEN));
   return h;
 }
 
@@ -311,7 +324,6 @@ static void fused_rhs_launch(Ctx* c, const StepParams* dp, int w, R* ru, R* rhs)
   const int by = (c->tune_by == 2 || c->tune_by == 4) ? c->tune_by : 8;   // autotuned block height
   dim3 grid(div_up(c->g.n1m, 32), div_up(c->g.n2m, by), c->g.n3m), block(32, by);
   StencilArgs a = make_args(c);
-  if (c->forc_q_ready) a.fq = c->forc_q;
   switch (w) {
     case 0: fused_rhs_kernel<R, 0><<<grid, block, 0, c->stream>>>(a, dp, ru, rhs); break;
     case 1: fused_rhs_kernel<R, 1><<<grid, block, 0, c->stream>>>(a, dp, ru, rhs); break;
@@ -497,15 +509,12 @@ __global__ void cfl_kernel(StencilArgs A, const double* __restrict__ padx, const
     R vxp = (i + 1 < g.n1m) ? F.u[c0 + 1] : R(padx[j + (size_t)g.n2m * k]);
     R vyp = (j + 1 < g.n2m) ? F.v[c0 + g.P] : R(pady[i + (size_t)g.n1m * k]);
     R vzp = F.w[cidx(g, i, j, (k + 1 == g.n3m) ? 0 : k + 1)];
-    R qcf;
-    if (sizeof(R) == 8)   // FP64 form: the reference's operation order (x*0.5*dx)
-      qcf = fabs((F.u[c0] + vxp) * R(0.5) * R(g.dx1)) + fabs((F.v[c0] + vyp) * R(0.5) * R(g.dx2)) +
-            fabs((F.w[c0] + vzp) * R(0.5) * R(g.dx3));
-    else
-      qcf = fabs((F.u[c0] + vxp) * h1) + fabs((F.v[c0] + vyp) * h2) + fabs((F.w[c0] + vzp) * h3);
-    // fmax drops NaN: a non-finite velocity or temperature raises the guard
-    if (!isfinite(qcf) || !isfinite(F.t[c0])) atomicOr(nonfinite, 1);
-    mr = fmax(mr, qcf);
+    // (x*0.5)*dx of cfl.f90 equals x*(0.5*dx) bit for bit (scaling by 0.5 is
+    // exact), so the FP64 value is the reference's with one multiply less
+    R qcf = fabs((F.u[c0] + vxp) * h1) + fabs((F.v[c0] + vyp) * h2) + fabs((F.w[c0] + vzp) * h3);
+    // a max would drop a NaN: a non-finite velocity or temperature raises the guard
+    if (bits_nonfinite(qcf) || bits_nonfinite(F.t[c0])) atomicOr(nonfinite, 1);
+    mr = max_nonneg(mr, qcf);
   }
   double m = warp_max((double)mr);
   __shared__ double sm[32];
@@ -595,28 +604,6 @@ void k_invtr_rhs(Ctx* c, int which, const StepParams* dp, double* rhs_out) {
                                                                    ru_of(c, which), rhs_out); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "invtr_rhs");
-}
-
-__global__ void forc_quotient_kernel(size_t n, const double* __restrict__ fx, const double* __restrict__ fy,
-                                     const double* __restrict__ fz, double xlen, double ylen, double zlen,
-                                     double* __restrict__ q) {
-  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  q[t] = fx[t] / xlen;
-  q[n + t] = fy[t] / ylen;
-  q[2 * n + t] = fz[t] / zlen;
-}
-
-// forcx/xlen, forcy/ylen, forcz/zlen for the explicit terms of this step
-// (the forcing fields change once per step, before tschem)
-void k_forcing_quotient(Ctx* c) {
-  const size_t n = c->g.cells;
-  { MIBM_PROF(c, "forcing_quotient");
-    forc_quotient_kernel<<<div_up(n, 256), 256, 0, c->stream>>>(n, c->df[MIBM_F_FORCX], c->df[MIBM_F_FORCY],
-                                                               c->df[MIBM_F_FORCZ], c->g.xlen, c->g.ylen,
-                                                               c->g.zlen, c->forc_q); }
-  ++c->launches;
-  if (MIBM_LAUNCH_CHECK(c, "forcing quotient")) c->forc_q_ready = true;
 }
 
 void k_fused_rhs(Ctx* c, const StepParams* dp) {
