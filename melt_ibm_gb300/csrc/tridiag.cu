@@ -369,9 +369,17 @@ int tri_chunk_col(int n) {
 // extended table of (n, M): element arrays a, b, q, s, P, Q, DP at offsets
 // 0, n, .., 6n, element e stored at (e % M) * G + e / M (a warp reads one
 // word per lane, or one broadcast word); then PL (P at each chunk end), QF (Q
-// at each chunk start), DPF (DP at each chunk start), then the four scalars
-// ackl_b, api, ami, 1/den of the base table.
-static size_t ext_len(int n, int m) { return m ? 7 * (size_t)n + 3 * (size_t)(n / m) + 4 : 0; }
+// at each chunk start), DPF (DP at each chunk start), the four scalars
+// ackl_b, api, ami, 1/den of the base table, and the chunk coefficients AC,
+// BC (G each) of the one-pass correction:
+//   x_e = D_e + DP'_e (y_in + AC_h xn) + Q'_e (f_in + BC_h xn).
+// The periodic correction s (tridiag_periodic.f90:47-49) obeys the
+// homogeneous recurrences inside a chunk that holds none of its two source
+// rows, so there s = AC_h DP + BC_h Q with AC_h the forward-only value of s
+// before the chunk and BC_h the final s after it; the first chunk (y_in = 0)
+// keeps s in its DP' slots (AC = 1, BC = 0) and the last (f_in = 0) in its Q'
+// slots (AC = 0, BC = 1).  Two FMAs per element instead of three.
+static size_t ext_len(int n, int m) { return m ? 7 * (size_t)n + 5 * (size_t)(n / m) + 4 : 0; }
 
 static void build_ext(const std::vector<double>& t, int n, int m, double* out) {
   int G = n / m;
@@ -386,8 +394,17 @@ static void build_ext(const std::vector<double>& t, int n, int m, double* out) {
     out[2 * (size_t)n + pos(e)] = q[e];
     out[3 * (size_t)n + pos(e)] = s[e];
   }
+  // forward-only part of s (the first loop of tridiag_periodic's s)
+  std::vector<double> sf(n);
+  sf[0] = -t[4 * (size_t)n + 2];
+  for (int e = 1; e < n; ++e) sf[e] = -t[n + e] * sf[e - 1];
+  double* AC = out + 7 * (size_t)n + 3 * G + 4;
+  double* BC = AC + G;
   for (int h = 0; h < G; ++h) {
     int st = h * m, en = st + m - 1;
+    if (h == 0) { AC[h] = 1.0; BC[h] = 0.0; }
+    else if (h == G - 1) { AC[h] = 0.0; BC[h] = 1.0; }
+    else { AC[h] = sf[st - 1]; BC[h] = s[en + 1]; }
     double pv = 1.0;
     for (int e = st; e <= en; ++e) { pv = -b[e] * pv; P[e] = pv; out[4 * (size_t)n + pos(e)] = pv; }
     out[7 * (size_t)n + h] = pv;
@@ -395,8 +412,8 @@ static void build_ext(const std::vector<double>& t, int n, int m, double* out) {
     for (int e = en; e >= st; --e) {
       qv = q[e] * qv;
       dv = P[e] + q[e] * dv;
-      out[5 * (size_t)n + pos(e)] = qv;
-      out[6 * (size_t)n + pos(e)] = dv;
+      out[5 * (size_t)n + pos(e)] = (h == G - 1 && G > 1) ? s[e] : qv;
+      out[6 * (size_t)n + pos(e)] = h == 0 ? s[e] : dv;
     }
     out[7 * (size_t)n + G + h] = qv;
     out[7 * (size_t)n + 2 * G + h] = dv;
@@ -452,8 +469,8 @@ static void fill_slot(int n, int m, double betadx, double* out) {
   if (m) build_ext(t, n, m, out + L.off_ext);
 }
 
-// slot length for lines up to nmax and any chunk (ext_len <= 7n + 3*32 + 4)
-static size_t slot_len(int nmax) { return 4 * (size_t)nmax + 4 + 7 * (size_t)nmax + 3 * 32 + 4; }
+// slot length for lines up to nmax and any chunk (ext_len <= 7n + 5*32 + 4)
+static size_t slot_len(int nmax) { return 4 * (size_t)nmax + 4 + 7 * (size_t)nmax + 5 * 32 + 4; }
 
 template <typename V, int M>
 __device__ __forceinline__ void load_chunk(const V* __restrict__ p, V (&r)[M]) {
@@ -544,19 +561,22 @@ __global__ void __launch_bounds__(256) solve_xc_kernel(Grid g, V* __restrict__ r
   }
   V f_in = __shfl_down_sync(FULL, Uv, 1, GP);
   if (hl + 1 >= G) f_in = V(0);
+  // periodic closure from the reduced solution at element 0 (first chunk,
+  // y_in = 0) and element n-2 (last chunk, f_in = 0), then the one-pass
+  // correction (build_ext)
+  const V* S = X + 7 * n + 3 * G;
+  const V x0 = r[0] + X[5 * n + h] * f_in;
+  const V xm = r[M - 2] + X[6 * n + (M - 2) * G + h] * y_in;
+  V f1 = __shfl_sync(FULL, x0, 0, GP);
+  V fnm1 = __shfl_sync(FULL, xm, G - 1, GP);
+  V rn = __shfl_sync(FULL, rlast, G - 1, GP);
+  V xn = (rn * S[0] - S[1] * f1 - S[2] * fnm1) * S[3];
+  const V al = y_in + S[4 + h] * xn, be = f_in + S[4 + G + h] * xn;
 #pragma unroll
   for (int i = 0; i < M; ++i) {
     int t = i * G + h;
-    r[i] = r[i] + X[6 * n + t] * y_in + X[5 * n + t] * f_in;
+    r[i] = r[i] + X[6 * n + t] * al + X[5 * n + t] * be;
   }
-  // periodic closure
-  const V* S = X + 7 * n + 3 * G;
-  V f1 = __shfl_sync(FULL, r[0], 0, GP);
-  V fnm1 = __shfl_sync(FULL, r[M - 2], G - 1, GP);
-  V rn = __shfl_sync(FULL, rlast, G - 1, GP);
-  V xn = (rn * S[0] - S[1] * f1 - S[2] * fnm1) * S[3];
-#pragma unroll
-  for (int i = 0; i < M; ++i) r[i] = xn * X[3 * n + i * G + h] + r[i];
   if (act) store_chunk<V, M>(row, r);
 }
 
@@ -612,20 +632,20 @@ __global__ void __launch_bounds__(32 * col_max_chunks(M)) solve_cc_kernel(Grid g
   __syncthreads();
   V f_in = V(0);
   for (int hh = G - 1; hh > w; --hh) f_in = sU[hh][lane] + X[7 * n + G + hh] * f_in;
-#pragma unroll
-  for (int i = 0; i < M; ++i) {
-    int t = i * G + w;
-    r[i] = r[i] + X[6 * n + t] * y_in + X[5 * n + t] * f_in;
-  }
-  if (w == 0) sF[0][lane] = r[0];
-  if (w == G - 1) { sF[1][lane] = r[M - 2]; sF[2][lane] = rlast; }
+  // periodic closure from the reduced solution at element 0 (first chunk,
+  // y_in = 0) and element n-2 (last chunk, f_in = 0), then the one-pass
+  // correction (build_ext)
+  if (w == 0) sF[0][lane] = r[0] + X[5 * n + w] * f_in;
+  if (w == G - 1) { sF[1][lane] = r[M - 2] + X[6 * n + (M - 2) * G + w] * y_in; sF[2][lane] = rlast; }
   __syncthreads();
   const V* S = X + 7 * n + 3 * G;
   V xn = (sF[2][lane] * S[0] - S[1] * sF[0][lane] - S[2] * sF[1][lane]) * S[3];
   if (!act) return;
+  const V al = y_in + S[4 + w] * xn, be = f_in + S[4 + G + w] * xn;
 #pragma unroll
   for (int i = 0; i < M; ++i) {
-    V xv = xn * X[3 * n + i * G + w] + r[i];
+    const int t = i * G + w;
+    V xv = r[i] + X[6 * n + t] * al + X[5 * n + t] * be;
     int o = i * stride;
     if (ZL) {
       if (write_rhs) rp[o] = xv;
