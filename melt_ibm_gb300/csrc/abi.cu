@@ -72,6 +72,7 @@ static bool ensure_f32(Ctx* c) {
     if (!cuda_ok(c, cudaMalloc(&c->phi32, g.cells * sizeof(float)), "phi32")) return false;
     if (!cuda_ok(c, cudaMalloc(&c->res32, g.cells * sizeof(float)), "res32")) return false;
     if (!cuda_ok(c, cudaMalloc(&c->q32, 5 * g.cells * sizeof(float)), "q32")) return false;
+    if (!cuda_ok(c, cudaMalloc(&c->prod32, 6 * g.cells * sizeof(float)), "prod32")) return false;
     for (int q = 0; q < 4; ++q) k_cast_d2f(c, g.cells, c->df[kRuFields[q]], c->ru32 + (size_t)q * g.cells);
     c->q32_valid = false;
   }
@@ -130,6 +131,8 @@ static bool step_prepare(Ctx* c) {
   } else {
     c->q32_valid = false;
     if (!c->rhs4 && !cuda_ok(c, cudaMalloc(&c->rhs4, 4 * g.cells * sizeof(double)), "rhs4")) return false;
+    if (!c->prod && !cuda_ok(c, cudaMalloc(&c->prod, 6 * g.cells * sizeof(double)), "advection products"))
+      return false;
   }
   if (!tri_step_fill(c, bd, f32)) return false;
   if (!fft_prepare(c, false) || (f32 && !fft_prepare(c, true))) return false;

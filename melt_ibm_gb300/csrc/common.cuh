@@ -154,6 +154,8 @@ struct Ctx {
   StepParams* dparams = nullptr;          // [3] device copies (one per substep)
   StepParams* hparams = nullptr;          // pinned
   double* rhs4 = nullptr;                 // 4 RHS fields for the fused path
+  double* prod = nullptr;                 // 6 advection products (fused FP64 path)
+  float* prod32 = nullptr;                // the same in the precision form
   // precision form (FP32 compute, FP64 fields, refined projection)
   int precision = 0;                      // 0 = plain FP64, 1 = FP32 + refinement
   int nproj = 2;                          // Poisson solves per substep in precision form

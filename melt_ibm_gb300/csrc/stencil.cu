@@ -44,8 +44,10 @@ struct StencilArgs {
   const float* __restrict__ w32;
   const float* __restrict__ t32;
   const float* __restrict__ p32;
-  // forcx/xlen, forcy/ylen, forcz/zlen (3 fields) formed once per step by
-  // the fused step; nullptr elsewhere
+  // advection products of the fused step (6 fields, adv_products_kernel) in
+  // the FP64 form and in the precision form
+  const double* __restrict__ prod;
+  const float* __restrict__ prod32;
   int coff;
   int forcing;
 };
@@ -54,14 +56,14 @@ struct StencilArgs {
 // FP64 fields themselves, or their FP32 mirrors in the precision form
 template <typename R>
 struct Prog {
-  const R* u; const R* v; const R* w; const R* t; const R* p;
+  const R* u; const R* v; const R* w; const R* t; const R* p; const R* pd;
 };
 template <typename R> __device__ __forceinline__ Prog<R> prog(const StencilArgs& A);
 template <> __device__ __forceinline__ Prog<double> prog<double>(const StencilArgs& A) {
-  return Prog<double>{A.vx, A.vy, A.vz, A.temp, A.pr};
+  return Prog<double>{A.vx, A.vy, A.vz, A.temp, A.pr, A.prod};
 }
 template <> __device__ __forceinline__ Prog<float> prog<float>(const StencilArgs& A) {
-  return Prog<float>{A.u32, A.v32, A.w32, A.t32, A.p32};
+  return Prog<float>{A.u32, A.v32, A.w32, A.t32, A.p32, A.prod32};
 }
 
 static StencilArgs make_args(Ctx* c) {
@@ -76,6 +78,7 @@ static StencilArgs make_args(Ctx* c) {
   size_t n = c->g.cells;
   a.u32 = m; a.v32 = m ? m + n : nullptr; a.w32 = m ? m + 2 * n : nullptr;
   a.t32 = m ? m + 3 * n : nullptr; a.p32 = m ? m + 4 * n : nullptr;
+  a.prod = c->prod; a.prod32 = c->prod32;
   a.coff = c->coord_off;
   a.forcing = c->I(MIBM_I_FORCING);
   return a;
@@ -202,6 +205,62 @@ __device__ __forceinline__ R h_z(const StencilArgs& A, idx_t c0, idx_t dip, idx_
   return h;
 }
 
+// ---------------------------------------------------------------------
+// The advection terms of hdnl1-3 are differences of products at cell faces
+// and edges that neighbouring cells and the three momentum components share:
+//   h11 = Pc - Pc[i-1], h12 = E[j+1] - E, h13 = F[k+1] - F,
+//   h21 = E[i+1] - E,   h22 = Qc - Qc[j-1], h23 = H[k+1] - H,
+//   h31 = F[i+1] - F,   h32 = H[j+1] - H,   h33 = Rc - Rc[k-1]
+// with, at cell (i,j,k),
+//   Pc = (u[i+1]+u)^2, Qc = (v[j+1]+v)^2, Rc = (w[k+1]+w)^2,
+//   E = (v+v[i-1]) (u+u[j-1]), F = (w+w[i-1]) (u+u[k-1]), H = (w+w[j-1]) (v+v[k-1])
+// (hdnl1.f90:40-72, hdnl2.f90:40-73, hdnl3.f90:40-80 regrouped).  The fused
+// step forms the six products once per cell (15 FP64 operations) instead of
+// inside each component's stencil (39 for the three), the same values up to
+// the rounding of the products.
+// ---------------------------------------------------------------------
+template <typename R>
+__global__ void adv_products_kernel(StencilArgs A, R* __restrict__ out) {
+  CELL_INDEX
+  const Prog<R> F = prog<R>(A);
+  const R* u = F.u; const R* v = F.v; const R* w = F.w;
+  const size_t n = g.cells;
+  const R uc = u[c0], vc = v[c0], wc = w[c0];
+  const R a = u[c0 + dip] + uc, b = v[c0 + djp] + vc, d = w[c0 + dkp] + wc;
+  out[c0] = a * a;
+  out[n + c0] = b * b;
+  out[2 * n + c0] = d * d;
+  out[3 * n + c0] = (vc + v[c0 + dim]) * (uc + u[c0 + djm]);
+  out[4 * n + c0] = (wc + w[c0 + dim]) * (uc + u[c0 + dkm]);
+  out[5 * n + c0] = (wc + w[c0 + djm]) * (vc + v[c0 + dkm]);
+}
+
+template <typename R>
+__device__ __forceinline__ R h_prod(const StencilArgs& A, int W, idx_t c0, idx_t dip, idx_t dim, idx_t djp,
+                                    idx_t djm, idx_t dkp, idx_t dkm, const StepParams& p) {
+  const Prog<R> F = prog<R>(A);
+  const size_t n = A.g.cells;
+  const R* Pc = F.pd; const R* Qc = F.pd + n; const R* Rc = F.pd + 2 * n;
+  const R* E = F.pd + 3 * n; const R* Fx = F.pd + 4 * n; const R* H = F.pd + 5 * n;
+  const R udx1 = coef<R>(p, kQ1), udx2 = coef<R>(p, kQ2), udx3 = coef<R>(p, kQ3);
+  R h;
+  if (W == 0) {
+    h = -(udx1 * (Pc[c0] - Pc[c0 + dim]) + udx2 * (E[c0 + djp] - E[c0]) + udx3 * (Fx[c0 + dkp] - Fx[c0]));
+    if (A.forcing) h = add_forcing<R>(h, A.vofx, A.forcx, c0, coef<R>(p, kRXLEN));
+  } else if (W == 1) {
+    h = -(udx1 * (E[c0 + dip] - E[c0]) + udx2 * (Qc[c0] - Qc[c0 + djm]) + udx3 * (H[c0 + dkp] - H[c0]));
+    if (A.forcing) h = add_forcing<R>(h, A.vofy, A.forcy, c0, coef<R>(p, kRYLEN));
+  } else {
+    h = -(udx1 * (Fx[c0 + dip] - Fx[c0]) + udx2 * (H[c0 + djp] - H[c0]) + udx3 * (Rc[c0] - Rc[c0 + dkm]));
+    if (p.betagz != 0.0) {
+      R T_interp = (F.t[c0] + F.t[c0 + dkm]) * R(0.5);
+      h = h + coef<R>(p, kBETAGZ) * (T_interp - coef<R>(p, kTLIQ));
+    }
+    if (A.forcing) h = add_forcing<R>(h, A.vofz, A.forcz, c0, coef<R>(p, kRZLEN));
+  }
+  return h;
+}
+
 __device__ __forceinline__ double nint_d(double x) { return round(x); }   // Fortran NINT semantics
 
 template <typename R>
@@ -311,9 +370,7 @@ fused_rhs_kernel(StencilArgs A, const StepParams* __restrict__ pp, R* __restrict
   CELL_INDEX
   const StepParams& p = *pp;
   R h;
-  if (W == 0) h = h_x<R>(A, c0, dip, dim, djp, djm, dkp, dkm, p);
-  else if (W == 1) h = h_y<R>(A, c0, dip, dim, djp, djm, dkp, dkm, p);
-  else if (W == 2) h = h_z<R>(A, c0, dip, dim, djp, djm, dkp, dkm, p);
+  if (W < 3) h = h_prod<R>(A, W, c0, dip, dim, djp, djm, dkp, dkm, p);    // products of adv_products_kernel
   else h = h_t<R>(A, i, j, k, c0, dip, dim, djp, djm, dkp, dkm, p);
   rhs[c0] = rhs_value<R>(A, W, h, ru[c0], c0, dip, dim, djp, djm, dkp, dkm, p);
   ru[c0] = h;
@@ -606,7 +663,15 @@ void k_invtr_rhs(Ctx* c, int which, const StepParams* dp, double* rhs_out) {
   MIBM_LAUNCH_CHECK(c, "invtr_rhs");
 }
 
+template <typename R>
+static void adv_products_launch(Ctx* c, R* out) {
+  { MIBM_PROF(c, sizeof(R) == 8 ? "adv_products" : "adv_products_f32");
+    adv_products_kernel<R><<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), out); }
+  ++c->launches;
+}
+
 void k_fused_rhs(Ctx* c, const StepParams* dp) {
+  adv_products_launch<double>(c, c->prod);
   for (int w = 0; w < 4; ++w) {
     { MIBM_PROF(c, "fused_rhs");
       fused_rhs_launch<double>(c, dp, w, ru_of(c, w), c->rhs4 + (size_t)w * c->g.cells); }
@@ -631,6 +696,8 @@ static float time_fused_by(Ctx* c, const StepParams* dp, int by, int reps, R* ru
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
+  if (sizeof(R) == 8) adv_products_launch<double>(c, c->prod);   // read by the u component
+  else adv_products_launch<float>(c, c->prod32);
   auto run = [&]() {
     fused_rhs_launch<R>(c, dp, 0, ru_fields[0], rhs4);
     fused_rhs_launch<R>(c, dp, 3, ru_fields[3], rhs4 + 3 * n);
@@ -670,6 +737,7 @@ float stencil_time_by(Ctx* c, const StepParams* dp, int by, int reps) {
 
 // precision form: FP32 explicit terms and RHS into FP32 ru / rhs buffers
 void k_fused_rhs_f32(Ctx* c, const StepParams* dp, float* ru4, float* rhs4) {
+  adv_products_launch<float>(c, c->prod32);
   for (int w = 0; w < 4; ++w) {
     { MIBM_PROF(c, "fused_rhs_f32");
       fused_rhs_launch<float>(c, dp, w, ru4 + (size_t)w * c->g.cells, rhs4 + (size_t)w * c->g.cells); }
