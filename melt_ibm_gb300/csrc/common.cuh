@@ -47,6 +47,7 @@ enum Coef {
   kLT1, kLT2, kLT3, kLTC, // al/pec*dt*dxq, 2*(kLT1+kLT2+kLT3)
   kPD1, kPD2, kPD3,       // dt*kPX1, dt*kPX2, dt*kPX3
   kRXLEN, kRYLEN, kRZLEN, // 1/xlen, 1/ylen, 1/zlen           (hdnl1-3 forcing term)
+  kPB1, kPB2, kPB3, kPBC, // al*beta*dxq per direction, 1 + 2*(kPB1+kPB2+kPB3)  (prcalc)
   kNCoef
 };
 

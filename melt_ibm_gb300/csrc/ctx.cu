@@ -88,6 +88,8 @@ StepParams host_params(Ctx* c) {
   q[kLTC] = 2.0 * (q[kLT1] + q[kLT2] + q[kLT3]);
   q[kPD1] = p.dt * q[kPX1]; q[kPD2] = p.dt * q[kPX2]; q[kPD3] = p.dt * q[kPX3];
   q[kRXLEN] = 1.0 / g.xlen; q[kRYLEN] = 1.0 / g.ylen; q[kRZLEN] = 1.0 / g.zlen;
+  q[kPB1] = q[kBE] * g.dx1q; q[kPB2] = q[kBE] * g.dx2q; q[kPB3] = q[kBE] * g.dx3q;
+  q[kPBC] = 1.0 + 2.0 * (q[kPB1] + q[kPB2] + q[kPB3]);
   for (int i = 0; i < kNCoef; ++i) p.cf[i] = (float)q[i];
   return p;
 }

@@ -491,11 +491,13 @@ __global__ void divmax_kernel(StencilArgs A, unsigned long long* __restrict__ ou
 __global__ void prcalc_kernel(StencilArgs A, const StepParams* __restrict__ pp, const double* __restrict__ dph,
                               double* __restrict__ pr) {
   CELL_INDEX
-  double be = pp->cd[kBE];
-  double d = dph[c0];
-  pr[c0] = pr[c0] + d - be * ((dph[c0 + dip] - 2.0 * d + dph[c0 + dim]) * g.dx1q +
-                              (dph[c0 + djp] - 2.0 * d + dph[c0 + djm]) * g.dx2q +
-                              (dph[c0 + dkp] - 2.0 * d + dph[c0 + dkm]) * g.dx3q);
+  // p + phi - al*beta*lap(phi) (prcalc.f90:17-33) as
+  // p + (1 + 2 al beta sum dxq) phi - sum (al beta dxq)(phi[+] + phi[-]):
+  // the coefficients formed on the host, 8 FP64 operations instead of 14
+  const double d = dph[c0];
+  const double t = pp->cd[kPB1] * (dph[c0 + dip] + dph[c0 + dim]) + pp->cd[kPB2] * (dph[c0 + djp] + dph[c0 + djm]) +
+                   pp->cd[kPB3] * (dph[c0 + dkp] + dph[c0 + dkm]);
+  pr[c0] = (pr[c0] + pp->cd[kPBC] * d) - t;
 }
 
 __global__ void add_kernel(Grid g, double* __restrict__ q, const double* __restrict__ r) {
