@@ -792,26 +792,41 @@ __device__ bool probe_grad_sep(const LagArgs& A, const double pos[3], int pi1, i
   moment_matrix(S[0], S[1], S[2], Ai);
   if (!inv4(Ai)) return false;
   const double gam[4] = {Ai[0], Ai[1], Ai[2], Ai[3]};     // A^{-1} p(x0), p(x0) = e0
-  // sums over the cage of the field times the weighted basis: MT (weights),
-  // MD[d] (derivative of the weights along d)
+  // sums over the cage of the field times the weighted basis p = (1, d0, d1,
+  // d2): MT (weights), MD[d] (derivative of the weights along d).  Weights
+  // and basis factor by axis, so the sums are contracted one axis at a time
+  // (x, then y, then z): about 250 FP64 operations instead of 675.
+  double wd[3][3], dwd[3][3];
+  for (int a = 0; a < 3; ++a)
+    for (int r = 0; r < 3; ++r) { wd[a][r] = w[a][r] * dd[a][r]; dwd[a][r] = dw[a][r] * dd[a][r]; }
   double MT[4] = {0, 0, 0, 0}, MD[3][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}};
-  for (int kk = 0; kk < 3; ++kk)
+  for (int kk = 0; kk < 3; ++kk) {
+    const int kk_ = wrap(keul[kk] - 1, g.n3m);
+    // y sums of the x sums A = sum w0 q, B = sum w0 d0 q, C = sum dw0 q, D = sum dw0 d0 q
+    double SA = 0, SAd = 0, SAw = 0, SAwd = 0, SB = 0, SBw = 0, SC = 0, SCd = 0, SD = 0;
     for (int jj = 0; jj < 3; ++jj) {
-      int jj_ = fmod_pos(pi2 - 1 + jj - 1, g.n2m), kk_ = wrap(keul[kk] - 1, g.n3m);
-      double wyz = w[1][jj] * w[2][kk], dyz = dw[1][jj] * w[2][kk], ydz = w[1][jj] * dw[2][kk];
+      const int jj_ = fmod_pos(pi2 - 1 + jj - 1, g.n2m);
+      double qa = 0, qb = 0, qc = 0, qd = 0;
       for (int ii = 0; ii < 3; ++ii) {
-        int ii_ = fmod_pos(pi1 - 1 + ii - 1, g.n1m);
-        double T = q[cidx(g, ii_, jj_, kk_)];
-        double pb[4] = {1.0, dd[0][ii], dd[1][jj], dd[2][kk]};
-        double a0 = w[0][ii] * wyz * T, a1 = dw[0][ii] * wyz * T, a2 = w[0][ii] * dyz * T, a3 = w[0][ii] * ydz * T;
-        for (int r = 0; r < 4; ++r) {
-          MT[r] = fma(a0, pb[r], MT[r]);
-          MD[0][r] = fma(a1, pb[r], MD[0][r]);
-          MD[1][r] = fma(a2, pb[r], MD[1][r]);
-          MD[2][r] = fma(a3, pb[r], MD[2][r]);
-        }
+        const double T = q[cidx(g, fmod_pos(pi1 - 1 + ii - 1, g.n1m), jj_, kk_)];
+        qa = fma(w[0][ii], T, qa); qb = fma(wd[0][ii], T, qb);
+        qc = fma(dw[0][ii], T, qc); qd = fma(dwd[0][ii], T, qd);
       }
+      SA = fma(w[1][jj], qa, SA); SAd = fma(wd[1][jj], qa, SAd);
+      SAw = fma(dw[1][jj], qa, SAw); SAwd = fma(dwd[1][jj], qa, SAwd);
+      SB = fma(w[1][jj], qb, SB); SBw = fma(dw[1][jj], qb, SBw);
+      SC = fma(w[1][jj], qc, SC); SCd = fma(wd[1][jj], qc, SCd);
+      SD = fma(w[1][jj], qd, SD);
     }
+    const double z = w[2][kk], zd = wd[2][kk], dz = dw[2][kk], dzd = dwd[2][kk];
+    MT[0] = fma(z, SA, MT[0]); MT[1] = fma(z, SB, MT[1]); MT[2] = fma(z, SAd, MT[2]); MT[3] = fma(zd, SA, MT[3]);
+    MD[0][0] = fma(z, SC, MD[0][0]); MD[0][1] = fma(z, SD, MD[0][1]);
+    MD[0][2] = fma(z, SCd, MD[0][2]); MD[0][3] = fma(zd, SC, MD[0][3]);
+    MD[1][0] = fma(z, SAw, MD[1][0]); MD[1][1] = fma(z, SBw, MD[1][1]);
+    MD[1][2] = fma(z, SAwd, MD[1][2]); MD[1][3] = fma(zd, SAw, MD[1][3]);
+    MD[2][0] = fma(dz, SA, MD[2][0]); MD[2][1] = fma(dz, SB, MD[2][1]);
+    MD[2][2] = fma(dz, SAd, MD[2][2]); MD[2][3] = fma(dzd, SA, MD[2][3]);
+  }
   for (int d = 0; d < 3; ++d) {
     double dA[16];
     double X[3], Y[3], Z[3];
@@ -861,18 +876,24 @@ __device__ bool probe_value_sep(const LagArgs& A, const double pos[3], int i0, i
   double Ai[16];
   moment_matrix(S[0], S[1], S[2], Ai);
   if (!inv4(Ai)) return false;
+  // sum over the cage of q w p, contracted one axis at a time (as in
+  // probe_grad_sep)
   double MT[4] = {0, 0, 0, 0};
-  for (int kk = 0; kk < 3; ++kk)
+  for (int kk = 0; kk < 3; ++kk) {
+    const int kk_ = wrap(k1w - 1 + kk - 1, g.n3m);
+    double SA = 0, SAd = 0, SB = 0;
     for (int jj = 0; jj < 3; ++jj) {
-      int jj_ = fmod_pos(j0 - 1 + jj - 1, g.n2m), kk_ = wrap(k1w - 1 + kk - 1, g.n3m);
-      double wyz = w[1][jj] * w[2][kk];
+      const int jj_ = fmod_pos(j0 - 1 + jj - 1, g.n2m);
+      double qa = 0, qb = 0;
       for (int ii = 0; ii < 3; ++ii) {
-        int ii_ = fmod_pos(i0 - 1 + ii - 1, g.n1m);
-        double a0 = w[0][ii] * wyz * q[cidx(g, ii_, jj_, kk_)];
-        double pb[4] = {1.0, dd[0][ii], dd[1][jj], dd[2][kk]};
-        for (int r = 0; r < 4; ++r) MT[r] = fma(a0, pb[r], MT[r]);
+        const double T = q[cidx(g, fmod_pos(i0 - 1 + ii - 1, g.n1m), jj_, kk_)];
+        qa = fma(w[0][ii], T, qa); qb = fma(w[0][ii] * dd[0][ii], T, qb);
       }
+      SA = fma(w[1][jj], qa, SA); SAd = fma(w[1][jj] * dd[1][jj], qa, SAd); SB = fma(w[1][jj], qb, SB);
     }
+    MT[0] = fma(w[2][kk], SA, MT[0]); MT[1] = fma(w[2][kk], SB, MT[1]);
+    MT[2] = fma(w[2][kk], SAd, MT[2]); MT[3] = fma(w[2][kk] * dd[2][kk], SA, MT[3]);
+  }
   double v = 0;
   for (int r = 0; r < 4; ++r) v = fma(Ai[r], MT[r], v);
   val = v;
