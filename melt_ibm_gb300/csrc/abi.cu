@@ -170,14 +170,20 @@ static void step_enqueue_f32(Ctx* c) {
     if (!c->prologue_done) lagr_substep_prologue(c, ns);
     c->prologue_done = false;
     k_fused_rhs_f32(c, dp, c->ru32, c->rhs32);
-    for (int q = 0; q < 4; ++q) {
-      if (q == 3) lagr_loads_early(c, dp);   // u, v, w solved: loads beside the T solves
-      int f = (q < 3) ? 0 : 1;
-      const float* T = tf + (size_t)((ns * 2 + f) * 3) * tlen;
-      float* r = c->rhs32 + (size_t)q * g.cells;
-      k_solve_x_f32(c, r, T);
-      k_solve_y_f32(c, r, T + tlen);
-      k_solve_z_f32(c, r, T + 2 * tlen, c->df[kStepFid[q]], q == 3 ? t_mirror : nullptr);
+    {
+      // u, v, w: one launch per direction (they share the velocity tables)
+      const float* Tv = tf + (size_t)((ns * 2 + 0) * 3) * tlen;
+      double* qv[3] = {c->df[kStepFid[0]], c->df[kStepFid[1]], c->df[kStepFid[2]]};
+      k_solve_x_f32(c, c->rhs32, Tv, 3);
+      k_solve_y_f32(c, c->rhs32, Tv + tlen, 3);
+      k_solve_z_f32(c, c->rhs32, Tv + 2 * tlen, qv, 3, nullptr);
+      lagr_loads_early(c, dp);                  // u, v, w solved: loads beside the T solves
+      const float* Tt = tf + (size_t)((ns * 2 + 1) * 3) * tlen;
+      float* r = c->rhs32 + 3 * g.cells;
+      double* qt[1] = {c->df[kStepFid[3]]};
+      k_solve_x_f32(c, r, Tt, 1);
+      k_solve_y_f32(c, r, Tt + tlen, 1);
+      k_solve_z_f32(c, r, Tt + 2 * tlen, qt, 1, t_mirror);
     }
     const double* mean3 = lagr_particle_fused(c, dp, t_mirror, ns < 2 ? c->dparams + ns + 1 : nullptr, ns + 1);
     if (c->status != MIBM_OK) return;
@@ -203,14 +209,20 @@ static void step_enqueue_f64(Ctx* c) {
     if (!c->prologue_done) lagr_substep_prologue(c, ns);
     c->prologue_done = false;
     k_fused_rhs(c, dp);
-    for (int q = 0; q < 4; ++q) {
-      if (q == 3) lagr_loads_early(c, dp);   // u, v, w solved: loads beside the T solves
-      int f = (q < 3) ? 0 : 1;
-      const double* T = tables + (size_t)((ns * 2 + f) * 3) * tlen;
-      double* r = c->rhs4 + (size_t)q * g.cells;
-      k_solve_x_T(c, r, T);
-      k_solve_y_T(c, r, T + tlen);
-      k_solve_z_T(c, r, T + 2 * tlen, c->df[kStepFid[q]], 0);
+    {
+      // u, v, w: one launch per direction (they share the velocity tables)
+      const double* Tv = tables + (size_t)((ns * 2 + 0) * 3) * tlen;
+      double* qv[3] = {c->df[kStepFid[0]], c->df[kStepFid[1]], c->df[kStepFid[2]]};
+      k_solve_x_T(c, c->rhs4, Tv, 3);
+      k_solve_y_T(c, c->rhs4, Tv + tlen, 3);
+      k_solve_z_T(c, c->rhs4, Tv + 2 * tlen, qv, 3, 0);
+      lagr_loads_early(c, dp);                  // u, v, w solved: loads beside the T solves
+      const double* Tt = tables + (size_t)((ns * 2 + 1) * 3) * tlen;
+      double* r = c->rhs4 + 3 * g.cells;
+      double* qt[1] = {c->df[kStepFid[3]]};
+      k_solve_x_T(c, r, Tt, 1);
+      k_solve_y_T(c, r, Tt + tlen, 1);
+      k_solve_z_T(c, r, Tt + 2 * tlen, qt, 1, 0);
     }
     const double* mean3 = lagr_particle_fused(c, dp, nullptr, ns < 2 ? c->dparams + ns + 1 : nullptr, ns + 1);
     if (c->status != MIBM_OK) return;

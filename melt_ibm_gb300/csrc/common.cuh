@@ -325,14 +325,14 @@ void k_tempforce_apply(Ctx* c);
 void k_solve_x(Ctx* c, double* rhs, double betadx);
 void k_solve_y(Ctx* c, double* rhs, double betadx);
 void k_solve_z(Ctx* c, double* rhs, double betadx, double* q);
-void k_solve_x_T(Ctx* c, double* rhs, const double* T);
-void k_solve_y_T(Ctx* c, double* rhs, const double* T);
-void k_solve_z_T(Ctx* c, double* rhs, const double* T, double* q, int write_rhs);
+void k_solve_x_T(Ctx* c, double* rhs, const double* T, int nfield);
+void k_solve_y_T(Ctx* c, double* rhs, const double* T, int nfield);
+void k_solve_z_T(Ctx* c, double* rhs, const double* T, double* const* q, int nfield, int write_rhs);
 bool tri_step_fill(Ctx* c, const double betadx[3][2][3], bool f32);
 const double* tri_step_enqueue(Ctx* c, bool f32, int* len_out, const float** f32_out);
-void k_solve_x_f32(Ctx* c, float* rhs, const float* T);
-void k_solve_y_f32(Ctx* c, float* rhs, const float* T);
-void k_solve_z_f32(Ctx* c, float* rhs, const float* T, double* q, float* mirror);
+void k_solve_x_f32(Ctx* c, float* rhs, const float* T, int nfield);
+void k_solve_y_f32(Ctx* c, float* rhs, const float* T, int nfield);
+void k_solve_z_f32(Ctx* c, float* rhs, const float* T, double* const* q, int nfield, float* mirror);
 // fft.cu
 void k_phcalc(Ctx* c);
 void k_phcalc_f32(Ctx* c, const float* src, float* phi);

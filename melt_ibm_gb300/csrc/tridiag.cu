@@ -511,17 +511,19 @@ __device__ __forceinline__ void store_chunk(V* __restrict__ p, const V (&r)[M]) 
 // lanes, lane h < G of it holding cells [h*M, h*M + M); a warp solves 32/GP
 // lines.  Rows start on 16-byte boundaries (pitch multiple of 4).
 template <typename V, int M>
-__global__ void __launch_bounds__(256) solve_xc_kernel(Grid g, V* __restrict__ rhs, const V* __restrict__ X) {
+__global__ void __launch_bounds__(256) solve_xc_kernel(Grid g, V* __restrict__ rhs, const V* __restrict__ X,
+                                                       int nfield) {
   const unsigned FULL = 0xffffffffu;
   const int n = g.n1m, G = n / M, GP = line_lanes(G), LPW = 32 / GP;
   const int lane = threadIdx.x & 31, hl = lane % GP;
   const int warp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lines = g.n2m * g.n3m;
+  const int per = g.n2m * g.n3m, lines = per * nfield;   // nfield fields at stride cells
   if (warp * LPW >= lines) return;                   // whole warp
   const int line = warp * LPW + lane / GP;
   const bool act = line < lines && hl < G;
-  const int j = line % g.n2m, k = line / g.n2m;
-  V* row = act ? rhs + cidx(g, 0, j, k) + (size_t)hl * M : rhs;
+  const int f = line / per, l = line - f * per;
+  const int j = l % g.n2m, k = l / g.n2m;
+  V* row = act ? rhs + (size_t)f * g.cells + cidx(g, 0, j, k) + (size_t)hl * M : rhs;
   V r[M];
   if (act) load_chunk<V, M>(row, r);
   else {
@@ -584,9 +586,11 @@ __global__ void __launch_bounds__(256) solve_xc_kernel(Grid g, V* __restrict__ r
 // plane k (y-lines) or one row j (z-lines).  For z-lines the result is added
 // to q (solxk.f90:44-50), optionally also left in rhs, and in the precision
 // form copied to the FP32 mirror m32.
+struct QSet { double* p[3]; };   // fields the z-line increments are added to, per field of the launch
+
 template <typename V, int M, bool ZL>
-__global__ void __launch_bounds__(32 * col_max_chunks(M)) solve_cc_kernel(Grid g, V* __restrict__ rhs, const V* __restrict__ X,
-                                                        double* __restrict__ q, int write_rhs, float* __restrict__ m32) {
+__global__ void __launch_bounds__(32 * col_max_chunks(M)) solve_cc_kernel(Grid g, V* __restrict__ rhs_base, const V* __restrict__ X,
+                                                        QSet qs, int write_rhs, float* __restrict__ m32) {
   __shared__ V sC[kColMaxChunks][32];
   __shared__ V sU[kColMaxChunks][32];
   __shared__ V sF[3][32];
@@ -594,11 +598,16 @@ __global__ void __launch_bounds__(32 * col_max_chunks(M)) solve_cc_kernel(Grid g
   const int lane = threadIdx.x, w = threadIdx.y;
   const int x = blockIdx.x * 32 + lane;
   const bool act = x < g.n1m;
+  // field of the launch (blockIdx.y runs over the planes of each field in turn)
+  const int planes = ZL ? g.n2m : g.n3m;
+  const int f = blockIdx.y / planes, pl = blockIdx.y - f * planes;
+  V* __restrict__ rhs = rhs_base + (size_t)f * g.cells;
+  double* __restrict__ q = ZL ? qs.p[f] : nullptr;
   // element stride of the line (< 2^31 for every supported grid) and the
   // first cell of this thread's chunk
   const int stride = ZL ? (int)g.plane : g.P;
   const int e0 = w * M;
-  const size_t first = (ZL ? cidx(g, act ? x : 0, blockIdx.y, 0) : cidx(g, act ? x : 0, 0, blockIdx.y)) +
+  const size_t first = (ZL ? cidx(g, act ? x : 0, pl, 0) : cidx(g, act ? x : 0, 0, pl)) +
                        (size_t)e0 * stride;
   V* __restrict__ rp = rhs + first;
   V r[M];
@@ -748,15 +757,15 @@ static bool smem_ok(Ctx* c, const void* fn, size_t bytes) {
   }
 
 template <typename V>
-static bool solve_xc_launch(Ctx* c, V* rhs, const V* T, const char* name) {
+static bool solve_xc_launch(Ctx* c, V* rhs, const V* T, const char* name, int nfield) {
   TriLayout L = tri_layout(c->g.n1m, tri_chunk(c, 0));
   if (!L.m) return false;
   const V* X = T + L.off_ext;
   const int lpw = 32 / line_lanes(c->g.n1m / L.m);           // lines per warp
-  dim3 grid(div_up((size_t)c->g.n2m * c->g.n3m, 8 * (size_t)lpw));
+  dim3 grid(div_up((size_t)c->g.n2m * c->g.n3m * nfield, 8 * (size_t)lpw));
   {
     MIBM_PROF(c, name);
-#define XC(M) solve_xc_kernel<V, M><<<grid, 256, 0, c->stream>>>(c->g, rhs, X)
+#define XC(M) solve_xc_kernel<V, M><<<grid, 256, 0, c->stream>>>(c->g, rhs, X, nfield)
     MIBM_CHUNK_CASES(L.m, XC)
 #undef XC
   }
@@ -766,12 +775,13 @@ static bool solve_xc_launch(Ctx* c, V* rhs, const V* T, const char* name) {
 }
 
 template <typename V, bool ZL>
-static bool solve_cc_launch(Ctx* c, V* rhs, const V* T, double* q, int write_rhs, float* m32, const char* name) {
+static bool solve_cc_launch(Ctx* c, V* rhs, const V* T, const QSet& q, int nfield, int write_rhs, float* m32,
+                            const char* name) {
   TriLayout L = tri_layout(ZL ? c->g.n3m : c->g.n2m, tri_chunk(c, ZL ? 2 : 1));
   if (!L.m) return false;
   const V* X = T + L.off_ext;
   dim3 block(32, L.n / L.m);
-  dim3 grid(div_up(c->g.n1m, 32), ZL ? c->g.n2m : c->g.n3m);
+  dim3 grid(div_up(c->g.n1m, 32), (ZL ? c->g.n2m : c->g.n3m) * nfield);
   {
     MIBM_PROF(c, name);
 #define CC(M) solve_cc_kernel<V, M, ZL><<<grid, block, 0, c->stream>>>(c->g, rhs, X, q, write_rhs, m32)
@@ -783,63 +793,90 @@ static bool solve_cc_launch(Ctx* c, V* rhs, const V* T, double* q, int write_rhs
   return true;
 }
 
+// nfield consecutive fields at stride cells in rhs share the table T: one
+// launch for all of them (the three velocity components of the fused step),
+// so that the grid holds enough blocks to keep every SM busy to the end.
+// Lengths without a chunked instance fall back to the tile kernels, one
+// launch per field.
 template <typename V>
-static void solve_x_launch(Ctx* c, V* rhs, const V* T, const char* name) {
-  if (solve_xc_launch<V>(c, rhs, T, name)) return;
+static void solve_x_launch(Ctx* c, V* rhs, const V* T, const char* name, int nfield) {
+  if (solve_xc_launch<V>(c, rhs, T, name, nfield)) return;
   size_t sm = ((size_t)kLines * (c->g.n1m + 1) + 4 * (size_t)c->g.n1m + 4) * sizeof(V);
   if (!smem_ok(c, (const void*)solve_x_kernel<V>, sm)) return;
   dim3 grid(div_up(c->g.n2m, kLines), c->g.n3m);
-  { MIBM_PROF(c, name); solve_x_kernel<V><<<grid, 128, sm, c->stream>>>(c->g, rhs, T); }
-  ++c->launches;
+  for (int f = 0; f < nfield; ++f) {
+    { MIBM_PROF(c, name); solve_x_kernel<V><<<grid, 128, sm, c->stream>>>(c->g, rhs + (size_t)f * c->g.cells, T); }
+    ++c->launches;
+  }
   MIBM_LAUNCH_CHECK(c, name);
 }
 
 template <typename V>
-static void solve_y_launch(Ctx* c, V* rhs, const V* T, const char* name) {
-  if (solve_cc_launch<V, false>(c, rhs, T, nullptr, 0, nullptr, name)) return;
+static void solve_y_launch(Ctx* c, V* rhs, const V* T, const char* name, int nfield) {
+  if (solve_cc_launch<V, false>(c, rhs, T, QSet{}, nfield, 0, nullptr, name)) return;
   size_t sm = ((size_t)kLines * c->g.n2m + 4 * (size_t)c->g.n2m + 4) * sizeof(V);
   if (!smem_ok(c, (const void*)solve_y_kernel<V>, sm)) return;
   dim3 grid(div_up(c->g.n1m, kLines), c->g.n3m);
-  { MIBM_PROF(c, name); solve_y_kernel<V><<<grid, 128, sm, c->stream>>>(c->g, rhs, T); }
-  ++c->launches;
+  for (int f = 0; f < nfield; ++f) {
+    { MIBM_PROF(c, name); solve_y_kernel<V><<<grid, 128, sm, c->stream>>>(c->g, rhs + (size_t)f * c->g.cells, T); }
+    ++c->launches;
+  }
   MIBM_LAUNCH_CHECK(c, name);
 }
 
 template <typename V>
-static void solve_z_launch(Ctx* c, V* rhs, const V* T, double* q, int write_rhs, float* m32, const char* name) {
-  if (solve_cc_launch<V, true>(c, rhs, T, q, write_rhs, m32, name)) return;
+static void solve_z_launch(Ctx* c, V* rhs, const V* T, const QSet& q, int nfield, int write_rhs, float* m32,
+                           const char* name) {
+  if (solve_cc_launch<V, true>(c, rhs, T, q, nfield, write_rhs, m32, name)) return;
   size_t sm = ((size_t)kLines * c->g.n3m + 4 * (size_t)c->g.n3m + 4) * sizeof(V);
   if (!smem_ok(c, (const void*)solve_z_kernel<V>, sm)) return;
   dim3 grid(div_up(c->g.n1m, kLines), c->g.n2m);
-  { MIBM_PROF(c, name); solve_z_kernel<V><<<grid, 128, sm, c->stream>>>(c->g, rhs, T, q, write_rhs, m32); }
-  ++c->launches;
+  for (int f = 0; f < nfield; ++f) {
+    { MIBM_PROF(c, name);
+      solve_z_kernel<V><<<grid, 128, sm, c->stream>>>(c->g, rhs + (size_t)f * c->g.cells, T, q.p[f], write_rhs, m32); }
+    ++c->launches;
+  }
   MIBM_LAUNCH_CHECK(c, name);
 }
 
-void k_solve_x_T(Ctx* c, double* rhs, const double* T) { solve_x_launch<double>(c, rhs, T, "solve_x"); }
-void k_solve_y_T(Ctx* c, double* rhs, const double* T) { solve_y_launch<double>(c, rhs, T, "solve_y"); }
-void k_solve_z_T(Ctx* c, double* rhs, const double* T, double* q, int write_rhs) {
-  solve_z_launch<double>(c, rhs, T, q, write_rhs, nullptr, "solve_z");
+static QSet qset(double* const* q, int nfield) {
+  QSet s{};
+  for (int f = 0; f < nfield && f < 3; ++f) s.p[f] = q[f];
+  return s;
 }
-void k_solve_x_f32(Ctx* c, float* rhs, const float* T) { solve_x_launch<float>(c, rhs, T, "solve_x_f32"); }
-void k_solve_y_f32(Ctx* c, float* rhs, const float* T) { solve_y_launch<float>(c, rhs, T, "solve_y_f32"); }
-void k_solve_z_f32(Ctx* c, float* rhs, const float* T, double* q, float* mirror) {
-  solve_z_launch<float>(c, rhs, T, q, 0, mirror, "solve_z_f32");
+
+void k_solve_x_T(Ctx* c, double* rhs, const double* T, int nfield) {
+  solve_x_launch<double>(c, rhs, T, "solve_x", nfield);
+}
+void k_solve_y_T(Ctx* c, double* rhs, const double* T, int nfield) {
+  solve_y_launch<double>(c, rhs, T, "solve_y", nfield);
+}
+void k_solve_z_T(Ctx* c, double* rhs, const double* T, double* const* q, int nfield, int write_rhs) {
+  solve_z_launch<double>(c, rhs, T, qset(q, nfield), nfield, write_rhs, nullptr, "solve_z");
+}
+void k_solve_x_f32(Ctx* c, float* rhs, const float* T, int nfield) {
+  solve_x_launch<float>(c, rhs, T, "solve_x_f32", nfield);
+}
+void k_solve_y_f32(Ctx* c, float* rhs, const float* T, int nfield) {
+  solve_y_launch<float>(c, rhs, T, "solve_y_f32", nfield);
+}
+void k_solve_z_f32(Ctx* c, float* rhs, const float* T, double* const* q, int nfield, float* mirror) {
+  solve_z_launch<float>(c, rhs, T, qset(q, nfield), nfield, 0, mirror, "solve_z_f32");
 }
 
 void k_solve_x(Ctx* c, double* rhs, double betadx) {
   const double* T = table_for(c, 0, betadx);
-  if (T) k_solve_x_T(c, rhs, T);
+  if (T) k_solve_x_T(c, rhs, T, 1);
 }
 
 void k_solve_y(Ctx* c, double* rhs, double betadx) {
   const double* T = table_for(c, 1, betadx);
-  if (T) k_solve_y_T(c, rhs, T);
+  if (T) k_solve_y_T(c, rhs, T, 1);
 }
 
 void k_solve_z(Ctx* c, double* rhs, double betadx, double* q) {
   const double* T = table_for(c, 2, betadx);
-  if (T) k_solve_z_T(c, rhs, T, q, 1);
+  if (T) k_solve_z_T(c, rhs, T, &q, 1, 1);
 }
 
 // ---------------------------------------------------------------------
@@ -873,15 +910,15 @@ float tri_time_direction(Ctx* c, int dir, int m, bool f32, int reps) {
       if (f32) {
         float* r = (float*)rhs;
         const float* T = (const float*)tab;
-        if (dir == 0) solve_x_launch<float>(c, r, T, "tune");
-        else if (dir == 1) solve_y_launch<float>(c, r, T, "tune");
-        else solve_z_launch<float>(c, r, T, q, 0, nullptr, "tune");
+        if (dir == 0) solve_x_launch<float>(c, r, T, "tune", 1);
+        else if (dir == 1) solve_y_launch<float>(c, r, T, "tune", 1);
+        else solve_z_launch<float>(c, r, T, qset(&q, 1), 1, 0, nullptr, "tune");
       } else {
         double* r = (double*)rhs;
         const double* T = (const double*)tab;
-        if (dir == 0) solve_x_launch<double>(c, r, T, "tune");
-        else if (dir == 1) solve_y_launch<double>(c, r, T, "tune");
-        else solve_z_launch<double>(c, r, T, q, 0, nullptr, "tune");
+        if (dir == 0) solve_x_launch<double>(c, r, T, "tune", 1);
+        else if (dir == 1) solve_y_launch<double>(c, r, T, "tune", 1);
+        else solve_z_launch<double>(c, r, T, qset(&q, 1), 1, 0, nullptr, "tune");
       }
     };
     run();
