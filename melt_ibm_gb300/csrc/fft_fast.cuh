@@ -36,14 +36,17 @@ __host__ __device__ constexpr int radix_at(int n, int st) {
 }
 
 // lines per block and threads per block for length N and complex type C
-template <typename C, int N>
+// LONE = 1: the one-line shape of the y/z passes for the columns left over
+// after whole tiles of L (the Nyquist column kx = n1m/2 for even n1m), so that
+// a last tile of one real column does not transform L - 1 padding lines
+template <typename C, int N, int LONE = 0>
 struct Shape {
   static constexpr int kWork = sizeof(C) == 8 ? 4096 : 2048;   // values per block
   // lines per block: the largest power of two <= min(32, kWork / N)
   static constexpr int pow2_floor(int v) { int p = 1; while (2 * p <= v) p *= 2; return p; }
-  static constexpr int L = pow2_floor((kWork / N) < 1 ? 1 : ((kWork / N) > 32 ? 32 : kWork / N));
-  static constexpr int T = 256;
-  static constexpr int kMinBlocks = sizeof(C) == 8 ? 3 : 2;   // resident blocks per SM asked of ptxas
+  static constexpr int L = LONE ? 1 : pow2_floor((kWork / N) < 1 ? 1 : ((kWork / N) > 32 ? 32 : kWork / N));
+  static constexpr int T = LONE ? 64 : 256;
+  static constexpr int kMinBlocks = LONE ? 8 : (sizeof(C) == 8 ? 3 : 2);   // resident blocks per SM asked of ptxas
   static constexpr int ES = L + 1;
   static constexpr size_t smem = sizeof(C) * ((size_t)N + (size_t)N * ES);
 };
@@ -230,9 +233,10 @@ __global__ void __launch_bounds__(Shape<C, N>::T, Shape<C, N>::kMinBlocks) x_inv
 }
 
 // tile of L adjacent kx columns, line elements `step` apart in the spectrum
-template <typename C, int N>
+template <typename C, int N, int LONE>
 __device__ __forceinline__ void load_cols(C* buf, const C* __restrict__ spec, size_t base, size_t step, int nc) {
-  constexpr int L = Shape<C, N>::L, T = Shape<C, N>::T, ES = Shape<C, N>::ES, PER = (N * L + T - 1) / T;
+  typedef Shape<C, N, LONE> Sh;
+  constexpr int L = Sh::L, T = Sh::T, ES = Sh::ES, PER = (N * L + T - 1) / T;
   C v[PER];
 #pragma unroll
   for (int p = 0; p < PER; ++p) {
@@ -247,9 +251,10 @@ __device__ __forceinline__ void load_cols(C* buf, const C* __restrict__ spec, si
   }
 }
 
-template <typename C, int N>
+template <typename C, int N, int LONE>
 __device__ __forceinline__ void store_cols(const C* buf, C* __restrict__ spec, size_t base, size_t step, int nc) {
-  constexpr int L = Shape<C, N>::L, T = Shape<C, N>::T, ES = Shape<C, N>::ES, PER = (N * L + T - 1) / T;
+  typedef Shape<C, N, LONE> Sh;
+  constexpr int L = Sh::L, T = Sh::T, ES = Sh::ES, PER = (N * L + T - 1) / T;
 #pragma unroll
   for (int p = 0; p < PER; ++p) {
     const int t = threadIdx.x + p * T;
@@ -258,39 +263,43 @@ __device__ __forceinline__ void store_cols(const C* buf, C* __restrict__ spec, s
   }
 }
 
-// Y pass (forward or inverse) on L kx columns of plane k
-template <typename C, int N, bool INV>
-__global__ void __launch_bounds__(Shape<C, N>::T, Shape<C, N>::kMinBlocks) y_pass(FftArgs<C> F, C* __restrict__ spec) {
-  constexpr int L = Shape<C, N>::L, T = Shape<C, N>::T;
+// Y pass (forward or inverse) on L kx columns from kx_base + L*blockIdx.x of plane k
+template <typename C, int N, bool INV, int LONE = 0>
+__global__ void __launch_bounds__(Shape<C, N, LONE>::T, Shape<C, N, LONE>::kMinBlocks)
+y_pass(FftArgs<C> F, C* __restrict__ spec, int kx_base) {
+  typedef Shape<C, N, LONE> Sh;
+  constexpr int L = Sh::L, T = Sh::T;
   extern __shared__ __align__(16) unsigned char shraw[];
   C* tw = (C*)shraw;
   C* buf = tw + N;
   stage_twiddles<C, N, T>(tw, F.twy);
   const Grid& g = F.g;
-  const int kx0 = blockIdx.x * L, k = blockIdx.y;
+  const int kx0 = kx_base + blockIdx.x * L, k = blockIdx.y;
   const int nc = min(L, g.H - kx0);
   const size_t base = (size_t)kx0 + (size_t)g.HP * (size_t)g.n2m * k;
-  load_cols<C, N>(buf, spec, base, (size_t)g.HP, nc);
+  load_cols<C, N, LONE>(buf, spec, base, (size_t)g.HP, nc);
   __syncthreads();
   run<C, N, L, T, INV>(buf, tw);
-  store_cols<C, N>(buf, spec, base, (size_t)g.HP, nc);
+  store_cols<C, N, LONE>(buf, spec, base, (size_t)g.HP, nc);
 }
 
 // Z pass: forward, scale, eigenvalue division, zero mode, inverse
-template <typename C, int N>
-__global__ void __launch_bounds__(Shape<C, N>::T, Shape<C, N>::kMinBlocks) z_solve(FftArgs<C> F, C* __restrict__ spec) {
+template <typename C, int N, int LONE = 0>
+__global__ void __launch_bounds__(Shape<C, N, LONE>::T, Shape<C, N, LONE>::kMinBlocks)
+z_solve(FftArgs<C> F, C* __restrict__ spec, int kx_base) {
   typedef typename Real<C>::T R;
-  constexpr int L = Shape<C, N>::L, T = Shape<C, N>::T, ES = Shape<C, N>::ES;
+  typedef Shape<C, N, LONE> Sh;
+  constexpr int L = Sh::L, T = Sh::T, ES = Sh::ES;
   extern __shared__ __align__(16) unsigned char shraw[];
   C* tw = (C*)shraw;
   C* buf = tw + N;
   stage_twiddles<C, N, T>(tw, F.twz);
   const Grid& g = F.g;
-  const int kx0 = blockIdx.x * L, j = blockIdx.y;
+  const int kx0 = kx_base + blockIdx.x * L, j = blockIdx.y;
   const int nc = min(L, g.H - kx0);
   const size_t zstride = (size_t)g.HP * g.n2m;
   const size_t base = (size_t)kx0 + (size_t)g.HP * j;
-  load_cols<C, N>(buf, spec, base, zstride, nc);
+  load_cols<C, N, LONE>(buf, spec, base, zstride, nc);
   __syncthreads();
   run<C, N, L, T, false>(buf, tw);
   const R* __restrict__ eig = F.eig + (size_t)g.H * j;
@@ -309,7 +318,7 @@ __global__ void __launch_bounds__(Shape<C, N>::T, Shape<C, N>::kMinBlocks) z_sol
   }
   __syncthreads();
   run<C, N, L, T, true>(buf, tw);
-  store_cols<C, N>(buf, spec, base, zstride, nc);
+  store_cols<C, N, LONE>(buf, spec, base, zstride, nc);
 }
 
 // shared-memory opt-in for the instances above the default 48 KB
@@ -338,24 +347,46 @@ void launch_x_inv(Ctx* c, const FftArgs<C>& F, const C* spec, typename Real<C>::
   k<<<grid, Sh::T, Sh::smem, c->stream>>>(F, spec, dst);
 }
 
+// whole tiles of L columns, then the columns left over one line per block
+// (H = n1m/2 + 1 leaves the Nyquist column when L divides n1m/2)
 template <typename C, int N>
 void launch_y(Ctx* c, const FftArgs<C>& F, C* spec, int sign) {
   typedef Shape<C, N> Sh;
+  typedef Shape<C, N, 1> S1;
   auto kf = y_pass<C, N, false>;
   auto ki = y_pass<C, N, true>;
-  if (!smem_attr(c, kf, Sh::smem) || !smem_attr(c, ki, Sh::smem)) return;
-  dim3 grid(div_up(c->g.H, Sh::L), c->g.n3m);
-  if (sign < 0) kf<<<grid, Sh::T, Sh::smem, c->stream>>>(F, spec);
-  else ki<<<grid, Sh::T, Sh::smem, c->stream>>>(F, spec);
+  auto kf1 = y_pass<C, N, false, 1>;
+  auto ki1 = y_pass<C, N, true, 1>;
+  if (!smem_attr(c, kf, Sh::smem) || !smem_attr(c, ki, Sh::smem) || !smem_attr(c, kf1, S1::smem) ||
+      !smem_attr(c, ki1, S1::smem))
+    return;
+  const int tiles = c->g.H / Sh::L, rest = c->g.H - tiles * Sh::L;
+  if (tiles > 0) {
+    dim3 grid(tiles, c->g.n3m);
+    if (sign < 0) kf<<<grid, Sh::T, Sh::smem, c->stream>>>(F, spec, 0);
+    else ki<<<grid, Sh::T, Sh::smem, c->stream>>>(F, spec, 0);
+  }
+  if (rest > 0) {
+    dim3 grid(rest, c->g.n3m);
+    if (sign < 0) kf1<<<grid, S1::T, S1::smem, c->stream>>>(F, spec, tiles * Sh::L);
+    else ki1<<<grid, S1::T, S1::smem, c->stream>>>(F, spec, tiles * Sh::L);
+    if (tiles > 0) ++c->launches;      // the caller counts one launch per pass
+  }
 }
 
 template <typename C, int N>
 void launch_z(Ctx* c, const FftArgs<C>& F, C* spec) {
   typedef Shape<C, N> Sh;
+  typedef Shape<C, N, 1> S1;
   auto k = z_solve<C, N>;
-  if (!smem_attr(c, k, Sh::smem)) return;
-  dim3 grid(div_up(c->g.H, Sh::L), c->g.n2m);
-  k<<<grid, Sh::T, Sh::smem, c->stream>>>(F, spec);
+  auto k1 = z_solve<C, N, 1>;
+  if (!smem_attr(c, k, Sh::smem) || !smem_attr(c, k1, S1::smem)) return;
+  const int tiles = c->g.H / Sh::L, rest = c->g.H - tiles * Sh::L;
+  if (tiles > 0) k<<<dim3(tiles, c->g.n2m), Sh::T, Sh::smem, c->stream>>>(F, spec, 0);
+  if (rest > 0) {
+    k1<<<dim3(rest, c->g.n2m), S1::T, S1::smem, c->stream>>>(F, spec, tiles * Sh::L);
+    if (tiles > 0) ++c->launches;      // the caller counts one launch per pass
+  }
 }
 
 }  // namespace fastfft
