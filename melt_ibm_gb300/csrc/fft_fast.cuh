@@ -41,12 +41,18 @@ __host__ __device__ constexpr int radix_at(int n, int st) {
 // a last tile of one real column does not transform L - 1 padding lines
 template <typename C, int N, int LONE = 0>
 struct Shape {
-  static constexpr int kWork = sizeof(C) == 8 ? 4096 : 2048;   // values per block
-  // lines per block: the largest power of two <= min(32, kWork / N)
+  // values per block: small tiles, so that a pass has many blocks and the
+  // last wave leaves few SMs idle (these passes are FP64-issue bound), but
+  // at least 8 (FP64) or 16 (FP32) lines so that a block still moves 128
+  // contiguous bytes per spectrum row
+  static constexpr int kWork = sizeof(C) == 16 ? 1024 : 2048;
+  static constexpr int kMinL = sizeof(C) == 16 ? 8 : 16;
+  // lines per block: the largest power of two <= min(32, max(kMinL, kWork / N))
   static constexpr int pow2_floor(int v) { int p = 1; while (2 * p <= v) p *= 2; return p; }
-  static constexpr int L = LONE ? 1 : pow2_floor((kWork / N) < 1 ? 1 : ((kWork / N) > 32 ? 32 : kWork / N));
+  static constexpr int Lw = (kWork / N) < kMinL ? kMinL : ((kWork / N) > 32 ? 32 : kWork / N);
+  static constexpr int L = LONE ? 1 : pow2_floor(Lw);
   static constexpr int T = LONE ? 64 : 256;
-  static constexpr int kMinBlocks = LONE ? 8 : (sizeof(C) == 8 ? 3 : 2);   // resident blocks per SM asked of ptxas
+  static constexpr int kMinBlocks = LONE ? 8 : 3;   // resident blocks per SM asked of ptxas
   static constexpr int ES = L + 1;
   static constexpr size_t smem = sizeof(C) * ((size_t)N + (size_t)N * ES);
 };
