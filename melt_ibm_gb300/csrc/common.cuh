@@ -143,6 +143,8 @@ struct Ctx {
   cudaEvent_t ev_lfork = nullptr, ev_ldone = nullptr;   // structural loads on the side stream
   cudaStream_t side2 = nullptr;                         // narrow-band tagging beside the MLS weights and plan
   cudaEvent_t ev_tfork = nullptr, ev_tjoin = nullptr;
+  cudaStream_t side3 = nullptr;                         // MLS weights beside the scatter plan
+  cudaEvent_t ev_wfork = nullptr, ev_wjoin = nullptr;
   bool loads_pending = false;
   std::vector<void*> pinned;              // host arrays page-locked by mibm_pin_host_
   bool prologue_done = false;             // the next substep's geometry-only work is enqueued

@@ -287,6 +287,9 @@ void release(Ctx* c) {
   diag_free(c);
   if (c->side) { cudaStreamSynchronize(c->side); cudaStreamDestroy(c->side); }
   if (c->side2) { cudaStreamSynchronize(c->side2); cudaStreamDestroy(c->side2); }
+  if (c->side3) { cudaStreamSynchronize(c->side3); cudaStreamDestroy(c->side3); }
+  if (c->ev_wfork) cudaEventDestroy(c->ev_wfork);
+  if (c->ev_wjoin) cudaEventDestroy(c->ev_wjoin);
   if (c->ev_tfork) cudaEventDestroy(c->ev_tfork);
   if (c->ev_tjoin) cudaEventDestroy(c->ev_tjoin);
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
@@ -313,6 +316,9 @@ int mibm_context_create_(void) {
   if (!cuda_ok(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream") ||
       !cuda_ok(c, cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking), "stream") ||
       !cuda_ok(c, cudaStreamCreateWithFlags(&c->side2, cudaStreamNonBlocking), "stream") ||
+      !cuda_ok(c, cudaStreamCreateWithFlags(&c->side3, cudaStreamNonBlocking), "stream") ||
+      !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_wfork, cudaEventDisableTiming), "event") ||
+      !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_wjoin, cudaEventDisableTiming), "event") ||
       !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_tfork, cudaEventDisableTiming), "event") ||
       !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_tjoin, cudaEventDisableTiming), "event") ||
       !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "event") ||

@@ -2239,12 +2239,25 @@ void lagr_substep_prologue(Ctx* c, int slot) {
   LagState* s = lag_of(c);
   bool stationary = c->I(MIBM_I_STATIONARY) != 0;
   lagr_find_centroid_indices(c);
+  // the MLS weights and the scatter plan both read the cage indices and
+  // nothing the other writes: the weights go to a third stream
+  const bool wsplit = split && c->side3;
+  if (wsplit) {
+    cudaEventRecord(c->ev_wfork, c->stream);
+    cudaStreamWaitEvent(c->side3, c->ev_wfork, 0);
+    std::swap(c->stream, c->side3);
+  }
   if (!(stationary && s->weights_valid)) {
     mls_weight_launch(c);
     s->weights_valid = stationary;
     if (stationary) ++c->lag_gen;     // later steps skip the weights: another launch sequence
   }
+  if (wsplit) {
+    cudaEventRecord(c->ev_wjoin, c->stream);
+    std::swap(c->stream, c->side3);
+  }
   update_plan(c, slot < 3 ? c->dparams + slot : nullptr);
+  if (wsplit) cudaStreamWaitEvent(c->stream, c->ev_wjoin, 0);
   if (split) cudaStreamWaitEvent(c->stream, c->ev_tjoin, 0);
 }
 
