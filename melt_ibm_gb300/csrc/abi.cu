@@ -166,8 +166,8 @@ static void step_enqueue_f32(Ctx* c) {
   float* t_mirror = c->q32 + 3 * g.cells;
   for (int ns = 0; ns < 3; ++ns) {
     const StepParams* dp = c->dparams + ns;
-    lagr_join(c);
-    if (!c->prologue_done) lagr_substep_prologue(c, ns);
+    lagr_join_geom(c);            // the rest of the side branch is waited for before the forcing
+    if (!c->prologue_done) { lagr_join(c); lagr_substep_prologue(c, ns); }
     c->prologue_done = false;
     k_fused_rhs_f32(c, dp, c->ru32, c->rhs32);
     {
@@ -205,8 +205,8 @@ static void step_enqueue_f64(Ctx* c) {
   if (!tables) return;
   for (int ns = 0; ns < 3; ++ns) {
     const StepParams* dp = c->dparams + ns;
-    lagr_join(c);
-    if (!c->prologue_done) lagr_substep_prologue(c, ns);
+    lagr_join_geom(c);            // the rest of the side branch is waited for before the forcing
+    if (!c->prologue_done) { lagr_join(c); lagr_substep_prologue(c, ns); }
     c->prologue_done = false;
     k_fused_rhs(c, dp);
     {

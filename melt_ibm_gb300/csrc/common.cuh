@@ -140,6 +140,12 @@ struct Ctx {
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   bool join_pending = false;
+  // the part of the side branch the next substep's explicit terms need: the
+  // published rigid-body state (ev_pub) and the VOF fields (ev_tjoin when the
+  // tagging ran on its own stream); the cage indices, MLS weights and scatter
+  // plan (ev_join) are waited for only before the forcing
+  cudaEvent_t ev_pub = nullptr;
+  bool geom_join_pending = false, geom_join_tag = false;
   cudaEvent_t ev_lfork = nullptr, ev_ldone = nullptr;   // structural loads on the side stream
   cudaStream_t side2 = nullptr;                         // narrow-band tagging beside the MLS weights and plan
   cudaEvent_t ev_tfork = nullptr, ev_tjoin = nullptr;
@@ -372,6 +378,7 @@ void k_rigid_publish(Ctx* c, const double* geom, StepParams* next);
 void rigid_free(Ctx* c);
 void lagr_step_readback(Ctx* c);
 void lagr_join(Ctx* c);
+void lagr_join_geom(Ctx* c);
 void lagr_loads_early(Ctx* c, const StepParams* dp);
 bool lagr_fork_enabled(Ctx* c);
 void lagr_step_host_finish(Ctx* c);

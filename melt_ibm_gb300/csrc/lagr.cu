@@ -2222,6 +2222,7 @@ void lagr_substep_prologue(Ctx* c, int slot) {
   // same geometry and write disjoint buffers: the tagging goes to a stream of
   // its own and is joined back before the prologue ends
   const bool split = !c->I(MIBM_I_STATIONARY) && c->side2 && lagr_fork_enabled(c);
+  c->geom_join_tag = split;
   if (split) {
     cudaEventRecord(c->ev_tfork, c->stream);
     cudaStreamWaitEvent(c->side2, c->ev_tfork, 0);
@@ -2292,6 +2293,7 @@ const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror,
   if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0) return nullptr;
   if (!ensure_adjacency(c) || !ensure_lag_buffers(c)) return nullptr;
   LagState* s = lag_of(c);
+  lagr_join(c);                   // cage indices, MLS weights, scatter plan of this substep
   force_coefficients(c);
   bool str = c->I(MIBM_I_IMLSSTR) == 1;
   if (str) {                                 // reads the unforced u, v, w and p
@@ -2337,6 +2339,8 @@ const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror,
       tri_velocity_launch(c, vel, om);
     }
     if (str) k_rigid_publish(c, s->geom_out, next);
+    if (fork) cudaEventRecord(c->ev_pub, c->stream);
+    c->geom_join_tag = false;
     if (fork && next_prologue >= 0) {
       lagr_substep_prologue(c, next_prologue);
       c->prologue_done = true;
@@ -2347,6 +2351,7 @@ const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror,
     cudaEventRecord(c->ev_join, c->stream);
     std::swap(c->stream, c->side);
     c->join_pending = true;
+    c->geom_join_pending = true;
   }
   return c->status == MIBM_OK ? s->mean3 : nullptr;
 }
@@ -2356,6 +2361,17 @@ void lagr_join(Ctx* c) {
   if (!c->join_pending) return;
   cudaStreamWaitEvent(c->stream, c->ev_join, 0);
   c->join_pending = false;
+  c->geom_join_pending = false;
+}
+
+// the main stream waits for what the next substep's explicit terms read
+// from the side branch: the moved body (published state, geometry) and,
+// when the tagging ran on its own stream, the VOF fields
+void lagr_join_geom(Ctx* c) {
+  if (!c->geom_join_pending) return;
+  cudaStreamWaitEvent(c->stream, c->ev_pub, 0);
+  if (c->geom_join_tag) cudaStreamWaitEvent(c->stream, c->ev_tjoin, 0);
+  c->geom_join_pending = false;
 }
 
 // End of the fused step, in two halves so that the device half can sit in
