@@ -92,7 +92,8 @@ WORKLOAD_TEXT = {
 # compulsory field reads + writes of that kernel, N^3 cells): see the design doc.
 ALGO_PASSES = {
     "fused_rhs": 7.0,      # x/y/z/T average: reads u,v,w(,T),p,ru ; writes rhs, ru
-    "solve_x": 2.0, "solve_y": 2.0, "solve_z": 4.0,
+    # one launch for u, v, w (3 fields), one for T: mean of 3x and 1x the field passes
+    "solve_x": 4.0, "solve_y": 4.0, "solve_z": 8.0,
     "fft_x_fwd": 1.0 + 1.125, "fft_y": 2.25, "fft_z_solve": 2.25, "fft_x_inv": 1.125 + 1.0,
     "divg": 4.0, "updvp": 7.0, "prcalc": 3.0, "hdnl": 6.0,
 }
@@ -102,7 +103,7 @@ ALGO_PASSES = {
 # step, at the size given, per cell: profiles/fused_rhs_melt128_fp64_dram.md.
 # Other sizes scale by the cell count (the traffic is per-cell compulsory).
 NCU_TRAFFIC = {
-    "fused_rhs": {"bytes_per_cell": 96.4e6 / 128 ** 3, "measured_at": "128^3 (melt128_fixed)"},
+    "fused_rhs": {"bytes_per_cell": 139.6e6 / 128 ** 3, "measured_at": "128^3 (melt128_c1)"},
 }
 
 FIELDS = {"u": abi.MIBM_F_VX, "v": abi.MIBM_F_VY, "w": abi.MIBM_F_VZ, "T": abi.MIBM_F_TEMP, "p": abi.MIBM_F_PR}
