@@ -301,6 +301,11 @@ void mibm_hit_bhat_(double* bhat, const int* dir);
 /* reference reseeds at restart, hit.f90:39-42; exact continuation needs    */
 /* the stream position).                                                    */
 void mibm_hit_rng_(unsigned long long* state, const int* dir);
+/* mibm_selftest_: checks the library's integer-pipe FP64<->FP32 conversions  */
+/* (used by the precision form) against the hardware conversions, bit for  */
+/* bit, on edge cases and 2^26 random patterns.  Returns the number of      */
+/* mismatches (0 = pass), -1 without a usable GPU.                          */
+int  mibm_selftest_(void);
 /* Linear forcing (no counterpart in the reference, which offers only the */
 /* two forcings above): forc = C_HIT * u at each velocity's own staggered */
 /* position, stored as xlen * C_HIT * u so that the reference's explicit  */

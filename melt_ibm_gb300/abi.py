@@ -90,6 +90,7 @@ SIGNATURES: dict[str, tuple] = {
     "mibm_hit_modes_": (C.c_int, []),
     "mibm_hit_bhat_": (None, [C.c_void_p, _I]),
     "mibm_hit_rng_": (None, [C.c_void_p, _I]),
+    "mibm_selftest_": (C.c_int, []),
 }
 VOID_ROUTINES = [
     "tschem_", "hdnl1_", "hdnl2_", "hdnl3_", "hdnlte_", "invtr1_", "invtr2_", "invtr3_",

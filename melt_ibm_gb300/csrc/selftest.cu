@@ -1,0 +1,111 @@
+// selftest.cu -- mibm_selftest_: device checks of the library's own
+// arithmetic helpers against the hardware.  The integer-pipe conversions of
+// fpconv.cuh must equal the conversion instructions bit for bit (NaN: any
+// NaN) on edge cases (signed zeros, subnormals of both formats, the float
+// range limits, ties at every rounding boundary, infinities, NaNs) and on
+// random bit patterns.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "fpconv.cuh"
+
+namespace mibm {
+
+// splitmix64 of the thread's index: random bit patterns without host data
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z = (z + 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ bool same_f(float a, float b) {
+  return (a != a && b != b) || __float_as_uint(a) == __float_as_uint(b);
+}
+__device__ __forceinline__ bool same_d(double a, double b) {
+  return (a != a && b != b) || __double_as_longlong(a) == __double_as_longlong(b);
+}
+
+// edge[] then n_random random patterns; bad[0] counts d2f mismatches, bad[1]
+// f2d mismatches, bad[2..3] keep the first failing input bits
+__global__ void conv_selftest_kernel(const unsigned long long* __restrict__ edge, int n_edge, long long n_random,
+                                     unsigned long long* __restrict__ bad) {
+  const long long n = n_edge + n_random;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    uint64_t bits;
+    if (t < n_edge) bits = edge[t];
+    else {
+      bits = mix64((uint64_t)t);
+      // half of the random doubles near the float range, where rounding is exercised
+      if (t & 1) bits = (bits & 0x800fffffffffffffull) | ((uint64_t)(0x340 + (bits >> 52) % 0x140) << 52);
+    }
+    const double d = __longlong_as_double((long long)bits);
+    if (!same_f(d2f_bits(d), (float)d)) {
+      if (atomicAdd(&bad[0], 1ull) == 0) bad[2] = bits;
+    }
+    const float f = __uint_as_float((uint32_t)(bits >> 16));
+    if (!same_d(f2d_bits(f), (double)f)) {
+      if (atomicAdd(&bad[1], 1ull) == 0) bad[3] = (uint32_t)(bits >> 16);
+    }
+  }
+}
+
+static void edge_cases(std::vector<unsigned long long>& v) {
+  auto d = [&](double x) { unsigned long long b; memcpy(&b, &x, 8); v.push_back(b); };
+  auto f = [&](uint32_t fb) {          // a float pattern, placed so that (bits >> 16) is it
+    unsigned long long b = (unsigned long long)fb << 16;
+    v.push_back(b);
+  };
+  const double specials[] = {0.0, -0.0, 1.0, -1.0, 0.5, 3.0, 1e-300, -1e-300, 1e300, -1e300,
+                             3.4028234663852886e38, 3.4028235677973366e38, 3.4028235677973362e38,
+                             3.402823567797337e38, 1.1754943508222875e-38, 1.1754942106924411e-38,
+                             1.401298464324817e-45, 7.006492321624085e-46, 7.006492321624087e-46,
+                             2.1019476964872256e-45, 1e-45, 1e-46, 4.9e-324, 2.2250738585072014e-308};
+  for (double x : specials) { d(x); d(-x); }
+  const unsigned long long raw[] = {0x7ff0000000000000ull, 0xfff0000000000000ull, 0x7ff8000000000000ull,
+                                    0x7ff0000000000001ull, 0xfff8000000000123ull, 0x000fffffffffffffull,
+                                    0x0000000000000001ull, 0x3ff0000010000000ull, 0x3ff0000030000000ull,
+                                    0x3ff0000010000001ull, 0x3ff000000fffffffull, 0x47efffffefffffffull,
+                                    0x47effffff0000000ull, 0x380fffffffffffffull, 0x36a0000000000000ull,
+                                    0x3690000000000000ull, 0x3690000000000001ull};
+  for (unsigned long long b : raw) { v.push_back(b); v.push_back(b ^ 0x8000000000000000ull); }
+  // ties and neighbours at every float exponent, normal and subnormal
+  for (int e = 0x340; e < 0x480; ++e)
+    for (unsigned long long low : {0x10000000ull, 0x30000000ull, 0x0fffffffull, 0x10000001ull, 0x1fffffffull})
+      v.push_back(((unsigned long long)e << 52) | (0x5555500000000ull & ~0x1fffffffull) | low);
+  const uint32_t fr[] = {0x00000000u, 0x80000000u, 0x00000001u, 0x007fffffu, 0x00400000u, 0x00800000u,
+                         0x7f7fffffu, 0x7f800000u, 0xff800000u, 0x7fc00000u, 0x7f800001u, 0x3f800000u,
+                         0x80000001u, 0x807fffffu, 0x00000100u, 0x00012345u};
+  for (uint32_t x : fr) f(x);
+}
+
+}  // namespace mibm
+
+using namespace mibm;
+
+extern "C" int mibm_selftest_(void) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) { cudaGetLastError(); return -1; }
+  std::vector<unsigned long long> edge;
+  edge_cases(edge);
+  unsigned long long *dedge = nullptr, *dbad = nullptr;
+  unsigned long long hbad[4] = {0, 0, 0, 0};
+  const long long n_random = 1ll << 26;
+  bool ok = cudaMalloc(&dedge, edge.size() * 8) == cudaSuccess && cudaMalloc(&dbad, 32) == cudaSuccess &&
+            cudaMemcpy(dedge, edge.data(), edge.size() * 8, cudaMemcpyHostToDevice) == cudaSuccess &&
+            cudaMemset(dbad, 0, 32) == cudaSuccess;
+  if (ok) {
+    conv_selftest_kernel<<<1216, 256>>>(dedge, (int)edge.size(), n_random, dbad);
+    ok = cudaDeviceSynchronize() == cudaSuccess && cudaMemcpy(hbad, dbad, 32, cudaMemcpyDeviceToHost) == cudaSuccess;
+  }
+  cudaFree(dedge);
+  cudaFree(dbad);
+  if (!ok) { cudaGetLastError(); return -1; }
+  if (hbad[0] || hbad[1])
+    fprintf(stderr, "mibm_selftest_: d2f %llu mismatches (first 0x%016llx), f2d %llu (first 0x%08llx)\n", hbad[0],
+            hbad[2], hbad[1], hbad[3]);
+  return (int)std::min<unsigned long long>(hbad[0] + hbad[1], 1000000);
+}

@@ -14,6 +14,7 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "fpconv.cuh"
 
 namespace mibm {
 
@@ -116,8 +117,8 @@ __device__ __forceinline__ R add_forcing(R h, const double* __restrict__ vof, co
     if (vof_is_one(v)) return forc[c0] * rlen + h;
     return (v * forc[c0]) * rlen + h;
   } else {
-    if (vof_is_one(v)) return R(forc[c0]) * rlen + h;
-    return R(v * forc[c0]) * rlen + h;
+    if (vof_is_one(v)) return d2f_bits(forc[c0]) * rlen + h;
+    return d2f_bits(v * forc[c0]) * rlen + h;
   }
 }
 
@@ -278,7 +279,7 @@ __device__ __forceinline__ R h_t(const StencilArgs& A, int i, int j, int k, idx_
   R hs = udx1 * x31 + udx2 * x32 + udx3 * x33;     // h31 + h32 + h33
   const double vpd = A.vofp[c0];
   if (vof_is_one(vpd)) return -hs;                 // fluid cell: VOFp = 1, no solid term
-  R vp = R(vpd);
+  R vp = narrow<R>(vpd);
   R ht = -hs * vp;
   R sv = R(1.0) - vp;
   R h31, h32, h33;
@@ -407,7 +408,7 @@ __global__ void divg_f32_kernel(StencilArgs A, const StepParams* __restrict__ pp
   CELL_INDEX
   double du = A.vx[c0 + dip] - A.vx[c0], dv = A.vy[c0 + djp] - A.vy[c0], dw = A.vz[c0 + dkp] - A.vz[c0];
   double dq = fma(dw, g.dx3, fma(dv, g.dx2, du * g.dx1));
-  res[c0] = (float)dq * pp->cf[kUSDTAL];
+  res[c0] = d2f_bits(dq) * pp->cf[kUSDTAL];
 }
 
 // mean3 (fused step only): the mean IBM force of velforce.f90:21-50, removed
@@ -438,9 +439,9 @@ __global__ void updvp_f32_kernel(StencilArgs A, const StepParams* __restrict__ p
   float iy = (loc - phi[c0 + djm]) * pp->cf[kUP2];
   float iz = (loc - phi[c0 + dkm]) * pp->cf[kUP3];
   if (mean3f) { ix += mean3f[0]; iy += mean3f[1]; iz += mean3f[2]; }
-  double x = vx[c0] - (double)ix, y = vy[c0] - (double)iy, z = vz[c0] - (double)iz;
+  double x = vx[c0] - f2d_bits(ix), y = vy[c0] - f2d_bits(iy), z = vz[c0] - f2d_bits(iz);
   vx[c0] = x; vy[c0] = y; vz[c0] = z;
-  if (m32) { m32[c0] = (float)x; m32[c0 + g.cells] = (float)y; m32[c0 + 2 * g.cells] = (float)z; }
+  if (m32) { m32[c0] = d2f_bits(x); m32[c0 + g.cells] = d2f_bits(y); m32[c0 + 2 * g.cells] = d2f_bits(z); }
 }
 
 // precision form: p += phi - al beta lap(phi), increment in FP32, optional
@@ -453,9 +454,9 @@ __global__ void prcalc_f32_kernel(StencilArgs A, const StepParams* __restrict__ 
   float inc = d - be * ((phi[c0 + dip] - 2.0f * d + phi[c0 + dim]) * pp->cf[kDQ1] +
                         (phi[c0 + djp] - 2.0f * d + phi[c0 + djm]) * pp->cf[kDQ2] +
                         (phi[c0 + dkp] - 2.0f * d + phi[c0 + dkm]) * pp->cf[kDQ3]);
-  double q = pr[c0] + (double)inc;
+  double q = pr[c0] + f2d_bits(inc);
   pr[c0] = q;
-  if (m32) m32[c0] = (float)q;
+  if (m32) m32[c0] = d2f_bits(q);
 }
 
 // FP32 mirrors of u, v, w, T, p (field f at m32 + f*cells)
@@ -464,18 +465,18 @@ __global__ void mirror_kernel(size_t n, const double* __restrict__ u, const doub
                               const double* __restrict__ p, float* __restrict__ m32) {
   size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n) return;
-  m32[e] = (float)u[e]; m32[e + n] = (float)v[e]; m32[e + 2 * n] = (float)w[e];
-  m32[e + 3 * n] = (float)t[e]; m32[e + 4 * n] = (float)p[e];
+  m32[e] = d2f_bits(u[e]); m32[e + n] = d2f_bits(v[e]); m32[e + 2 * n] = d2f_bits(w[e]);
+  m32[e + 3 * n] = d2f_bits(t[e]); m32[e + 4 * n] = d2f_bits(p[e]);
 }
 
 __global__ void cast_d2f_kernel(size_t n, const double* __restrict__ a, float* __restrict__ b) {
   size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e < n) b[e] = (float)a[e];
+  if (e < n) b[e] = d2f_bits(a[e]);
 }
 
 __global__ void cast_f2d_kernel(size_t n, const float* __restrict__ a, double* __restrict__ b) {
   size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e < n) b[e] = (double)a[e];
+  if (e < n) b[e] = f2d_bits(a[e]);
 }
 
 // max |div u| (divgck semantics, divg.f90:26-56) into bits of `out`

@@ -39,6 +39,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "fpconv.cuh"
 
 namespace mibm {
 
@@ -303,9 +304,9 @@ __global__ void solve_z_kernel(Grid g, V* __restrict__ rhs, const V* __restrict_
       size_t c0 = cidx(g, i0 + l, j, k);
       V x = sm[t];
       if (write_rhs) rhs[c0] = x;
-      double qn = q[c0] + (double)x;
+      double qn = q[c0] + widen(x);
       q[c0] = qn;
-      if (m32) m32[c0] = (float)qn;
+      if (m32) m32[c0] = d2f_bits(qn);
     }
   }
 }
@@ -658,9 +659,9 @@ __global__ void __launch_bounds__(32 * col_max_chunks(M)) solve_cc_kernel(Grid g
     int o = i * stride;
     if (ZL) {
       if (write_rhs) rp[o] = xv;
-      double qn = qv[ZL ? i : 0] + (double)xv;
+      double qn = qv[ZL ? i : 0] + widen(xv);
       q[first + o] = qn;
-      if (m32) m32[first + o] = (float)qn;
+      if (m32) m32[first + o] = d2f_bits(qn);
     } else {
       rp[o] = xv;
     }

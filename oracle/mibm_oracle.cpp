@@ -2395,6 +2395,9 @@ void mibm_hit_bhat_(double* bhat, const int* dir) {
   }
 }
 
+// the device self-test has nothing to check in the CPU restatement
+int mibm_selftest_(void) { return 0; }
+
 void mibm_hit_rng_(unsigned long long* state, const int* dir) {
   Ctx* c = cur(); if (!ready(c)) return;
   if (!state || (*dir != 0 && *dir != 1)) { fail(c, MIBM_EINVAL, "hit_rng: dir 0 (get) or 1 (set)"); return; }

@@ -1,0 +1,11 @@
+"""The library's integer-pipe FP64<->FP32 conversions (fpconv.cuh), used by
+the precision form, equal the hardware conversion instructions bit for bit on
+edge cases (signed zeros, subnormals, range limits, rounding ties at every
+float exponent, infinities, NaNs) and on 2^26 random bit patterns."""
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_conversions_match_hardware(gpu_lib):
+    assert gpu_lib.mibm_selftest_() == 0
