@@ -86,90 +86,150 @@ __device__ void rot_matrix(double q[4], double AA[9]) {
 
 // newton_euler + the periodic wrap of update_part_pos.  geom: [.., .., Volume,
 // pos_CM(3), InertTensor(9)] of the body before the move.
+//
+// One warp.  On this part an FP64 instruction occupies a sub-partition's FP64
+// unit for the same time whether one lane or all 32 are active, so the
+// independent entries of each phase (the 3 components, the 4 quaternion
+// entries, the 9 matrix entries, sine beside cosine) are computed by as many
+// lanes at once; each entry keeps the operation sequence of the one-thread
+// version (no FMA contraction), so the values are the same.  The LU inverse
+// stays on lane 0.  Phases meet in shared memory after a __syncwarp().
 __global__ void newton_euler_kernel(const StepParams* __restrict__ pp, const double* __restrict__ geom,
                                     double dens_ratio, double xlen, double ylen, double zlen, RigidDev* r,
                                     int* __restrict__ flag) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (blockIdx.x != 0) return;
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x;
+  __shared__ double I[9], I_LHS[9], I_inv[9], AA[9], buf[9], om1[3], vel1[3], rhs[3], om[3], ob[3], quat[4];
+  __shared__ double sc[4];          // magOM, angle, ch, sh
+  __shared__ double qn_s;
+  __shared__ int singular;
   const double al = pp->al, ga = pp->ga, ro = pp->ro, dt = pp->dt;
-  const double Volume = geom[2];
-  double pos1[3] = {geom[3], geom[4], geom[5]};
-  double I[9];
-  for (int q = 0; q < 9; ++q) I[q] = geom[6 + q];
   const double* prn = r->load; const double* tau = r->load + 3;
   const double* rprn = r->load + 6; const double* rtau = r->load + 9;
   const double* prn1 = r->load1; const double* tau1 = r->load1 + 3;
   const double* rprn1 = r->load1 + 6; const double* rtau1 = r->load1 + 9;
-  const double e_z[3] = {0.0, 0.0, -1.0};
-  double vel1[3], om1[3], vel[3], pos[3], om[3] = {0, 0, 0}, quat[4] = {0, 0, 0, 0};
-  for (int d = 0; d < 3; ++d) { vel1[d] = r->vel[d]; om1[d] = r->om[d]; }
-  // translation, RigidAuxRoutines.f90:218-225
-  double pre_fac = 1.0 / Volume / dens_ratio;
-  for (int i = 0; i < 3; ++i)
-    vel[i] = vel1[i] + ga * dt * pre_fac * (-prn[i] + tau[i]) + ro * dt * pre_fac * (-prn1[i] + tau1[i]) +
-             al * dt * (1.0 - (1.0 / dens_ratio)) * e_z[i];
-  for (int i = 0; i < 3; ++i) pos[i] = pos1[i] + 0.5 * al * dt * (vel[i] + vel1[i]);
+  if (lane < 9) { I[lane] = geom[6 + lane]; I_LHS[lane] = geom[6 + lane]; }
+  if (lane < 3) { vel1[lane] = r->vel[lane]; om1[lane] = r->om[lane]; }
+  if (lane < 4) quat[lane] = 0.0;
+  if (lane == 0) singular = 0;
+  __syncwarp();
+  // translation, RigidAuxRoutines.f90:218-225 (lane i: component i)
+  double vel = 0.0, pos = 0.0;
+  if (lane < 3) {
+    const double e_z = lane == 2 ? -1.0 : 0.0;
+    const double pre_fac = 1.0 / geom[2] / dens_ratio;
+    vel = vel1[lane] + ga * dt * pre_fac * (-prn[lane] + tau[lane]) + ro * dt * pre_fac * (-prn1[lane] + tau1[lane]) +
+          al * dt * (1.0 - (1.0 / dens_ratio)) * e_z;
+    pos = geom[3 + lane] + 0.5 * al * dt * (vel + vel1[lane]);
+  }
   // rotation: iterative inertia-tensor update, RigidAuxRoutines.f90:243-296
   const double tolerance = 1.e-15;
   const int max_iter = 10000;
-  double I_LHS[9], I_prev[9], I_inv[9], AA[9], buf[9];
-  for (int q = 0; q < 9; ++q) I_LHS[q] = I[q];
   double Iresidual = 1.0;
   int n_iter = 1;
   while (n_iter <= max_iter && Iresidual > tolerance) {
-    for (int q = 0; q < 9; ++q) I_inv[q] = I_LHS[q];
-    if (!inv3(I_inv)) { atomicOr(flag, 2); return; }
-    double rhs[3];
-    for (int i = 0; i < 3; ++i) {
-      double m = 0.0;
-      for (int j = 0; j < 3; ++j) m += I[i + 3 * j] * om1[j];
-      rhs[i] = m + ga * dt * (-rprn[i] + rtau[i]) + ro * dt * (-rprn1[i] + rtau1[i]);
+    if (lane == 0) {
+      double a[9];
+      for (int q = 0; q < 9; ++q) a[q] = I_LHS[q];
+      if (!inv3(a)) singular = 1;
+      for (int q = 0; q < 9; ++q) I_inv[q] = a[q];
     }
-    for (int i = 0; i < 3; ++i) {
+    __syncwarp();
+    if (singular) { if (lane == 0) atomicOr(flag, 2); return; }
+    if (lane < 3) {
       double m = 0.0;
-      for (int j = 0; j < 3; ++j) m += I_inv[i + 3 * j] * rhs[j];
-      om[i] = m;
+      for (int j = 0; j < 3; ++j) m += I[lane + 3 * j] * om1[j];
+      rhs[lane] = m + ga * dt * (-rprn[lane] + rtau[lane]) + ro * dt * (-rprn1[lane] + rtau1[lane]);
     }
-    double ob[3];
-    for (int i = 0; i < 3; ++i) ob[i] = 0.5 * (om[i] + om1[i]);
-    double magOM = sqrt(ob[0] * ob[0] + ob[1] * ob[1] + ob[2] * ob[2]);
-    double angle = magOM * al * dt;
-    if (magOM < tolerance) { ob[0] = 0.0; ob[1] = 0.0; ob[2] = 0.0; }
-    else for (int i = 0; i < 3; ++i) ob[i] = ob[i] / magOM;
-    double ch = cos(0.5 * angle), sh = sin(0.5 * angle);
-    quat[0] = ch; quat[1] = sh * ob[0]; quat[2] = sh * ob[1]; quat[3] = sh * ob[2];
-    double qn = sqrt(quat[0] * quat[0] + quat[1] * quat[1] + quat[2] * quat[2] + quat[3] * quat[3]);
-    for (int i = 0; i < 4; ++i) quat[i] = quat[i] / qn;
-    rot_matrix(quat, AA);
-    for (int q = 0; q < 9; ++q) I_prev[q] = I_LHS[q];
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) {
-        double m = 0.0;
-        for (int k = 0; k < 3; ++k) m += I[i + 3 * k] * AA[j + 3 * k];
-        buf[i + 3 * j] = m;
+    __syncwarp();
+    if (lane < 3) {
+      double m = 0.0;
+      for (int j = 0; j < 3; ++j) m += I_inv[lane + 3 * j] * rhs[j];
+      om[lane] = m;
+      ob[lane] = 0.5 * (m + om1[lane]);
+    }
+    __syncwarp();
+    if (lane == 0) {
+      const double magOM = sqrt(ob[0] * ob[0] + ob[1] * ob[1] + ob[2] * ob[2]);
+      sc[0] = magOM;
+      sc[1] = magOM * al * dt;
+    }
+    __syncwarp();
+    const double magOM = sc[0], angle = sc[1];
+    if (lane < 3) ob[lane] = magOM < tolerance ? 0.0 : ob[lane] / magOM;
+    if (lane == 3) sc[2] = cos(0.5 * angle);
+    if (lane == 4) sc[3] = sin(0.5 * angle);
+    __syncwarp();
+    if (lane < 4) quat[lane] = lane == 0 ? sc[2] : sc[3] * ob[lane - 1];
+    __syncwarp();
+    // two normalisations, as the reference: quat / |quat|, then calc_rot_matrix's own
+    for (int pass = 0; pass < 2; ++pass) {
+      if (lane == 0) qn_s = sqrt(quat[0] * quat[0] + quat[1] * quat[1] + quat[2] * quat[2] + quat[3] * quat[3]);
+      __syncwarp();
+      const double qn = qn_s;
+      __syncwarp();
+      if (lane < 4) quat[lane] = quat[lane] / qn;
+      __syncwarp();
+    }
+    if (lane < 9) {
+      const double q0 = quat[0], q1 = quat[1], q2 = quat[2], q3 = quat[3];
+      double v;
+      switch (lane) {
+        case 0: v = q0 * q0 + q1 * q1 - q2 * q2 - q3 * q3; break;
+        case 3: v = 2.0 * (q1 * q2 + q0 * q3); break;
+        case 6: v = 2.0 * (q1 * q3 - q0 * q2); break;
+        case 1: v = 2.0 * (q1 * q2 - q0 * q3); break;
+        case 4: v = q0 * q0 - q1 * q1 + q2 * q2 - q3 * q3; break;
+        case 7: v = 2.0 * (q2 * q3 + q0 * q1); break;
+        case 2: v = 2.0 * (q1 * q3 + q0 * q2); break;
+        case 5: v = 2.0 * (q2 * q3 - q0 * q1); break;
+        default: v = q0 * q0 - q1 * q1 - q2 * q2 + q3 * q3; break;
       }
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) {
-        double m = 0.0;
-        for (int k = 0; k < 3; ++k) m += AA[i + 3 * k] * buf[k + 3 * j];
-        I_LHS[i + 3 * j] = m;
-      }
-    Iresidual = 0.0;
-    for (int q = 0; q < 9; ++q) Iresidual = fmax(Iresidual, fabs(I_LHS[q] - I_prev[q]));
+      AA[lane] = v;
+    }
+    __syncwarp();
+    const int i = lane % 3, j = lane / 3;
+    double prev = 0.0;
+    if (lane < 9) {
+      prev = I_LHS[lane];
+      double m = 0.0;
+      for (int k = 0; k < 3; ++k) m += I[i + 3 * k] * AA[j + 3 * k];
+      buf[lane] = m;
+    }
+    __syncwarp();
+    double d = 0.0;
+    if (lane < 9) {        // each lane reads and writes only its own entry of I_LHS here
+      double m = 0.0;
+      for (int k = 0; k < 3; ++k) m += AA[i + 3 * k] * buf[k + 3 * j];
+      d = fabs(m - prev);
+      I_LHS[lane] = m;
+    }
+    // residual: the maximum of the nine |changes| (fmax is exact, so the order is immaterial)
+    for (int off = 16; off > 0; off >>= 1) d = fmax(d, __shfl_xor_sync(FULL, d, off));
+    Iresidual = d;
     ++n_iter;
+    __syncwarp();
   }
   // periodicity corrections, RigidAuxRoutines.f90:40-51
-  const double L[3] = {xlen, ylen, zlen};
-  for (int d = 0; d < 3; ++d) {
-    if (pos[d] < 0.) pos[d] = pos[d] + L[d];
-    if (pos[d] > L[d]) pos[d] = pos[d] - L[d];
+  if (lane < 3) {
+    const double L = lane == 0 ? xlen : (lane == 1 ? ylen : zlen);
+    if (pos < 0.) pos = pos + L;
+    if (pos > L) pos = pos - L;
+    r->vel[lane] = vel;
+    r->om[lane] = om[lane];
+    r->xf[9 + lane] = pos;
+    r->xf[12 + lane] = geom[3 + lane];
   }
-  // update_xyz re-derives AA from the stored quaternion
-  rot_matrix(quat, AA);
-  for (int d = 0; d < 3; ++d) { r->vel[d] = vel[d]; r->om[d] = om[d]; }
-  for (int q = 0; q < 4; ++q) r->quat[q] = quat[q];
-  for (int q = 0; q < 9; ++q) { r->inert[q] = I_LHS[q]; r->xf[q] = AA[q]; }
-  for (int d = 0; d < 3; ++d) { r->xf[9 + d] = pos[d]; r->xf[12 + d] = pos1[d]; }
-  r->iters = n_iter - 1;
+  // update_xyz re-derives AA from the stored quaternion, which that call
+  // normalises once more in place
+  if (lane == 0) {
+    double q[4] = {quat[0], quat[1], quat[2], quat[3]}, A[9];
+    rot_matrix(q, A);
+    for (int k = 0; k < 4; ++k) r->quat[k] = q[k];
+    for (int k = 0; k < 9; ++k) { r->inert[k] = I_LHS[k]; r->xf[k] = A[k]; }
+    r->iters = n_iter - 1;
+  }
 }
 
 // update_xyz (RigidAuxRoutines.f90:818-868): vertices turned by AA^T about
