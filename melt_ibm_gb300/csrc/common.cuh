@@ -144,7 +144,7 @@ struct Ctx {
   // published rigid-body state (ev_pub) and the VOF fields (ev_tjoin when the
   // tagging ran on its own stream); the cage indices, MLS weights and scatter
   // plan (ev_join) are waited for only before the forcing
-  cudaEvent_t ev_pub = nullptr;
+  cudaEvent_t ev_pub = nullptr, ev_gfork = nullptr;
   bool geom_join_pending = false, geom_join_tag = false;
   cudaEvent_t ev_lfork = nullptr, ev_ldone = nullptr;   // structural loads on the side stream
   cudaStream_t side2 = nullptr;                         // narrow-band tagging beside the MLS weights and plan

@@ -295,6 +295,7 @@ void release(Ctx* c) {
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
   if (c->ev_pub) cudaEventDestroy(c->ev_pub);
+  if (c->ev_gfork) cudaEventDestroy(c->ev_gfork);
   if (c->ev_lfork) cudaEventDestroy(c->ev_lfork);
   if (c->ev_ldone) cudaEventDestroy(c->ev_ldone);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -325,6 +326,7 @@ int mibm_context_create_(void) {
       !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "event") ||
       !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming), "event") ||
       !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_pub, cudaEventDisableTiming), "event") ||
+      !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_gfork, cudaEventDisableTiming), "event") ||
       !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_lfork, cudaEventDisableTiming), "event") ||
       !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_ldone, cudaEventDisableTiming), "event")) {
     t_cur = c;

@@ -1904,26 +1904,35 @@ void lagr_stefan(Ctx* c, const StepParams* dp) {
 // the Newton-Euler update (particle.f90:108-117: centroids, normals,
 // volume, centre of mass and inertia tensor of the melted body); it also
 // rewrites `sur`, which nothing reads before the full refresh recomputes it.
-static void geometry_launch(Ctx* c, bool imelt, bool body_only = false) {
+// kGeomFaces: the per-face pass alone (areas, normals, centroids and the
+// block sums); kGeomRest: what follows it (vertex areas and normals, the
+// body's sums, edge lengths, skewness, cfac)
+enum GeomPart { kGeomAll, kGeomFaces, kGeomRest };
+
+static void geometry_launch(Ctx* c, bool imelt, bool body_only = false, GeomPart part = kGeomAll) {
   LagState* s = lag_of(c);
-  { MIBM_PROF(c, "face_geom");
-    face_geom_kernel<<<div_up(c->maxnf, kGeomBlock), kGeomBlock, 0, c->stream>>>(
-        c->maxnf, M<int>(c, MIBM_M_VERT_OF_FACE), M<int>(c, MIBM_M_GHOST_FACE), M<double>(c, MIBM_M_XYZV),
-        M<double>(c, MIBM_M_SUR), M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_TRI_BAR), s->face_part); }
+  if (part != kGeomRest) {
+    { MIBM_PROF(c, "face_geom");
+      face_geom_kernel<<<div_up(c->maxnf, kGeomBlock), kGeomBlock, 0, c->stream>>>(
+          c->maxnf, M<int>(c, MIBM_M_VERT_OF_FACE), M<int>(c, MIBM_M_GHOST_FACE), M<double>(c, MIBM_M_XYZV),
+          M<double>(c, MIBM_M_SUR), M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_TRI_BAR), s->face_part); }
+    ++c->launches;
+  }
   const int gnb = (int)div_up(c->maxnf, kGeomBlock);
   if (body_only) {
     { MIBM_PROF(c, "geom_reduce");
       geom_reduce_kernel<<<1, 256, 0, c->stream>>>(gnb, s->face_part, c->S(MIBM_S_DENS_RATIO), s->geom_out); }
-    c->launches += 2;
+    c->launches += 1;
     return;
   }
+  if (part == kGeomFaces) return;
   { MIBM_PROF(c, "vert_geom");
     vert_geom_kernel<<<div_up(c->maxnv, 128), 128, 0, c->stream>>>(
         c->maxnv, s->adj_off, s->adj_face, M<int>(c, MIBM_M_GHOST_VERT), M<double>(c, MIBM_M_SUR),
         M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_AVERT), M<double>(c, MIBM_M_VERT_NOR)); }
   { MIBM_PROF(c, "geom_reduce");
     geom_reduce_kernel<<<1, 256, 0, c->stream>>>(gnb, s->face_part, c->S(MIBM_S_DENS_RATIO), s->geom_out); }
-  c->launches += 3;
+  c->launches += 2;
   if (c->maxne > 0) {           // calculate_eLengths, calculate_skewness (particle.f90:173-176)
     MIBM_PROF(c, "edges");
     elength_kernel<<<div_up(c->maxne, 128), 128, 0, c->stream>>>(
@@ -2331,7 +2340,24 @@ const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror,
   if (imelt) lagr_stefan(c, dp);
   if (str) motion_launch(c, dp);
   bool remeshed = !fork && lagr_remesh_active(c) && remesh_check(c);
-  if (c->status == MIBM_OK) {
+  if (c->status == MIBM_OK && fork && next_prologue >= 0 && c->side3) {
+    // the next substep's geometry-only work needs the new face centroids and
+    // normals alone: it starts after the per-face pass, while a third stream
+    // finishes the refresh and publishes the moved body (ev_pub)
+    geometry_launch(c, imelt, false, kGeomFaces);
+    cudaEventRecord(c->ev_gfork, c->stream);
+    cudaStreamWaitEvent(c->side3, c->ev_gfork, 0);
+    std::swap(c->stream, c->side3);
+    geometry_launch(c, imelt, false, kGeomRest);
+    if (str) k_rigid_publish(c, s->geom_out, next);
+    cudaEventRecord(c->ev_pub, c->stream);
+    std::swap(c->stream, c->side3);
+    c->geom_join_tag = false;
+    lagr_substep_prologue(c, next_prologue);
+    c->prologue_done = true;
+    cudaStreamWaitEvent(c->stream, c->ev_pub, 0);     // the full join covers the refresh
+    MIBM_LAUNCH_CHECK(c, "particle");
+  } else if (c->status == MIBM_OK) {
     geometry_launch(c, imelt);
     if (remeshed) {
       const double *vel, *om;
