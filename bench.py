@@ -102,6 +102,12 @@ ALGO_PASSES = {
 # dram__bytes_write.sum, one pass) for the kernel that dominates the FP64
 # step, at the size given, per cell: profiles/fused_rhs_melt128_fp64_dram.md.
 # Other sizes scale by the cell count (the traffic is per-cell compulsory).
+# FP64 warp instructions of one step (ncu sm__inst_executed_pipe_fp64.sum over
+# every kernel of the step; profiles/fp64_census_melt128_c1.md).  The FP64
+# form is bounded by the FP64 issue rate (one warp instruction per 16 clocks
+# per SM on this part): this count over that rate is the step's FP64 floor.
+FP64_CENSUS = {"melt128_c1": {"warp_instructions_per_step": 66.4e6, "clocks_per_instruction_per_sm": 16}}
+
 NCU_TRAFFIC = {
     "fused_rhs": {"bytes_per_cell": 139.6e6 / 128 ** 3, "measured_at": "128^3 (melt128_c1)"},
 }
@@ -414,6 +420,17 @@ def run_gpu(args):
             "roofline": roofline, "gpu_launches": launches, "clocks": clocks, "fp32_refined": fp32,
             "diagnostics": diagnostics,
             "host_wall_ms_per_step": 1e3 * wall / args.steps, "kernels": kernels}
+    census = FP64_CENSUS.get(args.workload)
+    if census is not None and clocks and clocks.get("sm_mhz"):
+        import torch
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        floor_ms = (census["warp_instructions_per_step"] * census["clocks_per_instruction_per_sm"]
+                    / (sms * clocks["sm_mhz"] * 1e6) * 1e3)
+        line["fp64_issue"] = {"bound": "fp64", "step_floor_ms": floor_ms, "step_ms": ms_max / args.steps,
+                              "frac": floor_ms / (ms_max / args.steps),
+                              "warp_instructions_per_step": census["warp_instructions_per_step"],
+                              "source": "ncu FP64 warp-instruction census of this workload "
+                                        "(profiles/fp64_census_melt128_c1.md) at the sampled SM clock"}
     if dist.ws == 1 and not args.no_batch:
         line["batched"] = batched_measurement(lib, args.batch_steps, args.warmup)
     if dist.ws == 1 and not args.no_serve:
