@@ -321,6 +321,7 @@ void k_add_field(Ctx* c, double* q, const double* r);
 double k_cfl(Ctx* c);
 void k_cfl_async(Ctx* c, double* out);
 bool fft_prepare(Ctx* c, bool f32);
+void tri_build_table(int n, double betadx, std::vector<double>& t);
 bool cfl_finite(Ctx* c);
 void k_getdt_async(Ctx* c, double dt, double* out);
 double cfl_value(double reduced);

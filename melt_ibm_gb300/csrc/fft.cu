@@ -234,6 +234,9 @@ struct FftCache {
   float *fak1 = nullptr, *fak2 = nullptr, *fak3 = nullptr;
   double* eig = nullptr;    // FftArgs::eig, FP64 (built at the first FP64 solve)
   float* feig = nullptr;    // the same rounded to FP32 (first FP32 solve)
+  double* ztri = nullptr;   // FftArgs::ztri, FP64
+  float* fztri = nullptr;   // the same rounded to FP32
+  int zt_lines = 0;
 };
 static std::vector<FftCache> g_fft;
 
@@ -251,6 +254,65 @@ __global__ void eig_kernel(Grid g, const double* __restrict__ ak1, const double*
     if (out) out[t] = f;
     if (fout) fout[t] = (float)f;
   }
+}
+
+// z-line tables.  After the x and y transforms, the z pass solves, for each
+// line (kx, ky), (D_zz - lambda) phi = r with D_zz = dx3q (phi[k+1] - 2 phi[k]
+// + phi[k-1]) periodic and lambda = ak1(kx) + ak2(ky): in Fourier space along z
+// that is the division of phcalc.f90:57 (the eigenvalues of D_zz are -ak3,
+// phini.f90:28-56), so the periodic tridiagonal solve gives the same phi.  It
+// costs 10 FP64 operations per complex value against about 45 for the forward
+// transform, division and inverse.  D_zz - lambda = -(2 dx3q + lambda) (I -
+// rho (S + S^-1)), rho = dx3q / (2 dx3q + lambda), is the system the line
+// solver's tables factor (tridiag_periodic.f90) with betadx = dx3q / lambda;
+// its solution times -1/lambda, and the n3m / (n1m n2m n3m) of the unscaled
+// transforms, is folded into the right-hand-side factors.  ak2(ky) =
+// ak2(n2m - ky), so lines ky and n2m - ky share a table.  The line
+// kx = ky = 0 (lambda = 0, singular; its mean is the zero mode set to 0,
+// phcalc.f90:65) keeps the transform.  Layout, NT = H (n2m/2 + 1) lines,
+// lt = kx + H min(ky, n2m - ky): arrays a, b, q, s at e*NT + lt (offsets 0,
+// n, 2n, 3n times NT), then 4 scalars per line (ackl_b, api, ami, 1/den).
+static bool make_ztri(Ctx* c, FftCache* f, bool f32) {
+  if (f32 ? f->fztri != nullptr : f->ztri != nullptr) return true;
+  const Grid& g = c->g;
+  const int n = g.n3m, H = g.H, NT = H * (g.n2m / 2 + 1);
+  const size_t NS = (size_t)n * NT, len = 4 * NS + 4 * (size_t)NT;
+  std::vector<double> ak1(g.n1m), ak2(g.n2m);
+  if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "z-line tables")) return false;   // ak1/ak2 uploads
+  cudaMemcpy(ak1.data(), c->ak1, sizeof(double) * g.n1m, cudaMemcpyDeviceToHost);
+  cudaMemcpy(ak2.data(), c->ak2, sizeof(double) * g.n2m, cudaMemcpyDeviceToHost);
+  std::vector<double> tab(len, 0.0), t;
+  const double nfac = (double)n / ((double)g.n1m * (double)g.n2m * (double)g.n3m);
+  for (int kyr = 0; kyr <= g.n2m / 2; ++kyr)
+    for (int kx = 0; kx < H; ++kx) {
+      const int lt = kx + H * kyr;
+      const double lambda = ak1[kx] + ak2[kyr];
+      if (kx == 0 && kyr == 0) continue;                 // the zero line: transform path
+      tri_build_table(n, g.dx3q / lambda, t);
+      const double sigma = -(1.0 / lambda) * nfac;
+      for (int e = 0; e < n; ++e) {
+        tab[(size_t)e * NT + lt] = t[e] * sigma;
+        tab[NS + (size_t)e * NT + lt] = t[n + e];
+        tab[2 * NS + (size_t)e * NT + lt] = t[2 * n + e];
+        tab[3 * NS + (size_t)e * NT + lt] = t[3 * n + e];
+      }
+      tab[4 * NS + 4 * (size_t)lt + 0] = t[4 * n + 0] * sigma;
+      tab[4 * NS + 4 * (size_t)lt + 1] = t[4 * n + 1];
+      tab[4 * NS + 4 * (size_t)lt + 2] = t[4 * n + 2];
+      tab[4 * NS + 4 * (size_t)lt + 3] = t[4 * n + 3];
+    }
+  void* p = nullptr;
+  if (!cuda_ok(c, cudaMalloc(&p, len * (f32 ? sizeof(float) : sizeof(double))), "z-line tables")) return false;
+  if (f32) {
+    std::vector<float> tf(tab.begin(), tab.end());
+    cudaMemcpy(p, tf.data(), len * sizeof(float), cudaMemcpyHostToDevice);
+    f->fztri = (float*)p;
+  } else {
+    cudaMemcpy(p, tab.data(), len * sizeof(double), cudaMemcpyHostToDevice);
+    f->ztri = (double*)p;
+  }
+  f->zt_lines = NT;
+  return true;
 }
 
 static bool make_eig(Ctx* c, FftCache* f, bool f32) {
@@ -317,7 +379,7 @@ void fft_free(Ctx* c) {
       cudaFree(f.twx); cudaFree(f.twy); cudaFree(f.twz);
       cudaFree(f.ftwx); cudaFree(f.ftwy); cudaFree(f.ftwz);
       cudaFree(f.fak1); cudaFree(f.fak2); cudaFree(f.fak3);
-      cudaFree(f.eig); cudaFree(f.feig);
+      cudaFree(f.eig); cudaFree(f.feig); cudaFree(f.ztri); cudaFree(f.fztri);
       g_fft.erase(g_fft.begin() + q);
       return;
     }
@@ -327,7 +389,7 @@ void fft_free(Ctx* c) {
 // launched (and possibly captured into a graph).
 bool fft_prepare(Ctx* c, bool f32) {
   FftCache* fc = fft_of(c);
-  return make_eig(c, fc, f32);
+  return make_eig(c, fc, f32) && make_ztri(c, fc, f32);
 }
 
 template <typename C, typename S>
@@ -370,8 +432,9 @@ void k_phcalc(Ctx* c) {
   F.twx = fc->twx; F.twy = fc->twy; F.twz = fc->twz;
   F.ak1 = c->ak1; F.ak2 = c->ak2; F.ak3 = c->ak3;
   F.inv_nn = 1.0 / ((double)g.n1m * (double)g.n2m * (double)g.n3m);
-  if (!make_eig(c, fc, false)) return;
+  if (!make_eig(c, fc, false) || !make_ztri(c, fc, false)) return;
   F.eig = fc->eig;
+  F.ztri = fc->ztri; F.zt_lines = fc->zt_lines;
   phcalc_launch<double2, double>(c, F, c->df[MIBM_F_DPH], c->df[MIBM_F_DPH], "phcalc");
 }
 
@@ -387,8 +450,9 @@ void k_phcalc_f32(Ctx* c, const float* src, float* phi) {
   F.twx = fc->ftwx; F.twy = fc->ftwy; F.twz = fc->ftwz;
   F.ak1 = fc->fak1; F.ak2 = fc->fak2; F.ak3 = fc->fak3;
   F.inv_nn = (float)(1.0 / ((double)g.n1m * (double)g.n2m * (double)g.n3m));
-  if (!make_eig(c, fc, true)) return;
+  if (!make_eig(c, fc, true) || !make_ztri(c, fc, true)) return;
   F.eig = fc->feig;
+  F.ztri = fc->fztri; F.zt_lines = fc->zt_lines;
   phcalc_launch<float2, float>(c, F, src, phi, "phcalc_f32");
 }
 

@@ -49,6 +49,9 @@ struct FftArgs {
   // zero mode: the scale and the eigenvalue division of the z pass as one
   // multiply (an FP64 division is a long sequence of FP64 operations)
   const R* eig;
+  // z-line solve tables (fft.cu make_ztri), nullptr: z passes by FFT
+  const R* ztri;
+  int zt_lines;
 };
 
 template <typename C>

@@ -327,6 +327,64 @@ z_solve(FftArgs<C> F, C* __restrict__ spec, int kx_base) {
   store_cols<C, N, LONE>(buf, spec, base, zstride, nc);
 }
 
+// Z pass as a periodic tridiagonal solve per (kx, ky) line (fft.cu
+// make_ztri): a block of 32 lines (one warp, lines numbered kx fastest so
+// that the warp's accesses are adjacent) stages its lines in shared memory
+// with independent loads, runs the sweeps of tridiag_periodic.f90 with each
+// line's factors from there (one thread per line, real and imaginary parts
+// together), and writes them back.  The line kx = ky = 0 is left to the
+// transform kernel.  Shared memory: 32 lines x n3m complex values.
+template <typename C>
+__global__ void __launch_bounds__(32) z_tri(FftArgs<C> F, C* __restrict__ spec) {
+  typedef typename Real<C>::T R;
+  extern __shared__ __align__(16) unsigned char shraw[];
+  C* buf = (C*)shraw;                       // buf[e * 32 + lane]
+  const Grid& g = F.g;
+  const int n = g.n3m, H = g.H, NT = F.zt_lines;
+  const int lane = threadIdx.x;
+  const int l = blockIdx.x * 32 + lane;
+  const bool live = l < H * g.n2m;
+  const int kx = live ? l % H : 0, ky = live ? l / H : 0;
+  const size_t st = (size_t)g.HP * g.n2m;
+  C* __restrict__ base = spec + kx + (size_t)g.HP * ky;
+  for (int e = 0; e < n; ++e) buf[e * 32 + lane] = live ? base[(size_t)e * st] : C{};
+  if (!live || (kx == 0 && ky == 0)) return;
+  const int lt = kx + H * (ky <= g.n2m - ky ? ky : g.n2m - ky);
+  const size_t NS = (size_t)n * NT;
+  const R* __restrict__ a = F.ztri + lt;
+  const R* __restrict__ b = a + NS;
+  const R* __restrict__ q = a + 2 * NS;
+  const R* __restrict__ s = a + 3 * NS;
+  const R* __restrict__ sc = F.ztri + 4 * NS + 4 * (size_t)lt;
+  const R ackl = sc[0], api = sc[1], ami = sc[2], inv_den = sc[3];
+  C* x = buf + lane;
+  const C rn = x[(n - 1) * 32];
+  C y;
+  { const C r = x[0]; y = mk<C>(a[0] * r.x, a[0] * r.y); x[0] = y; }
+  for (int e = 1; e < n - 1; ++e) {
+    const C r = x[e * 32];
+    const R ae = a[(size_t)e * NT], be = b[(size_t)e * NT];
+    y = mk<C>(ae * r.x - be * y.x, ae * r.y - be * y.y);
+    x[e * 32] = y;
+  }
+  C f = mk<C>(R(0), R(0));
+  for (int e = n - 2; e >= 0; --e) {
+    const C yy = x[e * 32];
+    const R qe = q[(size_t)e * NT];
+    f = mk<C>(yy.x + qe * f.x, yy.y + qe * f.y);
+    x[e * 32] = f;
+  }
+  const C f1 = x[0], fnm1 = x[(n - 2) * 32];
+  const C xn = mk<C>((rn.x * ackl - api * f1.x - ami * fnm1.x) * inv_den,
+                     (rn.y * ackl - api * f1.y - ami * fnm1.y) * inv_den);
+  for (int e = 0; e < n - 1; ++e) {
+    const C v = x[e * 32];
+    const R se = s[(size_t)e * NT];
+    base[(size_t)e * st] = mk<C>(xn.x * se + v.x, xn.y * se + v.y);
+  }
+  base[(size_t)(n - 1) * st] = xn;
+}
+
 // shared-memory opt-in for the instances above the default 48 KB
 template <typename K>
 inline bool smem_attr(Ctx* c, K kern, size_t bytes) {
@@ -387,6 +445,14 @@ void launch_z(Ctx* c, const FftArgs<C>& F, C* spec) {
   auto k = z_solve<C, N>;
   auto k1 = z_solve<C, N, 1>;
   if (!smem_attr(c, k, Sh::smem) || !smem_attr(c, k1, S1::smem)) return;
+  const size_t tri_smem = sizeof(C) * 32 * (size_t)N;
+  if (F.ztri && N >= 3 && tri_smem <= 200 * 1024 && smem_attr(c, z_tri<C>, tri_smem)) {
+    // tridiagonal lines, and the zero line by transform
+    z_tri<C><<<div_up((size_t)c->g.H * c->g.n2m, 32), 32, tri_smem, c->stream>>>(F, spec);
+    k1<<<dim3(1, 1), S1::T, S1::smem, c->stream>>>(F, spec, 0);
+    ++c->launches;                 // the caller counts one launch per pass
+    return;
+  }
   const int tiles = c->g.H / Sh::L, rest = c->g.H - tiles * Sh::L;
   if (tiles > 0) k<<<dim3(tiles, c->g.n2m), Sh::T, Sh::smem, c->stream>>>(F, spec, 0);
   if (rest > 0) {

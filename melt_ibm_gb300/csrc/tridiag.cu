@@ -78,6 +78,10 @@ static void build_table(int n, double betadx, std::vector<double>& t) {
   t[4 * n + 3] = 1.0 / den;
 }
 
+// the factor table of build_table for callers outside this file (the z-line
+// Poisson solve of fft.cu)
+void tri_build_table(int n, double betadx, std::vector<double>& t) { build_table(n, betadx, t); }
+
 static size_t slot_len(int nmax);
 static void fill_slot(int n, int m, double betadx, double* out);
 int tri_chunk(Ctx* c, int dir);
