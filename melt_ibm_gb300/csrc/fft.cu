@@ -389,7 +389,7 @@ void fft_free(Ctx* c) {
 // launched (and possibly captured into a graph).
 bool fft_prepare(Ctx* c, bool f32) {
   FftCache* fc = fft_of(c);
-  return make_eig(c, fc, f32) && make_ztri(c, fc, f32);
+  return make_eig(c, fc, f32) && (f32 || make_ztri(c, fc, false));
 }
 
 template <typename C, typename S>
@@ -450,9 +450,11 @@ void k_phcalc_f32(Ctx* c, const float* src, float* phi) {
   F.twx = fc->ftwx; F.twy = fc->ftwy; F.twz = fc->ftwz;
   F.ak1 = fc->fak1; F.ak2 = fc->fak2; F.ak3 = fc->fak3;
   F.inv_nn = (float)(1.0 / ((double)g.n1m * (double)g.n2m * (double)g.n3m));
-  if (!make_eig(c, fc, true) || !make_ztri(c, fc, true)) return;
+  if (!make_eig(c, fc, true)) return;
   F.eig = fc->feig;
-  F.ztri = fc->fztri; F.zt_lines = fc->zt_lines;
+  // FP32 transforms cost little on the FP32 pipe: the z pass stays a
+  // transform (the tridiagonal lines are latency-bound and slower there)
+  F.ztri = nullptr; F.zt_lines = 0;
   phcalc_launch<float2, float>(c, F, src, phi, "phcalc_f32");
 }
 

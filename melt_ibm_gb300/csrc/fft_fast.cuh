@@ -359,24 +359,47 @@ __global__ void __launch_bounds__(32) z_tri(FftArgs<C> F, C* __restrict__ spec) 
   const R ackl = sc[0], api = sc[1], ami = sc[2], inv_den = sc[3];
   C* x = buf + lane;
   const C rn = x[(n - 1) * 32];
-  C y;
-  { const C r = x[0]; y = mk<C>(a[0] * r.x, a[0] * r.y); x[0] = y; }
-  for (int e = 1; e < n - 1; ++e) {
-    const C r = x[e * 32];
-    const R ae = a[(size_t)e * NT], be = b[(size_t)e * NT];
-    y = mk<C>(ae * r.x - be * y.x, ae * r.y - be * y.y);
-    x[e * 32] = y;
+  // the factors are read in groups of kG ahead of the recurrence that uses
+  // them, so that their global loads are in flight together
+  constexpr int kG = 8;
+  C y = mk<C>(R(0), R(0));
+  for (int e0 = 0; e0 < n - 1; e0 += kG) {
+    R ae[kG], be[kG];
+#pragma unroll
+    for (int u = 0; u < kG; ++u) {
+      const int e = e0 + u;
+      ae[u] = e < n - 1 ? a[(size_t)e * NT] : R(0);
+      be[u] = (e < n - 1 && e > 0) ? b[(size_t)e * NT] : R(0);
+    }
+#pragma unroll
+    for (int u = 0; u < kG; ++u) {
+      const int e = e0 + u;
+      if (e < n - 1) {
+        const C r = x[e * 32];
+        y = e == 0 ? mk<C>(ae[u] * r.x, ae[u] * r.y) : mk<C>(ae[u] * r.x - be[u] * y.x, ae[u] * r.y - be[u] * y.y);
+        x[e * 32] = y;
+      }
+    }
   }
   C f = mk<C>(R(0), R(0));
-  for (int e = n - 2; e >= 0; --e) {
-    const C yy = x[e * 32];
-    const R qe = q[(size_t)e * NT];
-    f = mk<C>(yy.x + qe * f.x, yy.y + qe * f.y);
-    x[e * 32] = f;
+  for (int e0 = n - 2; e0 >= 0; e0 -= kG) {
+    R qe[kG];
+#pragma unroll
+    for (int u = 0; u < kG; ++u) qe[u] = e0 - u >= 0 ? q[(size_t)(e0 - u) * NT] : R(0);
+#pragma unroll
+    for (int u = 0; u < kG; ++u) {
+      const int e = e0 - u;
+      if (e >= 0) {
+        const C yy = x[e * 32];
+        f = mk<C>(yy.x + qe[u] * f.x, yy.y + qe[u] * f.y);
+        x[e * 32] = f;
+      }
+    }
   }
   const C f1 = x[0], fnm1 = x[(n - 2) * 32];
   const C xn = mk<C>((rn.x * ackl - api * f1.x - ami * fnm1.x) * inv_den,
                      (rn.y * ackl - api * f1.y - ami * fnm1.y) * inv_den);
+#pragma unroll 8
   for (int e = 0; e < n - 1; ++e) {
     const C v = x[e * 32];
     const R se = s[(size_t)e * NT];
