@@ -228,8 +228,7 @@ static void step_enqueue_f64(Ctx* c) {
     if (c->status != MIBM_OK) return;
     k_divg(c, dp);
     k_phcalc(c);
-    k_updvp(c, dp, mean3);
-    k_prcalc(c, dp);
+    k_updvp_prcalc(c, dp, mean3);
     if (c->status != MIBM_OK) return;
   }
 }

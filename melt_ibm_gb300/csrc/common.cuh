@@ -317,6 +317,7 @@ void k_divmax(Ctx* c, unsigned long long* out);
 void k_divg(Ctx* c, const StepParams* dp);
 void k_updvp(Ctx* c, const StepParams* dp, const double* mean3 = nullptr);
 void k_prcalc(Ctx* c, const StepParams* dp);
+void k_updvp_prcalc(Ctx* c, const StepParams* dp, const double* mean3);
 void k_add_field(Ctx* c, double* q, const double* r);
 double k_cfl(Ctx* c);
 void k_cfl_async(Ctx* c, double* out);

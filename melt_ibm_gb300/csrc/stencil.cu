@@ -501,6 +501,25 @@ __global__ void prcalc_kernel(StencilArgs A, const StepParams* __restrict__ pp, 
   pr[c0] = (pr[c0] + pp->cd[kPBC] * d) - t;
 }
 
+// updvp then prcalc of the same substep in one pass (the fused step): both
+// read phi and write disjoint fields; each keeps its own operation order
+__global__ void updvp_prcalc_kernel(StencilArgs A, const StepParams* __restrict__ pp, const double* __restrict__ dph,
+                                    double* __restrict__ vx, double* __restrict__ vy, double* __restrict__ vz,
+                                    const double* __restrict__ mean3, double* __restrict__ pr) {
+  CELL_INDEX
+  const double udx1 = pp->cd[kUP1], udx2 = pp->cd[kUP2], udx3 = pp->cd[kUP3];
+  const double d = dph[c0];
+  const double pim = dph[c0 + dim], pjm = dph[c0 + djm], pkm = dph[c0 + dkm];
+  double mx = 0.0, my = 0.0, mz = 0.0;
+  if (mean3) { mx = mean3[0]; my = mean3[1]; mz = mean3[2]; }
+  vx[c0] = (vx[c0] - mx) - (d - pim) * udx1;
+  vy[c0] = (vy[c0] - my) - (d - pjm) * udx2;
+  vz[c0] = (vz[c0] - mz) - (d - pkm) * udx3;
+  const double t = pp->cd[kPB1] * (dph[c0 + dip] + pim) + pp->cd[kPB2] * (dph[c0 + djp] + pjm) +
+                   pp->cd[kPB3] * (dph[c0 + dkp] + pkm);
+  pr[c0] = (pr[c0] + pp->cd[kPBC] * d) - t;
+}
+
 __global__ void add_kernel(Grid g, double* __restrict__ q, const double* __restrict__ r) {
   size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < g.cells) q[t] = q[t] + r[t];
@@ -814,6 +833,15 @@ void k_divmax(Ctx* c, unsigned long long* out) {
     divmax_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), out); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "divmax");
+}
+
+void k_updvp_prcalc(Ctx* c, const StepParams* dp, const double* mean3) {
+  { MIBM_PROF(c, "updvp_prcalc");
+    updvp_prcalc_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, c->df[MIBM_F_DPH],
+                                                                        c->df[MIBM_F_VX], c->df[MIBM_F_VY],
+                                                                        c->df[MIBM_F_VZ], mean3, c->df[MIBM_F_PR]); }
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "updvp_prcalc");
 }
 
 void k_prcalc(Ctx* c, const StepParams* dp) {
