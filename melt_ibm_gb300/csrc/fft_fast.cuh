@@ -328,27 +328,22 @@ z_solve(FftArgs<C> F, C* __restrict__ spec, int kx_base) {
 }
 
 // Z pass as a periodic tridiagonal solve per (kx, ky) line (fft.cu
-// make_ztri): a block of 32 lines (one warp, lines numbered kx fastest so
-// that the warp's accesses are adjacent) stages its lines in shared memory
-// with independent loads, runs the sweeps of tridiag_periodic.f90 with each
-// line's factors from there (one thread per line, real and imaginary parts
-// together), and writes them back.  The line kx = ky = 0 is left to the
-// transform kernel.  Shared memory: 32 lines x n3m complex values.
+// make_ztri): one thread per line (lines numbered kx fastest, so that a
+// warp's accesses are adjacent), real and imaginary parts together, the
+// sweeps of tridiag_periodic.f90 with the line's factors, in place.  Each
+// sweep moves kG elements and their factors into registers with independent
+// loads before the kG dependent steps that use them.  The line kx = ky = 0 is
+// left to the transform kernel.
 template <typename C>
-__global__ void __launch_bounds__(32) z_tri(FftArgs<C> F, C* __restrict__ spec) {
+__global__ void __launch_bounds__(64) z_tri(FftArgs<C> F, C* __restrict__ spec) {
   typedef typename Real<C>::T R;
-  extern __shared__ __align__(16) unsigned char shraw[];
-  C* buf = (C*)shraw;                       // buf[e * 32 + lane]
+  constexpr int kG = 8;
   const Grid& g = F.g;
   const int n = g.n3m, H = g.H, NT = F.zt_lines;
-  const int lane = threadIdx.x;
-  const int l = blockIdx.x * 32 + lane;
-  const bool live = l < H * g.n2m;
-  const int kx = live ? l % H : 0, ky = live ? l / H : 0;
-  const size_t st = (size_t)g.HP * g.n2m;
-  C* __restrict__ base = spec + kx + (size_t)g.HP * ky;
-  for (int e = 0; e < n; ++e) buf[e * 32 + lane] = live ? base[(size_t)e * st] : C{};
-  if (!live || (kx == 0 && ky == 0)) return;
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= H * g.n2m) return;
+  const int kx = l % H, ky = l / H;
+  if (kx == 0 && ky == 0) return;
   const int lt = kx + H * (ky <= g.n2m - ky ? ky : g.n2m - ky);
   const size_t NS = (size_t)n * NT;
   const R* __restrict__ a = F.ztri + lt;
@@ -357,53 +352,70 @@ __global__ void __launch_bounds__(32) z_tri(FftArgs<C> F, C* __restrict__ spec) 
   const R* __restrict__ s = a + 3 * NS;
   const R* __restrict__ sc = F.ztri + 4 * NS + 4 * (size_t)lt;
   const R ackl = sc[0], api = sc[1], ami = sc[2], inv_den = sc[3];
-  C* x = buf + lane;
-  const C rn = x[(n - 1) * 32];
-  // the factors are read in groups of kG ahead of the recurrence that uses
-  // them, so that their global loads are in flight together
-  constexpr int kG = 8;
+  C* __restrict__ base = spec + kx + (size_t)g.HP * ky;
+  const size_t st = (size_t)g.HP * g.n2m;
+  const C rn = base[(size_t)(n - 1) * st];
   C y = mk<C>(R(0), R(0));
   for (int e0 = 0; e0 < n - 1; e0 += kG) {
+    C r[kG];
     R ae[kG], be[kG];
 #pragma unroll
     for (int u = 0; u < kG; ++u) {
       const int e = e0 + u;
-      ae[u] = e < n - 1 ? a[(size_t)e * NT] : R(0);
-      be[u] = (e < n - 1 && e > 0) ? b[(size_t)e * NT] : R(0);
+      const bool ok = e < n - 1;
+      r[u] = ok ? base[(size_t)e * st] : C{};
+      ae[u] = ok ? a[(size_t)e * NT] : R(0);
+      be[u] = (ok && e > 0) ? b[(size_t)e * NT] : R(0);
     }
 #pragma unroll
     for (int u = 0; u < kG; ++u) {
       const int e = e0 + u;
       if (e < n - 1) {
-        const C r = x[e * 32];
-        y = e == 0 ? mk<C>(ae[u] * r.x, ae[u] * r.y) : mk<C>(ae[u] * r.x - be[u] * y.x, ae[u] * r.y - be[u] * y.y);
-        x[e * 32] = y;
+        y = e == 0 ? mk<C>(ae[u] * r[u].x, ae[u] * r[u].y)
+                   : mk<C>(ae[u] * r[u].x - be[u] * y.x, ae[u] * r[u].y - be[u] * y.y);
+        base[(size_t)e * st] = y;
       }
     }
   }
   C f = mk<C>(R(0), R(0));
+  C xnm1 = f;                                          // element n-2 after the backward sweep
   for (int e0 = n - 2; e0 >= 0; e0 -= kG) {
+    C yy[kG];
     R qe[kG];
 #pragma unroll
-    for (int u = 0; u < kG; ++u) qe[u] = e0 - u >= 0 ? q[(size_t)(e0 - u) * NT] : R(0);
+    for (int u = 0; u < kG; ++u) {
+      const int e = e0 - u;
+      yy[u] = e >= 0 ? base[(size_t)e * st] : C{};
+      qe[u] = e >= 0 ? q[(size_t)e * NT] : R(0);
+    }
 #pragma unroll
     for (int u = 0; u < kG; ++u) {
       const int e = e0 - u;
       if (e >= 0) {
-        const C yy = x[e * 32];
-        f = mk<C>(yy.x + qe[u] * f.x, yy.y + qe[u] * f.y);
-        x[e * 32] = f;
+        f = mk<C>(yy[u].x + qe[u] * f.x, yy[u].y + qe[u] * f.y);
+        base[(size_t)e * st] = f;
+        if (e == n - 2) xnm1 = f;
       }
     }
   }
-  const C f1 = x[0], fnm1 = x[(n - 2) * 32];
-  const C xn = mk<C>((rn.x * ackl - api * f1.x - ami * fnm1.x) * inv_den,
-                     (rn.y * ackl - api * f1.y - ami * fnm1.y) * inv_den);
-#pragma unroll 8
-  for (int e = 0; e < n - 1; ++e) {
-    const C v = x[e * 32];
-    const R se = s[(size_t)e * NT];
-    base[(size_t)e * st] = mk<C>(xn.x * se + v.x, xn.y * se + v.y);
+  const C f1 = f;                                      // element 0 after the backward sweep
+  const C xn = mk<C>((rn.x * ackl - api * f1.x - ami * xnm1.x) * inv_den,
+                     (rn.y * ackl - api * f1.y - ami * xnm1.y) * inv_den);
+  for (int e0 = 0; e0 < n - 1; e0 += kG) {
+    C v[kG];
+    R se[kG];
+#pragma unroll
+    for (int u = 0; u < kG; ++u) {
+      const int e = e0 + u;
+      const bool ok = e < n - 1;
+      v[u] = ok ? base[(size_t)e * st] : C{};
+      se[u] = ok ? s[(size_t)e * NT] : R(0);
+    }
+#pragma unroll
+    for (int u = 0; u < kG; ++u) {
+      const int e = e0 + u;
+      if (e < n - 1) base[(size_t)e * st] = mk<C>(xn.x * se[u] + v[u].x, xn.y * se[u] + v[u].y);
+    }
   }
   base[(size_t)(n - 1) * st] = xn;
 }
@@ -468,10 +480,9 @@ void launch_z(Ctx* c, const FftArgs<C>& F, C* spec) {
   auto k = z_solve<C, N>;
   auto k1 = z_solve<C, N, 1>;
   if (!smem_attr(c, k, Sh::smem) || !smem_attr(c, k1, S1::smem)) return;
-  const size_t tri_smem = sizeof(C) * 32 * (size_t)N;
-  if (F.ztri && N >= 3 && tri_smem <= 200 * 1024 && smem_attr(c, z_tri<C>, tri_smem)) {
+  if (F.ztri && N >= 3) {
     // tridiagonal lines, and the zero line by transform
-    z_tri<C><<<div_up((size_t)c->g.H * c->g.n2m, 32), 32, tri_smem, c->stream>>>(F, spec);
+    z_tri<C><<<div_up((size_t)c->g.H * c->g.n2m, 64), 64, 0, c->stream>>>(F, spec);
     k1<<<dim3(1, 1), S1::T, S1::smem, c->stream>>>(F, spec, 0);
     ++c->launches;                 // the caller counts one launch per pass
     return;
