@@ -119,6 +119,7 @@ struct Ctx {
   double* pad_vy = nullptr;               // vy(i, n2, k), i<n1m, k<n3m
   void* dm[MIBM_NMESH] = {nullptr};       // mesh mirrors
   double* stage = nullptr;                // host<->device staging (one Fortran field)
+  void* mesh_stage = nullptr;             // one uploaded mesh array, compared with the device copy
   size_t stage_bytes = 0;
   // spectral work for phcalc: complex [k][j][kx], kx pitch HP
   double2* spec = nullptr;
@@ -153,6 +154,9 @@ struct Ctx {
   cudaEvent_t ev_wfork = nullptr, ev_wjoin = nullptr;
   bool loads_pending = false;
   std::vector<void*> pinned;              // host arrays page-locked by mibm_pin_host_
+  // device-accessible addresses of page-locked host fields: the pack and
+  // unpack kernels read and write them directly over the CPU-GPU link
+  double* hf_dev[MIBM_NFIELDS] = {nullptr};
   bool prologue_done = false;             // the next substep's geometry-only work is enqueued
   // substep 0's geometry-only work, enqueued by the previous step's last
   // substep: valid while geom_gen (bumped by every host call that may change

@@ -144,20 +144,43 @@ __global__ void pad_unpack(Grid g, const double* __restrict__ pad, int n1, int n
   }
 }
 
+// Takes an uploaded mesh array into the device copy, word by word, and sets
+// bit `id` of *changed when any word differs (bitwise: NaNs compare by
+// payload), so that an upload that changes nothing keeps what was derived
+// from the mesh.
+__global__ void mesh_take_kernel(const unsigned* __restrict__ src, unsigned* __restrict__ dst, size_t n, int id,
+                                 int* changed) {
+  bool diff = false;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    unsigned v = src[t];
+    diff |= v != dst[t];
+    dst[t] = v;
+  }
+  if (__any_sync(0xffffffffu, diff) && (threadIdx.x & 31) == 0) atomicOr(changed, 1 << id);
+}
+
+// A page-locked host field (mibm_pin_host_) is read or written by the
+// pack/unpack kernels in place over the CPU-GPU link, which moves it faster
+// than a staged copy followed by a repacking kernel; otherwise it goes
+// through the staging buffer with one contiguous copy.
 static void sync_field_from_host(Ctx* c, int id) {
   int ny, klo, nk;
   field_host_shape(c, id, ny, klo, nk);
   int n1 = c->g.n1m + 1;
   size_t bytes = (size_t)n1 * ny * nk * sizeof(double);
-  if (!cuda_ok(c, cudaMemcpyAsync(c->stage, c->hf[id], bytes, cudaMemcpyHostToDevice, c->stream), "H2D field")) return;
+  const double* src = c->hf_dev[id];
+  if (!src) {
+    if (!cuda_ok(c, cudaMemcpyAsync(c->stage, c->hf[id], bytes, cudaMemcpyHostToDevice, c->stream), "H2D field")) return;
+    src = c->stage;
+  }
   int koff = (klo == 0) ? 1 : 0;   // compact k=0 is host plane index koff
   dim3 grid(div_up(c->g.n1m, 128), c->g.n2m, c->g.n3m);
-  pack_kernel<<<grid, 128, 0, c->stream>>>(c->g, c->stage, n1, ny, koff, c->df[id]);
+  pack_kernel<<<grid, 128, 0, c->stream>>>(c->g, src, n1, ny, koff, c->df[id]);
   ++c->launches;
   if (id == MIBM_F_VX || id == MIBM_F_VY) {
     int which = id == MIBM_F_VX ? 0 : 1;
     dim3 pg(div_up(which == 0 ? c->g.n2m : c->g.n1m, 128), c->g.n3m);
-    pad_pack<<<pg, 128, 0, c->stream>>>(c->g, c->stage, n1, ny, koff, which, which == 0 ? c->pad_vx : c->pad_vy);
+    pad_pack<<<pg, 128, 0, c->stream>>>(c->g, src, n1, ny, koff, which, which == 0 ? c->pad_vx : c->pad_vy);
     ++c->launches;
   }
   MIBM_LAUNCH_CHECK(c, "pack");
@@ -168,18 +191,23 @@ static void sync_field_to_host(Ctx* c, int id) {
   field_host_shape(c, id, ny, klo, nk);
   int n1 = c->g.n1m + 1;
   int koff = (klo == 0) ? 1 : 0;
+  // in place into a page-locked host field, else into the staging buffer;
+  // either way only the owned cells, the ghost planes and the padding that
+  // cfl reads (vx column n1, vy row n2) are written
+  double* dst = c->hf_dev[id] ? c->hf_dev[id] : c->stage;
   dim3 grid(div_up(c->g.n1m, 128), c->g.n2m, nk);
-  unpack_kernel<<<grid, 128, 0, c->stream>>>(c->g, c->df[id], n1, ny, nk, koff, c->stage);
+  unpack_kernel<<<grid, 128, 0, c->stream>>>(c->g, c->df[id], n1, ny, nk, koff, dst);
   ++c->launches;
   size_t wx = (size_t)c->g.n1m, hy = (size_t)c->g.n2m;
   if (id == MIBM_F_VX || id == MIBM_F_VY) {
     int which = id == MIBM_F_VX ? 0 : 1;
     dim3 pg(div_up(which == 0 ? c->g.n2m : c->g.n1m, 128), nk);
-    pad_unpack<<<pg, 128, 0, c->stream>>>(c->g, which == 0 ? c->pad_vx : c->pad_vy, n1, ny, nk, koff, which, c->stage);
+    pad_unpack<<<pg, 128, 0, c->stream>>>(c->g, which == 0 ? c->pad_vx : c->pad_vy, n1, ny, nk, koff, which, dst);
     ++c->launches;
     if (which == 0) wx = n1; else hy = c->g.n2m + 1;
   }
   if (!MIBM_LAUNCH_CHECK(c, "unpack")) return;
+  if (c->hf_dev[id]) return;
   cudaMemcpy3DParms p{};
   p.srcPtr = make_cudaPitchedPtr(c->stage, (size_t)n1 * sizeof(double), n1, ny);
   p.dstPtr = make_cudaPitchedPtr(c->hf[id], (size_t)n1 * sizeof(double), n1, ny);
@@ -252,8 +280,10 @@ bool ensure_params(Ctx* c) {
 }
 
 static void unpin_host(Ctx* c) {
+  if (c->stream) cudaStreamSynchronize(c->stream);      // no kernel still reads or writes them
   for (void* p : c->pinned) cudaHostUnregister(p);
   c->pinned.clear();
+  for (int i = 0; i < MIBM_NFIELDS; ++i) c->hf_dev[i] = nullptr;
   cudaGetLastError();
 }
 
@@ -265,7 +295,7 @@ void release(Ctx* c) {
   if (c->graph) cudaGraphDestroy(c->graph);
   for (int i = 0; i < MIBM_NFIELDS; ++i) cudaFree(c->df[i]);
   for (int i = 0; i < MIBM_NMESH; ++i) cudaFree(c->dm[i]);
-  cudaFree(c->pad_vx); cudaFree(c->pad_vy); cudaFree(c->stage); cudaFree(c->spec);
+  cudaFree(c->pad_vx); cudaFree(c->pad_vy); cudaFree(c->stage); cudaFree(c->spec); cudaFree(c->mesh_stage);
   cudaFree(c->ak1); cudaFree(c->ak2); cudaFree(c->ak3);
   cudaFree(c->xc); cudaFree(c->xm); cudaFree(c->yc); cudaFree(c->ym); cudaFree(c->zc); cudaFree(c->zm);
   cudaFree(c->red); cudaFree(c->dflag); cudaFree(c->dparams); cudaFree(c->rhs4);
@@ -396,6 +426,7 @@ void mibm_register_field_(const int* id, double* base) {
   Ctx* c = current(); if (!c) return;
   if (*id < 0 || *id >= MIBM_NFIELDS) { fail(c, MIBM_EINVAL, "register_field: bad id"); return; }
   c->hf[*id] = base;
+  c->hf_dev[*id] = nullptr;          // a new array is not the page-locked one
 }
 void mibm_register_mesh_(const int* id, void* base) {
   Ctx* c = current(); if (!c) return;
@@ -441,11 +472,14 @@ void mibm_init_(void) {
   if (!cuda_ok(c, cudaMallocHost((void**)&c->hflag, 64), "pinned")) return;
   if (!cuda_ok(c, cudaMallocHost((void**)&c->step_host, 32 * sizeof(double)), "pinned")) return;
   memset(c->hflag, 0, 64);
+  size_t mesh_max = 0;
   for (int i = 0; i < MIBM_NMESH; ++i) {
     size_t b = mesh_bytes(c, i);
     if (b == 0) continue;
     if (!dev_alloc(c, &c->dm[i], b, "mesh")) return;
+    mesh_max = std::max(mesh_max, b);
   }
+  if (mesh_max && !dev_alloc(c, &c->mesh_stage, mesh_max, "mesh staging")) return;
   if (!ensure_params(c)) return;
   upload_coords(c);
   if (c->status != MIBM_OK) return;
@@ -454,6 +488,7 @@ void mibm_init_(void) {
   long long all = -1;
   mibm_sync_from_host_(&all);
   cudaStreamSynchronize(c->stream);
+  lagr_topology_changed(c);            // nothing derived from the mesh exists yet
   if (c->maxnf > 0 && !validate_mesh(c)) c->inited = false;
 }
 
@@ -463,17 +498,36 @@ void mibm_sync_from_host_(const long long* mask) {
   for (int i = 0; i < MIBM_NFIELDS; ++i)
     if (m & (1ull << i)) sync_field_from_host(c, i);
   precision_after_upload(c, m);
-  for (int i = 0; i < MIBM_NMESH && c->maxnf > 0; ++i)
-    if ((m >> 32) & (1ull << i))
-      cuda_ok(c, cudaMemcpyAsync(c->dm[i], c->hm[i], mesh_bytes(c, i), cudaMemcpyHostToDevice, c->stream), "H2D mesh");
-  // the scatter plan and the MLS weights depend on the mesh, the
-  // vertex->face lists on its connectivity
+  const bool mesh_up = c->maxnf > 0 && (m >> 32) != 0;
+  int* changed = c->dflag + 4;         // bit i: mesh array i differs from the device copy
+  if (mesh_up) cudaMemsetAsync(changed, 0, sizeof(int), c->stream);
+  for (int i = 0; i < MIBM_NMESH && mesh_up; ++i) {
+    size_t bytes = mesh_bytes(c, i);
+    if (!((m >> 32) & (1ull << i)) || bytes == 0) continue;
+    if (!cuda_ok(c, cudaMemcpyAsync(c->mesh_stage, c->hm[i], bytes, cudaMemcpyHostToDevice, c->stream), "H2D mesh"))
+      return;
+    size_t words = bytes / 4;
+    mesh_take_kernel<<<std::min<size_t>(div_up(words, 256), 1024), 256, 0, c->stream>>>(
+        (const unsigned*)c->mesh_stage, (unsigned*)c->dm[i], words, i, changed);
+    ++c->launches;
+  }
+  if (mesh_up) {
+    MIBM_LAUNCH_CHECK(c, "mesh upload");
+    cudaMemcpyAsync(c->hflag + 4, changed, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  }
+  if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "sync_from_host")) return;
+  const unsigned long long mchg = mesh_up ? (unsigned long long)(unsigned)c->hflag[4] : 0ull;
+  // what the next step's geometry-only work reads from the fields: the
+  // volume fractions (narrow-band tagging updates VOFp in place) and the
+  // signed distance; the scatter plan and the MLS weights depend on the
+  // mesh, the vertex->face lists on its connectivity
+  const unsigned long long geom_fields = (1ull << MIBM_F_VOFX) | (1ull << MIBM_F_VOFY) | (1ull << MIBM_F_VOFZ) |
+                                         (1ull << MIBM_F_VOFP) | (1ull << MIBM_F_SDF);
   const unsigned long long topo = (1ull << MIBM_M_VERT_OF_FACE) | (1ull << MIBM_M_GHOST_FACE);
-  ++c->geom_gen;                       // fields (VOF) or mesh from the host
-  if ((m >> 32) & topo) lagr_topology_changed(c);
-  else if ((m >> 32) != 0) lagr_invalidate(c);
-  cuda_ok(c, cudaStreamSynchronize(c->stream), "sync_from_host");
-  if (c->maxnf > 0 && ((m >> 32) & ((1ull << MIBM_M_VERT_OF_FACE) | (1ull << MIBM_M_GHOST_FACE)))) validate_mesh(c);
+  if (m & geom_fields) ++c->geom_gen;
+  if (mchg & topo) lagr_topology_changed(c);
+  else if (mchg) lagr_invalidate(c);
+  if (c->maxnf > 0 && (mchg & topo)) validate_mesh(c);
 }
 
 void mibm_sync_to_host_(const long long* mask) {
@@ -493,15 +547,20 @@ int mibm_pin_host_(const int* on) {
   if (!*on) { unpin_host(c); return MIBM_OK; }
   if (!c->pinned.empty()) return MIBM_OK;
   auto pin = [&](void* p, size_t bytes) {
-    if (!p || bytes == 0) return;
-    cudaError_t e = cudaHostRegister(p, bytes, cudaHostRegisterDefault);
-    if (e == cudaSuccess) c->pinned.push_back(p);
-    else cudaGetLastError();               // already page-locked, or not registrable: copies stay pageable
+    if (!p || bytes == 0) return false;
+    cudaError_t e = cudaHostRegister(p, bytes, cudaHostRegisterMapped);
+    if (e == cudaSuccess) { c->pinned.push_back(p); return true; }
+    cudaGetLastError();                    // already page-locked, or not registrable: copies stay pageable
+    return false;
   };
   for (int id = 0; id < MIBM_NFIELDS; ++id) {
     int ny, klo, nk;
     field_host_shape(c, id, ny, klo, nk);
-    pin(c->hf[id], (size_t)(c->g.n1m + 1) * ny * nk * sizeof(double));
+    if (pin(c->hf[id], (size_t)(c->g.n1m + 1) * ny * nk * sizeof(double))) {
+      void* dp = nullptr;
+      if (cudaHostGetDevicePointer(&dp, c->hf[id], 0) == cudaSuccess) c->hf_dev[id] = (double*)dp;
+      else cudaGetLastError();
+    }
   }
   for (int i = 0; i < MIBM_NMESH && c->maxnf > 0; ++i) pin(c->hm[i], mesh_bytes(c, i));
   return MIBM_OK;

@@ -21,7 +21,7 @@ from tests.helpers import FIELDS_OUT, pair, randomize, rel_l2, set_substep, smal
 pytestmark = pytest.mark.gpu
 A = abi
 TOL_ROUTINE = 1e-12     # one routine on identical inputs (FMA / summation order only)
-TOL_STEP = 1e-10        # spec plain-form tolerance after 1 and 10 steps
+TOL_STEP = 1e-10        # plain FP64 form: tolerance after 1 and 10 steps
 ALL = -1
 
 

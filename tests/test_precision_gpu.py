@@ -1,6 +1,6 @@
 """The precision form (FP32 compute on FP64 fields, refined projection).
 
-Spec bar: relative L2 error <= 1e-6 per field against the FP64 run
+Acceptance bar: relative L2 error <= 1e-6 per field against the FP64 run
 from identical inputs, and divergence <= 1e-10 after every step.
 """
 from __future__ import annotations
