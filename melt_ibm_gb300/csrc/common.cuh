@@ -327,6 +327,8 @@ double k_cfl(Ctx* c);
 void k_cfl_async(Ctx* c, double* out);
 bool fft_prepare(Ctx* c, bool f32);
 void tri_build_table(int n, double betadx, std::vector<double>& t);
+size_t tri_ext_len(int n, int m);
+void tri_build_ext_table(int n, int m, double betadx, std::vector<double>& out);
 bool cfl_finite(Ctx* c);
 void k_getdt_async(Ctx* c, double dt, double* out);
 double cfl_value(double reduced);

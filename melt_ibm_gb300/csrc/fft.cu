@@ -237,6 +237,7 @@ struct FftCache {
   double* ztri = nullptr;   // FftArgs::ztri, FP64
   float* fztri = nullptr;   // the same rounded to FP32
   int zt_lines = 0;
+  int zt_m = 0;             // FftArgs::zt_m
 };
 static std::vector<FftCache> g_fft;
 
@@ -272,11 +273,19 @@ __global__ void eig_kernel(Grid g, const double* __restrict__ ak1, const double*
 // phcalc.f90:65) keeps the transform.  Layout, NT = H (n2m/2 + 1) lines,
 // lt = kx + H min(ky, n2m - ky): arrays a, b, q, s at e*NT + lt (offsets 0,
 // n, 2n, 3n times NT), then 4 scalars per line (ackl_b, api, ami, 1/den).
+// Per-line tables of the z-line solves.  Chunked layout (zt_chunk(n) = M >
+// 0): the extended table of the chunked line solves (tridiag.cu), entry q of
+// line lt at q*NT + lt, with the a entries and the closure's ackl scaled by
+// sigma.  Otherwise the base table: a, b, q, s at e*NT + lt (plus k*NS),
+// then ackl, api, ami, 1/den per line.  Line 0 (the zero line) stays zero.
 static bool make_ztri(Ctx* c, FftCache* f, bool f32) {
   if (f32 ? f->fztri != nullptr : f->ztri != nullptr) return true;
   const Grid& g = c->g;
   const int n = g.n3m, H = g.H, NT = H * (g.n2m / 2 + 1);
-  const size_t NS = (size_t)n * NT, len = 4 * NS + 4 * (size_t)NT;
+  const int zm = zt_chunk(n, H * g.n2m);
+  const size_t NS = (size_t)n * NT;
+  const size_t E = zm ? tri_ext_len(n, zm) : 0;
+  const size_t len = zm ? E * NT : 4 * NS + 4 * (size_t)NT;
   std::vector<double> ak1(g.n1m), ak2(g.n2m);
   if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "z-line tables")) return false;   // ak1/ak2 uploads
   cudaMemcpy(ak1.data(), c->ak1, sizeof(double) * g.n1m, cudaMemcpyDeviceToHost);
@@ -288,8 +297,14 @@ static bool make_ztri(Ctx* c, FftCache* f, bool f32) {
       const int lt = kx + H * kyr;
       const double lambda = ak1[kx] + ak2[kyr];
       if (kx == 0 && kyr == 0) continue;                 // the zero line: transform path
-      tri_build_table(n, g.dx3q / lambda, t);
       const double sigma = -(1.0 / lambda) * nfac;
+      if (zm) {
+        tri_build_ext_table(n, zm, g.dx3q / lambda, t);
+        const size_t S = 7 * (size_t)n + 3 * (size_t)(n / zm);
+        for (size_t q = 0; q < E; ++q) tab[q * NT + lt] = (q < (size_t)n || q == S) ? t[q] * sigma : t[q];
+        continue;
+      }
+      tri_build_table(n, g.dx3q / lambda, t);
       for (int e = 0; e < n; ++e) {
         tab[(size_t)e * NT + lt] = t[e] * sigma;
         tab[NS + (size_t)e * NT + lt] = t[n + e];
@@ -312,6 +327,7 @@ static bool make_ztri(Ctx* c, FftCache* f, bool f32) {
     f->ztri = (double*)p;
   }
   f->zt_lines = NT;
+  f->zt_m = zm;
   return true;
 }
 
@@ -434,7 +450,7 @@ void k_phcalc(Ctx* c) {
   F.inv_nn = 1.0 / ((double)g.n1m * (double)g.n2m * (double)g.n3m);
   if (!make_eig(c, fc, false) || !make_ztri(c, fc, false)) return;
   F.eig = fc->eig;
-  F.ztri = fc->ztri; F.zt_lines = fc->zt_lines;
+  F.ztri = fc->ztri; F.zt_lines = fc->zt_lines; F.zt_m = fc->zt_m;
   phcalc_launch<double2, double>(c, F, c->df[MIBM_F_DPH], c->df[MIBM_F_DPH], "phcalc");
 }
 
@@ -454,7 +470,7 @@ void k_phcalc_f32(Ctx* c, const float* src, float* phi) {
   F.eig = fc->feig;
   // FP32 transforms cost little on the FP32 pipe: the z pass stays a
   // transform (the tridiagonal lines are latency-bound and slower there)
-  F.ztri = nullptr; F.zt_lines = 0;
+  F.ztri = nullptr; F.zt_lines = 0; F.zt_m = 0;
   phcalc_launch<float2, float>(c, F, src, phi, "phcalc_f32");
 }
 

@@ -52,7 +52,23 @@ struct FftArgs {
   // z-line solve tables (fft.cu make_ztri), nullptr: z passes by FFT
   const R* ztri;
   int zt_lines;
+  int zt_m;            // chunk length of the chunked z-line tables, 0: one thread per line
 };
+
+// chunk length of the chunked z-line Poisson solve for `lines` lines of n
+// cells: M = 16 or 8 with 2..kZtMaxChunks chunks (warps of a block), 0 =
+// none (one thread per line).  Chunking costs 10 FP64 operations per complex
+// cell against 8 for one sweep per line, so it only pays where one thread
+// per line leaves the GPU short of warps (measured: 128^3, 8320 lines, 97
+// -> 48 us per solve; 256^3, 33024 lines, 233 -> 289 us).
+constexpr int kZtMaxChunks = 16;
+constexpr int kZtChunkLines = 16384;
+inline int zt_chunk(int n, int lines) {
+  if (lines >= kZtChunkLines) return 0;
+  if (n % 16 == 0 && n / 16 >= 2 && n / 16 <= kZtMaxChunks) return 16;
+  if (n % 8 == 0 && n / 8 >= 2 && n / 8 <= kZtMaxChunks) return 8;
+  return 0;
+}
 
 template <typename C>
 __device__ __forceinline__ void load_tw(C* s, const C* tw, int n) {

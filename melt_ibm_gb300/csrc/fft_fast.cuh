@@ -473,6 +473,97 @@ void launch_y(Ctx* c, const FftArgs<C>& F, C* spec, int sign) {
   }
 }
 
+// The same lines chunked (the scheme of the chunked line solves of
+// tridiag.cu, on complex values with one table per line): a block holds 32
+// lines (lanes, consecutive in kx + H*ky) and the G = n/M chunks of M cells
+// (warps, in registers); forward and backward sweeps per chunk from zero
+// entries, the chunk entries by a serial scan over the lower chunks in
+// shared memory, the periodic closure from elements 0 and n-2, then one
+// correction pass.  Table entry q of line lt sits at q*NT + lt (32 lanes read
+// consecutive words); lanes without a line (past the end, and the zero line,
+// which the transform solves) use line 0's all-zero table and store nothing.
+template <typename C, int M>
+__global__ void __launch_bounds__(32 * kZtMaxChunks) z_tri_cc(FftArgs<C> F, C* __restrict__ spec) {
+  typedef typename Real<C>::T R;
+  __shared__ C sC[kZtMaxChunks][32];
+  __shared__ C sU[kZtMaxChunks][32];
+  __shared__ C sF[3][32];
+  const Grid& g = F.g;
+  const int n = g.n3m, G = n / M, H = g.H, NT = F.zt_lines;
+  const int lane = threadIdx.x, w = threadIdx.y;
+  const int l = blockIdx.x * 32 + lane;
+  const bool act = l > 0 && l < H * g.n2m;
+  const int kx = act ? l % H : 0, ky = act ? l / H : 0;
+  const int lt = kx + H * (ky <= g.n2m - ky ? ky : g.n2m - ky);
+  const R* __restrict__ X = F.ztri + lt;
+  auto T = [&](int q) { return X[(size_t)q * NT]; };
+  const size_t st = (size_t)g.HP * g.n2m;
+  C* __restrict__ rp = spec + kx + (size_t)g.HP * ky + (size_t)(w * M) * st;
+  C r[M];
+#pragma unroll
+  for (int i = 0; i < M; ++i) r[i] = act ? rp[(size_t)i * st] : mk<C>(R(0), R(0));
+  const C rlast = r[M - 1];
+  C cf = mk<C>(R(0), R(0));
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
+    const int t = i * G + w;
+    const R a = T(t), b = T(n + t);
+    cf = mk<C>(a * r[i].x - b * cf.x, a * r[i].y - b * cf.y);
+    r[i] = cf;
+  }
+  sC[w][lane] = cf;
+  __syncthreads();
+  C y_in = mk<C>(R(0), R(0));
+  for (int hh = 0; hh < w; ++hh) {
+    const R pl = T(7 * n + hh);
+    const C v = sC[hh][lane];
+    y_in = mk<C>(v.x + pl * y_in.x, v.y + pl * y_in.y);
+  }
+  C d = mk<C>(R(0), R(0));
+#pragma unroll
+  for (int i = M - 1; i >= 0; --i) {
+    const R q = T(2 * n + i * G + w);
+    d = mk<C>(r[i].x + q * d.x, r[i].y + q * d.y);
+    r[i] = d;
+  }
+  {
+    const R dpf = T(7 * n + 2 * G + w);
+    sU[w][lane] = mk<C>(r[0].x + dpf * y_in.x, r[0].y + dpf * y_in.y);
+  }
+  __syncthreads();
+  C f_in = mk<C>(R(0), R(0));
+  for (int hh = G - 1; hh > w; --hh) {
+    const R qf = T(7 * n + G + hh);
+    const C v = sU[hh][lane];
+    f_in = mk<C>(v.x + qf * f_in.x, v.y + qf * f_in.y);
+  }
+  if (w == 0) {
+    const R q0 = T(5 * n);
+    sF[0][lane] = mk<C>(r[0].x + q0 * f_in.x, r[0].y + q0 * f_in.y);
+  }
+  if (w == G - 1) {
+    const R dp = T(6 * n + (M - 2) * G + w);
+    sF[1][lane] = mk<C>(r[M - 2].x + dp * y_in.x, r[M - 2].y + dp * y_in.y);
+    sF[2][lane] = rlast;
+  }
+  __syncthreads();
+  const int S = 7 * n + 3 * G;
+  const R ackl = T(S), api = T(S + 1), ami = T(S + 2), inv_den = T(S + 3);
+  const C f0 = sF[0][lane], f1 = sF[1][lane], rn = sF[2][lane];
+  const C xn = mk<C>((rn.x * ackl - api * f0.x - ami * f1.x) * inv_den,
+                     (rn.y * ackl - api * f0.y - ami * f1.y) * inv_den);
+  if (!act) return;
+  const R ac = T(S + 4 + w), bc = T(S + 4 + G + w);
+  const C al = mk<C>(y_in.x + ac * xn.x, y_in.y + ac * xn.y);
+  const C be = mk<C>(f_in.x + bc * xn.x, f_in.y + bc * xn.y);
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
+    const int t = i * G + w;
+    const R dp = T(6 * n + t), qq = T(5 * n + t);
+    rp[(size_t)i * st] = mk<C>(r[i].x + dp * al.x + qq * be.x, r[i].y + dp * al.y + qq * be.y);
+  }
+}
+
 template <typename C, int N>
 void launch_z(Ctx* c, const FftArgs<C>& F, C* spec) {
   typedef Shape<C, N> Sh;
@@ -482,7 +573,10 @@ void launch_z(Ctx* c, const FftArgs<C>& F, C* spec) {
   if (!smem_attr(c, k, Sh::smem) || !smem_attr(c, k1, S1::smem)) return;
   if (F.ztri && N >= 3) {
     // tridiagonal lines, and the zero line by transform
-    z_tri<C><<<div_up((size_t)c->g.H * c->g.n2m, 64), 64, 0, c->stream>>>(F, spec);
+    const size_t lines = (size_t)c->g.H * c->g.n2m;
+    if (F.zt_m == 16) z_tri_cc<C, 16><<<div_up(lines, 32), dim3(32, c->g.n3m / 16), 0, c->stream>>>(F, spec);
+    else if (F.zt_m == 8) z_tri_cc<C, 8><<<div_up(lines, 32), dim3(32, c->g.n3m / 8), 0, c->stream>>>(F, spec);
+    else z_tri<C><<<div_up(lines, 64), 64, 0, c->stream>>>(F, spec);
     k1<<<dim3(1, 1), S1::T, S1::smem, c->stream>>>(F, spec, 0);
     ++c->launches;                 // the caller counts one launch per pass
     return;

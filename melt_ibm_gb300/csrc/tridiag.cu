@@ -474,6 +474,16 @@ static void fill_slot(int n, int m, double betadx, double* out) {
   if (m) build_ext(t, n, m, out + L.off_ext);
 }
 
+// the extended table of chunk length m for one line of n cells (ext_len(n, m)
+// values), for callers outside this file (the z-line Poisson solve of fft.cu)
+size_t tri_ext_len(int n, int m) { return ext_len(n, m); }
+void tri_build_ext_table(int n, int m, double betadx, std::vector<double>& out) {
+  std::vector<double> t;
+  build_table(n, betadx, t);
+  out.assign(ext_len(n, m), 0.0);
+  build_ext(t, n, m, out.data());
+}
+
 // slot length for lines up to nmax and any chunk (ext_len <= 7n + 5*32 + 4)
 static size_t slot_len(int nmax) { return 4 * (size_t)nmax + 4 + 7 * (size_t)nmax + 5 * 32 + 4; }
 

@@ -59,9 +59,11 @@ def test_stencil_routine_parity(oracle_lib, gpu_lib, routine, n):
     _cmp_fields(co, cg, STENCIL_ROUTINES[routine])
 
 
-@pytest.mark.parametrize("n", [16, 24, 48])
-def test_phcalc_parity(oracle_lib, gpu_lib, n):
-    case = Case(small_config(n=n))
+@pytest.mark.parametrize("n, n3", [(16, None), (24, None), (48, None), (192, 8)])
+def test_phcalc_parity(oracle_lib, gpu_lib, n, n3):
+    """Poisson solve; the z lines are chunked below 16384 (kx, ky) lines and
+    swept one per thread from there on (192 x 192 x 8: 18624 lines)."""
+    case = Case(small_config(n=n, n3=n3, velocity="random" if n3 is None else "rest"))
     randomize(case)
     co, cg = pair(case, oracle_lib, gpu_lib, initial_tag=False)
     for c, lib in ((co, oracle_lib), (cg, gpu_lib)):
