@@ -20,55 +20,6 @@
 
 namespace mibm {
 
-// In-place inverse of a 3x3 column-major matrix: LU with partial pivoting
-// (first maximal pivot, dgetrf) and inversion from the factors (dgetri).
-__device__ bool inv3(double* a) {
-  const int n = 3;
-  int ipiv[3];
-  for (int j = 0; j < n; ++j) {
-    int p = j;
-    double amax = fabs(a[j + n * j]);
-    for (int i = j + 1; i < n; ++i)
-      if (fabs(a[i + n * j]) > amax) { amax = fabs(a[i + n * j]); p = i; }
-    ipiv[j] = p;
-    if (a[p + n * j] == 0.0) return false;
-    if (p != j)
-      for (int cc = 0; cc < n; ++cc) { double t = a[j + n * cc]; a[j + n * cc] = a[p + n * cc]; a[p + n * cc] = t; }
-    double r = 1.0 / a[j + n * j];
-    for (int i = j + 1; i < n; ++i) a[i + n * j] *= r;
-    for (int cc = j + 1; cc < n; ++cc) {
-      double t = a[j + n * cc];
-      for (int i = j + 1; i < n; ++i) a[i + n * cc] -= t * a[i + n * j];
-    }
-  }
-  for (int j = 0; j < n; ++j) {
-    a[j + n * j] = 1.0 / a[j + n * j];
-    double ajj = -a[j + n * j];
-    for (int i = 0; i < j; ++i) {
-      double s = 0;
-      for (int k = i; k < j; ++k) s += a[i + n * k] * a[k + n * j];
-      a[i + n * j] = s;
-    }
-    for (int i = 0; i < j; ++i) a[i + n * j] *= ajj;
-  }
-  double work[3];
-  for (int j = n - 1; j >= 0; --j) {
-    for (int i = j + 1; i < n; ++i) { work[i] = a[i + n * j]; a[i + n * j] = 0.0; }
-    if (j < n - 1)
-      for (int i = 0; i < n; ++i) {
-        double s = 0;
-        for (int k = j + 1; k < n; ++k) s += a[i + n * k] * work[k];
-        a[i + n * j] -= s;
-      }
-  }
-  for (int j = n - 2; j >= 0; --j) {
-    int jp = ipiv[j];
-    if (jp != j)
-      for (int i = 0; i < n; ++i) { double t = a[i + n * j]; a[i + n * j] = a[i + n * jp]; a[i + n * jp] = t; }
-  }
-  return true;
-}
-
 // calc_rot_matrix (RigidAuxRoutines.f90:556-582): normalises q, AA column-major
 __device__ void rot_matrix(double q[4], double AA[9]) {
   double norm = sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
@@ -103,7 +54,6 @@ __global__ void newton_euler_kernel(const StepParams* __restrict__ pp, const dou
   __shared__ double I[9], I_LHS[9], I_inv[9], AA[9], buf[9], om1[3], vel1[3], rhs[3], om[3], ob[3], quat[4];
   __shared__ double sc[4];          // magOM, angle, ch, sh
   __shared__ double qn_s;
-  __shared__ int singular;
   const double al = pp->al, ga = pp->ga, ro = pp->ro, dt = pp->dt;
   const double* prn = r->load; const double* tau = r->load + 3;
   const double* rprn = r->load + 6; const double* rtau = r->load + 9;
@@ -112,7 +62,6 @@ __global__ void newton_euler_kernel(const StepParams* __restrict__ pp, const dou
   if (lane < 9) { I[lane] = geom[6 + lane]; I_LHS[lane] = geom[6 + lane]; }
   if (lane < 3) { vel1[lane] = r->vel[lane]; om1[lane] = r->om[lane]; }
   if (lane < 4) quat[lane] = 0.0;
-  if (lane == 0) singular = 0;
   __syncwarp();
   // translation, RigidAuxRoutines.f90:218-225 (lane i: component i)
   double vel = 0.0, pos = 0.0;
@@ -129,14 +78,25 @@ __global__ void newton_euler_kernel(const StepParams* __restrict__ pp, const dou
   double Iresidual = 1.0;
   int n_iter = 1;
   while (n_iter <= max_iter && Iresidual > tolerance) {
-    if (lane == 0) {
-      double a[9];
-      for (int q = 0; q < 9; ++q) a[q] = I_LHS[q];
-      if (!inv3(a)) singular = 1;
-      for (int q = 0; q < 9; ++q) I_inv[q] = a[q];
+    // the inverse of I_LHS (dgetrf + dgetri in the reference) by cofactors,
+    // entry (i, j) on lane i + 3j: a dependent FP64 chain of one cofactor, a
+    // 3-term determinant and one reciprocal instead of an LU's six
+    // reciprocals and eliminations on one thread; the same matrix up to
+    // rounding.  Singular (flag 2) when the determinant is exactly zero.
+    {
+      double cof = 0.0;
+      if (lane < 9) {
+        const int i = lane % 3, j = lane / 3;
+        const int r0 = (j + 1) % 3, r1 = (j + 2) % 3, c0 = (i + 1) % 3, c1 = (i + 2) % 3;
+        cof = I_LHS[r0 + 3 * c0] * I_LHS[r1 + 3 * c1] - I_LHS[r0 + 3 * c1] * I_LHS[r1 + 3 * c0];
+      }
+      const double c00 = __shfl_sync(FULL, cof, 0), c01 = __shfl_sync(FULL, cof, 1), c02 = __shfl_sync(FULL, cof, 2);
+      const double det = I_LHS[0] * c00 + I_LHS[3] * c01 + I_LHS[6] * c02;
+      if (det == 0.0) { if (lane == 0) atomicOr(flag, 2); return; }
+      const double rdet = 1.0 / det;
+      if (lane < 9) I_inv[lane] = cof * rdet;
     }
     __syncwarp();
-    if (singular) { if (lane == 0) atomicOr(flag, 2); return; }
     if (lane < 3) {
       double m = 0.0;
       for (int j = 0; j < 3; ++j) m += I[lane + 3 * j] * om1[j];
@@ -158,8 +118,7 @@ __global__ void newton_euler_kernel(const StepParams* __restrict__ pp, const dou
     __syncwarp();
     const double magOM = sc[0], angle = sc[1];
     if (lane < 3) ob[lane] = magOM < tolerance ? 0.0 : ob[lane] / magOM;
-    if (lane == 3) sc[2] = cos(0.5 * angle);
-    if (lane == 4) sc[3] = sin(0.5 * angle);
+    if (lane == 3) sincos(0.5 * angle, &sc[3], &sc[2]);
     __syncwarp();
     if (lane < 4) quat[lane] = lane == 0 ? sc[2] : sc[3] * ob[lane - 1];
     __syncwarp();
