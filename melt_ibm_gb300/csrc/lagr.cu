@@ -1098,29 +1098,72 @@ __device__ __forceinline__ void face_geom_one(int t, const int* __restrict__ vof
   pp[11] = v * (z1 * y1 + z2 * y2 + z3 * y3 + z4 * y4);
 }
 
-// One thread per face; the 12 per-face sums are added over the block (warp
-// shuffle tree, then the 4 warps in order) into part[12 * block + q].
+// the post-processing of calc_rigidBody_params (RigidAuxRoutines.f90:736-775)
+// from the 12 body sums: [Surface, Volume1, Volume, pos_CM(3), InertTensor(9)]
+__device__ void geom_finish(const double* sm, double dens_ratio, double* __restrict__ out) {
+  double Surface = sm[0], Volume1 = sm[1] / 6.0;
+  double Vol = sm[2], Cx = sm[3], Cy = sm[4], Cz = sm[5];
+  double r = 1.0 / (4.0 * Vol);
+  Cx = Cx * r; Cy = Cy * r; Cz = Cz * r;
+  Vol = Vol / 6.0;
+  out[0] = Surface; out[1] = Volume1; out[2] = Vol;
+  out[3] = Cx; out[4] = Cy; out[5] = Cz;
+  r = 1.0 / 120.0;
+  double Ixy = sm[9] * r - Vol * Cy * Cx;
+  double Ixz = sm[10] * r - Vol * Cz * Cx;
+  double Iyz = sm[11] * r - Vol * Cz * Cy;
+  double xx = sm[6] * r - Vol * Cx * Cx, yy = sm[7] * r - Vol * Cy * Cy, zz = sm[8] * r - Vol * Cz * Cz;
+  double Ixx = yy + zz, Iyy = zz + xx, Izz = xx + yy;
+  double I[9] = {Ixx, -Ixy, -Ixz, -Ixy, Iyy, -Iyz, -Ixz, -Iyz, Izz};
+  for (int q = 0; q < 9; ++q) out[6 + q] = I[q] * dens_ratio;
+}
+
+// One thread per face.  The 12 per-face sums are added over the block (one
+// quantity per warp: four values per lane in thread order, then a shuffle
+// tree) into part[12 * block + q]; the last block to finish (a ticket
+// counter, reset by that block) adds the block sums in block order the same
+// way and writes the body's scalars to out.  Each warp's dependent FP64
+// chain is a few additions per quantity: on this part an FP64 warp
+// instruction holds the pipe for about 64 cycles however few lanes run.
 constexpr int kGeomBlock = 128;
+static_assert(kGeomBlock == 128, "four values per lane in the block sums");
 __global__ void __launch_bounds__(kGeomBlock)
 face_geom_kernel(int nf, const int* __restrict__ vof, const int* __restrict__ ghost, const double* __restrict__ x,
                  double* __restrict__ sur, double* __restrict__ nor, double* __restrict__ bar,
-                 double* __restrict__ part /* 12 per block */) {
-  __shared__ double ws[kGeomBlock / 32][12];
+                 double* __restrict__ part /* 12 per block */, unsigned* __restrict__ ticket, double dens_ratio,
+                 double* __restrict__ out) {
+  const unsigned FULL = 0xffffffffu;
+  __shared__ double ws[12][kGeomBlock];
+  __shared__ double tot[12];
+  __shared__ bool last;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   double pp[12];
   for (int q = 0; q < 12; ++q) pp[q] = 0.0;
   if (t < nf && !ghost[t]) face_geom_one(t, vof, x, sur, nor, bar, pp);
-  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int q = 0; q < 12; ++q) {
-    double v = pp[q];
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-    if (lane == 0) ws[warp][q] = v;
+  for (int q = 0; q < 12; ++q) ws[q][threadIdx.x] = pp[q];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int q = warp; q < 12; q += kGeomBlock / 32) {
+    double v = ws[q][lane] + ws[q][lane + 32] + ws[q][lane + 64] + ws[q][lane + 96];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(FULL, v, off);
+    if (lane == 0) part[12 * (size_t)blockIdx.x + q] = v;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  for (int q = warp; q < 12; q += kGeomBlock / 32) {
+    double v = 0.0;
+    for (int b = lane; b < (int)gridDim.x; b += 32) v += __ldcg(part + 12 * (size_t)b + q);
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(FULL, v, off);
+    if (lane == 0) tot[q] = v;
   }
   __syncthreads();
-  if (threadIdx.x < 12) {
-    double v = ws[0][threadIdx.x];
-    for (int w = 1; w < kGeomBlock / 32; ++w) v += ws[w][threadIdx.x];
-    part[12 * (size_t)blockIdx.x + threadIdx.x] = v;
+  if (threadIdx.x == 0) {
+    geom_finish(tot, dens_ratio, out);
+    *ticket = 0u;
   }
 }
 
@@ -1142,42 +1185,6 @@ __global__ void vert_geom_kernel(int nv, const int* __restrict__ adj_off, const 
   if (ghostv[v]) { vnor[3 * v] = a0; vnor[3 * v + 1] = a1; vnor[3 * v + 2] = a2; return; }
   double m = sqrt(a0 * a0 + a1 * a1 + a2 * a2);
   vnor[3 * v] = a0 / m; vnor[3 * v + 1] = a1 / m; vnor[3 * v + 2] = a2 / m;
-}
-
-// fixed-order reduction of the 12 block sums by one block; writes
-// [Surface, Volume1, Volume, pos_CM(3), InertTensor(9)] into out (the
-// post-processing of calc_rigidBody_params, RigidAuxRoutines.f90:736-775)
-__global__ void geom_reduce_kernel(int nb, const double* __restrict__ part, double dens_ratio,
-                                   double* __restrict__ out) {
-  __shared__ double sm[12][256];
-  double s[12];
-  for (int q = 0; q < 12; ++q) s[q] = 0.0;
-  for (int t = threadIdx.x; t < nb; t += blockDim.x)
-    for (int q = 0; q < 12; ++q) s[q] += part[12 * (size_t)t + q];
-  for (int q = 0; q < 12; ++q) sm[q][threadIdx.x] = s[q];
-  __syncthreads();
-  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
-    if (threadIdx.x < off)
-      for (int q = 0; q < 12; ++q) sm[q][threadIdx.x] += sm[q][threadIdx.x + off];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    double Surface = sm[0][0], Volume1 = sm[1][0] / 6.0;
-    double Vol = sm[2][0], Cx = sm[3][0], Cy = sm[4][0], Cz = sm[5][0];
-    double r = 1.0 / (4.0 * Vol);
-    Cx = Cx * r; Cy = Cy * r; Cz = Cz * r;
-    Vol = Vol / 6.0;
-    out[0] = Surface; out[1] = Volume1; out[2] = Vol;
-    out[3] = Cx; out[4] = Cy; out[5] = Cz;
-    r = 1.0 / 120.0;
-    double Ixy = sm[9][0] * r - Vol * Cy * Cx;
-    double Ixz = sm[10][0] * r - Vol * Cz * Cx;
-    double Iyz = sm[11][0] * r - Vol * Cz * Cy;
-    double xx = sm[6][0] * r - Vol * Cx * Cx, yy = sm[7][0] * r - Vol * Cy * Cy, zz = sm[8][0] * r - Vol * Cz * Cz;
-    double Ixx = yy + zz, Iyy = zz + xx, Izz = xx + yy;
-    double I[9] = {Ixx, -Ixy, -Ixz, -Ixy, Iyy, -Iyz, -Ixz, -Iyz, Izz};
-    for (int q = 0; q < 9; ++q) out[6 + q] = I[q] * dens_ratio;
-  }
 }
 
 // calculate_eLengths (triaux.f90:277-306); flag bit 0 set when a live edge
@@ -1548,6 +1555,7 @@ struct LagState {
   int adj_nf = -1, adj_nv = -1;
   double* face_part = nullptr;
   double* geom_out = nullptr;   // device [Surface, Volume1, Vol, Cx, Cy, Cz, InertTensor(9)]
+  unsigned* geom_ticket = nullptr;   // blocks of face_geom_kernel done (0 between launches)
   double* loads_ev = nullptr;   // structural loads: 12 block sums per 32 faces
   int* rm_flag = nullptr;       // remesh trigger (device)
   double* mean3 = nullptr;
@@ -1652,7 +1660,9 @@ static bool ensure_lag_buffers(Ctx* c) {
   if (!s->face_part) {
     if (!cuda_ok(c, cudaMalloc(&s->face_part, sizeof(double) * 12 * std::max(1, c->maxnf)), "lag")) return false;
     if (!cuda_ok(c, cudaMalloc(&s->geom_out, sizeof(double) * 16), "lag")) return false;
+    if (!cuda_ok(c, cudaMalloc(&s->geom_ticket, sizeof(unsigned)), "lag")) return false;
     cudaMemsetAsync(s->geom_out, 0, sizeof(double) * 16, c->stream);
+    cudaMemsetAsync(s->geom_ticket, 0, sizeof(unsigned), c->stream);
     // [0..3) FP64 mean force, [4..6) the same rounded to FP32 (3 floats)
     if (!cuda_ok(c, cudaMalloc(&s->mean3, sizeof(double) * 8), "lag")) return false;
     cudaMemsetAsync(s->mean3, 0, sizeof(double) * 8, c->stream);
@@ -1915,24 +1925,16 @@ static void geometry_launch(Ctx* c, bool imelt, bool body_only = false, GeomPart
     { MIBM_PROF(c, "face_geom");
       face_geom_kernel<<<div_up(c->maxnf, kGeomBlock), kGeomBlock, 0, c->stream>>>(
           c->maxnf, M<int>(c, MIBM_M_VERT_OF_FACE), M<int>(c, MIBM_M_GHOST_FACE), M<double>(c, MIBM_M_XYZV),
-          M<double>(c, MIBM_M_SUR), M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_TRI_BAR), s->face_part); }
+          M<double>(c, MIBM_M_SUR), M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_TRI_BAR), s->face_part,
+          s->geom_ticket, c->S(MIBM_S_DENS_RATIO), s->geom_out); }
     ++c->launches;
   }
-  const int gnb = (int)div_up(c->maxnf, kGeomBlock);
-  if (body_only) {
-    { MIBM_PROF(c, "geom_reduce");
-      geom_reduce_kernel<<<1, 256, 0, c->stream>>>(gnb, s->face_part, c->S(MIBM_S_DENS_RATIO), s->geom_out); }
-    c->launches += 1;
-    return;
-  }
-  if (part == kGeomFaces) return;
+  if (body_only || part == kGeomFaces) return;
   { MIBM_PROF(c, "vert_geom");
     vert_geom_kernel<<<div_up(c->maxnv, 128), 128, 0, c->stream>>>(
         c->maxnv, s->adj_off, s->adj_face, M<int>(c, MIBM_M_GHOST_VERT), M<double>(c, MIBM_M_SUR),
         M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_AVERT), M<double>(c, MIBM_M_VERT_NOR)); }
-  { MIBM_PROF(c, "geom_reduce");
-    geom_reduce_kernel<<<1, 256, 0, c->stream>>>(gnb, s->face_part, c->S(MIBM_S_DENS_RATIO), s->geom_out); }
-  c->launches += 2;
+  c->launches += 1;
   if (c->maxne > 0) {           // calculate_eLengths, calculate_skewness (particle.f90:173-176)
     MIBM_PROF(c, "edges");
     elength_kernel<<<div_up(c->maxne, 128), 128, 0, c->stream>>>(
@@ -2435,7 +2437,7 @@ void lagr_free(Ctx* c) {
   for (size_t q = 0; q < g_lag.size(); ++q)
     if (g_lag[q]->c == c) {
       LagState* s = g_lag[q];
-      cudaFree(s->adj_off); cudaFree(s->adj_face); cudaFree(s->face_part); cudaFree(s->geom_out);
+      cudaFree(s->adj_off); cudaFree(s->adj_face); cudaFree(s->face_part); cudaFree(s->geom_out); cudaFree(s->geom_ticket);
       cudaFree(s->loads_ev); cudaFree(s->rm_flag);
       cudaFree(s->mean3); cudaFree(s->sdf_bits); cudaFree(s->winner); cudaFree(s->dist_buf);
       cudaFree(s->band_ub); cudaFree(s->face4); cudaFree(s->face_cell); cudaFree(s->cm32);
