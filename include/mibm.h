@@ -164,13 +164,18 @@ void mibm_register_int_(const int* id, int* addr);
 /* After registration: allocate device mirrors, wavenumbers (phini.f90:4-59),
  * coordinates; copies every registered array host -> device. */
 void mibm_init_(void);
-/* mask bit b (0..25) selects field b; bit 32+m selects mesh array m. */
+/* mask bit b (0..25) selects field b; bit 32+m selects mesh array m.     */
+/* An uploaded mesh array is compared word by word with the device copy;   */
+/* what the library derived from the mesh (scatter plan, MLS weights, the  */
+/* next step's geometry work) is redone only for arrays that changed, and */
+/* for uploads of the VOF fields or the signed distance.                   */
 void mibm_sync_from_host_(const long long* mask);
 void mibm_sync_to_host_(const long long* mask);
 /* Page-lock (on = 1) or release (on = 0) the registered host arrays of   */
-/* the bound context with cudaHostRegister, so that mibm_sync_*_ copy them  */
-/* by DMA at the host link's speed instead of through the driver's bounce   */
-/* buffers (no counterpart in the reference).  While pinned, the arrays     */
+/* the bound context with cudaHostRegister (mapped), so that mibm_sync_*_  */
+/* move them at the host link's speed: the repacking kernels read and     */
+/* write the fields in place, the mesh arrays are copied by DMA (no        */
+/* counterpart in the reference).  While pinned, the arrays                */
 /* must outlive the context or be released first; destroying the context   */
 /* releases them.  Arrays the host has already page-locked are left as they */
 /* are.  Returns a status.                                                  */
