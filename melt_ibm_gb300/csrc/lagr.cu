@@ -935,8 +935,9 @@ __global__ void heat_flux_sep_kernel(LagArgs A, const double* __restrict__ temp,
 //   e = 4  grad w   (wght_gradW, z at faces with nint, cage (icent, jcent))
 // so every warp runs one kind of evaluation.  Warp 0 then forms each face's
 // pressure force, viscous normal stress and their moments about pos_CM in
-// the reference's operation order (face_loads) and sums its 32 faces with a
-// fixed shuffle tree; loads_final_kernel adds the block sums in block order.
+// the reference's operation order (face_loads); the five warps sum the 32
+// faces' 12 values with fixed shuffle trees, and the last block to finish
+// adds the block sums in block order and updates the loads.
 // The MLS uses the separable construction of the precision form: it agrees
 // with the reference's rank-one accumulation in absolute coordinates to
 // that construction's round-off (amplified by its ~1e8 conditioning), and
@@ -956,8 +957,12 @@ loads_face_kernel(LagArgs A, const double* __restrict__ pr, const double* __rest
                   const double* __restrict__ vy, const double* __restrict__ vz, const double* __restrict__ tri_bar,
                   const double* __restrict__ tri_nor, const double* __restrict__ sur, const int* __restrict__ ghost,
                   const StepParams* __restrict__ pp, double h, double ren, double* __restrict__ part,
-                  int* __restrict__ flag) {
+                  int* __restrict__ flag, unsigned* __restrict__ ticket, RigidDev* __restrict__ r) {
+  const unsigned FULL = 0xffffffffu;
   __shared__ double ev[13][kLoadFaces];
+  __shared__ double cs[12][kLoadFaces];
+  __shared__ double tot[12];
+  __shared__ bool last;
   const int lf = threadIdx.x, e = threadIdx.y;
   const int t = blockIdx.x * kLoadFaces + lf;
   const bool live = t < A.nf && !ghost[t];
@@ -983,44 +988,49 @@ loads_face_kernel(LagArgs A, const double* __restrict__ pr, const double* __rest
     if (!ok) atomicOr(flag, 1);
   }
   __syncthreads();
-  if (e != 0) return;
-  double cf[12];
-  for (int q = 0; q < 12; ++q) cf[q] = 0.0;
-  if (live) {
-    double e13[13], rad[3];
-    for (int q = 0; q < 13; ++q) e13[q] = ev[q][lf];
-    for (int d = 0; d < 3; ++d) rad[d] = tri_bar[3 * t + d] - pp->pos[d];
-    face_loads(e13, nrm, rad, sur[t], h, ren, cf);
+  if (e == 0) {
+    double cf[12];
+    for (int q = 0; q < 12; ++q) cf[q] = 0.0;
+    if (live) {
+      double e13[13], rad[3];
+      for (int q = 0; q < 13; ++q) e13[q] = ev[q][lf];
+      for (int d = 0; d < 3; ++d) rad[d] = tri_bar[3 * t + d] - pp->pos[d];
+      face_loads(e13, nrm, rad, sur[t], h, ren, cf);
+    }
+    for (int q = 0; q < 12; ++q) cs[q][lf] = cf[q];
   }
-  for (int q = 0; q < 12; ++q) {
-    double v = cf[q];
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  __syncthreads();
+  // block sums, one quantity per warp at a time (a shuffle tree over the
+  // block's faces); the last block to finish (ticket, reset by that block)
+  // adds the block sums in block order the same way, moves the previous
+  // loads to the _m1 slots, stores the new ones and adds them to the running
+  // sums (mls_structLoads.f90:21-24, 207-262)
+  for (int q = e; q < 12; q += 5) {
+    double v = cs[q][lf];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(FULL, v, off);
     if (lf == 0) part[12 * (size_t)blockIdx.x + q] = v;
   }
-}
-
-// Sum of the block sums in block order; thread 0 moves the previous loads
-// to the _m1 slots, stores the new ones and adds them to the running sums
-// (mls_structLoads.f90:21-24, 207-262).
-__global__ void loads_final_kernel(int nb, const double* __restrict__ part, RigidDev* r) {
-  __shared__ double sm[12][256];
-  double acc[12];
-  for (int q = 0; q < 12; ++q) acc[q] = 0.0;
-  for (int b = threadIdx.x; b < nb; b += blockDim.x)
-    for (int q = 0; q < 12; ++q) acc[q] += part[12 * (size_t)b + q];
-  for (int q = 0; q < 12; ++q) sm[q][threadIdx.x] = acc[q];
+  __threadfence();
   __syncthreads();
-  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
-    if (threadIdx.x < off)
-      for (int q = 0; q < 12; ++q) sm[q][threadIdx.x] += sm[q][threadIdx.x + off];
-    __syncthreads();
+  if (lf == 0 && e == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  for (int q = e; q < 12; q += 5) {
+    double v = 0.0;
+    for (int b = lf; b < (int)gridDim.x; b += 32) v += __ldcg(part + 12 * (size_t)b + q);
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(FULL, v, off);
+    if (lf == 0) tot[q] = v;
   }
-  if (threadIdx.x == 0)
+  __syncthreads();
+  if (lf == 0 && e == 0) {
     for (int q = 0; q < 12; ++q) {        // packed [prn, tau, rprn, rtau]
       r->load1[q] = r->load[q];
-      r->load[q] = sm[q][0];
-      r->acc[q] = r->acc[q] + sm[q][0];
+      r->load[q] = tot[q];
+      r->acc[q] = r->acc[q] + tot[q];
     }
+    *ticket = 0u;
+  }
 }
 
 // face -> vertex: qw_v(v) = sum over adjacent faces (ascending) of q_f*(A_f/3/A_v)
@@ -1557,6 +1567,7 @@ struct LagState {
   double* geom_out = nullptr;   // device [Surface, Volume1, Vol, Cx, Cy, Cz, InertTensor(9)]
   unsigned* geom_ticket = nullptr;   // blocks of face_geom_kernel done (0 between launches)
   double* loads_ev = nullptr;   // structural loads: 12 block sums per 32 faces
+  unsigned* loads_ticket = nullptr;   // blocks of loads_face_kernel done (0 between launches)
   int* rm_flag = nullptr;       // remesh trigger (device)
   double* mean3 = nullptr;
   unsigned long long* sdf_bits = nullptr;
@@ -1970,19 +1981,21 @@ void lagr_geometry_to_host(Ctx* c) {
 
 static void struct_loads_launch(Ctx* c, const StepParams* dp) {
   LagState* s = lag_of(c);
-  if (!s->loads_ev &&
-      !cuda_ok(c, cudaMalloc(&s->loads_ev, sizeof(double) * 13 * std::max(1, c->maxnf)), "structLoads"))
-    return;
+  if (!s->loads_ev) {
+    if (!cuda_ok(c, cudaMalloc(&s->loads_ev, sizeof(double) * 13 * std::max(1, c->maxnf)), "structLoads") ||
+        !cuda_ok(c, cudaMalloc(&s->loads_ticket, sizeof(unsigned)), "structLoads"))
+      return;
+    cudaMemsetAsync(s->loads_ticket, 0, sizeof(unsigned), c->stream);
+  }
   double h = c->S(MIBM_S_H_EULERIAN);
   int nb = (int)div_up(c->maxnf, kLoadFaces);
   { MIBM_PROF(c, "loads_face");
     loads_face_kernel<<<nb, dim3(kLoadFaces, 5), 0, c->stream>>>(
         lag_args(c), c->df[MIBM_F_PR], c->df[MIBM_F_VX], c->df[MIBM_F_VY], c->df[MIBM_F_VZ],
         M<double>(c, MIBM_M_TRI_BAR), M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_SUR),
-        M<int>(c, MIBM_M_GHOST_FACE), dp, h, c->S(MIBM_S_REN), s->loads_ev, c->dflag); }
-  { MIBM_PROF(c, "loads_final");
-    loads_final_kernel<<<1, 256, 0, c->stream>>>(nb, s->loads_ev, c->drigid); }
-  c->launches += 2;
+        M<int>(c, MIBM_M_GHOST_FACE), dp, h, c->S(MIBM_S_REN), s->loads_ev, c->dflag, s->loads_ticket,
+        c->drigid); }
+  c->launches += 1;
 }
 
 // mls_structLoads on the device state; the loads stay in c->drigid.
@@ -2438,7 +2451,7 @@ void lagr_free(Ctx* c) {
     if (g_lag[q]->c == c) {
       LagState* s = g_lag[q];
       cudaFree(s->adj_off); cudaFree(s->adj_face); cudaFree(s->face_part); cudaFree(s->geom_out); cudaFree(s->geom_ticket);
-      cudaFree(s->loads_ev); cudaFree(s->rm_flag);
+      cudaFree(s->loads_ev); cudaFree(s->loads_ticket); cudaFree(s->rm_flag);
       cudaFree(s->mean3); cudaFree(s->sdf_bits); cudaFree(s->winner); cudaFree(s->dist_buf);
       cudaFree(s->band_ub); cudaFree(s->face4); cudaFree(s->face_cell); cudaFree(s->cm32);
       cudaFree(s->band_list); cudaFree(s->band_count);
