@@ -542,12 +542,19 @@ __global__ void __launch_bounds__(256) scatter_apply_kernel(int n, int nf, size_
 }
 
 // fixed-order sum of the recorded run sums per velocity component: 256
-// blocks over contiguous ranges of runs, then one block over the 256 partials
+// blocks over contiguous ranges of runs (shuffle trees, then the 8 warps in
+// order); the last block to finish (a ticket in mean3's slot 7, reset by that
+// block) adds the 256 block sums in block order, one component per warp, and
+// writes the means divided by the cell count (FP64 at mean3[0..2], an FP32
+// copy for the precision form at float offset 8)
 constexpr int kMeanBlocks = 256;
-__global__ void seg_partial_kernel(const int* __restrict__ nheads, const int* __restrict__ heads, size_t cells,
-                                   const int* __restrict__ key, const double* __restrict__ segval,
-                                   double* __restrict__ part) {
-  __shared__ double sm[3][256];
+__global__ void __launch_bounds__(256) seg_mean_kernel(const int* __restrict__ nheads, const int* __restrict__ heads,
+                                                      size_t cells, const int* __restrict__ key,
+                                                      const double* __restrict__ segval, double* __restrict__ part,
+                                                      double ncell, double* __restrict__ mean3) {
+  const unsigned FULL = 0xffffffffu;
+  __shared__ double ws[8][3];
+  __shared__ bool last;
   const int n = *nheads;
   int per = (n + gridDim.x - 1) / gridDim.x;
   int lo = blockIdx.x * per, hi = min(n, lo + per);
@@ -556,32 +563,36 @@ __global__ void seg_partial_kernel(const int* __restrict__ nheads, const int* __
     int comp = key_comp(key[heads[h]], cells);
     if (comp < 3) s[comp] += segval[h];
   }
-  for (int q = 0; q < 3; ++q) sm[q][threadIdx.x] = s[q];
-  __syncthreads();
-  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
-    if (threadIdx.x < off)
-      for (int q = 0; q < 3; ++q) sm[q][threadIdx.x] += sm[q][threadIdx.x + off];
-    __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int q = 0; q < 3; ++q) {
+    double v = s[q];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(FULL, v, off);
+    if (lane == 0) ws[warp][q] = v;
   }
-  if (threadIdx.x == 0)
-    for (int q = 0; q < 3; ++q) part[3 * blockIdx.x + q] = sm[q][0];
-}
-
-__global__ void seg_final_kernel(const double* __restrict__ part, double ncell, double* __restrict__ mean3) {
-  __shared__ double sm[3][kMeanBlocks];
-  for (int q = 0; q < 3; ++q) sm[q][threadIdx.x] = part[3 * threadIdx.x + q];
   __syncthreads();
-  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
-    if (threadIdx.x < off)
-      for (int q = 0; q < 3; ++q) sm[q][threadIdx.x] += sm[q][threadIdx.x + off];
-    __syncthreads();
+  if (threadIdx.x < 3) {
+    double v = ws[0][threadIdx.x];
+    for (int w = 1; w < 8; ++w) v += ws[w][threadIdx.x];
+    part[3 * (size_t)blockIdx.x + threadIdx.x] = v;
   }
-  if (threadIdx.x == 0)
-    for (int q = 0; q < 3; ++q) {
-      double m = sm[q][0] / ncell;
-      mean3[q] = m;
-      reinterpret_cast<float*>(mean3 + 4)[q] = (float)m;   // FP32 copy for the precision form
+  unsigned* ticket = reinterpret_cast<unsigned*>(mean3 + 7);
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  if (warp < 3) {
+    double v = 0.0;
+    for (int b = lane; b < (int)gridDim.x; b += 32) v += __ldcg(part + 3 * (size_t)b + warp);
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(FULL, v, off);
+    if (lane == 0) {
+      double m = v / ncell;
+      mean3[warp] = m;
+      reinterpret_cast<float*>(mean3 + 4)[warp] = (float)m;   // FP32 copy for the precision form
     }
+  }
+  if (threadIdx.x == 0) *ticket = 0u;
 }
 
 // ---------------------------------------------------------------------
@@ -1675,6 +1686,7 @@ static bool ensure_lag_buffers(Ctx* c) {
     cudaMemsetAsync(s->geom_out, 0, sizeof(double) * 16, c->stream);
     cudaMemsetAsync(s->geom_ticket, 0, sizeof(unsigned), c->stream);
     // [0..3) FP64 mean force, [4..6) the same rounded to FP32 (3 floats)
+    // [0..2] the means, [4..5] their FP32 copies, [7] seg_mean_kernel's ticket
     if (!cuda_ok(c, cudaMalloc(&s->mean3, sizeof(double) * 8), "lag")) return false;
     cudaMemsetAsync(s->mean3, 0, sizeof(double) * 8, c->stream);
   }
@@ -2331,10 +2343,9 @@ const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror,
   scatter(c, true, 0, 3, true);
   double ncell = (double)c->g.n1m * (double)c->g.n2m * (double)c->g.n3m;
   { MIBM_PROF(c, "seg_mean");
-    seg_partial_kernel<<<kMeanBlocks, 256, 0, c->stream>>>(s->nheads, s->heads, c->g.cells, s->res_key, s->segval,
-                                                           c->red + kRedPart);
-    seg_final_kernel<<<1, kMeanBlocks, 0, c->stream>>>(c->red + kRedPart, ncell, s->mean3); }
-  c->launches += 2;
+    seg_mean_kernel<<<kMeanBlocks, 256, 0, c->stream>>>(s->nheads, s->heads, c->g.cells, s->res_key, s->segval,
+                                                        c->red + kRedPart, ncell, s->mean3); }
+  c->launches += 1;
   // Fork: the rest of particle (heat flux, temperature forcing, Stefan
   // front, motion, geometry) reads and writes none of the buffers of the
   // pressure projection that the caller enqueues next, so it runs on the
