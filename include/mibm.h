@@ -308,8 +308,10 @@ void mibm_hit_bhat_(double* bhat, const int* dir);
 void mibm_hit_rng_(unsigned long long* state, const int* dir);
 /* mibm_selftest_: checks the library's integer-pipe FP64<->FP32 conversions  */
 /* (used by the precision form) against the hardware conversions, bit for  */
-/* bit, on edge cases and 2^26 random patterns.  Returns the number of      */
-/* mismatches (0 = pass), -1 without a usable GPU.                          */
+/* bit, on edge cases and 2^26 random patterns, and the line-solve factor   */
+/* table built on the device (by mibm_solxi_noalloc) against the host's     */
+/* build, bit for bit.  Returns the number of mismatches (0 = pass), -1     */
+/* without a usable GPU.                                                    */
 int  mibm_selftest_(void);
 /* Linear forcing (no counterpart in the reference, which offers only the */
 /* two forcings above): forc = C_HIT * u at each velocity's own staggered */
@@ -378,13 +380,19 @@ int  mibm_diagnostics_get_(double* out);
 /* `pitch` (elements), n2m rows and n3m planes, on `stream` (NULL = the   */
 /* legacy default stream).  Its only scratch, the line-factor table, is a  */
 /* file-scope device array sized for lines up to 512 cells (16.4 KB, held */
-/* by every GPU that loads the library until exit); n1m > 512 returns      */
-/* MIBM_EINVAL without launching.  The first call on a device looks up     */
-/* that array's device address (once per device, with the device          */
-/* current): make that first call before any stream capture.  All calls    */
-/* share the one table, rewritten in full by every call before it is read; */
-/* calls that overlap on the GPU race on it.  Nothing is allocated: no     */
-/* cudaMalloc, cudaFree or allocating library routine.  Returns a status.  */
+/* by every GPU that loads the library until exit); n1m > 512 (or n3m >    */
+/* 65535) returns MIBM_EINVAL without launching.  The first call on a      */
+/* device looks up that array's device address (once per device, with the */
+/* device current): make that first call before any stream capture.  Each */
+/* call writes the whole table on `stream` with a one-thread kernel and   */
+/* then solves; no host buffer is read.  All calls share the one table:    */
+/* calls whose work can overlap on the GPU race on it.  That includes two  */
+/* calls made one after the other from the host on DIFFERENT streams: the  */
+/* second call's table write can run while the first call's solve still   */
+/* reads the table.  Order such calls yourself (an event recorded after   */
+/* the first call and waited on by the second stream, or one stream).     */
+/* Nothing is allocated: no cudaMalloc, cudaFree or allocating library    */
+/* routine.  Returns a status.                                            */
 /* ------------------------------------------------------------------ */
 int mibm_solxi_noalloc(double* rhs, int n1m, int n2m, int n3m, int pitch, double betadx,
                        void* stream);

@@ -3,7 +3,9 @@
 // fpconv.cuh must equal the conversion instructions bit for bit (NaN: any
 // NaN) on edge cases (signed zeros, subnormals of both formats, the float
 // range limits, ties at every rounding boundary, infinities, NaNs) and on
-// random bit patterns.
+// random bit patterns.  The line-solve factor table evaluated on the device
+// (the allocation-free x-line solve builds it there) must equal the host's
+// evaluation bit for bit.
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
@@ -82,6 +84,8 @@ static void edge_cases(std::vector<unsigned long long>& v) {
   for (uint32_t x : fr) f(x);
 }
 
+long long tri_factors_selftest();   // tridiag.cu
+
 }  // namespace mibm
 
 using namespace mibm;
@@ -107,5 +111,8 @@ extern "C" int mibm_selftest_(void) {
   if (hbad[0] || hbad[1])
     fprintf(stderr, "mibm_selftest_: d2f %llu mismatches (first 0x%016llx), f2d %llu (first 0x%08llx)\n", hbad[0],
             hbad[2], hbad[1], hbad[3]);
-  return (int)std::min<unsigned long long>(hbad[0] + hbad[1], 1000000);
+  const long long tbad = tri_factors_selftest();
+  if (tbad < 0) return -1;
+  if (tbad) fprintf(stderr, "mibm_selftest_: %lld line-solve factor entries differ between host and device\n", tbad);
+  return (int)std::min<unsigned long long>(hbad[0] + hbad[1] + (unsigned long long)tbad, 1000000);
 }

@@ -35,6 +35,7 @@
 // free entry point): lines staged through shared memory in tiles of 32
 // lines, one thread running one line's sequential sweep.
 #include <cmath>
+#include <cstring>
 #include <mutex>
 #include <vector>
 
@@ -49,33 +50,71 @@ struct TriTable {
   std::vector<double> h;      // [a | b | q | s] * n, then ackl_b, api, ami, inv_den
 };
 
-// Host evaluation of the line-independent part of tridiag_periodic.
-static void build_table(int n, double betadx, std::vector<double>& t) {
-  double ackl_b = 1.0 / (1.0 + 2.0 * betadx);
-  double api = -betadx * ackl_b, ami = -betadx * ackl_b, aci = 1.0;
-  std::vector<double> q(n + 1), s(n + 1), p(n + 1);
-  q[1] = -api / aci;
-  s[1] = -ami / aci;
-  p[1] = 1.0;
-  for (int i = 2; i <= n; ++i) {
-    p[i] = 1.0 / (aci + ami * q[i - 1]);
-    q[i] = -api * p[i];
-    s[i] = -ami * s[i - 1] * p[i];
+// IEEE round-to-nearest operations in source order on both sides.  The host
+// side is compiled without floating-point contraction; the device side uses
+// the explicitly rounded intrinsics, which are never fused into FMAs.  The
+// two evaluations of tri_factors are therefore bit-identical.
+__host__ __device__ __forceinline__ double tf_mul(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __dmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+__host__ __device__ __forceinline__ double tf_add(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __dadd_rn(a, b);
+#else
+  return a + b;
+#endif
+}
+__host__ __device__ __forceinline__ double tf_div(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __ddiv_rn(a, b);
+#else
+  return a / b;
+#endif
+}
+
+// The line-independent part of tridiag_periodic.f90:22-49 for the system of
+// solxi.f90:30-44 (diagonal 1, off-diagonals -G/(1+2G), rhs scaled by
+// 1/(1+2G)), written into t[0 .. 4n+3] without any other storage:
+//   t[0..n)    a_i = (1/(1+2G)) p_i   (a_1 = (1/(1+2G)) / aci)
+//   t[n..2n)   b_i = ami p_i          (b_1 = 0)
+//   t[2n..3n)  q_i,  t[3n..4n)  s_i (after the backward pass of :45-46)
+//   t[4n..4n+3] 1/(1+2G), api, ami, 1/den (den of :47-49)
+// with the pivots p_i = 1/(aci + ami q_{i-1}) formed and used in place.
+__host__ __device__ inline void tri_factors(int n, double betadx, double* t) {
+  const double ackl_b = tf_div(1.0, tf_add(1.0, tf_mul(2.0, betadx)));
+  const double api = tf_mul(-betadx, ackl_b), ami = tf_mul(-betadx, ackl_b), aci = 1.0;
+  double* a = t;
+  double* b = t + n;
+  double* q = t + 2 * n;
+  double* s = t + 3 * n;
+  q[0] = tf_div(-api, aci);
+  s[0] = tf_div(-ami, aci);
+  a[0] = tf_div(ackl_b, aci);
+  b[0] = 0.0;
+  for (int i = 1; i < n; ++i) {
+    const double p = tf_div(1.0, tf_add(aci, tf_mul(ami, q[i - 1])));
+    q[i] = tf_mul(-api, p);
+    s[i] = tf_mul(tf_mul(-ami, s[i - 1]), p);
+    a[i] = tf_mul(ackl_b, p);
+    b[i] = tf_mul(ami, p);
   }
-  s[n] = 1.0;
-  for (int i = n - 1; i >= 1; --i) s[i] = s[i] + q[i] * s[i + 1];
-  double den = api * s[1] + ami * s[n - 1] + aci;
-  t.assign(4 * (size_t)n + 4, 0.0);
-  for (int i = 1; i <= n; ++i) {
-    t[i - 1] = (i == 1) ? ackl_b / aci : ackl_b * p[i];     // a_i
-    t[n + i - 1] = (i == 1) ? 0.0 : ami * p[i];              // b_i
-    t[2 * n + i - 1] = q[i];
-    t[3 * n + i - 1] = s[i];
-  }
+  s[n - 1] = 1.0;
+  for (int i = n - 2; i >= 0; --i) s[i] = tf_add(s[i], tf_mul(q[i], s[i + 1]));
+  const double den = tf_add(tf_add(tf_mul(api, s[0]), tf_mul(ami, s[n - 2])), aci);
   t[4 * n + 0] = ackl_b;
   t[4 * n + 1] = api;
   t[4 * n + 2] = ami;
-  t[4 * n + 3] = 1.0 / den;
+  t[4 * n + 3] = tf_div(1.0, den);
+}
+
+// Host evaluation of the factor table.
+static void build_table(int n, double betadx, std::vector<double>& t) {
+  t.assign(4 * (size_t)n + 4, 0.0);
+  tri_factors(n, betadx, t.data());
 }
 
 // the factor table of build_table for callers outside this file (the z-line
@@ -958,13 +997,21 @@ float tri_time_direction(Ctx* c, int dir, int m, bool f32, int reps) {
 // ---------------------------------------------------------------------
 // Allocation-free x-line solve (mibm_solxi_noalloc, see include/mibm.h).
 //
-// Same kernel and same factor table as solxi_, but the table lives in a
-// file-scope device array instead of memory the library allocates.  Every
-// GPU that loads the library holds this array until the process exits.
+// Same kernel and same factor table as the library's x-line solves, but the
+// table lives in a file-scope device array instead of memory the library
+// allocates.  Every GPU that loads the library holds this array until the
+// process exits.  The table is written on the device by a one-thread kernel
+// on the caller's stream (tri_factors, the function build_table runs on the
+// host, bit for bit), so the call touches no host buffer.
 // ---------------------------------------------------------------------
 constexpr int kNoAllocMaxN = 512;                      // longest x-line
 constexpr int kNoAllocTable = 4 * kNoAllocMaxN + 4;    // [a|b|q|s]*n + 4 scalars
 static __device__ __align__(256) double g_noalloc_table[kNoAllocTable];
+
+// The factor table of (n, betadx) written by one thread into `out`.
+__global__ void tri_factors_kernel(int n, double betadx, double* __restrict__ out) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) tri_factors(n, betadx, out);
+}
 
 // Host-side stand-in of g_noalloc_table is not a device address: the device
 // address is looked up once per device with that device current.
@@ -984,6 +1031,32 @@ static cudaError_t noalloc_table_address(int dev, double** out) {
   return cudaSuccess;
 }
 
+// Self-test (mibm_selftest_): the device evaluation of the factor table must
+// equal the host's build_table bit for bit.  Returns the number of differing
+// entries, or -1 on a CUDA error.
+long long tri_factors_selftest() {
+  const int ns[] = {2, 3, 16, 24, 127, 200, 256, 512};
+  const double bds[] = {1e-6, 0.004, 0.37, 0.9, 6.5, 40.0, 3.3e3};
+  double* dev = nullptr;
+  if (cudaMalloc(&dev, sizeof(double) * kNoAllocTable) != cudaSuccess) { cudaGetLastError(); return -1; }
+  long long bad = 0;
+  std::vector<double> ref, got(kNoAllocTable);
+  for (int n : ns)
+    for (double bd : bds) {
+      build_table(n, bd, ref);
+      tri_factors_kernel<<<1, 1>>>(n, bd, dev);
+      if (cudaMemcpy(got.data(), dev, sizeof(double) * ref.size(), cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cudaFree(dev);
+        cudaGetLastError();
+        return -1;
+      }
+      for (size_t q = 0; q < ref.size(); ++q)
+        if (memcmp(&ref[q], &got[q], sizeof(double)) != 0) ++bad;
+    }
+  cudaFree(dev);
+  return bad;
+}
+
 }  // namespace mibm
 
 extern "C" int mibm_solxi_noalloc(double* rhs, int n1m, int n2m, int n3m, int pitch, double betadx,
@@ -991,41 +1064,11 @@ extern "C" int mibm_solxi_noalloc(double* rhs, int n1m, int n2m, int n3m, int pi
   using namespace mibm;
   if (!rhs || n1m < 2 || n2m < 1 || n3m < 1 || pitch < n1m) return MIBM_EINVAL;
   if (n1m > kNoAllocMaxN) return MIBM_EINVAL;      // table would not fit the static scratch
+  if (n3m > 65535) return MIBM_EINVAL;             // one grid row of blocks per plane
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return MIBM_ECUDA;
   double* table = nullptr;
   if (noalloc_table_address(dev, &table) != cudaSuccess) return MIBM_ECUDA;
-  // line-independent factors, evaluated on the host into a fixed per-thread
-  // buffer (no heap), then copied in stream order ahead of the solve
-  static thread_local double host[kNoAllocTable];
-  {
-    int n = n1m;
-    double ackl_b = 1.0 / (1.0 + 2.0 * betadx);
-    double api = -betadx * ackl_b, ami = -betadx * ackl_b, aci = 1.0;
-    double* a = host; double* b = host + n; double* q = host + 2 * n; double* s = host + 3 * n;
-    // q, s and the pivots p of tridiag_periodic.f90:22-45 (0-based)
-    q[0] = -api / aci;
-    s[0] = -ami / aci;
-    a[0] = ackl_b / aci;
-    b[0] = 0.0;
-    for (int i = 1; i < n; ++i) {
-      double p = 1.0 / (aci + ami * q[i - 1]);
-      q[i] = -api * p;
-      s[i] = -ami * s[i - 1] * p;
-      a[i] = ackl_b * p;
-      b[i] = ami * p;
-    }
-    s[n - 1] = 1.0;
-    for (int i = n - 2; i >= 0; --i) s[i] = s[i] + q[i] * s[i + 1];
-    double den = api * s[0] + ami * s[n - 2] + aci;
-    host[4 * n + 0] = ackl_b;
-    host[4 * n + 1] = api;
-    host[4 * n + 2] = ami;
-    host[4 * n + 3] = 1.0 / den;
-  }
-  cudaStream_t st = (cudaStream_t)stream;
-  cudaError_t e = cudaMemcpyAsync(table, host, sizeof(double) * (4 * (size_t)n1m + 4), cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return MIBM_ECUDA;
   Grid g{};
   g.n1m = n1m; g.n2m = n2m; g.n3m = n3m; g.P = pitch;
   g.plane = (size_t)pitch * n2m; g.cells = g.plane * n3m;
@@ -1034,8 +1077,11 @@ extern "C" int mibm_solxi_noalloc(double* rhs, int n1m, int n2m, int n3m, int pi
       cudaFuncSetAttribute((const void*)solve_x_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
           cudaSuccess)
     return MIBM_ECUDA;
+  cudaStream_t st = (cudaStream_t)stream;
+  // the line-independent factors, in stream order ahead of the solve
+  tri_factors_kernel<<<1, 1, 0, st>>>(n1m, betadx, table);
+  if (cudaGetLastError() != cudaSuccess) return MIBM_ECUDA;
   dim3 grid(div_up(n2m, kLines), n3m);
   solve_x_kernel<double><<<grid, 128, sm, st>>>(g, rhs, table);
   return cudaGetLastError() == cudaSuccess ? MIBM_OK : MIBM_ECUDA;
 }
-

@@ -5,8 +5,13 @@ mibm_solxi_noalloc serves callers that own every byte of device memory
 whose HBM is reserved by a case pool) and so cannot let the library call
 cudaMalloc.  The test gives it a device buffer it did not allocate and
 checks that two calls in a row reproduce solxi_ on the same data, then that
-an oversize line is refused without a launch.  This file is collected last
-so that a run stopping at the first failure has already run every other test.
+an oversize line is refused without a launch.  Two more shapes go through the
+paths that the small case does not reach, checked against the oracle's
+solxi_: the longest line allowed (512 cells, whose shared-memory tile needs
+the opt-in above 48 KB) and a row pitch wider than the line with more than
+one block of rows (the padding between rows must come back untouched).
+This file is collected last so that a run stopping at the first failure has
+already run every other test.
 """
 from __future__ import annotations
 
@@ -66,3 +71,40 @@ def test_noalloc_solve_matches_solxi(gpu_lib):
                                     C.c_void_p(stream.cuda_stream))
     assert st == abi.MIBM_EINVAL
     assert torch.count_nonzero(big).item() == 0
+
+
+@pytest.mark.parametrize("n1m, n2m, n3m, pitch", [(512, 2, 2, 512), (200, 40, 3, 208)])
+def test_noalloc_solve_matches_oracle_at_limits(oracle_lib, gpu_lib, n1m, n2m, n3m, pitch):
+    """Lines are independent, so the first n2m rows and n3m planes of the
+    oracle's solve of an n1m x n1m x max(n3m, 4) case are the expected result
+    of the n2m-row, n3m-plane call."""
+    torch = pytest.importorskip("torch")
+    case = Case(small_config(n=n1m, n3=max(n3m, 4), velocity="rest"))
+    rng = np.random.default_rng(23 + n1m)
+    rhs0 = rng.standard_normal(case.fields[abi.MIBM_F_RHS].shape)
+    case.fields[abi.MIBM_F_RHS][...] = rhs0
+    case.attach(oracle_lib, initial_tag=False)
+    expect = {}
+    for b in (0.37, 6.5):
+        case.fields[abi.MIBM_F_RHS][...] = rhs0
+        case.bind(oracle_lib)
+        oracle_lib.solxi_(C.byref(C.c_double(b)))
+        oracle_lib.check("solxi_")
+        expect[b] = case.interior(abi.MIBM_F_RHS)[:, :n2m, :n3m].copy()
+    case.detach(oracle_lib)
+
+    # caller-owned buffer [k][j][pitch]: the row padding holds its own values
+    buf_h = rng.standard_normal((n3m, n2m, pitch))
+    buf_h[:, :, :n1m] = rhs0[:n1m, :n2m, :n3m].transpose(2, 1, 0)
+    dev = torch.cuda.current_device()
+    stream = torch.cuda.current_stream()
+    for b in (0.37, 6.5):                              # two calls in a row
+        buf = torch.from_numpy(buf_h.copy()).to(f"cuda:{dev}")
+        st = gpu_lib.mibm_solxi_noalloc(C.c_void_p(buf.data_ptr()), n1m, n2m, n3m, pitch, b,
+                                        C.c_void_p(stream.cuda_stream))
+        assert st == abi.MIBM_OK
+        torch.cuda.synchronize()
+        out = buf.cpu().numpy()
+        got = out[:, :, :n1m].transpose(2, 1, 0)
+        assert rel_l2(got, expect[b]) <= 1e-12, (n1m, b)
+        assert np.array_equal(out[:, :, n1m:], buf_h[:, :, n1m:])
