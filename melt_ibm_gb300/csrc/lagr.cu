@@ -544,8 +544,10 @@ __global__ void __launch_bounds__(256) scatter_apply_kernel(int n, int nf, size_
 // fixed-order sum of the recorded run sums per velocity component: 256
 // blocks over contiguous ranges of runs (shuffle trees, then the 8 warps in
 // order); the last block to finish (a ticket in mean3's slot 7, reset by that
-// block) adds the 256 block sums in block order, one component per warp, and
-// writes the means divided by the cell count (FP64 at mean3[0..2], an FP32
+// block) adds the 256 block sums, one component per warp: lane l sums blocks
+// l, l+32, l+64, ... in that order, then a fixed shuffle tree adds the 32
+// lane sums (a fixed order, so the result is deterministic); it writes the
+// means divided by the cell count (FP64 at mean3[0..2], an FP32
 // copy for the precision form at float offset 8)
 constexpr int kMeanBlocks = 256;
 __global__ void __launch_bounds__(256) seg_mean_kernel(const int* __restrict__ nheads, const int* __restrict__ heads,
@@ -948,7 +950,8 @@ __global__ void heat_flux_sep_kernel(LagArgs A, const double* __restrict__ temp,
 // pressure force, viscous normal stress and their moments about pos_CM in
 // the reference's operation order (face_loads); the five warps sum the 32
 // faces' 12 values with fixed shuffle trees, and the last block to finish
-// adds the block sums in block order and updates the loads.
+// adds the block sums (lane l takes blocks l, l+32, ... in order, then a
+// fixed shuffle tree) and updates the loads.
 // The MLS uses the separable construction of the precision form: it agrees
 // with the reference's rank-one accumulation in absolute coordinates to
 // that construction's round-off (amplified by its ~1e8 conditioning), and
@@ -1013,7 +1016,8 @@ loads_face_kernel(LagArgs A, const double* __restrict__ pr, const double* __rest
   __syncthreads();
   // block sums, one quantity per warp at a time (a shuffle tree over the
   // block's faces); the last block to finish (ticket, reset by that block)
-  // adds the block sums in block order the same way, moves the previous
+  // adds the block sums the same way (lane l takes blocks l, l+32, ... in
+  // order, then a fixed shuffle tree), moves the previous
   // loads to the _m1 slots, stores the new ones and adds them to the running
   // sums (mls_structLoads.f90:21-24, 207-262)
   for (int q = e; q < 12; q += 5) {
@@ -1142,8 +1146,9 @@ __device__ void geom_finish(const double* sm, double dens_ratio, double* __restr
 // One thread per face.  The 12 per-face sums are added over the block (one
 // quantity per warp: four values per lane in thread order, then a shuffle
 // tree) into part[12 * block + q]; the last block to finish (a ticket
-// counter, reset by that block) adds the block sums in block order the same
-// way and writes the body's scalars to out.  Each warp's dependent FP64
+// counter, reset by that block) adds the block sums the same way (lane l
+// takes blocks l, l+32, ... in order, then a fixed shuffle tree over the
+// lanes) and writes the body's scalars to out.  Each warp's dependent FP64
 // chain is a few additions per quantity: on this part an FP64 warp
 // instruction holds the pipe for about 64 cycles however few lanes run.
 constexpr int kGeomBlock = 128;
