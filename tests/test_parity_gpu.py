@@ -59,13 +59,17 @@ def test_stencil_routine_parity(oracle_lib, gpu_lib, routine, n):
     _cmp_fields(co, cg, STENCIL_ROUTINES[routine])
 
 
-@pytest.mark.parametrize("n, n3", [(16, None), (24, None), (48, None), (192, 8), (32, 256), (24, 18)])
+@pytest.mark.parametrize("n, n3", [(16, None), (24, None), (48, None), (192, 8), (32, 256), (24, 18),
+                                   (128, None), (256, None)])
 def test_phcalc_parity(oracle_lib, gpu_lib, n, n3):
     """Poisson solve; the z lines are chunked below 16384 (kx, ky) lines
-    (32 x 32 x 256: 16 chunks of 16, the largest block) and swept one per
-    thread from there on (192 x 192 x 8: 18624 lines) or where no chunk
-    length divides the line (24 x 24 x 18)."""
-    case = Case(small_config(n=n, n3=n3, velocity="random" if n3 is None else "rest"))
+    (32 x 32 x 256: 16 chunks of 16, the largest block; 128^3: 8320 lines)
+    and swept one per thread from there on (192 x 192 x 8: 18624 lines;
+    256^3: 33024) or where no chunk length divides the line (24 x 24 x 18).
+    128^3 and 256^3 run the compile-time x/y transforms of those lengths, the
+    instances the 128^3 and 256^3 configurations use."""
+    small = n3 is None and n <= 48
+    case = Case(small_config(n=n, n3=n3, velocity="random" if small else "rest"))
     randomize(case)
     co, cg = pair(case, oracle_lib, gpu_lib, initial_tag=False)
     for c, lib in ((co, oracle_lib), (cg, gpu_lib)):
