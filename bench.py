@@ -185,6 +185,29 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+class Nvtx:
+    """An NVTX range around a timed region (`bench_f64`, `bench_f32`), so that
+    an ncu capture can select exactly the timed steps with --nvtx
+    --nvtx-include "bench_f64/".  No-op without torch."""
+
+    def __init__(self, name: str):
+        self.name = name
+        try:
+            import torch
+            self.nvtx = torch.cuda.nvtx
+        except Exception:  # noqa: BLE001
+            self.nvtx = None
+
+    def __enter__(self):
+        if self.nvtx is not None:
+            self.nvtx.range_push(self.name)
+        return self
+
+    def __exit__(self, *exc):
+        if self.nvtx is not None:
+            self.nvtx.range_pop()
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -301,7 +324,7 @@ def run_gpu(args):
     # ---------------- timed region: device-resident ----------------
     dist.barrier()
     l0 = lib.mibm_launch_count_()
-    with ClockSampler(dev) as clk:
+    with ClockSampler(dev) as clk, Nvtx("bench_f64"):
         lib.mibm_timer_mark_(abi.ref_int(0))
         t0 = time.perf_counter()
         for _ in range(args.steps):
@@ -399,11 +422,12 @@ def run_gpu(args):
             nt32 += 1
         case32.sync_to_host(lib, 0)
         dist.barrier()
-        lib.mibm_timer_mark_(abi.ref_int(2))
-        for _ in range(args.steps):
-            case32.step(lib, nt32)
-            nt32 += 1
-        lib.mibm_timer_mark_(abi.ref_int(3))
+        with Nvtx("bench_f32"):
+            lib.mibm_timer_mark_(abi.ref_int(2))
+            for _ in range(args.steps):
+                case32.step(lib, nt32)
+                nt32 += 1
+            lib.mibm_timer_mark_(abi.ref_int(3))
         ms32 = dist.max(lib.mibm_timer_ms_(abi.ref_int(2), abi.ref_int(3)))
         lib.check("precision form")
         div32 = lib.mibm_divergence_max_()
@@ -515,18 +539,23 @@ def extra_workload_measurement(lib, workload: str, steps: int, warmup: int, npro
 
 def batched_measurement(lib, steps: int, warmup: int, seed: int = 100) -> dict:
     """Batched form on the batched configuration's mix: 32 cases (12 x 48^3,
-    10 x 64^3, 6 x 96^3, 4 x 128^3), icosphere level 2-4 and radius 0.3-0.6
-    uniform, St log-uniform in [0.5, 4], nu uniform in [0.005, 0.02], seeds
-    100-131, precision form, shapes autotuned; timed against stepping the
+    10 x 64^3, 6 x 96^3, 4 x 128^3), radius 0.3-0.6 uniform, icosphere level
+    2-4 by the resolution rule of serve.resolved_level, St log-uniform in
+    [0.5, 4], nu uniform in [0.005, 0.02], seeds 100-131, precision form,
+    shapes autotuned; timed against stepping the
     same cases one after another.  Host wall clock around whole batch steps
     (each ends with a device synchronisation)."""
     from melt_ibm_gb300.batch import BatchRunner
+    from melt_ibm_gb300.serve import resolved_level
     rng = np.random.default_rng(seed)
     sizes = [48] * 12 + [64] * 10 + [96] * 6 + [128] * 4
-    cfgs = [CaseConfig(n=n, mesh_level=int(rng.integers(2, 5)), rad_p=float(rng.uniform(0.3, 0.6)),
-                       ren=float(1.0 / rng.uniform(0.005, 0.02)),
-                       latheat=float(1.0 / np.exp(rng.uniform(np.log(0.5), np.log(4.0)))), seed=seed + q,
-                       v_on_ve=0.0) for q, n in enumerate(sizes)]
+    cfgs = []
+    for q, n in enumerate(sizes):
+        rad = float(rng.uniform(0.3, 0.6))
+        cfgs.append(CaseConfig(n=n, mesh_level=resolved_level(n, rad), rad_p=rad,
+                               ren=float(1.0 / rng.uniform(0.005, 0.02)),
+                               latheat=float(1.0 / np.exp(rng.uniform(np.log(0.5), np.log(4.0)))), seed=seed + q,
+                               v_on_ve=27.0))
     t0 = time.perf_counter()
     proto = [Case(c) for c in cfgs]
     setup_s = time.perf_counter() - t0
@@ -578,8 +607,8 @@ def batched_measurement(lib, steps: int, warmup: int, seed: int = 100) -> dict:
             "cells": cells, "steps": steps, "warmup": warmup, "ms_per_step": 1e3 * t_batch / steps,
             "sequential_value": cells * steps / t_seq / 1e6, "speedup_vs_sequential": t_seq / t_batch,
             "autotuned_shapes": shapes, "host_setup_s": setup_s, "form": "precision (f32 compute, f64 fields)",
-            "config": "32 cases: 12x48^3, 10x64^3, 6x96^3, 4x128^3; level 2-4, r 0.3-0.6, St log-U[0.5,4], "
-                      "nu U[0.005,0.02], seeds 100-131",
+            "config": "32 cases: 12x48^3, 10x64^3, 6x96^3, 4x128^3; r 0.3-0.6, level 2-4 by the mesh-resolution "
+                      "rule, St log-U[0.5,4], nu U[0.005,0.02], seeds 100-131",
             "timing": "host wall clock around batch steps (each ends synchronised)"}
 
 

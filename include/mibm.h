@@ -256,8 +256,16 @@ void mibm_set_graphs_(const int* on);
 /* reductions overlap, their step graphs run as one batch graph (one child */
 /* node per case, no edges: the device interleaves them), and each case    */
 /* gets exactly the result of stepping it alone.  create returns a handle  */
-/* > 0 (0 on error); step returns a status (ntime <= 0: each case uses its */
-/* own completed-step count + 1); destroy the batch before its contexts.   */
+/* > 0 (0 on error; an empty member list is allowed); step returns a     */
+/* status (ntime <= 0: each case uses its own completed-step count + 1).   */
+/* A case that fails during a batch step (non-finite field, allocation or  */
+/* CUDA error in its own work) is left out of the rest of that step with    */
+/* its status kept in its context, and the step returns that status; the  */
+/* other cases complete the step exactly as they would alone.  add/remove */
+/* change the members between steps (serving: cases join and leave);       */
+/* set_launch chooses 0 = one batch graph (default, rebuilt when members   */
+/* change) or 1 = each case's own step graph on its own stream (no rebuild */
+/* when members change).  Destroy the batch before its contexts.           */
 /* Autotuner (no counterpart in the reference): times the feasible chunk    */
 /* lengths of the x-, y- and z-line solves and the block heights of the    */
 /* explicit-term kernel on the bound context (scratch data; its state is   */
@@ -271,6 +279,9 @@ int  mibm_autotune_load_(const char* path);
 int mibm_batch_create_(const int* ids, const int* n);
 int mibm_batch_step_(const int* handle, const int* ntime);
 int mibm_batch_destroy_(const int* handle);
+int mibm_batch_add_(const int* handle, const int* id);
+int mibm_batch_remove_(const int* handle, const int* id);
+int mibm_batch_set_launch_(const int* handle, const int* mode);
 /* max over the owned cells of |div u| as divgck computes it
  * (divg.f90:26-56); synchronises with the device. */
 double mibm_divergence_max_(void);

@@ -76,6 +76,9 @@ SIGNATURES: dict[str, tuple] = {
     "mibm_batch_create_": (C.c_int, [C.c_void_p, _I]),
     "mibm_batch_step_": (C.c_int, [_I, _I]),
     "mibm_batch_destroy_": (C.c_int, [_I]),
+    "mibm_batch_add_": (C.c_int, [_I, _I]),
+    "mibm_batch_remove_": (C.c_int, [_I, _I]),
+    "mibm_batch_set_launch_": (C.c_int, [_I, _I]),
     "mibm_divergence_max_": (C.c_double, []),
     "mibm_set_remesh_callback_": (None, [C.c_void_p, C.c_void_p]),
     "mibm_pin_host_": (C.c_int, [_I]),

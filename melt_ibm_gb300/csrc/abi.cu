@@ -17,6 +17,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "common.cuh"
 
 namespace mibm {
@@ -465,6 +467,7 @@ static int autotune(Ctx* c) {
 // ---------------------------------------------------------------------
 struct Batch {
   std::vector<int> ids;
+  int launch = 0;                            // 0: one batch graph; 1: each case's graph on its own stream
   cudaStream_t stream = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -488,14 +491,32 @@ static void batch_drop_graph(Batch* b) {
   b->built_from.clear();
 }
 
+// One batch step.  A case that fails (non-finite field, allocation or CUDA
+// error in its own work) is left out of the rest of the step with its status
+// kept in its context; the other cases complete the step exactly as they
+// would alone.  Returns MIBM_OK, or the first failing case's status (the host
+// finds the failed cases with mibm_context_bind_ + mibm_last_status_).
 static int batch_step(Batch* b, int ntime) {
-  std::vector<Ctx*> cs;
-  for (int id : b->ids) {
-    Ctx* c = context_by_id(id);
-    if (!c || !ready(c)) { fail(c, MIBM_ESTATE, "batch: context " + std::to_string(id) + " is gone or not initialised"); return MIBM_ESTATE; }
-    if (c->status != MIBM_OK) return c->status;
-    cs.push_back(c);
+  std::vector<Ctx*> all;
+  {
+    std::lock_guard<std::mutex> g(g_batch_mu);
+    for (int id : b->ids) {
+      Ctx* c = context_by_id(id);
+      if (!c || !ready(c)) { fail(c, MIBM_ESTATE, "batch: context " + std::to_string(id) + " is gone or not initialised"); return MIBM_ESTATE; }
+      all.push_back(c);
+    }
   }
+  int first_bad = MIBM_OK;
+  auto drop_failed = [&](std::vector<Ctx*>& v) {
+    std::vector<Ctx*> keep;
+    for (Ctx* c : v) {
+      if (c->status == MIBM_OK) keep.push_back(c);
+      else if (first_bad == MIBM_OK) first_bad = c->status;
+    }
+    v.swap(keep);
+  };
+  std::vector<Ctx*> cs = all;
+  drop_failed(cs);
   // (A) CFL and dt reductions of every case, gcurv.f90:153-160; ntime <= 0:
   // every case counts its own steps (cases that joined at different times)
   for (Ctx* c : cs) {
@@ -506,8 +527,8 @@ static int batch_step(Batch* b, int ntime) {
     if (c->I(MIBM_I_IDTV) == 1) k_getdt_async(c, c->S(MIBM_S_DT), c->red_host + 1);
   }
   for (Ctx* c : cs) {
-    if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "batch cfl")) return c->status;
-    if (!cfl_finite(c)) return c->status;
+    if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "batch cfl")) continue;
+    if (!cfl_finite(c)) continue;
     *c->hs[MIBM_S_CFLM] = cfl_value(c->red_host[0]);
     if (c->I(MIBM_I_IDTV) == 1) {
       double dt = c->S(MIBM_S_DT);
@@ -515,6 +536,7 @@ static int batch_step(Batch* b, int ntime) {
       if (buf > 0.0) *c->hs[MIBM_S_DT] = dt * c->S(MIBM_S_CFLFIX) / buf;
     }
   }
+  drop_failed(cs);
   // (B) forcing (gcurv.f90:164-170) and the host part of each step
   for (Ctx* c : cs) {
     if (c->I(MIBM_I_FORCING) == 1) {
@@ -523,21 +545,23 @@ static int batch_step(Batch* b, int ntime) {
       else if (which == 2) k_hit_abc_force(c);
       else if (which == 3) k_hit_linear_force(c);
     }
-    if (c->status != MIBM_OK || !step_prepare(c)) return c->status != MIBM_OK ? c->status : MIBM_ESTATE;
+    if (c->status != MIBM_OK) continue;
+    if (!step_prepare(c)) { if (c->status == MIBM_OK) fail(c, MIBM_ESTATE, "batch: step preparation"); continue; }
     step_head(c);
-    if (c->status != MIBM_OK) return c->status;
   }
+  drop_failed(cs);
   // (C) device work: step graphs (captured where missing or stale)
-  bool all_graphs = true;
+  bool all_graphs = b->launch == 0;
   for (Ctx* c : cs) {
     bool graph = graphs_allowed(c);
     if (graph) {
       uint64_t key = step_key(c);
       if (!c->graph_exec || key != c->graph_key) graph = capture_step(c, key);
     }
-    all_graphs = all_graphs && graph;
-    if (c->status != MIBM_OK) return c->status;
+    all_graphs = all_graphs && graph && c->status == MIBM_OK;
   }
+  drop_failed(cs);
+  if (cs.empty()) return first_bad;
   if (all_graphs) {
     std::vector<cudaGraphExec_t> now;
     for (Ctx* c : cs) now.push_back(c->graph_exec);
@@ -562,30 +586,41 @@ static int batch_step(Batch* b, int ntime) {
   } else {
     for (Ctx* c : cs) {
       if (c->graph_exec && graphs_allowed(c)) {
-        if (!cuda_ok(c, cudaGraphLaunch(c->graph_exec, c->stream), "step graph")) return c->status;
-        c->launches += c->graph_kernels;
+        if (cuda_ok(c, cudaGraphLaunch(c->graph_exec, c->stream), "step graph")) c->launches += c->graph_kernels;
       } else {
         step_enqueue(c);
       }
-      if (c->status != MIBM_OK) return c->status;
     }
   }
   // (D) per-case host checks, time
-  int st = MIBM_OK;
   for (Ctx* c : cs) {
     step_finish(c);
-    if (c->status != MIBM_OK && st == MIBM_OK) st = c->status;
+    if (c->status != MIBM_OK) {
+      if (first_bad == MIBM_OK) first_bad = c->status;
+      continue;
+    }
     *c->hs[MIBM_S_TIME] = c->S(MIBM_S_TIME) + c->S(MIBM_S_DT);
   }
-  return st;
+  return first_bad;
 }
 
 }  // namespace mibm
 
 using namespace mibm;
 
-#define DROPIN_BEGIN          \
-  Ctx* c = current();         \
+// Every drop-in routine is one NVTX range named after the routine (the
+// per-routine tracing of the reference's TIMED build, tsch.f90:26-84, for
+// Nsight tools).  NVTX v3 is header-only: without a tool attached a range
+// costs a branch.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
+#define DROPIN_BEGIN                          \
+  NvtxRange mibm_nvtx_range_(__func__);       \
+  Ctx* c = current();                         \
   if (!ready(c)) return;
 // drop-in routines that write u, v, w, T or p: the FP32 mirrors of the
 // precision form are rebuilt before its next step
@@ -732,7 +767,7 @@ void mibm_set_precision_(const int* mode, const int* nproj) {
 // initial tagging); returns a handle > 0, or 0 with the status in
 // mibm_last_status_.
 int mibm_batch_create_(const int* ids, const int* n) {
-  if (!ids || *n < 1) { fail(nullptr, MIBM_EINVAL, "batch_create: empty batch"); return 0; }
+  if (*n < 0 || (!ids && *n > 0)) { fail(nullptr, MIBM_EINVAL, "batch_create: bad member list"); return 0; }
   Batch* b = new Batch();
   for (int q = 0; q < *n; ++q) {
     Ctx* c = context_by_id(ids[q]);
@@ -757,9 +792,51 @@ int mibm_batch_create_(const int* ids, const int* n) {
 // of the batch; ntime as in gcurv.f90:151, or <= 0 for each case's own step
 // count + 1.  Returns a status.
 int mibm_batch_step_(const int* handle, const int* ntime) {
+  NvtxRange range("mibm_batch_step_");
   Batch* b = batch_of(*handle);
   if (!b) { fail(nullptr, MIBM_EINVAL, "batch_step: unknown batch"); return MIBM_EINVAL; }
   return batch_step(b, *ntime);
+}
+
+// Membership of a batch between steps: add a context (initialised, not yet a
+// member) or remove one.  Returns a status.  Removing the last member leaves
+// an empty batch whose steps do nothing.
+int mibm_batch_add_(const int* handle, const int* id) {
+  Batch* b = batch_of(*handle);
+  if (!b) { fail(nullptr, MIBM_EINVAL, "batch_add: unknown batch"); return MIBM_EINVAL; }
+  Ctx* c = context_by_id(*id);
+  if (!c || !ready(c)) { fail(nullptr, MIBM_EINVAL, "batch_add: context not initialised"); return MIBM_EINVAL; }
+  std::lock_guard<std::mutex> g(g_batch_mu);
+  for (int q : b->ids)
+    if (q == *id) { fail(nullptr, MIBM_EINVAL, "batch_add: context already a member"); return MIBM_EINVAL; }
+  b->ids.push_back(*id);
+  return MIBM_OK;
+}
+
+int mibm_batch_remove_(const int* handle, const int* id) {
+  Batch* b = batch_of(*handle);
+  if (!b) { fail(nullptr, MIBM_EINVAL, "batch_remove: unknown batch"); return MIBM_EINVAL; }
+  std::lock_guard<std::mutex> g(g_batch_mu);
+  for (size_t q = 0; q < b->ids.size(); ++q)
+    if (b->ids[q] == *id) {
+      b->ids.erase(b->ids.begin() + q);
+      return MIBM_OK;
+    }
+  fail(nullptr, MIBM_EINVAL, "batch_remove: not a member");
+  return MIBM_EINVAL;
+}
+
+// How a batch step launches its cases' step graphs: 0 = one batch graph of
+// child-graph nodes (rebuilt when the members or their graphs change), 1 =
+// each case's own step graph on its own stream (nothing to rebuild when cases
+// join or leave).  The results are the same either way.
+int mibm_batch_set_launch_(const int* handle, const int* mode) {
+  Batch* b = batch_of(*handle);
+  if (!b) { fail(nullptr, MIBM_EINVAL, "batch_set_launch: unknown batch"); return MIBM_EINVAL; }
+  if (*mode != 0 && *mode != 1) { fail(nullptr, MIBM_EINVAL, "batch_set_launch: mode 0|1"); return MIBM_EINVAL; }
+  b->launch = *mode;
+  if (b->launch == 1) batch_drop_graph(b);
+  return MIBM_OK;
 }
 
 int mibm_batch_destroy_(const int* handle) {

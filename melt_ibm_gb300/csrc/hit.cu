@@ -6,16 +6,25 @@
 // (a few hundred modes); the physical-space sums
 //   forcx(i,j,k) = Re sum_{l,m,n} Fhat(1,l,m,n) e^{i kl xc_i} e^{i km ym_j} e^{i kn zm_k}
 // (and the staggered variants for forcy, forcz) run on the device.  The sum
-// factorises: H_c(l; j, k) = sum_{m,n} Fhat(c,l,m,n) e^{i km y_j} e^{i kn z_k}
-// is formed once per (l, j, k), then every cell needs nmodes complex
-// products instead of nmodes^3 -- the reference's O(nmodes^3 N^3) loops
-// become O(nmodes^2 N^2 + nmodes N^3).  The exponential tables are the
-// reference's (InitRandomForce, hit.f90:171-202), evaluated on the host.
+// factorises one axis at a time:
+//   G_c(l, n; j) = sum_m Fhat(c,l,m,n) e^{i km y_j}          (nmodes^3 N)
+//   H_c(l; j, k) = sum_n G_c(l, n; j) e^{i kn z_k}            (nmodes^2 N^2)
+// and, because only the real part is kept and e^{-i kl x} is the conjugate
+// of e^{i kl x}, the modes +l and -l fold into one coefficient:
+//   Re(e H(l)) + Re(conj(e) H(-l)) = Re(e (H(l) + conj(H(-l)))),
+// so every cell needs (nmodes+1)/2 complex-real products (the l = 0 one is a
+// plain real part) instead of nmodes^3 -- the reference's O(nmodes^3 N^3)
+// loops become O(nmodes^2 N^2 + nmodes N^3 / 2).  The sums are the
+// reference's in another order (agreement to round-off).  The exponential
+// tables are the reference's (InitRandomForce, hit.f90:171-202), evaluated
+// on the host.  The precision form evaluates the last, per-cell stage in
+// FP32 from FP32 copies of the tables (the forcing fields stay FP64).
 //
 // ABC forcing (CalcABC_HITForce, hit.f90:224-254) uses host tables of the
 // sines and cosines of each coordinate line.
 #include <cmath>
 #include <complex>
+#include <cstring>
 #include <vector>
 
 #include "common.cuh"
@@ -32,7 +41,12 @@ struct HitState {
   double2* d_ex = nullptr;            // [xc | xm] x nmodes x n1m  : e^{i k x}
   double2* d_ey = nullptr;            // [ym | yc] x nmodes x n2m
   double2* d_ez = nullptr;            // [zm | zc] x nmodes x n3m
-  double2* d_h = nullptr;             // 3 x nmodes x n2m x n3m
+  double2* d_g = nullptr;             // G: 3 x nmodes x nmodes x n2m
+  double2* d_h = nullptr;             // folded H: 3 x nb x n3m x n2m, nb = (nmodes + 1) / 2
+  float2* d_ex32 = nullptr;           // FP32 copy of d_ex (precision form)
+  float2* d_h32 = nullptr;            // FP32 copy of d_h (precision form)
+  double2* h_fhat = nullptr;          // pinned staging of Fhat (3 * nmodes^3)
+  cudaEvent_t fhat_copied = nullptr;  // the staging buffer has been read by its copy
   double* d_abc = nullptr;            // ABC tables: sin/cos per axis
 };
 
@@ -51,6 +65,8 @@ void hit_free(Ctx* c) {
     if (g_hit[q].first == c) {
       HitState* h = g_hit[q].second;
       cudaFree(h->d_fhat); cudaFree(h->d_ex); cudaFree(h->d_ey); cudaFree(h->d_ez); cudaFree(h->d_h);
+      cudaFree(h->d_g); cudaFree(h->d_ex32); cudaFree(h->d_h32); cudaFreeHost(h->h_fhat);
+      if (h->fhat_copied) cudaEventDestroy(h->fhat_copied);
       cudaFree(h->d_abc);
       delete h;
       g_hit.erase(g_hit.begin() + q);
@@ -86,7 +102,9 @@ static bool hit_setup(Ctx* c, HitState* h) {
   int nm = hit_nmodes(c->S(MIBM_S_KF_ON_KMIN));
   if (nm == h->nmodes && h->n1 == g.n1m && h->n2 == g.n2m && h->n3 == g.n3m && h->d_fhat) return true;
   cudaFree(h->d_fhat); cudaFree(h->d_ex); cudaFree(h->d_ey); cudaFree(h->d_ez); cudaFree(h->d_h);
-  h->d_fhat = nullptr; h->d_ex = h->d_ey = h->d_ez = h->d_h = nullptr;
+  cudaFree(h->d_g); cudaFree(h->d_ex32); cudaFree(h->d_h32); cudaFreeHost(h->h_fhat);
+  h->d_fhat = nullptr; h->d_ex = h->d_ey = h->d_ez = h->d_h = h->d_g = nullptr;
+  h->d_ex32 = nullptr; h->d_h32 = nullptr; h->h_fhat = nullptr;
   h->nmodes = nm; h->n1 = g.n1m; h->n2 = g.n2m; h->n3 = g.n3m;
   if (h->bhat.size() != 6 * (size_t)nm * nm * nm) h->bhat.assign(6 * (size_t)nm * nm * nm, 0.0);
   int nbuffer = (nm - 1) / 2 + 1;
@@ -112,15 +130,25 @@ static bool hit_setup(Ctx* c, HitState* h) {
   table(g.n2m, g.ylen, true, ey, (size_t)nm * g.n2m);        // exp_I_km_ysj (yc)
   table(g.n3m, g.zlen, false, ez, 0);                        // exp_I_kn_zk  (zm)
   table(g.n3m, g.zlen, true, ez, (size_t)nm * g.n3m);        // exp_I_kn_zsk (zc)
+  const int nb = (nm + 1) / 2;
+  std::vector<float2> ex32(ex.size());
+  for (size_t q = 0; q < ex.size(); ++q) ex32[q] = make_float2((float)ex[q].x, (float)ex[q].y);
   bool ok = cuda_ok(c, cudaMalloc(&h->d_fhat, sizeof(double2) * 3 * (size_t)nm * nm * nm), "hit") &&
             cuda_ok(c, cudaMalloc(&h->d_ex, sizeof(double2) * ex.size()), "hit") &&
             cuda_ok(c, cudaMalloc(&h->d_ey, sizeof(double2) * ey.size()), "hit") &&
             cuda_ok(c, cudaMalloc(&h->d_ez, sizeof(double2) * ez.size()), "hit") &&
-            cuda_ok(c, cudaMalloc(&h->d_h, sizeof(double2) * 3 * (size_t)nm * g.n2m * g.n3m), "hit");
+            cuda_ok(c, cudaMalloc(&h->d_g, sizeof(double2) * 3 * (size_t)nm * nm * g.n2m), "hit") &&
+            cuda_ok(c, cudaMalloc(&h->d_h, sizeof(double2) * 3 * (size_t)nb * g.n2m * g.n3m), "hit") &&
+            cuda_ok(c, cudaMalloc(&h->d_ex32, sizeof(float2) * ex32.size()), "hit") &&
+            cuda_ok(c, cudaMalloc(&h->d_h32, sizeof(float2) * 3 * (size_t)nb * g.n2m * g.n3m), "hit") &&
+            cuda_ok(c, cudaMallocHost(&h->h_fhat, sizeof(double2) * 3 * (size_t)nm * nm * nm), "hit");
   if (!ok) return false;
+  if (!h->fhat_copied && !cuda_ok(c, cudaEventCreateWithFlags(&h->fhat_copied, cudaEventDisableTiming), "hit"))
+    return false;
   cudaMemcpy(h->d_ex, ex.data(), sizeof(double2) * ex.size(), cudaMemcpyHostToDevice);
   cudaMemcpy(h->d_ey, ey.data(), sizeof(double2) * ey.size(), cudaMemcpyHostToDevice);
   cudaMemcpy(h->d_ez, ez.data(), sizeof(double2) * ez.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(h->d_ex32, ex32.data(), sizeof(float2) * ex32.size(), cudaMemcpyHostToDevice);
   return cuda_ok(c, cudaGetLastError(), "hit tables");
 }
 
@@ -128,50 +156,81 @@ __device__ __forceinline__ double2 cmul2(double2 a, double2 b) {
   return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
-// H_c(l; j, k) = sum_n sum_m Fhat(c,l,m,n) * (e_y(j,m) * e_z(k,n)); one thread per (c, l, j, k)
-__global__ void hit_h_kernel(Grid g, int nm, const double2* __restrict__ fhat, const double2* __restrict__ ey,
-                             const double2* __restrict__ ez, double2* __restrict__ H) {
+// G_c(l, n; j) = sum_m Fhat(c,l,m,n) e_y(j,m); one thread per (c, l, n, j)
+__global__ void hit_g_kernel(Grid g, int nm, const double2* __restrict__ fhat, const double2* __restrict__ ey,
+                             double2* __restrict__ G) {
   size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  size_t plane = (size_t)g.n2m * g.n3m;
-  if (t >= 3 * (size_t)nm * plane) return;
-  int c = (int)(t / ((size_t)nm * plane));
-  size_t r = t - (size_t)c * nm * plane;
-  int l = (int)(r / plane);
-  size_t jk = r - (size_t)l * plane;
-  int j = (int)(jk % g.n2m), k = (int)(jk / g.n2m);
-  // forcx, forcz use ym; forcy uses yc.  forcx, forcy use zm; forcz uses zc.
+  if (t >= 3 * (size_t)nm * nm * g.n2m) return;
+  const int j = (int)(t % g.n2m);
+  size_t r = t / g.n2m;
+  const int n = (int)(r % nm);
+  r /= nm;
+  const int l = (int)(r % nm), c = (int)(r / nm);
+  // forcx, forcz use ym; forcy uses yc
   const double2* eyc = ey + (c == 1 ? (size_t)nm * g.n2m : 0);
-  const double2* ezc = ez + (c == 2 ? (size_t)nm * g.n3m : 0);
   double2 acc = make_double2(0.0, 0.0);
-  for (int n = 0; n < nm; ++n) {
-    double2 zk = ezc[(size_t)n * g.n3m + k];
-    for (int m = 0; m < nm; ++m) {
-      double2 b = cmul2(eyc[(size_t)m * g.n2m + j], zk);                       // buff1
-      double2 f = fhat[(size_t)c + 3 * ((size_t)l + nm * ((size_t)m + (size_t)nm * n))];
-      double2 p = cmul2(f, b);
-      acc.x += p.x; acc.y += p.y;
-    }
+  for (int m = 0; m < nm; ++m) {
+    double2 p = cmul2(fhat[(size_t)c + 3 * ((size_t)l + nm * ((size_t)m + (size_t)nm * n))], eyc[(size_t)m * g.n2m + j]);
+    acc.x += p.x; acc.y += p.y;
   }
-  H[(size_t)c * nm * plane + (size_t)l * plane + jk] = acc;
+  G[t] = acc;
 }
 
-// forc_c(i,j,k) = Re sum_l e_x(i,l) * H_c(l; j, k)
-__global__ void hit_force_kernel(Grid g, int nm, const double2* __restrict__ ex, const double2* __restrict__ H,
+// H_c(l; j, k) = sum_n G_c(l, n; j) e_z(k, n), folded over +-l:
+//   K_c(0) = H_c(l0),  K_c(p) = H_c(l0 + p) + conj(H_c(l0 - p)),  p = 1 .. nb-1,
+// l0 = nb - 1 the zero wavenumber (waveN runs -(nb-1) .. nb-1).  One thread
+// per (c, p, j, k); K stored [c][p][k][j], with an FP32 copy when wanted.
+__global__ void hit_k_kernel(Grid g, int nm, const double2* __restrict__ G, const double2* __restrict__ ez,
+                             double2* __restrict__ K, float2* __restrict__ K32) {
+  const int nb = (nm + 1) / 2, l0 = nb - 1;
+  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t plane = (size_t)g.n2m * g.n3m;
+  if (t >= 3 * (size_t)nb * plane) return;
+  const size_t jk = t % plane;
+  const int j = (int)(jk % g.n2m), k = (int)(jk / g.n2m);
+  const size_t r = t / plane;
+  const int p = (int)(r % nb), c = (int)(r / nb);
+  // forcx, forcy use zm; forcz uses zc
+  const double2* ezc = ez + (c == 2 ? (size_t)nm * g.n3m : 0);
+  auto H = [&](int l) {
+    double2 acc = make_double2(0.0, 0.0);
+    const double2* Gl = G + (((size_t)c * nm + l) * nm) * g.n2m + j;
+    for (int n = 0; n < nm; ++n) {
+      double2 q = cmul2(Gl[(size_t)n * g.n2m], ezc[(size_t)n * g.n3m + k]);
+      acc.x += q.x; acc.y += q.y;
+    }
+    return acc;
+  };
+  double2 v = H(l0 + p);
+  if (p > 0) {
+    double2 w = H(l0 - p);
+    v.x += w.x;
+    v.y -= w.y;
+  }
+  K[t] = v;
+  if (K32) K32[t] = make_float2((float)v.x, (float)v.y);
+}
+
+// forc_c(i,j,k) = Re K_c(0) + sum_{p>=1} Re(e_x(i, l0+p) K_c(p))
+template <typename R, typename R2>
+__global__ void hit_force_kernel(Grid g, int nm, const R2* __restrict__ ex, const R2* __restrict__ K,
                                  double* __restrict__ fx, double* __restrict__ fy, double* __restrict__ fz) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   int j = blockIdx.y, k = blockIdx.z;
   if (i >= g.n1m) return;
+  const int nb = (nm + 1) / 2, l0 = nb - 1;
   size_t plane = (size_t)g.n2m * g.n3m, jk = (size_t)j + (size_t)g.n2m * k;
   double out[3];
   for (int c = 0; c < 3; ++c) {
-    const double2* exc = ex + (c == 0 ? 0 : (size_t)nm * g.n1m);   // forcx at xc, forcy/forcz at xm
-    double s = 0.0;
-    for (int l = 0; l < nm; ++l) {
-      double2 e = exc[(size_t)l * g.n1m + i];
-      double2 hh = H[(size_t)c * nm * plane + (size_t)l * plane + jk];
-      s += e.x * hh.x - e.y * hh.y;
+    const R2* exc = ex + (c == 0 ? 0 : (size_t)nm * g.n1m);   // forcx at xc, forcy/forcz at xm
+    const R2* Kc = K + (size_t)c * nb * plane + jk;
+    R s = Kc[0].x;
+    for (int p = 1; p < nb; ++p) {
+      R2 e = exc[(size_t)(l0 + p) * g.n1m + i];
+      R2 kk = Kc[(size_t)p * plane];
+      s += e.x * kk.x - e.y * kk.y;
     }
-    out[c] = s;
+    out[c] = (double)s;
   }
   size_t c0 = cidx(g, i, j, k);
   fx[c0] = out[0]; fy[c0] = out[1]; fz[c0] = out[2];
@@ -256,17 +315,27 @@ void k_hit_random_force(Ctx* c) {
   std::vector<double2> fhat;
   hit_update_modes(c, h, fhat);
   const Grid& g = c->g;
-  const int nm = h->nmodes;
-  cudaMemcpyAsync(h->d_fhat, fhat.data(), sizeof(double2) * fhat.size(), cudaMemcpyHostToDevice, c->stream);
-  size_t nh = 3 * (size_t)nm * g.n2m * g.n3m;
+  const int nm = h->nmodes, nb = (nm + 1) / 2;
+  // the pinned staging buffer is reused: its previous copy must have run
+  if (!cuda_ok(c, cudaEventSynchronize(h->fhat_copied), "hit")) return;
+  memcpy(h->h_fhat, fhat.data(), sizeof(double2) * fhat.size());
+  cudaMemcpyAsync(h->d_fhat, h->h_fhat, sizeof(double2) * fhat.size(), cudaMemcpyHostToDevice, c->stream);
+  cudaEventRecord(h->fhat_copied, c->stream);
+  const bool f32 = c->precision == 1;
+  size_t ng = 3 * (size_t)nm * nm * g.n2m, nk = 3 * (size_t)nb * g.n2m * g.n3m;
   { MIBM_PROF(c, "hit_modes");
-    hit_h_kernel<<<div_up(nh, 256), 256, 0, c->stream>>>(g, nm, h->d_fhat, h->d_ey, h->d_ez, h->d_h); }
+    hit_g_kernel<<<div_up(ng, 256), 256, 0, c->stream>>>(g, nm, h->d_fhat, h->d_ey, h->d_g);
+    hit_k_kernel<<<div_up(nk, 256), 256, 0, c->stream>>>(g, nm, h->d_g, h->d_ez, h->d_h, f32 ? h->d_h32 : nullptr); }
   { MIBM_PROF(c, "hit_force");
-    hit_force_kernel<<<dim3(div_up(g.n1m, 128), g.n2m, g.n3m), 128, 0, c->stream>>>(
-        g, nm, h->d_ex, h->d_h, c->df[MIBM_F_FORCX], c->df[MIBM_F_FORCY], c->df[MIBM_F_FORCZ]); }
-  c->launches += 2;
-  // the host vector is read by the copy: wait before it goes out of scope
-  cuda_ok(c, cudaStreamSynchronize(c->stream), "hit");
+    dim3 grid(div_up(g.n1m, 128), g.n2m, g.n3m);
+    if (f32)
+      hit_force_kernel<float, float2><<<grid, 128, 0, c->stream>>>(
+          g, nm, h->d_ex32, h->d_h32, c->df[MIBM_F_FORCX], c->df[MIBM_F_FORCY], c->df[MIBM_F_FORCZ]);
+    else
+      hit_force_kernel<double, double2><<<grid, 128, 0, c->stream>>>(
+          g, nm, h->d_ex, h->d_h, c->df[MIBM_F_FORCX], c->df[MIBM_F_FORCY], c->df[MIBM_F_FORCZ]); }
+  c->launches += 3;
+  cuda_ok(c, cudaGetLastError(), "hit");
 }
 
 void k_hit_abc_force(Ctx* c) {

@@ -29,6 +29,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "mls_exp.h"
 
 namespace mibm {
 
@@ -66,9 +67,12 @@ __device__ __forceinline__ double coord(const LagArgs& A, int dir, int sel, int 
   return sel == 0 ? A.zc[t] : A.zm[t];
 }
 
-__device__ __forceinline__ double mls_gaussian(double r, double rcoef) { return (r > 1.0) ? 0.0 : exp(-sqd(r / rcoef)); }
+// Gaussian weight and its radial derivative (geom.f90:24-53).  exp is the
+// written-out mls_exp (mls_exp.h), shared with the oracle, so that the
+// plain form's MLS construction gives the oracle's bits.
+__device__ __forceinline__ double mls_gaussian(double r, double rcoef) { return (r > 1.0) ? 0.0 : mls_exp(-sqd(r / rcoef)); }
 __device__ __forceinline__ double mls_gauss_deriv(double r, double rcoef) {
-  return (r > 1.0) ? 0.0 : -2.0 * r / sqd(rcoef) * exp(-sqd(r / rcoef));
+  return (r > 1.0) ? 0.0 : -2.0 * r / sqd(rcoef) * mls_exp(-sqd(r / rcoef));
 }
 
 // In-place inverse of a 4x4 column-major matrix: LU with partial pivoting
@@ -176,6 +180,62 @@ __device__ __forceinline__ CageSpec cage_spec(int comp) {
   return CageSpec{0, 1, 1, 1, 1, false};             // xm, ym, zm ; pind(1), pind(2)
 }
 
+// The reference's MLS shape functions at pos for the 27-point cage centred on
+// (i0, j0, k0) with per-axis staggering sx, sy, sz (mls_shape of wght1/2/3/
+// temp, mlsWeight.f90:48-412, and of wght_press, mls_structLoads.f90:271-
+// 404): basis [1, x, y, z] in absolute coordinates, A = sum W p p^T by
+// rank-one updates in cage order, A^-1 by LU with partial pivoting, then
+// phi = (p(x)^T A^-1) B.  IEEE operations in the oracle's order (this file is
+// compiled without FMA contraction): the same bits.  Returns false on a
+// singular A.
+__device__ bool shape_lit(const LagArgs& A, const double pos[3], int i0, int j0, int k0, int sx, int sy, int sz,
+                          double out[27]) {
+  const Grid& g = A.g;
+  const double ptx[4] = {1.0, pos[0], pos[1], pos[2]};
+  // separable Gaussian weights (the reference evaluates the same 9 values)
+  double wz[3], wy[3], wx[3], cz[3], cy[3], cx[3];
+  for (int q = 0; q < 3; ++q) {
+    cz[q] = coord(A, 2, sz, k0 - 1 + q);
+    cy[q] = coord(A, 1, sy, j0 - 1 + q);
+    cx[q] = coord(A, 0, sx, i0 - 1 + q);
+    wz[q] = mls_gaussian(fabs(cz[q] - pos[2]) / (A.wscl / g.dx3), A.wcon);
+    wy[q] = mls_gaussian(fabs(cy[q] - pos[1]) / (A.wscl / g.dx2), A.wcon);
+    wx[q] = mls_gaussian(fabs(cx[q] - pos[0]) / (A.wscl / g.dx1), A.wcon);
+  }
+  double Am[16];
+  for (int q = 0; q < 16; ++q) Am[q] = 0.0;
+  for (int kk = 0; kk < 3; ++kk)
+    for (int jj = 0; jj < 3; ++jj) {
+      double w23 = wy[jj] * wz[kk];
+      for (int ii = 0; ii < 3; ++ii) {
+        double wtx = wx[ii] * w23;
+        double pk[4] = {1.0, cx[ii], cy[jj], cz[kk]};
+        for (int cc = 0; cc < 4; ++cc) {
+          double tt = wtx * pk[cc];
+          for (int r = 0; r < 4; ++r) Am[r + 4 * cc] = Am[r + 4 * cc] + tt * pk[r];
+        }
+      }
+    }
+  if (!inv4(Am)) return false;
+  double ptxA[4];
+  for (int cc = 0; cc < 4; ++cc) {
+    double s = 0;
+    for (int r = 0; r < 4; ++r) s += ptx[r] * Am[r + 4 * cc];
+    ptxA[cc] = s;
+  }
+  for (int kk = 0; kk < 3; ++kk)
+    for (int jj = 0; jj < 3; ++jj) {
+      double w23 = wy[jj] * wz[kk];
+      for (int ii = 0; ii < 3; ++ii) {
+        double wtx = wx[ii] * w23;
+        // B(:,n) = wtx * [1, x, y, z]
+        out[ii + 3 * jj + 9 * kk] =
+            ptxA[0] * (wtx * 1.0) + ptxA[1] * (wtx * cx[ii]) + ptxA[2] * (wtx * cy[jj]) + ptxA[3] * (wtx * cz[kk]);
+      }
+    }
+  return true;
+}
+
 // One thread per (triangle, component): the serial order of the reference,
 // and the fewest FP64 operations (the part's scarce resource).
 __global__ void mls_weight_kernel(LagArgs A, const double* __restrict__ tri_bar, const int* __restrict__ ghost,
@@ -186,54 +246,167 @@ __global__ void mls_weight_kernel(LagArgs A, const double* __restrict__ tri_bar,
   if (t >= A.nf || ghost[t]) return;
   const Grid& g = A.g;
   double pos[3] = {tri_bar[3 * t], tri_bar[3 * t + 1], tri_bar[3 * t + 2]};
-  double ptx[4] = {1.0, pos[0], pos[1], pos[2]};
   CageSpec cs = cage_spec(comp);
   int i0 = pind[6 * t + cs.ix], j0 = pind[6 * t + cs.iy];
   int k0 = cs.znint ? fnint(pos[2] * g.dx3) + 1 : ffloor(pos[2] * g.dx3) + 1;
-  // separable Gaussian weights (the reference evaluates the same 9 values)
-  double wz[3], wy[3], wx[3], cz[3], cy[3], cx[3];
-  for (int q = 0; q < 3; ++q) {
-    cz[q] = coord(A, 2, cs.sz, k0 - 1 + q);
-    cy[q] = coord(A, 1, cs.sy, j0 - 1 + q);
-    cx[q] = coord(A, 0, cs.sx, i0 - 1 + q);
-    wz[q] = mls_gaussian(fabs(cz[q] - pos[2]) / (A.wscl / g.dx3), A.wcon);
-    wy[q] = mls_gaussian(fabs(cy[q] - pos[1]) / (A.wscl / g.dx2), A.wcon);
-    wx[q] = mls_gaussian(fabs(cx[q] - pos[0]) / (A.wscl / g.dx1), A.wcon);
+  double* out = (comp == 0) ? p1 : (comp == 1) ? p2 : (comp == 2) ? p3 : pt;
+  double phi[27];
+  if (!shape_lit(A, pos, i0, j0, k0, cs.sx, cs.sy, cs.sz, phi)) { atomicOr(flag, 1); return; }
+  out += 27 * (size_t)t;
+  for (int n = 0; n < 27; ++n) out[n] = phi[n];
+}
+
+// Weight and weight derivative of one cage coordinate for the literal
+// gradient, as wght_grad_field evaluates them (mls_heatFlux.f90:166-185):
+// norp = |pos - pc| / (wscl/dx); W = gaussian(norp); dW = 0 at norp < eps,
+// else gauss_deriv(norp) * ((pos - pc) / |pos - pc| / (wscl/dx)).  The
+// Gaussian's exp is evaluated once for both (the same value either way).
+__device__ __forceinline__ void lit_axis_weight(const LagArgs& A, double pos, double pc, double dx, double eps,
+                                                double& W, double& dW) {
+  const double diff = pos - pc;
+  const double norp = fabs(diff) / (A.wscl / dx);
+  if (norp > 1.0) {
+    W = 0.0;
+    dW = 0.0;
+    return;
   }
+  const double e = mls_exp(-sqd(norp / A.wcon));
+  W = e;
+  dW = (norp < eps) ? 0.0 : (-2.0 * norp / sqd(A.wcon) * e) * (diff / fabs(diff) / (A.wscl / dx));
+}
+
+// The reference's MLS gradient at a probe, literally (wght_gradT,
+// mls_heatFlux.f90:161-376; wght_gradP/U/V/W, mls_structLoads.f90:406-1298):
+// basis [1, x, y, z] in absolute coordinates; A, dA/dx_d, B, dB/dx_d
+// accumulated point by point in cage order (z layer, y, x) as the reference's
+// rank-one DGEMM updates; A^-1 by LU with partial pivoting; gamma = A^-1 p(x);
+//   d phi / dx_d = (A^-1 (e_d - dA_d gamma))^T B + gamma^T dB_d,
+// contracted with the field over the cage.  Cage i, j around (pi1, pi2);
+// z layers [k1-1, k1, k1] (the repeated layer of mls_heatFlux.f90:213) with
+// k1 = floor(z*dx3)+1, or nint for the w-velocity; coordinates per axis from
+// the field's staggering (sel 0 = face, 1 = centre); field values at the
+// wrapped cage, z from [k1w-1, k1w, k1w+1].  Every operation is the oracle's
+// (wght_grad_field) in its order, so the two agree bit for bit.  B and dB are
+// not stored: each entry is a product of per-axis weight factors and a basis
+// entry, recomputed where it is used from the same factors in the same order
+// (the same bits); dA_d is accumulated in its own pass per direction.
+// Returns false on a singular A.
+__device__ bool probe_grad_lit(const LagArgs& A, const double pos[3], int pi1, int pi2, int sx, int sy, int sz,
+                               bool knint, const double* __restrict__ q, double grad[3]) {
+  const Grid& g = A.g;
+  const double eps = 2.220446049250313e-16;       // EPSILON(1.0d0)
+  const double ptx[4] = {1.0, pos[0], pos[1], pos[2]};
+  const int k1 = knint ? fnint(pos[2] * g.dx3) + 1 : ffloor(pos[2] * g.dx3) + 1;
+  const int kin[3] = {k1 - 1, k1, k1};
+  const int k1w = fmod_pos(k1 - 1, g.n3m) + 1;
+  const int keul[3] = {k1w - 1, k1w, k1w + 1};
+  double pc[3][3], W[3][3], dW[3][3];             // [axis][point]
+  for (int r = 0; r < 3; ++r) {
+    pc[0][r] = coord(A, 0, sx, pi1 - 1 + r);
+    pc[1][r] = coord(A, 1, sy, pi2 - 1 + r);
+    pc[2][r] = coord(A, 2, sz, kin[r]);
+  }
+  const double dxa[3] = {g.dx1, g.dx2, g.dx3};
+  for (int a = 0; a < 3; ++a)
+    for (int r = 0; r < 3; ++r) lit_axis_weight(A, pos[a], pc[a][r], dxa[a], eps, W[a][r], dW[a][r]);
   double Am[16];
-  for (int q = 0; q < 16; ++q) Am[q] = 0.0;
-  double W[27];
-  for (int kk = 0; kk < 3; ++kk)
-    for (int jj = 0; jj < 3; ++jj) {
-      double w23 = wy[jj] * wz[kk];
-      for (int ii = 0; ii < 3; ++ii) {
-        double wtx = wx[ii] * w23;
-        W[ii + 3 * jj + 9 * kk] = wtx;
-        double pk[4] = {1.0, cx[ii], cy[jj], cz[kk]};
+  for (int e = 0; e < 16; ++e) Am[e] = 0.0;
+  for (int nk = 0; nk < 3; ++nk)
+    for (int j = 0; j < 3; ++j) {
+      const double w23 = W[1][j] * W[2][nk];
+      for (int i = 0; i < 3; ++i) {
+        const double wtx = W[0][i] * w23;
+        const double pk[4] = {1.0, pc[0][i], pc[1][j], pc[2][nk]};
         for (int cc = 0; cc < 4; ++cc) {
-          double tt = wtx * pk[cc];
-          for (int r = 0; r < 4; ++r) Am[r + 4 * cc] = Am[r + 4 * cc] + tt * pk[r];
+          const double t = wtx * pk[cc];
+          for (int r = 0; r < 4; ++r) Am[r + 4 * cc] = Am[r + 4 * cc] + t * pk[r];
         }
       }
     }
-  if (!inv4(Am)) { atomicOr(flag, 1); return; }
-  double ptxA[4];
-  for (int cc = 0; cc < 4; ++cc) {
-    double s = 0;
-    for (int r = 0; r < 4; ++r) s += ptx[r] * Am[r + 4 * cc];
-    ptxA[cc] = s;
+  if (!inv4(Am)) return false;
+  double gam[4];
+  for (int r = 0; r < 4; ++r) {                   // DGEMV('N', invA, ptx)
+    double t = 0;
+    for (int cc = 0; cc < 4; ++cc) t += Am[r + 4 * cc] * ptx[cc];
+    gam[r] = t;
   }
-  double* out = (comp == 0) ? p1 : (comp == 1) ? p2 : (comp == 2) ? p3 : pt;
-  out += 27 * (size_t)t;
-  for (int kk = 0; kk < 3; ++kk)
-    for (int jj = 0; jj < 3; ++jj)
-      for (int ii = 0; ii < 3; ++ii) {
-        int n = ii + 3 * jj + 9 * kk;
-        double wtx = W[n];
-        // B(:,n) = wtx * [1, x, y, z]
-        double s = ptxA[0] * (wtx * 1.0) + ptxA[1] * (wtx * cx[ii]) + ptxA[2] * (wtx * cy[jj]) + ptxA[3] * (wtx * cz[kk]);
-        out[n] = s;
+  const int kk_[3] = {wrap(keul[0] - 1, g.n3m), wrap(keul[1] - 1, g.n3m), wrap(keul[2] - 1, g.n3m)};
+  for (int d = 0; d < 3; ++d) {
+    double dA[16];
+    for (int e = 0; e < 16; ++e) dA[e] = 0.0;
+    for (int nk = 0; nk < 3; ++nk)
+      for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i) {
+          const double dwd = d == 0 ? (dW[0][i] * W[1][j]) * W[2][nk]
+                           : d == 1 ? (W[0][i] * dW[1][j]) * W[2][nk]
+                                    : (W[0][i] * W[1][j]) * dW[2][nk];
+          const double pk[4] = {1.0, pc[0][i], pc[1][j], pc[2][nk]};
+          for (int cc = 0; cc < 4; ++cc) {
+            const double t = dwd * pk[cc];
+            for (int r = 0; r < 4; ++r) dA[r + 4 * cc] = dA[r + 4 * cc] + t * pk[r];
+          }
+        }
+    double pk_d[4] = {0.0, 0.0, 0.0, 0.0};
+    pk_d[d + 1] = 1.0;
+    for (int r = 0; r < 4; ++r) {                 // pk = -dA gamma + pk
+      double t = 0;
+      for (int cc = 0; cc < 4; ++cc) t += dA[r + 4 * cc] * gam[cc];
+      pk_d[r] = pk_d[r] - t;
+    }
+    double dgam[4];
+    for (int r = 0; r < 4; ++r) {
+      double t = 0;
+      for (int cc = 0; cc < 4; ++cc) t += Am[r + 4 * cc] * pk_d[cc];
+      dgam[r] = t;
+    }
+    double gsum = 0;
+    for (int nk = 0; nk < 3; ++nk)
+      for (int j = 0; j < 3; ++j) {
+        const int jj = fmod_pos(pi2 - 1 + j - 1, g.n2m);
+        const double w23 = W[1][j] * W[2][nk];
+        for (int i = 0; i < 3; ++i) {
+          const double wtx = W[0][i] * w23;
+          const double dwd = d == 0 ? (dW[0][i] * W[1][j]) * W[2][nk]
+                           : d == 1 ? (W[0][i] * dW[1][j]) * W[2][nk]
+                                    : (W[0][i] * W[1][j]) * dW[2][nk];
+          const double pk[4] = {1.0, pc[0][i], pc[1][j], pc[2][nk]};
+          double t1 = 0, t2 = 0;
+          for (int r = 0; r < 4; ++r) t1 += dgam[r] * (wtx * pk[r]);
+          for (int r = 0; r < 4; ++r) t2 += gam[r] * (dwd * pk[r]);
+          const double T = q[cidx(g, fmod_pos(pi1 - 1 + i - 1, g.n1m), jj, kk_[nk])];
+          gsum += (t1 + t2) * T;
+        }
       }
+    grad[d] = gsum;
+  }
+  return true;
+}
+
+// The reference's MLS value at a probe, literally (wght_press,
+// mls_structLoads.f90:271-404): shape functions of the cell-centred cage
+// around (i0, j0), z layers k1-1, k1, k1+1 with k1 = floor(z*dx3)+1, summed
+// against the field in cage order as the oracle does.
+__device__ bool probe_value_lit(const LagArgs& A, const double pos[3], int i0, int j0, const double* __restrict__ q,
+                                double& val) {
+  const Grid& g = A.g;
+  const int k1 = ffloor(pos[2] * g.dx3) + 1;
+  double phi[27];
+  if (!shape_lit(A, pos, i0, j0, k1, 1, 1, 1, phi)) return false;
+  const int k1w = fmod_pos(k1 - 1, g.n3m) + 1;
+  double v = 0.0;
+  int inw = 0;
+  for (int kk = 0; kk < 3; ++kk) {
+    const int kc = wrap(k1w - 1 + kk - 1, g.n3m);
+    for (int j = 0; j < 3; ++j) {
+      const int jj = fmod_pos(j0 - 1 + j - 1, g.n2m);
+      for (int i = 0; i < 3; ++i) {
+        v = v + q[cidx(g, fmod_pos(i0 - 1 + i - 1, g.n1m), jj, kc)] * phi[inw];
+        ++inw;
+      }
+    }
+  }
+  val = v;
+  return true;
 }
 
 // ---------------------------------------------------------------------
@@ -913,10 +1086,12 @@ __device__ bool probe_value_sep(const LagArgs& A, const double pos[3], int i0, i
   return true;
 }
 
+// mls_heatFlux.f90:77-158 at both probes of every face with the separable
+// construction (precision form, moving body): one thread per (face, side).
 __global__ void heat_flux_sep_kernel(LagArgs A, const double* __restrict__ temp, const double* __restrict__ tri_bar,
-                                     const double* __restrict__ tri_nor, const int* __restrict__ ghost,
-                                     const int* __restrict__ pind, double h, double pec, double* __restrict__ qw_o,
-                                     double* __restrict__ qw_i, int* __restrict__ flag) {
+                                 const double* __restrict__ tri_nor, const int* __restrict__ ghost,
+                                 const int* __restrict__ pind, double h, double pec, double* __restrict__ qw_o,
+                                 double* __restrict__ qw_i, int* __restrict__ flag) {
   int gid = blockIdx.x * blockDim.x + threadIdx.x;
   int t = gid >> 1, side = gid & 1;
   if (t >= A.nf) return;
@@ -936,6 +1111,160 @@ __global__ void heat_flux_sep_kernel(LagArgs A, const double* __restrict__ temp,
   qout[t] = qv / pec;
 }
 
+// The literal heat flux of the plain form (mls_heatFlux.f90:77-158 with
+// wght_gradT), spread over a block of 4 warps for 32 probes (lane = probe,
+// probe q = face q/2, side q%2): warp 0 forms the probe's per-axis weights
+// (shared), then the moment matrix A by the reference's rank-one updates, its
+// inverse and gamma; warp w = 1..3 forms dA_d (d = w - 1) meanwhile and, once
+// A^-1 and gamma are published, the direction-d gradient.  Every value comes
+// from exactly the operations of probe_grad_lit in its order (the oracle's
+// bits); the split only gives the device four times the independent work per
+// probe that one thread would have.
+constexpr int kHfProbes = 32;
+__global__ void __launch_bounds__(4 * kHfProbes)
+heat_flux_lit_kernel(LagArgs A, const double* __restrict__ temp, const double* __restrict__ tri_bar,
+                     const double* __restrict__ tri_nor, const int* __restrict__ ghost,
+                     const int* __restrict__ pind, double h, double pec, double* __restrict__ qw_o,
+                     double* __restrict__ qw_i, int* __restrict__ flag) {
+  __shared__ double sW[3][3][kHfProbes], sdW[3][3][kHfProbes], spc[3][3][kHfProbes];
+  __shared__ double sAi[16][kHfProbes], sgam[4][kHfProbes], sgrad[3][kHfProbes];
+  __shared__ int sok[kHfProbes];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int gid = blockIdx.x * kHfProbes + lane;
+  const int t = gid >> 1, side = gid & 1;
+  const bool valid = t < A.nf;
+  const bool live = valid && !ghost[t];
+  const Grid& g = A.g;
+  const double eps = 2.220446049250313e-16;       // EPSILON(1.0d0)
+  double pos[3] = {0.0, 0.0, 0.0};
+  int pi1 = 0, pi2 = 0, k1 = 0;
+  if (live) {
+    const double n0 = tri_nor[3 * t], n1 = tri_nor[3 * t + 1], n2 = tri_nor[3 * t + 2];
+    const double s = sqrt(n0 * n0 + n1 * n1 + n2 * n2);
+    for (int d = 0; d < 3; ++d) {
+      const double nd = tri_nor[3 * t + d];
+      pos[d] = side == 0 ? tri_bar[3 * t + d] + h * nd / s : tri_bar[3 * t + d] - h * nd / s;
+    }
+    pi1 = pind[6 * t + 3 * side + 0];
+    pi2 = pind[6 * t + 3 * side + 1];
+    k1 = ffloor(pos[2] * g.dx3) + 1;
+  }
+  if (w == 0 && live) {
+    const int kin[3] = {k1 - 1, k1, k1};          // the repeated layer of mls_heatFlux.f90:213
+    const double dxa[3] = {g.dx1, g.dx2, g.dx3};
+    for (int r = 0; r < 3; ++r) {
+      const double pc[3] = {coord(A, 0, 1, pi1 - 1 + r), coord(A, 1, 1, pi2 - 1 + r), coord(A, 2, 1, kin[r])};
+      for (int a = 0; a < 3; ++a) {
+        double W, dW;
+        lit_axis_weight(A, pos[a], pc[a], dxa[a], eps, W, dW);
+        spc[a][r][lane] = pc[a];
+        sW[a][r][lane] = W;
+        sdW[a][r][lane] = dW;
+      }
+    }
+  }
+  __syncthreads();
+  double dA[16];
+  const int d = w - 1;
+  if (w == 0) {
+    int ok = 0;
+    if (live) {
+      double Am[16];
+      for (int e = 0; e < 16; ++e) Am[e] = 0.0;
+      for (int nk = 0; nk < 3; ++nk)
+        for (int j = 0; j < 3; ++j) {
+          const double w23 = sW[1][j][lane] * sW[2][nk][lane];
+          for (int i = 0; i < 3; ++i) {
+            const double wtx = sW[0][i][lane] * w23;
+            const double pk[4] = {1.0, spc[0][i][lane], spc[1][j][lane], spc[2][nk][lane]};
+            for (int cc = 0; cc < 4; ++cc) {
+              const double tt = wtx * pk[cc];
+              for (int r = 0; r < 4; ++r) Am[r + 4 * cc] = Am[r + 4 * cc] + tt * pk[r];
+            }
+          }
+        }
+      if (inv4(Am)) {
+        ok = 1;
+        const double ptx[4] = {1.0, pos[0], pos[1], pos[2]};
+        for (int r = 0; r < 4; ++r) {               // DGEMV('N', invA, ptx)
+          double tt = 0;
+          for (int cc = 0; cc < 4; ++cc) tt += Am[r + 4 * cc] * ptx[cc];
+          sgam[r][lane] = tt;
+        }
+        for (int e = 0; e < 16; ++e) sAi[e][lane] = Am[e];
+      }
+    }
+    sok[lane] = ok;
+  } else if (live) {
+    for (int e = 0; e < 16; ++e) dA[e] = 0.0;
+    for (int nk = 0; nk < 3; ++nk)
+      for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i) {
+          const double dwd = d == 0 ? (sdW[0][i][lane] * sW[1][j][lane]) * sW[2][nk][lane]
+                           : d == 1 ? (sW[0][i][lane] * sdW[1][j][lane]) * sW[2][nk][lane]
+                                    : (sW[0][i][lane] * sW[1][j][lane]) * sdW[2][nk][lane];
+          const double pk[4] = {1.0, spc[0][i][lane], spc[1][j][lane], spc[2][nk][lane]};
+          for (int cc = 0; cc < 4; ++cc) {
+            const double tt = dwd * pk[cc];
+            for (int r = 0; r < 4; ++r) dA[r + 4 * cc] = dA[r + 4 * cc] + tt * pk[r];
+          }
+        }
+  }
+  __syncthreads();
+  if (w > 0 && live && sok[lane]) {
+    double gam[4];
+    for (int r = 0; r < 4; ++r) gam[r] = sgam[r][lane];
+    double pk_d[4] = {0.0, 0.0, 0.0, 0.0};
+    pk_d[d + 1] = 1.0;
+    for (int r = 0; r < 4; ++r) {                   // pk = -dA gamma + pk
+      double tt = 0;
+      for (int cc = 0; cc < 4; ++cc) tt += dA[r + 4 * cc] * gam[cc];
+      pk_d[r] = pk_d[r] - tt;
+    }
+    double dgam[4];
+    for (int r = 0; r < 4; ++r) {
+      double tt = 0;
+      for (int cc = 0; cc < 4; ++cc) tt += sAi[r + 4 * cc][lane] * pk_d[cc];
+      dgam[r] = tt;
+    }
+    const int k1w = fmod_pos(k1 - 1, g.n3m) + 1;
+    const int kk_[3] = {wrap(k1w - 2, g.n3m), wrap(k1w - 1, g.n3m), wrap(k1w, g.n3m)};
+    double gsum = 0;
+    for (int nk = 0; nk < 3; ++nk)
+      for (int j = 0; j < 3; ++j) {
+        const int jj = fmod_pos(pi2 - 1 + j - 1, g.n2m);
+        const double w23 = sW[1][j][lane] * sW[2][nk][lane];
+        for (int i = 0; i < 3; ++i) {
+          const double wtx = sW[0][i][lane] * w23;
+          const double dwd = d == 0 ? (sdW[0][i][lane] * sW[1][j][lane]) * sW[2][nk][lane]
+                           : d == 1 ? (sW[0][i][lane] * sdW[1][j][lane]) * sW[2][nk][lane]
+                                    : (sW[0][i][lane] * sW[1][j][lane]) * sdW[2][nk][lane];
+          const double pk[4] = {1.0, spc[0][i][lane], spc[1][j][lane], spc[2][nk][lane]};
+          double t1 = 0, t2 = 0;
+          for (int r = 0; r < 4; ++r) t1 += dgam[r] * (wtx * pk[r]);
+          for (int r = 0; r < 4; ++r) t2 += gam[r] * (dwd * pk[r]);
+          const double T = temp[cidx(g, fmod_pos(pi1 - 1 + i - 1, g.n1m), jj, kk_[nk])];
+          gsum += (t1 + t2) * T;
+        }
+      }
+    sgrad[d][lane] = gsum;
+  }
+  __syncthreads();
+  if (w == 0 && valid) {
+    double* qout = side == 0 ? qw_o : qw_i;
+    if (!live) {
+      qout[t] = 0.0;
+    } else if (!sok[lane]) {
+      atomicOr(flag, 1);
+      qout[t] = 0.0;
+    } else {
+      const double qv = tri_nor[3 * t] * sgrad[0][lane] + tri_nor[3 * t + 1] * sgrad[1][lane] +
+                        tri_nor[3 * t + 2] * sgrad[2][lane];
+      qout[t] = qv / pec;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------
 // Structural loads (mls_structLoads.f90:1-269).  A block takes 32 faces;
 // warp e of the block evaluates, at each face's positive probe
@@ -952,10 +1281,11 @@ __global__ void heat_flux_sep_kernel(LagArgs A, const double* __restrict__ temp,
 // faces' 12 values with fixed shuffle trees, and the last block to finish
 // adds the block sums (lane l takes blocks l, l+32, ... in order, then a
 // fixed shuffle tree) and updates the loads.
-// The MLS uses the separable construction of the precision form: it agrees
-// with the reference's rank-one accumulation in absolute coordinates to
-// that construction's round-off (amplified by its ~1e8 conditioning), and
-// keeps the 5 evaluations in registers.
+// Lit (the plain form): the reference's MLS construction (probe_value_lit,
+// probe_grad_lit), the oracle's bits per face.  Otherwise (the precision
+// form) the separable construction, which agrees with the reference's
+// rank-one accumulation in absolute coordinates to that construction's
+// round-off (amplified by its ~1e8 conditioning) at a fifth of the cost.
 // ---------------------------------------------------------------------
 constexpr int kLoadFaces = 32;
 
@@ -966,6 +1296,7 @@ __device__ __forceinline__ void struct_probe(const double* __restrict__ tri_bar,
   for (int d = 0; d < 3; ++d) pos[d] = tri_bar[3 * t + d] + h * nrm[d] / s;
 }
 
+template <bool Lit>
 __global__ void __launch_bounds__(kLoadFaces * 5)
 loads_face_kernel(LagArgs A, const double* __restrict__ pr, const double* __restrict__ vx,
                   const double* __restrict__ vy, const double* __restrict__ vz, const double* __restrict__ tri_bar,
@@ -989,14 +1320,15 @@ loads_face_kernel(LagArgs A, const double* __restrict__ pr, const double* __rest
     bool ok;
     if (e == 0) {
       double v = 0.0;
-      ok = probe_value_sep(A, pos, icent, jcent, pr, v);
+      ok = Lit ? probe_value_lit(A, pos, icent, jcent, pr, v) : probe_value_sep(A, pos, icent, jcent, pr, v);
       ev[0][lf] = ok ? v : 0.0;
     } else {
       double gr[3] = {0, 0, 0};
-      if (e == 1) ok = probe_grad_sep(A, pos, icent, jcent, 1, 1, 1, false, pr, gr);
-      else if (e == 2) ok = probe_grad_sep(A, pos, istag, jcent, 0, 1, 1, false, vx, gr);
-      else if (e == 3) ok = probe_grad_sep(A, pos, icent, jstag, 1, 0, 1, false, vy, gr);
-      else ok = probe_grad_sep(A, pos, icent, jcent, 1, 1, 0, true, vz, gr);
+      const double* q = e == 1 ? pr : e == 2 ? vx : e == 3 ? vy : vz;
+      const int pi1 = e == 2 ? istag : icent, pi2 = e == 3 ? jstag : jcent;
+      const int sx = e == 2 ? 0 : 1, sy = e == 3 ? 0 : 1, sz = e == 4 ? 0 : 1;
+      ok = Lit ? probe_grad_lit(A, pos, pi1, pi2, sx, sy, sz, e == 4, q, gr)
+               : probe_grad_sep(A, pos, pi1, pi2, sx, sy, sz, e == 4, q, gr);
       for (int d = 0; d < 3; ++d) ev[1 + 3 * (e - 1) + d][lf] = ok ? gr[d] : 0.0;
     }
     if (!ok) atomicOr(flag, 1);
@@ -1899,17 +2231,32 @@ void lagr_find_probe_indices(Ctx* c) {
   MIBM_LAUNCH_CHECK(c, "findProbeIndices");
 }
 
-// Both forms use the separable construction (heat_flux_sep_kernel): it
-// agrees with the reference's rank-one accumulation in absolute coordinates
-// to that construction's conditioning error (1e-9 relative at 24^3) and
-// costs a quarter of its FP64 operations.
+// Which MLS construction evaluates gradients and values at the probes.  The
+// reference's (absolute coordinates, condition numbers 1e7-1e8) returns the
+// oracle's bits only when its inputs are the oracle's bits: the plain form
+// uses it for a body that does not move (fixed, melting or not: the
+// geometry follows the Stefan update, which is bit-exact) and for the
+// drop-in calls.  Once a body moves, its position carries the fluid solver's
+// round-off from the first step on, and the reference's construction turns
+// any last-bit difference of the geometry into ~1e-9 noise (its conditioning
+// times the rounding unit); there, and in the precision form, the separable
+// construction is used, which has none of that noise and agrees with the
+// reference's to it, at a quarter of its FP64 operations.
+static bool literal_mls(Ctx* c) { return c->precision == 0 && c->I(MIBM_I_IMLSSTR) != 1; }
+
 static void heat_flux_launch(Ctx* c) {
   LagState* s = lag_of(c);
   { MIBM_PROF(c, "heat_flux");
-    heat_flux_sep_kernel<<<div_up(2 * (size_t)c->maxnf, 128), 128, 0, c->stream>>>(
-        lag_args(c), c->df[MIBM_F_TEMP], M<double>(c, MIBM_M_TRI_BAR), M<double>(c, MIBM_M_TRI_NOR),
-        M<int>(c, MIBM_M_GHOST_FACE), M<int>(c, MIBM_M_PIND), c->S(MIBM_S_H_EULERIAN), c->S(MIBM_S_PEC),
-        M<double>(c, MIBM_M_QW_O), M<double>(c, MIBM_M_QW_I), c->dflag); }
+    if (literal_mls(c))
+      heat_flux_lit_kernel<<<div_up(2 * (size_t)c->maxnf, kHfProbes), 4 * kHfProbes, 0, c->stream>>>(
+          lag_args(c), c->df[MIBM_F_TEMP], M<double>(c, MIBM_M_TRI_BAR), M<double>(c, MIBM_M_TRI_NOR),
+          M<int>(c, MIBM_M_GHOST_FACE), M<int>(c, MIBM_M_PIND), c->S(MIBM_S_H_EULERIAN), c->S(MIBM_S_PEC),
+          M<double>(c, MIBM_M_QW_O), M<double>(c, MIBM_M_QW_I), c->dflag);
+    else
+      heat_flux_sep_kernel<<<div_up(2 * (size_t)c->maxnf, 128), 128, 0, c->stream>>>(
+          lag_args(c), c->df[MIBM_F_TEMP], M<double>(c, MIBM_M_TRI_BAR), M<double>(c, MIBM_M_TRI_NOR),
+          M<int>(c, MIBM_M_GHOST_FACE), M<int>(c, MIBM_M_PIND), c->S(MIBM_S_H_EULERIAN), c->S(MIBM_S_PEC),
+          M<double>(c, MIBM_M_QW_O), M<double>(c, MIBM_M_QW_I), c->dflag); }
   { MIBM_PROF(c, "face_to_vert");
     face_to_vert_kernel<<<div_up(c->maxnv, 128), 128, 0, c->stream>>>(
         c->maxnv, s->adj_off, s->adj_face, M<double>(c, MIBM_M_SUR), M<double>(c, MIBM_M_AVERT),
@@ -1996,7 +2343,10 @@ void lagr_geometry_to_host(Ctx* c) {
   for (int q = 0; q < 9; ++q) c->hs[MIBM_S_INERT_TENSOR][q] = c->red_host[6 + q];
 }
 
-static void struct_loads_launch(Ctx* c, const StepParams* dp) {
+// literal: the reference's MLS construction (the drop-in mls_structloads_
+// of the plain form); the fused step of a moving body uses the separable one
+// (see literal_mls).
+static void struct_loads_launch(Ctx* c, const StepParams* dp, bool literal) {
   LagState* s = lag_of(c);
   if (!s->loads_ev) {
     if (!cuda_ok(c, cudaMalloc(&s->loads_ev, sizeof(double) * 13 * std::max(1, c->maxnf)), "structLoads") ||
@@ -2007,7 +2357,8 @@ static void struct_loads_launch(Ctx* c, const StepParams* dp) {
   double h = c->S(MIBM_S_H_EULERIAN);
   int nb = (int)div_up(c->maxnf, kLoadFaces);
   { MIBM_PROF(c, "loads_face");
-    loads_face_kernel<<<nb, dim3(kLoadFaces, 5), 0, c->stream>>>(
+    auto kern = literal ? loads_face_kernel<true> : loads_face_kernel<false>;
+    kern<<<nb, dim3(kLoadFaces, 5), 0, c->stream>>>(
         lag_args(c), c->df[MIBM_F_PR], c->df[MIBM_F_VX], c->df[MIBM_F_VY], c->df[MIBM_F_VZ],
         M<double>(c, MIBM_M_TRI_BAR), M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_SUR),
         M<int>(c, MIBM_M_GHOST_FACE), dp, h, c->S(MIBM_S_REN), s->loads_ev, c->dflag, s->loads_ticket,
@@ -2019,7 +2370,7 @@ static void struct_loads_launch(Ctx* c, const StepParams* dp) {
 void lagr_struct_loads(Ctx* c, const StepParams* dp) {
   if (c->maxnf == 0) return;
   if (!ensure_lag_buffers(c) || !rigid_ensure(c)) return;
-  struct_loads_launch(c, dp);
+  struct_loads_launch(c, dp, c->precision == 0);
   if (MIBM_LAUNCH_CHECK(c, "mls_structLoads")) check_flag(c, "mls_structLoads");
 }
 
@@ -2323,7 +2674,7 @@ void lagr_loads_early(Ctx* c, const StepParams* dp) {
   cudaEventRecord(c->ev_lfork, c->stream);
   cudaStreamWaitEvent(c->side, c->ev_lfork, 0);
   std::swap(c->stream, c->side);
-  struct_loads_launch(c, dp);
+  struct_loads_launch(c, dp, false);
   cudaEventRecord(c->ev_ldone, c->stream);
   std::swap(c->stream, c->side);
   c->loads_pending = true;
@@ -2342,7 +2693,7 @@ const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror,
       cudaStreamWaitEvent(c->stream, c->ev_ldone, 0);
       c->loads_pending = false;
     } else {
-      struct_loads_launch(c, dp);
+      struct_loads_launch(c, dp, false);
     }
   }
   scatter(c, true, 0, 3, true);

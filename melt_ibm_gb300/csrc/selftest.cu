@@ -5,7 +5,8 @@
 // range limits, ties at every rounding boundary, infinities, NaNs) and on
 // random bit patterns.  The line-solve factor table evaluated on the device
 // (the allocation-free x-line solve builds it there) must equal the host's
-// evaluation bit for bit.
+// evaluation bit for bit.  The written-out exp of the MLS weights (mls_exp.h)
+// must give the host's bits on the device.
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
@@ -13,6 +14,7 @@
 
 #include "common.cuh"
 #include "fpconv.cuh"
+#include "mls_exp.h"
 
 namespace mibm {
 
@@ -86,6 +88,35 @@ static void edge_cases(std::vector<unsigned long long>& v) {
 
 long long tri_factors_selftest();   // tridiag.cu
 
+// mls_exp on the device over n arguments spread over [-750, 712] and the
+// weights' range [-11.2, 0]; out[t] = bits of the result
+__global__ void mls_exp_selftest_kernel(long long n, unsigned long long* __restrict__ out) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const double x = (t & 1) ? -11.2 * (double)(t >> 1) / (double)(n >> 1) : -750.0 + 1462.0 * (double)t / (double)n;
+    out[t] = (unsigned long long)__double_as_longlong(mls_exp(x));
+  }
+}
+
+static long long mls_exp_selftest() {
+  const long long n = 1 << 20;
+  unsigned long long* d = nullptr;
+  if (cudaMalloc(&d, n * 8) != cudaSuccess) { cudaGetLastError(); return -1; }
+  std::vector<unsigned long long> h(n);
+  mls_exp_selftest_kernel<<<608, 256>>>(n, d);
+  bool ok = cudaMemcpy(h.data(), d, n * 8, cudaMemcpyDeviceToHost) == cudaSuccess;
+  cudaFree(d);
+  if (!ok) { cudaGetLastError(); return -1; }
+  long long bad = 0;
+  for (long long t = 0; t < n; ++t) {
+    const double x = (t & 1) ? -11.2 * (double)(t >> 1) / (double)(n >> 1) : -750.0 + 1462.0 * (double)t / (double)n;
+    const double r = mls_exp(x);
+    unsigned long long b;
+    memcpy(&b, &r, 8);
+    if (b != h[t]) ++bad;
+  }
+  return bad;
+}
+
 }  // namespace mibm
 
 using namespace mibm;
@@ -114,5 +145,9 @@ extern "C" int mibm_selftest_(void) {
   const long long tbad = tri_factors_selftest();
   if (tbad < 0) return -1;
   if (tbad) fprintf(stderr, "mibm_selftest_: %lld line-solve factor entries differ between host and device\n", tbad);
-  return (int)std::min<unsigned long long>(hbad[0] + hbad[1] + (unsigned long long)tbad, 1000000);
+  const long long ebad = mls_exp_selftest();
+  if (ebad < 0) return -1;
+  if (ebad) fprintf(stderr, "mibm_selftest_: mls_exp differs between host and device at %lld arguments\n", ebad);
+  return (int)std::min<unsigned long long>(hbad[0] + hbad[1] + (unsigned long long)tbad + (unsigned long long)ebad,
+                                           1000000);
 }

@@ -20,8 +20,10 @@ LIB = os.path.join(OUT_DIR, "libmibm_oracle.so")
 def build(force: bool = False) -> str:
     os.makedirs(OUT_DIR, exist_ok=True)
     hdr = os.path.join(os.path.dirname(HERE), "include", "mibm.h")
+    # the written-out exp of the MLS weights, shared with the library
+    mexp = os.path.join(os.path.dirname(HERE), "melt_ibm_gb300", "csrc", "mls_exp.h")
     if (not force and os.path.exists(LIB)
-            and os.path.getmtime(LIB) >= max(os.path.getmtime(SRC), os.path.getmtime(hdr))):
+            and os.path.getmtime(LIB) >= max(os.path.getmtime(SRC), os.path.getmtime(hdr), os.path.getmtime(mexp))):
         return LIB
     cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
            "-o", LIB + ".tmp", SRC]

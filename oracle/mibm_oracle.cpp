@@ -40,6 +40,7 @@
 #include <vector>
 
 #include "../include/mibm.h"
+#include "../melt_ibm_gb300/csrc/mls_exp.h"
 
 #ifdef _OPENMP
 #include <omp.h>
@@ -765,9 +766,13 @@ int lu_inverse(double* a, int n) {
 // ------------------------------------------------------------------------
 // MLS shape functions: geom.f90:24-53, mlsWeight.f90:48-412
 // ------------------------------------------------------------------------
-inline double mls_gaussian(double r, double rcoef) { return (r > 1.0) ? 0.0 : std::exp(-sq(r / rcoef)); }
+// The reference's exp is the Fortran runtime's; the oracle and the library
+// share one written-out exp (mls_exp.h: Cody-Waite reduction, degree-13
+// Taylor polynomial, within 1 ulp of libm) so that the ill-conditioned MLS
+// construction gives the same bits on both sides.
+inline double mls_gaussian(double r, double rcoef) { return (r > 1.0) ? 0.0 : mibm::mls_exp(-sq(r / rcoef)); }
 inline double mls_gauss_deriv(double r, double rcoef) {
-  return (r > 1.0) ? 0.0 : -2.0 * r / sq(rcoef) * std::exp(-sq(r / rcoef));
+  return (r > 1.0) ? 0.0 : -2.0 * r / sq(rcoef) * mibm::mls_exp(-sq(r / rcoef));
 }
 
 // grid selectors for the staggered positions: 0 = c (face), 1 = m (centre)
@@ -2228,22 +2233,32 @@ int mibm_autotune_load_(const char*) { return MIBM_OK; }
 static std::map<int, std::vector<int>> g_obatch;
 static int g_obatch_next = 1;
 int mibm_batch_create_(const int* ids, const int* n) {
-  if (!ids || *n < 1) return 0;
+  if (*n < 0 || (!ids && *n > 0)) return 0;
   int h = g_obatch_next++;
   g_obatch[h] = std::vector<int>(ids, ids + *n);
   return h;
 }
+// a case that fails is left out of the rest of the step (its status stays
+// in its context); the others complete the step; the first failure is returned
 int mibm_batch_step_(const int* handle, const int* ntime) {
   auto it = g_obatch.find(*handle);
   if (it == g_obatch.end()) return MIBM_EINVAL;
+  int first_bad = MIBM_OK;
   for (int id : it->second) {
     if (mibm_context_bind_(&id) != MIBM_OK) return MIBM_EINVAL;
     Ctx* c = cur();
     if (!ready(c)) return MIBM_ESTATE;
+    if (c->status != MIBM_OK) {
+      if (first_bad == MIBM_OK) first_bad = c->status;
+      continue;
+    }
     const int nt = *ntime > 0 ? *ntime : c->steps_done + 1;
     c->I(MIBM_I_NTIME) = nt;
     cfl(*c);
-    if (c->status != MIBM_OK) return c->status;
+    if (c->status != MIBM_OK) {
+      if (first_bad == MIBM_OK) first_bad = c->status;
+      continue;
+    }
     if (c->I(MIBM_I_IDTV) == 1) {
       if (nt != 1) c->S(MIBM_S_DT) = c->S(MIBM_S_DTMAX);
       get_dt(*c);
@@ -2255,10 +2270,35 @@ int mibm_batch_step_(const int* handle, const int* ntime) {
       else if (which == 3) LinearHITForce(*c);
     }
     tschem(*c);
-    if (c->status != MIBM_OK) return c->status;
+    if (c->status != MIBM_OK) {
+      if (first_bad == MIBM_OK) first_bad = c->status;
+      continue;
+    }
     ++c->steps_done;
     c->S(MIBM_S_TIME) = c->S(MIBM_S_TIME) + c->S(MIBM_S_DT);
   }
+  return first_bad;
+}
+int mibm_batch_add_(const int* handle, const int* id) {
+  auto it = g_obatch.find(*handle);
+  if (it == g_obatch.end()) return MIBM_EINVAL;
+  for (int q : it->second)
+    if (q == *id) return MIBM_EINVAL;
+  it->second.push_back(*id);
+  return MIBM_OK;
+}
+int mibm_batch_remove_(const int* handle, const int* id) {
+  auto it = g_obatch.find(*handle);
+  if (it == g_obatch.end()) return MIBM_EINVAL;
+  for (size_t q = 0; q < it->second.size(); ++q)
+    if (it->second[q] == *id) {
+      it->second.erase(it->second.begin() + q);
+      return MIBM_OK;
+    }
+  return MIBM_EINVAL;
+}
+int mibm_batch_set_launch_(const int* handle, const int* mode) {
+  if (g_obatch.find(*handle) == g_obatch.end() || (*mode != 0 && *mode != 1)) return MIBM_EINVAL;
   return MIBM_OK;
 }
 int mibm_batch_destroy_(const int* handle) { return g_obatch.erase(*handle) ? MIBM_OK : MIBM_EINVAL; }
@@ -2415,6 +2455,7 @@ void interp_(double* arrold, double* arrnew, const int* n1o, const int* n2o, con
 
 // Oracle-only helpers used by the known-answer tests.
 int oracle_lu_inverse(double* a, int n) { return lu_inverse(a, n); }
+double oracle_mls_exp(double x) { return mibm::mls_exp(x); }
 void oracle_dft(double* re, double* im, int n, int sign) {
   std::vector<cd> x(n);
   for (int i = 0; i < n; ++i) x[i] = cd(re[i], im[i]);

@@ -45,8 +45,11 @@ def test_diagnostics_parity_after_steps(oracle_lib, gpu_lib, imlsstr):
         c.run(lib, 2)
     d_o, d_g = _diag(co, oracle_lib), _diag(cg, gpu_lib)
     # means of fields that agree to 1e-10; near-zero means (u, w_rel ...)
-    # get an absolute floor of the same order times the rms
-    _close(d_g, d_o, tol=1e-9, floor=1e-10 * max(1.0, d_o[A.MIBM_D_URMS]))
+    # get an absolute floor of the same order times the rms.  With a moving
+    # body the velocities relative to it carry the body's MLS noise (~1e-10
+    # absolute after a few steps, whichever side computes it): floor 1e-9.
+    floor = (1e-9 if imlsstr else 1e-10) * max(1.0, d_o[A.MIBM_D_URMS])
+    _close(d_g, d_o, tol=1e-9, floor=floor)
     assert d_o[A.MIBM_D_NFLUID] == d_g[A.MIBM_D_NFLUID]
     assert 0 < d_o[A.MIBM_D_NFLUID] < case.n1m * case.n2m * case.n3m
 

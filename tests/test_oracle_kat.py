@@ -361,3 +361,22 @@ def test_diagnostics_shear_flow_kat(oracle_lib):
     eps = out[D.MIBM_D_DISS]
     lam = np.sqrt(15 * nu * out[D.MIBM_D_URMS] ** 2 / eps)
     assert abs(out[D.MIBM_D_RE_LAMBDA] - out[D.MIBM_D_URMS] * lam / nu) < 1e-10
+
+
+def test_mls_exp_within_one_ulp_of_libm(oracle_lib):
+    """The written-out exp of the MLS weights (mls_exp.h, shared by the
+    oracle and the library) is within 1 ulp of the host libm over the
+    weights' range exp(-(r/0.3)^2), r <= 1, and over the normal range, with
+    the special values right."""
+    import math
+    f = oracle_lib.dll.oracle_mls_exp
+    f.restype, f.argtypes = C.c_double, [C.c_double]
+    rng = np.random.default_rng(11)
+    xs = np.concatenate([-rng.uniform(0.0, 11.2, 200000), rng.uniform(-708.0, 709.0, 50000),
+                         np.array([0.0, -0.0, 1e-300, -1e-300, 0.5 * math.log(2), -0.5 * math.log(2), 1.0, -1.0])])
+    worst = 0.0
+    for x in xs:
+        got, ref = f(float(x)), math.exp(float(x))
+        worst = max(worst, abs(got - ref) / math.ulp(ref))
+    assert worst <= 1.0, worst
+    assert f(0.0) == 1.0 and f(-800.0) == 0.0 and math.isinf(f(710.0)) and math.isnan(f(float("nan")))

@@ -1,5 +1,6 @@
-"""Serving loop: admission policy (host-only executor, no GPU) and, on the
-GPU, every served case equals the same case run alone."""
+"""Serving loop: admission and fault policy (host-only executor, no GPU)
+and, on the GPU, every served case equals the same case run alone -- also
+when other cases are cancelled, fail inside a step, or wait for memory."""
 from __future__ import annotations
 
 import time
@@ -9,33 +10,50 @@ import pytest
 
 from melt_ibm_gb300 import abi
 from melt_ibm_gb300.case import CaseConfig
-from melt_ibm_gb300.serve import DeviceExecutor, Request, Server, serving_requests
+from melt_ibm_gb300.serve import DeviceExecutor, DeviceOOM, Request, Server, serving_requests
 from tests.helpers import FIELDS_OUT, small_config
 
 
 class HostExecutor:
-    """Stands in for the device: footprint n^3 bytes, steps take 1 ms."""
+    """Stands in for the device: footprint n^3 bytes, steps take 1 ms.
+    `capacity` simulates a device smaller than the budget (admissions beyond
+    it raise DeviceOOM); `fail_at` = {rid: k} makes case rid fail in its k-th
+    step, as the library reports a case that failed inside a batch step."""
 
-    def __init__(self):
+    def __init__(self, capacity=None, fail_at=None):
         self.cases, self.log, self.resident = {}, [], 0
         self.max_resident = 0
+        self.capacity = capacity
+        self.fail_at = dict(fail_at or {})
+        self.steps = {}
 
     def estimate(self, req):
         return req.cfg.n ** 3
 
     def attach(self, req, case):
+        if self.capacity is not None and self.resident + self.estimate(req) > self.capacity:
+            self.log.append(("oom", req.rid))
+            raise DeviceOOM(f"request {req.rid}")
         self.cases[req.rid] = case
+        self.steps[req.rid] = 0
         self.resident += self.estimate(req)
         self.max_resident = max(self.max_resident, self.resident)
         self.log.append(("attach", req.rid))
 
     def detach(self, rid):
         case = self.cases.pop(rid)
+        self.steps.pop(rid)
         self.resident -= case.cfg.n ** 3
         self.log.append(("detach", rid))
 
     def step(self):
         time.sleep(0.001)
+        failed = {}
+        for rid in self.steps:
+            self.steps[rid] += 1
+            if self.fail_at.get(rid) == self.steps[rid]:
+                failed[rid] = "injected"
+        return {"admission": False, "failed": failed}
 
 
 def _requests():
@@ -57,8 +75,90 @@ def test_admission_respects_budget_and_order():
 
 
 def test_request_too_large_for_budget_is_refused():
-    with pytest.raises(ValueError):
-        Server(HostExecutor(), 10).run(_requests()[:1])
+    stats = Server(HostExecutor(), 10).run(_requests()[:2])
+    assert set(stats.failed) == {0, 1} and not stats.finished
+
+
+def test_cancel_queued_and_resident_cases():
+    ex = HostExecutor()
+    reqs = _requests()
+    reqs[5].arrival = 0.5                          # still queued when cancelled
+
+    def on_step(server, k):
+        if k == 1:
+            server.cancel(0)                       # resident
+            server.cancel(5)                       # queued, not yet arrived
+
+    stats = Server(ex, 1 << 30, on_step=on_step).run(reqs)
+    assert sorted(stats.cancelled) == [0, 5]
+    assert sorted(f.rid for f in stats.finished) == [1, 2, 3, 4]
+    assert ("attach", 5) not in ex.log
+    assert ex.log.index(("detach", 0)) < len(ex.log) and not ex.cases
+
+
+def _burst():
+    """The same requests, all arrived at once and long enough to overlap:
+    they compete for memory."""
+    reqs = _requests()
+    for r in reqs:
+        r.arrival = 0.0
+        r.steps += 60
+    return reqs
+
+
+def test_simulated_oom_is_retried_after_a_completion():
+    ex = HostExecutor(capacity=32 ** 3 + 2 * 24 ** 3)
+    stats = Server(ex, 1 << 30).run(_burst())          # the budget would admit everything
+    ooms = [q for q, (kind, _) in enumerate(ex.log) if kind == "oom"]
+    assert stats.oom_retries == len(ooms) >= 1
+    assert len(stats.finished) == 6 and not stats.failed
+    assert ex.max_resident <= ex.capacity
+    # each retry came after a resident case had completed, and the request
+    # was admitted in the end, still in arrival order
+    for q in ooms[1:]:
+        assert any(kind == "detach" for kind, _ in ex.log[ooms[0]:q])
+    rid = ex.log[ooms[0]][1]
+    at = ex.log.index(("attach", rid))
+    assert any(kind == "detach" for kind, _ in ex.log[ooms[0]:at])
+    admitted = [r for kind, r in ex.log if kind == "attach"]
+    assert admitted == sorted(admitted)
+
+
+def test_oom_with_nothing_resident_is_refused():
+    ex = HostExecutor(capacity=10)
+    stats = Server(ex, 1 << 30).run(_requests()[:2])
+    assert set(stats.failed) == {0, 1}
+
+
+def test_reduced_budget_holds_admissions():
+    ex = HostExecutor()
+    reduced = 32 ** 3                                  # the largest single request still fits
+    after = []
+
+    def on_step(server, k):
+        if k == 0:
+            server.set_budget(reduced)                 # below what is resident now
+            after.append(len(ex.log))
+
+    stats = Server(ex, 1 << 30, on_step=on_step).run(_burst())
+    assert len(stats.finished) == 6 and not stats.failed
+    # replay the log from the budget change: every admission made after it fits the new budget
+    sizes = {r.rid: r.cfg.n ** 3 for r in _requests()}
+    live = set()
+    for q, (kind, rid) in enumerate(ex.log):
+        if kind == "attach":
+            live.add(rid)
+            if q >= after[0]:
+                assert sum(sizes[x] for x in live) <= reduced, (q, live)
+        elif kind == "detach":
+            live.discard(rid)
+
+
+def test_failed_case_leaves_the_others_running():
+    ex = HostExecutor(fail_at={2: 2})
+    stats = Server(ex, 1 << 30).run(_requests())
+    assert set(stats.failed) == {2}
+    assert sorted(f.rid for f in stats.finished) == [0, 1, 3, 4, 5]
 
 
 def test_serving_requests_follow_the_configured_laws():
@@ -88,6 +188,54 @@ def test_served_cases_equal_cases_run_alone(gpu_lib):
     assert len(stats.finished) == len(reqs)
     assert max(stats.active) >= 2                      # the cases did share batch steps
     for r in reqs:
+        c = Case(r.cfg)
+        c.attach(gpu_lib)
+        c.bind(gpu_lib)
+        gpu_lib.mibm_set_precision_(abi.ref_int(r.precision), abi.ref_int(2))
+        c.run(gpu_lib, r.steps)
+        c.sync_to_host(gpu_lib, -1)
+        for k, f in FIELDS_OUT.items():
+            assert np.array_equal(c.interior(f), results[r.rid][k]), (r.rid, k)
+        c.detach(gpu_lib)
+
+
+@pytest.mark.gpu
+def test_faults_leave_other_cases_bitwise_unchanged(gpu_lib):
+    """A cancelled resident case, a case whose velocity turns non-finite
+    between two steps (the CFL guard fails it inside the batch step), and an
+    admission that runs out of (simulated) device memory and waits for a
+    completion: every case that completes equals the same case run alone,
+    bit for bit."""
+    from melt_ibm_gb300.case import Case
+    reqs = _requests()
+    results = {}
+
+    def keep(req, case):
+        case.sync_to_host(gpu_lib, -1)
+        results[req.rid] = {k: case.interior(f).copy() for k, f in FIELDS_OUT.items()}
+
+    ex = DeviceExecutor(gpu_lib)
+    one = ex.model_bytes(reqs[0].cfg, 1)
+    ex.capacity = int(2.5 * one)                       # room for two resident cases
+
+    def on_step(server, k):
+        if k == 1:
+            server.cancel(1)
+        if k == 2 and 0 in ex.cases:
+            c = ex.cases[0]
+            c.sync_to_host(gpu_lib, -1)
+            c.fields[abi.MIBM_F_VX][3, 2, 4] = np.nan
+            c.sync_from_host(gpu_lib, 1 << abi.MIBM_F_VX)
+
+    stats = Server(ex, budget_bytes=1 << 40, on_finish=keep, on_step=on_step).run(reqs)
+    ex.close()
+    assert stats.cancelled == [1]
+    assert list(stats.failed) == [0] and "status 10" in stats.failed[0]     # MIBM_ENONFINITE
+    assert stats.oom_retries >= 1
+    assert sorted(results) == [2, 3, 4, 5]
+    for r in reqs:
+        if r.rid not in results:
+            continue
         c = Case(r.cfg)
         c.attach(gpu_lib)
         c.bind(gpu_lib)
