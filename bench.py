@@ -100,19 +100,23 @@ def step_bytes_per_cell(form: str, forcing: bool, tagging: bool, nproj: int = 2)
     return {"bytes": float(total), "passes": total / 8.0}
 
 
-# DRAM bytes per launch measured with ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum, one pass, the launch list of the kernel that
-# dominates the FP64 step) per cell, at the size given; other sizes scale by
-# the cell count (the traffic is per-cell compulsory).
+# DRAM bytes per launch of the kernel that dominates the FP64 step, measured
+# with ncu (dram__bytes_read.sum + dram__bytes_write.sum, one pass, over the
+# launches of one timed step: the mean of its u, v, w, T launches), per
+# workload; a workload without its own figure scales the nearest one by the
+# cell count (the traffic is per-cell).
 NCU_TRAFFIC = {
-    "fused_rhs": {"bytes_per_cell": 139.6e6 / 128 ** 3, "measured_at": "128^3 (melt128_c1)"},
+    "melt256_c2": {"fused_rhs": {"bytes_per_launch": 1.2905e9, "measured_at": "256^3 (melt256_c2)"}},
+    "melt128_c1": {"fused_rhs": {"bytes_per_launch": 139.6e6, "measured_at": "128^3 (melt128_c1)"}},
 }
 
 # FP64 warp instructions of one step (ncu sm__inst_executed_pipe_fp64.sum
-# summed over every kernel launch of one step of the workload).  The FP64
-# form is bounded by the FP64 issue rate (one warp instruction per 16 clocks
-# per SM on this part): this count over that rate is the step's FP64 floor.
-FP64_CENSUS = {"melt128_c1": {"warp_instructions_per_step": 63.0e6, "clocks_per_instruction_per_sm": 16}}
+# summed over every kernel launch of one timed step of the workload).  The
+# FP64 form is bounded by the FP64 issue rate (one warp instruction per 16
+# clocks per SM on this part): this count over that rate is the step's FP64
+# floor.
+FP64_CENSUS = {"melt256_c2": {"warp_instructions_per_step": 493.26e6, "clocks_per_instruction_per_sm": 16},
+               "melt128_c1": {"warp_instructions_per_step": 63.0e6, "clocks_per_instruction_per_sm": 16}}
 
 FIELDS = {"u": abi.MIBM_F_VX, "v": abi.MIBM_F_VY, "w": abi.MIBM_F_VZ, "T": abi.MIBM_F_TEMP, "p": abi.MIBM_F_PR}
 FIELD_MASK = sum(1 << f for f in FIELDS.values())
@@ -365,12 +369,19 @@ def run_gpu(args):
     if passes is not None:
         algo_bytes = passes * 8.0 * n3
         achieved = algo_bytes / (avg_ms * 1e-3) / 1e9
-        tr = NCU_TRAFFIC.get(dname)
-        traffic = tr["bytes_per_cell"] * n3 if tr else None
+        tr = NCU_TRAFFIC.get(args.workload, {}).get(dname)
+        traffic = tr["bytes_per_launch"] if tr else None
+        if tr is None:                       # scale the nearest measurement by the cell count
+            for wl, kk in NCU_TRAFFIC.items():
+                if dname in kk:
+                    tr = kk[dname]
+                    traffic = tr["bytes_per_launch"] * n3 / WORKLOADS[wl]["n"] ** 3
+                    break
         roofline = {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peaks["hbm_gbs"],
                     "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
-                    "traffic_source": (f"ncu dram bytes per launch measured at {tr['measured_at']}, "
-                                       f"scaled by cells") if tr else None,
+                    "traffic_source": (f"ncu dram bytes per launch measured at {tr['measured_at']}"
+                                       + ("" if args.workload in tr["measured_at"] else ", scaled by cells"))
+                    if tr else None,
                     "algo_bytes_per_launch": algo_bytes, "avg_launch_ms": avg_ms,
                     "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs)",
                     "note": "FP64 stencils are bounded by the FP64 issue rate (about 1.2 TFLOP/s of FP64 FMA "
