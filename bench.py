@@ -500,6 +500,8 @@ def run_gpu(args):
     if dist.ws == 1 and args.extra_workload and args.extra_workload != args.workload:
         line["extra_workload"] = extra_workload_measurement(lib, args.extra_workload, args.steps, args.warmup,
                                                             args.nproj)
+    if dist.ws == 1 and args.remesh_steps > 0:
+        line["config1_remesh"] = remesh_measurement(lib, args.remesh_steps, args.remesh_long_steps)
     if dist.ws == 1 and not args.no_batch:
         line["batched"] = batched_measurement(lib, args.batch_steps, args.warmup)
     if dist.ws == 1 and not args.no_serve:
@@ -545,6 +547,61 @@ def extra_workload_measurement(lib, workload: str, steps: int, warmup: int, npro
                      "step_roofline_frac": gbs / pk["hbm_gbs"], "divergence_max": lib.mibm_divergence_max_()}
         c.detach(lib)
     out["speedup_f32_vs_f64"] = out["f32"]["value"] / out["f64"]["value"]
+    return out
+
+
+def remesh_measurement(lib, steps: int, long_steps: int) -> dict:
+    """The 128^3 free-body configuration with remeshing on (melt128_c1_remesh):
+    `steps` steps timed (CUDA events; a step that may remesh runs without a
+    step graph and reads the trigger once per substep), then continued to
+    `long_steps`, reporting where Re_lambda goes under the linear forcing.  A
+    run that reaches the reference's exit condition (the body melted below
+    27 cell volumes) or a remesher abort stops there and says so."""
+    workload = "melt128_c1_remesh"
+    case = Case(CaseConfig(**WORKLOADS[workload]))
+    n3 = case.n1m * case.n2m * case.n3m
+    case.attach(lib)
+    case.use_library_remesher(lib)
+    lib.check("remesher")
+    v0 = case.S(abi.MIBM_S_VOLUME)
+    nt = 1
+    lib.mibm_timer_mark_(abi.ref_int(6))
+    stopped = None
+    try:
+        for _ in range(steps):
+            case.step(lib, nt)
+            nt += 1
+    except RuntimeError as e:
+        stopped = str(e)
+    lib.mibm_timer_mark_(abi.ref_int(7))
+    ms = lib.mibm_timer_ms_(abi.ref_int(6), abi.ref_int(7))
+    done = nt - 1
+    out = {"workload": workload, "description": WORKLOAD_TEXT[workload], "steps": done,
+           "value": n3 * done / (ms * 1e-3) / 1e6 if done else 0.0, "unit": "Mcell-steps/s",
+           "ms_per_step": ms / max(1, done), "remesh_events": int(lib.mibm_remesh_count_()),
+           "volume_over_initial": case.S(abi.MIBM_S_VOLUME) / v0}
+    stats = np.zeros(8)
+    lib.mibm_remesh_stats_(stats.ctypes.data)
+    out["last_remesh"] = {"edge_collapses": stats[0], "vertex_deletions": stats[1], "edge_relaxations": stats[2],
+                          "volume_residual": stats[5] - stats[3], "largest_drift": stats[6]}
+    series = []
+    diag = np.zeros(abi.MIBM_NDIAG)
+    if lib.mibm_diagnostics_(diag.ctypes.data) == 0:
+        series.append({"step": done, "re_lambda": float(diag[abi.MIBM_D_RE_LAMBDA])})
+    if stopped is None:
+        try:
+            while nt <= long_steps:
+                case.step(lib, nt)
+                if nt % 100 == 0 and lib.mibm_diagnostics_(diag.ctypes.data) == 0:
+                    series.append({"step": nt, "re_lambda": float(diag[abi.MIBM_D_RE_LAMBDA]),
+                                   "volume_over_initial": case.S(abi.MIBM_S_VOLUME) / v0,
+                                   "remesh_events": int(lib.mibm_remesh_count_())})
+                nt += 1
+        except RuntimeError as e:
+            stopped = f"after {nt - 1} steps: {e}"
+    out["re_lambda_series"] = series
+    out["stopped"] = stopped
+    case.detach(lib)
     return out
 
 
@@ -657,6 +714,10 @@ def main():
     ap.add_argument("--no-fp32", action="store_true", help="skip the precision-form measurement")
     ap.add_argument("--nproj", type=int, default=2, help="Poisson solves per substep in the precision form")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-form measurement")
+    ap.add_argument("--remesh-steps", type=int, default=100,
+                    help="steps of the 128^3 free-body configuration with remeshing (0: skip)")
+    ap.add_argument("--remesh-long-steps", type=int, default=1000,
+                    help="continue that case to this step for the Re_lambda series")
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     ap.add_argument("--serve-seconds", type=float, default=30.0,

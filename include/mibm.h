@@ -350,6 +350,28 @@ void mibm_linear_hit_force_(void);
 typedef int (*mibm_remesh_fn)(void* user);
 void mibm_set_remesh_callback_(mibm_remesh_fn fn, void* user);
 int  mibm_remesh_count_(void);
+/* The reference's remesher as host code of the library (remesh.cu): QEM    */
+/* edge collapses and vertex deletions (remesh_coarsen.f90:2-760), then     */
+/* volume-conserving edge relaxation (remesh_smooth.f90:3-474).  Arrays in */
+/* the reference's layouts with 1-based indices: xyzv, vmelt (3, nv),       */
+/* tri_nor (3, nf), elengths (ne), vert_of_face, edge_of_face (3, nf),      */
+/* vert_of_edge (2, ne), ghost flags (0/1), and face_of_edge (2, ne), which */
+/* the caller keeps between calls (rebuilt as partaux.f90:221-245 builds it */
+/* when it does not describe the mesh, e.g. all zero).  Returns 0; 1       */
+/* topology not preserved, 2 reduced to a tetrahedron, 3 volume residual    */
+/* above 1e-14 (the reference's aborts), 4 singular QEM system, 5 a         */
+/* neighbour walk failed, 6 bad arguments.  stats (8 doubles, may be NULL): */
+/* edge collapses, vertex deletions, edge relaxations, vol_melt,            */
+/* vol_coarse, vol_smooth, largest drift, extra volume passes.              */
+/* mibm_remesh_builtin_ is the same remesher in the form of a remesh        */
+/* callback, on the bound context's registered host arrays (face_of_edge    */
+/* kept per context): mibm_set_remesh_callback_(mibm_remesh_builtin_, NULL). */
+/* mibm_remesh_stats_: the statistics of its last call on the bound context. */
+int mibm_remesh_mesh(int nv, int ne, int nf, double* xyzv, double* tri_nor, double* vmelt, double* elengths,
+                     int* vert_of_face, int* edge_of_face, int* vert_of_edge, int* face_of_edge,
+                     int* ghost_face, int* ghost_edge, int* ghost_vert, double e_thresh, double* stats);
+int  mibm_remesh_builtin_(void* user);
+int  mibm_remesh_stats_(double* out);
 
 /* Per-step diagnostics.  The reference's CalcDissipation (diss.f90:11-201), */
 /* vorticity (vorticity.f90:1-109) and calcFluidVelAvgs (calcSlipVels.f90:   */

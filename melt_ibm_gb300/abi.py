@@ -83,6 +83,9 @@ SIGNATURES: dict[str, tuple] = {
     "mibm_set_remesh_callback_": (None, [C.c_void_p, C.c_void_p]),
     "mibm_pin_host_": (C.c_int, [_I]),
     "mibm_remesh_count_": (C.c_int, []),
+    "mibm_remesh_mesh": (C.c_int, [C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 11 + [C.c_double, C.c_void_p]),
+    "mibm_remesh_builtin_": (C.c_int, [C.c_void_p]),
+    "mibm_remesh_stats_": (C.c_int, [C.c_void_p]),
     "mibm_diagnostics_": (C.c_int, [C.c_void_p]),
     "mibm_set_diagnostics_": (None, [_I]),
     "mibm_diagnostics_get_": (C.c_int, [C.c_void_p]),

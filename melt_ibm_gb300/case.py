@@ -367,6 +367,35 @@ class Case:
         for nt in range(start, start + nsteps):
             self.step(lib, nt)
 
+    def use_library_remesher(self, lib: abi.Lib, remesher: abi.Lib | None = None) -> None:
+        """Set the library's remesher (QEM coarsening + volume-conserving
+        smoothing, the reference's remesh_coarsen / remesh_smooth) as this
+        case's remesh callback in `lib`.  With `remesher` None (or `lib`
+        itself) that is `mibm_remesh_builtin_`; otherwise `remesher` is a
+        libmibm.so whose host function `mibm_remesh_mesh` is called on this
+        case's registered arrays (another library exporting the same ABI
+        gets the same remesher), with face_of_edge kept here between calls."""
+        A = abi
+        self.bind(lib)
+        if remesher is None or remesher.path == lib.path:
+            fn = abi.C.cast(lib.dll.mibm_remesh_builtin_, abi.C.c_void_p)
+            lib.mibm_set_remesh_callback_(fn, None)
+            return
+        M = self.mesh_arrays
+        foe = np.zeros((2, self.maxne), dtype=np.int32, order="F")
+        stats = np.zeros(8)
+
+        def call(user):
+            P = lambda mid: M[mid].ctypes.data
+            return int(remesher.mibm_remesh_mesh(
+                self.maxnv, self.maxne, self.maxnf, P(A.MIBM_M_XYZV), P(A.MIBM_M_TRI_NOR), P(A.MIBM_M_VMELT),
+                P(A.MIBM_M_ELENGTHS), P(A.MIBM_M_VERT_OF_FACE), P(A.MIBM_M_EDGE_OF_FACE), P(A.MIBM_M_VERT_OF_EDGE),
+                foe.ctypes.data, P(A.MIBM_M_GHOST_FACE), P(A.MIBM_M_GHOST_EDGE), P(A.MIBM_M_GHOST_VERT),
+                self.S(A.MIBM_S_E_THRESH), stats.ctypes.data))
+
+        self._remesh_trampoline = (abi.REMESH_FN(call), foe, stats)     # kept alive with the case
+        lib.mibm_set_remesh_callback_(abi.C.cast(self._remesh_trampoline[0], abi.C.c_void_p), None)
+
     def sync_to_host(self, lib: abi.Lib, mask: int = -1) -> None:
         self.bind(lib)
         lib.mibm_sync_to_host_(abi.ref_ll(mask))

@@ -917,6 +917,13 @@ int mibm_remesh_count_(void) {
   return c->remesh_count;
 }
 
+// statistics of the library remesher's last call on the bound context
+int mibm_remesh_stats_(double* out) {
+  Ctx* c = current(); if (!c || !out) return MIBM_EINVAL;
+  for (int q = 0; q < 8; ++q) out[q] = c->remesh_stats[q];
+  return MIBM_OK;
+}
+
 // Diagnostics (diag.cu): computed now, or per step inside tschem_.
 int mibm_diagnostics_(double* out) {
   Ctx* c = current(); if (!ready(c)) return c ? c->status : MIBM_ESTATE;

@@ -203,6 +203,10 @@ struct Ctx {
   mibm_remesh_fn remesh_fn = nullptr;
   void* remesh_user = nullptr;
   int remesh_count = 0;
+  // the library's remesher (remesh.cu): statistics of its last call on this
+  // context [edge collapses, vertex deletions, edge relaxations, vol_melt,
+  // vol_coarse, vol_smooth, largest vertex drift, extra volume passes]
+  double remesh_stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   // per-step diagnostics (diag.cu): requested, last values, device state
   bool diag_on = false, diag_valid = false;
   double diag_last[MIBM_NDIAG] = {0};

@@ -81,3 +81,43 @@ def test_remesh_trigger_without_remesher_stops(gpu_lib):
     assert gpu_lib.mibm_last_status_() == A.MIBM_ESTATE
     assert b"remesh" in gpu_lib.mibm_last_message()
     c.detach(gpu_lib)
+
+
+def test_library_remesher_parity(oracle_lib, gpu_lib):
+    """A real remesh event with the library's remesher (remesh_coarsen +
+    remesh_smooth as host code): a fixed, melting spheroid whose shortest
+    edges (the lowest 1.5 %) sit below E_thresh from the start.  The GPU run
+    uses the remesh callback mibm_remesh_builtin_; the oracle run hands its
+    own arrays to the same host remesher (mibm_remesh_mesh).  The body does
+    not move, so both hand the remesher the same mesh to round-off: the same
+    topology comes back, the smoothed vertices agree to 1e-10 (the smoothing
+    amplifies last-bit differences), and the fields agree at the plain-form
+    tolerance after the steps that follow."""
+    cfg = small_config(n=32, level=3, iremesh=1, rad_p=0.55, axes=(1.0, 0.75, 0.75), imlsstr=0)
+    case = Case(cfg)
+    x = case.mesh_arrays[A.MIBM_M_XYZV]
+    e = case.mesh_arrays[A.MIBM_M_VERT_OF_EDGE] - 1
+    el = np.sort(np.linalg.norm(x[:, e[0]] - x[:, e[1]], axis=0))
+    case.set_S(A.MIBM_S_E_THRESH, float(el[int(0.015 * el.size)]))
+    co, cg = pair(case, oracle_lib, gpu_lib)
+    co.use_library_remesher(oracle_lib, remesher=gpu_lib)
+    cg.use_library_remesher(gpu_lib)
+    co.run(oracle_lib, 3)
+    cg.run(gpu_lib, 3)
+    cg.sync_to_host(gpu_lib, ALL)
+    cg.bind(gpu_lib)
+    n_gpu = gpu_lib.mibm_remesh_count_()
+    stats = np.zeros(8)
+    assert gpu_lib.mibm_remesh_stats_(stats.ctypes.data) == 0 and stats[0] + stats[1] >= 1
+    co.bind(oracle_lib)
+    assert n_gpu >= 1 and oracle_lib.mibm_remesh_count_() == n_gpu
+    for mid in (A.MIBM_M_GHOST_FACE, A.MIBM_M_GHOST_EDGE, A.MIBM_M_GHOST_VERT, A.MIBM_M_VERT_OF_FACE,
+                A.MIBM_M_EDGE_OF_FACE, A.MIBM_M_VERT_OF_EDGE):
+        assert np.array_equal(cg.mesh_arrays[mid], co.mesh_arrays[mid]), mid
+    live_v = co.mesh_arrays[A.MIBM_M_GHOST_VERT] == 0
+    assert live_v.sum() < case.maxnv
+    a, b = cg.mesh_arrays[A.MIBM_M_XYZV][:, live_v], co.mesh_arrays[A.MIBM_M_XYZV][:, live_v]
+    assert np.abs(a - b).max() <= 1e-10
+    for name, fid in FIELDS_OUT.items():
+        err = rel_l2(cg.interior(fid), co.interior(fid))
+        assert err <= 1e-10, f"{name}: {err:.3e}"
