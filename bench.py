@@ -501,7 +501,9 @@ def run_gpu(args):
         line["extra_workload"] = extra_workload_measurement(lib, args.extra_workload, args.steps, args.warmup,
                                                             args.nproj)
     if dist.ws == 1 and args.remesh_steps > 0:
-        line["config1_remesh"] = remesh_measurement(lib, args.remesh_steps, args.remesh_long_steps)
+        line["config1_remesh"] = remesh_measurement(lib, args.remesh_steps)
+    if dist.ws == 1 and args.relambda_steps > 0:
+        line["config1_re_lambda"] = relambda_measurement(lib, args.relambda_steps)
     if dist.ws == 1 and not args.no_batch:
         line["batched"] = batched_measurement(lib, args.batch_steps, args.warmup)
     if dist.ws == 1 and not args.no_serve:
@@ -550,13 +552,12 @@ def extra_workload_measurement(lib, workload: str, steps: int, warmup: int, npro
     return out
 
 
-def remesh_measurement(lib, steps: int, long_steps: int) -> dict:
-    """The 128^3 free-body configuration with remeshing on (melt128_c1_remesh):
-    `steps` steps timed (CUDA events; a step that may remesh runs without a
-    step graph and reads the trigger once per substep), then continued to
-    `long_steps`, reporting where Re_lambda goes under the linear forcing.  A
-    run that reaches the reference's exit condition (the body melted below
-    27 cell volumes) or a remesher abort stops there and says so."""
+def remesh_measurement(lib, steps: int) -> dict:
+    """The 128^3 free-body configuration with remeshing on (melt128_c1_remesh),
+    `steps` steps timed with CUDA events (a step that may remesh runs without
+    a step graph and reads the trigger once per substep).  A run that
+    reaches the reference's exit condition (the body melted below 27 cell
+    volumes) or a remesher abort stops there and says so."""
     workload = "melt128_c1_remesh"
     case = Case(CaseConfig(**WORKLOADS[workload]))
     n3 = case.n1m * case.n2m * case.n3m
@@ -572,37 +573,43 @@ def remesh_measurement(lib, steps: int, long_steps: int) -> dict:
             case.step(lib, nt)
             nt += 1
     except RuntimeError as e:
-        stopped = str(e)
+        stopped = f"after {nt - 1} steps: {e}"
     lib.mibm_timer_mark_(abi.ref_int(7))
     ms = lib.mibm_timer_ms_(abi.ref_int(6), abi.ref_int(7))
     done = nt - 1
     out = {"workload": workload, "description": WORKLOAD_TEXT[workload], "steps": done,
            "value": n3 * done / (ms * 1e-3) / 1e6 if done else 0.0, "unit": "Mcell-steps/s",
            "ms_per_step": ms / max(1, done), "remesh_events": int(lib.mibm_remesh_count_()),
-           "volume_over_initial": case.S(abi.MIBM_S_VOLUME) / v0}
+           "volume_over_initial": case.S(abi.MIBM_S_VOLUME) / v0, "stopped": stopped}
     stats = np.zeros(8)
     lib.mibm_remesh_stats_(stats.ctypes.data)
     out["last_remesh"] = {"edge_collapses": stats[0], "vertex_deletions": stats[1], "edge_relaxations": stats[2],
                           "volume_residual": stats[5] - stats[3], "largest_drift": stats[6]}
-    series = []
-    diag = np.zeros(abi.MIBM_NDIAG)
-    if lib.mibm_diagnostics_(diag.ctypes.data) == 0:
-        series.append({"step": done, "re_lambda": float(diag[abi.MIBM_D_RE_LAMBDA])})
-    if stopped is None:
-        try:
-            while nt <= long_steps:
-                case.step(lib, nt)
-                if nt % 100 == 0 and lib.mibm_diagnostics_(diag.ctypes.data) == 0:
-                    series.append({"step": nt, "re_lambda": float(diag[abi.MIBM_D_RE_LAMBDA]),
-                                   "volume_over_initial": case.S(abi.MIBM_S_VOLUME) / v0,
-                                   "remesh_events": int(lib.mibm_remesh_count_())})
-                nt += 1
-        except RuntimeError as e:
-            stopped = f"after {nt - 1} steps: {e}"
-    out["re_lambda_series"] = series
-    out["stopped"] = stopped
     case.detach(lib)
     return out
+
+
+def relambda_measurement(lib, steps: int, every: int = 250) -> dict:
+    """Where the linear forcing takes Re_lambda: the 128^3 configuration's
+    fluid (nu = 0.005, C_HIT of melt128_c1) with the body held solid, `steps`
+    steps, Re_lambda every `every` steps and its mean over the second half."""
+    w = dict(WORKLOADS["melt128_c1"])
+    w.update(imelt=0, imlsstr=0)
+    case = Case(CaseConfig(**w))
+    case.attach(lib)
+    diag = np.zeros(abi.MIBM_NDIAG)
+    series = []
+    for nt in range(1, steps + 1):
+        case.step(lib, nt)
+        if nt % every == 0 and lib.mibm_diagnostics_(diag.ctypes.data) == 0:
+            series.append({"step": nt, "time": case.S(abi.MIBM_S_TIME),
+                           "re_lambda": float(diag[abi.MIBM_D_RE_LAMBDA]),
+                           "kinetic_energy": float(diag[abi.MIBM_D_KENERG])})
+    case.detach(lib)
+    late = [p["re_lambda"] for p in series if p["step"] > steps // 2]
+    return {"c_hit": w["c_hit"], "nu": 1.0 / w["ren"], "steps": steps, "series": series,
+            "re_lambda_mean_second_half": float(np.mean(late)) if late else None,
+            "body": "held solid (imelt = 0, imlsstr = 0)"}
 
 
 def batched_measurement(lib, steps: int, warmup: int, seed: int = 100) -> dict:
@@ -716,8 +723,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-form measurement")
     ap.add_argument("--remesh-steps", type=int, default=100,
                     help="steps of the 128^3 free-body configuration with remeshing (0: skip)")
-    ap.add_argument("--remesh-long-steps", type=int, default=1000,
-                    help="continue that case to this step for the Re_lambda series")
+    ap.add_argument("--relambda-steps", type=int, default=3500,
+                    help="steps of the Re_lambda series under the linear forcing (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     ap.add_argument("--serve-seconds", type=float, default=30.0,
