@@ -243,6 +243,13 @@ void interp_(double* arrold, double* arrnew, const int* n1o, const int* n2o,
  * terms, RHS, line solves and FFTs on FP64 fields, with the pressure
  * projection repeated `nproj` times on the FP64 divergence residual. */
 void mibm_set_precision_(const int* mode, const int* nproj);
+/* mibm_set_tma_: the precision form's y- and z-line solves read their     */
+/* lines through bulk tensor copies (TMA) into shared memory (1, default)   */
+/* or straight from global memory (0).  Both give the same bits; lines      */
+/* longer than 256 cells or grids narrower than 32 cells always take the    */
+/* second path.  A staged copy that does not complete within about a second */
+/* is reported as MIBM_ETIMEOUT by the next cfl_.                           */
+void mibm_set_tma_(const int* on);
 /* Step graphs (no counterpart in the reference): from its second call on,  */
 /* tschem_ captures its device work into a CUDA graph and replays it while */
 /* nothing it reads by value from the host changes (flags, constants, the */

@@ -68,6 +68,7 @@ SIGNATURES: dict[str, tuple] = {
     "mibm_profile_get_": (C.c_int, [_I, C.c_char_p, _I, _D, C.POINTER(C.c_longlong)]),
     "mibm_solxi_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_void_p]),
     "mibm_set_precision_": (None, [_I, _I]),
+    "mibm_set_tma_": (None, [_I]),
     "mibm_set_graphs_": (None, [_I]),
     "mibm_autotune_": (C.c_int, []),
     "mibm_autotune_get_": (C.c_int, [C.c_void_p]),

@@ -187,7 +187,7 @@ static void step_enqueue_f32(Ctx* c) {
       k_solve_y_f32(c, r, Tt + tlen, 1);
       k_solve_z_f32(c, r, Tt + 2 * tlen, qt, 1, t_mirror);
     }
-    const double* mean3 = lagr_particle_fused(c, dp, t_mirror, ns < 2 ? c->dparams + ns + 1 : nullptr, ns + 1);
+    const double* mean3 = lagr_particle_fused(c, dp, c->q32, ns < 2 ? c->dparams + ns + 1 : nullptr, ns + 1);
     if (c->status != MIBM_OK) return;
     for (int it = 0; it < c->nproj; ++it) {
       bool last = it + 1 == c->nproj;
@@ -761,6 +761,15 @@ void mibm_set_precision_(const int* mode, const int* nproj) {
   c->precision = *mode;
   c->nproj = *nproj;
   ++c->geom_gen;                       // the MLS weights of the two forms differ
+}
+
+// Staged FP32 line solves on (1, default) or off (0): bit-identical results
+// either way; the switch exists to compare the two data paths.
+void mibm_set_tma_(const int* on) {
+  Ctx* c = current(); if (!ready(c)) return;
+  if (*on != 0 && *on != 1) { fail(c, MIBM_EINVAL, "set_tma: 0|1"); return; }
+  if (c->tma != *on) ++c->tune_gen;    // the step graph holds the other kernels
+  c->tma = *on;
 }
 
 // Batched form (see Batch above).  ids: contexts after mibm_init_ (and the

@@ -198,6 +198,7 @@ struct Ctx {
   int tune_m[3] = {-1, -1, -1};           // line-solve chunk length per direction
   int tune_by = 8;                        // block height of the explicit-term kernel
   uint64_t tune_gen = 0;
+  int tma = 1;                            // FP32 y/z line solves staged by bulk tensor copies
   double* step_host = nullptr;            // pinned: geometry scalars read back at step end
   // remeshing hand-off: the host's remesher and the hand-offs done
   mibm_remesh_fn remesh_fn = nullptr;
@@ -352,6 +353,7 @@ bool tri_step_fill(Ctx* c, const double betadx[3][2][3], bool f32);
 const double* tri_step_enqueue(Ctx* c, bool f32, int* len_out, const float** f32_out);
 void k_solve_x_f32(Ctx* c, float* rhs, const float* T, int nfield);
 void k_solve_y_f32(Ctx* c, float* rhs, const float* T, int nfield);
+// mirror: FP32 copies of the q fields written beside them (field f at mirror + f*cells), or null
 void k_solve_z_f32(Ctx* c, float* rhs, const float* T, double* const* q, int nfield, float* mirror);
 // fft.cu
 void k_phcalc(Ctx* c);
@@ -369,7 +371,9 @@ void lagr_geometry_refresh(Ctx* c, bool imelt);
 void lagr_tag_narrow_band(Ctx* c);
 void lagr_tag_initial(Ctx* c);
 void lagr_particle(Ctx* c, const StepParams* dp);
-const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror, StepParams* next,
+// m32: base of the FP32 mirrors (precision form; the temperature forcing
+// keeps T's mirror equal to the forced field), or null
+const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* m32, StepParams* next,
                                   int next_prologue);
 void lagr_substep_prologue(Ctx* c, int slot);
 int lagr_take_plan_request(Ctx* c);

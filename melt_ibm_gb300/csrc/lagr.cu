@@ -2125,10 +2125,11 @@ static void update_plan(Ctx* c, const StepParams* dp) {
   MIBM_LAUNCH_CHECK(c, "scatter plan");
 }
 
-static ScatterOut scatter_out(Ctx* c, bool into_fields, float* t_mirror) {
+// m32: base of the FP32 mirrors (u, v, w, T at 0, cells, 2 cells, 3 cells)
+// that the scatter keeps equal to the forced fields, or null
+static ScatterOut scatter_out(Ctx* c, bool into_fields, float* m32) {
   ScatterOut O;
-  O.m32[0] = O.m32[1] = O.m32[2] = nullptr;
-  O.m32[3] = into_fields ? t_mirror : nullptr;
+  for (int q = 0; q < 4; ++q) O.m32[q] = (into_fields && m32) ? m32 + (size_t)q * c->g.cells : nullptr;
   static const int fo[4] = {MIBM_F_FORXC, MIBM_F_FORYC, MIBM_F_FORZC, MIBM_F_FORTEMP};
   static const int fq[4] = {MIBM_F_VX, MIBM_F_VY, MIBM_F_VZ, MIBM_F_TEMP};
   for (int q = 0; q < 4; ++q) O.f[q] = c->df[into_fields ? fq[q] : fo[q]];
@@ -2150,11 +2151,11 @@ static void force_coefficients(Ctx* c) {
   ++c->launches;
 }
 
-static void scatter(Ctx* c, bool into_fields, int lo, int hi, bool record, float* t_mirror = nullptr) {
+static void scatter(Ctx* c, bool into_fields, int lo, int hi, bool record, float* m32 = nullptr) {
   LagState* s = lag_of(c);
   { MIBM_PROF(c, "scatter_apply");
     scatter_apply_kernel<<<(unsigned)std::min<size_t>(kScatterBlocks, div_up(s->plan_n, 256)), 256, 0, c->stream>>>(
-        s->plan_n, c->maxnf, c->g.cells, s->res_key, s->res_src, c->tri_coef, scatter_out(c, into_fields, t_mirror), lo, hi,
+        s->plan_n, c->maxnf, c->g.cells, s->res_key, s->res_src, c->tri_coef, scatter_out(c, into_fields, m32), lo, hi,
         s->heads, s->nheads, record ? s->segval : nullptr); }
   ++c->launches;
 }
@@ -2680,7 +2681,7 @@ void lagr_loads_early(Ctx* c, const StepParams* dp) {
   c->loads_pending = true;
 }
 
-const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror, StepParams* next,
+const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* m32, StepParams* next,
                                   int next_prologue) {
   if (c->I(MIBM_I_IMLSFOR) != 1 || c->maxnf == 0) return nullptr;
   if (!ensure_adjacency(c) || !ensure_lag_buffers(c)) return nullptr;
@@ -2718,7 +2719,7 @@ const double* lagr_particle_fused(Ctx* c, const StepParams* dp, float* t_mirror,
     lagr_find_probe_indices(c);
     heat_flux_launch(c);
   }
-  scatter(c, true, 3, 4, false, t_mirror);
+  scatter(c, true, 3, 4, false, m32);
   if (imelt) lagr_stefan(c, dp);
   if (str) motion_launch(c, dp);
   bool remeshed = !fork && lagr_remesh_active(c) && remesh_check(c);

@@ -903,11 +903,15 @@ void k_cfl_async(Ctx* c, double* out) {
 }
 
 // After the stream has completed a k_cfl_async: the non-finite guard.
+// Bit 1 of the same word: a bounded wait of the staged line solves ran out
+// in the step before (tridiag.cu).
 bool cfl_finite(Ctx* c) {
-  if (!c->hflag[2]) return true;
+  const int f = c->hflag[2];
+  if (!f) return true;
   c->hflag[2] = 0;
   cudaMemsetAsync(c->dflag + 2, 0, sizeof(int), c->stream);
-  fail(c, MIBM_ENONFINITE, "cfl: non-finite velocity or temperature");
+  if (f & 2) fail(c, MIBM_ETIMEOUT, "line solve: a staged tile copy did not complete within its wait limit");
+  else fail(c, MIBM_ENONFINITE, "cfl: non-finite velocity or temperature");
   return false;
 }
 

@@ -41,6 +41,7 @@
 
 #include "common.cuh"
 #include "fpconv.cuh"
+#include "tma.cuh"
 
 namespace mibm {
 
@@ -182,8 +183,11 @@ static const double* table_for(Ctx* c, int dir, double betadx) {
 
 static void steptab_free(Ctx* c);
 
+static void tmaps_free(Ctx* c);
+
 void tri_free(Ctx* c) {
   steptab_free(c);
+  tmaps_free(c);
   for (size_t q = 0; q < g_tri.size(); ++q)
     if (g_tri[q].first == c) {
       cudaFree(g_tri[q].second->cache.dev);
@@ -714,9 +718,157 @@ __global__ void __launch_bounds__(32 * col_max_chunks(M)) solve_cc_kernel(Grid g
       if (write_rhs) rp[o] = xv;
       double qn = qv[ZL ? i : 0] + widen(xv);
       q[first + o] = qn;
-      if (m32) m32[first + o] = d2f_bits(qn);
+      if (m32) m32[(size_t)f * g.cells + first + o] = d2f_bits(qn);
     } else {
       rp[o] = xv;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------
+// y- and z-lines in FP32 with the lines staged by bulk tensor copies
+// ---------------------------------------------------------------------
+// The same arithmetic as solve_cc_kernel<float, M, ZL>, bit for bit, in a
+// persistent kernel: each block walks tiles t = blockIdx.x, + gridDim.x, ...
+// of 32 adjacent x times one whole line (a plane j for z-lines, k for
+// y-lines) of one field.  One thread copies the next tiles' lines (and, for
+// z-lines, the FP64 field the increment is added to) into a ring of `nstage`
+// shared-memory stages with cp.async.bulk.tensor while the block solves the
+// current one, so the loads of several tiles are always in flight and the
+// registers hold only the chunk (the FP64 field waits in shared memory).
+// The factor table is copied to shared memory once per block.  Results are
+// written with coalesced stores (32 consecutive x per warp instruction).
+// A stage wait that runs out of time (about a second: a copy that never
+// completes) sets bit 2 of `err` and the block leaves after its other copies
+// have landed or timed out; the host reports MIBM_ETIMEOUT.
+struct ColMaps {
+  CUtensorMap rhs;    // nfield rhs fields; box (32, 1, n3m, 1) for z-lines, (32, n2m, 1, 1) for y-lines
+  CUtensorMap q[3];   // z-lines: per field, the FP64 field the increment is added to; box (32, 1, n3m, 1)
+};
+
+template <int M, bool ZL>
+__global__ void __launch_bounds__(32 * col_max_chunks(M), 1) solve_cc_tma_kernel(
+    const __grid_constant__ ColMaps maps, Grid g, float* __restrict__ rhs_base, const float* __restrict__ Xg,
+    int xlen, QSet qs, float* __restrict__ m32, int nfield, int nstage, int* __restrict__ err) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ float sC[kColMaxChunks][32];
+  __shared__ float sU[kColMaxChunks][32];
+  __shared__ float sF[3][32];
+  const int n = ZL ? g.n3m : g.n2m, G = n / M;
+  const int lane = threadIdx.x, w = threadIdx.y, tid = w * 32 + lane, nthr = 32 * G;
+  const int planes = ZL ? g.n2m : g.n3m, nxt = (g.n1m + 31) / 32;
+  const int ntiles = nxt * planes * nfield;
+  const uint32_t stage_bytes = (uint32_t)n * 32u * (ZL ? 12u : 4u);
+  // barriers at a 1024-byte boundary (the launch adds that much slack), the
+  // stages from 128 bytes after it: every copy destination 128-byte aligned
+  unsigned char* smem = smem_raw + ((1024u - (tma::smem_addr(smem_raw) & 1023u)) & 1023u);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
+  unsigned char* stage0 = smem + 128;
+  float* X = reinterpret_cast<float*>(stage0 + (size_t)nstage * stage_bytes);
+  auto sR = [&](int s) { return reinterpret_cast<float*>(stage0 + (size_t)s * stage_bytes); };
+  auto sQ = [&](int s) { return reinterpret_cast<double*>(stage0 + (size_t)s * stage_bytes + (size_t)n * 128); };
+  auto issue = [&](int tile, int s) {
+    const int xt = tile % nxt, rest = tile / nxt, pl = rest % planes, f = rest / planes;
+    tma::mbar_arrive_expect_tx(bars + s, stage_bytes);
+    if (ZL) {
+      tma::load_4d(sR(s), &maps.rhs, bars + s, xt * 32, pl, 0, f);
+      tma::load_4d(sQ(s), &maps.q[f], bars + s, xt * 32, pl, 0, 0);
+    } else {
+      tma::load_4d(sR(s), &maps.rhs, bars + s, xt * 32, 0, pl, f);
+    }
+  };
+  if (tid == 0) {
+    for (int s = 0; s < nstage; ++s) tma::mbar_init(bars + s, 1);
+    tma::fence_proxy_async();
+    for (int s = 0; s < nstage; ++s) {
+      const int tile = blockIdx.x + s * gridDim.x;
+      if (tile < ntiles) issue(tile, s);
+    }
+  }
+  for (int q = tid; q < xlen; q += nthr) X[q] = Xg[q];
+  __syncthreads();
+  const int stride = ZL ? (int)g.plane : g.P;
+  const int e0 = w * M;
+  for (int li = 0;; ++li) {
+    const int tile = blockIdx.x + li * gridDim.x;
+    if (tile >= ntiles) break;
+    const int s = li % nstage;
+    const bool ok = tma::mbar_wait(bars + s, (uint32_t)((li / nstage) & 1));
+    if (!__syncthreads_and(ok)) {
+      if (tid == 0) {
+        atomicOr(err, 2);
+        for (int k = 1; k < nstage; ++k) {   // the copies still in flight
+          const int L = li + k;
+          if (blockIdx.x + L * gridDim.x < ntiles) tma::mbar_wait(bars + L % nstage, (uint32_t)((L / nstage) & 1));
+        }
+      }
+      return;
+    }
+    const int xt = tile % nxt, rest = tile / nxt, pl = rest % planes, f = rest / planes;
+    const int x = xt * 32 + lane;
+    const bool act = x < g.n1m;
+    const float* R = sR(s);
+    float r[M];
+#pragma unroll
+    for (int i = 0; i < M; ++i) r[i] = R[(e0 + i) * 32 + lane];
+    const float rlast = r[M - 1];
+    float C = 0.f;
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+      int t = i * G + w;
+      C = X[t] * r[i] - X[n + t] * C;
+      r[i] = C;
+    }
+    sC[w][lane] = C;
+    __syncthreads();
+    float y_in = 0.f;
+    for (int hh = 0; hh < w; ++hh) y_in = sC[hh][lane] + X[7 * n + hh] * y_in;
+    float D = 0.f;
+#pragma unroll
+    for (int i = M - 1; i >= 0; --i) {
+      D = r[i] + X[2 * n + i * G + w] * D;
+      r[i] = D;
+    }
+    sU[w][lane] = r[0] + X[7 * n + 2 * G + w] * y_in;
+    __syncthreads();
+    float f_in = 0.f;
+    for (int hh = G - 1; hh > w; --hh) f_in = sU[hh][lane] + X[7 * n + G + hh] * f_in;
+    if (w == 0) sF[0][lane] = r[0] + X[5 * n + w] * f_in;
+    if (w == G - 1) { sF[1][lane] = r[M - 2] + X[6 * n + (M - 2) * G + w] * y_in; sF[2][lane] = rlast; }
+    __syncthreads();
+    const float* S = X + 7 * n + 3 * G;
+    const float xn = (sF[2][lane] * S[0] - S[1] * sF[0][lane] - S[2] * sF[1][lane]) * S[3];
+    if (act) {
+      const float al = y_in + S[4 + w] * xn, be = f_in + S[4 + G + w] * xn;
+      const size_t first = (ZL ? cidx(g, x, pl, 0) : cidx(g, x, 0, pl)) + (size_t)e0 * stride;
+      if (ZL) {
+        double* __restrict__ q = qs.p[f];
+        float* __restrict__ mf = m32 ? m32 + (size_t)f * g.cells : nullptr;
+        const double* Q = sQ(s);
+#pragma unroll
+        for (int i = 0; i < M; ++i) {
+          const int t = i * G + w;
+          const float xv = r[i] + X[6 * n + t] * al + X[5 * n + t] * be;
+          const double qn = Q[(e0 + i) * 32 + lane] + widen(xv);
+          q[first + (size_t)i * stride] = qn;
+          if (mf) mf[first + (size_t)i * stride] = d2f_bits(qn);
+        }
+      } else {
+        float* __restrict__ rp = rhs_base + (size_t)f * g.cells + first;
+#pragma unroll
+        for (int i = 0; i < M; ++i) {
+          const int t = i * G + w;
+          rp[(size_t)i * stride] = r[i] + X[6 * n + t] * al + X[5 * n + t] * be;
+        }
+      }
+    }
+    __syncthreads();   // stage s, sC, sU, sF are free again
+    if (tid == 0) {
+      const int next = tile + nstage * gridDim.x;
+      if (next < ntiles) {
+        tma::fence_proxy_async();
+        issue(next, s);
+      }
     }
   }
 }
@@ -810,6 +962,109 @@ static bool smem_ok(Ctx* c, const void* fn, size_t bytes) {
     case 16: CALL(16); break;         \
   }
 
+// Tensor maps of the TMA line solves, cached per context by (address, box)
+// so that a captured step graph replays with identical parameters.
+struct TmapEntry {
+  const void* base;
+  int elem, nfield, box[4];
+  CUtensorMap map;
+};
+static std::vector<std::pair<Ctx*, std::vector<TmapEntry>*>> g_tmaps;
+static std::mutex g_tmaps_mu;
+
+static bool tmap_of(Ctx* c, const void* base, int elem, int nfield, const int box[4], CUtensorMap* out) {
+  std::lock_guard<std::mutex> lk(g_tmaps_mu);
+  std::vector<TmapEntry>* v = nullptr;
+  for (auto& e : g_tmaps)
+    if (e.first == c) v = e.second;
+  if (!v) {
+    v = new std::vector<TmapEntry>();
+    g_tmaps.emplace_back(c, v);
+  }
+  for (const TmapEntry& e : *v)
+    if (e.base == base && e.elem == elem && e.nfield == nfield && !memcmp(e.box, box, sizeof(e.box))) {
+      *out = e.map;
+      return true;
+    }
+  TmapEntry e{};
+  e.base = base; e.elem = elem; e.nfield = nfield;
+  memcpy(e.box, box, sizeof(e.box));
+  if (!tma::encode_fields(&e.map, base, elem, c->g.n1m, c->g.n2m, c->g.n3m, c->g.P, c->g.cells, nfield, box))
+    return false;
+  if (v->size() > 64) v->clear();
+  v->push_back(e);
+  *out = e.map;
+  return true;
+}
+
+static void tmaps_free(Ctx* c) {
+  std::lock_guard<std::mutex> lk(g_tmaps_mu);
+  for (size_t q = 0; q < g_tmaps.size(); ++q)
+    if (g_tmaps[q].first == c) {
+      delete g_tmaps[q].second;
+      g_tmaps.erase(g_tmaps.begin() + q);
+      return;
+    }
+}
+
+// stages of the TMA line solve: z-lines two (the FP32 line and the FP64
+// field, 96 KB per stage at 256 cells), y-lines four (32 KB each); one block
+// per SM, its copies issued that many tiles ahead
+static int tma_stages(bool zl) {
+  static const char* e = getenv("MIBM_TMA_STAGES_Y");
+  if (!zl && e) return std::max(1, std::min(6, atoi(e)));
+  return zl ? 2 : 4;
+}
+
+template <bool ZL>
+static bool solve_cc_tma_launch(Ctx* c, float* rhs, const float* X, int M, const QSet& q, int nfield,
+                                float* m32, const char* name) {
+  const int n = ZL ? c->g.n3m : c->g.n2m;
+  if (!c->tma || n > 256 || c->g.n1m < 32 || nfield < 1 || nfield > 3) return false;
+  const int G = n / M;
+  const int xlen = (int)ext_len(n, M);
+  const int nstage = tma_stages(ZL);
+  const size_t stage_bytes = (size_t)n * 32 * (ZL ? 12 : 4);
+  const size_t smem = 1024 + 128 + nstage * stage_bytes + sizeof(float) * (size_t)xlen;
+  int dev = 0, optin = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t static_smem = sizeof(float) * (2 * kColMaxChunks * 32 + 3 * 32);
+  if (smem + static_smem > (size_t)optin) return false;
+  ColMaps maps{};
+  const int box_r[4] = {32, ZL ? 1 : n, ZL ? n : 1, 1};
+  if (!tmap_of(c, rhs, 4, nfield, box_r, &maps.rhs)) return false;
+  if (ZL)
+    for (int f = 0; f < nfield; ++f) {
+      const int box_q[4] = {32, 1, n, 1};
+      if (!tmap_of(c, q.p[f], 8, 1, box_q, &maps.q[f])) return false;
+    }
+  const void* fn = nullptr;
+#define TMA_FN(MM) fn = (const void*)solve_cc_tma_kernel<MM, ZL>
+  MIBM_CHUNK_CASES(M, TMA_FN)
+#undef TMA_FN
+  if (!fn) return false;
+  if (!cuda_ok(c, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "tma smem"))
+    return false;
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32 * G, smem);
+  const int ntiles = ((c->g.n1m + 31) / 32) * (ZL ? c->g.n2m : c->g.n3m) * nfield;
+  const int grid = std::max(1, std::min(ntiles, std::max(1, per_sm) * std::max(1, sms)));
+  dim3 block(32, G);
+  {
+    MIBM_PROF(c, name);
+#define TMA_CC(MM)                                                                                          \
+  solve_cc_tma_kernel<MM, ZL><<<grid, block, smem, c->stream>>>(maps, c->g, rhs, X, xlen, q, m32, nfield, \
+                                                                 nstage, c->dflag + 2)
+    MIBM_CHUNK_CASES(M, TMA_CC)
+#undef TMA_CC
+  }
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, name);
+  return true;
+}
+
 template <typename V>
 static bool solve_xc_launch(Ctx* c, V* rhs, const V* T, const char* name, int nfield) {
   TriLayout L = tri_layout(c->g.n1m, tri_chunk(c, 0));
@@ -834,6 +1089,8 @@ static bool solve_cc_launch(Ctx* c, V* rhs, const V* T, const QSet& q, int nfiel
   TriLayout L = tri_layout(ZL ? c->g.n3m : c->g.n2m, tri_chunk(c, ZL ? 2 : 1));
   if (!L.m) return false;
   const V* X = T + L.off_ext;
+  if constexpr (sizeof(V) == 4)
+    if (!write_rhs && solve_cc_tma_launch<ZL>(c, rhs, X, L.m, q, nfield, m32, name)) return true;
   dim3 block(32, L.n / L.m);
   dim3 grid(div_up(c->g.n1m, 32), (ZL ? c->g.n2m : c->g.n3m) * nfield);
   {
