@@ -1007,14 +1007,10 @@ static void tmaps_free(Ctx* c) {
     }
 }
 
-// stages of the TMA line solve: z-lines two (the FP32 line and the FP64
-// field, 96 KB per stage at 256 cells), y-lines four (32 KB each); one block
-// per SM, its copies issued that many tiles ahead
-static int tma_stages(bool zl) {
-  static const char* e = getenv("MIBM_TMA_STAGES_Y");
-  if (!zl && e) return std::max(1, std::min(6, atoi(e)));
-  return zl ? 2 : 4;
-}
+// stages of the TMA line solve: two, the copies issued two tiles ahead
+// (z-lines: the FP32 line and the FP64 field, 96 KB per stage at 256 cells;
+// y-lines: 32 KB -- four stages measured the same as two); one block per SM
+static int tma_stages(bool) { return 2; }
 
 template <bool ZL>
 static bool solve_cc_tma_launch(Ctx* c, float* rhs, const float* X, int M, const QSet& q, int nfield,

@@ -83,6 +83,7 @@ class ServeStats:
     step_ms: list = field(default_factory=list)        # latency of every batch step
     admission: list = field(default_factory=list)      # the step carried an admission (first two steps of a case)
     active: list = field(default_factory=list)         # cases in each batch step
+    resident_cells: list = field(default_factory=list)  # cells of the resident cases in each batch step
     cell_steps: float = 0.0
     finished: list = field(default_factory=list)
     admitted: int = 0
@@ -95,6 +96,15 @@ class ServeStats:
         st = np.array(self.step_ms) if self.step_ms else np.zeros(1)
         adm = np.array(self.admission, dtype=bool) if self.admission else np.zeros(len(st), dtype=bool)
         steady = st[~adm] if (~adm).any() else st
+        # latency per resident Mcell: the step of a mix of grids 64^3..256^3
+        # lasts as long as its work, so p99/p50 of the raw latency measures
+        # the mix; this ratio measures the jitter at a given load
+        cells = np.array(self.resident_cells, dtype=float) if len(self.resident_cells) == len(st) else None
+        if cells is not None and (cells > 0).all():
+            per = st / (cells / 1e6)
+            per_steady = per[~adm] if (~adm).any() else per
+        else:
+            per_steady = np.zeros(1)
         ct = np.array([f.completed - f.arrival for f in self.finished]) if self.finished else np.zeros(1)
         qt = np.array([f.admitted - f.arrival for f in self.finished]) if self.finished else np.zeros(1)
         return {
@@ -112,6 +122,8 @@ class ServeStats:
             "step_latency_ms_outside_admission": {"p50": float(np.percentile(steady, 50)),
                                                   "p99": float(np.percentile(steady, 99)),
                                                   "max": float(steady.max())},
+            "step_latency_us_per_resident_mcell_outside_admission": {
+                "p50": float(np.percentile(per_steady, 50)), "p99": float(np.percentile(per_steady, 99))},
             "case_completion_s": {"p50": float(np.percentile(ct, 50)), "p99": float(np.percentile(ct, 99))},
             "admission_wait_s": {"p50": float(np.percentile(qt, 50)), "p99": float(np.percentile(qt, 99))},
             "mean_active_cases": float(np.mean(self.active)) if self.active else 0.0,
@@ -385,6 +397,7 @@ class Server:
                 stats.step_ms.append((time.perf_counter() - ts) * 1e3)
                 stats.admission.append(bool(info.get("admission", False)))
                 stats.active.append(len(active))
+                stats.resident_cells.append(sum(a[0].cfg.n * a[0].cfg.n * a[0].cfg.nz for a in active.values()))
                 nstep += 1
                 failed = info.get("failed", {})
                 for rid, why in failed.items():
