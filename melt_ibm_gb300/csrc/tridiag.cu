@@ -427,9 +427,35 @@ int tri_chunk_col(int n) {
 // before the chunk and BC_h the final s after it; the first chunk (y_in = 0)
 // keeps s in its DP' slots (AC = 1, BC = 0) and the last (f_in = 0) in its Q'
 // slots (AC = 0, BC = 1).  Two FMAs per element instead of three.
-static size_t ext_len(int n, int m) { return m ? 7 * (size_t)n + 5 * (size_t)(n / m) + 4 : 0; }
+__host__ __device__ constexpr size_t ext_len(int n, int m) { return m ? 7 * (size_t)n + 5 * (size_t)(n / m) + 4 : 0; }
 
-static void build_ext(const std::vector<double>& t, int n, int m, double* out) {
+// x-line scan factors after the extended table (line-solve slots only).
+// The chunk entry values of an x-line are exclusive scans of the affine
+// chunk maps y -> C + PL y (forward) and f -> U + QF f (backward, lanes in
+// descending order), by warp shuffles in rounds of offset 2^r.  Round r
+// multiplies by the composite factor of the 2^r lanes a lane already
+// covers; the FP64 kernel reads it from W_r[h] instead of forming it with
+// a second shuffle and an FP64 multiply per round (the products are those
+// the shuffle scan forms, in its order, so the result is the same).
+// Layout at ext_len(n, m): WF[5][G] (lanes h - 2^r + 1 .. h), WB[5][G]
+// (lanes h .. h + 2^r - 1).
+constexpr int kScanRounds = 5;
+static size_t scan_len(int n, int m) { return m ? 2 * kScanRounds * (size_t)(n / m) : 0; }
+
+// W[r][h] for the factors f in scan order (position h)
+static void build_scan(const std::vector<double>& f, double* W) {
+  const int G = (int)f.size();
+  std::vector<double> cur(f);
+  for (int r = 0; r < kScanRounds; ++r) {
+    const int off = 1 << r;
+    for (int h = 0; h < G; ++h) W[r * G + h] = cur[h];
+    std::vector<double> nxt(cur);
+    for (int h = off; h < G; ++h) nxt[h] = cur[h] * cur[h - off];
+    cur.swap(nxt);
+  }
+}
+
+static void build_ext(const std::vector<double>& t, int n, int m, double* out, bool scans = false) {
   int G = n / m;
   std::vector<double> a(t.begin(), t.begin() + n), b(t.begin() + n, t.begin() + 2 * n);
   std::vector<double> q(t.begin() + 2 * n, t.begin() + 3 * n), s(t.begin() + 3 * n, t.begin() + 4 * n);
@@ -467,6 +493,20 @@ static void build_ext(const std::vector<double>& t, int n, int m, double* out) {
     out[7 * (size_t)n + 2 * G + h] = dv;
   }
   for (int w = 0; w < 4; ++w) out[7 * (size_t)n + 3 * G + w] = t[4 * (size_t)n + w];
+  if (!scans) return;
+  // forward: PL in lane order; backward: QF of lanes G-1 .. 0, whose scan
+  // entry at position G-1-h is the composite of lanes h .. h + 2^r - 1
+  double* WF = out + ext_len(n, m);
+  double* WB = WF + kScanRounds * G;
+  std::vector<double> fF(G), fB(G), Wtmp(kScanRounds * (size_t)G);
+  for (int h = 0; h < G; ++h) {
+    fF[h] = out[7 * (size_t)n + h];
+    fB[h] = out[7 * (size_t)n + G + (G - 1 - h)];
+  }
+  build_scan(fF, WF);
+  build_scan(fB, Wtmp.data());
+  for (int r = 0; r < kScanRounds; ++r)
+    for (int h = 0; h < G; ++h) WB[r * G + h] = Wtmp[r * (size_t)G + (G - 1 - h)];
 }
 
 // one table slot: base table (tile kernels) and the extended table of the
@@ -481,7 +521,7 @@ static TriLayout tri_layout(int n, int m) {
   L.n = n;
   L.m = m;
   L.off_ext = 4 * (size_t)n + 4;
-  L.len = L.off_ext + ext_len(n, m);
+  L.len = L.off_ext + ext_len(n, m) + scan_len(n, m);
   return L;
 }
 
@@ -514,7 +554,7 @@ static void fill_slot(int n, int m, double betadx, double* out) {
   build_table(n, betadx, t);
   TriLayout L = tri_layout(n, m);
   std::copy(t.begin(), t.end(), out);
-  if (m) build_ext(t, n, m, out + L.off_ext);
+  if (m) build_ext(t, n, m, out + L.off_ext, true);
 }
 
 // the extended table of chunk length m for one line of n cells (ext_len(n, m)
@@ -527,8 +567,11 @@ void tri_build_ext_table(int n, int m, double betadx, std::vector<double>& out) 
   build_ext(t, n, m, out.data());
 }
 
-// slot length for lines up to nmax and any chunk (ext_len <= 7n + 5*32 + 4)
-static size_t slot_len(int nmax) { return 4 * (size_t)nmax + 4 + 7 * (size_t)nmax + 5 * 32 + 4; }
+// slot length for lines up to nmax and any chunk (ext_len + scan_len <=
+// 7n + 5*32 + 4 + 2*5*32)
+static size_t slot_len(int nmax) {
+  return 4 * (size_t)nmax + 4 + 7 * (size_t)nmax + 5 * 32 + 4 + 2 * kScanRounds * 32;
+}
 
 template <typename V, int M>
 __device__ __forceinline__ void load_chunk(const V* __restrict__ p, V (&r)[M]) {
@@ -598,11 +641,20 @@ __global__ void __launch_bounds__(256) solve_xc_kernel(Grid g, V* __restrict__ r
     C = X[t] * r[i] - X[n + t] * C;
     r[i] = C;
   }
-  // y_in: exclusive scan of the affine chunk maps y -> C + PL y
+  // y_in: exclusive scan of the affine chunk maps y -> C + PL y.  FP64: each
+  // round multiplies by the composite factor the table holds for it
+  // (build_scan); FP32 forms it with a second shuffle (cheaper than a load).
+  const V* WF = X + ext_len(n, M);
+  const V* WB = WF + kScanRounds * G;
   V Cv = act ? C : V(0), Pv = act ? X[7 * n + h] : V(1);
-  for (int off = 1; off < GP; off <<= 1) {
-    V Co = __shfl_up_sync(FULL, Cv, off, GP), Po = __shfl_up_sync(FULL, Pv, off, GP);
-    if (hl >= off) { Cv = Cv + Pv * Co; Pv = Pv * Po; }
+  for (int off = 1, r = 0; off < GP; off <<= 1, ++r) {
+    V Co = __shfl_up_sync(FULL, Cv, off, GP);
+    if constexpr (sizeof(V) == 8) {
+      if (hl >= off) Cv = Cv + WF[r * G + h] * Co;
+    } else {
+      V Po = __shfl_up_sync(FULL, Pv, off, GP);
+      if (hl >= off) { Cv = Cv + Pv * Co; Pv = Pv * Po; }
+    }
   }
   V y_in = __shfl_up_sync(FULL, Cv, 1, GP);
   if (hl == 0) y_in = V(0);
@@ -615,9 +667,14 @@ __global__ void __launch_bounds__(256) solve_xc_kernel(Grid g, V* __restrict__ r
   }
   // f_in: exclusive suffix scan of f -> u + QF f, u = D_first + DPF y_in
   V Uv = act ? r[0] + X[7 * n + 2 * G + h] * y_in : V(0), Qv = act ? X[7 * n + G + h] : V(1);
-  for (int off = 1; off < GP; off <<= 1) {
-    V Uo = __shfl_down_sync(FULL, Uv, off, GP), Qo = __shfl_down_sync(FULL, Qv, off, GP);
-    if (hl + off < G) { Uv = Uv + Qv * Uo; Qv = Qv * Qo; }
+  for (int off = 1, r = 0; off < GP; off <<= 1, ++r) {
+    V Uo = __shfl_down_sync(FULL, Uv, off, GP);
+    if constexpr (sizeof(V) == 8) {
+      if (hl + off < G) Uv = Uv + WB[r * G + h] * Uo;
+    } else {
+      V Qo = __shfl_down_sync(FULL, Qv, off, GP);
+      if (hl + off < G) { Uv = Uv + Qv * Uo; Qv = Qv * Qo; }
+    }
   }
   V f_in = __shfl_down_sync(FULL, Uv, 1, GP);
   if (hl + 1 >= G) f_in = V(0);
