@@ -324,6 +324,16 @@ void mibm_hit_bhat_(double* bhat, const int* dir);
 /* reference reseeds at restart, hit.f90:39-42; exact continuation needs    */
 /* the stream position).                                                    */
 void mibm_hit_rng_(unsigned long long* state, const int* dir);
+/* Bounds build (the library compiled with -DMIBM_BOUNDS, a debug build):    */
+/* kernels check cell, line, mesh and scatter indices against their arrays;  */
+/* an index out of range skips the access and is counted on the device (no  */
+/* trap).  mibm_bounds_check_: synchronises, returns the accesses skipped    */
+/* since the last call and resets the count (-1: not a bounds build).       */
+/* mibm_bounds_selftest_: one planted out-of-range index in a kernel of its */
+/* own, checked before the access: 0 when the check caught it, 1 when not, */
+/* -1 when not a bounds build.                                              */
+int  mibm_bounds_check_(void);
+int  mibm_bounds_selftest_(void);
 /* mibm_selftest_: checks the library's integer-pipe FP64<->FP32 conversions  */
 /* (used by the precision form) against the hardware conversions, bit for  */
 /* bit, on edge cases and 2^26 random patterns, and the line-solve factor   */

@@ -4,6 +4,10 @@ Each translation unit under csrc/ is compiled by its own nvcc process (in
 parallel) for ``-gencode arch=compute_103a,code=sm_103a`` and the objects are
 linked into ``melt_ibm_gb300/_build/libmibm.so``.  Rebuilds only when a
 source or header is newer than the library.
+
+``build(bounds=True)`` makes the bounds build, ``_build/libmibm_bounds.so``
+(``-DMIBM_BOUNDS``: kernels check their indices and count what they skip;
+``mibm_bounds_check_`` reports it), a debug library beside the normal one.
 """
 from __future__ import annotations
 
@@ -45,23 +49,29 @@ def sources() -> list[str]:
     return sorted(glob.glob(os.path.join(CSRC, "*.cu")))
 
 
-def _stale() -> bool:
-    if not os.path.exists(LIB):
+LIB_BOUNDS = os.path.join(OUT, "libmibm_bounds.so")
+
+
+def _stale(lib: str) -> bool:
+    if not os.path.exists(lib):
         return True
-    deps = sources() + glob.glob(os.path.join(CSRC, "*.cuh")) + [os.path.join(ROOT, "include", "mibm.h")]
-    lib_t = os.path.getmtime(LIB)
+    deps = sources() + glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h")) + \
+        [os.path.join(ROOT, "include", "mibm.h")]
+    lib_t = os.path.getmtime(lib)
     return any(os.path.getmtime(d) > lib_t for d in deps)
 
 
-def build(force: bool = False, verbose: bool = False, extra: list[str] | None = None) -> str:
-    if not force and not _stale():
-        return LIB
-    os.makedirs(OUT, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, extra: list[str] | None = None, bounds: bool = False) -> str:
+    lib = LIB_BOUNDS if bounds else LIB
+    if not force and not _stale(lib):
+        return lib
+    objdir = os.path.join(OUT, "bounds") if bounds else OUT
+    os.makedirs(objdir, exist_ok=True)
     nvcc = _nvcc()
-    extra = extra or []
+    extra = list(extra or []) + (["-DMIBM_BOUNDS"] if bounds else [])
 
     def compile_one(src: str) -> str:
-        obj = os.path.join(OUT, os.path.basename(src) + ".o")
+        obj = os.path.join(objdir, os.path.basename(src) + ".o")
         cmd = [nvcc, *ARCH, *FLAGS, *PER_FILE.get(os.path.basename(src), []), *extra, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -72,14 +82,14 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
 
     with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
         objs = list(ex.map(compile_one, sources()))
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [nvcc, *ARCH, "-shared", "--cudart", "static", "-o", tmp, *objs]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv, bounds="--bounds" in sys.argv))

@@ -245,7 +245,42 @@ class ProfScope {
 void prof_release(Ctx* c);
 void prof_flush_if_full(Ctx* c);
 
+// ---------------------------------------------------------------------
+// Bounds build (compiled with -DMIBM_BOUNDS): checked indices that fall
+// outside their array are counted in a device word of the translation unit
+// and the access is skipped or redirected to element 0 -- no trap, the
+// context stays usable.  mibm_bounds_check_() collects the counts of every
+// unit.  In the normal build the checks compile to nothing.
+// ---------------------------------------------------------------------
+#ifdef MIBM_BOUNDS
+static __device__ unsigned g_bounds_hits;
+__device__ __forceinline__ bool bounds_ok(size_t i, size_t n) {
+  if (i < n) return true;
+  atomicAdd(&g_bounds_hits, 1u);
+  return false;
+}
+void bounds_register(unsigned (*take)());
+namespace {
+unsigned bounds_take_unit() {
+  unsigned v = 0, z = 0;
+  if (cudaMemcpyFromSymbol(&v, g_bounds_hits, sizeof v) != cudaSuccess) return 0;
+  cudaMemcpyToSymbol(g_bounds_hits, &z, sizeof z);
+  return v;
+}
+struct BoundsUnit { BoundsUnit() { bounds_register(&bounds_take_unit); } };
+static BoundsUnit g_bounds_unit;
+}  // namespace
+#define MIBM_IDX_OK(i, n) ::mibm::bounds_ok((size_t)(i), (size_t)(n))
+#else
+#define MIBM_IDX_OK(i, n) true
+#endif
+
 inline __host__ __device__ size_t cidx(const Grid& g, int i, int j, int k) {
+#if defined(MIBM_BOUNDS) && defined(__CUDA_ARCH__)
+  // the whole allocation: pitch columns, rows, planes
+  if (!(bounds_ok((size_t)i, (size_t)g.P) & bounds_ok((size_t)j, (size_t)g.n2m) & bounds_ok((size_t)k, (size_t)g.n3m)))
+    return 0;
+#endif
   return (size_t)i + (size_t)g.P * ((size_t)j + (size_t)g.n2m * (size_t)k);
 }
 inline __host__ __device__ int wrap(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }

@@ -701,10 +701,11 @@ __global__ void __launch_bounds__(256) scatter_apply_kernel(int n, int nf, size_
     double sum = 0.0;
     for (int q = e0 + lane; q < e1 && key[q] == k; q += 32) {
       const int sr = src[q] - comp * per;
+      if (!MIBM_IDX_OK(sr, per)) continue;
       sum = fma(cf[sr / 27], phi[sr], sum);
     }
     for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(FULL, sum, off);
-    if (lane == 0) {
+    if (lane == 0 && MIBM_IDX_OK((size_t)k - (size_t)comp * cells, cells)) {
       const size_t cell = (size_t)k - (size_t)comp * cells;
       const double v = O.f[comp][cell] + sum;
       O.f[comp][cell] = v;
@@ -1653,6 +1654,7 @@ struct TagArgs {
 
 __device__ __forceinline__ void tri_verts(const TagArgs& T, int f, double V0[3], double V1[3], double V2[3]) {
   int a = T.vof[3 * f] - 1, b = T.vof[3 * f + 1] - 1, c = T.vof[3 * f + 2] - 1;
+  if (!(MIBM_IDX_OK(a, T.L.nv) & MIBM_IDX_OK(b, T.L.nv) & MIBM_IDX_OK(c, T.L.nv))) a = b = c = 0;
   for (int d = 0; d < 3; ++d) { V0[d] = T.x[3 * a + d]; V1[d] = T.x[3 * b + d]; V2[d] = T.x[3 * c + d]; }
 }
 

@@ -151,3 +151,52 @@ extern "C" int mibm_selftest_(void) {
   return (int)std::min<unsigned long long>(hbad[0] + hbad[1] + (unsigned long long)tbad + (unsigned long long)ebad,
                                            1000000);
 }
+
+// ---------------------------------------------------------------------
+// Bounds build: the registry of the translation units' hit counters and the
+// two entry points (include/mibm.h).  Every unit that includes common.cuh
+// registers its counter from a static constructor.
+// ---------------------------------------------------------------------
+namespace mibm {
+
+static std::vector<unsigned (*)()>& bounds_units() {
+  static std::vector<unsigned (*)()> units;
+  return units;
+}
+
+void bounds_register(unsigned (*take)()) { bounds_units().push_back(take); }
+
+#ifdef MIBM_BOUNDS
+// one checked access at index n of an array of n elements: the check skips
+// it and counts it
+__global__ void bounds_selftest_kernel(int* __restrict__ buf, int n) {
+  if (MIBM_IDX_OK(n, n)) buf[n] = 1;
+}
+#endif
+
+}  // namespace mibm
+
+extern "C" int mibm_bounds_check_(void) {
+#ifdef MIBM_BOUNDS
+  if (cudaDeviceSynchronize() != cudaSuccess) { cudaGetLastError(); return -2; }
+  unsigned long long hits = 0;
+  for (auto take : mibm::bounds_units()) hits += take();
+  return (int)std::min<unsigned long long>(hits, 1u << 30);
+#else
+  return -1;
+#endif
+}
+
+extern "C" int mibm_bounds_selftest_(void) {
+#ifdef MIBM_BOUNDS
+  int* d = nullptr;
+  if (cudaMalloc(&d, 4 * sizeof(int)) != cudaSuccess) { cudaGetLastError(); return -2; }
+  const int before = mibm_bounds_check_();
+  mibm::bounds_selftest_kernel<<<1, 1>>>(d, 4);
+  const int hits = mibm_bounds_check_();
+  cudaFree(d);
+  return (before == 0 && hits == 1) ? 0 : 1;
+#else
+  return -1;
+#endif
+}

@@ -139,6 +139,11 @@ __device__ __forceinline__ R add_forcing(R h, const double* __restrict__ vof, co
   const idx_t djm = (j == 0) ? (g.n2m - 1) * P : -P;                 \
   const idx_t dkp = (k + 1 == g.n3m) ? -(g.n3m - 1) * PL : PL;       \
   const idx_t dkm = (k == 0) ? (g.n3m - 1) * PL : -PL;               \
+  if (!(MIBM_IDX_OK(k, g.n3m) & MIBM_IDX_OK(c0 + dip, g.cells) &     \
+        MIBM_IDX_OK(c0 + dim, g.cells) & MIBM_IDX_OK(c0 + djp, g.cells) & \
+        MIBM_IDX_OK(c0 + djm, g.cells) & MIBM_IDX_OK(c0 + dkp, g.cells) & \
+        MIBM_IDX_OK(c0 + dkm, g.cells)))                              \
+    return;                                                          \
   (void)dip; (void)dim; (void)djp; (void)djm; (void)dkp; (void)dkm; (void)P;
 
 // ---------------------------------------------------------------------

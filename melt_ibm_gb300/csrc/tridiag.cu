@@ -625,8 +625,10 @@ __global__ void __launch_bounds__(256) solve_xc_kernel(Grid g, V* __restrict__ r
   const int f = line / per, l = line - f * per;
   const int j = l % g.n2m, k = l / g.n2m;
   V* row = act ? rhs + (size_t)f * g.cells + cidx(g, 0, j, k) + (size_t)hl * M : rhs;
+  // the bounds build: a row outside the field is neither read nor written
+  const bool inb = !act || MIBM_IDX_OK(cidx(g, 0, j, k) + (size_t)hl * M + M - 1, g.cells);
   V r[M];
-  if (act) load_chunk<V, M>(row, r);
+  if (act && inb) load_chunk<V, M>(row, r);
   else {
 #pragma unroll
     for (int i = 0; i < M; ++i) r[i] = V(0);
@@ -694,7 +696,7 @@ __global__ void __launch_bounds__(256) solve_xc_kernel(Grid g, V* __restrict__ r
     int t = i * G + h;
     r[i] = r[i] + X[6 * n + t] * al + X[5 * n + t] * be;
   }
-  if (act) store_chunk<V, M>(row, r);
+  if (act && inb) store_chunk<V, M>(row, r);
 }
 
 // y- and z-lines: block = 32 adjacent i (lanes) x G chunks (warps) of one
@@ -712,7 +714,7 @@ __global__ void __launch_bounds__(32 * col_max_chunks(M)) solve_cc_kernel(Grid g
   const int n = ZL ? g.n3m : g.n2m, G = n / M;
   const int lane = threadIdx.x, w = threadIdx.y;
   const int x = blockIdx.x * 32 + lane;
-  const bool act = x < g.n1m;
+  const bool act0 = x < g.n1m;
   // field of the launch (blockIdx.y runs over the planes of each field in turn)
   const int planes = ZL ? g.n2m : g.n3m;
   const int f = blockIdx.y / planes, pl = blockIdx.y - f * planes;
@@ -722,11 +724,14 @@ __global__ void __launch_bounds__(32 * col_max_chunks(M)) solve_cc_kernel(Grid g
   // first cell of this thread's chunk
   const int stride = ZL ? (int)g.plane : g.P;
   const int e0 = w * M;
-  const size_t first = (ZL ? cidx(g, act ? x : 0, pl, 0) : cidx(g, act ? x : 0, 0, pl)) +
+  const size_t first = (ZL ? cidx(g, act0 ? x : 0, pl, 0) : cidx(g, act0 ? x : 0, 0, pl)) +
                        (size_t)e0 * stride;
   V* __restrict__ rp = rhs + first;
   V r[M];
   double qv[ZL ? M : 1];
+  // the bounds build treats a line outside the field as inactive (loads
+  // and stores skipped; the thread still takes part in the barriers)
+  const bool act = act0 && MIBM_IDX_OK(first + (size_t)(M - 1) * stride, g.cells);
 #pragma unroll
   for (int i = 0; i < M; ++i) r[i] = act ? rp[i * stride] : V(0);
   if (ZL) {   // the field the increment is added to, fetched with the line (more loads in flight)
@@ -898,7 +903,9 @@ __global__ void __launch_bounds__(32 * col_max_chunks(M), 1) solve_cc_tma_kernel
     if (act) {
       const float al = y_in + S[4 + w] * xn, be = f_in + S[4 + G + w] * xn;
       const size_t first = (ZL ? cidx(g, x, pl, 0) : cidx(g, x, 0, pl)) + (size_t)e0 * stride;
-      if (ZL) {
+      if (!MIBM_IDX_OK(first + (size_t)(M - 1) * stride, g.cells)) {
+        // the bounds build skips the stores; the block still reaches the barrier below
+      } else if (ZL) {
         double* __restrict__ q = qs.p[f];
         float* __restrict__ mf = m32 ? m32 + (size_t)f * g.cells : nullptr;
         const double* Q = sQ(s);

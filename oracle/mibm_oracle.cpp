@@ -2225,6 +2225,8 @@ double mibm_timer_ms_(const int* a, const int* b) { return g_marks[*b] - g_marks
 void mibm_profile_(const int*) {}
 void mibm_set_precision_(const int*, const int*) {}
 void mibm_set_tma_(const int*) {}
+int mibm_bounds_check_(void) { return -1; }
+int mibm_bounds_selftest_(void) { return -1; }
 void mibm_set_graphs_(const int*) {}
 int mibm_autotune_(void) { return MIBM_OK; }
 int mibm_autotune_get_(int* out) { for (int q = 0; q < 4; ++q) out[q] = 0; return MIBM_OK; }

@@ -73,3 +73,11 @@ def test_singular_mls_is_reported(oracle_lib):
     oracle_lib.findcentroidindices_()
     oracle_lib.mlsweight_()
     assert oracle_lib.mibm_last_status_() == abi.MIBM_ENUMERIC
+
+
+def test_normal_builds_are_not_bounds_builds(mibm_lib, oracle_lib):
+    """The bounds entry points answer -1 outside the -DMIBM_BOUNDS build (no
+    device work), in both libraries."""
+    for lib in (mibm_lib, oracle_lib):
+        assert lib.mibm_bounds_check_() == -1
+        assert lib.mibm_bounds_selftest_() == -1
