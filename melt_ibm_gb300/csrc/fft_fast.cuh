@@ -131,6 +131,85 @@ __device__ __forceinline__ void run(C* buf, const C* tw) {
   }
 }
 
+// 16-point DFT in registers, x[k] := sum_n x[n] W16^{nk} (forward sign, or
+// the conjugate for INV), as 4 x 4: DFT4 over a of x[4a + b] for each b,
+// the twiddles W16^{bc}, DFT4 over b for each c (output k = c + 4d).  The
+// W16 powers are the table's entries W_N^{(N/16) m}.
+template <typename C, int N, bool INV>
+__device__ __forceinline__ void dft16(C (&x)[16], const C* tw) {
+  C z[4][4];
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    C v[4] = {x[b], x[4 + b], x[8 + b], x[12 + b]};
+    butterfly<C, 4, INV>(v);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) z[b][c] = v[c];
+  }
+#pragma unroll
+  for (int b = 1; b < 4; ++b)
+#pragma unroll
+    for (int c = 1; c < 4; ++c) {
+      C w = tw[(N / 16) * b * c];
+      if (INV) w.y = -w.y;
+      z[b][c] = cmul(z[b][c], w);
+    }
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    C v[4] = {z[0][c], z[1][c], z[2][c], z[3][c]};
+    butterfly<C, 4, INV>(v);
+#pragma unroll
+    for (int d = 0; d < 4; ++d) x[c + 4 * d] = v[d];
+  }
+}
+
+// The 256-point transform of L = 16 lines with 256 threads as 16 x 16
+// (n = 16 n1 + n2, k = k1 + 16 k2): pass 1, thread (line tid/16, n2 =
+// tid%16), the 16-point DFTs over n1 and the twiddles W256^{n2 k1}, written
+// to element 16 k1 + n2 (each thread reads and writes only the elements of
+// its own n2, so no barrier between); pass 2, thread (line tid%16, k1 =
+// tid/16), the 16-point DFTs over n2, written to element k1 + 16 k2 after a
+// barrier.  Two shared-memory round trips and three barriers instead of the
+// four and eight of the radix-4 stages; the lane order of each pass keeps
+// its 8-byte accesses free of bank conflicts with the padded layout
+// (element e of line l at e*(L+1) + l).
+template <typename C, int N, int L, int T, bool INV>
+__device__ __forceinline__ void run16x16(C* buf, const C* tw) {
+  static_assert(N == 256 && L == 16 && T == 256, "16 x 16 engine: 256 points, 16 lines, 256 threads");
+  constexpr int ES = L + 1;
+  C x[16];
+  {
+    const int l = threadIdx.x >> 4, n2 = threadIdx.x & 15;
+#pragma unroll
+    for (int n1 = 0; n1 < 16; ++n1) x[n1] = buf[(16 * n1 + n2) * ES + l];
+    dft16<C, N, INV>(x, tw);
+#pragma unroll
+    for (int k1 = 1; k1 < 16; ++k1) {
+      C w = tw[(n2 * k1) & (N - 1)];
+      if (INV) w.y = -w.y;
+      x[k1] = cmul(x[k1], w);
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < 16; ++k1) buf[(16 * k1 + n2) * ES + l] = x[k1];
+  }
+  __syncthreads();
+  const int l = threadIdx.x & 15, k1 = threadIdx.x >> 4;
+#pragma unroll
+  for (int n2 = 0; n2 < 16; ++n2) x[n2] = buf[(16 * k1 + n2) * ES + l];
+  dft16<C, N, INV>(x, tw);
+  __syncthreads();
+#pragma unroll
+  for (int k2 = 0; k2 < 16; ++k2) buf[(k1 + 16 * k2) * ES + l] = x[k2];
+  __syncthreads();
+}
+
+// the transform of the block's L lines in buf: the 16 x 16 engine where it
+// applies (FP32, 256 points, the 16-line tiles), else the radix-4/2/3 stages
+template <typename C, int N, int L, int T, bool INV>
+__device__ __forceinline__ void transform(C* buf, const C* tw) {
+  if constexpr (sizeof(C) == 8 && N == 256 && L == 16 && T == 256) run16x16<C, N, L, T, INV>(buf, tw);
+  else run<C, N, L, T, INV>(buf, tw);
+}
+
 template <typename C, int N, int T>
 __device__ __forceinline__ void stage_twiddles(C* s, const C* __restrict__ tw) {
   for (int m = threadIdx.x; m < N; m += T) s[m] = tw[m];
@@ -168,7 +247,7 @@ __global__ void __launch_bounds__(Shape<C, N>::T, Shape<C, N>::kMinBlocks) x_fwd
     if ((N * L) % T == 0 || t < N * L) buf[(t % N) * ES + t / N] = v[p];
   }
   __syncthreads();
-  run<C, N, L, T, false>(buf, tw);
+  transform<C, N, L, T, false>(buf, tw);
   const int H = g.H;
   for (int t = threadIdx.x; t < H * L; t += T) {
     const int l = t / H, kx = t - l * H;
@@ -224,7 +303,7 @@ __global__ void __launch_bounds__(Shape<C, N>::T, Shape<C, N>::kMinBlocks) x_inv
     if ((N * L) % T == 0 || t < N * L) buf[(t % N) * ES + t / N] = v[p];
   }
   __syncthreads();
-  run<C, N, L, T, true>(buf, tw);
+  transform<C, N, L, T, true>(buf, tw);
 #pragma unroll
   for (int p = 0; p < PER; ++p) {
     const int t = threadIdx.x + p * T;
@@ -285,7 +364,7 @@ y_pass(FftArgs<C> F, C* __restrict__ spec, int kx_base) {
   const size_t base = (size_t)kx0 + (size_t)g.HP * (size_t)g.n2m * k;
   load_cols<C, N, LONE>(buf, spec, base, (size_t)g.HP, nc);
   __syncthreads();
-  run<C, N, L, T, INV>(buf, tw);
+  transform<C, N, L, T, INV>(buf, tw);
   store_cols<C, N, LONE>(buf, spec, base, (size_t)g.HP, nc);
 }
 
@@ -307,7 +386,7 @@ z_solve(FftArgs<C> F, C* __restrict__ spec, int kx_base) {
   const size_t base = (size_t)kx0 + (size_t)g.HP * j;
   load_cols<C, N, LONE>(buf, spec, base, zstride, nc);
   __syncthreads();
-  run<C, N, L, T, false>(buf, tw);
+  transform<C, N, L, T, false>(buf, tw);
   const R* __restrict__ eig = F.eig + (size_t)g.H * j;
   const size_t eig_k = (size_t)g.H * g.n2m;
   for (int t = threadIdx.x; t < N * L; t += T) {
@@ -323,7 +402,7 @@ z_solve(FftArgs<C> F, C* __restrict__ spec, int kx_base) {
     buf[k * ES + l] = v;
   }
   __syncthreads();
-  run<C, N, L, T, true>(buf, tw);
+  transform<C, N, L, T, true>(buf, tw);
   store_cols<C, N, LONE>(buf, spec, base, zstride, nc);
 }
 
