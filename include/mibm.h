@@ -250,6 +250,11 @@ void mibm_set_precision_(const int* mode, const int* nproj);
 /* second path.  A staged copy that does not complete within about a second */
 /* is reported as MIBM_ETIMEOUT by the next cfl_.                           */
 void mibm_set_tma_(const int* on);
+/* mibm_set_fused_uvw_: the precision form's explicit terms and RHS of u, v, */
+/* w in one kernel that forms the advection products from the velocity     */
+/* mirrors itself (1, default), or through the products kernel as in the    */
+/* FP64 form (0).  Both give the same bits.                                  */
+void mibm_set_fused_uvw_(const int* on);
 /* Step graphs (no counterpart in the reference): from its second call on,  */
 /* tschem_ captures its device work into a CUDA graph and replays it while */
 /* nothing it reads by value from the host changes (flags, constants, the */

@@ -69,6 +69,7 @@ SIGNATURES: dict[str, tuple] = {
     "mibm_solxi_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_void_p]),
     "mibm_set_precision_": (None, [_I, _I]),
     "mibm_set_tma_": (None, [_I]),
+    "mibm_set_fused_uvw_": (None, [_I]),
     "mibm_bounds_check_": (C.c_int, []),
     "mibm_bounds_selftest_": (C.c_int, []),
     "mibm_set_graphs_": (None, [_I]),

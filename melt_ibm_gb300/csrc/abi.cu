@@ -772,6 +772,16 @@ void mibm_set_tma_(const int* on) {
   c->tma = *on;
 }
 
+// The precision form's u, v, w explicit terms in one kernel (1, default) or
+// through the advection products as in the FP64 form (0): the same bits;
+// the switch exists to compare the two.
+void mibm_set_fused_uvw_(const int* on) {
+  Ctx* c = current(); if (!ready(c)) return;
+  if (*on != 0 && *on != 1) { fail(c, MIBM_EINVAL, "set_fused_uvw: 0|1"); return; }
+  if (c->fused_uvw != *on) ++c->tune_gen;
+  c->fused_uvw = *on;
+}
+
 // Batched form (see Batch above).  ids: contexts after mibm_init_ (and the
 // initial tagging); returns a handle > 0, or 0 with the status in
 // mibm_last_status_.

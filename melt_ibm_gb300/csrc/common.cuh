@@ -199,6 +199,7 @@ struct Ctx {
   int tune_by = 8;                        // block height of the explicit-term kernel
   uint64_t tune_gen = 0;
   int tma = 1;                            // FP32 y/z line solves staged by bulk tensor copies
+  int fused_uvw = 1;                      // FP32 u, v, w explicit terms in one kernel from the mirrors
   double* step_host = nullptr;            // pinned: geometry scalars read back at step end
   // remeshing hand-off: the host's remesher and the hand-offs done
   mibm_remesh_fn remesh_fn = nullptr;

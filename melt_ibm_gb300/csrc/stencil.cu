@@ -382,6 +382,124 @@ fused_rhs_kernel(StencilArgs A, const StepParams* __restrict__ pp, R* __restrict
   ru[c0] = h;
 }
 
+// Precision form: the explicit terms and RHS of u, v and w in one pass over
+// the FP32 mirrors.  The advection products that adv_products_kernel writes
+// for the FP64 form (Pc, Qc, Rc, E, Fx, H at a cell and at its neighbours)
+// are formed here from the velocities by the same operations in the same
+// order -- the products rounded on their own (__fmul_rn), so that none is
+// fused into the difference that follows -- and the rest is h_prod's and
+// rhs_value's: the same bits as the products kernel followed by
+// fused_rhs_kernel<float, 0..2>, with about 100 instead of 180 bytes of
+// traffic per cell and one launch instead of four.
+__global__ void __launch_bounds__(256, 2)
+fused_uvw_f32_kernel(StencilArgs A, const StepParams* __restrict__ pp, float* __restrict__ ru3,
+                     float* __restrict__ rhs3) {
+  CELL_INDEX
+  const StepParams& p = *pp;
+  const float* __restrict__ u = A.u32;
+  const float* __restrict__ v = A.v32;
+  const float* __restrict__ w = A.w32;
+  const float* __restrict__ pr = A.p32;
+  const size_t n = g.cells;
+  // every value the cell needs, loaded before any is used: the loads are
+  // independent, so they are all in flight at once (the kernel is bound by
+  // their latency)
+  const double vfx = A.forcing ? A.vofx[c0] : 1.0, vfy = A.forcing ? A.vofy[c0] : 1.0;
+  const double vfz = A.forcing ? A.vofz[c0] : 1.0;
+  const double fcx = A.forcing ? A.forcx[c0] : 0.0, fcy = A.forcing ? A.forcy[c0] : 0.0;
+  const double fcz = A.forcing ? A.forcz[c0] : 0.0;
+  const float ru0 = ru3[c0], ru1 = ru3[n + c0], ru2 = ru3[2 * n + c0];
+  const float uc = u[c0], uip = u[c0 + dip], um = u[c0 + dim], ujp = u[c0 + djp], ujm = u[c0 + djm];
+  const float ukp = u[c0 + dkp], ukm = u[c0 + dkm], uipjm = u[c0 + dip + djm], uipkm = u[c0 + dip + dkm];
+  const float vc = v[c0], vip = v[c0 + dip], vim = v[c0 + dim], vjp = v[c0 + djp], vm = v[c0 + djm];
+  const float vkp = v[c0 + dkp], vkm = v[c0 + dkm], vjpim = v[c0 + djp + dim], vjpkm = v[c0 + djp + dkm];
+  const float wc = w[c0], wip = w[c0 + dip], wim = w[c0 + dim], wjp = w[c0 + djp], wjm = w[c0 + djm];
+  const float wkp = w[c0 + dkp], wm = w[c0 + dkm], wkpim = w[c0 + dkp + dim], wkpjm = w[c0 + dkp + djm];
+  const float pc = pr[c0], pim = pr[c0 + dim], pjm = pr[c0 + djm], pkm = pr[c0 + dkm];
+  const float tc = p.betagz != 0.0 ? A.t32[c0] : 0.f, tkm = p.betagz != 0.0 ? A.t32[c0 + dkm] : 0.f;
+  // products at c0
+  const float Pc0 = __fmul_rn(uip + uc, uip + uc);
+  const float Qc0 = __fmul_rn(vjp + vc, vjp + vc);
+  const float Rc0 = __fmul_rn(wkp + wc, wkp + wc);
+  const float E0 = __fmul_rn(vc + vim, uc + ujm);
+  const float F0 = __fmul_rn(wc + wim, uc + ukm);
+  const float H0 = __fmul_rn(wc + wjm, vc + vkm);
+  // products at the neighbours the differences need (each the product of
+  // the cell it belongs to: Pc(c) = (u[c+i] + u[c])^2, E(c) = (v[c] +
+  // v[c-i]) (u[c] + u[c-j]), Fx(c) = (w[c] + w[c-i]) (u[c] + u[c-k]),
+  // H(c) = (w[c] + w[c-j]) (v[c] + v[c-k]))
+  const float Pcm = __fmul_rn(uc + um, uc + um);
+  const float Qcm = __fmul_rn(vc + vm, vc + vm);
+  const float Rcm = __fmul_rn(wc + wm, wc + wm);
+  const float Ejp = __fmul_rn(vjp + vjpim, ujp + uc);
+  const float Eip = __fmul_rn(vip + vc, uip + uipjm);
+  const float Fkp = __fmul_rn(wkp + wkpim, ukp + uc);
+  const float Fip = __fmul_rn(wip + wc, uip + uipkm);
+  const float Hkp = __fmul_rn(wkp + wkpjm, vkp + vc);
+  const float Hjp = __fmul_rn(wjp + wc, vjp + vjpkm);
+  const float udx1 = p.cf[kQ1], udx2 = p.cf[kQ2], udx3 = p.cf[kQ3];
+  // h_prod's expressions, add_forcing's forcing term
+  auto forced = [&](float h, double vf, double fc, float rlen) {
+    if (!A.forcing) return h;
+    return (vof_is_one(vf) ? d2f_bits(fc) : d2f_bits(vf * fc)) * rlen + h;
+  };
+  float hu = -(udx1 * (Pc0 - Pcm) + udx2 * (Ejp - E0) + udx3 * (Fkp - F0));
+  hu = forced(hu, vfx, fcx, p.cf[kRXLEN]);
+  float hv = -(udx1 * (Eip - E0) + udx2 * (Qc0 - Qcm) + udx3 * (Hkp - H0));
+  hv = forced(hv, vfy, fcy, p.cf[kRYLEN]);
+  float hw = -(udx1 * (Fip - F0) + udx2 * (Hjp - H0) + udx3 * (Rc0 - Rcm));
+  if (p.betagz != 0.0) {
+    const float T_interp = (tc + tkm) * 0.5f;
+    hw = hw + p.cf[kBETAGZ] * (T_interp - p.cf[kTLIQ]);
+  }
+  hw = forced(hw, vfz, fcz, p.cf[kRZLEN]);
+  // rhs_value's expressions (lap_dt, pressure gradient, RK combination)
+  const float gdt = p.cf[kGDT], rdt = p.cf[kRDT];
+  const float L1 = p.cf[kLV1], L2 = p.cf[kLV2], L3 = p.cf[kLV3], LC = p.cf[kLVC];
+  const float du = (L1 * (uip + um) + L2 * (ujp + ujm) + L3 * (ukp + ukm)) - LC * uc;
+  const float dv = (L1 * (vip + vim) + L2 * (vjp + vm) + L3 * (vkp + vkm)) - LC * vc;
+  const float dw = (L1 * (wip + wim) + L2 * (wjp + wjm) + L3 * (wkp + wm)) - LC * wc;
+  rhs3[c0] = gdt * hu + (rdt * ru0 + (du - p.cf[kPD1] * (pc - pim)));
+  rhs3[n + c0] = gdt * hv + (rdt * ru1 + (dv - p.cf[kPD2] * (pc - pjm)));
+  rhs3[2 * n + c0] = gdt * hw + (rdt * ru2 + (dw - p.cf[kPD3] * (pc - pkm)));
+  ru3[c0] = hu;
+  ru3[n + c0] = hv;
+  ru3[2 * n + c0] = hw;
+}
+
+// Precision form: the temperature's explicit term and RHS (hdnlte + invtrte)
+// as fused_rhs_kernel<float, 3> computes them, with every value of a fluid
+// cell loaded before any is used (the kernel is bound by load latency); a
+// cell that is not fully fluid takes h_t's solid-advection branch.  The
+// same bits as fused_rhs_kernel<float, 3>.
+__global__ void __launch_bounds__(256, 3)
+fused_t_f32_kernel(StencilArgs A, const StepParams* __restrict__ pp, float* __restrict__ ru,
+                   float* __restrict__ rhs) {
+  CELL_INDEX
+  const StepParams& p = *pp;
+  const float* __restrict__ T = A.t32;
+  const double vpd = A.vofp[c0];
+  const float ruc = ru[c0];
+  const float tc = T[c0], tip = T[c0 + dip], tim = T[c0 + dim], tjp = T[c0 + djp], tjm = T[c0 + djm];
+  const float tkp = T[c0 + dkp], tkm = T[c0 + dkm];
+  const float uip = A.u32[c0 + dip], uc = A.u32[c0], vjp = A.v32[c0 + djp], vc = A.v32[c0];
+  const float wkp = A.w32[c0 + dkp], wc = A.w32[c0];
+  float h;
+  if (vof_is_one(vpd)) {
+    const float udx1 = p.cf[kH1], udx2 = p.cf[kH2], udx3 = p.cf[kH3];
+    const float x31 = uip * (tip + tc) - uc * (tc + tim);
+    const float x32 = vjp * (tjp + tc) - vc * (tc + tjm);
+    const float x33 = wkp * (tkp + tc) - wc * (tc + tkm);
+    const float hs = udx1 * x31 + udx2 * x32 + udx3 * x33;
+    h = -hs;
+  } else {
+    h = h_t<float>(A, i, j, k, c0, dip, dim, djp, djm, dkp, dkm, p);
+  }
+  const float d = (p.cf[kLT1] * (tip + tim) + p.cf[kLT2] * (tjp + tjm) + p.cf[kLT3] * (tkp + tkm)) - p.cf[kLTC] * tc;
+  rhs[c0] = p.cf[kGDT] * h + (p.cf[kRDT] * ruc + d);
+  ru[c0] = h;
+}
+
 template <typename R>
 static void fused_rhs_launch(Ctx* c, const StepParams* dp, int w, R* ru, R* rhs) {
   const int by = (c->tune_by == 2 || c->tune_by == 4) ? c->tune_by : 8;   // autotuned block height
@@ -393,6 +511,18 @@ static void fused_rhs_launch(Ctx* c, const StepParams* dp, int w, R* ru, R* rhs)
     case 2: fused_rhs_kernel<R, 2><<<grid, block, 0, c->stream>>>(a, dp, ru, rhs); break;
     default: fused_rhs_kernel<R, 3><<<grid, block, 0, c->stream>>>(a, dp, ru, rhs); break;
   }
+}
+
+static void fused_uvw_launch(Ctx* c, const StepParams* dp, float* ru4, float* rhs4) {
+  const int by = (c->tune_by == 2 || c->tune_by == 4) ? c->tune_by : 8;   // autotuned block height
+  dim3 grid(div_up(c->g.n1m, 32), div_up(c->g.n2m, by), c->g.n3m), block(32, by);
+  fused_uvw_f32_kernel<<<grid, block, 0, c->stream>>>(make_args(c), dp, ru4, rhs4);
+}
+
+static void fused_t_launch(Ctx* c, const StepParams* dp, float* ru, float* rhs) {
+  const int by = (c->tune_by == 2 || c->tune_by == 4) ? c->tune_by : 8;   // autotuned block height
+  dim3 grid(div_up(c->g.n1m, 32), div_up(c->g.n2m, by), c->g.n3m), block(32, by);
+  fused_t_f32_kernel<<<grid, block, 0, c->stream>>>(make_args(c), dp, ru, rhs);
 }
 
 // ---------------------------------------------------------------------
@@ -707,8 +837,9 @@ void k_fused_rhs(Ctx* c, const StepParams* dp) {
   MIBM_LAUNCH_CHECK(c, "fused_rhs");
 }
 
-// Autotuner support: time the explicit-term kernel (components u and T) with
-// block height `by`, best of `reps` runs after one warm-up, in ms.  The RK
+// Autotuner support: time the explicit-term kernel (components u and T; in
+// the precision form u, v, w and T) with block height `by`, best of `reps`
+// runs after one warm-up, in ms.  The RK
 // history it overwrites is saved first and restored, so the context's state
 // is unchanged.  ru4/rhs4: the form's history and RHS buffers.
 template <typename R>
@@ -723,11 +854,22 @@ static float time_fused_by(Ctx* c, const StepParams* dp, int by, int reps, R* ru
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
+  const bool uvw = sizeof(R) == 4 && c->fused_uvw;
   if (sizeof(R) == 8) adv_products_launch<double>(c, c->prod);   // read by the u component
-  else adv_products_launch<float>(c, c->prod32);
+  else if (!uvw) adv_products_launch<float>(c, c->prod32);
   auto run = [&]() {
-    fused_rhs_launch<R>(c, dp, 0, ru_fields[0], rhs4);
-    fused_rhs_launch<R>(c, dp, 3, ru_fields[3], rhs4 + 3 * n);
+    if constexpr (sizeof(R) == 4) {
+      if (uvw) {
+        fused_uvw_launch(c, dp, ru_fields[0], rhs4);
+        fused_t_launch(c, dp, ru_fields[3], rhs4 + 3 * n);
+      } else {
+        fused_rhs_launch<R>(c, dp, 0, ru_fields[0], rhs4);
+        fused_rhs_launch<R>(c, dp, 3, ru_fields[3], rhs4 + 3 * n);
+      }
+    } else {
+      fused_rhs_launch<R>(c, dp, 0, ru_fields[0], rhs4);
+      fused_rhs_launch<R>(c, dp, 3, ru_fields[3], rhs4 + 3 * n);
+    }
   };
   float best = -1.f;
   run();
@@ -763,13 +905,25 @@ float stencil_time_by(Ctx* c, const StepParams* dp, int by, int reps) {
 }
 
 // precision form: FP32 explicit terms and RHS into FP32 ru / rhs buffers
+// the precision form's explicit terms: u, v, w in one kernel (or, with the
+// one-pass kernel switched off, through the products as in the FP64 form),
+// then T
 void k_fused_rhs_f32(Ctx* c, const StepParams* dp, float* ru4, float* rhs4) {
-  adv_products_launch<float>(c, c->prod32);
-  for (int w = 0; w < 4; ++w) {
-    { MIBM_PROF(c, "fused_rhs_f32");
-      fused_rhs_launch<float>(c, dp, w, ru4 + (size_t)w * c->g.cells, rhs4 + (size_t)w * c->g.cells); }
+  if (c->fused_uvw) {
+    { MIBM_PROF(c, "fused_uvw_f32"); fused_uvw_launch(c, dp, ru4, rhs4); }
     ++c->launches;
+  } else {
+    adv_products_launch<float>(c, c->prod32);
+    for (int w = 0; w < 3; ++w) {
+      { MIBM_PROF(c, "fused_rhs_f32");
+        fused_rhs_launch<float>(c, dp, w, ru4 + (size_t)w * c->g.cells, rhs4 + (size_t)w * c->g.cells); }
+      ++c->launches;
+    }
   }
+  { MIBM_PROF(c, "fused_rhs_f32");
+    if (c->fused_uvw) fused_t_launch(c, dp, ru4 + 3 * c->g.cells, rhs4 + 3 * c->g.cells);
+    else fused_rhs_launch<float>(c, dp, 3, ru4 + 3 * c->g.cells, rhs4 + 3 * c->g.cells); }
+  ++c->launches;
   MIBM_LAUNCH_CHECK(c, "fused_rhs_f32");
 }
 

@@ -2225,6 +2225,7 @@ double mibm_timer_ms_(const int* a, const int* b) { return g_marks[*b] - g_marks
 void mibm_profile_(const int*) {}
 void mibm_set_precision_(const int*, const int*) {}
 void mibm_set_tma_(const int*) {}
+void mibm_set_fused_uvw_(const int*) {}
 int mibm_bounds_check_(void) { return -1; }
 int mibm_bounds_selftest_(void) { return -1; }
 void mibm_set_graphs_(const int*) {}
