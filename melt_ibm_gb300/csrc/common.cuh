@@ -48,6 +48,7 @@ enum Coef {
   kPD1, kPD2, kPD3,       // dt*kPX1, dt*kPX2, dt*kPX3
   kRXLEN, kRYLEN, kRZLEN, // 1/xlen, 1/ylen, 1/zlen           (hdnl1-3 forcing term)
   kPB1, kPB2, kPB3, kPBC, // al*beta*dxq per direction, 1 + 2*(kPB1+kPB2+kPB3)  (prcalc)
+  kDVI,                   // dx1/(dt*al)                     (precision-form divg, equal spacings)
   kNCoef
 };
 

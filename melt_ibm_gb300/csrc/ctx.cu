@@ -90,6 +90,7 @@ StepParams host_params(Ctx* c) {
   q[kRXLEN] = 1.0 / g.xlen; q[kRYLEN] = 1.0 / g.ylen; q[kRZLEN] = 1.0 / g.zlen;
   q[kPB1] = q[kBE] * g.dx1q; q[kPB2] = q[kBE] * g.dx2q; q[kPB3] = q[kBE] * g.dx3q;
   q[kPBC] = 1.0 + 2.0 * (q[kPB1] + q[kPB2] + q[kPB3]);
+  q[kDVI] = g.dx1 * q[kUSDTAL];
   for (int i = 0; i < kNCoef; ++i) p.cf[i] = (float)q[i];
   return p;
 }

@@ -538,12 +538,20 @@ __global__ void divg_kernel(StencilArgs A, const StepParams* __restrict__ pp, do
 
 // precision form: the divergence residual of the FP64 velocity, formed in
 // FP64 (the face differences cancel to round-off of u), then rounded once to
-// FP32 as the right-hand side of the FP32 Poisson solve
+// FP32 as the right-hand side of the FP32 Poisson solve.  ISO (equal grid
+// spacings in the three directions): the sum of the differences in FP64 and
+// the spacing folded into the FP32 factor, five FP64 operations per cell
+// instead of six (the kernel is bound by FP64 issue).
+template <bool ISO>
 __global__ void divg_f32_kernel(StencilArgs A, const StepParams* __restrict__ pp, float* __restrict__ res) {
   CELL_INDEX
   double du = A.vx[c0 + dip] - A.vx[c0], dv = A.vy[c0 + djp] - A.vy[c0], dw = A.vz[c0 + dkp] - A.vz[c0];
-  double dq = fma(dw, g.dx3, fma(dv, g.dx2, du * g.dx1));
-  res[c0] = d2f_bits(dq) * pp->cf[kUSDTAL];
+  if constexpr (ISO) {
+    res[c0] = d2f_bits((du + dv) + dw) * pp->cf[kDVI];
+  } else {
+    double dq = fma(dw, g.dx3, fma(dv, g.dx2, du * g.dx1));
+    res[c0] = d2f_bits(dq) * pp->cf[kUSDTAL];
+  }
 }
 
 // mean3 (fused step only): the mean IBM force of velforce.f90:21-50, removed
@@ -959,7 +967,11 @@ void k_prcalc_f32(Ctx* c, const StepParams* dp, const float* phi, bool mirror) {
 }
 
 void k_divg_f32(Ctx* c, const StepParams* dp, float* res) {
-  { MIBM_PROF(c, "divg_f32"); divg_f32_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, res); }
+  { MIBM_PROF(c, "divg_f32");
+    if (c->g.dx1 == c->g.dx2 && c->g.dx1 == c->g.dx3)
+      divg_f32_kernel<true><<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, res);
+    else
+      divg_f32_kernel<false><<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, res); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "divg_f32");
 }
