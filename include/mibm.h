@@ -250,10 +250,12 @@ void mibm_set_precision_(const int* mode, const int* nproj);
 /* second path.  A staged copy that does not complete within about a second */
 /* is reported as MIBM_ETIMEOUT by the next cfl_.                           */
 void mibm_set_tma_(const int* on);
-/* mibm_set_fused_uvw_: the precision form's explicit terms and RHS of u, v, */
-/* w in one kernel that forms the advection products from the velocity     */
-/* mirrors itself (1, default), or through the products kernel as in the    */
-/* FP64 form (0).  Both give the same bits.                                  */
+/* mibm_set_fused_uvw_: the precision form's one-pass kernels (1, default): */
+/* the explicit terms and RHS of u, v, w in one kernel that forms the       */
+/* advection products from the velocity mirrors itself, and the velocity   */
+/* and pressure updates of each projection in one kernel; 0: the products  */
+/* kernel, one RHS kernel per component and separate updates, as in the    */
+/* FP64 form.  Both give the same bits.                                     */
 void mibm_set_fused_uvw_(const int* on);
 /* Step graphs (no counterpart in the reference): from its second call on,  */
 /* tschem_ captures its device work into a CUDA graph and replays it while */

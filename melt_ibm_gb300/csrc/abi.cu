@@ -193,8 +193,12 @@ static void step_enqueue_f32(Ctx* c) {
       bool last = it + 1 == c->nproj;
       k_divg_f32(c, dp, c->res32);                     // FP64 residual, rounded once
       k_phcalc_f32(c, c->res32, c->phi32);             // FP32 Poisson solve
-      k_updvp_f32(c, dp, c->phi32, it == 0 ? mean3 : nullptr, last);
-      k_prcalc_f32(c, dp, c->phi32, last);
+      if (c->fused_uvw) {
+        k_updvp_prcalc_f32(c, dp, c->phi32, it == 0 ? mean3 : nullptr, last);
+      } else {
+        k_updvp_f32(c, dp, c->phi32, it == 0 ? mean3 : nullptr, last);
+        k_prcalc_f32(c, dp, c->phi32, last);
+      }
     }
     if (c->status != MIBM_OK) return;
   }
@@ -772,9 +776,10 @@ void mibm_set_tma_(const int* on) {
   c->tma = *on;
 }
 
-// The precision form's u, v, w explicit terms in one kernel (1, default) or
-// through the advection products as in the FP64 form (0): the same bits;
-// the switch exists to compare the two.
+// The precision form's one-pass kernels (u, v, w explicit terms in one
+// kernel, velocity and pressure updates in one kernel; 1, default) or the
+// products path and separate updates as in the FP64 form (0): the same
+// bits; the switch exists to compare the two.
 void mibm_set_fused_uvw_(const int* on) {
   Ctx* c = current(); if (!ready(c)) return;
   if (*on != 0 && *on != 1) { fail(c, MIBM_EINVAL, "set_fused_uvw: 0|1"); return; }

@@ -200,7 +200,7 @@ struct Ctx {
   int tune_by = 8;                        // block height of the explicit-term kernel
   uint64_t tune_gen = 0;
   int tma = 1;                            // FP32 y/z line solves staged by bulk tensor copies
-  int fused_uvw = 1;                      // FP32 u, v, w explicit terms in one kernel from the mirrors
+  int fused_uvw = 1;                      // FP32 one-pass kernels (u, v, w explicit terms; projection update)
   double* step_host = nullptr;            // pinned: geometry scalars read back at step end
   // remeshing hand-off: the host's remesher and the hand-offs done
   mibm_remesh_fn remesh_fn = nullptr;
@@ -336,6 +336,7 @@ void k_fused_rhs_f32(Ctx* c, const StepParams* dp, float* ru4, float* rhs4);
 void k_updvp_f32(Ctx* c, const StepParams* dp, const float* phi, const double* mean3, bool mirror);
 void k_prcalc_f32(Ctx* c, const StepParams* dp, const float* phi, bool mirror);
 void k_divg_f32(Ctx* c, const StepParams* dp, float* res);
+void k_updvp_prcalc_f32(Ctx* c, const StepParams* dp, const float* phi, const double* mean3, bool mirror);
 void k_mirror_fields(Ctx* c);
 // HIT forcing (hit.cu)
 void k_hit_random_force(Ctx* c);

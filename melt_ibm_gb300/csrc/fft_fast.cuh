@@ -52,7 +52,11 @@ struct Shape {
   static constexpr int Lw = (kWork / N) < kMinL ? kMinL : ((kWork / N) > 32 ? 32 : kWork / N);
   static constexpr int L = LONE ? 1 : pow2_floor(Lw);
   static constexpr int T = LONE ? 64 : 256;
-  static constexpr int kMinBlocks = LONE ? 8 : 3;   // resident blocks per SM asked of ptxas
+  // resident blocks per SM asked of ptxas: four for the 256-point FP32 x and
+  // z passes (latency-bound; measured faster, though the z pass spills a
+  // little), three elsewhere (the y pass at four spills more and runs slower)
+  static constexpr int kMinBlocks = LONE ? 8 : (sizeof(C) == 8 && N == 256 ? 4 : 3);
+  static constexpr int kMinBlocksY = LONE ? 8 : 3;
   static constexpr int ES = L + 1;
   static constexpr size_t smem = sizeof(C) * ((size_t)N + (size_t)N * ES);
 };
@@ -350,7 +354,7 @@ __device__ __forceinline__ void store_cols(const C* buf, C* __restrict__ spec, s
 
 // Y pass (forward or inverse) on L kx columns from kx_base + L*blockIdx.x of plane k
 template <typename C, int N, bool INV, int LONE = 0>
-__global__ void __launch_bounds__(Shape<C, N, LONE>::T, Shape<C, N, LONE>::kMinBlocks)
+__global__ void __launch_bounds__(Shape<C, N, LONE>::T, Shape<C, N, LONE>::kMinBlocksY)
 y_pass(FftArgs<C> F, C* __restrict__ spec, int kx_base) {
   typedef Shape<C, N, LONE> Sh;
   constexpr int L = Sh::L, T = Sh::T;

@@ -602,6 +602,37 @@ __global__ void prcalc_f32_kernel(StencilArgs A, const StepParams* __restrict__ 
   if (m32) m32[c0] = d2f_bits(q);
 }
 
+// precision form: updvp_f32_kernel and prcalc_f32_kernel in one pass (they
+// read the same phi), every load issued before the first use; the same
+// expressions, so the same bits.  m32: the mirrors' base (u, v, w at 0,
+// cells, 2 cells; p at 4 cells), or null
+__global__ void updvp_prcalc_f32_kernel(StencilArgs A, const StepParams* __restrict__ pp,
+                                        const float* __restrict__ phi, double* __restrict__ vx,
+                                        double* __restrict__ vy, double* __restrict__ vz,
+                                        double* __restrict__ pr, const float* __restrict__ mean3f,
+                                        float* __restrict__ m32) {
+  CELL_INDEX
+  const float loc = phi[c0], fim = phi[c0 + dim], fjm = phi[c0 + djm], fkm = phi[c0 + dkm];
+  const float fip = phi[c0 + dip], fjp = phi[c0 + djp], fkp = phi[c0 + dkp];
+  const double u0 = vx[c0], v0 = vy[c0], w0 = vz[c0], p0 = pr[c0];
+  float ix = (loc - fim) * pp->cf[kUP1];
+  float iy = (loc - fjm) * pp->cf[kUP2];
+  float iz = (loc - fkm) * pp->cf[kUP3];
+  if (mean3f) { ix += mean3f[0]; iy += mean3f[1]; iz += mean3f[2]; }
+  const double x = u0 - f2d_bits(ix), y = v0 - f2d_bits(iy), z = w0 - f2d_bits(iz);
+  vx[c0] = x; vy[c0] = y; vz[c0] = z;
+  const float be = pp->cf[kBE];
+  const float inc = loc - be * ((fip - 2.0f * loc + fim) * pp->cf[kDQ1] +
+                                (fjp - 2.0f * loc + fjm) * pp->cf[kDQ2] +
+                                (fkp - 2.0f * loc + fkm) * pp->cf[kDQ3]);
+  const double q = p0 + f2d_bits(inc);
+  pr[c0] = q;
+  if (m32) {
+    m32[c0] = d2f_bits(x); m32[c0 + g.cells] = d2f_bits(y); m32[c0 + 2 * g.cells] = d2f_bits(z);
+    m32[c0 + 4 * g.cells] = d2f_bits(q);
+  }
+}
+
 // FP32 mirrors of u, v, w, T, p (field f at m32 + f*cells)
 __global__ void mirror_kernel(size_t n, const double* __restrict__ u, const double* __restrict__ v,
                               const double* __restrict__ w, const double* __restrict__ t,
@@ -956,6 +987,16 @@ void k_updvp_f32(Ctx* c, const StepParams* dp, const float* phi, const double* m
                                                                      mirror ? c->q32 : nullptr); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "updvp_f32");
+}
+
+void k_updvp_prcalc_f32(Ctx* c, const StepParams* dp, const float* phi, const double* mean3, bool mirror) {
+  { MIBM_PROF(c, "updvp_prcalc_f32");
+    const float* mean3f = mean3 ? reinterpret_cast<const float*>(mean3 + 4) : nullptr;
+    updvp_prcalc_f32_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(
+        make_args(c), dp, phi, c->df[MIBM_F_VX], c->df[MIBM_F_VY], c->df[MIBM_F_VZ], c->df[MIBM_F_PR], mean3f,
+        mirror ? c->q32 : nullptr); }
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "updvp_prcalc_f32");
 }
 
 void k_prcalc_f32(Ctx* c, const StepParams* dp, const float* phi, bool mirror) {
