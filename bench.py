@@ -694,22 +694,25 @@ def batched_measurement(lib, steps: int, warmup: int, seed: int = 100) -> dict:
             "timing": "host wall clock around batch steps (each ends synchronised)"}
 
 
-def serving_measurement(lib, seconds: float, steps: int, budget_gb: float, seed: int = 7) -> dict:
+def serving_measurement(lib, seconds: float, steps: int, budget_gb: float, seed: int = 7,
+                        step_cells: int | None = 8 << 20) -> dict:
     """Serving form: Poisson arrivals at 2 cases/s for `seconds`, grids
     {64, 96, 128, 192}^3 with probabilities {0.4, 0.3, 0.2, 0.1}, the batched
     configuration's parameter laws, `steps` steps per case in the precision
-    form, admission against an HBM budget of `budget_gb` GB; the run lasts
-    until every request has completed."""
+    form, admission against an HBM budget of `budget_gb` GB, a work budget
+    of `step_cells` cells per batch step (the cases that waited longest,
+    at least one); the run lasts until every request has completed."""
     from melt_ibm_gb300.serve import DeviceExecutor, Server, serving_requests
     reqs = serving_requests(seconds, rate=2.0, seed=seed, steps=steps)
     ex = DeviceExecutor(lib)
     try:
-        stats = Server(ex, int(budget_gb * 1e9), prepare_workers=4).run(reqs)
+        stats = Server(ex, int(budget_gb * 1e9), prepare_workers=4, step_cells=step_cells).run(reqs)
     finally:
         ex.close()
     out = stats.summary()
     out.update({"requests": len(reqs), "arrival_window_s": seconds, "rate_per_s": 2.0, "steps_per_case": steps,
-                "hbm_budget_gb": budget_gb, "seed": seed, "form": "precision (f32 compute, f64 fields)",
+                "hbm_budget_gb": budget_gb, "step_cells_budget": step_cells, "seed": seed,
+                "form": "precision (f32 compute, f64 fields)",
                 "unit_cell_steps": "cell-steps/s over the whole run (first arrival to last completion)"})
     return out
 

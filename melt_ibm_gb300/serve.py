@@ -9,12 +9,17 @@ arrive over time.  The server
   footprint fits the HBM budget (a request that does not fit blocks those
   behind it, so none is starved), attaching each as its own context whose
   fields and mesh stay resident on the device until the case completes;
-* advances every resident case by one time step per loop iteration through
+* advances the resident cases by one time step per loop iteration through
   one persistent batch (`mibm_batch_step_`), whose members change as cases
   join or leave (`mibm_batch_add_` / `mibm_batch_remove_`); each case's own
   step graph is launched on its own stream, so a membership change rebuilds
   nothing -- new work joins the running mix at the next step, finished
   cases free their memory at once;
+* with a work budget per batch step (``step_cells``), advances in each
+  iteration the resident cases that have waited longest, as many as fit
+  the budget in cells (at least one): the latency of a batch step then
+  follows the budget rather than how much work happens to be resident,
+  while every case still gets its steps in order and the GPU stays busy;
 * records the latency of every batch step (and which steps carried an
   admission: a case's first two steps run its direct launches and its graph
   capture) and the completion time of every case (completion - arrival:
@@ -83,7 +88,7 @@ class ServeStats:
     step_ms: list = field(default_factory=list)        # latency of every batch step
     admission: list = field(default_factory=list)      # the step carried an admission (first two steps of a case)
     active: list = field(default_factory=list)         # cases in each batch step
-    resident_cells: list = field(default_factory=list)  # cells of the resident cases in each batch step
+    stepped_cells: list = field(default_factory=list)   # cells advanced by each batch step
     cell_steps: float = 0.0
     finished: list = field(default_factory=list)
     admitted: int = 0
@@ -96,10 +101,10 @@ class ServeStats:
         st = np.array(self.step_ms) if self.step_ms else np.zeros(1)
         adm = np.array(self.admission, dtype=bool) if self.admission else np.zeros(len(st), dtype=bool)
         steady = st[~adm] if (~adm).any() else st
-        # latency per resident Mcell: the step of a mix of grids 64^3..256^3
+        # latency per Mcell advanced: the step of a mix of grids 64^3..256^3
         # lasts as long as its work, so p99/p50 of the raw latency measures
         # the mix; this ratio measures the jitter at a given load
-        cells = np.array(self.resident_cells, dtype=float) if len(self.resident_cells) == len(st) else None
+        cells = np.array(self.stepped_cells, dtype=float) if len(self.stepped_cells) == len(st) else None
         if cells is not None and (cells > 0).all():
             per = st / (cells / 1e6)
             per_steady = per[~adm] if (~adm).any() else per
@@ -122,7 +127,7 @@ class ServeStats:
             "step_latency_ms_outside_admission": {"p50": float(np.percentile(steady, 50)),
                                                   "p99": float(np.percentile(steady, 99)),
                                                   "max": float(steady.max())},
-            "step_latency_us_per_resident_mcell_outside_admission": {
+            "step_latency_us_per_mcell_outside_admission": {
                 "p50": float(np.percentile(per_steady, 50)), "p99": float(np.percentile(per_steady, 99))},
             "case_completion_s": {"p50": float(np.percentile(ct, 50)), "p99": float(np.percentile(ct, 99))},
             "admission_wait_s": {"p50": float(np.percentile(qt, 50)), "p99": float(np.percentile(qt, 99))},
@@ -186,6 +191,7 @@ class DeviceExecutor:
         self.capacity = device_capacity
         self.bytes: dict[int, int] = {}
         self.age: dict[int, int] = {}
+        self.members: set[int] = set()          # cases in the batch now
         self.measured: dict[tuple, int] = {}    # device bytes per (n, precision), measured at first admission
 
     @staticmethod
@@ -238,6 +244,7 @@ class DeviceExecutor:
         if self.lib.mibm_batch_add_(abi.ref_int(self.batch), abi.ref_int(case.ctx[self.lib.path])) != 0:
             case.detach(self.lib)
             raise RuntimeError(f"batch_add: {self.lib.mibm_last_message().decode()}")
+        self.members.add(req.rid)
         self.cases[req.rid] = case
         self.bytes[req.rid] = need
         self.age[req.rid] = 0
@@ -252,27 +259,44 @@ class DeviceExecutor:
         case = self.cases.pop(rid)
         self.bytes.pop(rid, None)
         self.age.pop(rid, None)
-        if self.batch:
+        if self.batch and rid in self.members:
             self.lib.mibm_batch_remove_(abi.ref_int(self.batch), abi.ref_int(case.ctx[self.lib.path]))
+        self.members.discard(rid)
         case.detach(self.lib)
         return case
 
-    def step(self) -> dict:
-        """One batch step of every resident case.  Returns whether the step
-        carried an admission and the cases that failed in it."""
+    def _members(self, rids) -> None:
+        """Make the batch's members exactly `rids` (launch mode 1 rebuilds
+        nothing when members change)."""
+        want = set(rids)
+        for rid in list(self.members - want):
+            self.lib.mibm_batch_remove_(abi.ref_int(self.batch), abi.ref_int(self.cases[rid].ctx[self.lib.path]))
+            self.members.discard(rid)
+        for rid in sorted(want - self.members):
+            if self.lib.mibm_batch_add_(abi.ref_int(self.batch), abi.ref_int(self.cases[rid].ctx[self.lib.path])) != 0:
+                raise RuntimeError(f"batch_add: {self.lib.mibm_last_message().decode()}")
+            self.members.add(rid)
+
+    def step(self, rids=None) -> dict:
+        """One batch step of the resident cases `rids` (all when None).
+        Returns whether the step carried an admission and the cases that
+        failed in it."""
         self._ensure_batch()
-        admission = any(a < 2 for a in self.age.values())
+        rids = list(self.cases) if rids is None else list(rids)
+        self._members(rids)
+        admission = any(self.age[r] < 2 for r in rids)
         st = int(self.lib.mibm_batch_step_(abi.ref_int(self.batch), abi.ref_int(0)))
         failed = {}
         if st != 0:
-            for rid, case in self.cases.items():
+            for rid in rids:
+                case = self.cases[rid]
                 case.bind(self.lib)
                 cst = int(self.lib.mibm_last_status_())
                 if cst != 0:
                     failed[rid] = (cst, f"status {cst}: {self.lib.mibm_last_message().decode()}")
             if not failed:
                 raise RuntimeError(f"batch_step ({st}): {self.lib.mibm_last_message().decode()}")
-        for rid in self.age:
+        for rid in rids:
             self.age[rid] += 1
         return {"admission": admission, "failed": failed}
 
@@ -286,9 +310,10 @@ class DeviceExecutor:
 
 class Server:
     def __init__(self, executor, budget_bytes: int, prepare_workers: int = 2, keep_results: bool = False,
-                 on_finish=None, on_step=None):
+                 on_finish=None, on_step=None, step_cells: int | None = None):
         self.ex = executor
         self.budget = int(budget_bytes)
+        self.step_cells = step_cells        # work budget of a batch step in cells (None: every resident case)
         self.workers = prepare_workers
         self.keep_results = keep_results
         self.on_finish = on_finish          # callback(request, case) before the case is detached
@@ -311,7 +336,7 @@ class Server:
     def run(self, requests: list[Request], max_wall_s: float | None = None) -> ServeStats:
         pending = deque(sorted(requests, key=lambda r: r.arrival))
         futures: dict[int, cf.Future] = {}
-        active: dict[int, list] = {}         # rid -> [request, steps done, admitted time, bytes]
+        active: dict[int, list] = {}         # rid -> [request, steps done, admitted time, bytes, last stepped]
         used = 0
         oom_hold = False                     # an admission ran out of memory: wait for a completion
         stats = ServeStats(wall_s=0.0)
@@ -385,19 +410,34 @@ class Server:
                     used += need
                     stats.peak_bytes = max(stats.peak_bytes, used)
                     stats.admitted += 1
-                    active[r.rid] = [r, 0, now(), need]
+                    active[r.rid] = [r, 0, now(), need, -1]
                 if not active:
                     # idle: wait for the next arrival or preparation
                     time.sleep(0.002)
                     continue
                 if self.on_step is not None:
                     self.on_step(self, nstep)
+                    if not active:
+                        continue
+                cells = lambda a: a[0].cfg.n * a[0].cfg.n * a[0].cfg.nz
+                if self.step_cells is None:
+                    chosen = list(active)
+                else:
+                    # the cases that have waited longest, as many as fit the budget
+                    chosen, total = [], 0
+                    for rid in sorted(active, key=lambda r: (active[r][4], r)):
+                        if chosen and total + cells(active[rid]) > self.step_cells:
+                            continue
+                        chosen.append(rid)
+                        total += cells(active[rid])
                 ts = time.perf_counter()
-                info = self.ex.step() or {}
+                info = (self.ex.step(chosen) if self.step_cells is not None else self.ex.step()) or {}
                 stats.step_ms.append((time.perf_counter() - ts) * 1e3)
                 stats.admission.append(bool(info.get("admission", False)))
                 stats.active.append(len(active))
-                stats.resident_cells.append(sum(a[0].cfg.n * a[0].cfg.n * a[0].cfg.nz for a in active.values()))
+                stats.stepped_cells.append(sum(cells(active[r]) for r in chosen))
+                for rid in chosen:
+                    active[rid][4] = nstep
                 nstep += 1
                 failed = info.get("failed", {})
                 for rid, why in failed.items():
@@ -418,7 +458,10 @@ class Server:
                         stats.failed[rid] = msg
                     self.ex.detach(rid)
                     release(rid)
-                for rid, a in list(active.items()):
+                for rid in chosen:
+                    if rid not in active:
+                        continue
+                    a = active[rid]
                     a[1] += 1
                     stats.cell_steps += a[0].cfg.n * a[0].cfg.n * a[0].cfg.nz
                     if a[1] >= a[0].steps:

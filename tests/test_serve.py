@@ -173,7 +173,10 @@ def test_serving_requests_follow_the_configured_laws():
 
 
 @pytest.mark.gpu
-def test_served_cases_equal_cases_run_alone(gpu_lib):
+@pytest.mark.parametrize("step_cells", [None, 32 ** 3])
+def test_served_cases_equal_cases_run_alone(gpu_lib, step_cells):
+    """Every case equals the same case run alone, with all resident cases in
+    every batch step and with a work budget that advances a subset per step."""
     from melt_ibm_gb300.case import Case
     reqs = _requests()
     results = {}
@@ -183,10 +186,12 @@ def test_served_cases_equal_cases_run_alone(gpu_lib):
         results[req.rid] = {k: case.interior(f).copy() for k, f in FIELDS_OUT.items()}
 
     ex = DeviceExecutor(gpu_lib)
-    stats = Server(ex, budget_bytes=1 << 40, on_finish=keep).run(reqs)
+    stats = Server(ex, budget_bytes=1 << 40, on_finish=keep, step_cells=step_cells).run(reqs)
     ex.close()
     assert len(stats.finished) == len(reqs)
-    assert max(stats.active) >= 2                      # the cases did share batch steps
+    assert max(stats.active) >= 2                      # the cases were resident together
+    if step_cells is not None:
+        assert max(stats.stepped_cells) <= max(step_cells, max(r.cfg.n ** 3 for r in reqs))
     for r in reqs:
         c = Case(r.cfg)
         c.attach(gpu_lib)
@@ -245,3 +250,43 @@ def test_faults_leave_other_cases_bitwise_unchanged(gpu_lib):
         for k, f in FIELDS_OUT.items():
             assert np.array_equal(c.interior(f), results[r.rid][k]), (r.rid, k)
         c.detach(gpu_lib)
+
+
+class BudgetExecutor(HostExecutor):
+    """HostExecutor that records which cases each batch step advanced."""
+
+    def __init__(self):
+        super().__init__()
+        self.advanced = []
+
+    def step(self, rids=None):
+        rids = list(self.steps) if rids is None else list(rids)
+        self.advanced.append(list(rids))
+        for rid in rids:
+            self.steps[rid] += 1
+        return {"admission": False, "failed": {}}
+
+
+def test_step_budget_round_robin_keeps_every_case_in_order():
+    """With a work budget per batch step, each step advances the cases that
+    waited longest within the budget (at least one), every case still gets
+    exactly its steps, and no step exceeds the budget unless one case alone
+    does."""
+    reqs = [Request(rid=q, arrival=0.0, cfg=small_config(n=n), steps=5)
+            for q, n in enumerate([32, 16, 24, 16, 32, 24])]
+    ex = BudgetExecutor()
+    budget = 32 ** 3 + 16 ** 3
+    stats = Server(ex, budget_bytes=1 << 40, step_cells=budget).run(reqs)
+    assert sorted(f.rid for f in stats.finished) == list(range(6))
+    assert all(f.steps == 5 for f in stats.finished)
+    size = {r.rid: r.cfg.n ** 3 for r in reqs}
+    for rids in ex.advanced:
+        assert len(rids) >= 1
+        assert len(rids) == 1 or sum(size[r] for r in rids) <= budget
+    # no starvation: the case that has waited longest is always advanced,
+    # so no case waits more batch steps than there are resident cases
+    last = {}
+    for k, rids in enumerate(ex.advanced):
+        for r in rids:
+            assert r not in last or k - last[r] <= len(reqs), (r, k, last[r])
+            last[r] = k
