@@ -28,8 +28,8 @@ cpu_baseline / --impl reference
            MPI + FFTW + HDF5) cannot be built on this machine or the GPU machine.
 
 Inputs are larger than L2 (each field is N^3 doubles; > 30 fields resident).
-Multi-GPU: independent replicas, one per rank (the case does not shard across
-GPUs in this build); value = all ranks' cell-steps / max time over ranks.
+Multi-GPU: independent replicas, one per rank (a case runs on one GPU);
+value = all ranks' cell-steps / max time over ranks.
 """
 from __future__ import annotations
 

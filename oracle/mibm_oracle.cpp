@@ -1672,8 +1672,8 @@ void update_part_pos(Ctx& c) {
 }
 
 // ------------------------------------------------------------------------
-// particle.f90:1-230 (single particle; remeshing is outside this build's
-// scope and is skipped when its flag is off)
+// particle.f90:1-230 (single particle; the remeshing hand-off of
+// particle.f90:119-160 calls the host's remesher through the callback)
 // ------------------------------------------------------------------------
 void geometry_refresh(Ctx& c) {   // particle.f90:165-193
   c.S(MIBM_S_SURFACE) = calculate_area(c);
@@ -1720,7 +1720,7 @@ void particle(Ctx& c) {
     update_part_pos(c);
     if (c.status != MIBM_OK) return;
   }
-  // particle.f90:119-160: the remesher itself is the host's (see mibm.h)
+  // particle.f90:119-160: the remesher itself is host code behind the callback
   bool did_remesh = false;
   if (c.I(MIBM_I_IREMESH) == 1 && c.maxne > 0 && calculate_eLengths(c, c.S(MIBM_S_E_THRESH))) {
     if (!c.remesh_fn) {
