@@ -152,6 +152,32 @@ static bool step_prepare(Ctx* c) {
   return c->status == MIBM_OK;
 }
 
+// FP64 form: the temperature's line solves run on their own stream beside
+// the velocity's (they read and write only the temperature's RHS and T,
+// which the velocity solves do not touch), so that each kernel's last wave is
+// filled by the other's blocks; joined before the forcing, which reads T.
+// Not while kernels are timed one by one, and not in the precision form,
+// whose staged z solves hold every SM (measured: 30.19 -> 30.10 ms per 256^3
+// FP64 step, 4.43 -> 4.35 ms at 128^3; no gain in the precision form).
+static bool tsolve_fork(Ctx* c) { return c->tsolve && !c->profiling && c->precision == 0; }
+
+static void tsolve_begin(Ctx* c) {
+  if (!tsolve_fork(c)) return;
+  cudaEventRecord(c->ev_sfork, c->stream);
+  cudaStreamWaitEvent(c->tsolve, c->ev_sfork, 0);
+  std::swap(c->stream, c->tsolve);
+}
+
+static void tsolve_end(Ctx* c) {
+  if (!tsolve_fork(c)) return;
+  std::swap(c->stream, c->tsolve);
+  cudaEventRecord(c->ev_sjoin, c->tsolve);
+}
+
+static void tsolve_join(Ctx* c) {
+  if (tsolve_fork(c)) cudaStreamWaitEvent(c->stream, c->ev_sjoin, 0);
+}
+
 // Precision form: FP32 explicit terms, RHS, line solves and FFTs; u, v, w,
 // T, p stay FP64 and every FP32 kernel reads their FP32 mirrors.  The
 // projection is repeated `nproj` times, each on the divergence residual of
@@ -173,19 +199,23 @@ static void step_enqueue_f32(Ctx* c) {
     c->prologue_done = false;
     k_fused_rhs_f32(c, dp, c->ru32, c->rhs32);
     {
-      // u, v, w: one launch per direction (they share the velocity tables)
-      const float* Tv = tf + (size_t)((ns * 2 + 0) * 3) * tlen;
-      double* qv[3] = {c->df[kStepFid[0]], c->df[kStepFid[1]], c->df[kStepFid[2]]};
-      k_solve_x_f32(c, c->rhs32, Tv, 3);
-      k_solve_y_f32(c, c->rhs32, Tv + tlen, 3);
-      k_solve_z_f32(c, c->rhs32, Tv + 2 * tlen, qv, 3, nullptr);
-      lagr_loads_early(c, dp);                  // u, v, w solved: loads beside the T solves
+      // T on its own stream, then u, v, w: one launch per direction (they
+      // share the velocity tables)
+      tsolve_begin(c);
       const float* Tt = tf + (size_t)((ns * 2 + 1) * 3) * tlen;
       float* r = c->rhs32 + 3 * g.cells;
       double* qt[1] = {c->df[kStepFid[3]]};
       k_solve_x_f32(c, r, Tt, 1);
       k_solve_y_f32(c, r, Tt + tlen, 1);
       k_solve_z_f32(c, r, Tt + 2 * tlen, qt, 1, t_mirror);
+      tsolve_end(c);
+      const float* Tv = tf + (size_t)((ns * 2 + 0) * 3) * tlen;
+      double* qv[3] = {c->df[kStepFid[0]], c->df[kStepFid[1]], c->df[kStepFid[2]]};
+      k_solve_x_f32(c, c->rhs32, Tv, 3);
+      k_solve_y_f32(c, c->rhs32, Tv + tlen, 3);
+      k_solve_z_f32(c, c->rhs32, Tv + 2 * tlen, qv, 3, nullptr);
+      lagr_loads_early(c, dp);                  // u, v, w solved: loads beside the forcing's preparation
+      tsolve_join(c);
     }
     const double* mean3 = lagr_particle_fused(c, dp, c->q32, ns < 2 ? c->dparams + ns + 1 : nullptr, ns + 1);
     if (c->status != MIBM_OK) return;
@@ -216,19 +246,23 @@ static void step_enqueue_f64(Ctx* c) {
     c->prologue_done = false;
     k_fused_rhs(c, dp);
     {
-      // u, v, w: one launch per direction (they share the velocity tables)
-      const double* Tv = tables + (size_t)((ns * 2 + 0) * 3) * tlen;
-      double* qv[3] = {c->df[kStepFid[0]], c->df[kStepFid[1]], c->df[kStepFid[2]]};
-      k_solve_x_T(c, c->rhs4, Tv, 3);
-      k_solve_y_T(c, c->rhs4, Tv + tlen, 3);
-      k_solve_z_T(c, c->rhs4, Tv + 2 * tlen, qv, 3, 0);
-      lagr_loads_early(c, dp);                  // u, v, w solved: loads beside the T solves
+      // T on its own stream, then u, v, w: one launch per direction (they
+      // share the velocity tables)
+      tsolve_begin(c);
       const double* Tt = tables + (size_t)((ns * 2 + 1) * 3) * tlen;
       double* r = c->rhs4 + 3 * g.cells;
       double* qt[1] = {c->df[kStepFid[3]]};
       k_solve_x_T(c, r, Tt, 1);
       k_solve_y_T(c, r, Tt + tlen, 1);
       k_solve_z_T(c, r, Tt + 2 * tlen, qt, 1, 0);
+      tsolve_end(c);
+      const double* Tv = tables + (size_t)((ns * 2 + 0) * 3) * tlen;
+      double* qv[3] = {c->df[kStepFid[0]], c->df[kStepFid[1]], c->df[kStepFid[2]]};
+      k_solve_x_T(c, c->rhs4, Tv, 3);
+      k_solve_y_T(c, c->rhs4, Tv + tlen, 3);
+      k_solve_z_T(c, c->rhs4, Tv + 2 * tlen, qv, 3, 0);
+      lagr_loads_early(c, dp);                  // u, v, w solved: loads beside the forcing's preparation
+      tsolve_join(c);
     }
     const double* mean3 = lagr_particle_fused(c, dp, nullptr, ns < 2 ? c->dparams + ns + 1 : nullptr, ns + 1);
     if (c->status != MIBM_OK) return;

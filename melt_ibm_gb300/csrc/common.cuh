@@ -153,6 +153,8 @@ struct Ctx {
   cudaEvent_t ev_tfork = nullptr, ev_tjoin = nullptr;
   cudaStream_t side3 = nullptr;                         // MLS weights beside the scatter plan
   cudaEvent_t ev_wfork = nullptr, ev_wjoin = nullptr;
+  cudaStream_t tsolve = nullptr;                        // the temperature's line solves beside the velocity's
+  cudaEvent_t ev_sfork = nullptr, ev_sjoin = nullptr;
   bool loads_pending = false;
   std::vector<void*> pinned;              // host arrays page-locked by mibm_pin_host_
   // device-accessible addresses of page-locked host fields: the pack and

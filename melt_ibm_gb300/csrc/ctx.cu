@@ -319,6 +319,9 @@ void release(Ctx* c) {
   if (c->side) { cudaStreamSynchronize(c->side); cudaStreamDestroy(c->side); }
   if (c->side2) { cudaStreamSynchronize(c->side2); cudaStreamDestroy(c->side2); }
   if (c->side3) { cudaStreamSynchronize(c->side3); cudaStreamDestroy(c->side3); }
+  if (c->tsolve) { cudaStreamSynchronize(c->tsolve); cudaStreamDestroy(c->tsolve); }
+  if (c->ev_sfork) cudaEventDestroy(c->ev_sfork);
+  if (c->ev_sjoin) cudaEventDestroy(c->ev_sjoin);
   if (c->ev_wfork) cudaEventDestroy(c->ev_wfork);
   if (c->ev_wjoin) cudaEventDestroy(c->ev_wjoin);
   if (c->ev_tfork) cudaEventDestroy(c->ev_tfork);
@@ -350,6 +353,9 @@ int mibm_context_create_(void) {
       !cuda_ok(c, cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking), "stream") ||
       !cuda_ok(c, cudaStreamCreateWithFlags(&c->side2, cudaStreamNonBlocking), "stream") ||
       !cuda_ok(c, cudaStreamCreateWithFlags(&c->side3, cudaStreamNonBlocking), "stream") ||
+      !cuda_ok(c, cudaStreamCreateWithFlags(&c->tsolve, cudaStreamNonBlocking), "stream") ||
+      !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_sfork, cudaEventDisableTiming), "event") ||
+      !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_sjoin, cudaEventDisableTiming), "event") ||
       !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_wfork, cudaEventDisableTiming), "event") ||
       !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_wjoin, cudaEventDisableTiming), "event") ||
       !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_tfork, cudaEventDisableTiming), "event") ||
