@@ -243,12 +243,13 @@ void interp_(double* arrold, double* arrnew, const int* n1o, const int* n2o,
  * terms, RHS, line solves and FFTs on FP64 fields, with the pressure
  * projection repeated `nproj` times on the FP64 divergence residual. */
 void mibm_set_precision_(const int* mode, const int* nproj);
-/* mibm_set_tma_: the precision form's y- and z-line solves read their     */
-/* lines through bulk tensor copies (TMA) into shared memory (1, default)   */
-/* or straight from global memory (0).  Both give the same bits; lines      */
-/* longer than 256 cells or grids narrower than 32 cells always take the    */
-/* second path.  A staged copy that does not complete within about a second */
-/* is reported as MIBM_ETIMEOUT by the next cfl_.                           */
+/* mibm_set_tma_: the precision form's y- and z-line solves and the y and z */
+/* passes of its 256-point transforms read their lines through bulk tensor  */
+/* copies (TMA) into shared memory (1, default) or straight from global     */
+/* memory (0).  Both give the same bits; lines longer than 256 cells or     */
+/* grids narrower than 32 cells always take the second path.  A staged copy */
+/* that does not complete within about a second is reported as             */
+/* MIBM_ETIMEOUT by the next cfl_.                                          */
 void mibm_set_tma_(const int* on);
 /* mibm_set_fused_uvw_: the precision form's one-pass kernels (1, default): */
 /* the explicit terms and RHS of u, v, w in one kernel that forms the       */

@@ -536,6 +536,128 @@ void launch_x_inv(Ctx* c, const FftArgs<C>& F, const C* spec, typename Real<C>::
 
 // whole tiles of L columns, then the columns left over one line per block
 // (H = n1m/2 + 1 leaves the Nyquist column when L divides n1m/2)
+// Y and Z passes of the precision form's 256-point transforms with the
+// columns staged by bulk tensor copies: a persistent kernel over tiles of 16
+// adjacent kx columns (128 bytes per row) -- of one plane k for the y pass
+// (MODE 1 forward, 2 inverse), of one ky for the z pass (MODE 0: forward,
+// the eigenvalue division, inverse) -- each copied into a ring of
+// shared-memory stages ahead of the block; the transforms run in place on
+// the stage in the dense layout (16 x 16 engine), the results go back with
+// coalesced stores.  The same operations as y_pass / z_solve<float2, 256>
+// on the whole tiles (the lone Nyquist column stays with the one-line
+// kernels).  Stage waits are bounded (about a second); a timeout sets bit 2
+// of `err` and the block leaves after its other copies have landed.
+template <int MODE, int NSTAGE>
+__global__ void __launch_bounds__(256, 2)
+col_pass_tma(const __grid_constant__ CUtensorMap map, FftArgs<float2> F, float2* __restrict__ spec, int ntiles,
+             int* __restrict__ err) {
+  constexpr int N = 256, L = 16, T = 256;
+  constexpr uint32_t kStage = N * L * sizeof(float2);
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char* smem = smem_raw + ((1024u - (tma::smem_addr(smem_raw) & 1023u)) & 1023u);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
+  float2* tw = reinterpret_cast<float2*>(smem + 128);
+  float2* stage0 = reinterpret_cast<float2*>(smem + 128 + N * sizeof(float2));
+  const Grid& g = F.g;
+  const int tiles_x = g.H / L;
+  auto issue = [&](int tile, int s) {
+    const int kt = tile % tiles_x, o = tile / tiles_x;     // o: ky (z pass) or k (y pass)
+    tma::mbar_arrive_expect_tx(bars + s, kStage);
+    if (MODE == 0) tma::load_4d(stage0 + (size_t)s * N * L, &map, bars + s, kt * L, o, 0, 0);
+    else tma::load_4d(stage0 + (size_t)s * N * L, &map, bars + s, kt * L, 0, o, 0);
+  };
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NSTAGE; ++s) tma::mbar_init(bars + s, 1);
+    tma::fence_proxy_async();
+    for (int s = 0; s < NSTAGE; ++s) {
+      const int tile = blockIdx.x + s * gridDim.x;
+      if (tile < ntiles) issue(tile, s);
+    }
+  }
+  stage_twiddles<float2, N, T>(tw, MODE == 0 ? F.twz : F.twy);
+  __syncthreads();
+  const size_t lstride = MODE == 0 ? (size_t)g.HP * g.n2m : (size_t)g.HP;   // element stride of a line
+  const size_t eig_k = (size_t)g.H * g.n2m;
+  for (int li = 0;; ++li) {
+    const int tile = blockIdx.x + li * gridDim.x;
+    if (tile >= ntiles) break;
+    const int s = li % NSTAGE;
+    const bool ok = tma::mbar_wait(bars + s, (uint32_t)((li / NSTAGE) & 1));
+    if (!__syncthreads_and(ok)) {
+      if (threadIdx.x == 0) {
+        atomicOr(err, 2);
+        for (int kq = 1; kq < NSTAGE; ++kq) {
+          const int Lq = li + kq;
+          if (blockIdx.x + Lq * gridDim.x < ntiles) tma::mbar_wait(bars + Lq % NSTAGE, (uint32_t)((Lq / NSTAGE) & 1));
+        }
+      }
+      return;
+    }
+    const int kt = tile % tiles_x, o = tile / tiles_x, kx0 = kt * L;
+    float2* buf = stage0 + (size_t)s * N * L;
+    if (MODE == 0) {
+      const int j = o;
+      run16x16<float2, N, L, T, false, true>(buf, tw);
+      const float* __restrict__ eig = F.eig + (size_t)g.H * j;
+      for (int t = threadIdx.x; t < N * L; t += T) {
+        const int l = t % L, k = t / L;
+        float2 v = buf[t];
+        // buft / float(n1m*n2m*n3m) / (-ak3(k)-ak1(i)-ak2(j)), zero mode := 0
+        if (k == 0 && kx0 + l == 0 && j == 0) v = mk<float2>(0.f, 0.f);
+        else { const float f = eig[(size_t)(kx0 + l) + eig_k * k]; v.x *= f; v.y *= f; }
+        buf[t] = v;
+      }
+      __syncthreads();
+      run16x16<float2, N, L, T, true, true>(buf, tw);
+    } else {
+      run16x16<float2, N, L, T, MODE == 2, true>(buf, tw);
+    }
+    const size_t base = MODE == 0 ? (size_t)kx0 + (size_t)g.HP * o : (size_t)kx0 + (size_t)g.HP * g.n2m * o;
+    for (int t = threadIdx.x; t < N * L; t += T) {
+      const int l = t % L, e = t / L;
+      spec[base + l + lstride * e] = buf[t];
+    }
+    __syncthreads();   // stage s is free again
+    if (threadIdx.x == 0) {
+      const int next = tile + NSTAGE * gridDim.x;
+      if (next < ntiles) {
+        tma::fence_proxy_async();
+        issue(next, s);
+      }
+    }
+  }
+}
+
+// the TMA y (MODE 1 forward, 2 inverse) or z (MODE 0) pass on the whole
+// 16-column tiles of a 256-point FP32 transform; false when it does not
+// apply (the caller then launches the shared-memory tile kernel)
+template <typename C, int N, int MODE>
+bool launch_col_tma(Ctx* c, const FftArgs<C>& F, C* spec) {
+  if constexpr (!(sizeof(C) == 8 && N == 256)) {
+    return false;
+  } else {
+    constexpr int kStages = 3;
+    const Grid& g = c->g;
+    const int tiles_x = g.H / 16;
+    if (!c->tma || tiles_x < 1 || ((uintptr_t)spec & 15) != 0) return false;
+    CUtensorMap map;
+    const int box[4] = {16, MODE == 0 ? 1 : N, MODE == 0 ? N : 1, 1};
+    if (!tma::encode_fields(&map, spec, 8, g.H, g.n2m, g.n3m, g.HP, (size_t)g.HP * g.n2m * g.n3m, 1, box))
+      return false;
+    const size_t smem = 1024 + 128 + N * sizeof(float2) + (size_t)kStages * N * 16 * sizeof(float2);
+    auto k = col_pass_tma<MODE, kStages>;
+    if (!smem_attr(c, k, smem)) return false;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, smem);
+    const int ntiles = tiles_x * (MODE == 0 ? g.n2m : g.n3m);
+    const int grid = std::max(1, std::min(ntiles, std::max(1, per_sm) * std::max(1, sms)));
+    k<<<grid, 256, smem, c->stream>>>(map, F, spec, ntiles, c->dflag + 2);
+    return true;
+  }
+}
+
 template <typename C, int N>
 void launch_y(Ctx* c, const FftArgs<C>& F, C* spec, int sign) {
   typedef Shape<C, N> Sh;
@@ -548,7 +670,7 @@ void launch_y(Ctx* c, const FftArgs<C>& F, C* spec, int sign) {
       !smem_attr(c, ki1, S1::smem))
     return;
   const int tiles = c->g.H / Sh::L, rest = c->g.H - tiles * Sh::L;
-  if (tiles > 0) {
+  if (tiles > 0 && !(sign < 0 ? launch_col_tma<C, N, 1>(c, F, spec) : launch_col_tma<C, N, 2>(c, F, spec))) {
     dim3 grid(tiles, c->g.n3m);
     if (sign < 0) kf<<<grid, Sh::T, Sh::smem, c->stream>>>(F, spec, 0);
     else ki<<<grid, Sh::T, Sh::smem, c->stream>>>(F, spec, 0);
@@ -652,119 +774,6 @@ __global__ void __launch_bounds__(32 * kZtMaxChunks) z_tri_cc(FftArgs<C> F, C* _
   }
 }
 
-// Z pass of the precision form's 256-point transforms with the columns
-// staged by bulk tensor copies: a persistent kernel over tiles of 16
-// adjacent kx columns (128 bytes per z row) of one ky, each copied into a
-// ring of shared-memory stages ahead of the block; the transforms run in
-// place on the stage in the dense layout (16 x 16 engine), the results go
-// back with coalesced stores.  The same operations as z_solve<float2, 256>
-// on the whole tiles (the lone Nyquist column stays with the one-line
-// kernel).  Stage waits are bounded (about a second); a timeout sets bit 2
-// of `err` and the block leaves after its other copies have landed.
-template <int NSTAGE>
-__global__ void __launch_bounds__(256, 2)
-z_solve_tma(const __grid_constant__ CUtensorMap map, FftArgs<float2> F, float2* __restrict__ spec, int ntiles,
-            int* __restrict__ err) {
-  constexpr int N = 256, L = 16, T = 256;
-  constexpr uint32_t kStage = N * L * sizeof(float2);
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  unsigned char* smem = smem_raw + ((1024u - (tma::smem_addr(smem_raw) & 1023u)) & 1023u);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
-  float2* tw = reinterpret_cast<float2*>(smem + 128);
-  float2* stage0 = reinterpret_cast<float2*>(smem + 128 + N * sizeof(float2));
-  const Grid& g = F.g;
-  const int tiles_x = g.H / L;
-  auto issue = [&](int tile, int s) {
-    const int kt = tile % tiles_x, ky = tile / tiles_x;
-    tma::mbar_arrive_expect_tx(bars + s, kStage);
-    tma::load_4d(stage0 + (size_t)s * N * L, &map, bars + s, kt * L, ky, 0, 0);
-  };
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < NSTAGE; ++s) tma::mbar_init(bars + s, 1);
-    tma::fence_proxy_async();
-    for (int s = 0; s < NSTAGE; ++s) {
-      const int tile = blockIdx.x + s * gridDim.x;
-      if (tile < ntiles) issue(tile, s);
-    }
-  }
-  stage_twiddles<float2, N, T>(tw, F.twz);
-  __syncthreads();
-  const size_t zstride = (size_t)g.HP * g.n2m;
-  const size_t eig_k = (size_t)g.H * g.n2m;
-  for (int li = 0;; ++li) {
-    const int tile = blockIdx.x + li * gridDim.x;
-    if (tile >= ntiles) break;
-    const int s = li % NSTAGE;
-    const bool ok = tma::mbar_wait(bars + s, (uint32_t)((li / NSTAGE) & 1));
-    if (!__syncthreads_and(ok)) {
-      if (threadIdx.x == 0) {
-        atomicOr(err, 2);
-        for (int kq = 1; kq < NSTAGE; ++kq) {
-          const int Lq = li + kq;
-          if (blockIdx.x + Lq * gridDim.x < ntiles) tma::mbar_wait(bars + Lq % NSTAGE, (uint32_t)((Lq / NSTAGE) & 1));
-        }
-      }
-      return;
-    }
-    const int kt = tile % tiles_x, j = tile / tiles_x, kx0 = kt * L;
-    float2* buf = stage0 + (size_t)s * N * L;
-    run16x16<float2, N, L, T, false, true>(buf, tw);
-    const float* __restrict__ eig = F.eig + (size_t)g.H * j;
-    for (int t = threadIdx.x; t < N * L; t += T) {
-      const int l = t % L, k = t / L;
-      float2 v = buf[t];
-      // buft / float(n1m*n2m*n3m) / (-ak3(k)-ak1(i)-ak2(j)), zero mode := 0
-      if (k == 0 && kx0 + l == 0 && j == 0) v = mk<float2>(0.f, 0.f);
-      else { const float f = eig[(size_t)(kx0 + l) + eig_k * k]; v.x *= f; v.y *= f; }
-      buf[t] = v;
-    }
-    __syncthreads();
-    run16x16<float2, N, L, T, true, true>(buf, tw);
-    const size_t base = (size_t)kx0 + (size_t)g.HP * j;
-    for (int t = threadIdx.x; t < N * L; t += T) {
-      const int l = t % L, e = t / L;
-      spec[base + l + zstride * e] = buf[t];
-    }
-    __syncthreads();   // stage s is free again
-    if (threadIdx.x == 0) {
-      const int next = tile + NSTAGE * gridDim.x;
-      if (next < ntiles) {
-        tma::fence_proxy_async();
-        issue(next, s);
-      }
-    }
-  }
-}
-
-// the TMA z pass on the whole 16-column tiles of a 256-point FP32 z transform;
-// false when it does not apply (the caller then launches z_solve)
-template <typename C, int N>
-bool launch_z_tma(Ctx* c, const FftArgs<C>& F, C* spec) {
-  if constexpr (!(sizeof(C) == 8 && N == 256)) {
-    return false;
-  } else {
-    constexpr int kStages = 3;
-    const Grid& g = c->g;
-    const int tiles_x = g.H / 16;
-    if (!c->tma || tiles_x < 1 || ((uintptr_t)spec & 15) != 0) return false;
-    CUtensorMap map;
-    const int box[4] = {16, 1, N, 1};
-    if (!tma::encode_fields(&map, spec, 8, g.H, g.n2m, g.n3m, g.HP, (size_t)g.HP * g.n2m * g.n3m, 1, box))
-      return false;
-    const size_t smem = 1024 + 128 + N * sizeof(float2) + (size_t)kStages * N * 16 * sizeof(float2);
-    auto k = z_solve_tma<kStages>;
-    if (!smem_attr(c, k, smem)) return false;
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, smem);
-    const int ntiles = tiles_x * g.n2m;
-    const int grid = std::max(1, std::min(ntiles, std::max(1, per_sm) * std::max(1, sms)));
-    k<<<grid, 256, smem, c->stream>>>(map, F, spec, ntiles, c->dflag + 2);
-    return true;
-  }
-}
-
 template <typename C, int N>
 void launch_z(Ctx* c, const FftArgs<C>& F, C* spec) {
   typedef Shape<C, N> Sh;
@@ -783,7 +792,7 @@ void launch_z(Ctx* c, const FftArgs<C>& F, C* spec) {
     return;
   }
   const int tiles = c->g.H / Sh::L, rest = c->g.H - tiles * Sh::L;
-  if (tiles > 0 && !launch_z_tma<C, N>(c, F, spec))
+  if (tiles > 0 && !launch_col_tma<C, N, 0>(c, F, spec))
     k<<<dim3(tiles, c->g.n2m), Sh::T, Sh::smem, c->stream>>>(F, spec, 0);
   if (rest > 0) {
     k1<<<dim3(rest, c->g.n2m), S1::T, S1::smem, c->stream>>>(F, spec, tiles * Sh::L);
