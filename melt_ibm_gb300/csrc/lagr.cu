@@ -1761,18 +1761,17 @@ __global__ void band_ub_kernel(TagArgs T, const float4* __restrict__ face4, cons
   atomicMin(&band_ub[cidx(g, im, jm, km)], __float_as_uint(ub));
 }
 
-// one thread per (triangle, band cell); pass 0: distance (stored) and the
-// minimum per cell, pass 1: the earliest triangle at that distance, pass 2:
-// the winner writes the signed distance and the VOF
-// pass 0 runs over the compact list of band_select_kernel (entry t < *count)
+// one thread per (triangle, band cell) of the compact list of
+// band_select_kernel (entry t < *count; the pairs it culls can neither hold
+// a cell's minimum nor win it); pass 0: distance (stored) and the minimum
+// per cell, pass 1: the earliest triangle at that distance, pass 2: the
+// winner writes the signed distance and the VOF
 __global__ void band_kernel(TagArgs T, int pass, unsigned long long* __restrict__ sdf_bits, int* __restrict__ winner,
                             double* __restrict__ vofp, double* __restrict__ dist_buf, const int4* __restrict__ face_cell,
                             const int* __restrict__ list, const int* __restrict__ count) {
   long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (pass == 0) {
-    if (gid >= *count) return;
-    gid = list[gid];
-  }
+  if (gid >= *count) return;
+  gid = list[gid];
   int f = (int)(gid / 125), q = (int)(gid % 125);
   const LagArgs& A = T.L;
   if (f >= A.nf || T.ghost[f]) return;
