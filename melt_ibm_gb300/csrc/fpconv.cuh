@@ -66,6 +66,61 @@ __device__ __forceinline__ float d2f_bits(double d) {
   return __uint_as_float(sign | (q + up));   // q + up == 2^23 is the smallest normal
 }
 
+// ---------------------------------------------------------------------
+// (a1 - a0) + (b1 - b0) + (c1 - c0) of six FP64 values, rounded once to
+// FP32, on the integer pipe.  Each value's 53-bit significand is shifted
+// right to the weight of the last bit of the largest input (exponent E),
+// given its sign, and the six are summed in 64-bit integers (|sum| < 2^56);
+// the sum is rounded to nearest, ties to even.  The shifts drop bits below
+// that weight only, so the result is within 6 * 2^-52 times the largest
+// |input| of the exact sum before its rounding (FP64 arithmetic: within
+// about 8 * 2^-52), and it is the correctly rounded exact sum when every
+// input is a multiple of that weight.  Zero and subnormal inputs are taken
+// with the implicit bit (below 2^-1021 in magnitude); a sum below the normal
+// FP32 range is flushed to a signed zero, one above it is infinity; an
+// infinite or NaN input gives NaN.
+// ---------------------------------------------------------------------
+__device__ __forceinline__ int fx_exp(double x) {
+  return (int)(((uint32_t)((uint64_t)__double_as_longlong(x) >> 32) >> 20) & 0x7ffu);
+}
+
+// x's significand (with the implicit bit) shifted right by sh >= 0, signed
+__device__ __forceinline__ int64_t fx_aligned(double x, int sh) {
+  const uint64_t b = (uint64_t)__double_as_longlong(x);
+  const uint64_t m = (b & 0x000fffffffffffffull) | 0x0010000000000000ull;
+  const uint64_t s = (uint64_t)((int64_t)b >> 63);           // 0 or all ones
+  return (int64_t)(((m >> (sh < 63 ? sh : 63)) ^ s) - s);
+}
+
+// S * 2^(E - 1075) to FP32, round to nearest even
+__device__ __forceinline__ float fx_round_f32(int64_t S, int E) {
+  const uint64_t s = (uint64_t)(S >> 63);
+  const uint64_t A0 = ((uint64_t)S ^ s) - s;
+  if (A0 == 0) return 0.0f;
+  const uint32_t sign = (uint32_t)s & 0x80000000u;
+  const int lz = __clzll((long long)A0);
+  const uint64_t A = A0 << lz;                               // leading one at bit 63
+  uint32_t q = (uint32_t)(A >> 40);                          // 24 significant bits
+  const uint32_t r = (uint32_t)(A >> 39) & 1u, sticky = (uint32_t)((A & 0x7fffffffffull) != 0);
+  q += r & (sticky | (q & 1u));
+  const int ef = 63 - lz + E - 1075 + 127;                   // biased exponent of the leading one
+  if (ef <= 0) return __uint_as_float(sign);
+  if (ef >= 255) return __uint_as_float(sign | 0x7f800000u);
+  const uint32_t bits = ((uint32_t)ef << 23) + (q - 0x800000u);   // a carry of q moves into the exponent
+  return __uint_as_float(sign | (bits >= 0x7f800000u ? 0x7f800000u : bits));
+}
+
+__device__ __forceinline__ float sum3_diff_f32(double a1, double a0, double b1, double b0, double c1, double c0) {
+  const int ea1 = fx_exp(a1), ea0 = fx_exp(a0), eb1 = fx_exp(b1), eb0 = fx_exp(b0), ec1 = fx_exp(c1),
+            ec0 = fx_exp(c0);
+  const int E = max(max(max(ea1, ea0), max(eb1, eb0)), max(ec1, ec0));
+  if (E == 0x7ff) return __uint_as_float(0x7fc00000u);
+  const int64_t S = (fx_aligned(a1, E - ea1) - fx_aligned(a0, E - ea0)) +
+                    (fx_aligned(b1, E - eb1) - fx_aligned(b0, E - eb0)) +
+                    (fx_aligned(c1, E - ec1) - fx_aligned(c0, E - ec0));
+  return fx_round_f32(S, E);
+}
+
 // the compute type R of a templated kernel from / to FP64 (identity for FP64)
 __device__ __forceinline__ double widen(double x) { return x; }
 __device__ __forceinline__ double widen(float x) { return f2d_bits(x); }

@@ -6,7 +6,9 @@
 // random bit patterns.  The line-solve factor table evaluated on the device
 // (the allocation-free x-line solve builds it there) must equal the host's
 // evaluation bit for bit.  The written-out exp of the MLS weights (mls_exp.h)
-// must give the host's bits on the device.
+// must give the host's bits on the device.  The integer-pipe sum of three
+// FP64 differences (sum3_diff_f32) must give FP64 arithmetic's bits where
+// that is exact, and agree with it to its error bound elsewhere.
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
@@ -86,6 +88,66 @@ static void edge_cases(std::vector<unsigned long long>& v) {
   for (uint32_t x : fr) f(x);
 }
 
+// sum3_diff_f32 against FP64 arithmetic on n random sextuples.  Even t:
+// k * 2^s with |k| < 2^50 and one s per sextuple, where FP64 arithmetic is
+// exact, so both must give the same bits; odd t: values of random sign and
+// exponent spread over 2^-40 .. 2^40, within 2^-48 of the largest |input|
+// plus two FP32 units of the result.  bad[0] counts failures, bad[1] keeps
+// the first t.
+__global__ void sum3_selftest_kernel(long long n, unsigned long long* __restrict__ bad) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    double x[6];
+    const uint64_t r0 = mix64((uint64_t)t * 7u + 1u);
+    const int s = (int)(r0 % 81u) - 60;
+    double amax = 0.0;
+    for (int q = 0; q < 6; ++q) {
+      const uint64_t r = mix64((uint64_t)t * 7u + 2u + (uint64_t)q);
+      if ((t & 1) == 0) {
+        const int64_t k = (int64_t)(r >> 14) - (int64_t)(1ll << 49);            // |k| < 2^50
+        x[q] = ldexp((double)(k >> (r & 31)), s);                                 // spread the magnitudes
+      } else {
+        const double m = 1.0 + (double)(r >> 12) * 0x1.0p-52;
+        x[q] = ldexp((r & 1) ? -m : m, (int)((r >> 1) % 81u) - 40);
+      }
+      amax = fmax(amax, fabs(x[q]));
+    }
+    if ((t & 7) == 3) x[1] = x[0];                                               // exact cancellations
+    if ((t & 15) == 5) { x[3] = x[2]; x[5] = x[4]; }
+    const float got = sum3_diff_f32(x[0], x[1], x[2], x[3], x[4], x[5]);
+    const double fp = ((x[0] - x[1]) + (x[2] - x[3])) + (x[4] - x[5]);
+    bool ok;
+    if ((t & 1) == 0) {
+      ok = __float_as_uint(got) == __float_as_uint(d2f_bits(fp));
+    } else {
+      const float ref = d2f_bits(fp);
+      const double ulp = ldexp(1.0, ilogb(fmax(fabs((double)ref), fabs((double)got)) + 1e-300) - 23);
+      ok = fabs((double)got - (double)ref) <= ldexp(amax, -48) + 2.0 * ulp;
+    }
+    if (t == 0) {          // equal pairs give +0; an infinity or a NaN gives NaN
+      const double inf = __longlong_as_double(0x7ff0000000000000ll), nan = __longlong_as_double(0x7ff8000000000000ll);
+      const float z = sum3_diff_f32(1.5, 1.5, -2.0, -2.0, 0.0, 0.0);
+      const float a = sum3_diff_f32(inf, 1.0, 0.0, 0.0, 0.0, 0.0), b = sum3_diff_f32(1.0, 1.0, 2.0, nan, 0.0, 0.0);
+      ok = ok && __float_as_uint(z) == 0u && a != a && b != b;
+    }
+    if (!ok && atomicAdd(&bad[0], 1ull) == 0) bad[1] = (unsigned long long)t;
+  }
+}
+
+static long long sum3_selftest() {
+  unsigned long long* d = nullptr;
+  unsigned long long h[2] = {0, 0};
+  if (cudaMalloc(&d, 16) != cudaSuccess) { cudaGetLastError(); return -1; }
+  bool ok = cudaMemset(d, 0, 16) == cudaSuccess;
+  if (ok) {
+    sum3_selftest_kernel<<<1216, 256>>>(1ll << 24, d);
+    ok = cudaDeviceSynchronize() == cudaSuccess && cudaMemcpy(h, d, 16, cudaMemcpyDeviceToHost) == cudaSuccess;
+  }
+  cudaFree(d);
+  if (!ok) { cudaGetLastError(); return -1; }
+  if (h[0]) fprintf(stderr, "mibm_selftest_: sum3_diff_f32 fails at %llu sextuples (first t = %llu)\n", h[0], h[1]);
+  return (long long)h[0];
+}
+
 long long tri_factors_selftest();   // tridiag.cu
 
 // mls_exp on the device over n arguments spread over [-750, 712] and the
@@ -148,7 +210,10 @@ extern "C" int mibm_selftest_(void) {
   const long long ebad = mls_exp_selftest();
   if (ebad < 0) return -1;
   if (ebad) fprintf(stderr, "mibm_selftest_: mls_exp differs between host and device at %lld arguments\n", ebad);
-  return (int)std::min<unsigned long long>(hbad[0] + hbad[1] + (unsigned long long)tbad + (unsigned long long)ebad,
+  const long long sbad = sum3_selftest();
+  if (sbad < 0) return -1;
+  return (int)std::min<unsigned long long>(hbad[0] + hbad[1] + (unsigned long long)tbad + (unsigned long long)ebad +
+                                               (unsigned long long)sbad,
                                            1000000);
 }
 

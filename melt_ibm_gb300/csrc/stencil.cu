@@ -536,19 +536,22 @@ __global__ void divg_kernel(StencilArgs A, const StepParams* __restrict__ pp, do
   dph[c0] = dq * usdtal;
 }
 
-// precision form: the divergence residual of the FP64 velocity, formed in
-// FP64 (the face differences cancel to round-off of u), then rounded once to
-// FP32 as the right-hand side of the FP32 Poisson solve.  ISO (equal grid
-// spacings in the three directions): the sum of the differences in FP64 and
-// the spacing folded into the FP32 factor, five FP64 operations per cell
-// instead of six (the kernel is bound by FP64 issue).
+// precision form: the divergence residual of the FP64 velocity, formed at
+// FP64 accuracy (the face differences cancel to round-off of u), then rounded
+// once to FP32 as the right-hand side of the FP32 Poisson solve.  ISO (equal
+// grid spacings in the three directions): the sum of the three differences is
+// formed in 64-bit integers on the integer pipe (sum3_diff_f32: FP64
+// accuracy, no FP64 instruction; five FP64 operations per cell bounded the
+// kernel at 2.4 times its memory time) and the spacing is folded into the
+// FP32 factor; otherwise the differences are scaled in FP64.
 template <bool ISO>
 __global__ void divg_f32_kernel(StencilArgs A, const StepParams* __restrict__ pp, float* __restrict__ res) {
   CELL_INDEX
-  double du = A.vx[c0 + dip] - A.vx[c0], dv = A.vy[c0 + djp] - A.vy[c0], dw = A.vz[c0 + dkp] - A.vz[c0];
   if constexpr (ISO) {
-    res[c0] = d2f_bits((du + dv) + dw) * pp->cf[kDVI];
+    res[c0] = sum3_diff_f32(A.vx[c0 + dip], A.vx[c0], A.vy[c0 + djp], A.vy[c0], A.vz[c0 + dkp], A.vz[c0]) *
+              pp->cf[kDVI];
   } else {
+    double du = A.vx[c0 + dip] - A.vx[c0], dv = A.vy[c0 + djp] - A.vy[c0], dw = A.vz[c0 + dkp] - A.vz[c0];
     double dq = fma(dw, g.dx3, fma(dv, g.dx2, du * g.dx1));
     res[c0] = d2f_bits(dq) * pp->cf[kUSDTAL];
   }
