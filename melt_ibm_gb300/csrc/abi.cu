@@ -219,12 +219,23 @@ static void step_enqueue_f32(Ctx* c) {
     }
     const double* mean3 = lagr_particle_fused(c, dp, c->q32, ns < 2 ? c->dparams + ns + 1 : nullptr, ns + 1);
     if (c->status != MIBM_OK) return;
+    // one-pass form: each sweep but the last also forms the next sweep's
+    // residual, with u, v, w moved between the fields and vel1 (the same bits)
+    bool in_vel1 = false, have_res = false;
     for (int it = 0; it < c->nproj; ++it) {
       bool last = it + 1 == c->nproj;
-      k_divg_f32(c, dp, c->res32);                     // FP64 residual, rounded once
+      if (!have_res) k_divg_f32(c, dp, c->res32);      // FP64 residual, rounded once
+      have_res = false;
       k_phcalc_f32(c, c->res32, c->phi32);             // FP32 Poisson solve
       if (c->fused_uvw) {
-        k_updvp_prcalc_f32(c, dp, c->phi32, it == 0 ? mean3 : nullptr, last);
+        const double* m = it == 0 ? mean3 : nullptr;
+        if (!last && k_updvp_prcalc_divg_f32(c, dp, c->phi32, m, in_vel1, c->res32)) {
+          in_vel1 = !in_vel1;
+          have_res = true;
+        } else {
+          k_updvp_prcalc_f32(c, dp, c->phi32, m, last, in_vel1);
+          in_vel1 = false;
+        }
       } else {
         k_updvp_f32(c, dp, c->phi32, it == 0 ? mean3 : nullptr, last);
         k_prcalc_f32(c, dp, c->phi32, last);

@@ -179,6 +179,7 @@ struct Ctx {
   float* rhs32 = nullptr;                 // 4 RHS / line-solve fields (FP32)
   float* phi32 = nullptr;                 // FP32 pressure correction
   float* res32 = nullptr;                 // FP32 copy of the FP64 divergence residual
+  double* vel1 = nullptr;                 // u, v, w after a projection sweep that is not the last (3 fields)
   // FP32 mirrors of u, v, w, T, p (5 fields, field order of the Stencil
   // kernels) read by the FP32 stencils.  The kernels that write the FP64
   // fields in the precision form also write the mirror; anything else that
@@ -338,7 +339,10 @@ void k_fused_rhs_f32(Ctx* c, const StepParams* dp, float* ru4, float* rhs4);
 void k_updvp_f32(Ctx* c, const StepParams* dp, const float* phi, const double* mean3, bool mirror);
 void k_prcalc_f32(Ctx* c, const StepParams* dp, const float* phi, bool mirror);
 void k_divg_f32(Ctx* c, const StepParams* dp, float* res);
-void k_updvp_prcalc_f32(Ctx* c, const StepParams* dp, const float* phi, const double* mean3, bool mirror);
+void k_updvp_prcalc_f32(Ctx* c, const StepParams* dp, const float* phi, const double* mean3, bool mirror,
+                        bool from_vel1 = false);
+bool k_updvp_prcalc_divg_f32(Ctx* c, const StepParams* dp, const float* phi, const double* mean3, bool from_vel1,
+                             float* res);
 void k_mirror_fields(Ctx* c);
 // HIT forcing (hit.cu)
 void k_hit_random_force(Ctx* c);

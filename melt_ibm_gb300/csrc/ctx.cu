@@ -301,7 +301,7 @@ void release(Ctx* c) {
   cudaFree(c->xc); cudaFree(c->xm); cudaFree(c->yc); cudaFree(c->ym); cudaFree(c->zc); cudaFree(c->zm);
   cudaFree(c->red); cudaFree(c->dflag); cudaFree(c->dparams); cudaFree(c->rhs4);
   cudaFree(c->ru32); cudaFree(c->rhs32); cudaFree(c->phi32); cudaFree(c->divmax);
-  cudaFree(c->res32); cudaFree(c->q32); cudaFree(c->prod); cudaFree(c->prod32);
+  cudaFree(c->res32); cudaFree(c->vel1); cudaFree(c->q32); cudaFree(c->prod); cudaFree(c->prod32);
   cudaFree(c->tri_coef); cudaFree(c->lag_red);
   if (c->red_host) cudaFreeHost(c->red_host);
   if (c->hflag) cudaFreeHost(c->hflag);

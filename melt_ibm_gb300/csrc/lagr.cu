@@ -1811,12 +1811,6 @@ __global__ void band_kernel(TagArgs T, int pass, unsigned long long* __restrict_
   sdf_bits[c0] = (unsigned long long)__double_as_longlong(sgnd);
 }
 
-__global__ void sdf_finish_kernel(Grid g, const unsigned long long* __restrict__ bits, double* __restrict__ sdf) {
-  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= g.cells) return;
-  sdf[t] = __longlong_as_double((long long)bits[t]);
-}
-
 // initial full tagging: one thread per cell of the bounding box
 __device__ bool ray_tri(const double C[3], const double Q[3], const double V0[3], const double V1[3],
                         const double V2[3], double ip[3]) {
@@ -1919,7 +1913,6 @@ struct LagState {
   unsigned* loads_ticket = nullptr;   // blocks of loads_face_kernel done (0 between launches)
   int* rm_flag = nullptr;       // remesh trigger (device)
   double* mean3 = nullptr;
-  unsigned long long* sdf_bits = nullptr;
   int* winner = nullptr;
   double* dist_buf = nullptr;
   // narrow-band culling: per cell an FP32 upper bound of the nearest face
@@ -2392,13 +2385,16 @@ void lagr_geometry_refresh(Ctx* c, bool imelt) {
   lagr_geometry_to_host(c);
 }
 
+// the narrow band keeps its minimum distances as integer bit patterns in the
+// signed-distance field's own memory (non-negative doubles order as their
+// bits) and leaves the signed distances there: no copy pass
+static unsigned long long* sdf_bits_of(Ctx* c) { return reinterpret_cast<unsigned long long*>(c->df[MIBM_F_SDF]); }
+
 void lagr_tag_narrow_band(Ctx* c) {
   if (c->maxnf == 0) return;
   LagState* s = lag_of(c);
-  if (!s->sdf_bits) {
-    if (!cuda_ok(c, cudaMalloc(&s->sdf_bits, sizeof(unsigned long long) * c->g.cells), "band")) return;
-    if (!cuda_ok(c, cudaMalloc(&s->winner, sizeof(int) * c->g.cells), "band")) return;
-  }
+  if (!s->winner && !cuda_ok(c, cudaMalloc(&s->winner, sizeof(int) * c->g.cells), "band")) return;
+  unsigned long long* const sdf_bits = sdf_bits_of(c);
   TagArgs T;
   T.L = lag_args(c);
   if (!s->dist_buf) {
@@ -2416,7 +2412,7 @@ void lagr_tag_narrow_band(Ctx* c) {
   T.x = M<double>(c, MIBM_M_XYZV); T.vof = M<int>(c, MIBM_M_VERT_OF_FACE); T.ghost = M<int>(c, MIBM_M_GHOST_FACE);
   T.bar = M<double>(c, MIBM_M_TRI_BAR); T.nor = M<double>(c, MIBM_M_TRI_NOR);
   { MIBM_PROF(c, "sdf_reset");
-    sdf_reset_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, s->sdf_bits, s->winner, s->band_ub); }
+    sdf_reset_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, sdf_bits, s->winner, s->band_ub); }
   size_t nthr = (size_t)c->maxnf * 125;
   { MIBM_PROF(c, "band_bound");
     band_prep_kernel<<<div_up(c->maxnf, 128), 128, 0, c->stream>>>(T, s->face4, s->face_cell);
@@ -2426,12 +2422,10 @@ void lagr_tag_narrow_band(Ctx* c) {
                                                                   s->dist_buf, s->band_list, s->band_count); }
   for (int pass = 0; pass < 3; ++pass) {
     MIBM_PROF(c, "band");
-    band_kernel<<<div_up(nthr, 128), 128, 0, c->stream>>>(T, pass, s->sdf_bits, s->winner, c->df[MIBM_F_VOFP],
+    band_kernel<<<div_up(nthr, 128), 128, 0, c->stream>>>(T, pass, sdf_bits, s->winner, c->df[MIBM_F_VOFP],
                                                            s->dist_buf, s->face_cell, s->band_list, s->band_count);
   }
-  { MIBM_PROF(c, "sdf_finish");
-    sdf_finish_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, s->sdf_bits, c->df[MIBM_F_SDF]); }
-  c->launches += 8;
+  c->launches += 7;
   k_interp_vof(c);
   MIBM_LAUNCH_CHECK(c, "narrowBandTagging");
 }
@@ -2465,13 +2459,10 @@ void lagr_tag_initial(Ctx* c) {
   T.bar = M<double>(c, MIBM_M_TRI_BAR); T.nor = M<double>(c, MIBM_M_TRI_NOR);
   size_t ncell = (size_t)nb[0] * nb[1] * nb[2];
   LagState* s = lag_of(c);
-  if (!s->sdf_bits) {
-    if (!cuda_ok(c, cudaMalloc(&s->sdf_bits, sizeof(unsigned long long) * c->g.cells), "band")) return;
-    if (!cuda_ok(c, cudaMalloc(&s->winner, sizeof(int) * c->g.cells), "band")) return;
-  }
+  if (!s->winner && !cuda_ok(c, cudaMalloc(&s->winner, sizeof(int) * c->g.cells), "band")) return;
   double* tmp = nullptr;
   if (!cuda_ok(c, cudaMalloc(&tmp, sizeof(double) * std::max<size_t>(1, ncell)), "initial tag")) return;
-  sdf_reset_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, s->sdf_bits, s->winner, nullptr);
+  sdf_reset_kernel<<<div_up(c->g.cells, 256), 256, 0, c->stream>>>(c->g, sdf_bits_of(c), s->winner, nullptr);
   initial_tag_kernel<<<div_up(ncell, 128), 128, 0, c->stream>>>(T, b0[0], b0[1], b0[2], nb[0], nb[1], nb[2], tmp);
   for (int pass = 0; pass < 2; ++pass)
     initial_claim_kernel<<<div_up(ncell, 256), 256, 0, c->stream>>>(c->g, b0[0], b0[1], b0[2], nb[0], nb[1], nb[2], tmp,
@@ -2821,7 +2812,7 @@ void lagr_free(Ctx* c) {
       LagState* s = g_lag[q];
       cudaFree(s->adj_off); cudaFree(s->adj_face); cudaFree(s->face_part); cudaFree(s->geom_out); cudaFree(s->geom_ticket);
       cudaFree(s->loads_ev); cudaFree(s->loads_ticket); cudaFree(s->rm_flag);
-      cudaFree(s->mean3); cudaFree(s->sdf_bits); cudaFree(s->winner); cudaFree(s->dist_buf);
+      cudaFree(s->mean3); cudaFree(s->winner); cudaFree(s->dist_buf);
       cudaFree(s->band_ub); cudaFree(s->face4); cudaFree(s->face_cell); cudaFree(s->cm32);
       cudaFree(s->band_list); cudaFree(s->band_count);
       cudaFree(s->key); cudaFree(s->src); cudaFree(s->tmp_key); cudaFree(s->tmp_src); cudaFree(s->hist);

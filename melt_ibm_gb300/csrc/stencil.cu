@@ -609,15 +609,19 @@ __global__ void prcalc_f32_kernel(StencilArgs A, const StepParams* __restrict__ 
 // read the same phi), every load issued before the first use; the same
 // expressions, so the same bits.  m32: the mirrors' base (u, v, w at 0,
 // cells, 2 cells; p at 4 cells), or null
+// OOP: u, v, w read from (ux, uy, uz) and written to (vx, vy, vz) (after a
+// sweep of updvp_prcalc_divg_f32_kernel); otherwise in place in (vx, vy, vz)
+template <bool OOP>
 __global__ void updvp_prcalc_f32_kernel(StencilArgs A, const StepParams* __restrict__ pp,
-                                        const float* __restrict__ phi, double* __restrict__ vx,
-                                        double* __restrict__ vy, double* __restrict__ vz,
+                                        const float* __restrict__ phi, const double* __restrict__ ux,
+                                        const double* __restrict__ uy, const double* __restrict__ uz,
+                                        double* __restrict__ vx, double* __restrict__ vy, double* __restrict__ vz,
                                         double* __restrict__ pr, const float* __restrict__ mean3f,
                                         float* __restrict__ m32) {
   CELL_INDEX
   const float loc = phi[c0], fim = phi[c0 + dim], fjm = phi[c0 + djm], fkm = phi[c0 + dkm];
   const float fip = phi[c0 + dip], fjp = phi[c0 + djp], fkp = phi[c0 + dkp];
-  const double u0 = vx[c0], v0 = vy[c0], w0 = vz[c0], p0 = pr[c0];
+  const double u0 = (OOP ? ux : vx)[c0], v0 = (OOP ? uy : vy)[c0], w0 = (OOP ? uz : vz)[c0], p0 = pr[c0];
   float ix = (loc - fim) * pp->cf[kUP1];
   float iy = (loc - fjm) * pp->cf[kUP2];
   float iz = (loc - fkm) * pp->cf[kUP3];
@@ -633,6 +637,49 @@ __global__ void updvp_prcalc_f32_kernel(StencilArgs A, const StepParams* __restr
   if (m32) {
     m32[c0] = d2f_bits(x); m32[c0 + g.cells] = d2f_bits(y); m32[c0 + 2 * g.cells] = d2f_bits(z);
     m32[c0 + 4 * g.cells] = d2f_bits(q);
+  }
+}
+
+// precision form, a projection sweep that is not the last: the update of
+// updvp_prcalc_f32_kernel with u, v, w written out of place (from (ux, uy,
+// uz) to (vx, vy, vz); p in place; no mirrors), together with the next
+// sweep's divergence residual of the updated velocity (divg_f32_kernel).
+// The updates of the three upwind neighbours (i+1, j+1, k+1) are formed
+// again here by the same operations, so they have the bits that their own
+// threads write: the residual equals divg_f32_kernel's on the written
+// fields, and the sweep reads the velocity once instead of twice.
+template <bool ISO>
+__global__ void updvp_prcalc_divg_f32_kernel(StencilArgs A, const StepParams* __restrict__ pp,
+                                             const float* __restrict__ phi, const double* __restrict__ ux,
+                                             const double* __restrict__ uy, const double* __restrict__ uz,
+                                             double* __restrict__ vx, double* __restrict__ vy,
+                                             double* __restrict__ vz, double* __restrict__ pr,
+                                             const float* __restrict__ mean3f, float* __restrict__ res) {
+  CELL_INDEX
+  const float loc = phi[c0], fim = phi[c0 + dim], fjm = phi[c0 + djm], fkm = phi[c0 + dkm];
+  const float fip = phi[c0 + dip], fjp = phi[c0 + djp], fkp = phi[c0 + dkp];
+  const double u0 = ux[c0], v0 = uy[c0], w0 = uz[c0], p0 = pr[c0];
+  const double un = ux[c0 + dip], vn = uy[c0 + djp], wn = uz[c0 + dkp];
+  float ix = (loc - fim) * pp->cf[kUP1], iy = (loc - fjm) * pp->cf[kUP2], iz = (loc - fkm) * pp->cf[kUP3];
+  float jx = (fip - loc) * pp->cf[kUP1], jy = (fjp - loc) * pp->cf[kUP2], jz = (fkp - loc) * pp->cf[kUP3];
+  if (mean3f) {
+    ix += mean3f[0]; iy += mean3f[1]; iz += mean3f[2];
+    jx += mean3f[0]; jy += mean3f[1]; jz += mean3f[2];
+  }
+  const double x = u0 - f2d_bits(ix), y = v0 - f2d_bits(iy), z = w0 - f2d_bits(iz);
+  const double xn = un - f2d_bits(jx), yn = vn - f2d_bits(jy), zn = wn - f2d_bits(jz);
+  vx[c0] = x; vy[c0] = y; vz[c0] = z;
+  const float be = pp->cf[kBE];
+  const float inc = loc - be * ((fip - 2.0f * loc + fim) * pp->cf[kDQ1] +
+                                (fjp - 2.0f * loc + fjm) * pp->cf[kDQ2] +
+                                (fkp - 2.0f * loc + fkm) * pp->cf[kDQ3]);
+  pr[c0] = p0 + f2d_bits(inc);
+  if constexpr (ISO) {
+    res[c0] = sum3_diff_f32(xn, x, yn, y, zn, z) * pp->cf[kDVI];
+  } else {
+    const double du = xn - x, dv = yn - y, dw = zn - z;
+    const double dq = fma(dw, g.dx3, fma(dv, g.dx2, du * g.dx1));
+    res[c0] = d2f_bits(dq) * pp->cf[kUSDTAL];
   }
 }
 
@@ -992,14 +1039,53 @@ void k_updvp_f32(Ctx* c, const StepParams* dp, const float* phi, const double* m
   MIBM_LAUNCH_CHECK(c, "updvp_f32");
 }
 
-void k_updvp_prcalc_f32(Ctx* c, const StepParams* dp, const float* phi, const double* mean3, bool mirror) {
+void k_updvp_prcalc_f32(Ctx* c, const StepParams* dp, const float* phi, const double* mean3, bool mirror,
+                        bool from_vel1) {
   { MIBM_PROF(c, "updvp_prcalc_f32");
     const float* mean3f = mean3 ? reinterpret_cast<const float*>(mean3 + 4) : nullptr;
-    updvp_prcalc_f32_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(
-        make_args(c), dp, phi, c->df[MIBM_F_VX], c->df[MIBM_F_VY], c->df[MIBM_F_VZ], c->df[MIBM_F_PR], mean3f,
-        mirror ? c->q32 : nullptr); }
+    double* const* f = c->df;
+    if (from_vel1) {
+      const double* u = c->vel1;
+      updvp_prcalc_f32_kernel<true><<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(
+          make_args(c), dp, phi, u, u + c->g.cells, u + 2 * c->g.cells, f[MIBM_F_VX], f[MIBM_F_VY], f[MIBM_F_VZ],
+          f[MIBM_F_PR], mean3f, mirror ? c->q32 : nullptr);
+    } else {
+      updvp_prcalc_f32_kernel<false><<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(
+          make_args(c), dp, phi, nullptr, nullptr, nullptr, f[MIBM_F_VX], f[MIBM_F_VY], f[MIBM_F_VZ], f[MIBM_F_PR],
+          mean3f, mirror ? c->q32 : nullptr);
+    } }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "updvp_prcalc_f32");
+}
+
+// a projection sweep that is not the last, fused with the next sweep's
+// divergence residual (res): u, v, w move between the fields and vel1
+// (from_vel1: from vel1 to the fields, else the other way); false when the
+// scratch cannot be allocated (the caller takes the unfused sweep)
+bool k_updvp_prcalc_divg_f32(Ctx* c, const StepParams* dp, const float* phi, const double* mean3, bool from_vel1,
+                             float* res) {
+  if (!c->vel1 && cudaMalloc(&c->vel1, 3 * c->g.cells * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    c->vel1 = nullptr;
+    return false;
+  }
+  { MIBM_PROF(c, "updvp_prcalc_divg_f32");
+    const float* mean3f = mean3 ? reinterpret_cast<const float*>(mean3 + 4) : nullptr;
+    const size_t n = c->g.cells;
+    double* const* f = c->df;
+    const double* s[3] = {f[MIBM_F_VX], f[MIBM_F_VY], f[MIBM_F_VZ]};
+    double* d[3] = {c->vel1, c->vel1 + n, c->vel1 + 2 * n};
+    if (from_vel1)
+      for (int q = 0; q < 3; ++q) { s[q] = d[q]; d[q] = f[MIBM_F_VX + q]; }
+    if (c->g.dx1 == c->g.dx2 && c->g.dx1 == c->g.dx3)
+      updvp_prcalc_divg_f32_kernel<true><<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(
+          make_args(c), dp, phi, s[0], s[1], s[2], d[0], d[1], d[2], f[MIBM_F_PR], mean3f, res);
+    else
+      updvp_prcalc_divg_f32_kernel<false><<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(
+          make_args(c), dp, phi, s[0], s[1], s[2], d[0], d[1], d[2], f[MIBM_F_PR], mean3f, res); }
+  ++c->launches;
+  MIBM_LAUNCH_CHECK(c, "updvp_prcalc_divg_f32");
+  return true;
 }
 
 void k_prcalc_f32(Ctx* c, const StepParams* dp, const float* phi, bool mirror) {

@@ -196,10 +196,11 @@ class DeviceExecutor:
 
     @staticmethod
     def model_bytes(cfg: CaseConfig, precision: int) -> int:
-        """Device footprint model: 26 FP64 fields + RHS scratch (4 FP64 or 15
-        FP32 fields in the precision form) + spectrum + reductions + mesh."""
+        """Device footprint model: 26 FP64 fields + RHS scratch (4 FP64, or 15
+        FP32 fields and the 3 FP64 velocity fields between projection sweeps
+        in the precision form) + spectrum + reductions + mesh."""
         n3 = cfg.n * cfg.n * cfg.nz
-        per_cell = 26 * 8 + (4 * 8 if precision == 0 else 15 * 4) + 8 + 16 + 16
+        per_cell = 26 * 8 + (4 * 8 if precision == 0 else 15 * 4 + 3 * 8) + 8 + 16 + 16
         nf = 20 * 4 ** cfg.mesh_level
         return int(per_cell * n3 + 4000 * nf + (64 << 20))
 
