@@ -67,18 +67,21 @@ __device__ __forceinline__ float d2f_bits(double d) {
 }
 
 // ---------------------------------------------------------------------
-// (a1 - a0) + (b1 - b0) + (c1 - c0) of six FP64 values, rounded once to
-// FP32, on the integer pipe.  Each value's 53-bit significand is shifted
-// right to the weight of the last bit of the largest input (exponent E),
-// given its sign, and the six are summed in 64-bit integers (|sum| < 2^56);
-// the sum is rounded to nearest, ties to even.  The shifts drop bits below
-// that weight only, so the result is within 6 * 2^-52 times the largest
-// |input| of the exact sum before its rounding (FP64 arithmetic: within
-// about 8 * 2^-52), and it is the correctly rounded exact sum when every
-// input is a multiple of that weight.  Zero and subnormal inputs are taken
-// with the implicit bit (below 2^-1021 in magnitude); a sum below the normal
-// FP32 range is flushed to a signed zero, one above it is infinity; an
-// infinite or NaN input gives NaN.
+// Sums of FP64 values on the integer pipe: (a1 - a0) + (b1 - b0) + (c1 - c0)
+// (sum3_diff_*) and a + b + c + d + e + f (sum6_*), rounded once to FP32 or
+// FP64.  Each value's 53-bit significand is shifted right to the weight of
+// the last bit of the largest input (exponent E), given its sign, and the
+// six are summed in 64-bit integers (|sum| < 2^56); the sum is rounded to
+// nearest, ties to even.  The shifts drop bits below that weight only, so
+// the result is within 6 * 2^-52 times the largest |input| of the exact sum
+// before its rounding (FP64 arithmetic: within about 8 * 2^-52), and it is
+// the correctly rounded exact sum when every input is a multiple of that
+// weight.  Zero and subnormal inputs are taken with the implicit bit (below
+// 2^-1021 in magnitude); a sum below the normal range of the result type is
+// flushed to a signed zero, one above it is infinity; an infinite or NaN
+// input gives NaN.  FP64 instructions issue at 1/32 of the integer rate on
+// this part, so a stencil that only adds and subtracts FP64 neighbours is
+// cheaper this way.
 // ---------------------------------------------------------------------
 __device__ __forceinline__ int fx_exp(double x) {
   return (int)(((uint32_t)((uint64_t)__double_as_longlong(x) >> 32) >> 20) & 0x7ffu);
@@ -92,14 +95,23 @@ __device__ __forceinline__ int64_t fx_aligned(double x, int sh) {
   return (int64_t)(((m >> (sh < 63 ? sh : 63)) ^ s) - s);
 }
 
-// S * 2^(E - 1075) to FP32, round to nearest even
-__device__ __forceinline__ float fx_round_f32(int64_t S, int E) {
+// |S| normalised (leading one at bit 63) with its sign and leading-zero count
+__device__ __forceinline__ uint64_t fx_norm(int64_t S, uint64_t& sign, int& lz) {
   const uint64_t s = (uint64_t)(S >> 63);
   const uint64_t A0 = ((uint64_t)S ^ s) - s;
-  if (A0 == 0) return 0.0f;
-  const uint32_t sign = (uint32_t)s & 0x80000000u;
-  const int lz = __clzll((long long)A0);
-  const uint64_t A = A0 << lz;                               // leading one at bit 63
+  sign = s & 0x8000000000000000ull;
+  lz = __clzll((long long)A0);
+  return A0 << lz;
+}
+
+// S * 2^(E - 1075) to FP32, round to nearest even (E == 0x7ff: NaN)
+__device__ __forceinline__ float fx_round_f32(int64_t S, int E) {
+  if (E == 0x7ff) return __uint_as_float(0x7fc00000u);
+  if (S == 0) return 0.0f;
+  uint64_t sg;
+  int lz;
+  const uint64_t A = fx_norm(S, sg, lz);
+  const uint32_t sign = (uint32_t)(sg >> 32);
   uint32_t q = (uint32_t)(A >> 40);                          // 24 significant bits
   const uint32_t r = (uint32_t)(A >> 39) & 1u, sticky = (uint32_t)((A & 0x7fffffffffull) != 0);
   q += r & (sticky | (q & 1u));
@@ -110,15 +122,59 @@ __device__ __forceinline__ float fx_round_f32(int64_t S, int E) {
   return __uint_as_float(sign | (bits >= 0x7f800000u ? 0x7f800000u : bits));
 }
 
-__device__ __forceinline__ float sum3_diff_f32(double a1, double a0, double b1, double b0, double c1, double c0) {
+// S * 2^(E - 1075) to FP64, round to nearest even (E == 0x7ff: NaN)
+__device__ __forceinline__ double fx_round_f64(int64_t S, int E) {
+  if (E == 0x7ff) return __longlong_as_double(0x7ff8000000000000ll);
+  if (S == 0) return 0.0;
+  uint64_t sign;
+  int lz;
+  const uint64_t A = fx_norm(S, sign, lz);
+  uint64_t q = A >> 11;                                      // 53 significant bits
+  const uint64_t r = (A >> 10) & 1u, sticky = (uint64_t)((A & 0x3ffull) != 0);
+  q += r & (sticky | (q & 1u));
+  const int ef = 63 - lz + E - 1075 + 1023;                  // biased exponent of the leading one
+  if (ef <= 0) return __longlong_as_double((long long)sign);
+  if (ef >= 2047) return __longlong_as_double((long long)(sign | 0x7ff0000000000000ull));
+  const uint64_t bits = ((uint64_t)ef << 52) + (q - 0x0010000000000000ull);
+  return __longlong_as_double((long long)(sign | (bits >= 0x7ff0000000000000ull ? 0x7ff0000000000000ull : bits)));
+}
+
+__device__ __forceinline__ int fx_max6(int a, int b, int c, int d, int e, int f) {
+  return max(max(max(a, b), max(c, d)), max(e, f));
+}
+
+__device__ __forceinline__ int64_t fx_sum3_diff(double a1, double a0, double b1, double b0, double c1, double c0,
+                                                int& E) {
   const int ea1 = fx_exp(a1), ea0 = fx_exp(a0), eb1 = fx_exp(b1), eb0 = fx_exp(b0), ec1 = fx_exp(c1),
             ec0 = fx_exp(c0);
-  const int E = max(max(max(ea1, ea0), max(eb1, eb0)), max(ec1, ec0));
-  if (E == 0x7ff) return __uint_as_float(0x7fc00000u);
-  const int64_t S = (fx_aligned(a1, E - ea1) - fx_aligned(a0, E - ea0)) +
-                    (fx_aligned(b1, E - eb1) - fx_aligned(b0, E - eb0)) +
-                    (fx_aligned(c1, E - ec1) - fx_aligned(c0, E - ec0));
+  E = fx_max6(ea1, ea0, eb1, eb0, ec1, ec0);
+  return (fx_aligned(a1, E - ea1) - fx_aligned(a0, E - ea0)) + (fx_aligned(b1, E - eb1) - fx_aligned(b0, E - eb0)) +
+         (fx_aligned(c1, E - ec1) - fx_aligned(c0, E - ec0));
+}
+
+__device__ __forceinline__ int64_t fx_sum6(double a, double b, double c, double d, double e, double f, int& E) {
+  const int ea = fx_exp(a), eb = fx_exp(b), ec = fx_exp(c), ed = fx_exp(d), ee = fx_exp(e), ef = fx_exp(f);
+  E = fx_max6(ea, eb, ec, ed, ee, ef);
+  return (fx_aligned(a, E - ea) + fx_aligned(b, E - eb)) + (fx_aligned(c, E - ec) + fx_aligned(d, E - ed)) +
+         (fx_aligned(e, E - ee) + fx_aligned(f, E - ef));
+}
+
+__device__ __forceinline__ float sum3_diff_f32(double a1, double a0, double b1, double b0, double c1, double c0) {
+  int E;
+  const int64_t S = fx_sum3_diff(a1, a0, b1, b0, c1, c0, E);
   return fx_round_f32(S, E);
+}
+
+__device__ __forceinline__ double sum3_diff_f64(double a1, double a0, double b1, double b0, double c1, double c0) {
+  int E;
+  const int64_t S = fx_sum3_diff(a1, a0, b1, b0, c1, c0, E);
+  return fx_round_f64(S, E);
+}
+
+__device__ __forceinline__ double sum6_f64(double a, double b, double c, double d, double e, double f) {
+  int E;
+  const int64_t S = fx_sum6(a, b, c, d, e, f, E);
+  return fx_round_f64(S, E);
 }
 
 // the compute type R of a templated kernel from / to FP64 (identity for FP64)

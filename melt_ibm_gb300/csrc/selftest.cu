@@ -6,9 +6,9 @@
 // random bit patterns.  The line-solve factor table evaluated on the device
 // (the allocation-free x-line solve builds it there) must equal the host's
 // evaluation bit for bit.  The written-out exp of the MLS weights (mls_exp.h)
-// must give the host's bits on the device.  The integer-pipe sum of three
-// FP64 differences (sum3_diff_f32) must give FP64 arithmetic's bits where
-// that is exact, and agree with it to its error bound elsewhere.
+// must give the host's bits on the device.  The integer-pipe sums of FP64
+// values (sum3_diff_f32/f64, sum6_f64) must give FP64 arithmetic's bits
+// where that is exact, and agree with it to their error bound elsewhere.
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
@@ -88,11 +88,12 @@ static void edge_cases(std::vector<unsigned long long>& v) {
   for (uint32_t x : fr) f(x);
 }
 
-// sum3_diff_f32 against FP64 arithmetic on n random sextuples.  Even t:
-// k * 2^s with |k| < 2^50 and one s per sextuple, where FP64 arithmetic is
-// exact, so both must give the same bits; odd t: values of random sign and
-// exponent spread over 2^-40 .. 2^40, within 2^-48 of the largest |input|
-// plus two FP32 units of the result.  bad[0] counts failures, bad[1] keeps
+// sum3_diff_f32, sum3_diff_f64 and sum6_f64 against FP64 arithmetic on n
+// random sextuples.  Even t: k * 2^s with |k| < 2^50 and one s per
+// sextuple, where FP64 arithmetic is exact, so both must give the same bits;
+// odd t: values of random sign and exponent spread over 2^-40 .. 2^40,
+// within 2^-48 (FP32: plus two units of the result) or 2^-47 (FP64) of the
+// largest |input|.  bad[0] counts failures, bad[1] keeps
 // the first t.
 __global__ void sum3_selftest_kernel(long long n, unsigned long long* __restrict__ bad) {
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
@@ -114,20 +115,28 @@ __global__ void sum3_selftest_kernel(long long n, unsigned long long* __restrict
     if ((t & 7) == 3) x[1] = x[0];                                               // exact cancellations
     if ((t & 15) == 5) { x[3] = x[2]; x[5] = x[4]; }
     const float got = sum3_diff_f32(x[0], x[1], x[2], x[3], x[4], x[5]);
+    const double got64 = sum3_diff_f64(x[0], x[1], x[2], x[3], x[4], x[5]);
+    const double six64 = sum6_f64(x[0], x[1], x[2], x[3], x[4], x[5]);
     const double fp = ((x[0] - x[1]) + (x[2] - x[3])) + (x[4] - x[5]);
+    const double fp6 = ((x[0] + x[1]) + (x[2] + x[3])) + (x[4] + x[5]);
     bool ok;
     if ((t & 1) == 0) {
-      ok = __float_as_uint(got) == __float_as_uint(d2f_bits(fp));
+      ok = __float_as_uint(got) == __float_as_uint(d2f_bits(fp)) && same_d(got64, fp) && same_d(six64, fp6);
     } else {
       const float ref = d2f_bits(fp);
       const double ulp = ldexp(1.0, ilogb(fmax(fabs((double)ref), fabs((double)got)) + 1e-300) - 23);
       ok = fabs((double)got - (double)ref) <= ldexp(amax, -48) + 2.0 * ulp;
+      // FP64 results: both within 8 * 2^-52 of the largest |input| of the
+      // exact sum (truncations and the final rounding; FP64 arithmetic's five
+      // roundings), so within 2^-47 of each other
+      ok = ok && fabs(got64 - fp) <= ldexp(amax, -47) && fabs(six64 - fp6) <= ldexp(amax, -47);
     }
     if (t == 0) {          // equal pairs give +0; an infinity or a NaN gives NaN
       const double inf = __longlong_as_double(0x7ff0000000000000ll), nan = __longlong_as_double(0x7ff8000000000000ll);
       const float z = sum3_diff_f32(1.5, 1.5, -2.0, -2.0, 0.0, 0.0);
       const float a = sum3_diff_f32(inf, 1.0, 0.0, 0.0, 0.0, 0.0), b = sum3_diff_f32(1.0, 1.0, 2.0, nan, 0.0, 0.0);
-      ok = ok && __float_as_uint(z) == 0u && a != a && b != b;
+      const double z64 = sum3_diff_f64(1.5, 1.5, -2.0, -2.0, 0.0, 0.0), a64 = sum6_f64(inf, 1.0, 0.0, 0.0, 0.0, 0.0);
+      ok = ok && __float_as_uint(z) == 0u && a != a && b != b && __double_as_longlong(z64) == 0ll && a64 != a64;
     }
     if (!ok && atomicAdd(&bad[0], 1ull) == 0) bad[1] = (unsigned long long)t;
   }
@@ -144,7 +153,7 @@ static long long sum3_selftest() {
   }
   cudaFree(d);
   if (!ok) { cudaGetLastError(); return -1; }
-  if (h[0]) fprintf(stderr, "mibm_selftest_: sum3_diff_f32 fails at %llu sextuples (first t = %llu)\n", h[0], h[1]);
+  if (h[0]) fprintf(stderr, "mibm_selftest_: the integer-pipe sums fail at %llu sextuples (first t = %llu)\n", h[0], h[1]);
   return (long long)h[0];
 }
 

@@ -325,11 +325,20 @@ __global__ void hdnl_kernel(StencilArgs A, int which, const StepParams* __restri
 // Diffusion term of the RHS with its factor folded into the coefficients:
 // sum_d L_d*(q[+d] - 2 q + q[-d]) = sum_d L_d*(q[+d] + q[-d]) - LC*q,
 // L_d = al/ren*dt*dxq_d (or al/pec*dt*dxq_d) and LC = 2*(L1 + L2 + L3).
-template <typename R>
+// ISO (FP64, equal grid spacings, L1 = L2 = L3): the six neighbours summed in
+// 64-bit integers on the integer pipe and rounded once (sum6_f64), two FP64
+// operations per cell instead of seven, within FP64 round-off of the
+// reference's order.
+template <typename R, bool ISO = false>
 __device__ __forceinline__ R lap_dt(const R* q, idx_t c0, idx_t dip, idx_t dim, idx_t djp, idx_t djm,
                                     idx_t dkp, idx_t dkm, R L1, R L2, R L3, R LC) {
-  R s = L1 * (q[c0 + dip] + q[c0 + dim]) + L2 * (q[c0 + djp] + q[c0 + djm]) + L3 * (q[c0 + dkp] + q[c0 + dkm]);
-  return s - LC * q[c0];
+  if constexpr (ISO && sizeof(R) == 8) {
+    const R s = L1 * sum6_f64(q[c0 + dip], q[c0 + dim], q[c0 + djp], q[c0 + djm], q[c0 + dkp], q[c0 + dkm]);
+    return s - LC * q[c0];
+  } else {
+    R s = L1 * (q[c0 + dip] + q[c0 + dim]) + L2 * (q[c0 + djp] + q[c0 + djm]) + L3 * (q[c0 + dkp] + q[c0 + dkm]);
+    return s - LC * q[c0];
+  }
 }
 
 // rhs = dt*(ga*H + ro*ru + al/ren*lap(u) - al*grad p) (invtr1.f90:57-60 and
@@ -338,21 +347,21 @@ __device__ __forceinline__ R lap_dt(const R* q, idx_t c0, idx_t dip, idx_t dim, 
 // dt and the substep coefficients formed once per substep on the host: the
 // same value up to rounding, with 11 (velocity) or 9 (temperature) FP64
 // operations per cell instead of 18 and 17.
-template <typename R>
+template <typename R, bool ISO = false>
 __device__ __forceinline__ R rhs_value(const StencilArgs& A, int which, R h, R ru, idx_t c0, idx_t dip,
                                        idx_t dim, idx_t djp, idx_t djm, idx_t dkp, idx_t dkm,
                                        const StepParams& p) {
   const Prog<R> F = prog<R>(A);
   const R gdt = coef<R>(p, kGDT), rdt = coef<R>(p, kRDT);
   if (which == 3) {
-    R d = lap_dt<R>(F.t, c0, dip, dim, djp, djm, dkp, dkm, coef<R>(p, kLT1), coef<R>(p, kLT2),
+    R d = lap_dt<R, ISO>(F.t, c0, dip, dim, djp, djm, dkp, dkm, coef<R>(p, kLT1), coef<R>(p, kLT2),
                     coef<R>(p, kLT3), coef<R>(p, kLTC));
     return gdt * h + (rdt * ru + d);
   }
   const R* q = which == 0 ? F.u : (which == 1 ? F.v : F.w);
   const idx_t dpm = which == 0 ? dim : (which == 1 ? djm : dkm);
   const R pd = coef<R>(p, which == 0 ? kPD1 : (which == 1 ? kPD2 : kPD3));
-  R d = lap_dt<R>(q, c0, dip, dim, djp, djm, dkp, dkm, coef<R>(p, kLV1), coef<R>(p, kLV2), coef<R>(p, kLV3),
+  R d = lap_dt<R, ISO>(q, c0, dip, dim, djp, djm, dkp, dkm, coef<R>(p, kLV1), coef<R>(p, kLV2), coef<R>(p, kLV3),
                   coef<R>(p, kLVC));
   return gdt * h + (rdt * ru + (d - pd * (F.p[c0] - F.p[c0 + dpm])));
 }
@@ -369,8 +378,9 @@ __global__ void invtr_rhs_kernel(StencilArgs A, int which, const StepParams* __r
 
 // fused path: explicit term computed in registers (hdnl + invtr RHS); R is
 // the compute type, ru and rhs are stored in R
-// (one instance per component W, so each carries only its own stencil)
-template <typename R, int W>
+// (one instance per component W, so each carries only its own stencil; ISO:
+// the FP64 diffusion sum of lap_dt on the integer pipe)
+template <typename R, int W, bool ISO = false>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 3)
 fused_rhs_kernel(StencilArgs A, const StepParams* __restrict__ pp, R* __restrict__ ru, R* __restrict__ rhs) {
   CELL_INDEX
@@ -378,7 +388,7 @@ fused_rhs_kernel(StencilArgs A, const StepParams* __restrict__ pp, R* __restrict
   R h;
   if (W < 3) h = h_prod<R>(A, W, c0, dip, dim, djp, djm, dkp, dkm, p);    // products of adv_products_kernel
   else h = h_t<R>(A, i, j, k, c0, dip, dim, djp, djm, dkp, dkm, p);
-  rhs[c0] = rhs_value<R>(A, W, h, ru[c0], c0, dip, dim, djp, djm, dkp, dkm, p);
+  rhs[c0] = rhs_value<R, ISO>(A, W, h, ru[c0], c0, dip, dim, djp, djm, dkp, dkm, p);
   ru[c0] = h;
 }
 
@@ -500,17 +510,27 @@ fused_t_f32_kernel(StencilArgs A, const StepParams* __restrict__ pp, float* __re
   ru[c0] = h;
 }
 
-template <typename R>
-static void fused_rhs_launch(Ctx* c, const StepParams* dp, int w, R* ru, R* rhs) {
+static bool equal_spacings(const Grid& g) { return g.dx1 == g.dx2 && g.dx1 == g.dx3; }
+
+template <typename R, bool ISO>
+static void fused_rhs_launch_by(Ctx* c, const StepParams* dp, int w, R* ru, R* rhs) {
   const int by = (c->tune_by == 2 || c->tune_by == 4) ? c->tune_by : 8;   // autotuned block height
   dim3 grid(div_up(c->g.n1m, 32), div_up(c->g.n2m, by), c->g.n3m), block(32, by);
   StencilArgs a = make_args(c);
   switch (w) {
-    case 0: fused_rhs_kernel<R, 0><<<grid, block, 0, c->stream>>>(a, dp, ru, rhs); break;
-    case 1: fused_rhs_kernel<R, 1><<<grid, block, 0, c->stream>>>(a, dp, ru, rhs); break;
-    case 2: fused_rhs_kernel<R, 2><<<grid, block, 0, c->stream>>>(a, dp, ru, rhs); break;
-    default: fused_rhs_kernel<R, 3><<<grid, block, 0, c->stream>>>(a, dp, ru, rhs); break;
+    case 0: fused_rhs_kernel<R, 0, ISO><<<grid, block, 0, c->stream>>>(a, dp, ru, rhs); break;
+    case 1: fused_rhs_kernel<R, 1, ISO><<<grid, block, 0, c->stream>>>(a, dp, ru, rhs); break;
+    case 2: fused_rhs_kernel<R, 2, ISO><<<grid, block, 0, c->stream>>>(a, dp, ru, rhs); break;
+    default: fused_rhs_kernel<R, 3, ISO><<<grid, block, 0, c->stream>>>(a, dp, ru, rhs); break;
   }
+}
+
+// FP64 with equal spacings: the diffusion sums on the integer pipe; the FP32
+// instances keep the FP32 arithmetic (one-pass kernels give their bits)
+template <typename R>
+static void fused_rhs_launch(Ctx* c, const StepParams* dp, int w, R* ru, R* rhs) {
+  if (sizeof(R) == 8 && equal_spacings(c->g)) fused_rhs_launch_by<R, true>(c, dp, w, ru, rhs);
+  else fused_rhs_launch_by<R, false>(c, dp, w, ru, rhs);
 }
 
 static void fused_uvw_launch(Ctx* c, const StepParams* dp, float* ru4, float* rhs4) {
@@ -528,12 +548,22 @@ static void fused_t_launch(Ctx* c, const StepParams* dp, float* ru, float* rhs) 
 // ---------------------------------------------------------------------
 // projection stencils
 // ---------------------------------------------------------------------
+// divg.f90: dph = div(u) / (dt al).  ISO (equal grid spacings): the sum of
+// the three face differences formed in 64-bit integers on the integer pipe
+// and rounded once (sum3_diff_f64), times dx1/(dt al): one FP64 operation
+// per cell instead of six, within FP64 round-off of the reference's order.
+template <bool ISO>
 __global__ void divg_kernel(StencilArgs A, const StepParams* __restrict__ pp, double* __restrict__ dph) {
   CELL_INDEX
-  double usdtal = pp->cd[kUSDTAL];
-  double dq = (A.vx[c0 + dip] - A.vx[c0]) * g.dx1 + (A.vy[c0 + djp] - A.vy[c0]) * g.dx2 +
-              (A.vz[c0 + dkp] - A.vz[c0]) * g.dx3;
-  dph[c0] = dq * usdtal;
+  if constexpr (ISO) {
+    dph[c0] = sum3_diff_f64(A.vx[c0 + dip], A.vx[c0], A.vy[c0 + djp], A.vy[c0], A.vz[c0 + dkp], A.vz[c0]) *
+              pp->cd[kDVI];
+  } else {
+    double usdtal = pp->cd[kUSDTAL];
+    double dq = (A.vx[c0 + dip] - A.vx[c0]) * g.dx1 + (A.vy[c0 + djp] - A.vy[c0]) * g.dx2 +
+                (A.vz[c0 + dkp] - A.vz[c0]) * g.dx3;
+    dph[c0] = dq * usdtal;
+  }
 }
 
 // precision form: the divergence residual of the FP64 velocity, formed at
@@ -727,6 +757,11 @@ __global__ void prcalc_kernel(StencilArgs A, const StepParams* __restrict__ pp, 
 
 // updvp then prcalc of the same substep in one pass (the fused step): both
 // read phi and write disjoint fields; each keeps its own operation order
+// ISO (equal grid spacings): the six neighbours of the pressure update's
+// Laplacian summed in 64-bit integers on the integer pipe (sum6_f64) and
+// scaled once: three FP64 operations for the pressure instead of eight,
+// within FP64 round-off of the reference's order (prcalc.f90)
+template <bool ISO>
 __global__ void updvp_prcalc_kernel(StencilArgs A, const StepParams* __restrict__ pp, const double* __restrict__ dph,
                                     double* __restrict__ vx, double* __restrict__ vy, double* __restrict__ vz,
                                     const double* __restrict__ mean3, double* __restrict__ pr) {
@@ -734,13 +769,15 @@ __global__ void updvp_prcalc_kernel(StencilArgs A, const StepParams* __restrict_
   const double udx1 = pp->cd[kUP1], udx2 = pp->cd[kUP2], udx3 = pp->cd[kUP3];
   const double d = dph[c0];
   const double pim = dph[c0 + dim], pjm = dph[c0 + djm], pkm = dph[c0 + dkm];
+  const double pip = dph[c0 + dip], pjp = dph[c0 + djp], pkp = dph[c0 + dkp];
   double mx = 0.0, my = 0.0, mz = 0.0;
   if (mean3) { mx = mean3[0]; my = mean3[1]; mz = mean3[2]; }
   vx[c0] = (vx[c0] - mx) - (d - pim) * udx1;
   vy[c0] = (vy[c0] - my) - (d - pjm) * udx2;
   vz[c0] = (vz[c0] - mz) - (d - pkm) * udx3;
-  const double t = pp->cd[kPB1] * (dph[c0 + dip] + pim) + pp->cd[kPB2] * (dph[c0 + djp] + pjm) +
-                   pp->cd[kPB3] * (dph[c0 + dkp] + pkm);
+  double t;
+  if constexpr (ISO) t = pp->cd[kPB1] * sum6_f64(pip, pim, pjp, pjm, pkp, pkm);
+  else t = pp->cd[kPB1] * (pip + pim) + pp->cd[kPB2] * (pjp + pjm) + pp->cd[kPB3] * (pkp + pkm);
   pr[c0] = (pr[c0] + pp->cd[kPBC] * d) - t;
 }
 
@@ -1017,7 +1054,11 @@ void k_fused_rhs_f32(Ctx* c, const StepParams* dp, float* ru4, float* rhs4) {
 }
 
 void k_divg(Ctx* c, const StepParams* dp) {
-  { MIBM_PROF(c, "divg"); divg_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, c->df[MIBM_F_DPH]); }
+  { MIBM_PROF(c, "divg");
+    if (equal_spacings(c->g))
+      divg_kernel<true><<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, c->df[MIBM_F_DPH]);
+    else
+      divg_kernel<false><<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, c->df[MIBM_F_DPH]); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "divg");
 }
@@ -1138,9 +1179,10 @@ void k_divmax(Ctx* c, unsigned long long* out) {
 
 void k_updvp_prcalc(Ctx* c, const StepParams* dp, const double* mean3) {
   { MIBM_PROF(c, "updvp_prcalc");
-    updvp_prcalc_kernel<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, c->df[MIBM_F_DPH],
-                                                                        c->df[MIBM_F_VX], c->df[MIBM_F_VY],
-                                                                        c->df[MIBM_F_VZ], mean3, c->df[MIBM_F_PR]); }
+    auto kern = equal_spacings(c->g) ? updvp_prcalc_kernel<true> : updvp_prcalc_kernel<false>;
+    kern<<<cell_grid(c->g), kCellBlock, 0, c->stream>>>(make_args(c), dp, c->df[MIBM_F_DPH], c->df[MIBM_F_VX],
+                                                         c->df[MIBM_F_VY], c->df[MIBM_F_VZ], mean3,
+                                                         c->df[MIBM_F_PR]); }
   ++c->launches;
   MIBM_LAUNCH_CHECK(c, "updvp_prcalc");
 }
