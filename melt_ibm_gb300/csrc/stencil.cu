@@ -241,7 +241,11 @@ __global__ void adv_products_kernel(StencilArgs A, R* __restrict__ out) {
   out[5 * n + c0] = (wc + w[c0 + djm]) * (vc + v[c0 + dkm]);
 }
 
-template <typename R>
+// ISO (FP64, equal grid spacings, udx1 = udx2 = udx3): the three
+// differences summed in 64-bit integers on the integer pipe and rounded once
+// (sum3_diff_f64), one FP64 operation instead of six, within FP64 round-off
+// of the reference's order
+template <typename R, bool ISO = false>
 __device__ __forceinline__ R h_prod(const StencilArgs& A, int W, idx_t c0, idx_t dip, idx_t dim, idx_t djp,
                                     idx_t djm, idx_t dkp, idx_t dkm, const StepParams& p) {
   const Prog<R> F = prog<R>(A);
@@ -250,6 +254,21 @@ __device__ __forceinline__ R h_prod(const StencilArgs& A, int W, idx_t c0, idx_t
   const R* E = F.pd + 3 * n; const R* Fx = F.pd + 4 * n; const R* H = F.pd + 5 * n;
   const R udx1 = coef<R>(p, kQ1), udx2 = coef<R>(p, kQ2), udx3 = coef<R>(p, kQ3);
   R h;
+  if constexpr (ISO && sizeof(R) == 8) {
+    if (W == 0) h = -(udx1 * sum3_diff_f64(Pc[c0], Pc[c0 + dim], E[c0 + djp], E[c0], Fx[c0 + dkp], Fx[c0]));
+    else if (W == 1) h = -(udx1 * sum3_diff_f64(E[c0 + dip], E[c0], Qc[c0], Qc[c0 + djm], H[c0 + dkp], H[c0]));
+    else h = -(udx1 * sum3_diff_f64(Fx[c0 + dip], Fx[c0], H[c0 + djp], H[c0], Rc[c0], Rc[c0 + dkm]));
+    if (W == 2 && p.betagz != 0.0) {
+      R T_interp = (F.t[c0] + F.t[c0 + dkm]) * R(0.5);
+      h = h + coef<R>(p, kBETAGZ) * (T_interp - coef<R>(p, kTLIQ));
+    }
+    if (A.forcing) {
+      if (W == 0) h = add_forcing<R>(h, A.vofx, A.forcx, c0, coef<R>(p, kRXLEN));
+      else if (W == 1) h = add_forcing<R>(h, A.vofy, A.forcy, c0, coef<R>(p, kRYLEN));
+      else h = add_forcing<R>(h, A.vofz, A.forcz, c0, coef<R>(p, kRZLEN));
+    }
+    return h;
+  }
   if (W == 0) {
     h = -(udx1 * (Pc[c0] - Pc[c0 + dim]) + udx2 * (E[c0 + djp] - E[c0]) + udx3 * (Fx[c0 + dkp] - Fx[c0]));
     if (A.forcing) h = add_forcing<R>(h, A.vofx, A.forcx, c0, coef<R>(p, kRXLEN));
@@ -379,14 +398,15 @@ __global__ void invtr_rhs_kernel(StencilArgs A, int which, const StepParams* __r
 // fused path: explicit term computed in registers (hdnl + invtr RHS); R is
 // the compute type, ru and rhs are stored in R
 // (one instance per component W, so each carries only its own stencil; ISO:
-// the FP64 diffusion sum of lap_dt on the integer pipe)
+// the FP64 advection differences of h_prod and the diffusion sum of lap_dt
+// on the integer pipe)
 template <typename R, int W, bool ISO = false>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 3)
 fused_rhs_kernel(StencilArgs A, const StepParams* __restrict__ pp, R* __restrict__ ru, R* __restrict__ rhs) {
   CELL_INDEX
   const StepParams& p = *pp;
   R h;
-  if (W < 3) h = h_prod<R>(A, W, c0, dip, dim, djp, djm, dkp, dkm, p);    // products of adv_products_kernel
+  if (W < 3) h = h_prod<R, ISO>(A, W, c0, dip, dim, djp, djm, dkp, dkm, p);   // products of adv_products_kernel
   else h = h_t<R>(A, i, j, k, c0, dip, dim, djp, djm, dkp, dkm, p);
   rhs[c0] = rhs_value<R, ISO>(A, W, h, ru[c0], c0, dip, dim, djp, djm, dkp, dkm, p);
   ru[c0] = h;
@@ -525,7 +545,8 @@ static void fused_rhs_launch_by(Ctx* c, const StepParams* dp, int w, R* ru, R* r
   }
 }
 
-// FP64 with equal spacings: the diffusion sums on the integer pipe; the FP32
+// FP64 with equal spacings: the advection and diffusion sums on the integer
+// pipe; the FP32
 // instances keep the FP32 arithmetic (one-pass kernels give their bits)
 template <typename R>
 static void fused_rhs_launch(Ctx* c, const StepParams* dp, int w, R* ru, R* rhs) {
