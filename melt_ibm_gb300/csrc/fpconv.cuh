@@ -68,29 +68,40 @@ __device__ __forceinline__ float d2f_bits(double d) {
 
 // ---------------------------------------------------------------------
 // Sums of FP64 values on the integer pipe: (a1 - a0) + (b1 - b0) + (c1 - c0)
-// (sum3_diff_*) and a + b + c + d + e + f (sum6_*), rounded once to FP32 or
-// FP64.  Each value's 53-bit significand is shifted right to the weight of
+// (sum3_diff_*), a + b + c + d + e + f (sum6_*), |a1 + a0| + |b1 + b0| +
+// |c1 + c0| (sum3_abs_pair_f64) and |a| + |b| + |c| (sum3_abs_f64), rounded
+// once to FP32 or FP64.  Each value's 53-bit significand is shifted right to the weight of
 // the last bit of the largest input (exponent E), given its sign, and the
 // six are summed in 64-bit integers (|sum| < 2^56); the sum is rounded to
 // nearest, ties to even.  The shifts drop bits below that weight only, so
 // the result is within 6 * 2^-52 times the largest |input| of the exact sum
 // before its rounding (FP64 arithmetic: within about 8 * 2^-52), and it is
 // the correctly rounded exact sum when every input is a multiple of that
-// weight.  Zero and subnormal inputs are taken with the implicit bit (below
-// 2^-1021 in magnitude); a sum below the normal range of the result type is
-// flushed to a signed zero, one above it is infinity; an infinite or NaN
-// input gives NaN.  FP64 instructions issue at 1/32 of the integer rate on
+// weight (zeros and subnormals included; in the difference form a zero or a
+// subnormal counts as a value below 2^-1021 unless it cancels); a sum below
+// the normal range of the result type is flushed to a signed zero, one above
+// it is infinity; an infinite or NaN input gives NaN.  FP64 instructions issue at 1/32 of the integer rate on
 // this part, so a stencil that only adds and subtracts FP64 neighbours is
 // cheaper this way.
 // ---------------------------------------------------------------------
+// the exponent field; EXACT0: 1 for zero and subnormals (their weight)
+template <bool EXACT0 = true>
 __device__ __forceinline__ int fx_exp(double x) {
-  return (int)(((uint32_t)((uint64_t)__double_as_longlong(x) >> 32) >> 20) & 0x7ffu);
+  const int e = (int)(((uint32_t)((uint64_t)__double_as_longlong(x) >> 32) >> 20) & 0x7ffu);
+  if constexpr (EXACT0) return e > 0 ? e : 1;
+  return e;
 }
 
-// x's significand (with the implicit bit) shifted right by sh >= 0, signed
+// x's significand shifted right by sh >= 0, signed.  EXACT0: the implicit
+// bit for normal x only; otherwise for every x, which takes a zero or a
+// subnormal as a value below 2^-1021 -- exact enough where such inputs come
+// in pairs that cancel or beside normal values that shift them out (the
+// difference forms), and two operations cheaper
+template <bool EXACT0 = true>
 __device__ __forceinline__ int64_t fx_aligned(double x, int sh) {
   const uint64_t b = (uint64_t)__double_as_longlong(x);
-  const uint64_t m = (b & 0x000fffffffffffffull) | 0x0010000000000000ull;
+  uint64_t m = (b & 0x000fffffffffffffull) | 0x0010000000000000ull;
+  if constexpr (EXACT0) m = (b & 0x7ff0000000000000ull) ? m : (b & 0x000fffffffffffffull);
   const uint64_t s = (uint64_t)((int64_t)b >> 63);           // 0 or all ones
   return (int64_t)(((m >> (sh < 63 ? sh : 63)) ^ s) - s);
 }
@@ -143,13 +154,16 @@ __device__ __forceinline__ int fx_max6(int a, int b, int c, int d, int e, int f)
   return max(max(max(a, b), max(c, d)), max(e, f));
 }
 
+// the difference form: equal inputs cancel exactly whatever their decoding,
+// so zeros take the cheaper one
 __device__ __forceinline__ int64_t fx_sum3_diff(double a1, double a0, double b1, double b0, double c1, double c0,
                                                 int& E) {
-  const int ea1 = fx_exp(a1), ea0 = fx_exp(a0), eb1 = fx_exp(b1), eb0 = fx_exp(b0), ec1 = fx_exp(c1),
-            ec0 = fx_exp(c0);
+  const int ea1 = fx_exp<false>(a1), ea0 = fx_exp<false>(a0), eb1 = fx_exp<false>(b1), eb0 = fx_exp<false>(b0),
+            ec1 = fx_exp<false>(c1), ec0 = fx_exp<false>(c0);
   E = fx_max6(ea1, ea0, eb1, eb0, ec1, ec0);
-  return (fx_aligned(a1, E - ea1) - fx_aligned(a0, E - ea0)) + (fx_aligned(b1, E - eb1) - fx_aligned(b0, E - eb0)) +
-         (fx_aligned(c1, E - ec1) - fx_aligned(c0, E - ec0));
+  return (fx_aligned<false>(a1, E - ea1) - fx_aligned<false>(a0, E - ea0)) +
+         (fx_aligned<false>(b1, E - eb1) - fx_aligned<false>(b0, E - eb0)) +
+         (fx_aligned<false>(c1, E - ec1) - fx_aligned<false>(c0, E - ec0));
 }
 
 __device__ __forceinline__ int64_t fx_sum6(double a, double b, double c, double d, double e, double f, int& E) {
@@ -157,6 +171,32 @@ __device__ __forceinline__ int64_t fx_sum6(double a, double b, double c, double 
   E = fx_max6(ea, eb, ec, ed, ee, ef);
   return (fx_aligned(a, E - ea) + fx_aligned(b, E - eb)) + (fx_aligned(c, E - ec) + fx_aligned(d, E - ed)) +
          (fx_aligned(e, E - ee) + fx_aligned(f, E - ef));
+}
+
+// |a1 + a0| + |b1 + b0| + |c1 + c0| (each pair summed exactly, then its
+// magnitude), rounded once to FP64
+__device__ __forceinline__ double sum3_abs_pair_f64(double a1, double a0, double b1, double b0, double c1,
+                                                    double c0) {
+  const int ea1 = fx_exp(a1), ea0 = fx_exp(a0), eb1 = fx_exp(b1), eb0 = fx_exp(b0), ec1 = fx_exp(c1),
+            ec0 = fx_exp(c0);
+  const int E = fx_max6(ea1, ea0, eb1, eb0, ec1, ec0);
+  int64_t sa = fx_aligned(a1, E - ea1) + fx_aligned(a0, E - ea0);
+  int64_t sb = fx_aligned(b1, E - eb1) + fx_aligned(b0, E - eb0);
+  int64_t sc = fx_aligned(c1, E - ec1) + fx_aligned(c0, E - ec0);
+  sa = sa < 0 ? -sa : sa;
+  sb = sb < 0 ? -sb : sb;
+  sc = sc < 0 ? -sc : sc;
+  return fx_round_f64(sa + sb + sc, E);
+}
+
+// |a| + |b| + |c|, rounded once to FP64
+__device__ __forceinline__ double sum3_abs_f64(double a, double b, double c) {
+  const double x = __longlong_as_double(__double_as_longlong(a) & 0x7fffffffffffffffll);
+  const double y = __longlong_as_double(__double_as_longlong(b) & 0x7fffffffffffffffll);
+  const double z = __longlong_as_double(__double_as_longlong(c) & 0x7fffffffffffffffll);
+  const int ex = fx_exp(x), ey = fx_exp(y), ez = fx_exp(z);
+  const int E = max(max(ex, ey), ez);
+  return fx_round_f64(fx_aligned(x, E - ex) + fx_aligned(y, E - ey) + fx_aligned(z, E - ez), E);
 }
 
 __device__ __forceinline__ float sum3_diff_f32(double a1, double a0, double b1, double b0, double c1, double c0) {

@@ -7,7 +7,7 @@
 // (the allocation-free x-line solve builds it there) must equal the host's
 // evaluation bit for bit.  The written-out exp of the MLS weights (mls_exp.h)
 // must give the host's bits on the device.  The integer-pipe sums of FP64
-// values (sum3_diff_f32/f64, sum6_f64) must give FP64 arithmetic's bits
+// values (sum3_diff_f32/f64, sum6_f64, sum3_abs_pair_f64, sum3_abs_f64) must give FP64 arithmetic's bits
 // where that is exact, and agree with it to their error bound elsewhere.
 #include <algorithm>
 #include <cstdio>
@@ -88,8 +88,8 @@ static void edge_cases(std::vector<unsigned long long>& v) {
   for (uint32_t x : fr) f(x);
 }
 
-// sum3_diff_f32, sum3_diff_f64 and sum6_f64 against FP64 arithmetic on n
-// random sextuples.  Even t: k * 2^s with |k| < 2^50 and one s per
+// sum3_diff_f32, sum3_diff_f64, sum6_f64, sum3_abs_pair_f64 and sum3_abs_f64
+// against FP64 arithmetic on n random sextuples.  Even t: k * 2^s with |k| < 2^50 and one s per
 // sextuple, where FP64 arithmetic is exact, so both must give the same bits;
 // odd t: values of random sign and exponent spread over 2^-40 .. 2^40,
 // within 2^-48 (FP32: plus two units of the result) or 2^-47 (FP64) of the
@@ -119,9 +119,14 @@ __global__ void sum3_selftest_kernel(long long n, unsigned long long* __restrict
     const double six64 = sum6_f64(x[0], x[1], x[2], x[3], x[4], x[5]);
     const double fp = ((x[0] - x[1]) + (x[2] - x[3])) + (x[4] - x[5]);
     const double fp6 = ((x[0] + x[1]) + (x[2] + x[3])) + (x[4] + x[5]);
+    const double ap64 = sum3_abs_pair_f64(x[0], x[1], x[2], x[3], x[4], x[5]);
+    const double fpap = (fabs(x[0] + x[1]) + fabs(x[2] + x[3])) + fabs(x[4] + x[5]);
+    const double a364 = sum3_abs_f64(x[0], x[2], x[4]);
+    const double fpa3 = (fabs(x[0]) + fabs(x[2])) + fabs(x[4]);
     bool ok;
     if ((t & 1) == 0) {
-      ok = __float_as_uint(got) == __float_as_uint(d2f_bits(fp)) && same_d(got64, fp) && same_d(six64, fp6);
+      ok = __float_as_uint(got) == __float_as_uint(d2f_bits(fp)) && same_d(got64, fp) && same_d(six64, fp6) &&
+           same_d(ap64, fpap) && same_d(a364, fpa3);
     } else {
       const float ref = d2f_bits(fp);
       const double ulp = ldexp(1.0, ilogb(fmax(fabs((double)ref), fabs((double)got)) + 1e-300) - 23);
@@ -129,14 +134,23 @@ __global__ void sum3_selftest_kernel(long long n, unsigned long long* __restrict
       // FP64 results: both within 8 * 2^-52 of the largest |input| of the
       // exact sum (truncations and the final rounding; FP64 arithmetic's five
       // roundings), so within 2^-47 of each other
-      ok = ok && fabs(got64 - fp) <= ldexp(amax, -47) && fabs(six64 - fp6) <= ldexp(amax, -47);
+      ok = ok && fabs(got64 - fp) <= ldexp(amax, -47) && fabs(six64 - fp6) <= ldexp(amax, -47) &&
+           fabs(ap64 - fpap) <= ldexp(amax, -47) && fabs(a364 - fpa3) <= ldexp(amax, -47);
     }
-    if (t == 0) {          // equal pairs give +0; an infinity or a NaN gives NaN
+    if (t == 0) {          // equal pairs give +0; an infinity or a NaN gives NaN; zeros
       const double inf = __longlong_as_double(0x7ff0000000000000ll), nan = __longlong_as_double(0x7ff8000000000000ll);
       const float z = sum3_diff_f32(1.5, 1.5, -2.0, -2.0, 0.0, 0.0);
       const float a = sum3_diff_f32(inf, 1.0, 0.0, 0.0, 0.0, 0.0), b = sum3_diff_f32(1.0, 1.0, 2.0, nan, 0.0, 0.0);
       const double z64 = sum3_diff_f64(1.5, 1.5, -2.0, -2.0, 0.0, 0.0), a64 = sum6_f64(inf, 1.0, 0.0, 0.0, 0.0, 0.0);
       ok = ok && __float_as_uint(z) == 0u && a != a && b != b && __double_as_longlong(z64) == 0ll && a64 != a64;
+      // zeros contribute nothing; a sum below the normal range is flushed to zero
+      const double sub = __longlong_as_double(3ll);                     // 3 * 2^-1074
+      ok = ok && __double_as_longlong(sum6_f64(0.0, 0.0, 0.0, 0.0, 0.0, 0.0)) == 0ll &&
+           __double_as_longlong(sum3_abs_pair_f64(0.0, 0.0, 0.0, 0.0, 0.0, 0.0)) == 0ll &&
+           __double_as_longlong(sum3_abs_f64(0.0, -0.0, 0.0)) == 0ll &&
+           __float_as_uint(sum3_diff_f32(0.0, 0.0, 0.0, 0.0, 0.0, 0.0)) == 0u &&
+           sum6_f64(1.0, 0.0, 0.0, 0.0, 0.0, 0.0) == 1.0 && sum3_abs_f64(-2.5, 0.0, 0.0) == 2.5 &&
+           sum6_f64(sub, sub, 0.0, 0.0, 0.0, 0.0) == 0.0 && sum3_diff_f64(1.0, sub, 0.0, 0.0, 0.0, 0.0) == 1.0;
     }
     if (!ok && atomicAdd(&bad[0], 1ull) == 0) bad[1] = (unsigned long long)t;
   }

@@ -854,8 +854,11 @@ __device__ __forceinline__ double warp_max(double v) {
 // cfl.f90:11-26: i+1, j+1, k+1 are not wrapped -- column n1 / row n2 are the
 // stored padding values, plane n3m+1 is the periodic ghost.
 // R = float: the precision form on the FP32 mirrors (dt only sets the step
-// size; the FP32 maximum is rounded up to double unchanged)
-template <typename R>
+// size; the FP32 maximum is rounded up to double unchanged).  ISO (FP64,
+// equal spacings): the three magnitudes summed on the integer pipe
+// (sum3_abs_pair_f64) and scaled once, within FP64 round-off of cfl.f90's
+// order, one FP64 operation per cell instead of eight.
+template <typename R, bool ISO = false>
 __global__ void cfl_kernel(StencilArgs A, const double* __restrict__ padx, const double* __restrict__ pady,
                            double* __restrict__ part, int* __restrict__ nonfinite) {
   const Grid& g = A.g;
@@ -872,7 +875,9 @@ __global__ void cfl_kernel(StencilArgs A, const double* __restrict__ padx, const
     R vzp = F.w[cidx(g, i, j, (k + 1 == g.n3m) ? 0 : k + 1)];
     // (x*0.5)*dx of cfl.f90 equals x*(0.5*dx) bit for bit (scaling by 0.5 is
     // exact), so the FP64 value is the reference's with one multiply less
-    R qcf = fabs((F.u[c0] + vxp) * h1) + fabs((F.v[c0] + vyp) * h2) + fabs((F.w[c0] + vzp) * h3);
+    R qcf;
+    if constexpr (ISO && sizeof(R) == 8) qcf = sum3_abs_pair_f64(F.u[c0], vxp, F.v[c0], vyp, F.w[c0], vzp) * h1;
+    else qcf = fabs((F.u[c0] + vxp) * h1) + fabs((F.v[c0] + vyp) * h2) + fabs((F.w[c0] + vzp) * h3);
     // a max would drop a NaN: a non-finite velocity or temperature raises the guard
     if (bits_nonfinite(qcf) || bits_nonfinite(F.t[c0])) atomicOr(nonfinite, 1);
     mr = max_nonneg(mr, qcf);
@@ -888,8 +893,10 @@ __global__ void cfl_kernel(StencilArgs A, const double* __restrict__ padx, const
   }
 }
 
-// get_dt advective term: max(|u| dt dx1 + |v| dt dx2 + |w| dt dx3)
-template <typename R>
+// get_dt advective term: max(|u| dt dx1 + |v| dt dx2 + |w| dt dx3); ISO
+// (FP64, equal spacings): (|u| + |v| + |w|) on the integer pipe
+// (sum3_abs_f64) times dt dx1, within FP64 round-off of the reference's order
+template <typename R, bool ISO = false>
 __global__ void getdt_kernel(StencilArgs A, double dt, double* __restrict__ part) {
   const Grid& g = A.g;
   const Prog<R> F = prog<R>(A);
@@ -900,7 +907,9 @@ __global__ void getdt_kernel(StencilArgs A, double dt, double* __restrict__ part
     int i = t % g.n1m, row = t / g.n1m;
     size_t c0 = cidx(g, i, row % g.n2m, row / g.n2m);
     R v;
-    if (sizeof(R) == 8)   // FP64 form: the reference's operation order
+    if constexpr (ISO && sizeof(R) == 8)
+      v = sum3_abs_f64(F.u[c0], F.v[c0], F.w[c0]) * d1;
+    else if (sizeof(R) == 8)   // FP64 form: the reference's operation order
       v = fabs(F.u[c0]) * R(dt) * R(g.dx1) + fabs(F.v[c0]) * R(dt) * R(g.dx2) + fabs(F.w[c0]) * R(dt) * R(g.dx3);
     else
       v = fabs(F.u[c0]) * d1 + fabs(F.v[c0]) * d2 + fabs(F.w[c0]) * d3;
@@ -1259,6 +1268,9 @@ void k_cfl_async(Ctx* c, double* out) {
   bool f32 = c->precision == 1 && c->q32_valid;
   { MIBM_PROF(c, "cfl");
     if (f32) cfl_kernel<float><<<nb, 256, 0, c->stream>>>(make_args(c), c->pad_vx, c->pad_vy, c->red + kRedPart, c->dflag + 2);
+    else if (equal_spacings(c->g))
+      cfl_kernel<double, true><<<nb, 256, 0, c->stream>>>(make_args(c), c->pad_vx, c->pad_vy, c->red + kRedPart,
+                                                         c->dflag + 2);
     else cfl_kernel<double><<<nb, 256, 0, c->stream>>>(make_args(c), c->pad_vx, c->pad_vy, c->red + kRedPart, c->dflag + 2); }
   max_reduce_kernel<<<1, 1024, 0, c->stream>>>(c->red + kRedPart, nb, c->red + kRedOut);
   c->launches += 2;
@@ -1285,6 +1297,8 @@ void k_getdt_async(Ctx* c, double dt, double* out) {
   bool f32 = c->precision == 1 && c->q32_valid;
   { MIBM_PROF(c, "getdt");
     if (f32) getdt_kernel<float><<<nb, 256, 0, c->stream>>>(make_args(c), dt, c->red + kRedPart + c->red_elems / 2);
+    else if (equal_spacings(c->g))
+      getdt_kernel<double, true><<<nb, 256, 0, c->stream>>>(make_args(c), dt, c->red + kRedPart + c->red_elems / 2);
     else getdt_kernel<double><<<nb, 256, 0, c->stream>>>(make_args(c), dt, c->red + kRedPart + c->red_elems / 2); }
   max_reduce_kernel<<<1, 1024, 0, c->stream>>>(c->red + kRedPart + c->red_elems / 2, nb, c->red + kRedOut + 1);
   c->launches += 2;
