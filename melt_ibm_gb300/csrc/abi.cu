@@ -403,7 +403,7 @@ static bool capture_step(Ctx* c, uint64_t key) {
     return false;
   }
   cudaGraphExec_t ex = nullptr;
-  if (cudaGraphInstantiate(&ex, gr, 0) != cudaSuccess) {
+  if (cudaGraphInstantiate(&ex, gr, cudaGraphInstantiateFlagUseNodePriority) != cudaSuccess) {
     cudaGraphDestroy(gr);
     cudaGetLastError();
     c->use_graph = false;
@@ -621,7 +621,7 @@ static int batch_step(Batch* b, int ntime) {
         cudaGraphNode_t node;
         ok = cudaGraphAddChildGraphNode(&node, b->graph, nullptr, 0, cs[q]->graph) == cudaSuccess;
       }
-      ok = ok && cudaGraphInstantiate(&b->exec, b->graph, 0) == cudaSuccess;
+      ok = ok && cudaGraphInstantiate(&b->exec, b->graph, cudaGraphInstantiateFlagUseNodePriority) == cudaSuccess;
       if (!ok) { cudaGetLastError(); batch_drop_graph(b); all_graphs = false; }
       else b->built_from = now;
     }

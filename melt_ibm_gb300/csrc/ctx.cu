@@ -349,11 +349,21 @@ int mibm_context_create_(void) {
     g_ctx[c->id] = c;
   }
   cudaGetDevice(&c->device);
-  if (!cuda_ok(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream") ||
-      !cuda_ok(c, cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking), "stream") ||
-      !cuda_ok(c, cudaStreamCreateWithFlags(&c->side2, cudaStreamNonBlocking), "stream") ||
-      !cuda_ok(c, cudaStreamCreateWithFlags(&c->side3, cudaStreamNonBlocking), "stream") ||
-      !cuda_ok(c, cudaStreamCreateWithFlags(&c->tsolve, cudaStreamNonBlocking), "stream") ||
+  // The IBM streams (side, side2, side3) carry chains of small latency-bound
+  // kernels that the main stream waits for at its joins; at the greatest
+  // priority their blocks take SM slots as soon as they free up, beside the
+  // main stream's large grids (256^3 FP64 step 26.48 -> 26.12 ms, 128^3 free
+  // body 3.94 -> 3.87 ms FP64 and 2.21 -> 2.12 ms precision form; the main
+  // stream at the greatest priority instead: slower).  The step graphs keep
+  // these priorities per node (cudaGraphInstantiateFlagUseNodePriority).
+  int prio_least = 0, prio_greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+  const int p_main = prio_least, p_side = prio_greatest;
+  if (!cuda_ok(c, cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, p_main), "stream") ||
+      !cuda_ok(c, cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, p_side), "stream") ||
+      !cuda_ok(c, cudaStreamCreateWithPriority(&c->side2, cudaStreamNonBlocking, p_side), "stream") ||
+      !cuda_ok(c, cudaStreamCreateWithPriority(&c->side3, cudaStreamNonBlocking, p_side), "stream") ||
+      !cuda_ok(c, cudaStreamCreateWithPriority(&c->tsolve, cudaStreamNonBlocking, p_main), "stream") ||
       !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_sfork, cudaEventDisableTiming), "event") ||
       !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_sjoin, cudaEventDisableTiming), "event") ||
       !cuda_ok(c, cudaEventCreateWithFlags(&c->ev_wfork, cudaEventDisableTiming), "event") ||
