@@ -1267,26 +1267,32 @@ heat_flux_lit_kernel(LagArgs A, const double* __restrict__ temp, const double* _
 }
 
 // ---------------------------------------------------------------------
-// Structural loads (mls_structLoads.f90:1-269).  A block takes 32 faces;
-// warp e of the block evaluates, at each face's positive probe
-// x_p = X + h n/|n|,
+// Structural loads (mls_structLoads.f90:1-269).  Faces go in groups of 32
+// (lane = face); each group is five one-warp blocks, and warp e evaluates, at
+// each face's positive probe x_p = X + h n/|n|,
 //   e = 0  the pressure (wght_press: cell-centred cage, z layers k1-1..k1+1
 //          without the repeated layer, mls_structLoads.f90:271-404)
 //   e = 1  grad p   (wght_gradP, cage (icent, jcent))
 //   e = 2  grad u   (wght_gradU, x at faces, cage (istag, jcent))
 //   e = 3  grad v   (wght_gradV, y at faces, cage (icent, jstag))
 //   e = 4  grad w   (wght_gradW, z at faces with nint, cage (icent, jcent))
-// so every warp runs one kind of evaluation.  Warp 0 then forms each face's
+// so every warp runs one kind of evaluation, and stores it in the group's
+// slots.  One-warp blocks spread over the SMs evenly (five-warp blocks of 32
+// faces left a few SMs with two blocks of the FP64-bound evaluations).  The
+// last of the five warps to finish (a group ticket) forms each face's
 // pressure force, viscous normal stress and their moments about pos_CM in
-// the reference's operation order (face_loads); the five warps sum the 32
-// faces' 12 values with fixed shuffle trees, and the last block to finish
-// adds the block sums (lane l takes blocks l, l+32, ... in order, then a
-// fixed shuffle tree) and updates the loads.
+// the reference's operation order (face_loads) and sums the 32 faces' 12
+// values with fixed shuffle trees; the last group to finish (the global
+// ticket) adds the group sums (lane l takes groups l, l+32, ... in order, then
+// a fixed shuffle tree) and updates the loads.  Tickets are reset by the
+// warps that close them.
 // Lit (the plain form): the reference's MLS construction (probe_value_lit,
 // probe_grad_lit), the oracle's bits per face.  Otherwise (the precision
 // form) the separable construction, which agrees with the reference's
 // rank-one accumulation in absolute coordinates to that construction's
 // round-off (amplified by its ~1e8 conditioning) at a fifth of the cost.
+// scratch: [groups][13][32] evaluations, then [groups][12] group sums;
+// tickets: [0] groups done, [1 + g] warps of group g done.
 // ---------------------------------------------------------------------
 constexpr int kLoadFaces = 32;
 
@@ -1298,19 +1304,18 @@ __device__ __forceinline__ void struct_probe(const double* __restrict__ tri_bar,
 }
 
 template <bool Lit>
-__global__ void __launch_bounds__(kLoadFaces * 5)
+__global__ void __launch_bounds__(kLoadFaces)
 loads_face_kernel(LagArgs A, const double* __restrict__ pr, const double* __restrict__ vx,
                   const double* __restrict__ vy, const double* __restrict__ vz, const double* __restrict__ tri_bar,
                   const double* __restrict__ tri_nor, const double* __restrict__ sur, const int* __restrict__ ghost,
-                  const StepParams* __restrict__ pp, double h, double ren, double* __restrict__ part,
-                  int* __restrict__ flag, unsigned* __restrict__ ticket, RigidDev* __restrict__ r) {
+                  const StepParams* __restrict__ pp, double h, double ren, double* __restrict__ scratch,
+                  int* __restrict__ flag, unsigned* __restrict__ tickets, RigidDev* __restrict__ r) {
   const unsigned FULL = 0xffffffffu;
-  __shared__ double ev[13][kLoadFaces];
-  __shared__ double cs[12][kLoadFaces];
-  __shared__ double tot[12];
-  __shared__ bool last;
-  const int lf = threadIdx.x, e = threadIdx.y;
-  const int t = blockIdx.x * kLoadFaces + lf;
+  const int lf = threadIdx.x;
+  const int grp = blockIdx.x / 5, e = blockIdx.x % 5, ngrp = gridDim.x / 5;
+  double* evg = scratch + (size_t)grp * 13 * kLoadFaces;
+  double* part = scratch + (size_t)ngrp * 13 * kLoadFaces;
+  const int t = grp * kLoadFaces + lf;
   const bool live = t < A.nf && !ghost[t];
   const Grid& g = A.g;
   double pos[3], nrm[3];
@@ -1322,7 +1327,7 @@ loads_face_kernel(LagArgs A, const double* __restrict__ pr, const double* __rest
     if (e == 0) {
       double v = 0.0;
       ok = Lit ? probe_value_lit(A, pos, icent, jcent, pr, v) : probe_value_sep(A, pos, icent, jcent, pr, v);
-      ev[0][lf] = ok ? v : 0.0;
+      evg[lf] = ok ? v : 0.0;
     } else {
       double gr[3] = {0, 0, 0};
       const double* q = e == 1 ? pr : e == 2 ? vx : e == 3 ? vy : vz;
@@ -1330,54 +1335,55 @@ loads_face_kernel(LagArgs A, const double* __restrict__ pr, const double* __rest
       const int sx = e == 2 ? 0 : 1, sy = e == 3 ? 0 : 1, sz = e == 4 ? 0 : 1;
       ok = Lit ? probe_grad_lit(A, pos, pi1, pi2, sx, sy, sz, e == 4, q, gr)
                : probe_grad_sep(A, pos, pi1, pi2, sx, sy, sz, e == 4, q, gr);
-      for (int d = 0; d < 3; ++d) ev[1 + 3 * (e - 1) + d][lf] = ok ? gr[d] : 0.0;
+      for (int d = 0; d < 3; ++d) evg[(1 + 3 * (e - 1) + d) * kLoadFaces + lf] = ok ? gr[d] : 0.0;
     }
     if (!ok) atomicOr(flag, 1);
   }
-  __syncthreads();
-  if (e == 0) {
-    double cf[12];
-    for (int q = 0; q < 12; ++q) cf[q] = 0.0;
-    if (live) {
-      double e13[13], rad[3];
-      for (int q = 0; q < 13; ++q) e13[q] = ev[q][lf];
-      for (int d = 0; d < 3; ++d) rad[d] = tri_bar[3 * t + d] - pp->pos[d];
-      face_loads(e13, nrm, rad, sur[t], h, ren, cf);
-    }
-    for (int q = 0; q < 12; ++q) cs[q][lf] = cf[q];
+  // the last of the group's five warps forms the loads of its 32 faces
+  __threadfence();
+  __syncwarp();
+  unsigned done = 0;
+  if (lf == 0) done = atomicAdd(&tickets[1 + grp], 1u);
+  if (__shfl_sync(FULL, done, 0) != 4u) return;
+  __threadfence();
+  double cf[12];
+  for (int q = 0; q < 12; ++q) cf[q] = 0.0;
+  if (live) {
+    double e13[13], rad[3];
+    for (int q = 0; q < 13; ++q) e13[q] = __ldcg(evg + q * kLoadFaces + lf);
+    for (int d = 0; d < 3; ++d) rad[d] = tri_bar[3 * t + d] - pp->pos[d];
+    face_loads(e13, nrm, rad, sur[t], h, ren, cf);
   }
-  __syncthreads();
-  // block sums, one quantity per warp at a time (a shuffle tree over the
-  // block's faces); the last block to finish (ticket, reset by that block)
-  // adds the block sums the same way (lane l takes blocks l, l+32, ... in
-  // order, then a fixed shuffle tree), moves the previous
-  // loads to the _m1 slots, stores the new ones and adds them to the running
-  // sums (mls_structLoads.f90:21-24, 207-262)
-  for (int q = e; q < 12; q += 5) {
-    double v = cs[q][lf];
+  // group sums (a shuffle tree over the group's faces per quantity)
+  for (int q = 0; q < 12; ++q) {
+    double v = cf[q];
     for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(FULL, v, off);
-    if (lf == 0) part[12 * (size_t)blockIdx.x + q] = v;
+    if (lf == 0) part[12 * (size_t)grp + q] = v;
   }
+  if (lf == 0) tickets[1 + grp] = 0u;
   __threadfence();
-  __syncthreads();
-  if (lf == 0 && e == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
-  __syncthreads();
-  if (!last) return;
+  __syncwarp();
+  unsigned gdone = 0;
+  if (lf == 0) gdone = atomicAdd(&tickets[0], 1u);
+  if (__shfl_sync(FULL, gdone, 0) != (unsigned)ngrp - 1u) return;
   __threadfence();
-  for (int q = e; q < 12; q += 5) {
+  // the last group: the loads (lane l takes groups l, l+32, ... in order, then
+  // a fixed shuffle tree), the previous loads to the _m1 slots, the new ones
+  // stored and added to the running sums (mls_structLoads.f90:21-24, 207-262)
+  double tot[12];
+  for (int q = 0; q < 12; ++q) {
     double v = 0.0;
-    for (int b = lf; b < (int)gridDim.x; b += 32) v += __ldcg(part + 12 * (size_t)b + q);
+    for (int b = lf; b < ngrp; b += 32) v += __ldcg(part + 12 * (size_t)b + q);
     for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(FULL, v, off);
-    if (lf == 0) tot[q] = v;
+    tot[q] = v;
   }
-  __syncthreads();
-  if (lf == 0 && e == 0) {
+  if (lf == 0) {
     for (int q = 0; q < 12; ++q) {        // packed [prn, tau, rprn, rtau]
       r->load1[q] = r->load[q];
       r->load[q] = tot[q];
       r->acc[q] = r->acc[q] + tot[q];
     }
-    *ticket = 0u;
+    tickets[0] = 0u;
   }
 }
 
@@ -1909,8 +1915,8 @@ struct LagState {
   double* face_part = nullptr;
   double* geom_out = nullptr;   // device [Surface, Volume1, Vol, Cx, Cy, Cz, InertTensor(9)]
   unsigned* geom_ticket = nullptr;   // blocks of face_geom_kernel done (0 between launches)
-  double* loads_ev = nullptr;   // structural loads: 12 block sums per 32 faces
-  unsigned* loads_ticket = nullptr;   // blocks of loads_face_kernel done (0 between launches)
+  double* loads_ev = nullptr;   // structural loads: per 32-face group 13 x 32 evaluations, then 12 group sums
+  unsigned* loads_ticket = nullptr;   // groups done, then warps done per group (0 between launches)
   int* rm_flag = nullptr;       // remesh trigger (device)
   double* mean3 = nullptr;
   int* winner = nullptr;
@@ -2343,17 +2349,17 @@ void lagr_geometry_to_host(Ctx* c) {
 // (see literal_mls).
 static void struct_loads_launch(Ctx* c, const StepParams* dp, bool literal) {
   LagState* s = lag_of(c);
+  const int nb = (int)div_up(std::max(1, c->maxnf), kLoadFaces);   // groups of 32 faces
   if (!s->loads_ev) {
-    if (!cuda_ok(c, cudaMalloc(&s->loads_ev, sizeof(double) * 13 * std::max(1, c->maxnf)), "structLoads") ||
-        !cuda_ok(c, cudaMalloc(&s->loads_ticket, sizeof(unsigned)), "structLoads"))
+    if (!cuda_ok(c, cudaMalloc(&s->loads_ev, sizeof(double) * (13 * kLoadFaces + 12) * (size_t)nb), "structLoads") ||
+        !cuda_ok(c, cudaMalloc(&s->loads_ticket, sizeof(unsigned) * (size_t)(nb + 1)), "structLoads"))
       return;
-    cudaMemsetAsync(s->loads_ticket, 0, sizeof(unsigned), c->stream);
+    cudaMemsetAsync(s->loads_ticket, 0, sizeof(unsigned) * (size_t)(nb + 1), c->stream);
   }
   double h = c->S(MIBM_S_H_EULERIAN);
-  int nb = (int)div_up(c->maxnf, kLoadFaces);
   { MIBM_PROF(c, "loads_face");
     auto kern = literal ? loads_face_kernel<true> : loads_face_kernel<false>;
-    kern<<<nb, dim3(kLoadFaces, 5), 0, c->stream>>>(
+    kern<<<5 * nb, kLoadFaces, 0, c->stream>>>(
         lag_args(c), c->df[MIBM_F_PR], c->df[MIBM_F_VX], c->df[MIBM_F_VY], c->df[MIBM_F_VZ],
         M<double>(c, MIBM_M_TRI_BAR), M<double>(c, MIBM_M_TRI_NOR), M<double>(c, MIBM_M_SUR),
         M<int>(c, MIBM_M_GHOST_FACE), dp, h, c->S(MIBM_S_REN), s->loads_ev, c->dflag, s->loads_ticket,
