@@ -116,7 +116,7 @@ NCU_TRAFFIC = {
 # clocks per SM on this part): this count over that rate is the step's FP64
 # floor.
 FP64_CENSUS = {"melt256_c2": {"warp_instructions_per_step": 404.58e6, "clocks_per_instruction_per_sm": 16},
-               "melt128_c1": {"warp_instructions_per_step": 51.91e6, "clocks_per_instruction_per_sm": 16}}
+               "melt128_c1": {"warp_instructions_per_step": 51.88e6, "clocks_per_instruction_per_sm": 16}}
 
 FIELDS = {"u": abi.MIBM_F_VX, "v": abi.MIBM_F_VY, "w": abi.MIBM_F_VZ, "T": abi.MIBM_F_TEMP, "p": abi.MIBM_F_PR}
 FIELD_MASK = sum(1 << f for f in FIELDS.values())
