@@ -305,6 +305,20 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def autotune_shapes(lib, case, args):
+    """The library's autotuner on the bound case before its timed steps (as a
+    host does once per grid and form): line-solve chunk lengths and the
+    explicit-term block height; returns the chosen shapes."""
+    if args.no_autotune:
+        return None
+    case.bind(lib)
+    if lib.mibm_autotune_() != 0:
+        lib.check("autotune")
+    got = np.zeros(4, dtype=np.int32)
+    lib.mibm_autotune_get_(got.ctypes.data)
+    return {"chunk_x": int(got[0]), "chunk_y": int(got[1]), "chunk_z": int(got[2]), "rhs_block_y": int(got[3])}
+
+
 def run_gpu(args):
     from melt_ibm_gb300 import build as mbuild
     dist = Dist()
@@ -319,6 +333,7 @@ def run_gpu(args):
     case32 = case.clone()                  # identical inputs for the precision form
     case.attach(lib)
     lib.check("attach")
+    shapes64 = autotune_shapes(lib, case, args)
     n3 = case.n1m * case.n2m * case.n3m
     nt = 1
     for _ in range(args.warmup):
@@ -434,6 +449,7 @@ def run_gpu(args):
         case32.bind(lib)
         lib.mibm_set_precision_(abi.ref_int(1), abi.ref_int(args.nproj))
         lib.check("set_precision")
+        shapes32 = autotune_shapes(lib, case32, args)
         nt32 = 1
         for _ in range(args.warmup):
             case32.step(lib, nt32)
@@ -477,7 +493,7 @@ def run_gpu(args):
         fp32 = {"value": v32, "unit": "Mcell-steps/s", "ms_per_step": ms32 / args.steps, "roofline": roof32,
                 "speedup_vs_fp64": v32 / value, "nproj": args.nproj,
                 "rel_l2_vs_fp64": errs, "divergence_max": div32, "divergence_max_fp64": div64,
-                "compared_after_steps": args.warmup + args.steps, "kernels": kern32,
+                "compared_after_steps": args.warmup + args.steps, "kernels": kern32, "autotuned_shapes": shapes32,
                 "dtype": "f32 compute, f64 fields (u, v, w, T, p), f64 MLS / Stefan / divergence residual"}
     dist.barrier()
     if dist.rank != 0:
@@ -492,7 +508,7 @@ def run_gpu(args):
                     "d2h_bytes_per_step": d2h, "host_arrays_pinned": pinned},
             "roofline": roofline, "gpu_launches": launches, "clocks": clocks, "fp32_refined": fp32,
             "diagnostics": diagnostics,
-            "host_wall_ms_per_step": 1e3 * wall / args.steps, "kernels": kernels}
+            "host_wall_ms_per_step": 1e3 * wall / args.steps, "kernels": kernels, "autotuned_shapes": shapes64}
     census = FP64_CENSUS.get(args.workload)
     if census is not None and clocks and clocks.get("sm_mhz"):
         import torch
@@ -731,6 +747,8 @@ def main():
     ap.add_argument("--no-fp32", action="store_true", help="skip the precision-form measurement")
     ap.add_argument("--nproj", type=int, default=2, help="Poisson solves per substep in the precision form")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-form measurement")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="time the headline case at the default shapes instead of the autotuned ones")
     ap.add_argument("--remesh-steps", type=int, default=100,
                     help="steps of the 128^3 free-body configuration with remeshing (0: skip)")
     ap.add_argument("--relambda-steps", type=int, default=3500,
