@@ -200,7 +200,8 @@ struct Ctx {
   bool profiling = false;                 // per-kernel event profiling on (no graphs then)
   // shapes chosen by the autotuner (tune.cu); -1 / 8 = the default rules
   int tune_m[3] = {-1, -1, -1};           // line-solve chunk length per direction
-  int tune_by = 8;                        // block height of the explicit-term kernel
+  int tune_by = 2;                        // block height of the explicit-term kernels (32 x 2 threads: the
+                                          // autotuner's choice at 48^3, 128^3 and 256^3)
   uint64_t tune_gen = 0;
   int tma = 1;                            // FP32 y/z line solves staged by bulk tensor copies
   int fused_uvw = 1;                      // FP32 one-pass kernels (u, v, w explicit terms; projection update)
